@@ -1,0 +1,87 @@
+// Shared device-side definitions for the cosmos_gb300 kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace cg {
+
+#define CG_HD __host__ __device__ __forceinline__
+#define CG_D __device__ __forceinline__
+
+struct Pt { double x, y, z; };
+
+CG_HD Pt shift_pt(Pt p, int axis, double d) {
+    if (axis == 0) p.x = p.x + d; else p.y = p.y + d;
+    return p;
+}
+
+template <class T> struct V5 { T v[5]; };
+
+// Ghost-cell index along a line of n cells.  Transmissive mirrors the reference's
+// insertBoundaryCells (Solvers/EulerSolvers.cpp:13-19, :52-73): g[-1]=c[0], g[-2]=c[1],
+// g[n]=c[n-1], g[n+1]=c[n-2].  Periodic wraps (an extension; the reference has no periodic BC).
+CG_HD int ghost_index(int k, int n, int bc) {
+    if (bc == 1) { k %= n; return k < 0 ? k + n : k; }
+    if (k < 0) return -1 - k;
+    if (k >= n) return 2 * n - 1 - k;
+    return k;
+}
+
+// std::min / std::max semantics as used by the reference.
+template <class T> CG_HD T mn(T a, T b) { return (b < a) ? b : a; }
+template <class T> CG_HD T mx(T a, T b) { return (a < b) ? b : a; }
+
+// Device-resident step controller.  The time step is computed on the device from the last
+// wavespeed reduction so that whole runs replay from a captured CUDA graph with no host sync.
+struct StepCtl {
+    double t;          // simulation time at the start of the current step
+    double t_final;
+    double cfl;
+    double dx;
+    double dt;         // the current step's dt (0 when inactive)
+    int it;            // completed steps (the reference's currentIteration)
+    int it_limit;      // stop after this many steps (INT_MAX for none)
+    int active;        // 1 while the current step runs, 0 once t >= t_final or it >= it_limit
+    int status;        // sticky error bits, see COSMOS_STATUS_* in the public header
+    unsigned long long smax[2];  // wavespeed maxima (bit patterns of non-negative doubles), ping-pong by it parity
+    unsigned long long newton_cap_hits;  // con2prim solves that reached the 1000-iteration cap
+};
+
+// Status bits written by kernels (mirrored in include/cosmos_gb300.h)
+enum : int {
+    ST_NONFINITE = 1,       // a non-finite state was produced
+    ST_NEWTON_CAP = 2,      // a con2prim Newton solve stopped at its iteration cap
+    ST_TIMEOUT = 4,         // a bounded device wait gave up
+    ST_NEGATIVE = 8,        // non-positive density or pressure produced by the FP32 path
+};
+
+// Max of non-negative doubles (ordering of their bit patterns equals numeric ordering).
+CG_D void atomic_max_nonneg(unsigned long long* slot, double v) {
+    if (!(v > 0.0)) return;  // also drops NaN, like the reference's `if (w > max)` test
+    atomicMax(slot, (unsigned long long)__double_as_longlong(v));
+}
+
+CG_D double warp_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        double w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = (w > v) ? w : v;
+    }
+    return v;
+}
+
+// Block-wide max reduction into *slot; every thread passes its value (0 if none).
+template <int NT>
+CG_D void block_max_to(unsigned long long* slot, double v) {
+    __shared__ double red[NT / 32];
+    v = warp_max(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        double w = lane < NT / 32 ? red[lane] : 0.0;
+        w = warp_max(w);
+        if (lane == 0) atomic_max_nonneg(slot, w);
+    }
+}
+
+}  // namespace cg

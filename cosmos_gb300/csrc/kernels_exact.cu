@@ -1,0 +1,449 @@
+// FP64 reference-exact kernels.  Compiled with --fmad=false so that every double operation is
+// rounded exactly as the reference's (built with -ffp-contract=off) -- results are bit-identical.
+#include "launch.h"
+#include "policies.cuh"
+
+namespace cg {
+
+namespace {
+
+constexpr int kXThreads = 128;  // X sweep tile: 128 evolutions, 127 fluxes, 126 updates
+constexpr int kYThreads = 64;   // Y sweep: columns per block
+constexpr int kYSeg = 16;       // Y sweep: rows marched per thread
+
+template <class Sys>
+ExactPolicy<Sys> make_policy(const SweepArgs& a, const Sys& sys) {
+    ExactPolicy<Sys> p;
+    p.sys = sys;
+    p.lm.axis = a.G.axis;
+    p.lm.nx = a.G.nx;
+    p.dims = a.G.dims;
+    p.order = a.order;
+    p.ny = a.G.ny;
+    p.dx = a.dx;
+    p.dt = 0.0;
+    p.w = a.bias;
+    p.lim = a.lim;
+    p.capped = 0;
+    return p;
+}
+
+template <class Pol>
+cudaError_t run_sweep(const Pol& pol, const SweepArgs& a) {
+    const Geom& G = a.G;
+    const double* src = (const double*)a.src;
+    double* dst = (double*)a.dst;
+    if (G.axis == 0) {
+        dim3 grid((G.nx + kXThreads - 3) / (kXThreads - 2), G.ny);
+        if (a.order == 2) sweep_x_kernel<Pol, 2, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+        else sweep_x_kernel<Pol, 1, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+    } else {
+        dim3 grid((G.nx + kYThreads - 1) / kYThreads, (G.ny + kYSeg - 1) / kYSeg);
+        if (a.order == 2) sweep_y_kernel<Pol, 2, kYThreads, kYSeg><<<grid, kYThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+        else sweep_y_kernel<Pol, 1, kYThreads, kYSeg><<<grid, kYThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+    }
+    count_launch();
+    return cudaGetLastError();
+}
+
+GRExact make_gr(const SweepArgs& a) {
+    GRExact s;
+    s.g = a.gamma;
+    s.bh = BHExact{a.bh[0], a.bh[1], a.bh[2], a.bh[3], a.bh[4]};
+    s.h = a.dx;
+    s.capped = nullptr;
+    return s;
+}
+
+}  // namespace
+
+cudaError_t launch_sweep_exact(const SweepArgs& a) {
+    if (a.system == 0) return run_sweep(make_policy(a, NewtonExact<double>{a.gamma}), a);
+    if (a.system == 1) return run_sweep(make_policy(a, SRExact{a.gamma, nullptr}), a);
+    return run_sweep(make_policy(a, make_gr(a)), a);
+}
+
+cudaError_t launch_wavespeed_exact(const SweepArgs& a, unsigned long long* slot) {
+    constexpr int NT = 256;
+    Geom G = a.G;
+    SweepArgs b = a;
+    b.G.axis = 0;
+    SweepOut o = a.out;
+    if (slot) { o.smax = slot; o.ws_ctl = nullptr; }
+    const size_t n = (size_t)G.nx * G.ny;
+    int blocks = (int)((n + NT - 1) / NT);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    const double* src = (const double*)a.src;
+    if (a.system == 0) wavespeed_kernel<ExactPolicy<NewtonExact<double>>, NT><<<blocks, NT, 0, a.stream>>>(make_policy(b, NewtonExact<double>{a.gamma}), b.G, src, o);
+    else if (a.system == 1) wavespeed_kernel<ExactPolicy<SRExact>, NT><<<blocks, NT, 0, a.stream>>>(make_policy(b, SRExact{a.gamma, nullptr}), b.G, src, o);
+    else wavespeed_kernel<ExactPolicy<GRExact>, NT><<<blocks, NT, 0, a.stream>>>(make_policy(b, make_gr(a)), b.G, src, o);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ GR RK4 source step
+// Solvers/BlackHoleEulerForcingSolver.cpp:187-250: per cell away from the horizon (cell and its
+// 2 (1D) or 4 (2D) neighbours outside), conserved neighbours from a 1-ghost transmissive copy,
+// classical RK4 with interleaved fractional sweeps, converted back at the cell.
+__global__ void __launch_bounds__(128) rk_source_kernel(GRExact sys, Geom G, double dx, double w, int lim,
+                                                        const double* __restrict__ src, double* __restrict__ dst,
+                                                        DtSrc ds, int* status) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (j >= G.nx) return;
+    const size_t idx = (size_t)i * G.pitch + j;
+    double dt;
+    int capped = 0;
+    sys.capped = &capped;
+    bool on = ds.get(dt);
+    const BHExact& b = sys.bh;
+    if (on) {
+        if (G.dims == 1)
+            on = !b.excised(j * dx, 0.0, 0.0) && !b.excised((j - 1) * dx, 0.0, 0.0) && !b.excised((j + 1) * dx, 0.0, 0.0);
+        else
+            on = !b.excised(j * dx, i * dx, 0.0) && !b.excised((j - 1) * dx, i * dx, 0.0) &&
+                 !b.excised((j + 1) * dx, i * dx, 0.0) && !b.excised(j * dx, (i - 1) * dx, 0.0) &&
+                 !b.excised(j * dx, (i + 1) * dx, 0.0);
+    }
+    if (!on) {
+#pragma unroll
+        for (int f = 0; f < 5; f++) dst[f * G.fstride + idx] = src[f * G.fstride + idx];
+        return;
+    }
+    auto ld = [&](int ii, int jj, double* p) {
+        const size_t k = (size_t)ghost_index(ii, G.ny, 0) * G.pitch + ghost_index(jj, G.nx, 0);
+#pragma unroll
+        for (int f = 0; f < 5; f++) p[f] = src[f * G.fstride + k];
+    };
+    double p[5], cl[5], cm[5], cr[5], ct[5], cb[5], nc[5];
+    const double y = G.dims == 1 ? 0.0 : i * dx;
+    const Pt q{j * dx, y, 0.0};
+    ld(i, j - 1, p); sys.cons(p, Pt{(j - 1) * dx, y, 0.0}, cl);
+    ld(i, j, p); sys.cons(p, q, cm);
+    ld(i, j + 1, p); sys.cons(p, Pt{(j + 1) * dx, y, 0.0}, cr);
+    if (G.dims == 2) {
+        ld(i - 1, j, p); sys.cons(p, Pt{j * dx, (i - 1) * dx, 0.0}, ct);
+        ld(i + 1, j, p); sys.cons(p, Pt{j * dx, (i + 1) * dx, 0.0}, cb);
+    }
+    rk_cell_exact(sys, G.dims, cl, cm, cr, ct, cb, q, dx, dt, w, lim, nc);
+    sys.prim(nc, q, p);
+#pragma unroll
+    for (int f = 0; f < 5; f++) dst[f * G.fstride + idx] = p[f];
+    if (capped && status) atomicOr(status, ST_NEWTON_CAP);
+}
+
+cudaError_t launch_rk_source_exact(const SweepArgs& a) {
+    dim3 grid((a.G.nx + 127) / 128, a.G.ny);
+    rk_source_kernel<<<grid, 128, 0, a.stream>>>(make_gr(a), a.G, a.dx, a.bias, a.lim, (const double*)a.src,
+                                                 (double*)a.dst, a.ds, a.out.status);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ conversions
+__global__ void prim_in_exact_kernel(const double* __restrict__ aos, double* __restrict__ soa, Geom G) {
+    const size_t n = (size_t)G.nx * G.ny;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = c / G.nx, j = c % G.nx;
+#pragma unroll
+        for (int f = 0; f < 5; f++) soa[f * G.fstride + i * G.pitch + j] = aos[5 * c + f];
+    }
+}
+__global__ void prim_out_exact_kernel(const double* __restrict__ soa, double* __restrict__ aos, Geom G) {
+    const size_t n = (size_t)G.nx * G.ny;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = c / G.nx, j = c % G.nx;
+#pragma unroll
+        for (int f = 0; f < 5; f++) aos[5 * c + f] = soa[f * G.fstride + i * G.pitch + j];
+    }
+}
+static int grid_for(size_t n) {
+    size_t b = (n + 255) / 256;
+    return (int)(b > 152 * 32 ? 152 * 32 : (b ? b : 1));
+}
+cudaError_t launch_prim_in_exact(const double* aos, void* soa, const Geom& G, cudaStream_t st) {
+    prim_in_exact_kernel<<<grid_for((size_t)G.nx * G.ny), 256, 0, st>>>(aos, (double*)soa, G);
+    count_launch();
+    return cudaGetLastError();
+}
+cudaError_t launch_prim_out_exact(const void* soa, double* aos, const Geom& G, cudaStream_t st) {
+    prim_out_exact_kernel<<<grid_for((size_t)G.nx * G.ny), 256, 0, st>>>((const double*)soa, aos, G);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ step controller
+// Solvers/EulerSolvers.cpp:130-161: dt = CFL * (dx / s_max); x0.2 while it <= 5; clamped so
+// that t + dt does not pass t_final.  The solver loop `while (t < t_final)` becomes `active`.
+__global__ void dt_kernel(StepCtl* c) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (!(c->t < c->t_final) || c->it >= c->it_limit) {
+        c->active = 0;
+        c->dt = 0.0;
+        return;
+    }
+    const double smax = __longlong_as_double((long long)c->smax[c->it & 1]);
+    double dt = c->cfl * (c->dx / smax);
+    if (c->it <= 5) dt = dt * 0.2;
+    if ((c->t + dt) > c->t_final) dt = c->t_final - c->t;
+    if (!(dt > 0.0) || !isfinite(dt)) c->status |= ST_NONFINITE;
+    c->dt = dt;
+    c->active = 1;
+    c->smax[(c->it + 1) & 1] = 0ull;
+    c->t = c->t + dt;
+    c->it = c->it + 1;
+}
+cudaError_t launch_dt_kernel(StepCtl* ctl, cudaStream_t st) {
+    dt_kernel<<<1, 32, 0, st>>>(ctl);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ AMR flagging
+// Conserved state of a cell for the flag passes: FP64 storage holds primitives (converted with
+// the system's exact cons), FP32 storage holds conserved values already.
+struct ConsLoader {
+    int system, precision;
+    Geom G;
+    const void* state;
+    NewtonExact<double> nw;
+    SRExact sr;
+    GRExact gr;
+    CG_D void get(int i, int j, Pt q, double* u) const {
+        const size_t k = (size_t)ghost_index(i, G.ny, 0) * G.pitch + ghost_index(j, G.nx, 0);
+        if (precision == 1) {
+            const float* s = (const float*)state;
+#pragma unroll
+            for (int f = 0; f < 5; f++) u[f] = (double)s[f * G.fstride + k];
+            return;
+        }
+        const double* s = (const double*)state;
+        double p[5];
+#pragma unroll
+        for (int f = 0; f < 5; f++) p[f] = s[f * G.fstride + k];
+        cons_of(p, q, u);
+    }
+    CG_D void cons_of(const double* p, Pt q, double* u) const {
+        if (system == 0) nw.cons(p, q, u);
+        else if (system == 1) sr.cons(p, q, u);
+        else gr.cons(p, q, u);
+    }
+};
+
+// Refinement pass, AMR/EulerAMR.cpp:207-229 (1D) and :400-431 (2D); the SR and GR drivers read
+// the bottom neighbour at [i+2][j+2] (AMR/RelativisticEulerAMR.cpp:422,
+// AMR/BlackHoleEulerAMR.cpp:490), whose corner ghost keeps the default state (1,0,0,0,1).
+__global__ void amr_flags_kernel(ConsLoader L, double dx, double tol, unsigned char* coarse, unsigned char* fine) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    const Geom& G = L.G;
+    if (j >= G.nx) return;
+    double c[5], l[5], r[5], t[5], b[5];
+    bool hit = false;
+    if (G.dims == 1) {
+        L.get(0, j - 1, Pt{(j - 1) * dx, 0.0, 0.0}, l);
+        L.get(0, j, Pt{j * dx, 0.0, 0.0}, c);
+        L.get(0, j + 1, Pt{(j + 1) * dx, 0.0, 0.0}, r);
+#pragma unroll
+        for (int k = 0; k < 5; k++)
+            if (fabs((c[k] - l[k]) / dx) >= tol || fabs((r[k] - c[k]) / dx) >= tol) hit = true;
+    } else {
+        L.get(i - 1, j, Pt{j * dx, (i - 1) * dx, 0.0}, t);
+        L.get(i, j - 1, Pt{(j - 1) * dx, i * dx, 0.0}, l);
+        L.get(i, j, Pt{j * dx, i * dx, 0.0}, c);
+        L.get(i, j + 1, Pt{(j + 1) * dx, i * dx, 0.0}, r);
+        if (L.system == 0) L.get(i + 1, j, Pt{j * dx, (i + 1) * dx, 0.0}, b);
+        else if (i == G.ny - 1 && j == G.nx - 1) {
+            const double dflt[5] = {1.0, 0.0, 0.0, 0.0, 1.0};
+            if (L.precision == 1) {
+                // FP32 grids hold conserved values; the default state in conserved form
+                L.cons_of(dflt, Pt{(j + 1) * dx, (i + 1) * dx, 0.0}, b);
+            } else {
+                L.cons_of(dflt, Pt{(j + 1) * dx, (i + 1) * dx, 0.0}, b);
+            }
+        } else L.get(i + 1, j + 1, Pt{(j + 1) * dx, (i + 1) * dx, 0.0}, b);
+#pragma unroll
+        for (int k = 0; k < 5; k++)
+            if (fabs((c[k] - t[k]) / dx) >= tol || fabs((b[k] - c[k]) / dx) >= tol ||
+                fabs((c[k] - l[k]) / dx) >= tol || fabs((r[k] - c[k]) / dx) >= tol)
+                hit = true;
+    }
+    if (!hit) return;
+    if (G.dims == 1) {
+        coarse[j] = 0;
+        fine[2 * j] = 1;
+        fine[2 * j + 1] = 1;
+    } else {
+        coarse[(size_t)i * G.nx + j] = 0;
+        const size_t fw = 2 * (size_t)G.nx;
+        fine[(2 * i) * fw + 2 * j] = 1;
+        fine[(2 * i) * fw + 2 * j + 1] = 1;
+        fine[(2 * i + 1) * fw + 2 * j] = 1;
+        fine[(2 * i + 1) * fw + 2 * j + 1] = 1;
+    }
+}
+
+static ConsLoader make_loader(const SweepArgs& a, int precision, const void* state, const Geom& G) {
+    ConsLoader L;
+    L.system = a.system;
+    L.precision = precision;
+    L.G = G;
+    L.state = state;
+    L.nw = NewtonExact<double>{a.gamma};
+    L.sr = SRExact{a.gamma, nullptr};
+    L.gr = make_gr(a);
+    return L;
+}
+
+cudaError_t launch_amr_flags(const SweepArgs& a, int precision, double tol, unsigned char* coarse, unsigned char* fine) {
+    dim3 grid((a.G.nx + 127) / 128, a.G.ny);
+    amr_flags_kernel<<<grid, 128, 0, a.stream>>>(make_loader(a, precision, a.src, a.G), a.dx, tol, coarse, fine);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// Derefinement pass, AMR/EulerAMR.cpp:310-345 (1D) and :538-586 (2D); GR coordinates
+// AMR/BlackHoleEulerAMR.cpp:388-421 (1D fine cells read one fine cell to the left) and :632-686.
+// Restriction writes the coarse state (FP64 storage only holds primitives, converted with the
+// system's exact prim; FP32 storage receives the averaged conserved state).
+__global__ void amr_derefine_kernel(ConsLoader F, Geom CG, double dx, double tol, unsigned char* coarse,
+                                    unsigned char* fine, void* coarse_state) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (j >= CG.nx) return;
+    const double half = tol * 0.5, fdx = dx * 0.5;
+    bool marked = false;
+    double c[5], l[5], r[5], t[5], b[5], avg[5];
+    Pt qc;
+    if (CG.dims == 1) {
+        F.get(0, 2 * j, Pt{((j * 2) - 1) * fdx, 0.0, 0.0}, l);
+        F.get(0, 2 * j + 1, Pt{(j * 2) * fdx, 0.0, 0.0}, c);
+        F.get(0, 2 * j + 2, Pt{((j * 2) + 1) * fdx, 0.0, 0.0}, r);
+#pragma unroll
+        for (int k = 0; k < 5; k++)
+            if (fabs((c[k] - l[k]) / dx) >= half || fabs((r[k] - c[k]) / dx) >= half) marked = true;
+        if (marked || !fine[2 * j]) return;
+        fine[2 * j] = 0;
+        fine[2 * j + 1] = 0;
+        coarse[j] = 1;
+        double u0[5], u1[5];
+        F.get(0, 2 * j, Pt{(j * 2) * fdx, 0.0, 0.0}, u0);
+        F.get(0, 2 * j + 1, Pt{((j * 2) + 1) * fdx, 0.0, 0.0}, u1);
+#pragma unroll
+        for (int k = 0; k < 5; k++) avg[k] = 0.5 * (u0[k] + u1[k]);
+        qc = Pt{j * dx, 0.0, 0.0};
+    } else {
+        F.get(2 * i, 2 * j + 1, Pt{((j * 2) + 1) * fdx, (i * 2) * fdx, 0.0}, t);
+        F.get(2 * i + 1, 2 * j, Pt{(j * 2) * fdx, ((i * 2) + 1) * fdx, 0.0}, l);
+        F.get(2 * i + 1, 2 * j + 1, Pt{((j * 2) + 1) * fdx, ((i * 2) + 1) * fdx, 0.0}, c);
+        F.get(2 * i + 1, 2 * j + 2, Pt{((j * 2) + 2) * fdx, ((i * 2) + 1) * fdx, 0.0}, r);
+        F.get(2 * i + 2, 2 * j + 1, Pt{((j * 2) + 1) * fdx, ((i * 2) + 2) * fdx, 0.0}, b);
+#pragma unroll
+        for (int k = 0; k < 5; k++)
+            if (fabs((c[k] - t[k]) / dx) >= half || fabs((b[k] - c[k]) / dx) >= half ||
+                fabs((c[k] - l[k]) / dx) >= half || fabs((r[k] - c[k]) / dx) >= half)
+                marked = true;
+        const size_t fw = 2 * (size_t)CG.nx;
+        if (marked || !fine[(2 * i) * fw + 2 * j]) return;
+        fine[(2 * i) * fw + 2 * j] = 0;
+        fine[(2 * i) * fw + 2 * j + 1] = 0;
+        fine[(2 * i + 1) * fw + 2 * j] = 0;
+        fine[(2 * i + 1) * fw + 2 * j + 1] = 0;
+        coarse[(size_t)i * CG.nx + j] = 1;
+        double u0[5], u1[5], u2[5], u3[5];
+        F.get(2 * i, 2 * j, Pt{(j * 2) * fdx, (i * 2) * fdx, 0.0}, u0);
+        F.get(2 * i, 2 * j + 1, Pt{((j * 2) + 1) * fdx, (i * 2) * fdx, 0.0}, u1);
+        F.get(2 * i + 1, 2 * j, Pt{(j * 2) * fdx, ((i * 2) + 1) * fdx, 0.0}, u2);
+        F.get(2 * i + 1, 2 * j + 1, Pt{((j * 2) + 1) * fdx, ((i * 2) + 1) * fdx, 0.0}, u3);
+#pragma unroll
+        for (int k = 0; k < 5; k++) avg[k] = 0.25 * (((u0[k] + u1[k]) + u2[k]) + u3[k]);
+        qc = Pt{j * dx, i * dx, 0.0};
+    }
+    if (!coarse_state) return;
+    const size_t idx = (size_t)i * CG.pitch + j;
+    if (F.precision == 1) {
+        float* s = (float*)coarse_state;
+#pragma unroll
+        for (int k = 0; k < 5; k++) s[k * CG.fstride + idx] = (float)avg[k];
+    } else {
+        double p[5];
+        if (F.system == 0) F.nw.prim(avg, qc, p);
+        else if (F.system == 1) F.sr.prim(avg, qc, p);
+        else F.gr.prim(avg, qc, p);
+        double* s = (double*)coarse_state;
+#pragma unroll
+        for (int k = 0; k < 5; k++) s[k * CG.fstride + idx] = p[k];
+    }
+}
+
+cudaError_t launch_amr_derefine(const SweepArgs& a, int precision, const void* fine_state, const Geom& FG, double tol,
+                                unsigned char* coarse, unsigned char* fine, void* coarse_state) {
+    dim3 grid((a.G.nx + 127) / 128, a.G.ny);
+    amr_derefine_kernel<<<grid, 128, 0, a.stream>>>(make_loader(a, precision, fine_state, FG), a.G, a.dx, tol, coarse,
+                                                    fine, coarse_state);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ conservation sums
+// Sum of each stored field over the grid with Kahan-Babuska (Neumaier) compensation per thread,
+// then compensated double atomics are avoided: per-block partials go to a small buffer summed by
+// the last block in a fixed order, so the result is deterministic.
+__global__ void field_sums_kernel(const void* __restrict__ state, Geom G, int precision, double* partial,
+                                  unsigned int* counter, double* out5) {
+    double s[5] = {0, 0, 0, 0, 0}, comp[5] = {0, 0, 0, 0, 0};
+    const size_t n = (size_t)G.nx * G.ny;
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = c / G.nx, j = c % G.nx, k = i * G.pitch + j;
+#pragma unroll
+        for (int f = 0; f < 5; f++) {
+            const double v = precision == 1 ? (double)((const float*)state)[f * G.fstride + k]
+                                            : ((const double*)state)[f * G.fstride + k];
+            const double t = s[f] + v;
+            comp[f] += (fabs(s[f]) >= fabs(v)) ? ((s[f] - t) + v) : ((v - t) + s[f]);
+            s[f] = t;
+        }
+    }
+    __shared__ double red[5][256];
+#pragma unroll
+    for (int f = 0; f < 5; f++) red[f][threadIdx.x] = s[f] + comp[f];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int f = 0; f < 5; f++) {
+            double a = 0.0, ca = 0.0;
+            for (int q = 0; q < blockDim.x; q++) {
+                const double v = red[f][q], t = a + v;
+                ca += (fabs(a) >= fabs(v)) ? ((a - t) + v) : ((v - t) + a);
+                a = t;
+            }
+            partial[blockIdx.x * 5 + f] = a + ca;
+        }
+        __threadfence();
+        const unsigned int done = atomicAdd(counter, 1u);
+        if (done == gridDim.x - 1) {
+            __threadfence();
+            for (int f = 0; f < 5; f++) {
+                double a = 0.0, ca = 0.0;
+                for (unsigned q = 0; q < gridDim.x; q++) {
+                    const double v = ((volatile double*)partial)[q * 5 + f], t = a + v;
+                    ca += (fabs(a) >= fabs(v)) ? ((a - t) + v) : ((v - t) + a);
+                    a = t;
+                }
+                out5[f] = a + ca;
+            }
+            *counter = 0;
+        }
+    }
+}
+
+cudaError_t launch_field_sums(const void* soa, const Geom& G, int precision, double* out5, cudaStream_t st) {
+    // scratch: 152*4 blocks * 5 partials + a counter, carved from out5's companion buffer
+    constexpr int kBlocks = 152 * 4;
+    double* partial = out5 + 8;
+    unsigned int* counter = (unsigned int*)(out5 + 8 + kBlocks * 5);
+    field_sums_kernel<<<kBlocks, 256, 0, st>>>(soa, G, precision, partial, counter, out5);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace cg

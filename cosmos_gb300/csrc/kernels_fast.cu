@@ -1,0 +1,108 @@
+// FP32 bulk kernels (Newtonian system): conserved SoA float storage, FMA contraction on.
+#include "launch.h"
+#include "policies.cuh"
+
+namespace cg {
+
+namespace {
+
+constexpr int kXThreads = 256;  // X sweep tile: 256 evolutions, 255 fluxes, 254 updates
+constexpr int kYThreads = 128;
+constexpr int kYSeg = 32;
+
+NewtonFastPolicy make_fast(const SweepArgs& a) {
+    NewtonFastPolicy p;
+    const float g = (float)a.gamma, w = (float)a.bias;
+    p.P.g1 = g - 1.0f;
+    p.P.gam = g;
+    p.P.wa = 0.5f * (1.0f + w);
+    p.P.wb = 0.5f * (1.0f - w);
+    p.P.om = 1.0f - w;
+    p.P.op = 1.0f + w;
+    p.P.lim = a.lim;
+    p.lm.axis = a.G.axis;
+    p.lm.nx = a.G.nx;
+    p.dims = a.G.dims;
+    p.dx = a.dx;
+    p.dtdx = p.half_dtdx = p.dxdt = 0.0f;
+    return p;
+}
+
+}  // namespace
+
+cudaError_t launch_sweep_fast(const SweepArgs& a) {
+    if (a.system != 0) return cudaErrorNotSupported;
+    const Geom& G = a.G;
+    const float* src = (const float*)a.src;
+    float* dst = (float*)a.dst;
+    NewtonFastPolicy pol = make_fast(a);
+    if (G.axis == 0) {
+        dim3 grid((G.nx + kXThreads - 3) / (kXThreads - 2), G.ny);
+        if (a.order == 2) sweep_x_kernel<NewtonFastPolicy, 2, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+        else sweep_x_kernel<NewtonFastPolicy, 1, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+    } else {
+        dim3 grid((G.nx + kYThreads - 1) / kYThreads, (G.ny + kYSeg - 1) / kYSeg);
+        if (a.order == 2) sweep_y_kernel<NewtonFastPolicy, 2, kYThreads, kYSeg><<<grid, kYThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+        else sweep_y_kernel<NewtonFastPolicy, 1, kYThreads, kYSeg><<<grid, kYThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+    }
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wavespeed_fast(const SweepArgs& a, unsigned long long* slot) {
+    if (a.system != 0) return cudaErrorNotSupported;
+    constexpr int NT = 256;
+    SweepArgs b = a;
+    b.G.axis = 0;
+    SweepOut o = a.out;
+    if (slot) { o.smax = slot; o.ws_ctl = nullptr; }
+    const size_t n = (size_t)a.G.nx * a.G.ny;
+    int blocks = (int)((n + NT - 1) / NT);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    wavespeed_kernel<NewtonFastPolicy, NT><<<blocks, NT, 0, a.stream>>>(make_fast(b), b.G, (const float*)a.src, o);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// Primitive (double, AoS) -> conserved FP32 SoA.  The conserved state is formed in double with
+// the reference's formula (Euler/EulerStateVector.cpp:55-66) and rounded once.
+__global__ void prim_in_fast_kernel(const double* __restrict__ aos, float* __restrict__ soa, Geom G, double gamma) {
+    const size_t n = (size_t)G.nx * G.ny;
+    NewtonExact<double> S{gamma};
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = c / G.nx, j = c % G.nx;
+        double u[5];
+        S.cons(aos + 5 * c, Pt{0, 0, 0}, u);
+#pragma unroll
+        for (int f = 0; f < 5; f++) soa[f * G.fstride + i * G.pitch + j] = (float)u[f];
+    }
+}
+__global__ void prim_out_fast_kernel(const float* __restrict__ soa, double* __restrict__ aos, Geom G, double gamma) {
+    const size_t n = (size_t)G.nx * G.ny;
+    NewtonExact<double> S{gamma};
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = c / G.nx, j = c % G.nx;
+        double u[5];
+#pragma unroll
+        for (int f = 0; f < 5; f++) u[f] = (double)soa[f * G.fstride + i * G.pitch + j];
+        S.prim(u, Pt{0, 0, 0}, aos + 5 * c);
+    }
+}
+static int grid_for(size_t n) {
+    size_t b = (n + 255) / 256;
+    return (int)(b > 152 * 32 ? 152 * 32 : (b ? b : 1));
+}
+cudaError_t launch_prim_in_fast(const double* aos, void* soa, const Geom& G, int system, double gamma, cudaStream_t st) {
+    if (system != 0) return cudaErrorNotSupported;
+    prim_in_fast_kernel<<<grid_for((size_t)G.nx * G.ny), 256, 0, st>>>(aos, (float*)soa, G, gamma);
+    count_launch();
+    return cudaGetLastError();
+}
+cudaError_t launch_prim_out_fast(const void* soa, double* aos, const Geom& G, int system, double gamma, cudaStream_t st) {
+    if (system != 0) return cudaErrorNotSupported;
+    prim_out_fast_kernel<<<grid_for((size_t)G.nx * G.ny), 256, 0, st>>>((const float*)soa, aos, G, gamma);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace cg

@@ -1,0 +1,179 @@
+// Physics policies plugged into the generic sweep kernels (sweep_kernels.cuh).
+#pragma once
+#include "physics_exact.cuh"
+#include "physics_fast.cuh"
+#include "sweep_kernels.cuh"
+
+namespace cg {
+
+// Cell position helpers shared by the policies.  A sweep line is a row (axis 0) or a column
+// (axis 1); k indexes cells along it.  Cell (i, j) sits at (x, y) = (j dx, i dx)
+// (Solvers/BlackHoleEulerSecondOrderSolver.cpp:88-100); 1D grids are row i = 0, so y = 0 as in
+// the reference's 1D solvers.
+struct LineMap {
+    int axis, nx;
+    CG_D void ij(int line, int k, int& i, int& j) const {
+        if (axis == 0) { i = line; j = k; } else { i = k; j = line; }
+    }
+    CG_D bool mask_on(const unsigned char* mask, int line, int k) const {
+        if (!mask) return true;
+        int i, j;
+        ij(line, k, i, j);
+        return mask[(size_t)i * nx + j] != 0;
+    }
+};
+
+// ------------------------------------------------------------------ reference-exact, FP64
+// Primitive storage exactly like the reference's grids.  Sys = NewtonExact<double>, SRExact or
+// GRExact.  Coordinate-free systems share one half-step evolution per cell (both faces);
+// GR evolves each face at its own, separately rounded, coordinate.
+template <class Sys>
+struct ExactPolicy {
+    using S = double;
+    using X = double;
+    using Cell = V5<double>;
+    using Face = V5<double>;
+    static constexpr bool kShared = !Sys::kCoords;
+    Sys sys;
+    LineMap lm;
+    int dims, order, ny;
+    double dx, dt, w;
+    int lim;
+    int capped;
+
+    CG_D void set_dt(double d) { dt = d; capped = 0; sys.capped = &capped; }
+    CG_D Pt cell_pt(int line, int k) const {
+        int i, j;
+        lm.ij(line, k, i, j);
+        return Pt{j * dx, i * dx, 0.0};
+    }
+    // interface between cells f-1 and f: (f - 0.5) dx along the sweep axis
+    CG_D Pt face_pt(int line, int f) const {
+        if (lm.axis == 0) return Pt{(f - 0.5) * dx, line * dx, 0.0};
+        return Pt{line * dx, (f - 0.5) * dx, 0.0};
+    }
+    CG_D void recon(const Cell& l, const Cell& m, const Cell& r, int, int, Face& L, Face& R) const {
+        evolve_half_exact(sys, l.v, m.v, r.v, Pt{0.0, 0.0, 0.0}, lm.axis, dx, dt, w, lim, L.v, R.v);
+    }
+    // GR: the left cell of interface f evolves at xf - dx/2, the right cell at xf + dx/2
+    // (Solvers/BlackHoleEulerSecondOrderSolver.cpp:3-37)
+    CG_D void recon_side(const Cell& l, const Cell& m, const Cell& r, int line, int k, int side, Face& o) const {
+        if (side == 1) {
+            Pt xc = shift_pt(face_pt(line, k + 1), lm.axis, -(dx * 0.5));
+            evolve_half_exact(sys, l.v, m.v, r.v, xc, lm.axis, dx, dt, w, lim, (double*)nullptr, o.v);
+        } else {
+            Pt xc = shift_pt(face_pt(line, k), lm.axis, dx * 0.5);
+            evolve_half_exact(sys, l.v, m.v, r.v, xc, lm.axis, dx, dt, w, lim, o.v, (double*)nullptr);
+        }
+    }
+    CG_D void face_of(const Cell& c, Face& f) const { f = c; }
+    CG_D void flux(const Face& L, const Face& R, int line, int f, V5<double>& F) const {
+        force_exact(sys, L.v, R.v, face_pt(line, f), lm.axis, dx, dt, F.v);
+    }
+    // computeFORCEUpdate, Solvers/EulerFirstOrderSolver.cpp:96-101, then setConservedVariableVector
+    CG_D Cell update(const Cell& c, const V5<double>& FL, const V5<double>& FR, int line, int k) const {
+        Pt q = cell_pt(line, k);
+        double u[5], nu[5];
+        sys.cons(c.v, q, u);
+        const double d = dt / dx;
+#pragma unroll
+        for (int f = 0; f < 5; f++) nu[f] = u[f] + (d * (FL.v[f] - FR.v[f]));
+        Cell o;
+        sys.prim(nu, q, o.v);
+        return o;
+    }
+    CG_D bool excised_stencil(int line, int k) const;
+    CG_D bool active(int line, int k, const unsigned char* mask) const {
+        if (!lm.mask_on(mask, line, k)) return false;
+        if (Sys::kCoords) return !excised_stencil(line, k);
+        return true;
+    }
+    CG_D double wavespeed(const Cell& c, int line, int k) const;
+    CG_D void flush_status(int* st) const {
+        if (st && capped) atomicOr(st, ST_NEWTON_CAP);
+    }
+};
+
+template <class Sys>
+CG_D bool ExactPolicy<Sys>::excised_stencil(int, int) const { return false; }
+template <class Sys>
+CG_D double ExactPolicy<Sys>::wavespeed(const Cell& c, int, int) const { return sys.wavespeed(c.v, dims, Pt{0, 0, 0}); }
+
+// GR excision: the updated cell and its stencil along both axes must lie outside the horizon
+// (Solvers/BlackHoleEulerSecondOrderSolver.cpp:44-46 in 1D, :81-85 in 2D; reach 1 for FORCE,
+// Solvers/BlackHoleEulerFirstOrderSolver.cpp:94-95, :131-133).
+template <>
+CG_D bool ExactPolicy<GRExact>::excised_stencil(int line, int k) const {
+    int i, j;
+    lm.ij(line, k, i, j);
+    const int reach = order == 2 ? 2 : 1;
+    const BHExact& b = sys.bh;
+    if (dims == 1) {
+        for (int d = -reach; d <= reach; d++)
+            if (b.excised((j + d) * dx, 0.0, 0.0)) return true;
+        return false;
+    }
+    if (b.excised(j * dx, i * dx, 0.0)) return true;
+    for (int d = 1; d <= reach; d++) {
+        if (b.excised((j - d) * dx, i * dx, 0.0) || b.excised((j + d) * dx, i * dx, 0.0) ||
+            b.excised(j * dx, (i - d) * dx, 0.0) || b.excised(j * dx, (i + d) * dx, 0.0))
+            return true;
+    }
+    return false;
+}
+
+// GR CFL speed, Solvers/BlackHoleEulerSolvers.cpp:87-131: coordinates use spacing 1/N, and in 2D
+// the excision test reads (j/ncol, i/nrow) while the speed is evaluated at (i/nrow, j/ncol).
+template <>
+CG_D double ExactPolicy<GRExact>::wavespeed(const Cell& c, int line, int k) const {
+    int i, j;
+    lm.ij(line, k, i, j);
+    if (dims == 1) {
+        const double cs = 1.0 / lm.nx;
+        if (sys.bh.excised(j * cs, 0.0, 0.0)) return 0.0;
+        return fabs(sys.sound_speed(c.v, Pt{j * cs, 0.0, 0.0}));
+    }
+    const double rs = 1.0 / ny, cs = 1.0 / lm.nx;
+    if (sys.bh.excised(j * cs, i * rs, 0.0)) return 0.0;
+    return fabs(sys.sound_speed(c.v, Pt{i * rs, j * cs, 0.0}));
+}
+
+// ------------------------------------------------------------------ Newtonian FP32 bulk
+// Conserved FP32 storage; see physics_fast.cuh for the reformulations.
+struct NewtonFastPolicy {
+    using S = float;
+    using X = float;
+    using Cell = V5<float>;
+    using Face = V5<float>;
+    static constexpr bool kShared = true;
+    NewtonFastParams P;
+    LineMap lm;
+    int dims;
+    double dx;
+    float dtdx, half_dtdx, dxdt;
+
+    CG_D void set_dt(double dt) {
+        dtdx = (float)(dt / dx);
+        half_dtdx = (float)(0.5 * (dt / dx));
+        dxdt = (float)(dx / dt);
+    }
+    CG_D void recon(const Cell& l, const Cell& m, const Cell& r, int, int, Face& L, Face& R) const {
+        nf_recon(P, l.v, m.v, r.v, lm.axis, half_dtdx, L.v, R.v);
+    }
+    CG_D void recon_side(const Cell&, const Cell&, const Cell&, int, int, int, Face&) const {}
+    CG_D void face_of(const Cell& c, Face& f) const { f = c; }
+    CG_D void flux(const Face& L, const Face& R, int, int, V5<float>& F) const {
+        nf_force(P, L.v, R.v, lm.axis, dtdx, dxdt, F.v);
+    }
+    CG_D Cell update(const Cell& c, const V5<float>& FL, const V5<float>& FR, int, int) const {
+        Cell o;
+#pragma unroll
+        for (int f = 0; f < 5; f++) o.v[f] = c.v[f] + dtdx * (FL.v[f] - FR.v[f]);
+        return o;
+    }
+    CG_D bool active(int line, int k, const unsigned char* mask) const { return lm.mask_on(mask, line, k); }
+    CG_D double wavespeed(const Cell& c, int, int) const { return (double)nf_wavespeed(P, c.v, dims); }
+    CG_D void flush_status(int*) const {}
+};
+
+}  // namespace cg

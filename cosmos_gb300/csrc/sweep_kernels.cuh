@@ -1,0 +1,270 @@
+// Generic dimensional-sweep kernels (SLIC order 2 / FORCE order 1) over a physics policy.
+//
+// Reference loop being replaced: Solvers/EulerSecondOrderSolver.cpp:27-100 (and the FORCE,
+// SR and GR twins): for every cell, two interface fluxes from a 4-cell stencil, then the
+// conservative update.  Here every interface flux is computed once per tile and shared by its
+// two cells; every half-step evolution once per cell (for coordinate-free systems).
+//
+// Layout: structure of arrays, field f of cell (i, j) at base[f * fstride + i * pitch + j].
+// Sweeps are out of place (src -> dst): neighbours must see the pre-sweep state.
+#pragma once
+#include "device_common.cuh"
+
+namespace cg {
+
+struct Geom {
+    int nx, ny, pitch, dims, axis, bc;
+    size_t fstride;
+};
+
+// Where a sweep gets its time step: a fixed value (the per-sweep API) or the device step
+// controller (graph-replayed runs; scale 1 or 0.5, or 0.5 * (dt / nsub) for the GR source).
+struct DtSrc {
+    const StepCtl* ctl;
+    double fixed;
+    double scale;
+    int nsub;  // > 0 selects 0.5 * (dt / nsub)
+    CG_D bool get(double& dt) const {
+        if (!ctl) { dt = fixed; return true; }
+        if (!ctl->active) return false;
+        dt = nsub > 0 ? 0.5 * (ctl->dt / nsub) : ctl->dt * scale;
+        return true;
+    }
+};
+
+// Output side of a sweep: fused wavespeed maximum (for the next step's dt) and status bits.
+struct SweepOut {
+    unsigned long long* smax;  // non-null: reduce the updated cells' wavespeed into it
+    StepCtl* ws_ctl;           // non-null: reduce into ws_ctl->smax[ws_ctl->it & 1] instead
+    int* status;               // non-null: OR status bits into it
+    const unsigned char* mask; // optional per-cell update mask (AMR masked steps)
+    CG_D unsigned long long* slot() const { return ws_ctl ? &ws_ctl->smax[ws_ctl->it & 1] : smax; }
+};
+
+template <class Pol>
+CG_D void load_cell(const Pol& pol, const typename Pol::S* src, const Geom& G, int i, int j, typename Pol::Cell& c) {
+    const size_t idx = (size_t)i * G.pitch + j;
+#pragma unroll
+    for (int f = 0; f < 5; f++) c.v[f] = (typename Pol::X)src[f * G.fstride + idx];
+}
+template <class Pol>
+CG_D void store_cell(const typename Pol::Cell& c, typename Pol::S* dst, const Geom& G, int i, int j) {
+    const size_t idx = (size_t)i * G.pitch + j;
+#pragma unroll
+    for (int f = 0; f < 5; f++) dst[f * G.fstride + idx] = (typename Pol::S)c.v[f];
+}
+
+// ------------------------------------------------------------------ X sweep: one row tile
+// NT threads; cells s0-2 .. s0+NT-1 staged in shared memory; NT half-step evolutions,
+// NT-1 interface fluxes, NT-2 updates per block.
+template <class Pol, int ORDER, int NT>
+__global__ void __launch_bounds__(NT) sweep_x_kernel(Pol pol, Geom G, const typename Pol::S* __restrict__ src,
+                                                     typename Pol::S* __restrict__ dst, DtSrc ds, SweepOut out) {
+    using X = typename Pol::X;
+    constexpr int TS = NT - 2;
+    __shared__ X sc[5][NT + 2];
+    __shared__ X sl[5][NT];
+    __shared__ X sr[5][NT];
+    __shared__ X sf[5][NT];
+    const int t = threadIdx.x;
+    const int row = blockIdx.y;
+    const int s0 = blockIdx.x * TS;
+    const int n = G.nx;
+    const int send = min(s0 + TS, n);  // one past the last updated cell
+    double dt;
+    const bool act = ds.get(dt);
+    if (!act) {  // inactive step: keep the ping-pong buffers consistent
+        if (s0 + t < send) {
+            typename Pol::Cell c;
+            load_cell(pol, src, G, row, s0 + t, c);
+            store_cell<Pol>(c, dst, G, row, s0 + t);
+        }
+        return;
+    }
+    pol.set_dt(dt);
+    // stage cells s0-2+t (and two more) with ghost mapping along x
+    for (int q = t; q < NT + 2; q += NT) {
+        const int k = s0 - 2 + q;
+        if (k <= send + 1) {
+            typename Pol::Cell c;
+            load_cell(pol, src, G, row, ghost_index(k, n, G.bc), c);
+#pragma unroll
+            for (int f = 0; f < 5; f++) sc[f][q] = c.v[f];
+        }
+    }
+    __syncthreads();
+    auto cell_at = [&](int q, typename Pol::Cell& c) {
+#pragma unroll
+        for (int f = 0; f < 5; f++) c.v[f] = sc[f][q];
+    };
+    // interface s0+t lies between cells s0+t-1 and s0+t; needed when either side updates
+    auto iface_needed = [&](int fi) {
+        if (fi < s0 || fi > send) return false;
+        const bool a = fi - 1 >= s0 && pol.active(row, fi - 1, out.mask);
+        const bool b = fi < send && pol.active(row, fi, out.mask);
+        return a || b;
+    };
+    if (ORDER == 2 && Pol::kShared) {
+        // half-step evolution of cell s0-1+t from smem cells t, t+1, t+2
+        const int k = s0 - 1 + t;
+        if (k <= send && (iface_needed(k) || iface_needed(k + 1))) {
+            typename Pol::Cell a, b, c;
+            typename Pol::Face L, R;
+            cell_at(t, a); cell_at(t + 1, b); cell_at(t + 2, c);
+            pol.recon(a, b, c, row, k, L, R);
+#pragma unroll
+            for (int f = 0; f < 5; f++) { sl[f][t] = L.v[f]; sr[f][t] = R.v[f]; }
+        }
+        __syncthreads();
+    }
+    {
+        const int fi = s0 + t;
+        if (t < NT - 1 && iface_needed(fi)) {
+            typename Pol::Face L, R;
+            if (ORDER == 1) {
+                typename Pol::Cell a, b;
+                cell_at(t + 1, a); cell_at(t + 2, b);
+                pol.face_of(a, L); pol.face_of(b, R);
+            } else if (Pol::kShared) {
+#pragma unroll
+                for (int f = 0; f < 5; f++) { L.v[f] = sr[f][t]; R.v[f] = sl[f][t + 1]; }
+            } else {
+                typename Pol::Cell a, b, c, d;
+                cell_at(t, a); cell_at(t + 1, b); cell_at(t + 2, c); cell_at(t + 3, d);
+                pol.recon_side(a, b, c, row, fi - 1, 1, L);
+                pol.recon_side(b, c, d, row, fi, 0, R);
+            }
+            V5<X> F;
+            pol.flux(L, R, row, fi, F);
+#pragma unroll
+            for (int f = 0; f < 5; f++) sf[f][t] = F.v[f];
+        }
+    }
+    __syncthreads();
+    double w = 0.0;
+    unsigned long long* const wslot = out.slot();
+    const int k = s0 + t;
+    if (t < TS && k < send) {
+        typename Pol::Cell c, nc;
+        cell_at(t + 2, c);
+        if (pol.active(row, k, out.mask)) {
+            V5<X> FL, FR;
+#pragma unroll
+            for (int f = 0; f < 5; f++) { FL.v[f] = sf[f][t]; FR.v[f] = sf[f][t + 1]; }
+            nc = pol.update(c, FL, FR, row, k);
+        } else {
+            nc = c;
+        }
+        store_cell<Pol>(nc, dst, G, row, k);
+        if (wslot) w = pol.wavespeed(nc, row, k);
+    }
+    if (wslot) block_max_to<NT>(wslot, w);
+    pol.flush_status(out.status);
+}
+
+// ------------------------------------------------------------------ Y sweep: column march
+// One thread per column marches SEG rows keeping the stencil in registers.
+template <class Pol, int ORDER, int NT, int SEG>
+__global__ void __launch_bounds__(NT) sweep_y_kernel(Pol pol, Geom G, const typename Pol::S* __restrict__ src,
+                                                     typename Pol::S* __restrict__ dst, DtSrc ds, SweepOut out) {
+    using X = typename Pol::X;
+    using Cell = typename Pol::Cell;
+    using Face = typename Pol::Face;
+    const int j = blockIdx.x * NT + threadIdx.x;
+    const int y0 = blockIdx.y * SEG;
+    const int n = G.ny;
+    const int y1 = min(y0 + SEG, n);
+    const bool col_ok = j < G.nx;
+    double dt;
+    const bool act = ds.get(dt);
+    if (!act) {
+        if (col_ok)
+            for (int y = y0; y < y1; y++) {
+                Cell c;
+                load_cell(pol, src, G, y, j, c);
+                store_cell<Pol>(c, dst, G, y, j);
+            }
+        return;
+    }
+    pol.set_dt(dt);
+    double w = 0.0;
+    unsigned long long* const wslot = out.slot();
+    if (col_ok) {
+        auto ld = [&](int y, Cell& c) { load_cell(pol, src, G, ghost_index(y, n, G.bc), j, c); };
+        auto need = [&](int fi) {  // interface between fi-1 and fi
+            const bool a = fi - 1 >= y0 && fi - 1 < y1 && pol.active(j, fi - 1, out.mask);
+            const bool b = fi >= y0 && fi < y1 && pol.active(j, fi, out.mask);
+            return a || b;
+        };
+        // window: cm1 = y-1, c0 = y, c1 = y+1, c2 = y+2
+        Cell cm2, cm1, c0, c1, c2;
+        ld(y0 - 2, cm2); ld(y0 - 1, cm1); ld(y0, c0); ld(y0 + 1, c1);
+        V5<X> Fp, Fn;
+        Face R0;  // right face of the current cell (shared recon)
+        if (ORDER == 1) {
+            if (need(y0)) { Face L, R; pol.face_of(cm1, L); pol.face_of(c0, R); pol.flux(L, R, j, y0, Fp); }
+        } else if (Pol::kShared) {
+            Face Lm1, Rm1, L0;
+            if (need(y0)) {
+                pol.recon(cm2, cm1, c0, j, y0 - 1, Lm1, Rm1);
+                pol.recon(cm1, c0, c1, j, y0, L0, R0);
+                pol.flux(Rm1, L0, j, y0, Fp);
+            } else {
+                pol.recon(cm1, c0, c1, j, y0, L0, R0);
+            }
+        } else {
+            if (need(y0)) {
+                Face L, R;
+                pol.recon_side(cm2, cm1, c0, j, y0 - 1, 1, L);
+                pol.recon_side(cm1, c0, c1, j, y0, 0, R);
+                pol.flux(L, R, j, y0, Fp);
+            }
+        }
+        for (int y = y0; y < y1; y++) {
+            ld(y + 2, c2);
+            const bool nf = need(y + 1);
+            if (ORDER == 1) {
+                if (nf) { Face L, R; pol.face_of(c0, L); pol.face_of(c1, R); pol.flux(L, R, j, y + 1, Fn); }
+            } else if (Pol::kShared) {
+                Face L1, R1;
+                pol.recon(c0, c1, c2, j, y + 1, L1, R1);
+                if (nf) pol.flux(R0, L1, j, y + 1, Fn);
+                R0 = R1;
+            } else {
+                if (nf) {
+                    Face L, R;
+                    pol.recon_side(cm1, c0, c1, j, y, 1, L);
+                    pol.recon_side(c0, c1, c2, j, y + 1, 0, R);
+                    pol.flux(L, R, j, y + 1, Fn);
+                }
+            }
+            Cell nc = c0;
+            if (pol.active(j, y, out.mask)) nc = pol.update(c0, Fp, Fn, j, y);
+            store_cell<Pol>(nc, dst, G, y, j);
+            if (wslot) { double ws = pol.wavespeed(nc, j, y); w = (ws > w) ? ws : w; }
+            Fp = Fn;
+            cm1 = c0; c0 = c1; c1 = c2;
+        }
+    }
+    if (wslot) block_max_to<NT>(wslot, w);
+    pol.flush_status(out.status);
+}
+
+// ------------------------------------------------------------------ helpers
+template <class Pol, int NT>
+__global__ void __launch_bounds__(NT) wavespeed_kernel(Pol pol, Geom G, const typename Pol::S* __restrict__ src,
+                                                       SweepOut out) {
+    double w = 0.0;
+    const size_t ncell = (size_t)G.nx * G.ny;
+    for (size_t c = (size_t)blockIdx.x * NT + threadIdx.x; c < ncell; c += (size_t)gridDim.x * NT) {
+        const int i = (int)(c / G.nx), j = (int)(c % G.nx);
+        typename Pol::Cell cc;
+        load_cell(pol, src, G, i, j, cc);
+        // wavespeed takes (line, k) in the X-sweep convention: line = row i, k = column j
+        const double ws = pol.wavespeed(cc, i, j);
+        w = (ws > w) ? ws : w;
+    }
+    block_max_to<NT>(out.slot(), w);
+}
+
+}  // namespace cg

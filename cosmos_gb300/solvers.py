@@ -1,0 +1,364 @@
+"""Reference-named host API over the C ABI.
+
+Mirrors the reference's static solver classes (Solvers/*.hpp) with the same method names and
+argument meaning, on numpy arrays of primitive states: shape (nx, 5) for 1D and (ny, nx, 5) for
+2D with (rho, vx, vy, vz, p) per cell -- the reference's vector<StateVector> /
+vector<vector<StateVector>> indexed [row i = y][column j = x].
+
+  * solve / solve2D return a new array (the reference returns grids by value);
+  * the per-sweep functions (computeSLICTimeStep, computeXSLICTimeStep2D, ...) update the array
+    in place (the reference takes vector& and mutates it);
+  * every call runs on the GPU through libcosmos_gb300.so; extra keyword arguments select the
+    precision (FP64 reproduces the reference bit for bit; FP32 is the Newtonian bulk path) and
+    the boundary (transmissive as in the reference, or periodic).
+"""
+import ctypes
+import threading
+
+import numpy as np
+
+from . import _lib
+from ._lib import (BC_PERIODIC, BC_TRANSMISSIVE, FP32, FP64, GR, NEWTONIAN, SR, Params, SolveOpts,  # noqa: F401
+                   SolveResult, check, load)
+
+_tls = threading.local()
+
+
+class EulerMaterialParameters:
+    """Euler/EulerMaterialParameters.cpp:3-21 (default adiabatic index 1.0)."""
+
+    def __init__(self, adiabaticIndex=1.0):
+        self.adiabaticIndex = float(adiabaticIndex)
+
+    def setAdiabaticIndex(self, g):
+        self.adiabaticIndex = float(g)
+
+    def getAdiabaticIndex(self):
+        return self.adiabaticIndex
+
+
+class BlackHoleSpacetime:
+    """BlackHoleEuler/BlackHoleSpacetime.cpp:3-52 constructors: (), (M), (M, x, y, z), (M, a),
+    (M, a, x, y, z); defaults M = 1, a = 0, position (0.5, 0.5, 0)."""
+
+    def __init__(self, *args):
+        m, a, x, y, z = 1.0, 0.0, 0.5, 0.5, 0.0
+        if len(args) == 1:
+            m = args[0]
+        elif len(args) == 2:
+            m, a = args
+        elif len(args) == 4:
+            m, x, y, z = args
+        elif len(args) == 5:
+            m, a, x, y, z = args
+        elif len(args) != 0:
+            raise TypeError("BlackHoleSpacetime takes 0, 1, 2, 4 or 5 arguments")
+        self.mass, self.spin, self.x, self.y, self.z = map(float, (m, a, x, y, z))
+
+    def getBlackHoleMass(self):
+        return self.mass
+
+    def getBlackHoleSpin(self):
+        return self.spin
+
+
+class Context:
+    """A CUDA stream on one device (cosmos_ctx)."""
+
+    def __init__(self, device=0):
+        L = load()
+        h = ctypes.c_void_p()
+        check(L.cosmos_ctx_create(device, ctypes.byref(h)))
+        self.h = h
+
+    def synchronize(self):
+        check(load().cosmos_ctx_synchronize(self.h))
+
+    @property
+    def stream(self):
+        return load().cosmos_ctx_stream(self.h)
+
+    def close(self):
+        if self.h:
+            load().cosmos_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def default_context():
+    c = getattr(_tls, "ctx", None)
+    if c is None:
+        c = _tls.ctx = Context(0)
+    return c
+
+
+class Grid:
+    """A device-resident grid (cosmos_grid)."""
+
+    def __init__(self, system, shape, dx, gamma, precision=FP64, boundary=BC_TRANSMISSIVE, black_hole=None,
+                 ctx=None):
+        self.ctx = ctx or default_context()
+        p = Params()
+        load().cosmos_params_default(ctypes.byref(p))
+        p.system = system
+        if len(shape) == 1:
+            p.dims, p.nx, p.ny = 1, shape[0], 1
+        else:
+            p.dims, p.ny, p.nx = 2, shape[0], shape[1]
+        p.precision, p.boundary, p.gamma, p.dx = precision, boundary, float(gamma), float(dx)
+        if black_hole is not None:
+            p.bh_mass, p.bh_spin = black_hole.mass, black_hole.spin
+            p.bh_x, p.bh_y, p.bh_z = black_hole.x, black_hole.y, black_hole.z
+        self.params = p
+        self.shape = tuple(shape)
+        h = ctypes.c_void_p()
+        check(load().cosmos_grid_create(self.ctx.h, ctypes.byref(p), ctypes.byref(h)))
+        self.h = h
+
+    @property
+    def ncell(self):
+        return int(np.prod(self.shape))
+
+    def set_prim(self, prim):
+        a = np.ascontiguousarray(prim, dtype=np.float64)
+        if a.shape != self.shape + (5,):
+            raise ValueError(f"expected shape {self.shape + (5,)}, got {a.shape}")
+        check(load().cosmos_grid_set_prim(self.h, a.ctypes.data, a.size))
+
+    def get_prim(self, out=None):
+        o = np.empty(self.shape + (5,), dtype=np.float64) if out is None else out
+        check(load().cosmos_grid_get_prim(self.h, o.ctypes.data, o.size))
+        return o
+
+    def sweep(self, axis, order, dt, bias, limiter):
+        check(load().cosmos_grid_sweep(self.h, axis, order, float(dt), float(bias), int(limiter)))
+
+    def rk_source(self, dt, bias, limiter):
+        check(load().cosmos_grid_rk_source(self.h, float(dt), float(bias), int(limiter)))
+
+    def max_wavespeed(self):
+        v = ctypes.c_double()
+        check(load().cosmos_grid_max_wavespeed(self.h, ctypes.byref(v)))
+        return v.value
+
+    def stable_dt(self, cfl, t, t_final, iteration):
+        v = ctypes.c_double()
+        check(load().cosmos_grid_stable_dt(self.h, float(cfl), float(t), float(t_final), int(iteration),
+                                           ctypes.byref(v)))
+        return v.value
+
+    @staticmethod
+    def opts(order, cfl, t_final, bias, limiter, subcycles=1, max_steps=-1):
+        o = SolveOpts()
+        o.order, o.cfl, o.t_final, o.bias = int(order), float(cfl), float(t_final), float(bias)
+        o.limiter, o.subcycles, o.max_steps = int(limiter), int(subcycles), int(max_steps)
+        return o
+
+    def solve(self, order, cfl, t_final, bias, limiter, subcycles=1, max_steps=-1):
+        o = self.opts(order, cfl, t_final, bias, limiter, subcycles, max_steps)
+        r = SolveResult()
+        check(load().cosmos_grid_solve(self.h, ctypes.byref(o), ctypes.byref(r)))
+        return r
+
+    def run_begin(self, order, cfl, t_final, bias, limiter, subcycles=1, max_steps=-1):
+        o = self.opts(order, cfl, t_final, bias, limiter, subcycles, max_steps)
+        check(load().cosmos_grid_run_begin(self.h, ctypes.byref(o)))
+
+    def run_steps(self, n):
+        check(load().cosmos_grid_run_steps(self.h, int(n)))
+
+    def run_end(self):
+        r = SolveResult()
+        check(load().cosmos_grid_run_end(self.h, ctypes.byref(r)))
+        return r
+
+    def field_sums(self):
+        o = np.zeros(5)
+        check(load().cosmos_grid_field_sums(self.h, o.ctypes.data))
+        return o
+
+    def amr_flags(self, tol, coarse=None, fine=None):
+        nc = self.ncell
+        nf = nc * (4 if len(self.shape) == 2 else 2)
+        c = np.ones(nc, np.uint8) if coarse is None else np.ascontiguousarray(coarse, np.uint8).reshape(-1).copy()
+        f = np.zeros(nf, np.uint8) if fine is None else np.ascontiguousarray(fine, np.uint8).reshape(-1).copy()
+        check(load().cosmos_grid_amr_flags(self.h, float(tol), c.ctypes.data, f.ctypes.data))
+        return c, f
+
+    def amr_derefine(self, fine_grid, tol, coarse, fine):
+        c = np.ascontiguousarray(coarse, np.uint8).reshape(-1).copy()
+        f = np.ascontiguousarray(fine, np.uint8).reshape(-1).copy()
+        check(load().cosmos_grid_amr_derefine(self.h, fine_grid.h, float(tol), c.ctypes.data, f.ctypes.data))
+        return c, f
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().cosmos_grid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _shape(cells):
+    a = np.asarray(cells)
+    if a.ndim == 2 and a.shape[1] == 5:
+        return (a.shape[0],)
+    if a.ndim == 3 and a.shape[2] == 5:
+        return (a.shape[0], a.shape[1])
+    raise ValueError("cells must have shape (nx, 5) or (ny, nx, 5)")
+
+
+def _solve(system, cells, dx, cfl, t_final, bias, lim, mp, order, bh=None, subcycles=1, precision=FP64,
+           boundary=BC_TRANSMISSIVE, max_steps=-1):
+    g = Grid(system, _shape(cells), dx, mp.getAdiabaticIndex(), precision, boundary, bh)
+    try:
+        g.set_prim(cells)
+        r = g.solve(order, cfl, t_final, bias, lim, subcycles, max_steps)
+        out = g.get_prim()
+    finally:
+        g.close()
+    out_steps = r.steps
+    return out, out_steps
+
+
+def _sweep_inplace(system, cells, dx, dt, axis, order, bias, lim, mp, bh=None, precision=FP64,
+                   boundary=BC_TRANSMISSIVE):
+    g = Grid(system, _shape(cells), dx, mp.getAdiabaticIndex(), precision, boundary, bh)
+    try:
+        g.set_prim(cells)
+        g.sweep(axis, order, dt, bias, lim)
+        cells[...] = g.get_prim()
+    finally:
+        g.close()
+
+
+def _family(system, name):
+    """Build the First/SecondOrderSolver and Solvers classes of one system."""
+    bh_kw = system == GR
+
+    class SecondOrder:
+        __qualname__ = f"{name}SecondOrderSolver"
+
+        @staticmethod
+        def solve(initialCells, cellSpacing, CFLCoefficient, finalTime, bias, slopeLimiter, *rest, **kw):
+            sub, mp, bh = _unpack(rest, bh_kw)
+            return _solve(system, initialCells, cellSpacing, CFLCoefficient, finalTime, bias, slopeLimiter, mp, 2,
+                          bh, sub, **kw)[0]
+
+        solve2D = solve
+
+        @staticmethod
+        def computeSLICTimeStep(currentCells, cellSpacing, timeStep, bias, slopeLimiter, *rest, **kw):
+            _, mp, bh = _unpack(rest, bh_kw, has_sub=False)
+            _sweep_inplace(system, currentCells, cellSpacing, timeStep, 0, 2, bias, slopeLimiter, mp, bh, **kw)
+
+        computeXSLICTimeStep2D = computeSLICTimeStep
+
+        @staticmethod
+        def computeYSLICTimeStep2D(currentCells, cellSpacing, timeStep, bias, slopeLimiter, *rest, **kw):
+            _, mp, bh = _unpack(rest, bh_kw, has_sub=False)
+            _sweep_inplace(system, currentCells, cellSpacing, timeStep, 1, 2, bias, slopeLimiter, mp, bh, **kw)
+
+    class FirstOrder:
+        __qualname__ = f"{name}FirstOrderSolver"
+
+        @staticmethod
+        def solve(initialCells, cellSpacing, CFLCoefficient, finalTime, *rest, **kw):
+            sub, mp, bh = _unpack(rest, bh_kw)
+            return _solve(system, initialCells, cellSpacing, CFLCoefficient, finalTime, 0.0, 1, mp, 1, bh, sub,
+                          **kw)[0]
+
+        solve2D = solve
+
+        @staticmethod
+        def computeFORCETimeStep(currentCells, cellSpacing, timeStep, *rest, **kw):
+            _, mp, bh = _unpack(rest, bh_kw, has_sub=False)
+            _sweep_inplace(system, currentCells, cellSpacing, timeStep, 0, 1, 0.0, 1, mp, bh, **kw)
+
+        computeXFORCETimeStep2D = computeFORCETimeStep
+
+        @staticmethod
+        def computeYFORCETimeStep2D(currentCells, cellSpacing, timeStep, *rest, **kw):
+            _, mp, bh = _unpack(rest, bh_kw, has_sub=False)
+            _sweep_inplace(system, currentCells, cellSpacing, timeStep, 1, 1, 0.0, 1, mp, bh, **kw)
+
+    class Utilities:
+        __qualname__ = f"{name}Solvers"
+
+        @staticmethod
+        def computeMaximumWaveSpeed(currentCells, materialParameters, blackHole=None, **kw):
+            g = Grid(system, _shape(currentCells), 1.0, materialParameters.getAdiabaticIndex(), black_hole=blackHole,
+                     **kw)
+            try:
+                g.set_prim(currentCells)
+                return g.max_wavespeed()
+            finally:
+                g.close()
+
+        computeMaximumWaveSpeed2D = computeMaximumWaveSpeed
+
+        @staticmethod
+        def computeStableTimeStep(*args, **kw):
+            if len(args) == 4:  # (timeStep, currentTime, finalTime, currentIteration)
+                return load().cosmos_stable_dt_rule(*map(float, args[:3]), int(args[3]))
+            cells, dx, cfl, t, tf, it, mp = args[:7]
+            bh = args[7] if len(args) > 7 else None
+            g = Grid(system, _shape(cells), dx, mp.getAdiabaticIndex(), black_hole=bh, **kw)
+            try:
+                g.set_prim(cells)
+                return g.stable_dt(cfl, t, tf, it)
+            finally:
+                g.close()
+
+        computeStableTimeStep2D = computeStableTimeStep
+
+    return SecondOrder, FirstOrder, Utilities
+
+
+def _unpack(rest, gr, has_sub=True):
+    """Positional tail after the common arguments: Newtonian/SR (materialParameters); GR
+    ([subcyclingIterations,] materialParameters, blackHole)."""
+    if not gr:
+        return 1, rest[0], None
+    if has_sub:
+        return int(rest[0]), rest[1], rest[2]
+    return 1, rest[0], rest[1]
+
+
+EulerSecondOrderSolver, EulerFirstOrderSolver, EulerSolvers = _family(NEWTONIAN, "Euler")
+RelativisticEulerSecondOrderSolver, RelativisticEulerFirstOrderSolver, RelativisticEulerSolvers = _family(
+    SR, "RelativisticEuler")
+BlackHoleEulerSecondOrderSolver, BlackHoleEulerFirstOrderSolver, BlackHoleEulerSolvers = _family(GR, "BlackHoleEuler")
+
+
+class BlackHoleEulerForcingSolver:
+    """Solvers/BlackHoleEulerForcingSolver.hpp: RK4 source step (in place)."""
+
+    @staticmethod
+    def computeRungeKuttaTimeStep(currentCells, cellSpacing, timeStep, bias, slopeLimiter, materialParameters,
+                                  blackHole):
+        g = Grid(GR, _shape(currentCells), cellSpacing, materialParameters.getAdiabaticIndex(), black_hole=blackHole)
+        try:
+            g.set_prim(currentCells)
+            g.rk_source(timeStep, bias, slopeLimiter)
+            currentCells[...] = g.get_prim()
+        finally:
+            g.close()
+
+    computeRungeKuttaTimeStep2D = computeRungeKuttaTimeStep
+
+
+def solve_with_steps(system, cells, dx, cfl, t_final, bias, limiter, gamma, order=2, black_hole=None, subcycles=1,
+                     precision=FP64, boundary=BC_TRANSMISSIVE, max_steps=-1):
+    """solve() that also returns the step count (the reference prints it per step)."""
+    return _solve(system, cells, dx, cfl, t_final, bias, limiter, EulerMaterialParameters(gamma), order, black_hole,
+                  subcycles, precision, boundary, max_steps)

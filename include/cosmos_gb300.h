@@ -1,0 +1,170 @@
+/*
+ * cosmos_gb300 -- C ABI of the GB300 implementation of the Cosmos finite-volume SLIC/FORCE path
+ * (Newtonian, special-relativistic and black-hole (Kerr-Schild 3+1) Euler equations).
+ *
+ * The reference exposes this path as static C++ methods on value-semantics grids
+ * (vector<StateVector> / vector<vector<StateVector>>, primitive variables rho, vx, vy, vz, p).
+ * This ABI keeps the same operations and argument meaning with plain pointers:
+ *   - grids are device-resident handles (cosmos_grid) created from a cosmos_params;
+ *   - host data crosses as arrays of primitive states, 5 doubles per cell, row-major
+ *     [ny][nx] (row i = y, column j = x), exactly the reference's grid layout;
+ *   - every call returns a status code (COSMOS_OK == 0); cosmos_last_error() describes failures
+ *     (the reference itself has no error reporting).
+ * Reference paths are relative to the JonathanGorard/Cosmos tree.
+ *
+ * Precision: COSMOS_FP64 runs the reference's arithmetic in the reference's operation order
+ * (results are bit-identical to the reference's CPU solver); COSMOS_FP32 runs the Newtonian
+ * system with FP32 conserved storage and arithmetic.
+ *
+ * Threading: one cosmos_ctx per host thread; calls on a context are serialised on its stream.
+ */
+#ifndef COSMOS_GB300_H
+#define COSMOS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes */
+#define COSMOS_OK 0
+#define COSMOS_EINVAL 1       /* bad argument (size, enum, pointer) */
+#define COSMOS_ECUDA 2        /* CUDA runtime error */
+#define COSMOS_ENONFINITE 3   /* the solver produced a non-finite time step */
+#define COSMOS_EUNSUPPORTED 4 /* combination not provided (e.g. FP32 for the GR system) */
+#define COSMOS_ESTATE 5       /* call order violated */
+
+/* ---- device status bits reported by cosmos_solve_result.status */
+#define COSMOS_STATUS_NONFINITE 1  /* non-finite or non-positive dt was produced */
+#define COSMOS_STATUS_NEWTON_CAP 2 /* a con2prim Newton solve stopped at its 1000-iteration cap */
+
+/* ---- enumerations */
+enum { COSMOS_NEWTONIAN = 0, COSMOS_SR = 1, COSMOS_GR = 2 };
+enum { COSMOS_FP64 = 0, COSMOS_FP32 = 1 };
+enum { COSMOS_BC_TRANSMISSIVE = 0, COSMOS_BC_PERIODIC = 1 };
+/* Solvers/SlopeLimiters.cpp:55-69: 0 SuperBee, 1 van Leer, anything else MinBee */
+enum { COSMOS_SUPERBEE = 0, COSMOS_VANLEER = 1, COSMOS_MINBEE = 2 };
+
+/* Grid description.  Replaces the reference's (initialCells shape, cellSpacing,
+ * EulerMaterialParameters, BlackHoleSpacetime) arguments:
+ *   gamma  -- EulerMaterialParameters adiabatic index (Euler/EulerMaterialParameters.cpp:3-21)
+ *   bh_*   -- BlackHoleSpacetime(mass, spin, x, y, z) (BlackHoleEuler/BlackHoleSpacetime.cpp:3-52)
+ * dims 1 uses ny = 1.  boundary: the reference only has transmissive ghost cells
+ * (Solvers/EulerSolvers.cpp:3-85); periodic is an extension (Newtonian and SR only). */
+typedef struct cosmos_params {
+    int system;
+    int dims;
+    int nx;
+    int ny;
+    int precision;
+    int boundary;
+    double gamma;
+    double dx;
+    double bh_mass, bh_spin, bh_x, bh_y, bh_z;
+} cosmos_params;
+
+/* Solver options: the reference's solve() arguments (CFLCoefficient, finalTime, bias,
+ * slopeLimiter, subcyclingIterations; Solvers/EulerSecondOrderSolver.hpp:24-28,
+ * Solvers/BlackHoleEulerSecondOrderSolver.hpp:26-32) plus run control. */
+typedef struct cosmos_solve_opts {
+    int order;       /* 2 = SLIC (SecondOrderSolver), 1 = FORCE (FirstOrderSolver) */
+    double cfl;
+    double t_final;
+    double bias;
+    int limiter;
+    int subcycles;   /* GR only: RK source half-steps before and after the flux step */
+    int max_steps;   /* < 0: run until t >= t_final; otherwise stop after max_steps steps */
+} cosmos_solve_opts;
+
+typedef struct cosmos_solve_result {
+    int steps;       /* the reference's currentIteration at exit */
+    double t;        /* the reference's currentTime at exit */
+    int status;      /* COSMOS_STATUS_* bits */
+} cosmos_solve_result;
+
+typedef struct cosmos_ctx cosmos_ctx;
+typedef struct cosmos_grid cosmos_grid;
+
+/* ---- context */
+int cosmos_ctx_create(int device, cosmos_ctx** out);
+int cosmos_ctx_destroy(cosmos_ctx* ctx);
+int cosmos_ctx_synchronize(cosmos_ctx* ctx);
+void* cosmos_ctx_stream(cosmos_ctx* ctx); /* the cudaStream_t all work of this context runs on */
+const char* cosmos_last_error(void);      /* thread-local description of the last failure */
+unsigned long long cosmos_kernel_launches(void); /* kernels launched by this library (all threads) */
+const char* cosmos_version(void);
+
+void cosmos_params_default(cosmos_params* p);
+void cosmos_solve_opts_default(cosmos_solve_opts* o);
+
+/* ---- grids (device state: structure of arrays; FP64 keeps primitives, FP32 conserved) */
+int cosmos_grid_create(cosmos_ctx* ctx, const cosmos_params* p, cosmos_grid** out);
+int cosmos_grid_destroy(cosmos_grid* g);
+/* n_doubles must equal 5 * nx * ny.  Replaces constructing the reference's initialCells. */
+int cosmos_grid_set_prim(cosmos_grid* g, const double* prim, size_t n_doubles);
+/* Returns the grid as primitive states (the reference's returned grid). */
+int cosmos_grid_get_prim(cosmos_grid* g, double* prim, size_t n_doubles);
+
+/* One dimensional sweep with time step dt, in place on the grid.
+ * axis 0 / order 2: EulerSecondOrderSolver::computeXSLICTimeStep2D (2D) or computeSLICTimeStep (1D)
+ *   (Solvers/EulerSecondOrderSolver.cpp:27-73); axis 1: computeYSLICTimeStep2D (:75-100);
+ * order 1: EulerFirstOrderSolver::computeFORCETimeStep / computeX/YFORCETimeStep2D
+ *   (Solvers/EulerFirstOrderSolver.cpp:103-155);
+ * SR and GR twins: Solvers/RelativisticEulerSecondOrderSolver.cpp:27-130,
+ *   Solvers/BlackHoleEulerSecondOrderSolver.cpp:39-179 (with excision),
+ *   Solvers/BlackHoleEulerFirstOrderSolver.cpp:89-165. */
+int cosmos_grid_sweep(cosmos_grid* g, int axis, int order, double dt, double bias, int limiter);
+
+/* GR source term step: BlackHoleEulerForcingSolver::computeRungeKuttaTimeStep(2D)
+ * (Solvers/BlackHoleEulerForcingSolver.cpp:187-250; classical RK4 with interleaved
+ * fractional flux sweeps). */
+int cosmos_grid_rk_source(cosmos_grid* g, double dt, double bias, int limiter);
+
+/* EulerSolvers::computeMaximumWaveSpeed(2D) (Solvers/EulerSolvers.cpp:87-128) and twins
+ * (Solvers/RelativisticEulerSolvers.cpp:87-128, Solvers/BlackHoleEulerSolvers.cpp:87-131). */
+int cosmos_grid_max_wavespeed(cosmos_grid* g, double* out);
+/* EulerSolvers::computeStableTimeStep(2D) with the grid's state (Solvers/EulerSolvers.cpp:147-161). */
+int cosmos_grid_stable_dt(cosmos_grid* g, double cfl, double t, double t_final, int iteration, double* dt_out);
+/* EulerSolvers::computeStableTimeStep(dt, t, T, it) (Solvers/EulerSolvers.cpp:130-145). */
+double cosmos_stable_dt_rule(double dt, double t, double t_final, int iteration);
+
+/* Full solve on the device: EulerSecondOrderSolver::solve / solve2D
+ * (Solvers/EulerSecondOrderSolver.cpp:102-147), EulerFirstOrderSolver::solve / solve2D
+ * (Solvers/EulerFirstOrderSolver.cpp:171-216), the SR twins and
+ * BlackHoleEulerSecondOrderSolver::solve / solve2D (Solvers/BlackHoleEulerSecondOrderSolver.cpp:
+ * 144-218).  The time step is computed on the device every step and the step sequence replays
+ * from captured CUDA graphs. */
+int cosmos_grid_solve(cosmos_grid* g, const cosmos_solve_opts* o, cosmos_solve_result* r);
+
+/* Split form of cosmos_grid_solve for callers that time or pipeline steps:
+ * run_begin resets the step controller (t = 0, iteration 0) and enqueues the initial CFL
+ * reduction; run_steps enqueues n steps without synchronising; run_end synchronises and reports. */
+int cosmos_grid_run_begin(cosmos_grid* g, const cosmos_solve_opts* o);
+int cosmos_grid_run_steps(cosmos_grid* g, int n);
+int cosmos_grid_run_end(cosmos_grid* g, cosmos_solve_result* r);
+
+/* Per-field sums of the stored state (FP64 grids: primitives; FP32 grids: conserved),
+ * compensated FP64 accumulation, deterministic order.  Used for conservation drift. */
+int cosmos_grid_field_sums(cosmos_grid* g, double out[5]);
+
+/* AMR refinement flag pass of the Level-1 drivers (AMR/EulerAMR.cpp:207-229 1D, :400-431 2D;
+ * AMR/RelativisticEulerAMR.cpp:404-435; AMR/BlackHoleEulerAMR.cpp:276-300, :484-515):
+ * coarse[c] = 0 and its fine children = 1 where any conserved one-sided gradient reaches tol;
+ * other flags are left as passed in.  coarse: nx*ny bytes, fine: 2*nx (1D) or 4*nx*ny (2D). */
+int cosmos_grid_amr_flags(cosmos_grid* g, double tol, unsigned char* coarse, unsigned char* fine);
+/* AMR derefinement pass (AMR/EulerAMR.cpp:310-345, :538-586): on the fine grid with the coarse
+ * dx at tol/2; unflags children, flags the parent and restricts the coarse state. */
+int cosmos_grid_amr_derefine(cosmos_grid* coarse, cosmos_grid* fine, double tol, unsigned char* coarse_flags,
+                             unsigned char* fine_flags);
+
+/* One-shot drop-in for the reference's static solve entry points with host buffers:
+ * prim_in/prim_out are 5*nx*ny doubles (may alias). */
+int cosmos_solve_prim(const cosmos_params* p, const double* prim_in, double* prim_out, const cosmos_solve_opts* o,
+                      cosmos_solve_result* r);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COSMOS_GB300_H */

@@ -1,0 +1,74 @@
+"""Seeded synthetic states shared by the golden-fixture generator and the tests.
+
+Shapes and value ranges follow the benchmark configurations: Newtonian states with
+rho in [0.1, 1.5], |u|, |v| <= 1, p in [0.03, 1.5]; SR states with |v| well below 1; GR states
+around a Schwarzschild/Kerr hole with some cells inside the excision radius.
+"""
+import numpy as np
+
+SYS_GAMMA = {0: 1.4, 1: 5.0 / 3.0, 2: 5.0 / 3.0}
+
+
+def newton_state(rng, shape, vz=0.2):
+    p = np.zeros(tuple(shape) + (5,))
+    p[..., 0] = rng.uniform(0.1, 1.5, shape)
+    p[..., 1] = rng.uniform(-1.0, 1.0, shape)
+    p[..., 2] = rng.uniform(-1.0, 1.0, shape)
+    p[..., 3] = rng.uniform(-vz, vz, shape)
+    p[..., 4] = rng.uniform(0.03, 1.5, shape)
+    return p
+
+
+def sr_state(rng, shape):
+    p = np.zeros(tuple(shape) + (5,))
+    p[..., 0] = rng.uniform(0.5, 2.0, shape)
+    p[..., 1] = rng.uniform(-0.4, 0.4, shape)
+    p[..., 2] = rng.uniform(-0.4, 0.4, shape)
+    p[..., 3] = rng.uniform(-0.1, 0.1, shape)
+    p[..., 4] = rng.uniform(0.1, 1.5, shape)
+    return p
+
+
+def gr_state(rng, shape):
+    p = np.zeros(tuple(shape) + (5,))
+    p[..., 0] = rng.uniform(0.5, 1.5, shape)
+    p[..., 1] = rng.uniform(-0.2, 0.2, shape)
+    p[..., 2] = rng.uniform(-0.2, 0.2, shape)
+    p[..., 3] = rng.uniform(-0.05, 0.05, shape)
+    p[..., 4] = rng.uniform(0.05, 0.5, shape)
+    return p
+
+
+def state(system, rng, shape):
+    return {0: newton_state, 1: sr_state, 2: gr_state}[system](rng, shape)
+
+
+def sod(n=1000):
+    """Sod shock tube (Tests/EulerTests.cpp:3-30): left (1, 0, 1) for i <= n/2, right (0.125, 0, 0.1)."""
+    p = np.zeros((n, 5))
+    for i in range(n):
+        p[i] = (1.0, 0.0, 0.0, 0.0, 1.0) if i <= 0.5 * n else (0.125, 0.0, 0.0, 0.0, 0.1)
+    return p
+
+
+def four_quadrant(n, seed):
+    """2D four-quadrant Riemann problem, per-quadrant (rho, u, v, p) drawn by seed."""
+    rng = np.random.default_rng(seed)
+    q = np.zeros((4, 5))
+    q[:, 0] = rng.uniform(0.1, 1.5, 4)
+    q[:, 1] = rng.uniform(-1.0, 1.0, 4)
+    q[:, 2] = rng.uniform(-1.0, 1.0, 4)
+    q[:, 4] = rng.uniform(0.03, 1.5, 4)
+    p = np.zeros((n, n, 5))
+    h = n // 2
+    p[:h, :h] = q[0]
+    p[:h, h:] = q[1]
+    p[h:, :h] = q[2]
+    p[h:, h:] = q[3]
+    return p
+
+
+# GR test hole: a Schwarzschild (and a spinning) hole inside a unit box, so that a small grid has
+# excised cells, stencils crossing the horizon and plain cells.
+GR_BH = (0.1, 0.0, 0.5, 0.5, 0.0)
+GR_BH_SPIN = (0.1, 0.9, 0.47, 0.52, 0.0)
