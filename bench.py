@@ -1,0 +1,333 @@
+"""Benchmark: 2D Newtonian SLIC (MinBee), FP32 bulk vs FP64, 4096 x 4096 cells, periodic.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 4096]
+
+One "step" is one Strang step X(dt/2) Y(dt) X(dt/2) of the whole grid with the time step computed
+on the device from the previous step's CFL reduction (the reference's solve2D loop body,
+Solvers/EulerSecondOrderSolver.cpp:131-146).  Metric: cell-updates per second.
+
+Our arm prints one JSON line with
+  value           FP32 cell-updates/s with the state resident in HBM (CUDA events on the library's
+                  stream around K graph-replayed steps; the 335 MB state exceeds the 129 MB L2, so no
+                  flush is needed between steps),
+  e2e             the same steps through the C ABI with pinned host buffers: every step copies the
+                  grid's primitive state (5 doubles per cell) host->device, runs the step and copies
+                  the state back (the reference-facing per-step call, whose grids live on the host),
+  fp64            the plain FP64 (reference-exact) path on the same workload,
+  l1_rho_fp32_vs_fp64  relative L1 density error of the FP32 run against the FP64 run,
+  roofline        per-kernel achieved HBM GB/s for the dominant kernel (the X sweep) against the
+                  measured copy bandwidth in MEASURED_PEAKS.json,
+  cpu_baseline    the CPU oracle (FP64 restatement of the reference) on the host cores, bounded sample.
+--impl reference times the CPU path alone (all host threads) on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+WORKLOAD = "config2: 2D Newtonian Euler SLIC MinBee, 4096x4096 on [0,1]^2, gamma 1.4, CFL 0.9, periodic, " \
+           "four-quadrant Riemann data (seed 2)"
+METRIC = "cell-updates/s"
+
+
+def four_quadrant(n, seed):
+    import cases
+    return cases.four_quadrant(n, seed)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, gpu):
+        self.gpu, self.samples, self.proc = gpu, [], None
+
+    def __enter__(self):
+        q = "clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+            "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+            "clocks_event_reasons.sw_power_cap,utilization.gpu"
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        load = [s for s in self.samples if num(s[7]) and num(s[7]) > 50] or self.samples
+        sm = [num(s[0]) for s in load if num(s[0])]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in load for k in range(4) if s[3 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": num(load[0][1]), "reasons": reasons, "samples": len(self.samples),
+                "samples_under_load": len(load)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_per_launch(kernel):
+    """DRAM bytes per launch from the committed ncu summary (profiles/traffic.json), if present."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            t = json.load(f)
+        return t.get(kernel)
+    except Exception:
+        return None
+
+
+def cpu_baseline(n, seconds=12.0, threads=None):
+    """Time the CPU oracle (FP64 restatement of the reference, line-parallel on all host cores) on
+    the same workload: as many full-size Strang steps as fit in `seconds` (at least one)."""
+    from oracle.pyoracle import Oracle
+    O = Oracle()
+    cores = threads or os.cpu_count() or 1
+    O.set_threads(cores)
+    s = four_quadrant(n, 2)
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        s, k, _, _ = O.solve(0, s, 2, 1.0 / n, 0.9, 1e9, 0.0, 2, 1.4, 1, max_steps=1)
+        steps += k
+        el = time.perf_counter() - t0
+        if el >= seconds or steps >= 50:
+            break
+    rate = steps * n * n / el
+    return {"value": rate, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"{steps} full {n}x{n} Strang steps of the FP64 oracle (restatement of the reference, "
+                      f"bit-identical to it) in {el:.1f} s on {cores} host threads"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    n = args.n
+    base = cpu_baseline(n, seconds=max(8.0, 2.0 * args.steps))
+    line = {"metric": METRIC, "value": base["value"], "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": n * n / base["value"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "n": n, "cells": n * n},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import cosmos_gb300 as cg
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    L = cg.load()
+    ctx = cg.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    n = args.n
+    s0 = four_quadrant(n, 2)
+    cells = n * n
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(v):
+        if world == 1:
+            return v
+        import torch.distributed as dist
+        t = torch.tensor([v], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---------------- FP32 resident: value
+    g = cg.Grid(cg.NEWTONIAN, (n, n), 1.0 / n, 1.4, cg.FP32, cg.BC_PERIODIC, ctx=ctx)
+    g.set_prim(s0)
+    g.run_begin(2, 0.9, 1e30, 0.0, cg.MINBEE)
+    g.run_steps(args.warmup)
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = L.cosmos_kernel_launches()
+    barrier()
+    with Clocks(local) as clk:
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            g.run_steps(args.steps)
+            e1.record(stream)
+        e1.synchronize()
+    barrier()
+    launches = L.cosmos_kernel_launches() - launches0
+    ms = max_over_ranks(e0.elapsed_time(e1)) / args.steps
+    r = g.run_end()
+    value = cells * world / (ms * 1e-3)
+
+    # ---------------- per-kernel durations for the roofline (individual launches, events between)
+    dt_probe = 0.5 * 0.9 / n / 2.0
+    kern = {"x": [], "y": []}
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            g.sweep(0, 2, dt_probe, 0.0, cg.MINBEE)
+            g.sweep(1, 2, dt_probe, 0.0, cg.MINBEE)
+        for _ in range(max(4, args.steps // 2)):
+            for ax, key in ((0, "x"), (1, "y")):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                g.sweep(ax, 2, dt_probe, 0.0, cg.MINBEE)
+                b.record(stream)
+                kern[key].append((a, b))
+    torch.cuda.synchronize()
+    kx = statistics.mean(a.elapsed_time(b) for a, b in kern["x"])
+    ky = statistics.mean(a.elapsed_time(b) for a, b in kern["y"])
+    peak, peak_kind = peaks()
+    bytes_sweep = cells * 40  # 5 FP32 fields read + 5 written per cell (halo re-reads not counted)
+    x_gbs = bytes_sweep / (kx * 1e-3) / 1e9
+    y_gbs = bytes_sweep / (ky * 1e-3) / 1e9
+    step_gbs = cells * 120 / (ms * 1e-3) / 1e9
+
+    # ---------------- e2e: per step, host state in -> step -> host state out (pinned buffers)
+    host_in = torch.empty((n, n, 5), dtype=torch.float64, pin_memory=True)
+    host_out = torch.empty((n, n, 5), dtype=torch.float64, pin_memory=True)
+    host_in.numpy()[...] = s0
+    ge = cg.Grid(cg.NEWTONIAN, (n, n), 1.0 / n, 1.4, cg.FP32, cg.BC_PERIODIC, ctx=ctx)
+    ge.set_prim(s0)
+    ge.run_begin(2, 0.9, 1e30, 0.0, cg.MINBEE)
+    nbytes = cells * 5 * 8
+    e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(2):
+        L.cosmos_grid_set_prim(ge.h, host_in.data_ptr(), cells * 5)
+        ge.run_steps(1)
+        L.cosmos_grid_get_prim(ge.h, host_out.data_ptr(), cells * 5)
+    barrier()
+    with torch.cuda.stream(stream):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(e2e_steps):
+            cg._lib.check(L.cosmos_grid_set_prim(ge.h, host_in.data_ptr(), cells * 5))
+            ge.run_steps(1)
+            cg._lib.check(L.cosmos_grid_get_prim(ge.h, host_out.data_ptr(), cells * 5))
+        b.record(stream)
+        b.synchronize()
+    e2e_ms = max_over_ranks(a.elapsed_time(b)) / e2e_steps
+    e2e_value = cells * world / (e2e_ms * 1e-3)
+    ge.close()
+
+    # ---------------- FP64 (reference-exact) on the same workload, and the FP32-vs-FP64 error
+    nerr = args.err_steps
+    g32 = cg.Grid(cg.NEWTONIAN, (n, n), 1.0 / n, 1.4, cg.FP32, cg.BC_PERIODIC, ctx=ctx)
+    g32.set_prim(s0)
+    g32.solve(2, 0.9, 1e30, 0.0, cg.MINBEE, max_steps=nerr)
+    rho32 = g32.get_prim()[..., 0].copy()
+    g32.close()
+    g64 = cg.Grid(cg.NEWTONIAN, (n, n), 1.0 / n, 1.4, cg.FP64, cg.BC_PERIODIC, ctx=ctx)
+    g64.set_prim(s0)
+    g64.run_begin(2, 0.9, 1e30, 0.0, cg.MINBEE, max_steps=nerr)
+    with torch.cuda.stream(stream):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        g64.run_steps(nerr)
+        b.record(stream)
+        b.synchronize()
+    ms64 = max_over_ranks(a.elapsed_time(b)) / nerr
+    g64.run_end()
+    rho64 = g64.get_prim()[..., 0]
+    g64.close()
+    l1 = float(np.abs(rho32 - rho64).mean() / np.abs(rho64).mean())
+
+    if rank != 0:
+        return
+    base = cpu_baseline(n, seconds=args.cpu_seconds) if not args.no_cpu else None
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": n, "cells_per_gpu": cells, "precision": "fp32 bulk",
+                   "l2": "state 335 MB > 129 MB L2 (no flush needed)", "parallelism": f"replicas x{world}",
+                   "device_dt": True, "graph_replay": True, "steps_completed": r.steps},
+        "fp64": {"value": cells * world / (ms64 * 1e-3), "ms_per_step": ms64, "steps": nerr,
+                 "path": "plain FP64, bit-identical to the reference"},
+        "l1_rho_fp32_vs_fp64": l1, "l1_steps": nerr,
+        "fp32_over_fp64": ms64 / ms,
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                "ms_per_step": e2e_ms, "steps": e2e_steps,
+                "what": "per step: pinned host AoS FP64 primitives -> device, one Strang step, state -> host"},
+        "roofline": {"bound": "hbm", "kernel": "sweep_x_kernel<NewtonFastPolicy,2,256> (X sweep, FP32)",
+                     "achieved": x_gbs, "peak": peak, "unit": "GB/s", "frac": x_gbs / peak,
+                     "peak_source": peak_kind, "traffic": traffic_per_launch("sweep_x_fp32"),
+                     "algorithmic_bytes_per_launch": bytes_sweep, "ms_per_launch": kx,
+                     "y_sweep": {"achieved": y_gbs, "frac": y_gbs / peak, "ms_per_launch": ky},
+                     "step": {"achieved": step_gbs, "frac": step_gbs / peak, "bytes_per_cell_update": 120}},
+        "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+        "status": r.status,
+    }
+    if base:
+        line["cpu_baseline"] = base
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=4096)
+    ap.add_argument("--err-steps", type=int, default=10)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -122,6 +122,7 @@ int enqueue_step(cosmos_grid* g, int cur, int* cur_out, unsigned* nk) {
         a.G.axis = axis;
         a.ds.scale = scale;
         a.ds.nsub = 0;
+        a.ds.fsel = scale == 0.5 ? 1 : 0;  // the controller forms FP32 coefficients for dt and dt/2
         a.src = g->buf[cur];
         a.dst = g->buf[cur ^ 1];
         a.out.ws_ctl = ws ? g->ctl : nullptr;
@@ -337,6 +338,7 @@ int cosmos_grid_sweep(cosmos_grid* g, int axis, int order, double dt, double bia
     a.bias = bias;
     a.lim = limiter;
     a.ds.fixed = dt;
+    a.ds.ffix = make_fast_coef(dt, g->p.dx);
     a.src = g->buf[g->cur];
     a.dst = g->buf[g->cur ^ 1];
     a.out.status = g->status;

@@ -20,16 +20,23 @@ template <class T> struct V5 { T v[5]; };
 // Ghost-cell index along a line of n cells.  Transmissive mirrors the reference's
 // insertBoundaryCells (Solvers/EulerSolvers.cpp:13-19, :52-73): g[-1]=c[0], g[-2]=c[1],
 // g[n]=c[n-1], g[n+1]=c[n-2].  Periodic wraps (an extension; the reference has no periodic BC).
+// k is at most two cells outside [0, n) and n >= 2, so no modulo is needed.
 CG_HD int ghost_index(int k, int n, int bc) {
-    if (bc == 1) { k %= n; return k < 0 ? k + n : k; }
-    if (k < 0) return -1 - k;
-    if (k >= n) return 2 * n - 1 - k;
+    if (k < 0) return bc == 1 ? k + n : -1 - k;
+    if (k >= n) return bc == 1 ? k - n : 2 * n - 1 - k;
     return k;
 }
 
 // std::min / std::max semantics as used by the reference.
 template <class T> CG_HD T mn(T a, T b) { return (b < a) ? b : a; }
 template <class T> CG_HD T mx(T a, T b) { return (a < b) ? b : a; }
+
+// FP32 sweep coefficients for one time step: dt/dx, dt/(2 dx), dx/(4 dt).
+struct FastCoef { float dtdx, half_dtdx, q_dxdt; };
+
+CG_HD FastCoef make_fast_coef(double dt, double dx) {
+    return FastCoef{(float)(dt / dx), (float)(0.5 * (dt / dx)), (float)(0.25 * (dx / dt))};
+}
 
 // Device-resident step controller.  The time step is computed on the device from the last
 // wavespeed reduction so that whole runs replay from a captured CUDA graph with no host sync.
@@ -45,6 +52,7 @@ struct StepCtl {
     int status;        // sticky error bits, see COSMOS_STATUS_* in the public header
     unsigned long long smax[2];  // wavespeed maxima (bit patterns of non-negative doubles), ping-pong by it parity
     unsigned long long newton_cap_hits;  // con2prim solves that reached the 1000-iteration cap
+    FastCoef fc[2];    // FP32 coefficients of dt (fc[0]) and dt/2 (fc[1]), formed by the dt kernel
 };
 
 // Status bits written by kernels (mirrored in include/cosmos_gb300.h)
@@ -61,26 +69,28 @@ CG_D void atomic_max_nonneg(unsigned long long* slot, double v) {
     atomicMax(slot, (unsigned long long)__double_as_longlong(v));
 }
 
-CG_D double warp_max(double v) {
+template <class W>
+CG_D W warp_max(W v) {
     for (int o = 16; o > 0; o >>= 1) {
-        double w = __shfl_xor_sync(0xffffffffu, v, o);
+        W w = __shfl_xor_sync(0xffffffffu, v, o);
         v = (w > v) ? w : v;
     }
     return v;
 }
 
-// Block-wide max reduction into *slot; every thread passes its value (0 if none).
-template <int NT>
-CG_D void block_max_to(unsigned long long* slot, double v) {
-    __shared__ double red[NT / 32];
+// Block-wide max reduction into *slot; every thread passes its value (0 if none).  W is the
+// policy's arithmetic type (float for the FP32 path, so no FP64 instruction runs per cell).
+template <int NT, class W>
+CG_D void block_max_to(unsigned long long* slot, W v) {
+    __shared__ W red[NT / 32];
     v = warp_max(v);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) red[wid] = v;
     __syncthreads();
     if (wid == 0) {
-        double w = lane < NT / 32 ? red[lane] : 0.0;
+        W w = lane < NT / 32 ? red[lane] : W(0);
         w = warp_max(w);
-        if (lane == 0) atomic_max_nonneg(slot, w);
+        if (lane == 0) atomic_max_nonneg(slot, (double)w);
     }
 }
 

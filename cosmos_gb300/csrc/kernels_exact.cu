@@ -35,8 +35,13 @@ cudaError_t run_sweep(const Pol& pol, const SweepArgs& a) {
     double* dst = (double*)a.dst;
     if (G.axis == 0) {
         dim3 grid((G.nx + kXThreads - 3) / (kXThreads - 2), G.ny);
-        if (a.order == 2) sweep_x_kernel<Pol, 2, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
-        else sweep_x_kernel<Pol, 1, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+        if constexpr (Pol::kShared) {
+            if (a.order == 2) sweep_x_own_kernel<Pol, 2, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+            else sweep_x_own_kernel<Pol, 1, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+        } else {
+            if (a.order == 2) sweep_x_kernel<Pol, 2, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+            else sweep_x_kernel<Pol, 1, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+        }
     } else {
         dim3 grid((G.nx + kYThreads - 1) / kYThreads, (G.ny + kYSeg - 1) / kYSeg);
         if (a.order == 2) sweep_y_kernel<Pol, 2, kYThreads, kYSeg><<<grid, kYThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
@@ -188,6 +193,8 @@ __global__ void dt_kernel(StepCtl* c) {
     if ((c->t + dt) > c->t_final) dt = c->t_final - c->t;
     if (!(dt > 0.0) || !isfinite(dt)) c->status |= ST_NONFINITE;
     c->dt = dt;
+    c->fc[0] = make_fast_coef(dt, c->dx);
+    c->fc[1] = make_fast_coef(dt * 0.5, c->dx);
     c->active = 1;
     c->smax[(c->it + 1) & 1] = 0ull;
     c->t = c->t + dt;

@@ -10,41 +10,56 @@ constexpr int kXThreads = 256;  // X sweep tile: 256 evolutions, 255 fluxes, 254
 constexpr int kYThreads = 128;
 constexpr int kYSeg = 32;
 
-NewtonFastPolicy make_fast(const SweepArgs& a) {
-    NewtonFastPolicy p;
+template <int AXIS, int LIM, bool MASKED>
+NewtonFastPolicy<AXIS, LIM, MASKED> make_fast(const SweepArgs& a) {
+    NewtonFastPolicy<AXIS, LIM, MASKED> p;
     const float g = (float)a.gamma, w = (float)a.bias;
     p.P.g1 = g - 1.0f;
+    p.P.hg1 = 0.5f * (g - 1.0f);
     p.P.gam = g;
     p.P.wa = 0.5f * (1.0f + w);
     p.P.wb = 0.5f * (1.0f - w);
-    p.P.om = 1.0f - w;
-    p.P.op = 1.0f + w;
-    p.P.lim = a.lim;
-    p.lm.axis = a.G.axis;
+    p.P.hom = 0.5f * (1.0f - w);
+    p.P.hop = 0.5f * (1.0f + w);
+    p.lm.axis = AXIS;
     p.lm.nx = a.G.nx;
     p.dims = a.G.dims;
-    p.dx = a.dx;
-    p.dtdx = p.half_dtdx = p.dxdt = 0.0f;
+    p.dtdx = p.half_dtdx = p.q_dxdt = 0.0f;
     return p;
+}
+
+template <int AXIS, int LIM, bool MASKED>
+void run_fast(const SweepArgs& a) {
+    const Geom& G = a.G;
+    const float* src = (const float*)a.src;
+    float* dst = (float*)a.dst;
+    auto pol = make_fast<AXIS, LIM, MASKED>(a);
+    using Pol = decltype(pol);
+    if constexpr (AXIS == 0) {
+        dim3 grid((G.nx + kXThreads - 3) / (kXThreads - 2), G.ny);
+        if (a.order == 2) sweep_x_own_kernel<Pol, 2, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+        else sweep_x_own_kernel<Pol, 1, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+    } else {
+        dim3 grid((G.nx + kYThreads - 1) / kYThreads, (G.ny + kYSeg - 1) / kYSeg);
+        if (a.order == 2) sweep_y_kernel<Pol, 2, kYThreads, kYSeg><<<grid, kYThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+        else sweep_y_kernel<Pol, 1, kYThreads, kYSeg><<<grid, kYThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+    }
+}
+
+template <int AXIS, bool MASKED>
+void run_fast_lim(const SweepArgs& a) {
+    if (a.lim == 0) run_fast<AXIS, 0, MASKED>(a);
+    else if (a.lim == 1) run_fast<AXIS, 1, MASKED>(a);
+    else run_fast<AXIS, 2, MASKED>(a);  // Solvers/SlopeLimiters.cpp:66: any other id is MinBee
 }
 
 }  // namespace
 
 cudaError_t launch_sweep_fast(const SweepArgs& a) {
     if (a.system != 0) return cudaErrorNotSupported;
-    const Geom& G = a.G;
-    const float* src = (const float*)a.src;
-    float* dst = (float*)a.dst;
-    NewtonFastPolicy pol = make_fast(a);
-    if (G.axis == 0) {
-        dim3 grid((G.nx + kXThreads - 3) / (kXThreads - 2), G.ny);
-        if (a.order == 2) sweep_x_kernel<NewtonFastPolicy, 2, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
-        else sweep_x_kernel<NewtonFastPolicy, 1, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
-    } else {
-        dim3 grid((G.nx + kYThreads - 1) / kYThreads, (G.ny + kYSeg - 1) / kYSeg);
-        if (a.order == 2) sweep_y_kernel<NewtonFastPolicy, 2, kYThreads, kYSeg><<<grid, kYThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
-        else sweep_y_kernel<NewtonFastPolicy, 1, kYThreads, kYSeg><<<grid, kYThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
-    }
+    const bool masked = a.out.mask != nullptr;
+    if (a.G.axis == 0) masked ? run_fast_lim<0, true>(a) : run_fast_lim<0, false>(a);
+    else masked ? run_fast_lim<1, true>(a) : run_fast_lim<1, false>(a);
     count_launch();
     return cudaGetLastError();
 }
@@ -59,7 +74,8 @@ cudaError_t launch_wavespeed_fast(const SweepArgs& a, unsigned long long* slot) 
     const size_t n = (size_t)a.G.nx * a.G.ny;
     int blocks = (int)((n + NT - 1) / NT);
     if (blocks > 152 * 16) blocks = 152 * 16;
-    wavespeed_kernel<NewtonFastPolicy, NT><<<blocks, NT, 0, a.stream>>>(make_fast(b), b.G, (const float*)a.src, o);
+    auto pol = make_fast<0, 2, false>(b);
+    wavespeed_kernel<decltype(pol), NT><<<blocks, NT, 0, a.stream>>>(pol, b.G, (const float*)a.src, o);
     count_launch();
     return cudaGetLastError();
 }

@@ -31,9 +31,12 @@ template <class Sys>
 struct ExactPolicy {
     using S = double;
     using X = double;
+    using W = double;  // wavespeed reduction type
     using Cell = V5<double>;
     using Face = V5<double>;
+    struct Coef { double dt; };
     static constexpr bool kShared = !Sys::kCoords;
+    static constexpr bool kMasked = true;
     Sys sys;
     LineMap lm;
     int dims, order, ny;
@@ -41,7 +44,8 @@ struct ExactPolicy {
     int lim;
     int capped;
 
-    CG_D void set_dt(double d) { dt = d; capped = 0; sys.capped = &capped; }
+    CG_D Coef make_coef(const DtSrc&, double d) const { return Coef{d}; }
+    CG_D void use_coef(const Coef& c) { dt = c.dt; capped = 0; sys.capped = &capped; }
     CG_D Pt cell_pt(int line, int k) const {
         int i, j;
         lm.ij(line, k, i, j);
@@ -139,40 +143,49 @@ CG_D double ExactPolicy<GRExact>::wavespeed(const Cell& c, int line, int k) cons
 }
 
 // ------------------------------------------------------------------ Newtonian FP32 bulk
-// Conserved FP32 storage; see physics_fast.cuh for the reformulations.
+// Conserved FP32 storage; see physics_fast.cuh for the reformulations.  AXIS and LIM are fixed at
+// compile time; MASKED selects whether the AMR update mask is consulted at all.
+template <int AXIS, int LIM, bool MASKED>
 struct NewtonFastPolicy {
     using S = float;
     using X = float;
+    using W = float;
     using Cell = V5<float>;
     using Face = V5<float>;
+    using Coef = FastCoef;
     static constexpr bool kShared = true;
+    static constexpr bool kMasked = MASKED;
     NewtonFastParams P;
     LineMap lm;
     int dims;
-    double dx;
-    float dtdx, half_dtdx, dxdt;
+    float dtdx, half_dtdx, q_dxdt;
 
-    CG_D void set_dt(double dt) {
-        dtdx = (float)(dt / dx);
-        half_dtdx = (float)(0.5 * (dt / dx));
-        dxdt = (float)(dx / dt);
+    // FP32 coefficients come precomputed (device step controller or host), so no FP64
+    // instruction runs in the FP32 sweeps
+    CG_D Coef make_coef(const DtSrc& ds, double) const { return ds.fast_coef(); }
+    CG_D void use_coef(const Coef& c) {
+        dtdx = c.dtdx;
+        half_dtdx = c.half_dtdx;
+        q_dxdt = c.q_dxdt;
     }
     CG_D void recon(const Cell& l, const Cell& m, const Cell& r, int, int, Face& L, Face& R) const {
-        nf_recon(P, l.v, m.v, r.v, lm.axis, half_dtdx, L.v, R.v);
+        nf_recon<AXIS, LIM>(P, l.v, m.v, r.v, half_dtdx, L.v, R.v);
     }
     CG_D void recon_side(const Cell&, const Cell&, const Cell&, int, int, int, Face&) const {}
     CG_D void face_of(const Cell& c, Face& f) const { f = c; }
     CG_D void flux(const Face& L, const Face& R, int, int, V5<float>& F) const {
-        nf_force(P, L.v, R.v, lm.axis, dtdx, dxdt, F.v);
+        nf_force<AXIS>(P, L.v, R.v, half_dtdx, q_dxdt, F.v);
     }
     CG_D Cell update(const Cell& c, const V5<float>& FL, const V5<float>& FR, int, int) const {
         Cell o;
 #pragma unroll
-        for (int f = 0; f < 5; f++) o.v[f] = c.v[f] + dtdx * (FL.v[f] - FR.v[f]);
+        for (int f = 0; f < 5; f++) o.v[f] = fmaf(dtdx, FL.v[f] - FR.v[f], c.v[f]);
         return o;
     }
-    CG_D bool active(int line, int k, const unsigned char* mask) const { return lm.mask_on(mask, line, k); }
-    CG_D double wavespeed(const Cell& c, int, int) const { return (double)nf_wavespeed(P, c.v, dims); }
+    CG_D bool active(int line, int k, const unsigned char* mask) const {
+        return MASKED ? lm.mask_on(mask, line, k) : true;
+    }
+    CG_D float wavespeed(const Cell& c, int, int) const { return nf_wavespeed(P, c.v, dims); }
     CG_D void flush_status(int*) const {}
 };
 

@@ -23,13 +23,16 @@ struct DtSrc {
     const StepCtl* ctl;
     double fixed;
     double scale;
-    int nsub;  // > 0 selects 0.5 * (dt / nsub)
+    int nsub;        // > 0 selects 0.5 * (dt / nsub)
+    int fsel;        // FP32 coefficients: controller slot (0: dt, 1: dt/2)
+    FastCoef ffix;   // FP32 coefficients of `fixed`, formed on the host
     CG_D bool get(double& dt) const {
         if (!ctl) { dt = fixed; return true; }
         if (!ctl->active) return false;
         dt = nsub > 0 ? 0.5 * (ctl->dt / nsub) : ctl->dt * scale;
         return true;
     }
+    CG_D FastCoef fast_coef() const { return ctl ? ctl->fc[fsel] : ffix; }
 };
 
 // Output side of a sweep: fused wavespeed maximum (for the next step's dt) and status bits.
@@ -71,8 +74,16 @@ __global__ void __launch_bounds__(NT) sweep_x_kernel(Pol pol, Geom G, const type
     const int s0 = blockIdx.x * TS;
     const int n = G.nx;
     const int send = min(s0 + TS, n);  // one past the last updated cell
-    double dt;
-    const bool act = ds.get(dt);
+    // the step's coefficients are formed once per block (FP64 work is 1/64 rate on GB300)
+    __shared__ typename Pol::Coef s_coef;
+    __shared__ int s_act;
+    if (t == 0) {
+        double dt;
+        s_act = ds.get(dt);
+        if (s_act) s_coef = pol.make_coef(ds, dt);
+    }
+    __syncthreads();
+    const bool act = s_act != 0;
     if (!act) {  // inactive step: keep the ping-pong buffers consistent
         if (s0 + t < send) {
             typename Pol::Cell c;
@@ -81,7 +92,7 @@ __global__ void __launch_bounds__(NT) sweep_x_kernel(Pol pol, Geom G, const type
         }
         return;
     }
-    pol.set_dt(dt);
+    pol.use_coef(s_coef);
     // stage cells s0-2+t (and two more) with ghost mapping along x
     for (int q = t; q < NT + 2; q += NT) {
         const int k = s0 - 2 + q;
@@ -141,7 +152,7 @@ __global__ void __launch_bounds__(NT) sweep_x_kernel(Pol pol, Geom G, const type
         }
     }
     __syncthreads();
-    double w = 0.0;
+    typename Pol::W w = 0;
     unsigned long long* const wslot = out.slot();
     const int k = s0 + t;
     if (t < TS && k < send) {
@@ -162,6 +173,110 @@ __global__ void __launch_bounds__(NT) sweep_x_kernel(Pol pol, Geom G, const type
     pol.flush_status(out.status);
 }
 
+// ------------------------------------------------------------------ X sweep, cell ownership
+// For policies whose half-step evolution gives both faces of a cell (coordinate-free systems).
+// Thread t owns cell c = s0 - 1 + t for the whole sweep: it evolves c (both faces stay in
+// registers), computes the flux at c's right interface, and updates c with that flux and its
+// left neighbour's.  Shared memory carries only what crosses threads: the cells (stencil
+// neighbours), the left faces and the fluxes.  NT threads update NT - 2 cells.
+template <class Pol, int ORDER, int NT>
+__global__ void __launch_bounds__(NT) sweep_x_own_kernel(Pol pol, Geom G, const typename Pol::S* __restrict__ src,
+                                                         typename Pol::S* __restrict__ dst, DtSrc ds, SweepOut out) {
+    using X = typename Pol::X;
+    using Cell = typename Pol::Cell;
+    using Face = typename Pol::Face;
+    constexpr int TS = NT - 2;
+    __shared__ X sc[5][NT + 2];  // cells s0-2 .. s0+NT-1 (own cell of thread t at t+1)
+    __shared__ X sl[5][NT];      // left face of the cell owned by thread t
+    __shared__ X sf[5][NT];      // flux at the right interface of the cell owned by thread t
+    __shared__ typename Pol::Coef s_coef;
+    __shared__ int s_act;
+    const int t = threadIdx.x;
+    const int row = blockIdx.y;
+    const int s0 = blockIdx.x * TS;
+    const int n = G.nx;
+    const int send = min(s0 + TS, n);
+    const int c = s0 - 1 + t;  // owned cell (may be a ghost position)
+    if (t == 0) {
+        double dt;
+        s_act = ds.get(dt);
+        if (s_act) s_coef = pol.make_coef(ds, dt);
+    }
+    // own cell and, for the two edge threads, the extra stencil cell
+    const bool live = c <= send;  // cells beyond send neither update nor feed an interface
+    Cell own;
+    if (live) {
+        load_cell(pol, src, G, row, ghost_index(c, n, G.bc), own);
+#pragma unroll
+        for (int f = 0; f < 5; f++) sc[f][t + 1] = own.v[f];
+    }
+    if (t == 0) {
+        Cell e;
+        load_cell(pol, src, G, row, ghost_index(s0 - 2, n, G.bc), e);
+#pragma unroll
+        for (int f = 0; f < 5; f++) sc[f][0] = e.v[f];
+    }
+    if ((t == NT - 1 && live) || c == send) {  // c + 1 <= send + 1 <= n + 1: a valid ghost
+        Cell e;
+        load_cell(pol, src, G, row, ghost_index(c + 1, n, G.bc), e);
+#pragma unroll
+        for (int f = 0; f < 5; f++) sc[f][t + 2] = e.v[f];
+    }
+    __syncthreads();
+    if (!s_act) {  // inactive step: keep the ping-pong buffers consistent
+        if (t >= 1 && c < send) store_cell<Pol>(own, dst, G, row, c);
+        return;
+    }
+    pol.use_coef(s_coef);
+    Face L, R;
+    if (live) {
+        if (ORDER == 2) {
+            Cell a, b;
+#pragma unroll
+            for (int f = 0; f < 5; f++) { a.v[f] = sc[f][t]; b.v[f] = sc[f][t + 2]; }
+            pol.recon(a, own, b, row, c, L, R);
+        } else {
+            pol.face_of(own, L);
+            pol.face_of(own, R);
+        }
+#pragma unroll
+        for (int f = 0; f < 5; f++) sl[f][t] = L.v[f];
+    }
+    __syncthreads();
+    V5<X> Fr;
+    if (live && c < send && t < NT - 1) {  // right interface of c, between c and c + 1
+        Face Rn;
+        if (ORDER == 2) {
+#pragma unroll
+            for (int f = 0; f < 5; f++) Rn.v[f] = sl[f][t + 1];
+        } else {
+            Cell b;
+#pragma unroll
+            for (int f = 0; f < 5; f++) b.v[f] = sc[f][t + 2];
+            pol.face_of(b, Rn);
+        }
+        pol.flux(R, Rn, row, c + 1, Fr);
+#pragma unroll
+        for (int f = 0; f < 5; f++) sf[f][t] = Fr.v[f];
+    }
+    __syncthreads();
+    typename Pol::W w = 0;
+    unsigned long long* const wslot = out.slot();
+    if (t >= 1 && c < send) {
+        Cell nc = own;
+        if (pol.active(row, c, out.mask)) {
+            V5<X> Fl;
+#pragma unroll
+            for (int f = 0; f < 5; f++) Fl.v[f] = sf[f][t - 1];
+            nc = pol.update(own, Fl, Fr, row, c);
+        }
+        store_cell<Pol>(nc, dst, G, row, c);
+        if (wslot) w = pol.wavespeed(nc, row, c);
+    }
+    if (wslot) block_max_to<NT>(wslot, w);
+    pol.flush_status(out.status);
+}
+
 // ------------------------------------------------------------------ Y sweep: column march
 // One thread per column marches SEG rows keeping the stencil in registers.
 template <class Pol, int ORDER, int NT, int SEG>
@@ -175,9 +290,15 @@ __global__ void __launch_bounds__(NT) sweep_y_kernel(Pol pol, Geom G, const type
     const int n = G.ny;
     const int y1 = min(y0 + SEG, n);
     const bool col_ok = j < G.nx;
-    double dt;
-    const bool act = ds.get(dt);
-    if (!act) {
+    __shared__ typename Pol::Coef s_coef;
+    __shared__ int s_act;
+    if (threadIdx.x == 0) {
+        double dt;
+        s_act = ds.get(dt);
+        if (s_act) s_coef = pol.make_coef(ds, dt);
+    }
+    __syncthreads();
+    if (!s_act) {
         if (col_ok)
             for (int y = y0; y < y1; y++) {
                 Cell c;
@@ -186,12 +307,13 @@ __global__ void __launch_bounds__(NT) sweep_y_kernel(Pol pol, Geom G, const type
             }
         return;
     }
-    pol.set_dt(dt);
-    double w = 0.0;
+    pol.use_coef(s_coef);
+    typename Pol::W w = 0;
     unsigned long long* const wslot = out.slot();
     if (col_ok) {
         auto ld = [&](int y, Cell& c) { load_cell(pol, src, G, ghost_index(y, n, G.bc), j, c); };
         auto need = [&](int fi) {  // interface between fi-1 and fi
+            if (!Pol::kMasked) return true;  // unmasked: every interface in the segment is used
             const bool a = fi - 1 >= y0 && fi - 1 < y1 && pol.active(j, fi - 1, out.mask);
             const bool b = fi >= y0 && fi < y1 && pol.active(j, fi, out.mask);
             return a || b;
@@ -241,7 +363,7 @@ __global__ void __launch_bounds__(NT) sweep_y_kernel(Pol pol, Geom G, const type
             Cell nc = c0;
             if (pol.active(j, y, out.mask)) nc = pol.update(c0, Fp, Fn, j, y);
             store_cell<Pol>(nc, dst, G, y, j);
-            if (wslot) { double ws = pol.wavespeed(nc, j, y); w = (ws > w) ? ws : w; }
+            if (wslot) { const typename Pol::W ws = pol.wavespeed(nc, j, y); w = (ws > w) ? ws : w; }
             Fp = Fn;
             cm1 = c0; c0 = c1; c1 = c2;
         }
@@ -254,14 +376,14 @@ __global__ void __launch_bounds__(NT) sweep_y_kernel(Pol pol, Geom G, const type
 template <class Pol, int NT>
 __global__ void __launch_bounds__(NT) wavespeed_kernel(Pol pol, Geom G, const typename Pol::S* __restrict__ src,
                                                        SweepOut out) {
-    double w = 0.0;
+    typename Pol::W w = 0;
     const size_t ncell = (size_t)G.nx * G.ny;
     for (size_t c = (size_t)blockIdx.x * NT + threadIdx.x; c < ncell; c += (size_t)gridDim.x * NT) {
         const int i = (int)(c / G.nx), j = (int)(c % G.nx);
         typename Pol::Cell cc;
         load_cell(pol, src, G, i, j, cc);
         // wavespeed takes (line, k) in the X-sweep convention: line = row i, k = column j
-        const double ws = pol.wavespeed(cc, i, j);
+        const typename Pol::W ws = pol.wavespeed(cc, i, j);
         w = (ws > w) ? ws : w;
     }
     block_max_to<NT>(out.slot(), w);

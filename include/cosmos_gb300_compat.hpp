@@ -1,0 +1,400 @@
+// C++ drop-in shim: the reference's class and method names over the cosmos_gb300 C ABI.
+//
+// Code written against the reference (JonathanGorard/Cosmos) -- e.g. its Tests/*.cpp drivers --
+// compiles against this header instead of the reference's Euler/, RelativisticEuler/,
+// BlackHoleEuler/ and Solvers/ headers.  Grid-level methods (solve, solve2D, the per-sweep
+// compute*TimeStep*, computeMaximumWaveSpeed*, computeStableTimeStep*, the forcing step) run on
+// the GPU through the C ABI with the reference's arguments; the state classes keep the
+// reference's primitive storage (density, x/y/z velocity, pressure) and accessors.
+//
+// Differences a caller can see: every grid call returns the same values as the reference (FP64
+// path, bit-identical); failures throw std::runtime_error with cosmos_last_error()'s text (the
+// reference has no error reporting); no per-step status line is printed.
+#pragma once
+
+#include <cmath>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "cosmos_gb300.h"
+
+namespace cosmos_compat_detail {
+
+inline void check(int rc) {
+    if (rc != COSMOS_OK) throw std::runtime_error(std::string("cosmos_gb300: ") + cosmos_last_error());
+}
+
+struct Ctx {
+    cosmos_ctx* c = nullptr;
+    Ctx() { check(cosmos_ctx_create(0, &c)); }
+    ~Ctx() { cosmos_ctx_destroy(c); }
+};
+inline cosmos_ctx* ctx() {
+    static thread_local Ctx c;
+    return c.c;
+}
+
+// A device grid for the duration of one call.
+struct Grid {
+    cosmos_grid* g = nullptr;
+    Grid(int system, int dims, int nx, int ny, double dx, double gamma, const double* bh) {
+        cosmos_params p;
+        cosmos_params_default(&p);
+        p.system = system;
+        p.dims = dims;
+        p.nx = nx;
+        p.ny = dims == 1 ? 1 : ny;
+        p.dx = dx;
+        p.gamma = gamma;
+        if (bh) { p.bh_mass = bh[0]; p.bh_spin = bh[1]; p.bh_x = bh[2]; p.bh_y = bh[3]; p.bh_z = bh[4]; }
+        check(cosmos_grid_create(ctx(), &p, &g));
+    }
+    ~Grid() { cosmos_grid_destroy(g); }
+};
+
+template <class S> std::vector<double> pack1(const std::vector<S>& c) {
+    std::vector<double> a(c.size() * 5);
+    for (size_t i = 0; i < c.size(); i++) {
+        S s = c[i];
+        a[5 * i] = s.getDensity(); a[5 * i + 1] = s.getXVelocity(); a[5 * i + 2] = s.getYVelocity();
+        a[5 * i + 3] = s.getZVelocity(); a[5 * i + 4] = s.getPressure();
+    }
+    return a;
+}
+template <class S> void unpack1(const std::vector<double>& a, std::vector<S>& c) {
+    for (size_t i = 0; i < c.size(); i++) c[i] = S(a[5 * i], a[5 * i + 1], a[5 * i + 2], a[5 * i + 3], a[5 * i + 4]);
+}
+template <class S> std::vector<double> pack2(const std::vector<std::vector<S> >& g) {
+    std::vector<double> a;
+    a.reserve(g.size() * g[0].size() * 5);
+    for (const auto& row : g) {
+        std::vector<double> r = pack1(row);
+        a.insert(a.end(), r.begin(), r.end());
+    }
+    return a;
+}
+template <class S> void unpack2(const std::vector<double>& a, std::vector<std::vector<S> >& g) {
+    size_t k = 0;
+    for (auto& row : g)
+        for (auto& s : row) { s = S(a[k], a[k + 1], a[k + 2], a[k + 3], a[k + 4]); k += 5; }
+}
+
+}  // namespace cosmos_compat_detail
+
+// ----------------------------------------------------------------------------- material, spacetime
+class EulerMaterialParameters {  // Euler/EulerMaterialParameters.hpp
+public:
+    EulerMaterialParameters() : adiabaticIndex(1.0) {}
+    EulerMaterialParameters(double g) : adiabaticIndex(g) {}
+    void setAdiabaticIndex(double g) { adiabaticIndex = g; }
+    double getAdiabaticIndex() { return adiabaticIndex; }
+private:
+    double adiabaticIndex;
+};
+
+class BlackHoleSpacetime {  // BlackHoleEuler/BlackHoleSpacetime.hpp (parameters; the metric lives on the GPU)
+public:
+    BlackHoleSpacetime() : m(1.0), a(0.0), x(0.5), y(0.5), z(0.0) {}
+    BlackHoleSpacetime(double M) : m(M), a(0.0), x(0.5), y(0.5), z(0.0) {}
+    BlackHoleSpacetime(double M, double X, double Y, double Z) : m(M), a(0.0), x(X), y(Y), z(Z) {}
+    BlackHoleSpacetime(double M, double A) : m(M), a(A), x(0.5), y(0.5), z(0.0) {}
+    BlackHoleSpacetime(double M, double A, double X, double Y, double Z) : m(M), a(A), x(X), y(Y), z(Z) {}
+    void setBlackHoleMass(double v) { m = v; }
+    void setBlackHoleSpin(double v) { a = v; }
+    void setBlackHoleXPosition(double v) { x = v; }
+    void setBlackHoleYPosition(double v) { y = v; }
+    void setBlackHoleZPosition(double v) { z = v; }
+    double getBlackHoleMass() { return m; }
+    double getBlackHoleSpin() { return a; }
+    double getBlackHoleXPosition() { return x; }
+    double getBlackHoleYPosition() { return y; }
+    double getBlackHoleZPosition() { return z; }
+    void pack(double* o) const { o[0] = m; o[1] = a; o[2] = x; o[3] = y; o[4] = z; }
+private:
+    double m, a, x, y, z;
+};
+
+// ----------------------------------------------------------------------------- state vectors
+// Primitive storage and accessors as in Euler/EulerStateVector.hpp:8-48 (and the SR/GR twins).
+#define COSMOS_COMPAT_STATE(NAME)                                                                          \
+    class NAME {                                                                                           \
+    public:                                                                                                \
+        NAME() : density(1.0), xVelocity(0.0), yVelocity(0.0), zVelocity(0.0), pressure(1.0) {}          \
+        NAME(double r, double vx, double vy, double vz, double p)                                          \
+            : density(r), xVelocity(vx), yVelocity(vy), zVelocity(vz), pressure(p) {}                      \
+        void setPrimitiveVariableVector(std::vector<double> v) {                                           \
+            density = v[0]; xVelocity = v[1]; yVelocity = v[2]; zVelocity = v[3]; pressure = v[4];         \
+        }                                                                                                  \
+        std::vector<double> computePrimitiveVariableVector() {                                             \
+            return std::vector<double>{density, xVelocity, yVelocity, zVelocity, pressure};                \
+        }                                                                                                  \
+        void setDensity(double v) { density = v; }                                                         \
+        void setXVelocity(double v) { xVelocity = v; }                                                     \
+        void setYVelocity(double v) { yVelocity = v; }                                                     \
+        void setZVelocity(double v) { zVelocity = v; }                                                     \
+        void setPressure(double v) { pressure = v; }                                                       \
+        double getDensity() { return density; }                                                            \
+        double getXVelocity() { return xVelocity; }                                                        \
+        double getYVelocity() { return yVelocity; }                                                        \
+        double getZVelocity() { return zVelocity; }                                                        \
+        double getPressure() { return pressure; }                                                          \
+    private:                                                                                               \
+        double density, xVelocity, yVelocity, zVelocity, pressure;                                         \
+    };
+COSMOS_COMPAT_STATE(EulerStateVector)
+COSMOS_COMPAT_STATE(RelativisticEulerStateVector)
+COSMOS_COMPAT_STATE(BlackHoleEulerStateVector)
+#undef COSMOS_COMPAT_STATE
+
+// ----------------------------------------------------------------------------- solvers
+namespace cosmos_compat_detail {
+
+template <class S>
+std::vector<S> solve1(int sys, std::vector<S> cells, double dx, double cfl, double T, int order, double bias, int lim,
+                      EulerMaterialParameters mp, int sub = 1, const BlackHoleSpacetime* bh = nullptr) {
+    double b[5];
+    if (bh) bh->pack(b);
+    Grid g(sys, 1, (int)cells.size(), 1, dx, mp.getAdiabaticIndex(), bh ? b : nullptr);
+    std::vector<double> a = pack1(cells);
+    check(cosmos_grid_set_prim(g.g, a.data(), a.size()));
+    cosmos_solve_opts o;
+    cosmos_solve_opts_default(&o);
+    o.order = order; o.cfl = cfl; o.t_final = T; o.bias = bias; o.limiter = lim; o.subcycles = sub;
+    cosmos_solve_result r;
+    check(cosmos_grid_solve(g.g, &o, &r));
+    check(cosmos_grid_get_prim(g.g, a.data(), a.size()));
+    unpack1(a, cells);
+    return cells;
+}
+template <class S>
+std::vector<std::vector<S> > solve2(int sys, std::vector<std::vector<S> > cells, double dx, double cfl, double T,
+                                    int order, double bias, int lim, EulerMaterialParameters mp, int sub = 1,
+                                    const BlackHoleSpacetime* bh = nullptr) {
+    double b[5];
+    if (bh) bh->pack(b);
+    Grid g(sys, 2, (int)cells[0].size(), (int)cells.size(), dx, mp.getAdiabaticIndex(), bh ? b : nullptr);
+    std::vector<double> a = pack2(cells);
+    check(cosmos_grid_set_prim(g.g, a.data(), a.size()));
+    cosmos_solve_opts o;
+    cosmos_solve_opts_default(&o);
+    o.order = order; o.cfl = cfl; o.t_final = T; o.bias = bias; o.limiter = lim; o.subcycles = sub;
+    cosmos_solve_result r;
+    check(cosmos_grid_solve(g.g, &o, &r));
+    check(cosmos_grid_get_prim(g.g, a.data(), a.size()));
+    unpack2(a, cells);
+    return cells;
+}
+template <class S>
+void sweep1(int sys, std::vector<S>& cells, double dx, double dt, int order, double bias, int lim,
+            EulerMaterialParameters mp, const BlackHoleSpacetime* bh = nullptr) {
+    double b[5];
+    if (bh) bh->pack(b);
+    Grid g(sys, 1, (int)cells.size(), 1, dx, mp.getAdiabaticIndex(), bh ? b : nullptr);
+    std::vector<double> a = pack1(cells);
+    check(cosmos_grid_set_prim(g.g, a.data(), a.size()));
+    check(cosmos_grid_sweep(g.g, 0, order, dt, bias, lim));
+    check(cosmos_grid_get_prim(g.g, a.data(), a.size()));
+    unpack1(a, cells);
+}
+template <class S>
+void sweep2(int sys, std::vector<std::vector<S> >& cells, double dx, double dt, int axis, int order, double bias,
+            int lim, EulerMaterialParameters mp, const BlackHoleSpacetime* bh = nullptr) {
+    double b[5];
+    if (bh) bh->pack(b);
+    Grid g(sys, 2, (int)cells[0].size(), (int)cells.size(), dx, mp.getAdiabaticIndex(), bh ? b : nullptr);
+    std::vector<double> a = pack2(cells);
+    check(cosmos_grid_set_prim(g.g, a.data(), a.size()));
+    check(cosmos_grid_sweep(g.g, axis, order, dt, bias, lim));
+    check(cosmos_grid_get_prim(g.g, a.data(), a.size()));
+    unpack2(a, cells);
+}
+template <class S, class Cells>
+double max_speed(int sys, Cells& cells, int dims, EulerMaterialParameters mp, const BlackHoleSpacetime* bh = nullptr);
+template <class S>
+double max_speed1(int sys, std::vector<S>& c, EulerMaterialParameters mp, const BlackHoleSpacetime* bh = nullptr) {
+    double b[5];
+    if (bh) bh->pack(b);
+    Grid g(sys, 1, (int)c.size(), 1, 1.0, mp.getAdiabaticIndex(), bh ? b : nullptr);
+    std::vector<double> a = pack1(c);
+    check(cosmos_grid_set_prim(g.g, a.data(), a.size()));
+    double s;
+    check(cosmos_grid_max_wavespeed(g.g, &s));
+    return s;
+}
+template <class S>
+double max_speed2(int sys, std::vector<std::vector<S> >& c, EulerMaterialParameters mp,
+                  const BlackHoleSpacetime* bh = nullptr) {
+    double b[5];
+    if (bh) bh->pack(b);
+    Grid g(sys, 2, (int)c[0].size(), (int)c.size(), 1.0, mp.getAdiabaticIndex(), bh ? b : nullptr);
+    std::vector<double> a = pack2(c);
+    check(cosmos_grid_set_prim(g.g, a.data(), a.size()));
+    double s;
+    check(cosmos_grid_max_wavespeed(g.g, &s));
+    return s;
+}
+
+}  // namespace cosmos_compat_detail
+
+#define COSMOS_COMPAT_SOLVERS(PREFIX, STATE, SYS)                                                               \
+    class PREFIX##Solvers {                                                                                    \
+    public:                                                                                                    \
+        static double computeMaximumWaveSpeed(std::vector<STATE>& c, EulerMaterialParameters mp) {             \
+            return cosmos_compat_detail::max_speed1(SYS, c, mp);                                               \
+        }                                                                                                      \
+        static double computeMaximumWaveSpeed2D(std::vector<std::vector<STATE> >& c, EulerMaterialParameters mp) { \
+            return cosmos_compat_detail::max_speed2(SYS, c, mp);                                               \
+        }                                                                                                      \
+        static double computeStableTimeStep(double dt, double t, double T, int it) {                          \
+            return cosmos_stable_dt_rule(dt, t, T, it);                                                        \
+        }                                                                                                      \
+        static double computeStableTimeStep(std::vector<STATE> c, double dx, double cfl, double t, double T,   \
+                                            int it, EulerMaterialParameters mp) {                              \
+            return cosmos_stable_dt_rule(cfl * (dx / computeMaximumWaveSpeed(c, mp)), t, T, it);              \
+        }                                                                                                      \
+        static double computeStableTimeStep2D(std::vector<std::vector<STATE> > c, double dx, double cfl,       \
+                                              double t, double T, int it, EulerMaterialParameters mp) {        \
+            return cosmos_stable_dt_rule(cfl * (dx / computeMaximumWaveSpeed2D(c, mp)), t, T, it);            \
+        }                                                                                                      \
+    };                                                                                                         \
+    class PREFIX##FirstOrderSolver {                                                                           \
+    public:                                                                                                    \
+        static void computeFORCETimeStep(std::vector<STATE>& c, double dx, double dt, EulerMaterialParameters mp) { \
+            cosmos_compat_detail::sweep1(SYS, c, dx, dt, 1, 0.0, 1, mp);                                       \
+        }                                                                                                      \
+        static void computeXFORCETimeStep2D(std::vector<std::vector<STATE> >& c, double dx, double dt,          \
+                                            EulerMaterialParameters mp) {                                      \
+            cosmos_compat_detail::sweep2(SYS, c, dx, dt, 0, 1, 0.0, 1, mp);                                    \
+        }                                                                                                      \
+        static void computeYFORCETimeStep2D(std::vector<std::vector<STATE> >& c, double dx, double dt,          \
+                                            EulerMaterialParameters mp) {                                      \
+            cosmos_compat_detail::sweep2(SYS, c, dx, dt, 1, 1, 0.0, 1, mp);                                    \
+        }                                                                                                      \
+        static std::vector<STATE> solve(std::vector<STATE> c, double dx, double cfl, double T,                  \
+                                        EulerMaterialParameters mp) {                                          \
+            return cosmos_compat_detail::solve1(SYS, c, dx, cfl, T, 1, 0.0, 1, mp);                            \
+        }                                                                                                      \
+        static std::vector<std::vector<STATE> > solve2D(std::vector<std::vector<STATE> > c, double dx,           \
+                                                        double cfl, double T, EulerMaterialParameters mp) {    \
+            return cosmos_compat_detail::solve2(SYS, c, dx, cfl, T, 1, 0.0, 1, mp);                            \
+        }                                                                                                      \
+    };                                                                                                         \
+    class PREFIX##SecondOrderSolver {                                                                          \
+    public:                                                                                                    \
+        static void computeSLICTimeStep(std::vector<STATE>& c, double dx, double dt, double bias, int lim,      \
+                                        EulerMaterialParameters mp) {                                          \
+            cosmos_compat_detail::sweep1(SYS, c, dx, dt, 2, bias, lim, mp);                                    \
+        }                                                                                                      \
+        static void computeXSLICTimeStep2D(std::vector<std::vector<STATE> >& c, double dx, double dt, double bias, \
+                                           int lim, EulerMaterialParameters mp) {                              \
+            cosmos_compat_detail::sweep2(SYS, c, dx, dt, 0, 2, bias, lim, mp);                                 \
+        }                                                                                                      \
+        static void computeYSLICTimeStep2D(std::vector<std::vector<STATE> >& c, double dx, double dt, double bias, \
+                                           int lim, EulerMaterialParameters mp) {                              \
+            cosmos_compat_detail::sweep2(SYS, c, dx, dt, 1, 2, bias, lim, mp);                                 \
+        }                                                                                                      \
+        static std::vector<STATE> solve(std::vector<STATE> c, double dx, double cfl, double T, double bias,    \
+                                        int lim, EulerMaterialParameters mp) {                                 \
+            return cosmos_compat_detail::solve1(SYS, c, dx, cfl, T, 2, bias, lim, mp);                         \
+        }                                                                                                      \
+        static std::vector<std::vector<STATE> > solve2D(std::vector<std::vector<STATE> > c, double dx,           \
+                                                        double cfl, double T, double bias, int lim,            \
+                                                        EulerMaterialParameters mp) {                          \
+            return cosmos_compat_detail::solve2(SYS, c, dx, cfl, T, 2, bias, lim, mp);                         \
+        }                                                                                                      \
+    };
+COSMOS_COMPAT_SOLVERS(Euler, EulerStateVector, COSMOS_NEWTONIAN)
+COSMOS_COMPAT_SOLVERS(RelativisticEuler, RelativisticEulerStateVector, COSMOS_SR)
+#undef COSMOS_COMPAT_SOLVERS
+
+// GR solvers take (..., subcyclingIterations, EulerMaterialParameters, BlackHoleSpacetime)
+// (Solvers/BlackHoleEulerSecondOrderSolver.hpp:10-32, Solvers/BlackHoleEulerForcingSolver.hpp:19-22).
+class BlackHoleEulerSolvers {
+public:
+    static double computeStableTimeStep(std::vector<BlackHoleEulerStateVector> c, double dx, double cfl, double t,
+                                        double T, int it, EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        return cosmos_stable_dt_rule(cfl * (dx / cosmos_compat_detail::max_speed1(COSMOS_GR, c, mp, &bh)), t, T, it);
+    }
+    static double computeStableTimeStep2D(std::vector<std::vector<BlackHoleEulerStateVector> > c, double dx,
+                                          double cfl, double t, double T, int it, EulerMaterialParameters mp,
+                                          BlackHoleSpacetime bh) {
+        return cosmos_stable_dt_rule(cfl * (dx / cosmos_compat_detail::max_speed2(COSMOS_GR, c, mp, &bh)), t, T, it);
+    }
+};
+class BlackHoleEulerFirstOrderSolver {
+public:
+    static void computeFORCETimeStep(std::vector<BlackHoleEulerStateVector>& c, double dx, double dt,
+                                     EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        cosmos_compat_detail::sweep1(COSMOS_GR, c, dx, dt, 1, 0.0, 1, mp, &bh);
+    }
+    static void computeXFORCETimeStep2D(std::vector<std::vector<BlackHoleEulerStateVector> >& c, double dx, double dt,
+                                        EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        cosmos_compat_detail::sweep2(COSMOS_GR, c, dx, dt, 0, 1, 0.0, 1, mp, &bh);
+    }
+    static void computeYFORCETimeStep2D(std::vector<std::vector<BlackHoleEulerStateVector> >& c, double dx, double dt,
+                                        EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        cosmos_compat_detail::sweep2(COSMOS_GR, c, dx, dt, 1, 1, 0.0, 1, mp, &bh);
+    }
+    static std::vector<BlackHoleEulerStateVector> solve(std::vector<BlackHoleEulerStateVector> c, double dx, double cfl,
+                                                        double T, int sub, EulerMaterialParameters mp,
+                                                        BlackHoleSpacetime bh) {
+        return cosmos_compat_detail::solve1(COSMOS_GR, c, dx, cfl, T, 1, 0.0, 1, mp, sub, &bh);
+    }
+    static std::vector<std::vector<BlackHoleEulerStateVector> > solve2D(
+        std::vector<std::vector<BlackHoleEulerStateVector> > c, double dx, double cfl, double T, int sub,
+        EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        return cosmos_compat_detail::solve2(COSMOS_GR, c, dx, cfl, T, 1, 0.0, 1, mp, sub, &bh);
+    }
+};
+class BlackHoleEulerSecondOrderSolver {
+public:
+    static void computeSLICTimeStep(std::vector<BlackHoleEulerStateVector>& c, double dx, double dt, double bias,
+                                    int lim, EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        cosmos_compat_detail::sweep1(COSMOS_GR, c, dx, dt, 2, bias, lim, mp, &bh);
+    }
+    static void computeXSLICTimeStep2D(std::vector<std::vector<BlackHoleEulerStateVector> >& c, double dx, double dt,
+                                       double bias, int lim, EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        cosmos_compat_detail::sweep2(COSMOS_GR, c, dx, dt, 0, 2, bias, lim, mp, &bh);
+    }
+    static void computeYSLICTimeStep2D(std::vector<std::vector<BlackHoleEulerStateVector> >& c, double dx, double dt,
+                                       double bias, int lim, EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        cosmos_compat_detail::sweep2(COSMOS_GR, c, dx, dt, 1, 2, bias, lim, mp, &bh);
+    }
+    static std::vector<BlackHoleEulerStateVector> solve(std::vector<BlackHoleEulerStateVector> c, double dx, double cfl,
+                                                        double T, double bias, int lim, int sub,
+                                                        EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        return cosmos_compat_detail::solve1(COSMOS_GR, c, dx, cfl, T, 2, bias, lim, mp, sub, &bh);
+    }
+    static std::vector<std::vector<BlackHoleEulerStateVector> > solve2D(
+        std::vector<std::vector<BlackHoleEulerStateVector> > c, double dx, double cfl, double T, double bias, int lim,
+        int sub, EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        return cosmos_compat_detail::solve2(COSMOS_GR, c, dx, cfl, T, 2, bias, lim, mp, sub, &bh);
+    }
+};
+class BlackHoleEulerForcingSolver {
+public:
+    static void computeRungeKuttaTimeStep(std::vector<BlackHoleEulerStateVector>& c, double dx, double dt, double bias,
+                                          int lim, EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        double b[5];
+        bh.pack(b);
+        cosmos_compat_detail::Grid g(COSMOS_GR, 1, (int)c.size(), 1, dx, mp.getAdiabaticIndex(), b);
+        std::vector<double> a = cosmos_compat_detail::pack1(c);
+        cosmos_compat_detail::check(cosmos_grid_set_prim(g.g, a.data(), a.size()));
+        cosmos_compat_detail::check(cosmos_grid_rk_source(g.g, dt, bias, lim));
+        cosmos_compat_detail::check(cosmos_grid_get_prim(g.g, a.data(), a.size()));
+        cosmos_compat_detail::unpack1(a, c);
+    }
+    static void computeRungeKuttaTimeStep2D(std::vector<std::vector<BlackHoleEulerStateVector> >& c, double dx,
+                                            double dt, double bias, int lim, EulerMaterialParameters mp,
+                                            BlackHoleSpacetime bh) {
+        double b[5];
+        bh.pack(b);
+        cosmos_compat_detail::Grid g(COSMOS_GR, 2, (int)c[0].size(), (int)c.size(), dx, mp.getAdiabaticIndex(), b);
+        std::vector<double> a = cosmos_compat_detail::pack2(c);
+        cosmos_compat_detail::check(cosmos_grid_set_prim(g.g, a.data(), a.size()));
+        cosmos_compat_detail::check(cosmos_grid_rk_source(g.g, dt, bias, lim));
+        cosmos_compat_detail::check(cosmos_grid_get_prim(g.g, a.data(), a.size()));
+        cosmos_compat_detail::unpack2(a, c);
+    }
+};

@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 namespace orc {
@@ -569,6 +570,22 @@ static inline int ghost(int k, int n, int bc) {
     return k;
 }
 
+// Thread count for the line-parallel sweeps (1 by default; set by orc_set_threads).
+static int g_threads = 1;
+
+template <class F>
+static void parallel_lines(int nlines, F&& body) {
+    int nt = g_threads < 1 ? 1 : g_threads;
+    if (nt > nlines) nt = nlines;
+    if (nt <= 1) { body(0, nlines); return; }
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; t++) {
+        int a = (int)((long long)nlines * t / nt), b = (int)((long long)nlines * (t + 1) / nt);
+        pool.emplace_back([&body, a, b]() { body(a, b); });
+    }
+    for (auto& th : pool) th.join();
+}
+
 // One dimensional sweep over the whole grid.  Solvers/EulerSecondOrderSolver.cpp:27-100 (SLIC),
 // Solvers/EulerFirstOrderSolver.cpp:103-155 (FORCE), GR twins with excision masks
 // Solvers/BlackHoleEulerSecondOrderSolver.cpp:39-179, Solvers/BlackHoleEulerFirstOrderSolver.cpp:89-165.
@@ -579,10 +596,13 @@ static void sweep(const Sys& S, T* prim, int ny, int nx, int dims, int axis, int
                   double w, int lim, int bc, const unsigned char* mask, const BH* exc) {
     if (dims == 1) { ny = 1; axis = 0; }
     const int nlines = axis == 0 ? ny : nx, n = axis == 0 ? nx : ny;
+    // Lines are independent (each stencil stays inside its line), so they are split across
+    // threads; the result does not depend on the thread count.
+    parallel_lines(nlines, [&](int L0, int L1) {
     std::vector<T> line((size_t)(n + 4) * 5), out((size_t)n * 5);
     std::vector<T> flux((size_t)(n + 1) * 5), faceL((size_t)(n + 2) * 5), faceR((size_t)(n + 2) * 5);
     std::vector<char> needf(n + 1), active(n);
-    for (int L = 0; L < nlines; L++) {
+    for (int L = L0; L < L1; L++) {
         auto idx = [&](int k) -> size_t { return axis == 0 ? ((size_t)L * nx + k) : ((size_t)k * nx + L); };
         auto cpt = [&](int k) -> Pt { return axis == 0 ? cell_pt(L, k, dx) : cell_pt(k, L, dx); };
         for (int k = -2; k < n + 2; k++) {
@@ -654,6 +674,7 @@ static void sweep(const Sys& S, T* prim, int ny, int nx, int dims, int axis, int
         }
         for (int k = 0; k < n; k++) std::memcpy(prim + 5 * idx(k), &out[5 * k], 5 * sizeof(T));
     }
+    });
 }
 
 // Solvers/EulerSolvers.cpp:130-145
@@ -796,6 +817,8 @@ using namespace orc;
 
 // ========================================================================= C ABI
 extern "C" {
+
+void orc_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
 
 // sys: 0 Newtonian, 1 SR, 2 GR.  bh = {M, a, x, y, z} (GR only).
 void orc_sweep(int sys, double* prim, int ny, int nx, int dims, int axis, int order, double dx, double dt,

@@ -72,6 +72,11 @@ class Oracle:
         L.orc_amr_derefine.argtypes = [_i, _p, _p, _i, _i, _i, _d, _d, _d, _p, _p, _p]
         L.orc_tlm_newton.argtypes = [_p, _p, _p, _i, _i, _i, _d, _p, _i, _d, _i, _d, _i, _p]
         L.orc_tlm_newton.restype = _d
+        L.orc_set_threads.argtypes = [_i]
+
+    def set_threads(self, n):
+        """Line-parallel sweeps on n host threads (results do not depend on n)."""
+        self.L.orc_set_threads(int(n))
 
     # ---- grid operations (in place on a float64 copy; returns the new array)
     def sweep(self, system, prim, axis, order, dx, dt, bias, lim, gamma, bc=0, mask=None, bh=None):

@@ -220,3 +220,23 @@ def test_errors_are_reported(cg):
         g.sweep(1, 2, 0.01, 0.0, 1)  # no y axis in 1D
     with pytest.raises(cg.CosmosError):
         g.run_steps(1)  # run_begin not called
+
+
+@pytest.mark.parametrize("shape,axis", [((5, 600), 0), ((600, 5), 1), ((700,), 0), ((3, 3), 0), ((3, 3), 1)])
+def test_fp32_single_sweeps_vs_oracle(cg, oracle, shape, axis):
+    """FP32 X tiles (254 updated cells per block) and Y segments (32 rows) crossing boundaries:
+    one sweep against the FP64 oracle.  On random discontinuous data a few cells may take the
+    other branch of a limiter (FP32 vs FP64 rounding near r = 1 or the 1e-5 clamp); a tiling
+    error would instead give O(1) errors along whole tile edges."""
+    rng = np.random.default_rng(shape[0] * 1000 + axis)
+    for lim in (0, 1, 2):
+        for bc in (0, 1):
+            s = cases.newton_state(rng, shape)
+            g = grid_from(cg, 0, s, 0.01, precision=1, bc=bc)
+            g.sweep(axis, 2, 0.002, 0.0, lim)
+            got = g.get_prim()
+            want = oracle.sweep(0, s, axis, 2, 0.01, 0.002, 0.0, lim, 1.4, bc)
+            rel = (np.abs(got - want) / (np.abs(want) + 1e-3)).max(axis=-1)
+            assert np.median(rel) < 1e-6, (lim, bc, np.median(rel))
+            assert rel.max() < 1e-2, (lim, bc, rel.max())
+            assert (rel > 1e-5).mean() < 0.01, (lim, bc, (rel > 1e-5).mean())
