@@ -65,6 +65,7 @@ SIGNATURES = {
     "cosmos_grid_amr_derefine": (_i, [_p, _p, _d, _u8p, _u8p]),
     "cosmos_solve_prim": (_i, [ctypes.POINTER(Params), _p, _p, ctypes.POINTER(SolveOpts),
                                ctypes.POINTER(SolveResult)]),
+    "cosmos_field_sums_noalloc": (_i, [_p, _i, _i, _i, _i, _sz, _p, _p]),
 }
 
 _lib = None

@@ -32,6 +32,7 @@ UNITS = {
     "kernels_adjoint.cu": ["--fmad=false"],
     "capi.cu": [],
     "capi_batch.cu": [],
+    "noalloc.cu": [],
 }
 
 

@@ -42,6 +42,11 @@ int fail(int code, const char* fmt, ...) {
 
 }  // namespace
 
+namespace cg {
+// lets other translation units report an error through cosmos_last_error()
+void set_error(const char* msg) { t_err = msg ? msg : ""; }
+}  // namespace cg
+
 struct cosmos_ctx {
     int device;
     cudaStream_t stream;

@@ -158,6 +158,22 @@ int cosmos_grid_amr_flags(cosmos_grid* g, double tol, unsigned char* coarse, uns
 int cosmos_grid_amr_derefine(cosmos_grid* coarse, cosmos_grid* fine, double tol, unsigned char* coarse_flags,
                              unsigned char* fine_flags);
 
+/* Allocation-free conservation sums.  No counterpart in the reference: it exists for callers that
+ * cannot allocate device memory where they need the sums -- code recorded into a CUDA graph
+ * (allocation is not allowed during stream capture), host callbacks or foreign runtimes that own
+ * the device allocator, fixed-budget embedded callers.  Same sums as cosmos_grid_field_sums, on a
+ * caller-owned structure-of-arrays state: field f of cell (i, j) at
+ * state[f * field_stride + i * pitch + j], doubles (COSMOS_FP64) or floats (COSMOS_FP32).
+ * out5 is caller-owned device memory for 5 doubles; the work is enqueued on `stream` (a
+ * cudaStream_t, 0 for the legacy stream) and not synchronised.  It allocates nothing: its
+ * reduction scratch is a fixed device array of COSMOS_NOALLOC_MAX_ROWS rows (640 KB, held on
+ * every device that loads the library), so grids with more rows are rejected (COSMOS_EINVAL).
+ * The first call on a device looks up that array's device address (make it before any stream
+ * capture).  All calls share the array: calls whose kernels overlap on the GPU race. */
+#define COSMOS_NOALLOC_MAX_ROWS 16384
+int cosmos_field_sums_noalloc(const void* state, int precision, int nx, int ny, int pitch, size_t field_stride,
+                              double* out5, void* stream);
+
 /* One-shot drop-in for the reference's static solve entry points with host buffers:
  * prim_in/prim_out are 5*nx*ny doubles (may alias). */
 int cosmos_solve_prim(const cosmos_params* p, const double* prim_in, double* prim_out, const cosmos_solve_opts* o,
