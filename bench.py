@@ -310,8 +310,186 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+BATCH_WORKLOAD = "config5: 256 independent Newtonian Euler grids (1D and 2D), every side log-uniform in " \
+                 "[128, 2048] cells (seed 5), seeded Riemann data, SLIC MinBee, CFL 0.9, transmissive, dx = 1/nx"
+
+
+def batch_problem():
+    import cases
+    shapes = cases.batch_shapes()
+    states = [cases.riemann(sh, 1000 + k) for k, sh in enumerate(shapes)]
+    dxs = [1.0 / sh[-1] for sh in shapes]
+    return shapes, states, dxs
+
+
+def batch_cpu_baseline(shapes, states, dxs, seconds=12.0):
+    """The CPU oracle on the batched workload: one step of each grid in turn (the grids are
+    independent) until `seconds` have passed; cell-updates per second."""
+    from oracle.pyoracle import Oracle
+    O = Oracle()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    t0 = time.perf_counter()
+    cells = grids = 0
+    for k in range(len(shapes)):
+        O.solve(0, states[k], 2, dxs[k], 0.9, 1e9, 0.0, 2, 1.4, 0, max_steps=1)
+        cells += int(np.prod(shapes[k]))
+        grids += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    el = time.perf_counter() - t0
+    return {"value": cells / el, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"one FP64 oracle step of each of the first {grids} grids ({cells} cells) in {el:.1f} s "
+                      f"on {cores} host threads"}
+
+
+def run_batch(args):
+    import torch
+    import cosmos_gb300 as cg
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    L = cg.load()
+    ctx = cg.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    shapes, states, dxs = batch_problem()
+    cells = sum(int(np.prod(sh)) for sh in shapes)
+    bytes_step = sum(int(np.prod(sh)) * (120 if len(sh) == 2 else 40) for sh in shapes)
+
+    def timed(fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            fn()
+            b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    b = cg.Batch(shapes, dxs, 1.4, cg.FP32, cg.BC_TRANSMISSIVE, ctx=ctx)
+    for k, s in enumerate(states):
+        b.set_prim(k, s)
+    b.run_begin(0.9, 1e30, 0.0, cg.MINBEE)
+    tile_ms = {f"{nt}x{seg}{'c' if cap else ''}": b.time_shape(nt, seg, cap, steps=5)
+               for nt in (128, 256) for seg in (32, 64) for cap in (0, 1)}
+    tuned, _ = b.autotune(None)
+    b.run_steps(args.warmup)
+    launches0 = L.cosmos_kernel_launches()
+    with Clocks(local) as clk:
+        ms = timed(lambda: b.run_steps(args.steps)) / args.steps
+    launches = L.cosmos_kernel_launches() - launches0
+    res = b.run_end()
+    value = cells / (ms * 1e-3)
+    peak, peak_kind = peaks()
+    gbs = bytes_step / (ms * 1e-3) / 1e9
+
+    # the same grids advanced one by one (each its own graph-replayed steps), for comparison
+    ku = 5
+    singles = []
+    for k, sh in enumerate(shapes):
+        g = cg.Grid(cg.NEWTONIAN, sh, dxs[k], 1.4, cg.FP32, cg.BC_TRANSMISSIVE, ctx=ctx)
+        g.set_prim(states[k])
+        g.run_begin(2, 0.9, 1e30, 0.0, cg.MINBEE)
+        g.run_steps(3)
+        singles.append(g)
+    ms_u = timed(lambda: [g.run_steps(ku) for g in singles]) / ku
+    for g in singles:
+        g.close()
+
+    # FP64 batch (bit-identical to the reference per grid) and the FP32-vs-FP64 density error
+    nerr = 10
+    b64 = cg.Batch(shapes, dxs, 1.4, cg.FP64, cg.BC_TRANSMISSIVE, ctx=ctx)
+    b32 = cg.Batch(shapes, dxs, 1.4, cg.FP32, cg.BC_TRANSMISSIVE, ctx=ctx)
+    for k, s in enumerate(states):
+        b64.set_prim(k, s)
+        b32.set_prim(k, s)
+    b64.run_begin(0.9, 1e30, 0.0, cg.MINBEE, max_steps=nerr)
+    b64.autotune(None)
+    ms64 = timed(lambda: b64.run_steps(nerr)) / nerr
+    b64.run_end()
+    b32.run_begin(0.9, 1e30, 0.0, cg.MINBEE, max_steps=nerr)
+    b32.set_shape(*tuned)
+    b32.run_steps(nerr)
+    b32.run_end()
+    num = den = 0.0
+    for k in range(len(shapes)):
+        r64 = b64.get_prim(k)[..., 0]
+        num += float(np.abs(b32.get_prim(k)[..., 0] - r64).sum())
+        den += float(np.abs(r64).sum())
+    b64.close()
+    b32.close()
+
+    # e2e: per step, every grid's primitive state host -> device, one batched step, state -> host
+    hosts = [torch.empty(sh + (5,), dtype=torch.float64, pin_memory=True) for sh in shapes]
+    for h, s in zip(hosts, states):
+        h.numpy()[...] = s
+    be = cg.Batch(shapes, dxs, 1.4, cg.FP32, cg.BC_TRANSMISSIVE, ctx=ctx)
+    be.set_shape(*tuned)
+    be.run_begin(0.9, 1e30, 0.0, cg.MINBEE)
+
+    def e2e_step():
+        for k, h in enumerate(hosts):
+            cg._lib.check(L.cosmos_batch_set_prim(be.h, k, h.data_ptr(), h.numel()))
+        be.run_steps(1)
+        for k, h in enumerate(hosts):
+            cg._lib.check(L.cosmos_batch_get_prim(be.h, k, h.data_ptr(), h.numel()))
+    e2e_step()
+    e2e_steps = 3
+    e2e_ms = timed(lambda: [e2e_step() for _ in range(e2e_steps)]) / e2e_steps
+    be.close()
+    nbytes = cells * 5 * 8
+
+    base = None if args.no_cpu else batch_cpu_baseline(shapes, states, dxs, args.cpu_seconds)
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": BATCH_WORKLOAD, "grids": len(shapes), "grids_2d": sum(len(s) == 2 for s in shapes),
+                   "cells": cells, "precision": "fp32 bulk", "tile_shape": list(tuned),
+                   "l2": f"state {cells * 40 / 1e9:.2f} GB > 129 MB L2 (no flush needed)",
+                   "launch": "one persistent cooperative kernel per 10 steps, replayed from a CUDA graph"},
+        "tile_ms_per_step": tile_ms,
+        "unbatched": {"value": cells / (ms_u * 1e-3), "ms_per_step": ms_u,
+                      "what": "the same grids stepped one after another, each by its own graph-replayed steps"},
+        "fp64": {"value": cells / (ms64 * 1e-3), "ms_per_step": ms64, "steps": nerr,
+                 "path": "FP64 batch, bit-identical to the reference per grid"},
+        "l1_rho_fp32_vs_fp64": num / den, "l1_steps": nerr,
+        "e2e": {"value": cells / (e2e_ms * 1e-3), "unit": METRIC, "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms, "steps": e2e_steps,
+                "what": "per step: each grid's pinned host AoS FP64 primitives -> device, one batched step, "
+                        "states -> host"},
+        "roofline": {"bound": "hbm", "kernel": "batch_step_kernel<NewtonFastPolicy> (whole step, FP32)",
+                     "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak, "peak_source": peak_kind,
+                     "traffic": traffic_per_launch("batch_step_fp32"), "algorithmic_bytes_per_step": bytes_step,
+                     "bytes_per_cell_update": "40 (1D), 120 (2D)"},
+        "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+        "status": [r.status for r in res if r.status][:8],
+    }
+    if base:
+        line["cpu_baseline"] = base
+    print(json.dumps(line), flush=True)
+
+
+def run_batch_reference(args):
+    rank, _, _ = dist_env()
+    if rank != 0:
+        return
+    shapes, states, dxs = batch_problem()
+    cells = sum(int(np.prod(sh)) for sh in shapes)
+    base = batch_cpu_baseline(shapes, states, dxs, max(8.0, 2.0 * args.steps))
+    line = {"metric": METRIC, "value": base["value"], "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": cells / base["value"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": BATCH_WORKLOAD, "grids": len(shapes), "cells": cells},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="grid", choices=["grid", "batch"],
+                    help="grid: one 4096^2 grid (default); batch: 256 uneven grids in one persistent launch")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
@@ -323,7 +501,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.workload == "batch":
+        run_batch_reference(args) if args.impl == "reference" else run_batch(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -66,6 +66,18 @@ SIGNATURES = {
     "cosmos_solve_prim": (_i, [ctypes.POINTER(Params), _p, _p, ctypes.POINTER(SolveOpts),
                                ctypes.POINTER(SolveResult)]),
     "cosmos_field_sums_noalloc": (_i, [_p, _i, _i, _i, _i, _sz, _p, _p]),
+    "cosmos_batch_create": (_i, [_p, _i, _p, _p, _p, _p, _d, _i, _i, ctypes.POINTER(_p)]),
+    "cosmos_batch_destroy": (_i, [_p]),
+    "cosmos_batch_size": (_i, [_p, ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_longlong)]),
+    "cosmos_batch_set_prim": (_i, [_p, _i, _p, _sz]),
+    "cosmos_batch_get_prim": (_i, [_p, _i, _p, _sz]),
+    "cosmos_batch_run_begin": (_i, [_p, ctypes.POINTER(SolveOpts)]),
+    "cosmos_batch_run_steps": (_i, [_p, _i]),
+    "cosmos_batch_run_end": (_i, [_p, _p]),
+    "cosmos_batch_set_shape": (_i, [_p, _i, _i, _i]),
+    "cosmos_batch_time_shape": (_i, [_p, _i, _i, _i, _i, ctypes.POINTER(_d)]),
+    "cosmos_batch_autotune": (_i, [_p, ctypes.c_char_p, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i),
+                                   ctypes.POINTER(_d)]),
 }
 
 _lib = None

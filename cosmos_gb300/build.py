@@ -28,7 +28,8 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relax
 UNITS = {
     "kernels_exact.cu": ["--fmad=false"],
     "kernels_fast.cu": [],
-    "kernels_batch.cu": [],
+    "kernels_batch_fast.cu": [],
+    "kernels_batch_exact.cu": ["--fmad=false"],
     "kernels_adjoint.cu": ["--fmad=false"],
     "capi.cu": [],
     "capi_batch.cu": [],

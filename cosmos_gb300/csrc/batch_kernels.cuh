@@ -1,0 +1,190 @@
+// Batched Newtonian SLIC for many independent grids of uneven sizes in ONE persistent launch.
+//
+// Every grid keeps its own step controller (t, dt, iteration, CFL maximum), exactly as if each
+// were solved alone by the reference's solve / solve2D loop (Solvers/EulerSecondOrderSolver.cpp:
+// 102-147); the grids only share the launch.  One launch runs `nsteps` steps; each step is four
+// phases separated by grid-wide barriers:
+//   A  dt of every grid from its last CFL reduction (the reference's computeStableTimeStep);
+//   B  the X sweep of every grid (full dt for 1D grids, dt/2 for 2D grids);
+//   C  the Y sweep of every 2D grid (dt);
+//   D  the second X sweep of every 2D grid (dt/2), with each grid's CFL reduction fused in.
+// Work is a list of items per phase (X: a few rows of one grid, tiled; Y: a block of columns
+// times a run of rows), dealt to the resident blocks round-robin.  The barrier needs co-residency, so the
+// launch is cooperative; every wait is bounded and reports a timeout instead of hanging.
+#pragma once
+#include "policies.cuh"
+
+namespace cg {
+
+struct BatchGrid {
+    size_t off;   // element offset of the grid's state inside each pool buffer
+    Geom G;       // geometry (axis field unused)
+    double dx;
+};
+
+// X item: rows [a, b) of grid g, each row in tiles of NT - 2 cells; Y item: columns [a, a + NT)
+// and rows [b, c) of grid g.  Items hold several tiles so that the per-item set-up (descriptor
+// loads, time step, two barriers) and the CFL reduction are paid once per few thousand cells.
+struct BatchItem { int g, a, b, c; };
+
+struct GridBarrier {
+    unsigned int count;
+    unsigned int gen;
+    int err;
+};
+
+struct BatchDev {
+    const BatchGrid* grids;
+    StepCtl* ctl;
+    int ngrids;
+    const BatchItem* items[3];  // phases B, C, D
+    int nitems[3];
+    void* buf[2];
+    GridBarrier* bar;
+    int* gstep;                 // steps completed by the batch (buffer parity)
+};
+
+// dt of one step from the last CFL reduction (Solvers/EulerSolvers.cpp:130-161); the solver loop's
+// `while (t < t_final)` becomes `active`.
+CG_D void step_ctl_advance(StepCtl* c) {
+    if (!(c->t < c->t_final) || c->it >= c->it_limit) {
+        c->active = 0;
+        c->dt = 0.0;
+        return;
+    }
+    const double smax = __longlong_as_double((long long)c->smax[c->it & 1]);
+    double dt = c->cfl * (c->dx / smax);
+    if (c->it <= 5) dt = dt * 0.2;
+    if ((c->t + dt) > c->t_final) dt = c->t_final - c->t;
+    if (!(dt > 0.0) || !isfinite(dt)) c->status |= ST_NONFINITE;
+    c->dt = dt;
+    c->fc[0] = make_fast_coef(dt, c->dx);
+    c->fc[1] = make_fast_coef(dt * 0.5, c->dx);
+    c->active = 1;
+    c->smax[(c->it + 1) & 1] = 0ull;
+    c->t = c->t + dt;
+    c->it = c->it + 1;
+}
+
+// Grid-wide barrier for a cooperative launch.  Waits are bounded (about 4 s); a block that gives
+// up sets err, and every block returns at its next barrier.
+CG_D bool grid_sync(GridBarrier* b) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* vgen = &b->gen;
+        volatile int* verr = &b->err;
+        const unsigned int g = *vgen;
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(&b->count, 1u) == gridDim.x - 1) {
+            atomicExch(&b->count, 0u);
+            __threadfence();
+            atomicAdd(&b->gen, 1u);
+        } else {
+            long long spins = 0;
+            while (*vgen == g) {
+                if (*verr) { ok = 0; break; }
+                __nanosleep(64);
+                if (++spins > (1ll << 26)) { atomicOr(&b->err, ST_TIMEOUT); ok = 0; break; }
+            }
+        }
+        __threadfence();
+        s_ok = ok && !*verr;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Policies specialised per grid (dims, nx, dx) for one work item.
+template <class Pol>
+CG_D void bind_grid(Pol& p, const BatchGrid& bg) {
+    p.lm.nx = bg.G.nx;
+    p.dims = bg.G.dims;
+    if constexpr (Pol::kHasDx) p.dx = bg.dx;
+}
+
+// MINB: minimum resident blocks per SM requested from the compiler (1 = no register cap;
+// 768 / NT caps registers near 80 so that more warps hide latency, at the price of a few spills).
+template <class PolX, class PolY, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) batch_step_kernel(PolX polx0, PolY poly0, BatchDev B, int nsteps) {
+    using X = typename PolX::X;
+    using S = typename PolX::S;
+    using W = typename PolX::W;
+    __shared__ XTileSmem<X, NT> sm;
+    __shared__ typename PolX::Coef s_cx;
+    __shared__ typename PolY::Coef s_cy;
+    __shared__ int s_act;
+    const int step0 = *B.gstep;
+    for (int s = 0; s < nsteps; s++) {
+        const int p = (step0 + s) & 1;
+        // ---- A: per-grid time steps
+        for (int g = blockIdx.x * NT + threadIdx.x; g < B.ngrids; g += gridDim.x * NT) step_ctl_advance(&B.ctl[g]);
+        if (!grid_sync(B.bar)) return;
+        // ---- B, C, D
+        for (int ph = 0; ph < 3; ph++) {
+            // selects rather than indexing, so the descriptor stays in the parameter bank
+            void* b0 = p ? B.buf[1] : B.buf[0];
+            void* b1 = p ? B.buf[0] : B.buf[1];
+            const S* src = (const S*)(ph == 1 ? b1 : b0);
+            S* dst = (S*)(ph == 1 ? b0 : b1);
+            const BatchItem* items = ph == 0 ? B.items[0] : (ph == 1 ? B.items[1] : B.items[2]);
+            const int n = ph == 0 ? B.nitems[0] : (ph == 1 ? B.nitems[1] : B.nitems[2]);
+            for (int k = blockIdx.x; k < n; k += gridDim.x) {
+                const BatchItem it = items[k];
+                const BatchGrid bg = B.grids[it.g];
+                StepCtl* ctl = &B.ctl[it.g];
+                const bool one_d = bg.G.dims == 1;
+                DtSrc ds;
+                ds.ctl = ctl;
+                ds.fixed = 0.0;
+                ds.nsub = 0;
+                ds.scale = (ph == 1 || one_d) ? 1.0 : 0.5;
+                ds.fsel = (ph == 1 || one_d) ? 0 : 1;
+                SweepOut out;
+                out.smax = nullptr;
+                out.ws_ctl = nullptr;
+                out.status = &ctl->status;
+                out.mask = nullptr;
+                // CFL reduction on the last sweep of the grid's step
+                const bool ws = (ph == 0 && one_d) || ph == 2;
+                __syncthreads();  // the previous item's shared memory (coefficients, reduction) is no longer read
+                if (threadIdx.x == 0) {
+                    double dt;
+                    s_act = ds.get(dt);
+                    if (s_act) {
+                        if (ph == 1) s_cy = poly0.make_coef(ds, dt);
+                        else s_cx = polx0.make_coef(ds, dt);
+                    }
+                }
+                __syncthreads();
+                const bool act = s_act != 0;
+                W w = W(0);
+                Geom G = bg.G;
+                if (ph == 1) {
+                    G.axis = 1;
+                    PolY pol = poly0;
+                    bind_grid(pol, bg);
+                    if (act) pol.use_coef(s_cy);
+                    w = y_march_seg<PolY, 2, NT>(pol, G, src + bg.off, dst + bg.off, it.a, it.b, it.c, act, out, ws);
+                } else {
+                    G.axis = 0;
+                    PolX pol = polx0;
+                    bind_grid(pol, bg);
+                    if (act) pol.use_coef(s_cx);
+                    for (int row = it.a; row < it.b; row++)
+                        for (int s0 = 0; s0 < G.nx; s0 += NT - 2) {
+                            const W wt = x_own_tile<PolX, 2, NT>(pol, G, src + bg.off, dst + bg.off, row, s0, act, out,
+                                                                 ws, sm);
+                            w = wt > w ? wt : w;
+                        }
+                }
+                if (ws && act) block_max_to<NT>(&ctl->smax[ctl->it & 1], w);
+            }
+            if (!grid_sync(B.bar)) return;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *B.gstep = step0 + nsteps;
+}
+
+}  // namespace cg

@@ -45,12 +45,28 @@ int fail(int code, const char* fmt, ...) {
 namespace cg {
 // lets other translation units report an error through cosmos_last_error()
 void set_error(const char* msg) { t_err = msg ? msg : ""; }
+// lets other translation units keep launches recorded into a graph out of the launch count
+void set_capturing(bool on) { t_capturing = on; }
 }  // namespace cg
 
+// A context lives until cosmos_ctx_destroy has been called AND its last grid or batch is
+// destroyed: objects hold a reference, so teardown in any order never touches a freed stream.
 struct cosmos_ctx {
     int device;
     cudaStream_t stream;
+    std::atomic<int> refs;
 };
+
+namespace cg {
+void ctx_retain(cosmos_ctx* c) { c->refs.fetch_add(1); }
+void ctx_release(cosmos_ctx* c) {
+    if (c->refs.fetch_sub(1) != 1) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    cudaStreamDestroy(c->stream);
+    delete c;
+}
+}  // namespace cg
 
 struct cosmos_grid {
     cosmos_ctx* ctx;
@@ -227,6 +243,7 @@ int cosmos_ctx_create(int device, cosmos_ctx** out) {
     CK(cudaSetDevice(device));
     cosmos_ctx* c = new cosmos_ctx();
     c->device = device;
+    c->refs.store(1);
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete c;
@@ -237,11 +254,7 @@ int cosmos_ctx_create(int device, cosmos_ctx** out) {
 }
 
 int cosmos_ctx_destroy(cosmos_ctx* c) {
-    if (!c) return COSMOS_OK;
-    cudaSetDevice(c->device);
-    cudaStreamSynchronize(c->stream);
-    cudaStreamDestroy(c->stream);
-    delete c;
+    if (c) ctx_release(c);
     return COSMOS_OK;
 }
 
@@ -261,6 +274,7 @@ int cosmos_grid_create(cosmos_ctx* ctx, const cosmos_params* p, cosmos_grid** ou
     cosmos_grid* g = new cosmos_grid();
     memset((void*)g, 0, sizeof *g);
     g->ctx = ctx;
+    ctx_retain(ctx);
     g->p = *p;
     g->elem = p->precision == COSMOS_FP64 ? sizeof(double) : sizeof(float);
     g->G.nx = p->nx;
@@ -304,7 +318,9 @@ int cosmos_grid_destroy(cosmos_grid* g) {
     if (g->staging) cudaFree(g->staging);
     if (g->sums) cudaFree(g->sums);
     if (g->status) cudaFree(g->status);
+    cosmos_ctx* ctx = g->ctx;
     delete g;
+    ctx_release(ctx);
     return COSMOS_OK;
 }
 

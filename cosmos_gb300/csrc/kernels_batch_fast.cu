@@ -1,0 +1,59 @@
+// Batched persistent launch, FP32 Newtonian policy (contraction on).
+#include "batch_kernels.cuh"
+#include "launch.h"
+
+namespace cg {
+
+namespace {
+
+template <int LIM, int NT, int CAP>
+struct FastBatch {
+    using PX = NewtonFastPolicy<0, LIM, false>;
+    using PY = NewtonFastPolicy<1, LIM, false>;
+    static constexpr int MINB = CAP ? 768 / NT : 1;
+    static void* fn() { return (void*)batch_step_kernel<PX, PY, NT, MINB>; }
+    static cudaError_t launch(const BatchLaunch& L) {
+        PX px = make_newton_fast<0, LIM, false>(L.gamma, L.bias, 0, 2);
+        PY py = make_newton_fast<1, LIM, false>(L.gamma, L.bias, 0, 2);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(L.blocks);
+        cfg.blockDim = dim3(NT);
+        cfg.stream = L.stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, batch_step_kernel<PX, PY, NT, MINB>, px, py, *L.B, L.nsteps);
+    }
+};
+
+// Dispatch over the kernel variants: threads per block and register cap.
+template <int LIM, class F>
+auto by_shape(int nt, int cap, F&& f) -> decltype(f(FastBatch<LIM, 128, 0>())) {
+    if (nt == 128) return cap ? f(FastBatch<LIM, 128, 1>()) : f(FastBatch<LIM, 128, 0>());
+    return cap ? f(FastBatch<LIM, 256, 1>()) : f(FastBatch<LIM, 256, 0>());
+}
+
+template <class F>
+auto by_lim(int lim, int nt, int cap, F&& f) -> decltype(f(FastBatch<0, 128, 0>())) {
+    if (lim == 0) return by_shape<0>(nt, cap, f);
+    if (lim == 1) return by_shape<1>(nt, cap, f);
+    return by_shape<2>(nt, cap, f);
+}
+
+}  // namespace
+
+cudaError_t launch_batch_fast(const BatchLaunch& L) {
+    if (L.nt != 128 && L.nt != 256) return cudaErrorInvalidValue;
+    cudaError_t e = by_lim(L.lim, L.nt, L.cap, [&](auto k) { return decltype(k)::launch(L); });
+    count_launch();
+    return e;
+}
+
+void* batch_fast_fn(int nt, int cap, int lim) {
+    if (nt != 128 && nt != 256) return nullptr;
+    return by_lim(lim, nt, cap, [](auto k) { return decltype(k)::fn(); });
+}
+
+}  // namespace cg

@@ -12,20 +12,7 @@ constexpr int kYSeg = 32;
 
 template <int AXIS, int LIM, bool MASKED>
 NewtonFastPolicy<AXIS, LIM, MASKED> make_fast(const SweepArgs& a) {
-    NewtonFastPolicy<AXIS, LIM, MASKED> p;
-    const float g = (float)a.gamma, w = (float)a.bias;
-    p.P.g1 = g - 1.0f;
-    p.P.hg1 = 0.5f * (g - 1.0f);
-    p.P.gam = g;
-    p.P.wa = 0.5f * (1.0f + w);
-    p.P.wb = 0.5f * (1.0f - w);
-    p.P.hom = 0.5f * (1.0f - w);
-    p.P.hop = 0.5f * (1.0f + w);
-    p.lm.axis = AXIS;
-    p.lm.nx = a.G.nx;
-    p.dims = a.G.dims;
-    p.dtdx = p.half_dtdx = p.q_dxdt = 0.0f;
-    return p;
+    return make_newton_fast<AXIS, LIM, MASKED>(a.gamma, a.bias, a.G.nx, a.G.dims);
 }
 
 template <int AXIS, int LIM, bool MASKED>

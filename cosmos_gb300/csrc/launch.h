@@ -50,4 +50,21 @@ cudaError_t launch_field_sums(const void* soa, const Geom& G, int precision, dou
 // bookkeeping: every kernel launch made by the library bumps this counter
 void count_launch(unsigned n = 1);
 
+// ---- batched persistent launch (batch_kernels.cuh); BatchDev is declared there
+struct BatchDev;
+struct BatchLaunch {
+    const BatchDev* B;  // host copy of the device descriptor
+    int nsteps;
+    int nt, seg, cap, lim;  // tile shape (threads, Y rows, register cap) and limiter
+    double gamma, bias;
+    int blocks;             // resident blocks (cooperative grid size)
+    cudaStream_t stream;
+};
+// Tile shapes of the batched launch: (threads per block, rows per Y work item, register cap).
+constexpr int kBatchShapes[][3] = {{128, 32, 0}, {128, 64, 0}, {256, 32, 0}, {256, 64, 0},
+                                   {128, 32, 1}, {128, 64, 1}, {256, 32, 1}, {256, 64, 1}};
+constexpr int kNumBatchShapes = 8;
+cudaError_t launch_batch_fast(const BatchLaunch& L);
+cudaError_t launch_batch_exact(const BatchLaunch& L);
+
 }  // namespace cg

@@ -37,6 +37,7 @@ struct ExactPolicy {
     struct Coef { double dt; };
     static constexpr bool kShared = !Sys::kCoords;
     static constexpr bool kMasked = true;
+    static constexpr bool kHasDx = true;
     Sys sys;
     LineMap lm;
     int dims, order, ny;
@@ -155,6 +156,7 @@ struct NewtonFastPolicy {
     using Coef = FastCoef;
     static constexpr bool kShared = true;
     static constexpr bool kMasked = MASKED;
+    static constexpr bool kHasDx = false;  // dx enters through the precomputed coefficients
     NewtonFastParams P;
     LineMap lm;
     int dims;
@@ -188,5 +190,23 @@ struct NewtonFastPolicy {
     CG_D float wavespeed(const Cell& c, int, int) const { return nf_wavespeed(P, c.v, dims); }
     CG_D void flush_status(int*) const {}
 };
+
+template <int AXIS, int LIM, bool MASKED>
+inline NewtonFastPolicy<AXIS, LIM, MASKED> make_newton_fast(double gamma, double bias, int nx, int dims) {
+    NewtonFastPolicy<AXIS, LIM, MASKED> p;
+    const float g = (float)gamma, w = (float)bias;
+    p.P.g1 = g - 1.0f;
+    p.P.hg1 = 0.5f * (g - 1.0f);
+    p.P.gam = g;
+    p.P.wa = 0.5f * (1.0f + w);
+    p.P.wb = 0.5f * (1.0f - w);
+    p.P.hom = 0.5f * (1.0f - w);
+    p.P.hop = 0.5f * (1.0f + w);
+    p.lm.axis = AXIS;
+    p.lm.nx = nx;
+    p.dims = dims;
+    p.dtdx = p.half_dtdx = p.q_dxdt = 0.0f;
+    return p;
+}
 
 }  // namespace cg

@@ -179,29 +179,33 @@ __global__ void __launch_bounds__(NT) sweep_x_kernel(Pol pol, Geom G, const type
 // registers), computes the flux at c's right interface, and updates c with that flux and its
 // left neighbour's.  Shared memory carries only what crosses threads: the cells (stencil
 // neighbours), the left faces and the fluxes.  NT threads update NT - 2 cells.
+template <class X, int NT>
+struct XTileSmem {
+    X sc[5][NT + 2];  // cells s0-2 .. s0+NT-1 (own cell of thread t at t+1)
+    X sl[5][NT];      // left face of the cell owned by thread t
+    X sf[5][NT];      // flux at the right interface of the cell owned by thread t
+};
+
+// One X tile: updates cells s0 .. min(s0 + NT - 2, nx) - 1 of `row`.  `act` and the policy's
+// coefficients are block-uniform and already set; all NT threads call this together, and may call
+// it again at once for another tile (every shared array is last read before a barrier that the
+// next tile's writes to it follow).  Returns the thread's wavespeed maximum over its updated cell
+// when want_w (0 otherwise); the caller reduces it.
 template <class Pol, int ORDER, int NT>
-__global__ void __launch_bounds__(NT) sweep_x_own_kernel(Pol pol, Geom G, const typename Pol::S* __restrict__ src,
-                                                         typename Pol::S* __restrict__ dst, DtSrc ds, SweepOut out) {
+CG_D typename Pol::W x_own_tile(Pol& pol, const Geom& G, const typename Pol::S* __restrict__ src,
+                                typename Pol::S* __restrict__ dst, int row, int s0, bool act, const SweepOut& out,
+                                bool want_w, XTileSmem<typename Pol::X, NT>& sm) {
     using X = typename Pol::X;
     using Cell = typename Pol::Cell;
     using Face = typename Pol::Face;
     constexpr int TS = NT - 2;
-    __shared__ X sc[5][NT + 2];  // cells s0-2 .. s0+NT-1 (own cell of thread t at t+1)
-    __shared__ X sl[5][NT];      // left face of the cell owned by thread t
-    __shared__ X sf[5][NT];      // flux at the right interface of the cell owned by thread t
-    __shared__ typename Pol::Coef s_coef;
-    __shared__ int s_act;
+    auto& sc = sm.sc;
+    auto& sl = sm.sl;
+    auto& sf = sm.sf;
     const int t = threadIdx.x;
-    const int row = blockIdx.y;
-    const int s0 = blockIdx.x * TS;
     const int n = G.nx;
     const int send = min(s0 + TS, n);
     const int c = s0 - 1 + t;  // owned cell (may be a ghost position)
-    if (t == 0) {
-        double dt;
-        s_act = ds.get(dt);
-        if (s_act) s_coef = pol.make_coef(ds, dt);
-    }
     // own cell and, for the two edge threads, the extra stencil cell
     const bool live = c <= send;  // cells beyond send neither update nor feed an interface
     Cell own;
@@ -223,11 +227,10 @@ __global__ void __launch_bounds__(NT) sweep_x_own_kernel(Pol pol, Geom G, const 
         for (int f = 0; f < 5; f++) sc[f][t + 2] = e.v[f];
     }
     __syncthreads();
-    if (!s_act) {  // inactive step: keep the ping-pong buffers consistent
+    if (!act) {  // inactive step: keep the ping-pong buffers consistent
         if (t >= 1 && c < send) store_cell<Pol>(own, dst, G, row, c);
-        return;
+        return typename Pol::W(0);
     }
-    pol.use_coef(s_coef);
     Face L, R;
     if (live) {
         if (ORDER == 2) {
@@ -261,7 +264,6 @@ __global__ void __launch_bounds__(NT) sweep_x_own_kernel(Pol pol, Geom G, const 
     }
     __syncthreads();
     typename Pol::W w = 0;
-    unsigned long long* const wslot = out.slot();
     if (t >= 1 && c < send) {
         Cell nc = own;
         if (pol.active(row, c, out.mask)) {
@@ -271,25 +273,16 @@ __global__ void __launch_bounds__(NT) sweep_x_own_kernel(Pol pol, Geom G, const 
             nc = pol.update(own, Fl, Fr, row, c);
         }
         store_cell<Pol>(nc, dst, G, row, c);
-        if (wslot) w = pol.wavespeed(nc, row, c);
+        if (want_w) w = pol.wavespeed(nc, row, c);
     }
-    if (wslot) block_max_to<NT>(wslot, w);
     pol.flush_status(out.status);
+    return w;
 }
 
-// ------------------------------------------------------------------ Y sweep: column march
-// One thread per column marches SEG rows keeping the stencil in registers.
-template <class Pol, int ORDER, int NT, int SEG>
-__global__ void __launch_bounds__(NT) sweep_y_kernel(Pol pol, Geom G, const typename Pol::S* __restrict__ src,
-                                                     typename Pol::S* __restrict__ dst, DtSrc ds, SweepOut out) {
-    using X = typename Pol::X;
-    using Cell = typename Pol::Cell;
-    using Face = typename Pol::Face;
-    const int j = blockIdx.x * NT + threadIdx.x;
-    const int y0 = blockIdx.y * SEG;
-    const int n = G.ny;
-    const int y1 = min(y0 + SEG, n);
-    const bool col_ok = j < G.nx;
+template <class Pol, int ORDER, int NT>
+__global__ void __launch_bounds__(NT) sweep_x_own_kernel(Pol pol, Geom G, const typename Pol::S* __restrict__ src,
+                                                         typename Pol::S* __restrict__ dst, DtSrc ds, SweepOut out) {
+    __shared__ XTileSmem<typename Pol::X, NT> sm;
     __shared__ typename Pol::Coef s_coef;
     __shared__ int s_act;
     if (threadIdx.x == 0) {
@@ -298,18 +291,39 @@ __global__ void __launch_bounds__(NT) sweep_y_kernel(Pol pol, Geom G, const type
         if (s_act) s_coef = pol.make_coef(ds, dt);
     }
     __syncthreads();
-    if (!s_act) {
+    const bool act = s_act != 0;
+    if (act) pol.use_coef(s_coef);
+    unsigned long long* wslot = out.slot();
+    const auto w = x_own_tile<Pol, ORDER, NT>(pol, G, src, dst, blockIdx.y, blockIdx.x * (NT - 2), act, out,
+                                              wslot != nullptr, sm);
+    if (wslot) block_max_to<NT>(wslot, w);
+}
+
+// ------------------------------------------------------------------ Y sweep: column march
+// One thread per column marches SEG rows keeping the stencil in registers.
+// One Y segment: columns j0 .. j0 + NT - 1, rows y0 .. y1 - 1 (y1 <= ny).  `act` and the
+// policy's coefficients are block-uniform and already set.  Returns the thread's wavespeed
+// maximum over its updated cells when want_w (0 otherwise); the caller reduces it.
+template <class Pol, int ORDER, int NT>
+CG_D typename Pol::W y_march_seg(Pol& pol, const Geom& G, const typename Pol::S* __restrict__ src,
+                                 typename Pol::S* __restrict__ dst, int j0, int y0, int y1, bool act,
+                                 const SweepOut& out, bool want_w) {
+    using X = typename Pol::X;
+    using Cell = typename Pol::Cell;
+    using Face = typename Pol::Face;
+    const int j = j0 + threadIdx.x;
+    const int n = G.ny;
+    const bool col_ok = j < G.nx;
+    if (!act) {
         if (col_ok)
             for (int y = y0; y < y1; y++) {
                 Cell c;
                 load_cell(pol, src, G, y, j, c);
                 store_cell<Pol>(c, dst, G, y, j);
             }
-        return;
+        return typename Pol::W(0);
     }
-    pol.use_coef(s_coef);
     typename Pol::W w = 0;
-    unsigned long long* const wslot = out.slot();
     if (col_ok) {
         auto ld = [&](int y, Cell& c) { load_cell(pol, src, G, ghost_index(y, n, G.bc), j, c); };
         auto need = [&](int fi) {  // interface between fi-1 and fi
@@ -363,13 +377,33 @@ __global__ void __launch_bounds__(NT) sweep_y_kernel(Pol pol, Geom G, const type
             Cell nc = c0;
             if (pol.active(j, y, out.mask)) nc = pol.update(c0, Fp, Fn, j, y);
             store_cell<Pol>(nc, dst, G, y, j);
-            if (wslot) { const typename Pol::W ws = pol.wavespeed(nc, j, y); w = (ws > w) ? ws : w; }
+            if (want_w) { const typename Pol::W ws = pol.wavespeed(nc, j, y); w = (ws > w) ? ws : w; }
             Fp = Fn;
             cm1 = c0; c0 = c1; c1 = c2;
         }
     }
-    if (wslot) block_max_to<NT>(wslot, w);
     pol.flush_status(out.status);
+    return w;
+}
+
+template <class Pol, int ORDER, int NT, int SEG>
+__global__ void __launch_bounds__(NT) sweep_y_kernel(Pol pol, Geom G, const typename Pol::S* __restrict__ src,
+                                                     typename Pol::S* __restrict__ dst, DtSrc ds, SweepOut out) {
+    __shared__ typename Pol::Coef s_coef;
+    __shared__ int s_act;
+    if (threadIdx.x == 0) {
+        double dt;
+        s_act = ds.get(dt);
+        if (s_act) s_coef = pol.make_coef(ds, dt);
+    }
+    __syncthreads();
+    const bool act = s_act != 0;
+    if (act) pol.use_coef(s_coef);
+    unsigned long long* wslot = out.slot();
+    const int y0 = blockIdx.y * SEG;
+    const auto w = y_march_seg<Pol, ORDER, NT>(pol, G, src, dst, blockIdx.x * NT, y0, min(y0 + SEG, G.ny), act, out,
+                                               wslot != nullptr);
+    if (wslot) block_max_to<NT>(wslot, w);
 }
 
 // ------------------------------------------------------------------ helpers

@@ -13,6 +13,7 @@ vector<vector<StateVector>> indexed [row i = y][column j = x].
     the boundary (transmissive as in the reference, or periodic).
 """
 import ctypes
+import sys
 import threading
 
 import numpy as np
@@ -79,9 +80,9 @@ class Context:
         return load().cosmos_ctx_stream(self.h)
 
     def close(self):
-        if self.h:
+        if self.h and not sys.is_finalizing():
             load().cosmos_ctx_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -197,9 +198,91 @@ class Grid:
         return c, f
 
     def close(self):
-        if getattr(self, "h", None):
+        # at interpreter exit the process releases the device; no native teardown then
+        if getattr(self, "h", None) and not sys.is_finalizing():
             load().cosmos_grid_destroy(self.h)
-            self.h = None
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many independent Newtonian grids of uneven sizes advanced by one persistent launch
+    (cosmos_batch).  `shapes` holds one entry per grid: (nx,) for 1D, (ny, nx) for 2D; each grid
+    keeps its own dt and step count, as if the reference's solve / solve2D ran on it alone."""
+
+    def __init__(self, shapes, dx, gamma, precision=FP32, boundary=BC_TRANSMISSIVE, ctx=None):
+        self.ctx = ctx or default_context()
+        self.shapes = [tuple(int(v) for v in s) for s in shapes]
+        n = len(self.shapes)
+        dxs = np.broadcast_to(np.asarray(dx, dtype=np.float64), (n,)).copy()
+        dims = np.array([len(s) for s in self.shapes], dtype=np.int32)
+        nx = np.array([s[-1] for s in self.shapes], dtype=np.int32)
+        ny = np.array([s[0] if len(s) == 2 else 1 for s in self.shapes], dtype=np.int32)
+        h = ctypes.c_void_p()
+        check(load().cosmos_batch_create(self.ctx.h, n, dims.ctypes.data, nx.ctypes.data, ny.ctypes.data,
+                                         dxs.ctypes.data, float(gamma), int(boundary), int(precision),
+                                         ctypes.byref(h)))
+        self.h = h
+        self.dx = dxs
+
+    def __len__(self):
+        return len(self.shapes)
+
+    @property
+    def cells(self):
+        c = ctypes.c_longlong()
+        check(load().cosmos_batch_size(self.h, None, ctypes.byref(c)))
+        return c.value
+
+    def set_prim(self, k, prim):
+        a = np.ascontiguousarray(prim, dtype=np.float64)
+        if a.shape != self.shapes[k] + (5,):
+            raise ValueError(f"grid {k}: expected shape {self.shapes[k] + (5,)}, got {a.shape}")
+        check(load().cosmos_batch_set_prim(self.h, int(k), a.ctypes.data, a.size))
+
+    def get_prim(self, k, out=None):
+        o = np.empty(self.shapes[k] + (5,), dtype=np.float64) if out is None else out
+        check(load().cosmos_batch_get_prim(self.h, int(k), o.ctypes.data, o.size))
+        return o
+
+    def run_begin(self, cfl, t_final, bias, limiter, max_steps=-1):
+        o = Grid.opts(2, cfl, t_final, bias, limiter, 1, max_steps)
+        check(load().cosmos_batch_run_begin(self.h, ctypes.byref(o)))
+
+    def run_steps(self, n):
+        check(load().cosmos_batch_run_steps(self.h, int(n)))
+
+    def run_end(self):
+        r = (SolveResult * len(self.shapes))()
+        check(load().cosmos_batch_run_end(self.h, r))
+        return list(r)
+
+    def set_shape(self, threads, rows, cap=0):
+        check(load().cosmos_batch_set_shape(self.h, int(threads), int(rows), int(cap)))
+
+    def time_shape(self, threads, rows, cap=0, steps=3):
+        ms = ctypes.c_double()
+        check(load().cosmos_batch_time_shape(self.h, int(threads), int(rows), int(cap), int(steps), ctypes.byref(ms)))
+        return ms.value
+
+    def autotune(self, cache_path=None):
+        """Times every tile shape (threads, rows, cap), keeps the fastest; returns it and its ms/step."""
+        nt, seg, cap, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        path = cache_path.encode() if cache_path else None
+        check(load().cosmos_batch_autotune(self.h, path, ctypes.byref(nt), ctypes.byref(seg), ctypes.byref(cap),
+                                           ctypes.byref(ms)))
+        return (nt.value, seg.value, cap.value), ms.value
+
+    def close(self):
+        # at interpreter exit the process releases the device; no native teardown then
+        if getattr(self, "h", None) and not sys.is_finalizing():
+            load().cosmos_batch_destroy(self.h)
+        self.h = None
 
     def __del__(self):
         try:

@@ -88,6 +88,8 @@ typedef struct cosmos_grid cosmos_grid;
 
 /* ---- context */
 int cosmos_ctx_create(int device, cosmos_ctx** out);
+/* Releases the caller's reference: the stream is destroyed once the last grid or batch created on
+ * the context has been destroyed too, so objects may be destroyed in any order. */
 int cosmos_ctx_destroy(cosmos_ctx* ctx);
 int cosmos_ctx_synchronize(cosmos_ctx* ctx);
 void* cosmos_ctx_stream(cosmos_ctx* ctx); /* the cudaStream_t all work of this context runs on */
@@ -157,6 +159,33 @@ int cosmos_grid_amr_flags(cosmos_grid* g, double tol, unsigned char* coarse, uns
  * dx at tol/2; unflags children, flags the parent and restricts the coarse state. */
 int cosmos_grid_amr_derefine(cosmos_grid* coarse, cosmos_grid* fine, double tol, unsigned char* coarse_flags,
                              unsigned char* fine_flags);
+
+/* ---- batched grids: many independent Newtonian grids of uneven sizes (1D and 2D) advanced by
+ * one persistent cooperative launch per chunk of steps, replayed from a CUDA graph.  Each grid
+ * keeps its own time step, iteration count and CFL reduction -- the same results as running the
+ * reference's EulerSecondOrderSolver::solve / solve2D (Solvers/EulerSecondOrderSolver.cpp:102-147)
+ * on every grid separately (bit-identical with COSMOS_FP64).  dims/nx/ny/dx hold one entry per
+ * grid (ny ignored for 1D grids). */
+typedef struct cosmos_batch cosmos_batch;
+int cosmos_batch_create(cosmos_ctx* ctx, int ngrids, const int* dims, const int* nx, const int* ny, const double* dx,
+                        double gamma, int boundary, int precision, cosmos_batch** out);
+int cosmos_batch_destroy(cosmos_batch* b);
+int cosmos_batch_size(cosmos_batch* b, int* ngrids, long long* cells);
+int cosmos_batch_set_prim(cosmos_batch* b, int grid, const double* prim, size_t n_doubles);
+int cosmos_batch_get_prim(cosmos_batch* b, int grid, double* prim, size_t n_doubles);
+/* Resets every grid's controller (t = 0, iteration 0) and enqueues the initial CFL reductions;
+ * o->order must be 2.  results of run_end: one cosmos_solve_result per grid (may be NULL). */
+int cosmos_batch_run_begin(cosmos_batch* b, const cosmos_solve_opts* o);
+int cosmos_batch_run_steps(cosmos_batch* b, int n);
+int cosmos_batch_run_end(cosmos_batch* b, cosmos_solve_result* results);
+/* Tile shape of the persistent launch: threads per block (128 or 256), rows per Y-sweep work
+ * item (seg >= 1; the autotuner tries 32 and 64), and cap (1 = registers capped so that 768
+ * threads fit an SM, FP32 only; COSMOS_EUNSUPPORTED for FP64).  cosmos_batch_time_shape times `steps` steps of a shape and
+ * restores the state; cosmos_batch_autotune times every shape, keeps the fastest, and caches the
+ * choice in cache_path (one line per device and batch signature; NULL for no cache). */
+int cosmos_batch_set_shape(cosmos_batch* b, int nt, int seg, int cap);
+int cosmos_batch_time_shape(cosmos_batch* b, int nt, int seg, int cap, int steps, double* ms_per_step);
+int cosmos_batch_autotune(cosmos_batch* b, const char* cache_path, int* nt, int* seg, int* cap, double* ms_per_step);
 
 /* Allocation-free conservation sums.  No counterpart in the reference: it exists for callers that
  * cannot allocate device memory where they need the sums -- code recorded into a CUDA graph

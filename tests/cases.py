@@ -72,3 +72,33 @@ def four_quadrant(n, seed):
 # excised cells, stencils crossing the horizon and plain cells.
 GR_BH = (0.1, 0.0, 0.5, 0.5, 0.0)
 GR_BH_SPIN = (0.1, 0.9, 0.47, 0.52, 0.0)
+
+
+def riemann(shape, seed):
+    """Seeded Riemann problem on a 1D (nx,) or 2D (ny, nx) grid: two states split at the middle
+    in 1D, four quadrants in 2D, each (rho, u, v, p) drawn like four_quadrant's."""
+    rng = np.random.default_rng(seed)
+    q = np.zeros((4, 5))
+    q[:, 0] = rng.uniform(0.1, 1.5, 4)
+    q[:, 1] = rng.uniform(-1.0, 1.0, 4)
+    q[:, 2] = rng.uniform(-1.0, 1.0, 4)
+    q[:, 4] = rng.uniform(0.03, 1.5, 4)
+    p = np.zeros(tuple(shape) + (5,))
+    if len(shape) == 1:
+        h = shape[0] // 2
+        p[:h], p[h:] = q[0], q[1]
+        return p
+    hy, hx = shape[0] // 2, shape[1] // 2
+    p[:hy, :hx], p[:hy, hx:], p[hy:, :hx], p[hy:, hx:] = q[0], q[1], q[2], q[3]
+    return p
+
+
+def batch_shapes(count=256, lo=128, hi=2048, seed=5):
+    """Grid shapes of the batched workload: half 1D, half 2D (by seed), every side drawn
+    log-uniform from [lo, hi] cells."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        side = lambda: int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi))))))  # noqa: E731
+        out.append((side(),) if rng.random() < 0.5 else (side(), side()))
+    return out
