@@ -66,6 +66,7 @@ SIGNATURES = {
     "cosmos_solve_prim": (_i, [ctypes.POINTER(Params), _p, _p, ctypes.POINTER(SolveOpts),
                                ctypes.POINTER(SolveResult)]),
     "cosmos_field_sums_noalloc": (_i, [_p, _i, _i, _i, _i, _sz, _p, _p]),
+    "cosmos_grid_adjoint": (_i, [_p, ctypes.POINTER(SolveOpts), _i, _i, _p, _p, _p, _p, _p, _p]),
     "cosmos_batch_create": (_i, [_p, _i, _p, _p, _p, _p, _d, _i, _i, ctypes.POINTER(_p)]),
     "cosmos_batch_destroy": (_i, [_p]),
     "cosmos_batch_size": (_i, [_p, ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_longlong)]),

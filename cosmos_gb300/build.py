@@ -31,9 +31,11 @@ UNITS = {
     "kernels_batch_fast.cu": [],
     "kernels_batch_exact.cu": ["--fmad=false"],
     "kernels_adjoint.cu": ["--fmad=false"],
+    "kernels_adjoint_fast.cu": [],
     "capi.cu": [],
     "capi_batch.cu": [],
     "noalloc.cu": [],
+    "capi_adjoint.cu": [],
 }
 
 

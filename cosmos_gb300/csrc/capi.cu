@@ -7,6 +7,7 @@
 #include <string>
 
 #include "../../include/cosmos_gb300.h"
+#include "capi_internal.h"
 #include "launch.h"
 
 namespace cg {
@@ -49,14 +50,6 @@ void set_error(const char* msg) { t_err = msg ? msg : ""; }
 void set_capturing(bool on) { t_capturing = on; }
 }  // namespace cg
 
-// A context lives until cosmos_ctx_destroy has been called AND its last grid or batch is
-// destroyed: objects hold a reference, so teardown in any order never touches a freed stream.
-struct cosmos_ctx {
-    int device;
-    cudaStream_t stream;
-    std::atomic<int> refs;
-};
-
 namespace cg {
 void ctx_retain(cosmos_ctx* c) { c->refs.fetch_add(1); }
 void ctx_release(cosmos_ctx* c) {
@@ -68,23 +61,25 @@ void ctx_release(cosmos_ctx* c) {
 }
 }  // namespace cg
 
-struct cosmos_grid {
-    cosmos_ctx* ctx;
-    cosmos_params p;
-    Geom G;                  // geometry of the stored state (axis set per sweep)
-    size_t elem;             // bytes per stored scalar
-    void* buf[2];            // ping-pong state buffers (5 fields each)
-    int cur;                 // buffer holding the current state
-    StepCtl* ctl;            // device step controller
-    double* staging;         // device AoS primitives for set/get
-    double* sums;            // field-sum output + scratch
-    int* status;             // device status word for explicit sweeps
-    // run configuration and captured one-step graphs (one per starting buffer)
-    cosmos_solve_opts run;
-    bool run_ready;
-    cudaGraphExec_t step_graph[2];
-    unsigned step_kernels;   // kernels per captured step
-};
+namespace cg {
+SweepArgs base_args(cosmos_grid* g) {
+    SweepArgs a;
+    memset(&a, 0, sizeof a);
+    a.system = g->p.system;
+    a.G = g->G;
+    a.order = 2;
+    a.dx = g->p.dx;
+    a.gamma = g->p.gamma;
+    a.bh[0] = g->p.bh_mass; a.bh[1] = g->p.bh_spin; a.bh[2] = g->p.bh_x; a.bh[3] = g->p.bh_y; a.bh[4] = g->p.bh_z;
+    a.stream = g->ctx->stream;
+    return a;
+}
+
+cudaError_t sweep_launch(cosmos_grid* g, const SweepArgs& a) {
+    return g->p.precision == COSMOS_FP64 ? launch_sweep_exact(a) : launch_sweep_fast(a);
+}
+
+}  // namespace cg
 
 namespace {
 
@@ -104,23 +99,6 @@ bool valid_params(const cosmos_params* p, std::string& why) {
     if (p->system == COSMOS_GR && p->boundary != COSMOS_BC_TRANSMISSIVE) { why = "the GR system supports transmissive boundaries only"; return false; }
     if (p->precision == COSMOS_FP32 && p->system != COSMOS_NEWTONIAN) { why = "FP32 storage is provided for the Newtonian system"; return false; }
     return true;
-}
-
-SweepArgs base_args(cosmos_grid* g) {
-    SweepArgs a;
-    memset(&a, 0, sizeof a);
-    a.system = g->p.system;
-    a.G = g->G;
-    a.order = 2;
-    a.dx = g->p.dx;
-    a.gamma = g->p.gamma;
-    a.bh[0] = g->p.bh_mass; a.bh[1] = g->p.bh_spin; a.bh[2] = g->p.bh_x; a.bh[3] = g->p.bh_y; a.bh[4] = g->p.bh_z;
-    a.stream = g->ctx->stream;
-    return a;
-}
-
-cudaError_t sweep_launch(cosmos_grid* g, const SweepArgs& a) {
-    return g->p.precision == COSMOS_FP64 ? launch_sweep_exact(a) : launch_sweep_fast(a);
 }
 
 // Enqueue one full solver step starting from buffer `cur`; *cur_out receives the buffer holding

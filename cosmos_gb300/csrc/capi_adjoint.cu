@@ -1,0 +1,195 @@
+// C ABI of the hand-written adjoint: reverse-mode gradient of a final-density misfit through
+// nsteps SLIC steps of a Newtonian grid, with checkpoints every `checkpoint_every` steps.
+//
+// Forward: the grid's own graph-replayed steps (device dt from the CFL rule, or the caller's dts),
+// the state copied to a checkpoint store before every segment and each step's dt logged.
+// Backward, segment by segment from the last: the segment is recomputed from its checkpoint with
+// the same sweep kernels and the same dts, keeping every sweep's input; the sweep adjoints then
+// run in reverse order (X(dt/2) Y(dt) X(dt/2) per 2D step, X(dt) per 1D step).
+#include <algorithm>
+#include <climits>
+#include <cstddef>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "adjoint_kernels.cuh"
+#include "capi_internal.h"
+
+using namespace cg;
+
+namespace {
+
+int afail(int code, const std::string& msg) {
+    set_error(msg.c_str());
+    return code;
+}
+#define ACK(call)                                                                                    \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) return afail(COSMOS_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// Device scratch of one adjoint call, released on every exit path.
+struct Scratch {
+    cudaStream_t st = nullptr;
+    std::vector<void*> ptrs;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    StepCtl* patched = nullptr;  // controller whose dt pointers point into this scratch
+    cudaError_t alloc(void** p, size_t bytes) {
+        cudaError_t e = cudaMallocAsync(p, bytes, st);
+        if (e == cudaSuccess) ptrs.push_back(*p);
+        return e;
+    }
+    void unpatch() {
+        if (!patched) return;
+        // dt_log and dt_fixed are adjacent; a pageable source is staged before the call returns
+        const double* nul[2] = {nullptr, nullptr};
+        cudaMemcpyAsync((char*)patched + offsetof(StepCtl, dt_log), nul, sizeof nul, cudaMemcpyHostToDevice, st);
+        patched = nullptr;
+    }
+    ~Scratch() {
+        unpatch();
+        for (void* p : ptrs) cudaFreeAsync(p, st);
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
+}  // namespace
+
+extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, int nsteps, int checkpoint_every,
+                                   const double* target, const double* dts_in, double* grad_prim, double* loss,
+                                   double* dts_out, double* ms) {
+    if (!g || !o || !target || !grad_prim) return afail(COSMOS_EINVAL, "null grid, options, target or gradient");
+    if (g->p.system != COSMOS_NEWTONIAN) return afail(COSMOS_EUNSUPPORTED, "the adjoint covers the Newtonian system");
+    if (o->order != 2) return afail(COSMOS_EUNSUPPORTED, "the adjoint covers SLIC (order 2)");
+    if (nsteps < 1 || checkpoint_every < 1) return afail(COSMOS_EINVAL, "nsteps and checkpoint_every must be >= 1");
+    if (!dts_in && !(o->cfl > 0.0)) return afail(COSMOS_EINVAL, "cfl must be positive when no dts are given");
+    if (dts_in)
+        for (int s = 0; s < nsteps; s++)
+            if (!(dts_in[s] > 0.0)) return afail(COSMOS_EINVAL, "dts_in[" + std::to_string(s) + "] is not positive");
+    ACK(cudaSetDevice(g->ctx->device));
+    const bool fp64 = g->p.precision == COSMOS_FP64;
+    const Geom G0 = g->G;
+    const size_t ncell = (size_t)G0.nx * G0.ny;
+    const size_t sbytes = G0.fstride * 5 * g->elem;                         // one state, storage precision
+    const size_t abytes = G0.fstride * 5 * (fp64 ? sizeof(double) : sizeof(float));  // one adjoint state
+    const int K = std::min(checkpoint_every, nsteps);
+    const int nck = (nsteps + K - 1) / K;
+    const int spp = g->p.dims == 2 ? 3 : 1;  // sweeps per step
+    Scratch sc;
+    sc.st = g->ctx->stream;
+    cudaStream_t st = sc.st;
+    char *ck, *seg, *adj;
+    double *d_target, *d_dts, *d_rows, *d_loss;
+    ACK(sc.alloc((void**)&ck, (size_t)nck * sbytes));
+    ACK(sc.alloc((void**)&seg, (size_t)K * spp * sbytes));
+    ACK(sc.alloc((void**)&adj, 2 * abytes));
+    ACK(sc.alloc((void**)&d_target, ncell * sizeof(double)));
+    ACK(sc.alloc((void**)&d_dts, nsteps * sizeof(double)));
+    ACK(sc.alloc((void**)&d_rows, (size_t)G0.ny * sizeof(double)));
+    ACK(sc.alloc((void**)&d_loss, sizeof(double)));
+    for (auto& e : sc.ev) ACK(cudaEventCreate(&e));
+    ACK(cudaMemcpyAsync(d_target, target, ncell * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (dts_in) ACK(cudaMemcpyAsync(d_dts, dts_in, nsteps * sizeof(double), cudaMemcpyHostToDevice, st));
+
+    // ---- forward with checkpoints
+    ACK(cudaEventRecord(sc.ev[0], st));
+    cosmos_solve_opts fo = *o;
+    fo.t_final = 1e300;  // exactly nsteps steps
+    fo.max_steps = nsteps;
+    fo.subcycles = 1;
+    if (dts_in) fo.cfl = 1.0;
+    int rc = cosmos_grid_run_begin(g, &fo);
+    if (rc) return rc;
+    double* logp = dts_in ? nullptr : d_dts;
+    const double* fixp = dts_in ? d_dts : nullptr;
+    static_assert(offsetof(StepCtl, dt_fixed) == offsetof(StepCtl, dt_log) + sizeof(double*), "adjacent dt pointers");
+    const void* dtp[2] = {logp, fixp};
+    sc.patched = g->ctl;
+    ACK(cudaMemcpyAsync((char*)g->ctl + offsetof(StepCtl, dt_log), dtp, sizeof dtp, cudaMemcpyHostToDevice, st));
+    for (int c = 0; c < nck; c++) {
+        ACK(cudaMemcpyAsync(ck + (size_t)c * sbytes, g->buf[g->cur], sbytes, cudaMemcpyDeviceToDevice, st));
+        if ((rc = cosmos_grid_run_steps(g, std::min(K, nsteps - c * K)))) return rc;
+    }
+    ACK(cudaEventRecord(sc.ev[1], st));
+    sc.unpatch();  // the controller's dt pointers point into this call's scratch
+
+    // ---- loss and its adjoint seed at the final state
+    int cur = 0;
+    ACK(fp64 ? launch_adjoint_loss_exact(G0, g->buf[g->cur], d_target, adj, d_rows, d_loss, st)
+             : launch_adjoint_loss_fast(G0, g->buf[g->cur], d_target, adj, d_rows, d_loss, st));
+    std::vector<double> dts(nsteps);
+    ACK(cudaMemcpyAsync(dts.data(), d_dts, nsteps * sizeof(double), cudaMemcpyDeviceToHost, st));
+    StepCtl h;
+    ACK(cudaMemcpyAsync(&h, g->ctl, sizeof h, cudaMemcpyDeviceToHost, st));
+    ACK(cudaStreamSynchronize(st));  // the recomputation needs the dts on the host
+    if (h.status & ST_NONFINITE) return afail(COSMOS_ENONFINITE, "non-finite or non-positive time step in the forward run");
+    if (h.it != nsteps) return afail(COSMOS_ESTATE, "the forward run stopped after " + std::to_string(h.it) + " steps");
+
+    // ---- backward, one checkpoint segment at a time
+    SweepArgs fa = base_args(g);
+    fa.order = 2;
+    fa.bias = o->bias;
+    fa.lim = o->limiter;
+    fa.out.status = g->status;
+    AdjSweepParams ap;
+    ap.G = G0;
+    ap.dx = g->p.dx;
+    ap.bias = o->bias;
+    ap.gamma = g->p.gamma;
+    auto slot = [&](int q) { return seg + (size_t)q * sbytes; };
+    for (int c = nck - 1; c >= 0; c--) {
+        const int s0 = c * K, s1 = std::min(nsteps, s0 + K);
+        const int nsw = (s1 - s0) * spp;  // sweeps in the segment; their inputs go to slots 0..nsw-1
+        ACK(cudaMemcpyAsync(slot(0), ck + (size_t)c * sbytes, sbytes, cudaMemcpyDeviceToDevice, st));
+        auto sweep_of = [&](int q, int& axis, double& dt) {
+            const double d = dts[s0 + q / spp];
+            const int m = q % spp;
+            axis = spp == 3 && m == 1 ? 1 : 0;
+            dt = spp == 3 && m != 1 ? 0.5 * d : d;
+        };
+        for (int q = 0; q + 1 < nsw; q++) {  // the last sweep's output is not needed
+            int axis;
+            double dt;
+            sweep_of(q, axis, dt);
+            fa.G.axis = axis;
+            fa.ds.fixed = dt;
+            fa.ds.ffix = make_fast_coef(dt, g->p.dx);
+            fa.src = slot(q);
+            fa.dst = slot(q + 1);
+            ACK(sweep_launch(g, fa));
+        }
+        for (int q = nsw - 1; q >= 0; q--) {
+            int axis;
+            double dt;
+            sweep_of(q, axis, dt);
+            ap.G.axis = axis;
+            ap.dt = dt;
+            ap.state = slot(q);
+            ap.ubar_out = adj + (size_t)cur * abytes;
+            ap.ubar_in = adj + (size_t)(cur ^ 1) * abytes;
+            ACK(fp64 ? launch_adjoint_sweep_exact(ap, o->limiter, st) : launch_adjoint_sweep_fast(ap, o->limiter, st));
+            cur ^= 1;
+        }
+    }
+    // ---- gradient with respect to the initial primitives
+    ACK(fp64 ? launch_adjoint_grad_exact(G0, g->p.gamma, ck, adj + (size_t)cur * abytes, g->staging, st)
+             : launch_adjoint_grad_fast(G0, g->p.gamma, ck, adj + (size_t)cur * abytes, g->staging, st));
+    ACK(cudaEventRecord(sc.ev[2], st));
+    ACK(cudaMemcpyAsync(grad_prim, g->staging, ncell * 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    double lv = 0.0;
+    ACK(cudaMemcpyAsync(&lv, d_loss, sizeof lv, cudaMemcpyDeviceToHost, st));
+    ACK(cudaStreamSynchronize(st));
+    if (loss) *loss = lv;
+    if (dts_out) std::copy(dts.begin(), dts.end(), dts_out);
+    if (ms) {
+        float f = 0.f, b = 0.f;
+        ACK(cudaEventElapsedTime(&f, sc.ev[0], sc.ev[1]));
+        ACK(cudaEventElapsedTime(&b, sc.ev[1], sc.ev[2]));
+        ms[0] = f;
+        ms[1] = b;
+    }
+    return COSMOS_OK;
+}

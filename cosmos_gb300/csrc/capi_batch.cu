@@ -13,13 +13,9 @@
 
 #include "../../include/cosmos_gb300.h"
 #include "batch_kernels.cuh"
-#include "launch.h"
+#include "capi_internal.h"
 
 namespace cg {
-void set_error(const char* msg);
-void set_capturing(bool on);
-void ctx_retain(cosmos_ctx* c);
-void ctx_release(cosmos_ctx* c);
 void* batch_fast_fn(int nt, int cap, int lim);
 void* batch_exact_fn(int nt, int cap);
 }  // namespace cg

@@ -1,0 +1,43 @@
+// Internal layout of the C-ABI objects, shared by the translation units that implement them.
+#pragma once
+#include <atomic>
+
+#include "../../include/cosmos_gb300.h"
+#include "launch.h"
+
+// A context lives until cosmos_ctx_destroy has been called AND its last grid or batch is
+// destroyed: objects hold a reference, so teardown in any order never touches a freed stream.
+struct cosmos_ctx {
+    int device;
+    cudaStream_t stream;
+    std::atomic<int> refs;
+};
+
+struct cosmos_grid {
+    cosmos_ctx* ctx;
+    cosmos_params p;
+    cg::Geom G;              // geometry of the stored state (axis set per sweep)
+    size_t elem;             // bytes per stored scalar
+    void* buf[2];            // ping-pong state buffers (5 fields each)
+    int cur;                 // buffer holding the current state
+    cg::StepCtl* ctl;        // device step controller
+    double* staging;         // device AoS primitives for set/get
+    double* sums;            // field-sum output + scratch
+    int* status;             // device status word for explicit sweeps
+    // run configuration and captured one-step graphs (one per starting buffer)
+    cosmos_solve_opts run;
+    bool run_ready;
+    cudaGraphExec_t step_graph[2];
+    unsigned step_kernels;   // kernels per captured step
+};
+
+namespace cg {
+void ctx_retain(cosmos_ctx* c);
+void ctx_release(cosmos_ctx* c);
+void set_error(const char* msg);
+void set_capturing(bool on);
+// sweep arguments of a grid (geometry, physics, stream) with everything else zeroed
+SweepArgs base_args(cosmos_grid* g);
+// the sweep kernel of the grid's precision
+cudaError_t sweep_launch(cosmos_grid* g, const SweepArgs& a);
+}  // namespace cg

@@ -187,11 +187,17 @@ __global__ void dt_kernel(StepCtl* c) {
         c->dt = 0.0;
         return;
     }
-    const double smax = __longlong_as_double((long long)c->smax[c->it & 1]);
-    double dt = c->cfl * (c->dx / smax);
-    if (c->it <= 5) dt = dt * 0.2;
-    if ((c->t + dt) > c->t_final) dt = c->t_final - c->t;
+    double dt;
+    if (c->dt_fixed) {
+        dt = c->dt_fixed[c->it];
+    } else {
+        const double smax = __longlong_as_double((long long)c->smax[c->it & 1]);
+        dt = c->cfl * (c->dx / smax);
+        if (c->it <= 5) dt = dt * 0.2;
+        if ((c->t + dt) > c->t_final) dt = c->t_final - c->t;
+    }
     if (!(dt > 0.0) || !isfinite(dt)) c->status |= ST_NONFINITE;
+    if (c->dt_log) c->dt_log[c->it] = dt;
     c->dt = dt;
     c->fc[0] = make_fast_coef(dt, c->dx);
     c->fc[1] = make_fast_coef(dt * 0.5, c->dx);

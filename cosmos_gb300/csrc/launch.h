@@ -67,4 +67,17 @@ constexpr int kNumBatchShapes = 8;
 cudaError_t launch_batch_fast(const BatchLaunch& L);
 cudaError_t launch_batch_exact(const BatchLaunch& L);
 
+// ---- sweep adjoint (adjoint_kernels.cuh); _exact: FP64 primitive storage, _fast: FP32 conserved
+struct AdjSweepParams;
+cudaError_t launch_adjoint_sweep_exact(const AdjSweepParams& a, int lim, cudaStream_t st);
+cudaError_t launch_adjoint_sweep_fast(const AdjSweepParams& a, int lim, cudaStream_t st);
+cudaError_t launch_adjoint_loss_exact(const Geom& G, const void* state, const double* target, void* ubar,
+                                      double* row_sums, double* loss, cudaStream_t st);
+cudaError_t launch_adjoint_loss_fast(const Geom& G, const void* state, const double* target, void* ubar,
+                                     double* row_sums, double* loss, cudaStream_t st);
+cudaError_t launch_adjoint_grad_exact(const Geom& G, double gamma, const void* state, const void* ubar, double* grad,
+                                      cudaStream_t st);
+cudaError_t launch_adjoint_grad_fast(const Geom& G, double gamma, const void* state, const void* ubar, double* grad,
+                                     cudaStream_t st);
+
 }  // namespace cg

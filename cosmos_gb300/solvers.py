@@ -183,6 +183,27 @@ class Grid:
         check(load().cosmos_grid_field_sums(self.h, o.ctypes.data))
         return o
 
+    def adjoint(self, target, nsteps, cfl, bias, limiter, checkpoint_every=10, dts=None):
+        """Gradient of L = 1/2 sum (rho_T - target)^2 after `nsteps` SLIC steps from the current
+        state with respect to its primitives (dt of each step held fixed: `dts` if given, else the
+        CFL rule's).  Returns (loss, grad with the shape of get_prim(), dts, (forward_ms, backward_ms)).
+        The grid holds the final state afterwards."""
+        tgt = np.ascontiguousarray(target, dtype=np.float64)
+        if tgt.shape != self.shape:
+            raise ValueError(f"target must have shape {self.shape}, got {tgt.shape}")
+        o = self.opts(2, cfl, 1e300, bias, limiter, 1, nsteps)
+        grad = np.empty(self.shape + (5,), dtype=np.float64)
+        dts_out = np.empty(int(nsteps), dtype=np.float64)
+        din = None if dts is None else np.ascontiguousarray(dts, dtype=np.float64)
+        if din is not None and din.size < nsteps:
+            raise ValueError("dts must hold nsteps entries")
+        loss = ctypes.c_double()
+        ms = np.zeros(2)
+        check(load().cosmos_grid_adjoint(self.h, ctypes.byref(o), int(nsteps), int(checkpoint_every), tgt.ctypes.data,
+                                         None if din is None else din.ctypes.data, grad.ctypes.data,
+                                         ctypes.byref(loss), dts_out.ctypes.data, ms.ctypes.data))
+        return loss.value, grad, dts_out, (float(ms[0]), float(ms[1]))
+
     def amr_flags(self, tol, coarse=None, fine=None):
         nc = self.ncell
         nf = nc * (4 if len(self.shape) == 2 else 2)

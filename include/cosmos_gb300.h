@@ -187,6 +187,23 @@ int cosmos_batch_set_shape(cosmos_batch* b, int nt, int seg, int cap);
 int cosmos_batch_time_shape(cosmos_batch* b, int nt, int seg, int cap, int steps, double* ms_per_step);
 int cosmos_batch_autotune(cosmos_batch* b, const char* cache_path, int* nt, int* seg, int* cap, double* ms_per_step);
 
+/* ---- adjoint.  Reverse-mode gradient (hand-written sweep adjoints) of the scalar loss
+ *     L = 1/2 * sum over cells (rho_T - target)^2,
+ * rho_T the density after `nsteps` SLIC steps (o->order must be 2; o->bias, o->limiter used) of a
+ * Newtonian grid from its current state, with respect to that initial state's primitives.  No
+ * counterpart in the reference (it has no derivatives); it differentiates the reference's
+ * EulerSecondOrderSolver::solve / solve2D step (Solvers/EulerSecondOrderSolver.cpp:102-147) with
+ * each step's dt held fixed: the caller's dts_in[nsteps] if non-NULL, else the CFL rule's dts
+ * (o->cfl) of the forward run, which are returned in dts_out[nsteps] if non-NULL.  Checkpoints
+ * every `checkpoint_every` steps; each segment is recomputed once.  target: ny*nx doubles (row
+ * major, the grid's rows); grad_prim: 5*nx*ny doubles in the layout of cosmos_grid_set_prim;
+ * loss and ms (2 doubles: forward and backward milliseconds on the context's stream) may be NULL.
+ * On return the grid holds the final state.  FP64 grids differentiate the reference-exact FP64
+ * steps in FP64; FP32 grids the FP32 steps in FP32. */
+int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, int nsteps, int checkpoint_every,
+                        const double* target, const double* dts_in, double* grad_prim, double* loss,
+                        double* dts_out, double* ms);
+
 /* Allocation-free conservation sums.  No counterpart in the reference: it exists for callers that
  * cannot allocate device memory where they need the sums -- code recorded into a CUDA graph
  * (allocation is not allowed during stream capture), host callbacks or foreign runtimes that own

@@ -102,3 +102,22 @@ def batch_shapes(count=256, lo=128, hi=2048, seed=5):
         side = lambda: int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi))))))  # noqa: E731
         out.append((side(),) if rng.random() < 0.5 else (side(), side()))
     return out
+
+
+def smooth_state(shape, seed):
+    """Smooth periodic Newtonian state (sines of random phase), for derivative checks by finite
+    differences: no limiter branch lies within a small perturbation of most cells."""
+    rng = np.random.default_rng(seed)
+    nx = shape[-1]
+    ny = shape[0] if len(shape) == 2 else 1
+    x = (np.arange(nx) + 0.5) / nx
+    y = (np.arange(ny) + 0.5) / ny
+    X, Y = np.meshgrid(x, y)
+    ph = rng.uniform(0, 2 * np.pi, 6)
+    p = np.zeros((ny, nx, 5))
+    p[..., 0] = 1.0 + 0.3 * np.sin(2 * np.pi * X + ph[0]) * np.cos(2 * np.pi * Y + ph[1])
+    p[..., 1] = 0.3 * np.sin(2 * np.pi * (X + Y) + ph[2])
+    p[..., 2] = 0.2 * np.cos(2 * np.pi * X + ph[3]) if len(shape) == 2 else 0.0
+    p[..., 3] = 0.05 * np.sin(2 * np.pi * Y + ph[4])
+    p[..., 4] = 1.0 + 0.2 * np.cos(2 * np.pi * X + ph[5])
+    return p.reshape(tuple(shape) + (5,))

@@ -1,0 +1,47 @@
+"""The oracle's tangent-linear model (dual numbers through the FP64 restatement of the reference's
+SLIC step, fixed time steps) against central finite differences of its own forward, and its value
+part against the plain oracle sweeps: this pins the derivative that the GPU adjoint is checked
+against."""
+import numpy as np
+import pytest
+
+import cases
+
+
+def forward_loss(oracle, p, target, dx, dts, lim, bc):
+    """1/2 sum (rho_T - target)^2 from plain oracle sweeps (X(dt/2) Y(dt) X(dt/2) in 2D)."""
+    q = p.copy()
+    for dt in dts:
+        if q.ndim == 2:
+            q = oracle.sweep(0, q, 0, 2, dx, dt, 0.0, lim, 1.4, bc)
+        else:
+            q = oracle.sweep(0, q, 0, 2, dx, 0.5 * dt, 0.0, lim, 1.4, bc)
+            q = oracle.sweep(0, q, 1, 2, dx, dt, 0.0, lim, 1.4, bc)
+            q = oracle.sweep(0, q, 0, 2, dx, 0.5 * dt, 0.0, lim, 1.4, bc)
+    e = (q[..., 0] - target).ravel()
+    L = 0.0
+    for v in 0.5 * (e * e):  # cell order, like the oracle's accumulation
+        L = L + float(v)
+    return L, q
+
+
+@pytest.mark.parametrize("dims", [1, 2])
+@pytest.mark.parametrize("lim", [0, 1, 2])
+@pytest.mark.parametrize("bc", [0, 1])
+def test_oracle_tlm_matches_finite_differences(oracle, dims, lim, bc):
+    shape = (24,) if dims == 1 else (10, 12)
+    p0 = cases.smooth_state(shape, 3 + lim)
+    target = cases.smooth_state(shape, 11)[..., 0]
+    dx = 1.0 / shape[-1]
+    dts = np.full(6, 0.15 * dx)
+    L_plain, _ = forward_loss(oracle, p0, target, dx, dts, lim, bc)
+    rng = np.random.default_rng(dims * 10 + lim + 100 * bc)
+    for _ in range(3):
+        d = rng.standard_normal(p0.shape)
+        L0, dL = oracle.tlm_newton(p0, d, target, dx, dts, 0.0, lim, 1.4, bc)
+        assert L0 == L_plain  # the dual numbers' value part is the plain FP64 forward
+        h = 1e-7  # the map is piecewise smooth (limiter branches, the 1e-5 clamp): keep the step small
+        Lp, _ = oracle.tlm_newton(p0 + h * d, np.zeros_like(d), target, dx, dts, 0.0, lim, 1.4, bc)
+        Lm, _ = oracle.tlm_newton(p0 - h * d, np.zeros_like(d), target, dx, dts, 0.0, lim, 1.4, bc)
+        fd = (Lp - Lm) / (2 * h)
+        assert abs(fd - dL) <= 1e-6 * abs(dL) + 1e-10, (fd, dL)
