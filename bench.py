@@ -438,6 +438,7 @@ def run_batch(args):
     be.close()
     nbytes = cells * 5 * 8
 
+    adj = adjoint_measure(cg, ctx)
     base = None if args.no_cpu else batch_cpu_baseline(shapes, states, dxs, args.cpu_seconds)
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
@@ -461,6 +462,7 @@ def run_batch(args):
                      "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak, "peak_source": peak_kind,
                      "traffic": traffic_per_launch("batch_step_fp32"), "algorithmic_bytes_per_step": bytes_step,
                      "bytes_per_cell_update": "40 (1D), 120 (2D)"},
+        "adjoint": adj,
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
         "status": [r.status for r in res if r.status][:8],
@@ -468,6 +470,46 @@ def run_batch(args):
     if base:
         line["cpu_baseline"] = base
     print(json.dumps(line), flush=True)
+
+
+def adjoint_measure(cg, ctx, n=2048, nsteps=100, every=10):
+    """Adjoint of `nsteps` SLIC steps (checkpoint every `every`) of the loss 1/2 |rho_T - target|^2 on
+    the batch's largest grid size (n x n, FP32, seeded Riemann data, seeded target), timed against
+    its forward pass; plus a central finite-difference check of the FP64 gradient at 64 x 64."""
+    import cases
+    p0 = cases.riemann((n, n), 77)
+    rng = np.random.default_rng(78)
+    target = p0[..., 0] * (1.0 + 0.05 * rng.standard_normal((n, n)))
+    g = cg.Grid(cg.NEWTONIAN, (n, n), 1.0 / n, 1.4, cg.FP32, cg.BC_TRANSMISSIVE, ctx=ctx)
+    runs = []
+    for _ in range(3):
+        g.set_prim(p0)
+        runs.append(g.adjoint(target, nsteps, 0.9, 0.0, cg.MINBEE, checkpoint_every=every)[3])
+    g.close()
+    fwd = statistics.median(r[0] for r in runs)
+    bwd = statistics.median(r[1] for r in runs)
+    # finite differences of the FP64 forward (same fixed dts) in one seeded direction
+    m = 64
+    q0 = cases.smooth_state((m, m), 5)
+    tq = cases.smooth_state((m, m), 6)[..., 0]
+    gq = cg.Grid(cg.NEWTONIAN, (m, m), 1.0 / m, 1.4, cg.FP64, cg.BC_TRANSMISSIVE, ctx=ctx)
+    gq.set_prim(q0)
+    _, grad, dts, _ = gq.adjoint(tq, nsteps, 0.9, 0.0, cg.MINBEE, checkpoint_every=every)
+    d = np.random.default_rng(79).standard_normal(q0.shape)
+    h = 1e-7
+    ls = []
+    for sgn in (1.0, -1.0):
+        gq.set_prim(q0 + sgn * h * d)
+        ls.append(gq.adjoint(tq, nsteps, 0.9, 0.0, cg.MINBEE, checkpoint_every=every, dts=dts)[0])
+    gq.close()
+    fd = (ls[0] - ls[1]) / (2 * h)
+    an = float(np.sum(grad * d))
+    return {"grid": f"{n}x{n} FP32, seeded Riemann data", "steps": nsteps, "checkpoint_every": every,
+            "forward_ms": fwd, "backward_ms": bwd, "adjoint_over_forward": bwd / fwd,
+            "what": "backward = recomputation of each checkpoint segment + the sweep adjoints, per forward "
+                    "pass of the same steps (graph-replayed, checkpoints stored)",
+            "fd_check": {"grid": f"{m}x{m} FP64 smooth data", "steps": nsteps, "h": h,
+                         "directional_adjoint": an, "directional_fd": fd, "rel_err": abs(fd - an) / abs(an)}}
 
 
 def run_batch_reference(args):

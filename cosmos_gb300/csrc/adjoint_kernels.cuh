@@ -28,13 +28,18 @@
 
 namespace cg {
 
+// Reciprocal: approximate (about 1 ulp) in FP32, where the derivative does not need IEEE division;
+// exact in FP64.
+CG_D float adj_rcp(float x) { return __fdividef(1.0f, x); }
+CG_D double adj_rcp(double x) { return 1.0 / x; }
+
 // Newtonian flux along axis AX of a conserved state, and its transposed Jacobian.
 template <class T>
 struct AdjFlux {
     T g1;  // gamma - 1
     template <int AX>
     CG_D void flux(const T* u, T* f) const {
-        const T inv = T(1) / u[0];
+        const T inv = adj_rcp(u[0]);
         const T vn = u[1 + AX] * inv;
         const T p = g1 * (u[4] - T(0.5) * ((u[1] * u[1] + u[2] * u[2]) + u[3] * u[3]) * inv);
         f[0] = u[1 + AX];
@@ -47,7 +52,7 @@ struct AdjFlux {
     // ub += (dF/du)^T gb
     template <int AX>
     CG_D void vjp(const T* u, const T* gb, T* ub) const {
-        const T inv = T(1) / u[0];
+        const T inv = adj_rcp(u[0]);
         const T v0 = u[1] * inv, v1 = u[2] * inv, v2 = u[3] * inv;
         const T vn = AX == 0 ? v0 : v1;
         const T vv = (v0 * v0 + v1 * v1) + v2 * v2;
@@ -69,9 +74,9 @@ struct AdjFlux {
 template <class T, int LIM>
 CG_D T limiter_d(T r, T w, T& d) {
     if (r < T(0)) { d = T(0); return T(0); }
-    const T den = (T(1) - w) + (T(1) + w) * r;
-    const T xr = T(2) / den;
-    const T dxr = -T(2) * (T(1) + w) / (den * den);
+    const T iden = adj_rcp((T(1) - w) + (T(1) + w) * r);
+    const T xr = T(2) * iden;
+    const T dxr = -T(2) * (T(1) + w) * iden * iden;
     if (LIM == 0) {  // SuperBee
         if (r < T(0.5)) { d = T(2); return T(2) * r; }
         if (r < T(1)) { d = T(0); return T(1); }
@@ -81,10 +86,10 @@ CG_D T limiter_d(T r, T w, T& d) {
         if (T(2) < m) { m = T(2); d = T(0); }
         return m;
     } else if (LIM == 1) {  // van Leer
-        const T op = T(1) + r;
-        const T vl = (T(2) * r) / op;
+        const T iop = adj_rcp(T(1) + r);
+        const T vl = T(2) * r * iop;
         if (xr < vl) { d = dxr; return xr; }
-        d = T(2) / (op * op);
+        d = T(2) * iop * iop;
         return vl;
     }
     // MinBee
@@ -106,7 +111,7 @@ CG_D void adj_evolve(const AdjFlux<T>& F, const T* ul, const T* uc, const T* ur,
         const T num = fabs(dl) < T(1e-5) ? T(1e-5) : dl;
         const T den = fabs(dr) < T(1e-5) ? T(1e-5) : dr;
         T dxi;
-        const T sl = s * limiter_d<T, LIM>(num / den, w, dxi);
+        const T sl = s * limiter_d<T, LIM>(num * adj_rcp(den), w, dxi);
         UL[k] = uc[k] - T(0.5) * sl;
         UR[k] = uc[k] + T(0.5) * sl;
     }
@@ -126,7 +131,7 @@ template <class T, int AX, int LIM>
 CG_D void adj_evolve_vjp(const AdjFlux<T>& F, const T* ul, const T* uc, const T* ur, T w, T hs, const T* Ab,
                          const T* Bb, T* gl, T* gc, T* gr) {
     const T ca = T(0.5) * (T(1) + w), cb = T(0.5) * (T(1) - w);
-    T UL[5], UR[5], sv[5], xi[5], dxi[5], r[5], den[5];
+    T UL[5], UR[5], sv[5], xi[5], dxi[5], r[5], iden[5];
     bool cn[5], cd[5];
 #pragma unroll
     for (int k = 0; k < 5; k++) {
@@ -135,8 +140,8 @@ CG_D void adj_evolve_vjp(const AdjFlux<T>& F, const T* ul, const T* uc, const T*
         cn[k] = fabs(dl) < T(1e-5);
         cd[k] = fabs(dr) < T(1e-5);
         const T num = cn[k] ? T(1e-5) : dl;
-        den[k] = cd[k] ? T(1e-5) : dr;
-        r[k] = num / den[k];
+        iden[k] = adj_rcp(cd[k] ? T(1e-5) : dr);
+        r[k] = num * iden[k];
         xi[k] = limiter_d<T, LIM>(r[k], w, dxi[k]);
         const T sl = sv[k] * xi[k];
         UL[k] = uc[k] - T(0.5) * sl;
@@ -159,8 +164,8 @@ CG_D void adj_evolve_vjp(const AdjFlux<T>& F, const T* ul, const T* uc, const T*
         const T xib = slb * sv[k];
         const T sb = slb * xi[k];
         const T rb = xib * dxi[k];
-        const T dlb = ca * sb + (cn[k] ? T(0) : rb / den[k]);
-        const T drb = cb * sb - (cd[k] ? T(0) : rb * r[k] / den[k]);
+        const T dlb = ca * sb + (cn[k] ? T(0) : rb * iden[k]);
+        const T drb = cb * sb - (cd[k] ? T(0) : rb * r[k] * iden[k]);
         gl[k] = -dlb;
         gc[k] = (ULb[k] + URb[k]) + (dlb - drb);
         gr[k] = drb;
@@ -203,13 +208,18 @@ struct AdjSweepParams {
 // Transmissive mirror (exact for up to two cells out) or periodic wrap, clamped into the line for
 // the positions further out that only feed discarded halo work.
 CG_D int adj_map(int i, int n, bool per) {
-    if (per) return ((i % n) + n) % n;
+    if (per) {
+        if (i >= 0 && i < n) return i;
+        if (i < 0 && i >= -n) return i + n;
+        if (i >= n && i < 2 * n) return i - n;
+        return ((i % n) + n) % n;
+    }
     int m = i < 0 ? -1 - i : (i >= n ? 2 * n - 1 - i : i);
     return m < 0 ? 0 : (m >= n ? n - 1 : m);
 }
 
 template <class T, class S, bool PRIM, int AX, int LIM, int P, int W>
-__global__ void __launch_bounds__(P * W) adjoint_sweep_kernel(AdjSweepParams a) {
+__global__ void __launch_bounds__(P * W, (sizeof(T) == 4 ? 3 : 1)) adjoint_sweep_kernel(AdjSweepParams a) {
     constexpr int TS = P - 8;
     constexpr int NW = P * W;
     extern __shared__ __align__(16) unsigned char adj_smem[];
@@ -342,6 +352,12 @@ __global__ void __launch_bounds__(P * W) adjoint_sweep_kernel(AdjSweepParams a) 
         T acc[5];
 #pragma unroll
         for (int f = 0; f < 5; f++) acc[f] = ub_own[f];
+        if (k >= 2 && k <= n - 3) {
+            // interior (n >= 5): the right neighbour of k - 1, k itself, the left neighbour of k + 1
+            const int xl = si(along - 1), xr = si(along + 1);
+#pragma unroll
+            for (int f = 0; f < 5; f++) acc[f] += (sB[f * NW + xl] + sC[f * NW + me]) + sC[(5 + f) * NW + xr];
+        } else
 #pragma unroll
         for (int dd = -2; dd <= 2; dd++) {
             const int i = k + dd;
@@ -430,12 +446,12 @@ __global__ void adjoint_grad_kernel(Geom G, double gamma, const S* state, const 
 
 namespace cg {
 
-// Launch the sweep adjoint for one axis.  Tiles: X lines of 128 positions (120 updated cells) x 2
-// rows; Y lines of 64 positions (56 cells) x 8 columns (contiguous in memory).
+// Launch the sweep adjoint for one axis.  Tiles of 256 threads (three resident per SM in FP32): X lines of
+// 256 positions (248 updated cells); Y lines of 64 positions (56 cells) x 4 adjacent columns.
 template <class T, class S, bool PRIM, int AX, int LIM>
 cudaError_t launch_adjoint_sweep_t(const AdjSweepParams& a, cudaStream_t st) {
-    constexpr int P = AX == 0 ? 128 : 64;
-    constexpr int W = AX == 0 ? 2 : 8;
+    constexpr int P = AX == 0 ? 256 : 64;
+    constexpr int W = AX == 0 ? 1 : 4;
     constexpr int TS = P - 8;
     const size_t smem = (size_t)30 * P * W * sizeof(T);
     auto kern = adjoint_sweep_kernel<T, S, PRIM, AX, LIM, P, W>;

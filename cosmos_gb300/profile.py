@@ -2,10 +2,15 @@
 
     python -m cosmos_gb300.profile --kernel sweep --n 4096 --precision fp32 --axis 0 --launches 3
     python -m cosmos_gb300.profile --kernel step --n 4096 --precision fp32 --launches 4
+    python -m cosmos_gb300.profile --kernel adjoint --n 1024 --precision fp32 --launches 2
+    python -m cosmos_gb300.profile --kernel batch --grids 64 --launches 2
 
 Creates one grid of the config-2 problem (four-quadrant data, periodic, MinBee) and launches the
 requested kernels a few times, so that a profiler can capture exactly those launches on a
-bounded device footprint (two state buffers plus one staging buffer).
+bounded device footprint (two state buffers plus one staging buffer).  `adjoint` runs the
+gradient of `launches` SLIC steps (checkpoint every step: launches X and Y sweep adjoints per
+step); `batch` runs `launches` chunks of 10 steps of the first `grids` grids of the batched
+workload (256 grids, sides log-uniform in [128, 2048]).
 """
 import argparse
 import os
@@ -16,7 +21,8 @@ import numpy as np
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", choices=["sweep", "step", "rk"], default="sweep")
+    ap.add_argument("--kernel", choices=["sweep", "step", "rk", "adjoint", "batch"], default="sweep")
+    ap.add_argument("--grids", type=int, default=64)
     ap.add_argument("--system", type=int, default=0)
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
     ap.add_argument("--n", type=int, default=4096)
@@ -27,6 +33,20 @@ def main():
     sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
     import cosmos_gb300 as cg
 
+    if a.kernel == "batch":
+        sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests"))
+        import cases
+        shapes = cases.batch_shapes()[:a.grids]
+        b = cg.Batch(shapes, [1.0 / sh[-1] for sh in shapes], 1.4, cg.FP32, cg.BC_TRANSMISSIVE)
+        for k, sh in enumerate(shapes):
+            b.set_prim(k, cases.riemann(sh, 1000 + k))
+        b.run_begin(0.9, 1e30, 0.0, cg.MINBEE)
+        b.set_shape(128, 64, 1)
+        b.run_steps(10 * a.launches)
+        b.run_end()
+        b.ctx.synchronize()
+        print(f"ok: {a.launches} x batch chunk ({len(shapes)} grids, {b.cells} cells)")
+        return
     n = a.n
     rng = np.random.default_rng(2)
     q = np.zeros((4, 5))
@@ -45,6 +65,9 @@ def main():
     if a.kernel == "sweep":
         for _ in range(a.launches):
             g.sweep(a.axis, a.order, dt, 0.0, cg.MINBEE)
+    elif a.kernel == "adjoint":
+        tgt = s[..., 0] * 0.9
+        g.adjoint(tgt, a.launches, 0.8, 0.0, cg.MINBEE, checkpoint_every=1)
     elif a.kernel == "rk":
         for _ in range(a.launches):
             g.rk_source(dt, 0.0, 1)
