@@ -528,10 +528,185 @@ def run_batch_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- SR (config 3) and GR (config 4)
+SR_WORKLOAD = "config3: 2D special-relativistic Euler (gamma 5/3), SLIC MinBee, CFL 0.9, 2048x2048 on the periodic " \
+              "unit square, Kelvin-Helmholtz shear layers (vx = +-0.5 tanh profile, rho in {1, 2}, p = 1, " \
+              "vy = 0.01 sin(4 pi x + phase), phase seed 3; Lorentz factor <= 1.16); 200 steps"
+GR_WORKLOAD = "config4: 2D black-hole Euler in Kerr-Schild Schwarzschild spacetime (M = 1), SLIC van Leer + " \
+              "RK4 source (BlackHoleEulerForcingSolver, one subcycle), CFL 0.9, 1024x1024 on [-10, 10]^2 " \
+              "(dx = 20/1024, hole at (10, 10) of the grid's coordinates), excision r <= 2M, rho = 1 with 1% " \
+              "log-normal noise (seed 4), p = 0.01, transmissive; 100 steps"
+
+
+def gr_state(n, seed=4):
+    rng = np.random.default_rng(seed)
+    s = np.zeros((n, n, 5))
+    s[..., 0] = np.exp(0.01 * rng.standard_normal((n, n)))
+    s[..., 4] = 0.01
+    return s
+
+
+def grid_problem(kind, n):
+    """(system, state, dx, gamma, boundary, limiter, black hole, subcycles)"""
+    import cases
+    if kind == "sr":
+        return 1, cases.kelvin_helmholtz(n, 3), 1.0 / n, 5.0 / 3.0, 1, 2, None, 1
+    return 2, gr_state(n), 20.0 / n, 5.0 / 3.0, 0, 1, (1.0, 0.0, 10.0, 10.0, 0.0), 1
+
+
+def grid_cpu_baseline(kind, n, seconds):
+    """The CPU oracle (FP64 restatement of the reference, line-parallel on all host cores) on the
+    full-size grid: whole steps until `seconds` have passed (at least one)."""
+    from oracle.pyoracle import Oracle
+    O = Oracle()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    system, s, dx, gam, bc, lim, bh, sub = grid_problem(kind, n)
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        s, k, _, _ = O.solve(system, s, 2, dx, 0.9, 1e9, 0.0, lim, gam, bc, subcycles=sub, bh=bh, max_steps=1)
+        steps += k
+        el = time.perf_counter() - t0
+        if el >= seconds or steps >= 20:
+            break
+    return {"value": steps * n * n / el, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"{steps} full {n}x{n} steps of the FP64 oracle (bit-identical restatement of the reference) "
+                      f"in {el:.1f} s on {cores} host threads"}
+
+
+def run_grid(args, kind):
+    """One SR or GR grid: FP32 (SR) or FP64 (GR) steps resident in HBM, e2e through the C ABI with
+    host buffers, the FP64 path and the FP32-vs-FP64 density error (SR)."""
+    import torch
+    import cosmos_gb300 as cg
+    _, _, local = dist_env()
+    torch.cuda.set_device(local)
+    L = cg.load()
+    ctx = cg.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    n = args.n if args.n != 4096 else (2048 if kind == "sr" else 1024)
+    system, s0, dx, gam, bc, lim, bh, sub = grid_problem(kind, n)
+    cells = n * n
+    bhs = cg.BlackHoleSpacetime(*bh) if bh else None
+    prec = cg.FP32 if kind == "sr" else cg.FP64
+
+    def timed(fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            fn()
+            b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    def make(precision, above=2.0):
+        g = cg.Grid(system, (n, n), dx, gam, precision, bc, bhs, ctx=ctx, sr_c2p64_above=above)
+        g.set_prim(s0)
+        g.run_begin(2, 0.9, 1e30, 0.0, lim, subcycles=sub)
+        return g
+
+    steps = args.steps if args.steps != 200 or kind == "sr" else 100
+    g = make(prec)
+    g.run_steps(args.warmup)
+    launches0 = L.cosmos_kernel_launches()
+    with Clocks(local) as clk:
+        ms = timed(lambda: g.run_steps(steps)) / steps
+    launches = L.cosmos_kernel_launches() - launches0
+    r = g.run_end()
+    g.close()
+    value = cells / (ms * 1e-3)
+    extra = {}
+    nerr = 10
+    if kind == "sr":
+        # FP32 with the FP64 Newton stage in every primitive recovery
+        ga = make(cg.FP32, 0.0)
+        ga.run_steps(args.warmup)
+        ms_a = timed(lambda: ga.run_steps(steps)) / steps
+        ga.close()
+        # the FP64 (reference-exact) path and the density errors after nerr steps
+        g64 = make(cg.FP64)
+        ms64 = timed(lambda: g64.run_steps(nerr)) / nerr
+        rho64 = g64.get_prim()[..., 0]
+        g64.close()
+        errs = {}
+        for tag, above in (("fp32", 2.0), ("fp32_c2p64_always", 0.0)):
+            gg = make(cg.FP32, above)
+            gg.run_steps(nerr)
+            rr = gg.get_prim()[..., 0]
+            gg.close()
+            errs[tag] = float(np.abs(rr - rho64).mean() / np.abs(rho64).mean())
+        extra = {"fp64": {"value": cells / (ms64 * 1e-3), "ms_per_step": ms64, "steps": nerr,
+                          "path": "plain FP64, bit-identical to the reference"},
+                 "fp32_c2p64_always": {"value": cells / (ms_a * 1e-3), "ms_per_step": ms_a,
+                                       "what": "FP32 with the FP64 Newton stage in every primitive recovery"},
+                 "l1_rho_vs_fp64": errs, "l1_steps": nerr, "fp32_over_fp64": ms64 / ms}
+    # e2e: per step, host primitives -> device, one step, state -> host (pinned buffers)
+    host = torch.empty((n, n, 5), dtype=torch.float64, pin_memory=True)
+    host.numpy()[...] = s0
+    ge = make(prec)
+    nbytes = cells * 5 * 8
+
+    def e2e_step():
+        cg._lib.check(L.cosmos_grid_set_prim(ge.h, host.data_ptr(), cells * 5))
+        ge.run_steps(1)
+        cg._lib.check(L.cosmos_grid_get_prim(ge.h, host.data_ptr(), cells * 5))
+    e2e_step()
+    e2e_steps = 3
+    e2e_ms = timed(lambda: [e2e_step() for _ in range(e2e_steps)]) / e2e_steps
+    ge.close()
+    peak, peak_kind = peaks()
+    word = 4 if prec == cg.FP32 else 8
+    bpc = (30 if kind == "sr" else 50) * word  # 3 sweeps x 10 words (+ 2 RK source passes for GR)
+    gbs = cells * bpc / (ms * 1e-3) / 1e9
+    base = None if args.no_cpu else grid_cpu_baseline(kind, n, args.cpu_seconds)
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if prec == cg.FP32 else "f64", "data": "synthetic",
+        "config": {"workload": SR_WORKLOAD if kind == "sr" else GR_WORKLOAD, "n": n, "cells": cells,
+                   "precision": "fp32 bulk; primitive recovery finishes in FP64 for W > 2 or when the FP32 "
+                                "Newton iteration does not converge" if kind == "sr"
+                   else "fp64 (reference-exact)",
+                   "l2": f"state {cells * 10 * word / 1e6:.0f} MB (two buffers) > 129 MB L2 (no flush needed)"
+                   if cells * 10 * word > 129e6 else "state fits in L2",
+                   "device_dt": True, "graph_replay": True, "steps_completed": r.steps},
+        **extra,
+        "e2e": {"value": cells / (e2e_ms * 1e-3), "unit": METRIC, "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms, "steps": e2e_steps,
+                "what": "per step: pinned host AoS FP64 primitives -> device, one step, state -> host"},
+        "roofline": {"bound": "hbm", "kernel": "whole step (X, Y, X sweeps" + (", RK source" if kind == "gr" else "") + ")",
+                     "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak, "peak_source": peak_kind,
+                     "traffic": None, "bytes_per_cell_update": bpc,
+                     "note": "compute-bound: FP64 primitive recovery" + (" and metric" if kind == "gr" else "")},
+        "clocks": clk.summary(), "gpu_launches": int(launches), "status": r.status,
+    }
+    if base:
+        line["cpu_baseline"] = base
+    print(json.dumps(line), flush=True)
+
+
+def run_grid_reference(args, kind):
+    rank, _, _ = dist_env()
+    if rank != 0:
+        return
+    n = args.n if args.n != 4096 else (2048 if kind == "sr" else 1024)
+    base = grid_cpu_baseline(kind, n, max(8.0, 2.0 * args.steps))
+    line = {"metric": METRIC, "value": base["value"], "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": n * n / base["value"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": SR_WORKLOAD if kind == "sr" else GR_WORKLOAD, "n": n},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="grid", choices=["grid", "batch"],
-                    help="grid: one 4096^2 grid (default); batch: 256 uneven grids in one persistent launch")
+    ap.add_argument("--workload", default="grid", choices=["grid", "batch", "sr", "gr"],
+                    help="grid: one 4096^2 Newtonian grid (default); batch: 256 uneven grids in one persistent "
+                         "launch; sr: 2048^2 special-relativistic Kelvin-Helmholtz; gr: 1024^2 black-hole accretion")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
@@ -545,6 +720,8 @@ def main():
         args.warmup = 3
     if args.workload == "batch":
         run_batch_reference(args) if args.impl == "reference" else run_batch(args)
+    elif args.workload in ("sr", "gr"):
+        run_grid_reference(args, args.workload) if args.impl == "reference" else run_grid(args, args.workload)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -21,7 +21,8 @@ class Params(ctypes.Structure):
     _fields_ = [("system", ctypes.c_int), ("dims", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int),
                 ("precision", ctypes.c_int), ("boundary", ctypes.c_int), ("gamma", ctypes.c_double),
                 ("dx", ctypes.c_double), ("bh_mass", ctypes.c_double), ("bh_spin", ctypes.c_double),
-                ("bh_x", ctypes.c_double), ("bh_y", ctypes.c_double), ("bh_z", ctypes.c_double)]
+                ("bh_x", ctypes.c_double), ("bh_y", ctypes.c_double), ("bh_z", ctypes.c_double),
+                ("sr_c2p64_above", ctypes.c_double)]
 
 
 class SolveOpts(ctypes.Structure):

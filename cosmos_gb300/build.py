@@ -28,6 +28,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relax
 UNITS = {
     "kernels_exact.cu": ["--fmad=false"],
     "kernels_fast.cu": [],
+    "kernels_sr_fast.cu": [],
     "kernels_batch_fast.cu": [],
     "kernels_batch_exact.cu": ["--fmad=false"],
     "kernels_adjoint.cu": ["--fmad=false"],

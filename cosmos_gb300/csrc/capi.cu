@@ -71,6 +71,7 @@ SweepArgs base_args(cosmos_grid* g) {
     a.dx = g->p.dx;
     a.gamma = g->p.gamma;
     a.bh[0] = g->p.bh_mass; a.bh[1] = g->p.bh_spin; a.bh[2] = g->p.bh_x; a.bh[3] = g->p.bh_y; a.bh[4] = g->p.bh_z;
+    a.c2p64_above = g->p.sr_c2p64_above;
     a.stream = g->ctx->stream;
     return a;
 }
@@ -97,7 +98,7 @@ bool valid_params(const cosmos_params* p, std::string& why) {
     if (!(p->dx > 0.0)) { why = "dx must be positive"; return false; }
     if (!(p->gamma > 1.0)) { why = "gamma must exceed 1"; return false; }
     if (p->system == COSMOS_GR && p->boundary != COSMOS_BC_TRANSMISSIVE) { why = "the GR system supports transmissive boundaries only"; return false; }
-    if (p->precision == COSMOS_FP32 && p->system != COSMOS_NEWTONIAN) { why = "FP32 storage is provided for the Newtonian system"; return false; }
+    if (p->precision == COSMOS_FP32 && p->system == COSMOS_GR) { why = "FP32 storage is provided for the Newtonian and SR systems"; return false; }
     return true;
 }
 
@@ -193,6 +194,7 @@ void cosmos_params_default(cosmos_params* p) {
     p->bh_x = 0.5;
     p->bh_y = 0.5;
     p->bh_z = 0.0;
+    p->sr_c2p64_above = 2.0;  // SR FP32: primitive recovery finishes in FP64 above Lorentz factor 2
 }
 
 void cosmos_solve_opts_default(cosmos_solve_opts* o) {

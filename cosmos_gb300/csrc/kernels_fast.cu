@@ -1,4 +1,4 @@
-// FP32 bulk kernels (Newtonian system): conserved SoA float storage, FMA contraction on.
+// FP32 bulk kernels (Newtonian system; the SR system's live in kernels_sr_fast.cu): conserved SoA float storage, FMA contraction on.
 #include "launch.h"
 #include "policies.cuh"
 
@@ -43,6 +43,7 @@ void run_fast_lim(const SweepArgs& a) {
 }  // namespace
 
 cudaError_t launch_sweep_fast(const SweepArgs& a) {
+    if (a.system == 1) return launch_sweep_sr_fast(a);
     if (a.system != 0) return cudaErrorNotSupported;
     const bool masked = a.out.mask != nullptr;
     if (a.G.axis == 0) masked ? run_fast_lim<0, true>(a) : run_fast_lim<0, false>(a);
@@ -52,6 +53,7 @@ cudaError_t launch_sweep_fast(const SweepArgs& a) {
 }
 
 cudaError_t launch_wavespeed_fast(const SweepArgs& a, unsigned long long* slot) {
+    if (a.system == 1) return launch_wavespeed_sr_fast(a, slot);
     if (a.system != 0) return cudaErrorNotSupported;
     constexpr int NT = 256;
     SweepArgs b = a;
@@ -96,12 +98,14 @@ static int grid_for(size_t n) {
     return (int)(b > 152 * 32 ? 152 * 32 : (b ? b : 1));
 }
 cudaError_t launch_prim_in_fast(const double* aos, void* soa, const Geom& G, int system, double gamma, cudaStream_t st) {
+    if (system == 1) return launch_prim_in_sr_fast(aos, soa, G, gamma, st);
     if (system != 0) return cudaErrorNotSupported;
     prim_in_fast_kernel<<<grid_for((size_t)G.nx * G.ny), 256, 0, st>>>(aos, (float*)soa, G, gamma);
     count_launch();
     return cudaGetLastError();
 }
 cudaError_t launch_prim_out_fast(const void* soa, double* aos, const Geom& G, int system, double gamma, cudaStream_t st) {
+    if (system == 1) return launch_prim_out_sr_fast(soa, aos, G, gamma, st);
     if (system != 0) return cudaErrorNotSupported;
     prim_out_fast_kernel<<<grid_for((size_t)G.nx * G.ny), 256, 0, st>>>((const float*)soa, aos, G, gamma);
     count_launch();

@@ -15,6 +15,7 @@ struct SweepArgs {
     double dx, bias, gamma;
     int lim;
     double bh[5];  // mass, spin, x, y, z
+    double c2p64_above;  // SR FP32: Lorentz factor above which primitive recovery finishes in FP64 (<= 0: always)
     const void* src;
     void* dst;
     DtSrc ds;
@@ -43,6 +44,13 @@ cudaError_t launch_prim_in_fast(const double* aos, void* soa, const Geom& G, int
                                 cudaStream_t st);
 cudaError_t launch_prim_out_fast(const void* soa, double* aos, const Geom& G, int system, double gamma,
                                  cudaStream_t st);
+
+// FP32 bulk path of the special-relativistic system (kernels_sr_fast.cu); reached through the
+// launch_*_fast functions above for system 1
+cudaError_t launch_sweep_sr_fast(const SweepArgs& a);
+cudaError_t launch_wavespeed_sr_fast(const SweepArgs& a, unsigned long long* slot);
+cudaError_t launch_prim_in_sr_fast(const double* aos, void* soa, const Geom& G, double gamma, cudaStream_t st);
+cudaError_t launch_prim_out_sr_fast(const void* soa, double* aos, const Geom& G, double gamma, cudaStream_t st);
 
 // device-side sums for conservation checks (compensated, FP64 accumulation)
 cudaError_t launch_field_sums(const void* soa, const Geom& G, int precision, double* out5, cudaStream_t st);

@@ -2,6 +2,7 @@
 #pragma once
 #include "physics_exact.cuh"
 #include "physics_fast.cuh"
+#include "physics_sr_fast.cuh"
 #include "sweep_kernels.cuh"
 
 namespace cg {
@@ -190,6 +191,79 @@ struct NewtonFastPolicy {
     CG_D float wavespeed(const Cell& c, int, int) const { return nf_wavespeed(P, c.v, dims); }
     CG_D void flush_status(int*) const {}
 };
+
+// FP32 bulk policy of the special-relativistic system (physics_sr_fast.cuh): the sweep structure
+// of NewtonFastPolicy with the relativistic flux, whose primitive recovery ends in FP64.
+template <int AXIS, int LIM, bool MASKED>
+struct SRFastPolicy {
+    using S = float;
+    using X = float;
+    using W = float;
+    using Cell = V5<float>;
+    using Face = V5<float>;
+    using Coef = FastCoef;
+    static constexpr bool kShared = true;
+    static constexpr bool kMasked = MASKED;
+    static constexpr bool kHasDx = false;
+    NewtonFastParams NP;  // limiter and bias factors
+    SRFastParams P;
+    LineMap lm;
+    int dims;
+    float dtdx, half_dtdx, q_dxdt;
+    int flags;  // bit 0: a primitive recovery did not converge
+
+    CG_D Coef make_coef(const DtSrc& ds, double) const { return ds.fast_coef(); }
+    CG_D void use_coef(const Coef& c) {
+        dtdx = c.dtdx;
+        half_dtdx = c.half_dtdx;
+        q_dxdt = c.q_dxdt;
+    }
+    CG_D void recon(const Cell& l, const Cell& m, const Cell& r, int, int, Face& L, Face& R) {
+        sr_recon_fast<AXIS, LIM>(P, NP, l.v, m.v, r.v, half_dtdx, L.v, R.v, &flags);
+    }
+    CG_D void recon_side(const Cell&, const Cell&, const Cell&, int, int, int, Face&) const {}
+    CG_D void face_of(const Cell& c, Face& f) const { f = c; }
+    CG_D void flux(const Face& L, const Face& R, int, int, V5<float>& F) {
+        sr_force_fast<AXIS>(P, L.v, R.v, half_dtdx, q_dxdt, F.v, &flags);
+    }
+    CG_D Cell update(const Cell& c, const V5<float>& FL, const V5<float>& FR, int, int) const {
+        Cell o;
+#pragma unroll
+        for (int f = 0; f < 5; f++) o.v[f] = fmaf(dtdx, FL.v[f] - FR.v[f], c.v[f]);
+        return o;
+    }
+    CG_D bool active(int line, int k, const unsigned char* mask) const {
+        return MASKED ? lm.mask_on(mask, line, k) : true;
+    }
+    CG_D float wavespeed(const Cell& c, int, int) { return sr_wavespeed_fast(P, c.v, dims, &flags); }
+    CG_D void flush_status(int* st) const {
+        if (st && flags) atomicOr(st, ST_NEWTON_CAP);
+    }
+};
+
+template <int AXIS, int LIM, bool MASKED>
+inline SRFastPolicy<AXIS, LIM, MASKED> make_sr_fast(double gamma, double bias, int nx, int dims, double c2p64_above) {
+    SRFastPolicy<AXIS, LIM, MASKED> p;
+    const float w = (float)bias;
+    p.NP.g1 = p.NP.hg1 = p.NP.gam = 0.0f;
+    p.NP.wa = 0.5f * (1.0f + w);
+    p.NP.wb = 0.5f * (1.0f - w);
+    p.NP.hom = 0.5f * (1.0f - w);
+    p.NP.hop = 0.5f * (1.0f + w);
+    p.P.wa = p.NP.wa;
+    p.P.wb = p.NP.wb;
+    p.P.hom = p.NP.hom;
+    p.P.hop = p.NP.hop;
+    p.P.gf = (float)gamma;
+    p.P.g = gamma;
+    p.P.c2p64_above = c2p64_above;
+    p.lm.axis = AXIS;
+    p.lm.nx = nx;
+    p.dims = dims;
+    p.dtdx = p.half_dtdx = p.q_dxdt = 0.0f;
+    p.flags = 0;
+    return p;
+}
 
 template <int AXIS, int LIM, bool MASKED>
 inline NewtonFastPolicy<AXIS, LIM, MASKED> make_newton_fast(double gamma, double bias, int nx, int dims) {

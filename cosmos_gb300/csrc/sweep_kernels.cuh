@@ -421,6 +421,7 @@ __global__ void __launch_bounds__(NT) wavespeed_kernel(Pol pol, Geom G, const ty
         w = (ws > w) ? ws : w;
     }
     block_max_to<NT>(out.slot(), w);
+    pol.flush_status(out.status);
 }
 
 }  // namespace cg

@@ -102,10 +102,11 @@ class Grid:
     """A device-resident grid (cosmos_grid)."""
 
     def __init__(self, system, shape, dx, gamma, precision=FP64, boundary=BC_TRANSMISSIVE, black_hole=None,
-                 ctx=None):
+                 ctx=None, sr_c2p64_above=2.0):
         self.ctx = ctx or default_context()
         p = Params()
         load().cosmos_params_default(ctypes.byref(p))
+        p.sr_c2p64_above = float(sr_c2p64_above)
         p.system = system
         if len(shape) == 1:
             p.dims, p.nx, p.ny = 1, shape[0], 1

@@ -62,6 +62,11 @@ typedef struct cosmos_params {
     double gamma;
     double dx;
     double bh_mass, bh_spin, bh_x, bh_y, bh_z;
+    /* SR system with COSMOS_FP32 storage: each conserved-to-primitive Newton solve iterates in
+     * FP32, then finishes in FP64 (to the reference's 1e-8 step tolerance) when the state's
+     * Lorentz factor exceeds this value or the FP32 iteration did not converge; <= 0 finishes
+     * every solve in FP64.  Default 2. */
+    double sr_c2p64_above;
 } cosmos_params;
 
 /* Solver options: the reference's solve() arguments (CFLCoefficient, finalTime, bias,

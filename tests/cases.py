@@ -29,6 +29,18 @@ def sr_state(rng, shape):
     return p
 
 
+def sr_mild_state(rng, shape):
+    """SR states with moderate cell-to-cell jumps: every slope-extrapolated state stays physical
+    (positive pressure, (tau + D)^2 > |S|^2) under all three limiters."""
+    p = np.zeros(tuple(shape) + (5,))
+    p[..., 0] = rng.uniform(0.8, 1.25, shape)
+    p[..., 1] = rng.uniform(-0.3, 0.3, shape)
+    p[..., 2] = rng.uniform(-0.3, 0.3, shape)
+    p[..., 3] = rng.uniform(-0.05, 0.05, shape)
+    p[..., 4] = rng.uniform(0.8, 1.25, shape)
+    return p
+
+
 def gr_state(rng, shape):
     p = np.zeros(tuple(shape) + (5,))
     p[..., 0] = rng.uniform(0.5, 1.5, shape)
@@ -121,3 +133,22 @@ def smooth_state(shape, seed):
     p[..., 3] = 0.05 * np.sin(2 * np.pi * Y + ph[4])
     p[..., 4] = 1.0 + 0.2 * np.cos(2 * np.pi * X + ph[5])
     return p.reshape(tuple(shape) + (5,))
+
+
+def kelvin_helmholtz(n, seed, width=0.01, amp=0.01, modes=2):
+    """Special-relativistic Kelvin-Helmholtz shear layers on the periodic unit square: a band
+    0.25 < y < 0.75 with vx = +0.5 and rho = 2 inside, vx = -0.5 and rho = 1 outside, joined by
+    tanh profiles of the given width; p = 1; vy = amp * sin(2 pi modes x + phase), phase by seed.
+    The Lorentz factor stays below 1.16."""
+    rng = np.random.default_rng(seed)
+    phase = rng.uniform(0.0, 2.0 * np.pi)
+    x = (np.arange(n) + 0.5) / n
+    y = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(x, y)
+    s = np.tanh((Y - 0.25) / width) - np.tanh((Y - 0.75) / width) - 1.0
+    p = np.zeros((n, n, 5))
+    p[..., 0] = 1.5 + 0.5 * s
+    p[..., 1] = 0.5 * s
+    p[..., 2] = amp * np.sin(2.0 * np.pi * modes * X + phase)
+    p[..., 4] = 1.0
+    return p
