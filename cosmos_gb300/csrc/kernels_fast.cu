@@ -1,6 +1,7 @@
 // FP32 bulk kernels (Newtonian system; the SR system's live in kernels_sr_fast.cu): conserved SoA float storage, FMA contraction on.
 #include "launch.h"
 #include "policies.cuh"
+#include "sweep_pairs.cuh"
 
 namespace cg {
 
@@ -9,6 +10,10 @@ namespace {
 constexpr int kXThreads = 256;  // X sweep tile: 256 evolutions, 255 fluxes, 254 updates
 constexpr int kYThreads = 128;
 constexpr int kYSeg = 32;
+constexpr int kXPairThreads = 32;  // one warp per block
+constexpr int kXPairSegs = 2;      // 60-cell segments per warp
+constexpr int kYPairThreads = 64;  // 128 columns per block (two per thread)
+constexpr int kYPairSeg = 32;
 
 template <int AXIS, int LIM, bool MASKED>
 NewtonFastPolicy<AXIS, LIM, MASKED> make_fast(const SweepArgs& a) {
@@ -23,9 +28,21 @@ void run_fast(const SweepArgs& a) {
     auto pol = make_fast<AXIS, LIM, MASKED>(a);
     using Pol = decltype(pol);
     if constexpr (AXIS == 0) {
+        if (a.order == 2 && !MASKED) {
+            const int segs = (G.nx + 59) / 60;
+            const int per_block = (kXPairThreads / 32) * kXPairSegs;
+            dim3 grid((segs + per_block - 1) / per_block, G.ny);
+            sweep_x_pair_kernel<LIM, kXPairThreads, kXPairSegs><<<grid, kXPairThreads, 0, a.stream>>>(
+                pol.P, G.dims, G, src, dst, a.ds, a.out);
+            return;
+        }
         dim3 grid((G.nx + kXThreads - 3) / (kXThreads - 2), G.ny);
         if (a.order == 2) sweep_x_own_kernel<Pol, 2, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
         else sweep_x_own_kernel<Pol, 1, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
+    } else if (a.order == 2 && !MASKED) {
+        dim3 grid((G.nx + 2 * kYPairThreads - 1) / (2 * kYPairThreads), (G.ny + kYPairSeg - 1) / kYPairSeg);
+        sweep_y_pair_kernel<LIM, kYPairThreads, kYPairSeg><<<grid, kYPairThreads, 0, a.stream>>>(pol.P, G.dims, G, src, dst,
+                                                                                              a.ds, a.out);
     } else {
         dim3 grid((G.nx + kYThreads - 1) / kYThreads, (G.ny + kYSeg - 1) / kYSeg);
         if (a.order == 2) sweep_y_kernel<Pol, 2, kYThreads, kYSeg><<<grid, kYThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);

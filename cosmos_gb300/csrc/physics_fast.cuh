@@ -6,6 +6,10 @@
 //  * divisions use one approximate reciprocal each (rho, the limiter ratio, the limiter bound);
 //  * the limiters are written as min/max/select chains instead of branches;
 //  * constants are folded (0.5 factors, the gradient-ratio 2).
+// Every function is generic over the lane type V: `float` (one cell per thread) or `f2` (two
+// cells per thread on Blackwell's paired FP32 instructions).  All arithmetic goes through the
+// explicitly rounded helpers below, so both lane types evaluate the same operation sequence and
+// agree to FP32 rounding.
 // The sweep axis and the limiter are template parameters, so no run-time switch remains in the
 // per-cell code.
 #pragma once
@@ -14,6 +18,40 @@
 namespace cg {
 
 CG_D float frcp(float x) { return __fdividef(1.0f, x); }
+
+// ---- lane types and their arithmetic
+struct f2 {
+    float2 v;
+};
+CG_D float splat(float s, float) { return s; }
+CG_D f2 splat(float s, f2) { return f2{make_float2(s, s)}; }
+template <class V> CG_D V splat_v(float s) { return splat(s, V{}); }
+
+CG_D float vadd(float a, float b) { return __fadd_rn(a, b); }
+CG_D float vsub(float a, float b) { return __fsub_rn(a, b); }
+CG_D float vmul(float a, float b) { return __fmul_rn(a, b); }
+CG_D float vfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+CG_D float vrcp(float a) { return __fdividef(1.0f, a); }
+CG_D float vdiv(float a, float b) { return __fdividef(a, b); }
+CG_D float vmin(float a, float b) { return fminf(a, b); }
+CG_D float vmax(float a, float b) { return fmaxf(a, b); }
+CG_D float vabs(float a) { return fabsf(a); }
+CG_D float vsqrt(float a) { return sqrtf(a); }
+CG_D float vsel_lt(float a, float b, float x, float y) { return a < b ? x : y; }  // a < b ? x : y
+
+CG_D f2 vadd(f2 a, f2 b) { return f2{__fadd2_rn(a.v, b.v)}; }
+CG_D f2 vsub(f2 a, f2 b) { return f2{__ffma2_rn(b.v, make_float2(-1.0f, -1.0f), a.v)}; }
+CG_D f2 vmul(f2 a, f2 b) { return f2{__fmul2_rn(a.v, b.v)}; }
+CG_D f2 vfma(f2 a, f2 b, f2 c) { return f2{__ffma2_rn(a.v, b.v, c.v)}; }
+CG_D f2 vrcp(f2 a) { return f2{make_float2(__fdividef(1.0f, a.v.x), __fdividef(1.0f, a.v.y))}; }
+CG_D f2 vdiv(f2 a, f2 b) { return f2{make_float2(__fdividef(a.v.x, b.v.x), __fdividef(a.v.y, b.v.y))}; }
+CG_D f2 vmin(f2 a, f2 b) { return f2{make_float2(fminf(a.v.x, b.v.x), fminf(a.v.y, b.v.y))}; }
+CG_D f2 vmax(f2 a, f2 b) { return f2{make_float2(fmaxf(a.v.x, b.v.x), fmaxf(a.v.y, b.v.y))}; }
+CG_D f2 vabs(f2 a) { return f2{make_float2(fabsf(a.v.x), fabsf(a.v.y))}; }
+CG_D f2 vsqrt(f2 a) { return f2{make_float2(sqrtf(a.v.x), sqrtf(a.v.y))}; }
+CG_D f2 vsel_lt(f2 a, f2 b, f2 x, f2 y) {
+    return f2{make_float2(a.v.x < b.v.x ? x.v.x : y.v.x, a.v.y < b.v.y ? x.v.y : y.v.y)};
+}
 
 struct NewtonFastParams {
     float g1;        // gamma - 1
@@ -24,89 +62,105 @@ struct NewtonFastParams {
 };
 
 // Euler/EulerStateVector.cpp:68-89 (x) / :96-117 (y) on a conserved state
-template <int AXIS>
-CG_D void nf_flux(const NewtonFastParams& P, const float* u, float* f) {
-    const float ir = frcp(u[0]);
-    const float vn = (AXIS == 0 ? u[1] : u[2]) * ir;
-    const float q = u[1] * u[1] + u[2] * u[2] + u[3] * u[3];
-    const float p = P.g1 * u[4] - P.hg1 * q * ir;
+template <int AXIS, class V>
+CG_D void nf_flux(const NewtonFastParams& P, const V* u, V* f) {
+    const V ir = vrcp(u[0]);
+    const V vn = vmul(AXIS == 0 ? u[1] : u[2], ir);
+    const V q = vfma(u[1], u[1], vfma(u[2], u[2], vmul(u[3], u[3])));
+    const V p = vfma(splat_v<V>(P.g1), u[4], vmul(splat_v<V>(-P.hg1), vmul(q, ir)));
     f[0] = AXIS == 0 ? u[1] : u[2];
-    f[1] = AXIS == 0 ? u[1] * vn + p : u[1] * vn;
-    f[2] = AXIS == 1 ? u[2] * vn + p : u[2] * vn;
-    f[3] = u[3] * vn;
-    f[4] = (u[4] + p) * vn;
+    f[1] = AXIS == 0 ? vfma(u[1], vn, p) : vmul(u[1], vn);
+    f[2] = AXIS == 1 ? vfma(u[2], vn, p) : vmul(u[2], vn);
+    f[3] = vmul(u[3], vn);
+    f[4] = vmul(vadd(u[4], p), vn);
 }
 
 // Solvers/SlopeLimiters.cpp:8-69 as select chains; `xi` = 2 / ((1-w) + (1+w) r)
-template <int LIM>
-CG_D float nf_limiter(const NewtonFastParams& P, float r) {
-    const float xi = frcp(P.hom + P.hop * r);
+template <int LIM, class V>
+CG_D V nf_limiter(const NewtonFastParams& P, V r) {
+    const V zero = splat_v<V>(0.0f), one = splat_v<V>(1.0f), two = splat_v<V>(2.0f);
+    const V xi = vrcp(vfma(splat_v<V>(P.hop), r, splat_v<V>(P.hom)));
     if (LIM == 0) {  // SuperBee
-        const float hi = fminf(fminf(r, xi), 2.0f);
-        const float v = r < 0.5f ? 2.0f * r : (r < 1.0f ? 1.0f : hi);
-        return r < 0.0f ? 0.0f : v;
+        const V hi = vmin(vmin(r, xi), two);
+        const V v = vsel_lt(r, splat_v<V>(0.5f), vmul(two, r), vsel_lt(r, one, one, hi));
+        return vsel_lt(r, zero, zero, v);
     } else if (LIM == 1) {  // van Leer
-        const float v = fminf(__fdividef(2.0f * r, 1.0f + r), xi);
-        return r < 0.0f ? 0.0f : v;
+        const V v = vmin(vdiv(vmul(two, r), vadd(one, r)), xi);
+        return vsel_lt(r, zero, zero, v);
     }
     // MinBee: r for 0 <= r < 1, min(1, xi) above (xi > 1 > r whenever r < 1)
-    return fmaxf(fminf(fminf(r, 1.0f), xi), 0.0f);
+    return vmax(vmin(vmin(r, one), xi), zero);
 }
 
 // Solvers/SlopeLimiters.cpp:71-101 with the +1e-5 clamps of numerator and denominator
-template <int LIM>
-CG_D void nf_slope(const NewtonFastParams& P, const float* ul, const float* uc, const float* ur, float* s) {
+template <int LIM, class V>
+CG_D void nf_slope(const NewtonFastParams& P, const V* ul, const V* uc, const V* ur, V* s) {
+    const V eps = splat_v<V>(1e-5f);
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-        const float dl = uc[k] - ul[k], dr = ur[k] - uc[k];
-        const float num = fabsf(dl) < 1e-5f ? 1e-5f : dl;
-        const float den = fabsf(dr) < 1e-5f ? 1e-5f : dr;
-        s[k] = (P.wa * dl + P.wb * dr) * nf_limiter<LIM>(P, num * frcp(den));
+        const V dl = vsub(uc[k], ul[k]), dr = vsub(ur[k], uc[k]);
+        const V num = vsel_lt(vabs(dl), eps, eps, dl);
+        const V den = vsel_lt(vabs(dr), eps, eps, dr);
+        s[k] = vmul(vfma(splat_v<V>(P.wa), dl, vmul(splat_v<V>(P.wb), dr)),
+                    nf_limiter<LIM>(P, vmul(num, vrcp(den))));
     }
 }
 
 // Half-step evolution of a cell's extrapolated states (Solvers/EulerSolvers.cpp:163-223).
 // half_dtdx = 0.5 dt/dx.  fl/fr receive the evolved left/right face states (conserved).
-template <int AXIS, int LIM>
-CG_D void nf_recon(const NewtonFastParams& P, const float* ul, const float* um, const float* ur, float half_dtdx,
-                   float* fl, float* fr) {
-    float s[5], a[5], b[5], Fa[5], Fb[5];
+template <int AXIS, int LIM, class V>
+CG_D void nf_recon(const NewtonFastParams& P, const V* ul, const V* um, const V* ur, float half_dtdx, V* fl, V* fr) {
+    V s[5], a[5], b[5], Fa[5], Fb[5];
     nf_slope<LIM>(P, ul, um, ur, s);
 #pragma unroll
-    for (int k = 0; k < 5; k++) { a[k] = fmaf(-0.5f, s[k], um[k]); b[k] = fmaf(0.5f, s[k], um[k]); }
+    for (int k = 0; k < 5; k++) {
+        a[k] = vfma(splat_v<V>(-0.5f), s[k], um[k]);
+        b[k] = vfma(splat_v<V>(0.5f), s[k], um[k]);
+    }
     nf_flux<AXIS>(P, a, Fa);
     nf_flux<AXIS>(P, b, Fb);
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-        const float ev = half_dtdx * (Fa[k] - Fb[k]);
-        fl[k] = a[k] + ev;
-        fr[k] = b[k] + ev;
+        const V ev = vmul(splat_v<V>(half_dtdx), vsub(Fa[k], Fb[k]));
+        fl[k] = vadd(a[k], ev);
+        fr[k] = vadd(b[k], ev);
     }
 }
 
 // FORCE flux (Solvers/EulerFirstOrderSolver.cpp:3-24) of conserved states L | R:
 // 0.5 (LF + RI) with LF = 0.5 (fL + fR) + 0.5 (dx/dt)(L - R), RI = F(0.5 (L + R) + 0.5 (dt/dx)(fL - fR)).
-template <int AXIS>
-CG_D void nf_force(const NewtonFastParams& P, const float* L, const float* R, float half_dtdx, float q_dxdt,
-                   float* F) {
-    float fL[5], fR[5], us[5], fs[5];
+template <int AXIS, class V>
+CG_D void nf_force(const NewtonFastParams& P, const V* L, const V* R, float half_dtdx, float q_dxdt, V* F) {
+    V fL[5], fR[5], us[5], fs[5];
     nf_flux<AXIS>(P, L, fL);
     nf_flux<AXIS>(P, R, fR);
 #pragma unroll
-    for (int k = 0; k < 5; k++) us[k] = fmaf(0.5f, L[k] + R[k], half_dtdx * (fL[k] - fR[k]));
+    for (int k = 0; k < 5; k++)
+        us[k] = vfma(splat_v<V>(0.5f), vadd(L[k], R[k]), vmul(splat_v<V>(half_dtdx), vsub(fL[k], fR[k])));
     nf_flux<AXIS>(P, us, fs);
 #pragma unroll
-    for (int k = 0; k < 5; k++) F[k] = fmaf(0.25f, fL[k] + fR[k], fmaf(q_dxdt, L[k] - R[k], 0.5f * fs[k]));
+    for (int k = 0; k < 5; k++)
+        F[k] = vfma(splat_v<V>(0.25f), vadd(fL[k], fR[k]),
+                    vfma(splat_v<V>(q_dxdt), vsub(L[k], R[k]), vmul(splat_v<V>(0.5f), fs[k])));
+}
+
+// Conservative update U + (dt/dx)(F_left - F_right)
+template <class V>
+CG_D void nf_update(float dtdx, const V* c, const V* FL, const V* FR, V* o) {
+#pragma unroll
+    for (int f = 0; f < 5; f++) o[f] = vfma(splat_v<V>(dtdx), vsub(FL[f], FR[f]), c[f]);
 }
 
 // Solvers/EulerSolvers.cpp:87-128 (2D: max(|vx|, |vy| + c) as written in the reference)
-CG_D float nf_wavespeed(const NewtonFastParams& P, const float* u, int dims) {
-    const float ir = frcp(u[0]);
-    const float vx = u[1] * ir, vy = u[2] * ir;
-    const float p = P.g1 * u[4] - P.hg1 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) * ir;
-    const float c = sqrtf(P.gam * p * ir);  // NaN for p < 0 is dropped by the max, as in the reference
-    if (dims == 1) return fabsf(vx) + c;
-    return fmaxf(fabsf(vx), fabsf(vy) + c);
+template <class V>
+CG_D V nf_wavespeed(const NewtonFastParams& P, const V* u, int dims) {
+    const V ir = vrcp(u[0]);
+    const V vx = vmul(u[1], ir), vy = vmul(u[2], ir);
+    const V q = vfma(u[1], u[1], vfma(u[2], u[2], vmul(u[3], u[3])));
+    const V p = vfma(splat_v<V>(P.g1), u[4], vmul(splat_v<V>(-P.hg1), vmul(q, ir)));
+    const V c = vsqrt(vmul(vmul(splat_v<V>(P.gam), p), ir));  // NaN for p < 0 is dropped by the max, as in the reference
+    if (dims == 1) return vadd(vabs(vx), c);
+    return vmax(vabs(vx), vadd(vabs(vy), c));
 }
 
 }  // namespace cg

@@ -181,8 +181,7 @@ struct NewtonFastPolicy {
     }
     CG_D Cell update(const Cell& c, const V5<float>& FL, const V5<float>& FR, int, int) const {
         Cell o;
-#pragma unroll
-        for (int f = 0; f < 5; f++) o.v[f] = fmaf(dtdx, FL.v[f] - FR.v[f], c.v[f]);
+        nf_update(dtdx, c.v, FL.v, FR.v, o.v);
         return o;
     }
     CG_D bool active(int line, int k, const unsigned char* mask) const {

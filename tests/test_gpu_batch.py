@@ -175,3 +175,28 @@ def test_context_outlives_its_objects(cg):
     b.run_end()
     g.close()
     b.close()
+
+
+@pytest.mark.parametrize("shape", [(37, 300), (130, 61), (700,), (2, 2), (5, 3), (64, 121)])
+@pytest.mark.parametrize("bc", [0, 1])
+@pytest.mark.parametrize("lim", [0, 1, 2])
+def test_fp32_pair_kernels_match_one_cell_kernels(cg, shape, bc, lim):
+    """Single FP32 grids sweep on cell pairs (paired FP32 instructions; X across warp lanes by
+    shuffles, Y two columns per thread), the batched launch with the one-cell tile functions.
+    Both evaluate the same explicitly rounded operation sequence; they agree to FP32 rounding
+    (a last-bit difference in an extrapolated state can flip a limiter branch in a few cells)."""
+    rng = np.random.default_rng(hash((shape, bc, lim)) % 2**32)
+    s = cases.newton_state(rng, shape)
+    dx = 1.0 / shape[-1]
+    b = cg.solvers.Batch([shape], dx, 1.4, 1, bc)
+    b.set_prim(0, s)
+    b.run_begin(0.9, 1e9, 0.0, lim, max_steps=12)
+    b.run_steps(12)
+    res = b.run_end()
+    g = cg.Grid(0, shape, dx, 1.4, 1, bc)
+    g.set_prim(s)
+    r = g.solve(2, 0.9, 1e9, 0.0, lim, max_steps=12)
+    assert res[0].steps == r.steps == 12 and abs(res[0].t - r.t) <= 1e-6 * r.t
+    got, want = b.get_prim(0), g.get_prim()
+    rel = np.abs(got - want) / (np.abs(want) + 1e-3)
+    assert np.median(rel) < 1e-6 and rel.max() < 1e-2, (np.median(rel), rel.max())
