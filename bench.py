@@ -498,7 +498,7 @@ def adjoint_measure(cg, ctx, n=2048, nsteps=100, every=10):
     gq.set_prim(q0)
     _, grad, dts, _ = gq.adjoint(tq, nsteps, 0.9, 0.0, cg.MINBEE, checkpoint_every=every)
     d = np.random.default_rng(79).standard_normal(q0.shape)
-    h = 1e-7
+    h = 1e-8  # small: the map is piecewise smooth (limiter branches), FP64 round-off stays ~1e-8
     ls = []
     for sgn in (1.0, -1.0):
         gq.set_prim(q0 + sgn * h * d)

@@ -13,6 +13,7 @@
 // launch is cooperative; every wait is bounded and reports a timeout instead of hanging.
 #pragma once
 #include "policies.cuh"
+#include "sweep_pairs.cuh"
 
 namespace cg {
 
@@ -178,6 +179,86 @@ __global__ void __launch_bounds__(NT, MINB) batch_step_kernel(PolX polx0, PolY p
                                                                  ws, sm);
                             w = wt > w ? wt : w;
                         }
+                }
+                if (ws && act) block_max_to<NT>(&ctl->smax[ctl->it & 1], w);
+            }
+            if (!grid_sync(B.bar)) return;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *B.gstep = step0 + nsteps;
+}
+
+// The pair sweeps as the batched kernel calls them (one Y column pair; one X row segment).
+template <int LIM>
+__device__ __forceinline__ float batch_y_pair(const NewtonFastParams& P, int dims, const Geom& G, const float* src,
+                                           float* dst, int j, int y0, int y1, bool act, const FastCoef& cf, bool ws) {
+    return y_pair_march<LIM>(P, dims, G, src, dst, j, y0, y1, act, cf, ws);
+}
+template <int LIM>
+__device__ __forceinline__ float batch_x_pair(const NewtonFastParams& P, int dims, const Geom& G, const float* src,
+                                           float* dst, int row, int s0, bool act, const FastCoef& cf, bool ws) {
+    Cell2 m;
+    x_pair_load(G, src, row, s0, m);
+    return x_pair_update<LIM>(P, dims, G, dst, row, s0, m, act, cf, ws);
+}
+
+// FP32 batch on cell pairs (sweep_pairs.cuh): X items are whole rows of one grid, dealt to the
+// block's warps one 60-cell segment at a time; Y items are 2 NT columns (a pair per thread) x a
+// run of rows.  Same phases, barriers and per-grid controllers as batch_step_kernel.
+template <int LIM, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) batch_pair_kernel(NewtonFastParams P, BatchDev B, int nsteps) {
+    constexpr int W = NT / 32;
+    constexpr int TSW = 60;
+    __shared__ FastCoef s_cf;
+    __shared__ int s_act;
+    const int warp = threadIdx.x >> 5;
+    const int step0 = *B.gstep;
+    for (int s = 0; s < nsteps; s++) {
+        const int p = (step0 + s) & 1;
+        for (int g = blockIdx.x * NT + threadIdx.x; g < B.ngrids; g += gridDim.x * NT) step_ctl_advance(&B.ctl[g]);
+        if (!grid_sync(B.bar)) return;
+        for (int ph = 0; ph < 3; ph++) {
+            void* b0 = p ? B.buf[1] : B.buf[0];
+            void* b1 = p ? B.buf[0] : B.buf[1];
+            const float* src = (const float*)(ph == 1 ? b1 : b0);
+            float* dst = (float*)(ph == 1 ? b0 : b1);
+            const BatchItem* items = ph == 0 ? B.items[0] : (ph == 1 ? B.items[1] : B.items[2]);
+            const int n = ph == 0 ? B.nitems[0] : (ph == 1 ? B.nitems[1] : B.nitems[2]);
+            for (int k = blockIdx.x; k < n; k += gridDim.x) {
+                const BatchItem it = items[k];
+                const BatchGrid bg = B.grids[it.g];
+                StepCtl* ctl = &B.ctl[it.g];
+                const bool one_d = bg.G.dims == 1;
+                DtSrc ds;
+                ds.ctl = ctl;
+                ds.fixed = 0.0;
+                ds.nsub = 0;
+                ds.scale = (ph == 1 || one_d) ? 1.0 : 0.5;
+                ds.fsel = (ph == 1 || one_d) ? 0 : 1;
+                const bool ws = (ph == 0 && one_d) || ph == 2;
+                __syncthreads();  // the previous item's coefficients and reduction are no longer read
+                if (threadIdx.x == 0) {
+                    double dt;
+                    s_act = ds.get(dt);
+                    if (s_act) s_cf = ds.fast_coef();
+                }
+                __syncthreads();
+                const bool act = s_act != 0;
+                const FastCoef cf = s_cf;
+                const Geom& G = bg.G;
+                const float* sg = src + bg.off;
+                float* dg = dst + bg.off;
+                float w = 0.0f;
+                if (ph == 1) {
+                    const int j = it.a + 2 * threadIdx.x;
+                    if (j < G.nx) w = batch_y_pair<LIM>(P, G.dims, G, sg, dg, j, it.b, it.c, act, cf, ws);
+                } else {
+                    const int spr = (G.nx + TSW - 1) / TSW;
+                    const int total = (it.b - it.a) * spr;
+                    for (int q = warp; q < total; q += W) {  // warp-uniform
+                        const int row = it.a + q / spr, s0 = (q % spr) * TSW;
+                        w = fmaxf(w, batch_x_pair<LIM>(P, G.dims, G, sg, dg, row, s0, act, cf, ws));
+                    }
                 }
                 if (ws && act) block_max_to<NT>(&ctl->smax[ctl->it & 1], w);
             }

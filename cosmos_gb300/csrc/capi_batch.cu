@@ -88,23 +88,26 @@ void* kernel_fn(cosmos_batch* b, int nt, int seg, int cap, int lim) {
     return b->precision == COSMOS_FP32 ? batch_fast_fn(nt, cap, lim) : batch_exact_fn(nt, cap);
 }
 
-// Work lists for a tile shape.  X items: whole rows of one grid, as many as make about 8 tiles of
-// nt - 2 cells; Y items: nt columns x seg rows.
+// Work lists for a tile shape.  FP64 (one-cell tiles): X items are whole rows of one grid, as many
+// as make about 8 tiles of nt - 2 cells; Y items nt columns x seg rows.  FP32 (cell pairs): X items
+// are whole rows making about two 60-cell segments per warp; Y items 2 nt columns x seg rows.
 int build_items(cosmos_batch* b, int nt, int seg, int cap) {
     void* fn = kernel_fn(b, nt, seg, cap, b->run.limiter);
     if (!fn) return bfail(COSMOS_EUNSUPPORTED, "batch tile shape not provided for this precision");
     std::vector<BatchItem> ph[3];
     for (int g = 0; g < (int)b->grids.size(); g++) {
         const Geom& G = b->grids[g].G;
-        const int tiles = (G.nx + nt - 3) / (nt - 2);
-        const int rows = std::max(1, 8 / tiles);
+        const bool pairs = b->precision == COSMOS_FP32;
+        const int tiles = pairs ? (G.nx + 59) / 60 : (G.nx + nt - 3) / (nt - 2);
+        const int rows = std::max(1, (pairs ? 2 * (nt / 32) : 8) / tiles);
+        const int ycols = pairs ? 2 * nt : nt;
         for (int r = 0; r < G.ny; r += rows) {
             const BatchItem it{g, r, std::min(r + rows, G.ny), 0};
             ph[0].push_back(it);
             if (G.dims == 2) ph[2].push_back(it);
         }
         if (G.dims == 2)
-            for (int j0 = 0; j0 < G.nx; j0 += nt)
+            for (int j0 = 0; j0 < G.nx; j0 += ycols)
                 for (int y0 = 0; y0 < G.ny; y0 += seg) ph[1].push_back(BatchItem{g, j0, y0, std::min(y0 + seg, G.ny)});
     }
     for (int k = 0; k < 3; k++) {

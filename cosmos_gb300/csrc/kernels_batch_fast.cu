@@ -1,4 +1,4 @@
-// Batched persistent launch, FP32 Newtonian policy (contraction on).
+// Batched persistent launch, FP32 Newtonian system on cell pairs (sweep_pairs.cuh).
 #include "batch_kernels.cuh"
 #include "launch.h"
 
@@ -8,13 +8,10 @@ namespace {
 
 template <int LIM, int NT, int CAP>
 struct FastBatch {
-    using PX = NewtonFastPolicy<0, LIM, false>;
-    using PY = NewtonFastPolicy<1, LIM, false>;
-    static constexpr int MINB = CAP ? 768 / NT : 1;
-    static void* fn() { return (void*)batch_step_kernel<PX, PY, NT, MINB>; }
+    static constexpr int MINB = CAP ? 512 / NT : 1;  // cap: at most 128 registers
+    static void* fn() { return (void*)batch_pair_kernel<LIM, NT, MINB>; }
     static cudaError_t launch(const BatchLaunch& L) {
-        PX px = make_newton_fast<0, LIM, false>(L.gamma, L.bias, 0, 2);
-        PY py = make_newton_fast<1, LIM, false>(L.gamma, L.bias, 0, 2);
+        const NewtonFastParams P = make_newton_fast<0, LIM, false>(L.gamma, L.bias, 0, 2).P;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(L.blocks);
         cfg.blockDim = dim3(NT);
@@ -24,7 +21,7 @@ struct FastBatch {
         attr[0].val.cooperative = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        return cudaLaunchKernelEx(&cfg, batch_step_kernel<PX, PY, NT, MINB>, px, py, *L.B, L.nsteps);
+        return cudaLaunchKernelEx(&cfg, batch_pair_kernel<LIM, NT, MINB>, P, *L.B, L.nsteps);
     }
 };
 

@@ -12,27 +12,17 @@ struct Cell2 {
     f2 v[5];
 };
 
-// Y sweep: one thread marches rows y0 .. y0 + SEG - 1 of columns j, j + 1 (j even) with the
-// stencil in registers, loading each row one iteration ahead; every interface flux is computed
-// once.  A lone last column (odd nx) runs in both lanes.
-template <int LIM, int NT, int SEG>
-__global__ void __launch_bounds__(NT) sweep_y_pair_kernel(NewtonFastParams P, int dims, Geom G,
-                                                          const float* __restrict__ src, float* __restrict__ dst,
-                                                          DtSrc ds, SweepOut out) {
-    __shared__ FastCoef s_coef;
-    __shared__ int s_act;
-    if (threadIdx.x == 0) {
-        double dt;
-        s_act = ds.get(dt);
-        if (s_act) s_coef = ds.fast_coef();
-    }
-    __syncthreads();
-    const bool act = s_act != 0;
-    const int j = 2 * (blockIdx.x * NT + threadIdx.x);
+// ---- device functions shared by the single-grid kernels below and the batched launch
+
+// Y march of one thread over rows [y0, y1) of columns j, j + 1 (j even, j < nx) with the stencil
+// in registers, loading each row one iteration ahead; every interface flux is computed once.  A
+// lone last column (odd nx) runs in both lanes.  Returns the thread's wavespeed maximum over its
+// updated cells when want_w (0 otherwise).
+template <int LIM>
+CG_D float y_pair_march(const NewtonFastParams& P, int dims, const Geom& G, const float* __restrict__ src,
+                        float* __restrict__ dst, int j, int y0, int y1, bool act, const FastCoef& cf, bool want_w) {
     const int n = G.ny;
-    const int y0 = blockIdx.y * SEG, y1 = min(y0 + SEG, n);
-    const bool col_ok = j < G.nx, two = j + 1 < G.nx;
-    unsigned long long* wslot = out.slot();
+    const bool two = j + 1 < G.nx;
     float w = 0.0f;
     auto ld = [&](int y, Cell2& c) {
         const size_t b = (size_t)ghost_index(y, n, G.bc) * G.pitch + j;
@@ -56,65 +46,148 @@ __global__ void __launch_bounds__(NT) sweep_y_pair_kernel(NewtonFastParams P, in
             else *p = c.v[f].v.x;
         }
     };
-    if (col_ok) {
-        if (!act) {
-            for (int y = y0; y < y1; y++) {
-                Cell2 c;
-                ld(y, c);
-                st(y, c);
-            }
-        } else {
-            const FastCoef cf = s_coef;
-            Cell2 cm2, cm1, c0, c1, c2, ahead;
-            ld(y0 - 2, cm2);
-            ld(y0 - 1, cm1);
-            ld(y0, c0);
-            ld(y0 + 1, c1);
-            ld(y0 + 2, ahead);
-            f2 Lm1[5], Rm1[5], L0[5], R0[5], Fp[5], Fn[5];
-            nf_recon<1, LIM>(P, cm2.v, cm1.v, c0.v, cf.half_dtdx, Lm1, Rm1);
-            nf_recon<1, LIM>(P, cm1.v, c0.v, c1.v, cf.half_dtdx, L0, R0);
-            nf_force<1>(P, Rm1, L0, cf.half_dtdx, cf.q_dxdt, Fp);
-            for (int y = y0; y < y1; y++) {
-                // the next row is loaded one iteration ahead, so its latency overlaps this row's work
-                c2 = ahead;
-                if (y + 1 < y1) ld(y + 3, ahead);
-                f2 L1[5], R1[5];
-                nf_recon<1, LIM>(P, c0.v, c1.v, c2.v, cf.half_dtdx, L1, R1);
-                nf_force<1>(P, R0, L1, cf.half_dtdx, cf.q_dxdt, Fn);
-                Cell2 nc;
-                nf_update(cf.dtdx, c0.v, Fp, Fn, nc.v);
-                st(y, nc);
-                if (wslot) {
-                    const f2 ws = nf_wavespeed(P, nc.v, dims);
-                    // fmaxf drops a NaN (as the one-cell kernels' `ws > w` does); a lone column's
-                    // duplicated lane repeats the same value
-                    w = fmaxf(w, fmaxf(ws.v.x, ws.v.y));
-                }
+    if (!act) {  // inactive step: keep the ping-pong buffers consistent
+        for (int y = y0; y < y1; y++) {
+            Cell2 c;
+            ld(y, c);
+            st(y, c);
+        }
+        return w;
+    }
+    Cell2 cm2, cm1, c0, c1, c2, ahead;
+    ld(y0 - 2, cm2);
+    ld(y0 - 1, cm1);
+    ld(y0, c0);
+    ld(y0 + 1, c1);
+    ld(y0 + 2, ahead);
+    f2 Lm1[5], Rm1[5], L0[5], R0[5], Fp[5], Fn[5];
+    nf_recon<1, LIM>(P, cm2.v, cm1.v, c0.v, cf.half_dtdx, Lm1, Rm1);
+    nf_recon<1, LIM>(P, cm1.v, c0.v, c1.v, cf.half_dtdx, L0, R0);
+    nf_force<1>(P, Rm1, L0, cf.half_dtdx, cf.q_dxdt, Fp);
+    for (int y = y0; y < y1; y++) {
+        // the next row is loaded one iteration ahead, so its latency overlaps this row's work
+        c2 = ahead;
+        if (y + 1 < y1) ld(y + 3, ahead);
+        f2 L1[5], R1[5];
+        nf_recon<1, LIM>(P, c0.v, c1.v, c2.v, cf.half_dtdx, L1, R1);
+        nf_force<1>(P, R0, L1, cf.half_dtdx, cf.q_dxdt, Fn);
+        Cell2 nc;
+        nf_update(cf.dtdx, c0.v, Fp, Fn, nc.v);
+        st(y, nc);
+        if (want_w) {
+            const f2 ws = nf_wavespeed(P, nc.v, dims);
+            // fmaxf drops a NaN (as the one-cell kernels' `ws > w` does); a lone column's
+            // duplicated lane repeats the same value
+            w = fmaxf(w, fmaxf(ws.v.x, ws.v.y));
+        }
 #pragma unroll
-                for (int f = 0; f < 5; f++) {
-                    Fp[f] = Fn[f];
-                    R0[f] = R1[f];
-                }
-                c0 = c1;
-                c1 = c2;
-            }
+        for (int f = 0; f < 5; f++) {
+            Fp[f] = Fn[f];
+            R0[f] = R1[f];
+        }
+        c0 = c1;
+        c1 = c2;
+    }
+    return w;
+}
+
+// X sweep on one 64-cell row segment per warp: lane t holds the cells at positions s0 - 2 + 2t and
+// s0 - 1 + 2t (s0 even).  x_pair_load fills the lane's pair (ghost positions mapped; positions
+// more than two outside the row only feed the discarded halo work and are clamped to a valid
+// ghost).
+CG_D void x_pair_load(const Geom& G, const float* __restrict__ src, int row, int s0, Cell2& m) {
+    const int lane = threadIdx.x & 31;
+    const int n = G.nx;
+    const int p0 = s0 - 2 + 2 * lane;
+    const size_t rb = (size_t)row * G.pitch;
+    if (p0 >= 0 && p0 + 1 < n) {
+#pragma unroll
+        for (int f = 0; f < 5; f++) m.v[f].v = *reinterpret_cast<const float2*>(src + f * G.fstride + rb + p0);
+    } else {
+        const int qa = ghost_index(min(p0, n + 1), n, G.bc), qb = ghost_index(min(p0 + 1, n + 1), n, G.bc);
+#pragma unroll
+        for (int f = 0; f < 5; f++) m.v[f].v = make_float2(src[f * G.fstride + rb + qa], src[f * G.fstride + rb + qb]);
+    }
+}
+
+// Neighbour cells, the next cell's left face state and the previous pair's right-face flux cross
+// lanes by warp shuffles (no shared memory, no block barrier); lanes 1..30 update and store their
+// two cells (60 per segment).  All 32 lanes call it together.  Returns the lane's wavespeed
+// maximum over its stored cells when want_w.
+template <int LIM>
+CG_D float x_pair_update(const NewtonFastParams& P, int dims, const Geom& G, float* __restrict__ dst, int row, int s0,
+                         const Cell2& m, bool act, const FastCoef& cf, bool want_w) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int n = G.nx;
+    const int p0 = s0 - 2 + 2 * lane;
+    const size_t rb = (size_t)row * G.pitch;
+    Cell2 nc = m;
+    if (act) {
+        f2 l[5], r[5];
+#pragma unroll
+        for (int f = 0; f < 5; f++) {
+            l[f].v = make_float2(__shfl_up_sync(FULL, m.v[f].v.y, 1), m.v[f].v.x);
+            r[f].v = make_float2(m.v[f].v.y, __shfl_down_sync(FULL, m.v[f].v.x, 1));
+        }
+        f2 L[5], R[5];
+        nf_recon<0, LIM>(P, l, m.v, r, cf.half_dtdx, L, R);
+        f2 Rn[5];  // left face states of the cells right of this lane's two
+#pragma unroll
+        for (int f = 0; f < 5; f++) Rn[f].v = make_float2(L[f].v.y, __shfl_down_sync(FULL, L[f].v.x, 1));
+        f2 Fr[5], Fl[5];
+        nf_force<0>(P, R, Rn, cf.half_dtdx, cf.q_dxdt, Fr);
+#pragma unroll
+        for (int f = 0; f < 5; f++) Fl[f].v = make_float2(__shfl_up_sync(FULL, Fr[f].v.y, 1), Fr[f].v.x);
+        nf_update(cf.dtdx, m.v, Fl, Fr, nc.v);
+    }
+    float w = 0.0f;
+    if (lane >= 1 && lane <= 30 && p0 < n) {
+        if (p0 + 1 < n) {
+#pragma unroll
+            for (int f = 0; f < 5; f++) *reinterpret_cast<float2*>(dst + f * G.fstride + rb + p0) = nc.v[f].v;
+        } else {
+#pragma unroll
+            for (int f = 0; f < 5; f++) dst[f * G.fstride + rb + p0] = nc.v[f].v.x;
+        }
+        if (want_w && act) {
+            const f2 ws = nf_wavespeed(P, nc.v, dims);
+            w = p0 + 1 < n ? fmaxf(ws.v.x, ws.v.y) : fmaxf(ws.v.x, 0.0f);
         }
     }
+    return w;
+}
+
+// ---- single-grid kernels
+
+// Y sweep: threads march rows [y0, y0 + SEG) of column pairs.
+template <int LIM, int NT, int SEG>
+__global__ void __launch_bounds__(NT) sweep_y_pair_kernel(NewtonFastParams P, int dims, Geom G,
+                                                          const float* __restrict__ src, float* __restrict__ dst,
+                                                          DtSrc ds, SweepOut out) {
+    __shared__ FastCoef s_coef;
+    __shared__ int s_act;
+    if (threadIdx.x == 0) {
+        double dt;
+        s_act = ds.get(dt);
+        if (s_act) s_coef = ds.fast_coef();
+    }
+    __syncthreads();
+    const bool act = s_act != 0;
+    const int j = 2 * (blockIdx.x * NT + threadIdx.x);
+    const int y0 = blockIdx.y * SEG, y1 = min(y0 + SEG, G.ny);
+    unsigned long long* wslot = out.slot();
+    float w = 0.0f;
+    if (j < G.nx) w = y_pair_march<LIM>(P, dims, G, src, dst, j, y0, y1, act, s_coef, wslot != nullptr);
     if (wslot) block_max_to<NT>(wslot, w);
 }
 
-// X sweep on row segments of 64 cells: lane t holds the cells at positions s0 - 2 + 2t and
-// s0 - 1 + 2t.  Neighbour cells, the next cell's left face state and the previous cell pair's
-// right-face flux cross lanes by warp shuffles, so no shared memory and no block barrier is used;
-// lanes 1..30 update their two cells (60 cells per segment; the two cells at each end are the
-// stencil halo).  A warp walks SEGS consecutive segments of its row, loading the next segment
+// X sweep: a warp walks SEGS consecutive 60-cell segments of its row, loading the next segment
 // while it computes the current one.
 template <int LIM, int NT, int SEGS>
 __global__ void __launch_bounds__(NT) sweep_x_pair_kernel(NewtonFastParams P, int dims, Geom G,
                                                           const float* __restrict__ src, float* __restrict__ dst,
                                                           DtSrc ds, SweepOut out) {
-    constexpr unsigned FULL = 0xffffffffu;
     constexpr int TSW = 60;
     __shared__ FastCoef s_coef;
     __shared__ int s_act;
@@ -125,68 +198,19 @@ __global__ void __launch_bounds__(NT) sweep_x_pair_kernel(NewtonFastParams P, in
     }
     __syncthreads();
     const bool act = s_act != 0;
-    const int lane = threadIdx.x & 31;
     const int seg0 = (blockIdx.x * (NT / 32) + (threadIdx.x >> 5)) * SEGS;
     const int row = blockIdx.y;
     const int n = G.nx;
-    const size_t rb = (size_t)row * G.pitch;
     unsigned long long* wslot = out.slot();
     float w = 0.0f;
-    auto ld = [&](int s0, Cell2& m) {
-        const int p0 = s0 - 2 + 2 * lane;
-        if (p0 >= 0 && p0 + 1 < n) {
-#pragma unroll
-            for (int f = 0; f < 5; f++) m.v[f].v = *reinterpret_cast<const float2*>(src + f * G.fstride + rb + p0);
-        } else {
-            // ghost positions (at most two outside the row are used; further ones only feed the
-            // discarded halo work and are clamped to a valid ghost)
-            const int qa = ghost_index(min(p0, n + 1), n, G.bc), qb = ghost_index(min(p0 + 1, n + 1), n, G.bc);
-#pragma unroll
-            for (int f = 0; f < 5; f++) m.v[f].v = make_float2(src[f * G.fstride + rb + qa], src[f * G.fstride + rb + qb]);
-        }
-    };
     Cell2 ahead;
-    if (seg0 * TSW < n) ld(seg0 * TSW, ahead);
+    if (seg0 * TSW < n) x_pair_load(G, src, row, seg0 * TSW, ahead);
     for (int k = 0; k < SEGS; k++) {
         const int s0 = (seg0 + k) * TSW;
         if (s0 >= n) break;  // warp-uniform
-        Cell2 m = ahead;
-        if (k + 1 < SEGS && s0 + TSW < n) ld(s0 + TSW, ahead);
-        const int p0 = s0 - 2 + 2 * lane;
-        const bool upd = lane >= 1 && lane <= 30;
-        Cell2 nc = m;
-        if (act) {
-            const FastCoef cf = s_coef;
-            f2 l[5], r[5];
-#pragma unroll
-            for (int f = 0; f < 5; f++) {
-                l[f].v = make_float2(__shfl_up_sync(FULL, m.v[f].v.y, 1), m.v[f].v.x);
-                r[f].v = make_float2(m.v[f].v.y, __shfl_down_sync(FULL, m.v[f].v.x, 1));
-            }
-            f2 L[5], R[5];
-            nf_recon<0, LIM>(P, l, m.v, r, cf.half_dtdx, L, R);
-            f2 Rn[5];  // left face states of the cells right of this lane's two
-#pragma unroll
-            for (int f = 0; f < 5; f++) Rn[f].v = make_float2(L[f].v.y, __shfl_down_sync(FULL, L[f].v.x, 1));
-            f2 Fr[5], Fl[5];
-            nf_force<0>(P, R, Rn, cf.half_dtdx, cf.q_dxdt, Fr);
-#pragma unroll
-            for (int f = 0; f < 5; f++) Fl[f].v = make_float2(__shfl_up_sync(FULL, Fr[f].v.y, 1), Fr[f].v.x);
-            nf_update(cf.dtdx, m.v, Fl, Fr, nc.v);
-        }
-        if (upd && p0 < n) {
-            if (p0 + 1 < n) {
-#pragma unroll
-                for (int f = 0; f < 5; f++) *reinterpret_cast<float2*>(dst + f * G.fstride + rb + p0) = nc.v[f].v;
-            } else {
-#pragma unroll
-                for (int f = 0; f < 5; f++) dst[f * G.fstride + rb + p0] = nc.v[f].v.x;
-            }
-            if (wslot && act) {
-                const f2 ws = nf_wavespeed(P, nc.v, dims);
-                w = fmaxf(w, p0 + 1 < n ? fmaxf(ws.v.x, ws.v.y) : ws.v.x);
-            }
-        }
+        const Cell2 m = ahead;
+        if (k + 1 < SEGS && s0 + TSW < n) x_pair_load(G, src, row, s0 + TSW, ahead);
+        w = fmaxf(w, x_pair_update<LIM>(P, dims, G, dst, row, s0, m, act, s_coef, wslot != nullptr));
     }
     if (wslot) block_max_to<NT>(wslot, w);
 }
