@@ -29,6 +29,7 @@ UNITS = {
     "kernels_exact.cu": ["--fmad=false"],
     "kernels_fast.cu": [],
     "kernels_sr_fast.cu": [],
+    "kernels_gr_fast.cu": [],
     "kernels_batch_fast.cu": [],
     "kernels_batch_exact.cu": ["--fmad=false"],
     "kernels_adjoint.cu": ["--fmad=false"],

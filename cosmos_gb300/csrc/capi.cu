@@ -72,6 +72,7 @@ SweepArgs base_args(cosmos_grid* g) {
     a.gamma = g->p.gamma;
     a.bh[0] = g->p.bh_mass; a.bh[1] = g->p.bh_spin; a.bh[2] = g->p.bh_x; a.bh[3] = g->p.bh_y; a.bh[4] = g->p.bh_z;
     a.c2p64_above = g->p.sr_c2p64_above;
+    a.grt = &g->grt;
     a.stream = g->ctx->stream;
     return a;
 }
@@ -98,7 +99,6 @@ bool valid_params(const cosmos_params* p, std::string& why) {
     if (!(p->dx > 0.0)) { why = "dx must be positive"; return false; }
     if (!(p->gamma > 1.0)) { why = "gamma must exceed 1"; return false; }
     if (p->system == COSMOS_GR && p->boundary != COSMOS_BC_TRANSMISSIVE) { why = "the GR system supports transmissive boundaries only"; return false; }
-    if (p->precision == COSMOS_FP32 && p->system == COSMOS_GR) { why = "FP32 storage is provided for the Newtonian and SR systems"; return false; }
     return true;
 }
 
@@ -138,7 +138,7 @@ int enqueue_step(cosmos_grid* g, int cur, int* cur_out, unsigned* nk) {
         r.ds.nsub = o.subcycles;
         r.src = g->buf[cur];
         r.dst = g->buf[cur ^ 1];
-        CK(launch_rk_source_exact(r));
+        CK(g->p.precision == COSMOS_FP64 ? launch_rk_source_exact(r) : launch_rk_source_gr_fast(r));
         cur ^= 1;
         k++;
         return COSMOS_OK;
@@ -162,7 +162,7 @@ int enqueue_step(cosmos_grid* g, int cur, int* cur_out, unsigned* nk) {
         SweepArgs w = base_args(g);
         w.src = g->buf[cur];
         w.out.ws_ctl = g->ctl;
-        CK(launch_wavespeed_exact(w, nullptr));
+        CK(g->p.precision == COSMOS_FP64 ? launch_wavespeed_exact(w, nullptr) : launch_wavespeed_gr_fast(w, nullptr));
         k++;
     }
     *nk = k;
@@ -272,6 +272,10 @@ int cosmos_grid_create(cosmos_ctx* ctx, const cosmos_params* p, cosmos_grid** ou
     if (e == cudaSuccess) e = cudaMalloc(&g->staging, ncell * 5 * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&g->sums, (8 + 152 * 4 * 5 + 8) * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&g->status, sizeof(int));
+    if (e == cudaSuccess && p->system == COSMOS_GR && p->precision == COSMOS_FP32) {
+        e = cudaMalloc(&g->gr_mem, gr_tables_bytes(g->G.nx, g->G.ny));
+        if (e == cudaSuccess) e = build_gr_tables(base_args(g), g->gr_mem, &g->grt);
+    }
     if (e == cudaSuccess) e = cudaMemsetAsync(g->buf[0], 0, bytes, ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(g->buf[1], 0, bytes, ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(g->sums, 0, (8 + 152 * 4 * 5 + 8) * sizeof(double), ctx->stream);
@@ -298,6 +302,7 @@ int cosmos_grid_destroy(cosmos_grid* g) {
     if (g->staging) cudaFree(g->staging);
     if (g->sums) cudaFree(g->sums);
     if (g->status) cudaFree(g->status);
+    if (g->gr_mem) cudaFree(g->gr_mem);
     cosmos_ctx* ctx = g->ctx;
     delete g;
     ctx_release(ctx);
@@ -311,6 +316,7 @@ int cosmos_grid_set_prim(cosmos_grid* g, const double* prim, size_t n) {
     CK(cudaSetDevice(g->ctx->device));
     CK(cudaMemcpyAsync(g->staging, prim, want * sizeof(double), cudaMemcpyHostToDevice, g->ctx->stream));
     if (g->p.precision == COSMOS_FP64) CK(launch_prim_in_exact(g->staging, g->buf[g->cur], g->G, g->ctx->stream));
+    else if (g->p.system == COSMOS_GR) CK(launch_prim_in_gr_fast(base_args(g), g->staging, g->buf[g->cur]));
     else CK(launch_prim_in_fast(g->staging, g->buf[g->cur], g->G, g->p.system, g->p.gamma, g->ctx->stream));
     return COSMOS_OK;
 }
@@ -321,6 +327,7 @@ int cosmos_grid_get_prim(cosmos_grid* g, double* prim, size_t n) {
     if (n != want) return fail(COSMOS_EINVAL, "buffer holds %zu doubles, grid needs %zu", n, want);
     CK(cudaSetDevice(g->ctx->device));
     if (g->p.precision == COSMOS_FP64) CK(launch_prim_out_exact(g->buf[g->cur], g->staging, g->G, g->ctx->stream));
+    else if (g->p.system == COSMOS_GR) CK(launch_prim_out_gr_fast(base_args(g), g->buf[g->cur], g->staging));
     else CK(launch_prim_out_fast(g->buf[g->cur], g->staging, g->G, g->p.system, g->p.gamma, g->ctx->stream));
     CK(cudaMemcpyAsync(prim, g->staging, want * sizeof(double), cudaMemcpyDeviceToHost, g->ctx->stream));
     CK(cudaStreamSynchronize(g->ctx->stream));
@@ -360,7 +367,7 @@ int cosmos_grid_rk_source(cosmos_grid* g, double dt, double bias, int limiter) {
     a.src = g->buf[g->cur];
     a.dst = g->buf[g->cur ^ 1];
     a.out.status = g->status;
-    CK(launch_rk_source_exact(a));
+    CK(g->p.precision == COSMOS_FP64 ? launch_rk_source_exact(a) : launch_rk_source_gr_fast(a));
     g->cur ^= 1;
     return COSMOS_OK;
 }
@@ -517,6 +524,8 @@ int cosmos_grid_amr_derefine(cosmos_grid* coarse, cosmos_grid* fine, double tol,
         coarse->p.dims != fine->p.dims || fine->G.nx != 2 * coarse->G.nx ||
         (coarse->p.dims == 2 && fine->G.ny != 2 * coarse->G.ny))
         return fail(COSMOS_EINVAL, "fine grid must be the 2x refinement of the coarse grid");
+    if (coarse->p.system == COSMOS_GR && coarse->p.precision == COSMOS_FP32)
+        return fail(COSMOS_EUNSUPPORTED, "derefinement of FP32 black-hole grids is not provided");
     CK(cudaSetDevice(coarse->ctx->device));
     cudaStream_t st = coarse->ctx->stream;
     CK(cudaStreamSynchronize(fine->ctx->stream));

@@ -29,6 +29,9 @@ struct cosmos_grid {
     bool run_ready;
     cudaGraphExec_t step_graph[2];
     unsigned step_kernels;   // kernels per captured step
+    // black-hole grids with FP32 storage: metric tables built once at creation
+    void* gr_mem;
+    cg::GRTables grt;
 };
 
 namespace cg {

@@ -213,8 +213,9 @@ cudaError_t launch_dt_kernel(StepCtl* ctl, cudaStream_t st) {
 }
 
 // ------------------------------------------------------------------ AMR flagging
-// Conserved state of a cell for the flag passes: FP64 storage holds primitives (converted with
-// the system's exact cons), FP32 storage holds conserved values already.
+// Conserved state of a cell for the flag passes: FP64 storage and the FP32 black-hole storage hold
+// primitives (converted with the system's exact cons), FP32 Newtonian and SR storage holds
+// conserved values already.
 struct ConsLoader {
     int system, precision;
     Geom G;
@@ -224,16 +225,18 @@ struct ConsLoader {
     GRExact gr;
     CG_D void get(int i, int j, Pt q, double* u) const {
         const size_t k = (size_t)ghost_index(i, G.ny, 0) * G.pitch + ghost_index(j, G.nx, 0);
-        if (precision == 1) {
+        if (precision == 1 && system != 2) {  // FP32 Newtonian / SR storage is conserved
             const float* s = (const float*)state;
 #pragma unroll
             for (int f = 0; f < 5; f++) u[f] = (double)s[f * G.fstride + k];
             return;
         }
-        const double* s = (const double*)state;
+        // primitives: FP64 storage, and the FP32 black-hole storage
         double p[5];
 #pragma unroll
-        for (int f = 0; f < 5; f++) p[f] = s[f * G.fstride + k];
+        for (int f = 0; f < 5; f++)
+            p[f] = precision == 1 ? (double)((const float*)state)[f * G.fstride + k]
+                                  : ((const double*)state)[f * G.fstride + k];
         cons_of(p, q, u);
     }
     CG_D void cons_of(const double* p, Pt q, double* u) const {

@@ -61,6 +61,7 @@ void run_fast_lim(const SweepArgs& a) {
 
 cudaError_t launch_sweep_fast(const SweepArgs& a) {
     if (a.system == 1) return launch_sweep_sr_fast(a);
+    if (a.system == 2) return launch_sweep_gr_fast(a);
     if (a.system != 0) return cudaErrorNotSupported;
     const bool masked = a.out.mask != nullptr;
     if (a.G.axis == 0) masked ? run_fast_lim<0, true>(a) : run_fast_lim<0, false>(a);
@@ -71,6 +72,7 @@ cudaError_t launch_sweep_fast(const SweepArgs& a) {
 
 cudaError_t launch_wavespeed_fast(const SweepArgs& a, unsigned long long* slot) {
     if (a.system == 1) return launch_wavespeed_sr_fast(a, slot);
+    if (a.system == 2) return launch_wavespeed_gr_fast(a, slot);
     if (a.system != 0) return cudaErrorNotSupported;
     constexpr int NT = 256;
     SweepArgs b = a;

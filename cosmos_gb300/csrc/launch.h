@@ -8,6 +8,20 @@
 
 namespace cg {
 
+// Metric tables of a black-hole grid with FP32 storage (physics_gr_fast.cuh), built once in FP64.
+// Centres carry a two-cell border, faces f (between cells f - 1 and f) run over [-2, n + 2].
+struct GRTables {
+    const float* center;  // kMetFields x (ny + 4) x (nx + 4), index (i + 2) (nx + 4) + (j + 2)
+    const float* xface;   // kMetFields x (ny + 4) x (nx + 5), index (i + 2) (nx + 5) + (f + 2)
+    const float* yface;   // kMetFields x (ny + 5) x (nx + 4), index (f + 2) (nx + 4) + (j + 2)
+    const float* src;     // kSrcFields x ny x nx
+    const float* ws;      // kWsFields x ny x nx
+    const unsigned char* flags;  // per cell: bit 0 sweep active (reach 2), bit 1 reach 1, bit 2 source
+                                 // step active, bit 3 CFL point excised
+    int nx, ny;
+    size_t center_stride, xface_stride, yface_stride, cell_stride;
+};
+
 struct SweepArgs {
     int system;  // 0 Newtonian, 1 SR, 2 GR
     Geom G;
@@ -15,7 +29,8 @@ struct SweepArgs {
     double dx, bias, gamma;
     int lim;
     double bh[5];  // mass, spin, x, y, z
-    double c2p64_above;  // SR FP32: Lorentz factor above which primitive recovery finishes in FP64 (<= 0: always)
+    double c2p64_above;  // SR/GR FP32: Lorentz factor above which primitive recovery finishes in FP64 (<= 0: always)
+    const GRTables* grt;  // GR FP32: the grid's metric tables
     const void* src;
     void* dst;
     DtSrc ds;
@@ -51,6 +66,15 @@ cudaError_t launch_sweep_sr_fast(const SweepArgs& a);
 cudaError_t launch_wavespeed_sr_fast(const SweepArgs& a, unsigned long long* slot);
 cudaError_t launch_prim_in_sr_fast(const double* aos, void* soa, const Geom& G, double gamma, cudaStream_t st);
 cudaError_t launch_prim_out_sr_fast(const void* soa, double* aos, const Geom& G, double gamma, cudaStream_t st);
+
+// FP32 bulk path of the black-hole system (kernels_gr_fast.cu)
+size_t gr_tables_bytes(int nx, int ny);
+cudaError_t build_gr_tables(const SweepArgs& a, void* storage, GRTables* out);
+cudaError_t launch_sweep_gr_fast(const SweepArgs& a);
+cudaError_t launch_rk_source_gr_fast(const SweepArgs& a);
+cudaError_t launch_wavespeed_gr_fast(const SweepArgs& a, unsigned long long* slot);
+cudaError_t launch_prim_in_gr_fast(const SweepArgs& a, const double* aos, void* soa);
+cudaError_t launch_prim_out_gr_fast(const SweepArgs& a, const void* soa, double* aos);
 
 // device-side sums for conservation checks (compensated, FP64 accumulation)
 cudaError_t launch_field_sums(const void* soa, const Geom& G, int precision, double* out5, cudaStream_t st);

@@ -429,29 +429,14 @@ struct GRExact {
                 K[3 * i + j] = k;
             }
     }
-    // BlackHoleEuler/BlackHoleEulerStateVector.cpp:359-510
-    CG_D void source(const double* u, Pt q, double* s) const {
-        double gm[9];
-        bh.gamma(q.x, q.y, q.z, gm);
-        double dg = det3(gm);
-        double al, be[3];
-        bh.lapse_shift(q.x, q.y, q.z, al, be);
-        C2P c = c2p(u, sqrt(dg), 1e-8);
-        double g4m[16], gi[16];
+    // The metric part of the source term at q: inverse 4-metric, centred derivatives of the lapse,
+    // shift and spatial metric (spacing h), extrinsic curvature (BlackHoleSpacetime.cpp:115-151,
+    // :230-370).
+    CG_D void source_metric(Pt q, double al, double* gi, double* da, double* db, double* dgm, double* K) const {
+        double g4m[16];
         bh.g4(q.x, q.y, q.z, g4m);
         inverse4(g4m, gi);
-        double uu[4];
-        uu[0] = c.W / al;
-        uu[1] = ((al * uu[0]) * c.vx) - (be[0] * uu[0]);
-        uu[2] = ((al * uu[0]) * c.vy) - (be[1] * uu[0]);
-        uu[3] = ((al * uu[0]) * c.vz) - (be[2] * uu[0]);
-        double T[16];
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-#pragma unroll
-            for (int j = 0; j < 4; j++) T[4 * i + j] = (((c.rho * c.h) * uu[i]) * uu[j]) + (c.p * gi[4 * i + j]);
         const double hs = 0.5 * h;
-        double da[3], db[9], dgm[27];
 #pragma unroll
         for (int d = 0; d < 3; d++) {
             Pt p1 = off(q, d, hs), p0 = off(q, d, -hs);
@@ -466,8 +451,28 @@ struct GRExact {
 #pragma unroll
             for (int k = 0; k < 9; k++) dgm[9 * d + k] = (1.0 / h) * (g1[k] - g0[k]);
         }
-        double K[9];
         Kij(q, al, K);
+    }
+    // BlackHoleEuler/BlackHoleEulerStateVector.cpp:359-510
+    CG_D void source(const double* u, Pt q, double* s) const {
+        double gm[9];
+        bh.gamma(q.x, q.y, q.z, gm);
+        double dg = det3(gm);
+        double al, be[3];
+        bh.lapse_shift(q.x, q.y, q.z, al, be);
+        C2P c = c2p(u, sqrt(dg), 1e-8);
+        double gi[16], da[3], db[9], dgm[27], K[9];
+        source_metric(q, al, gi, da, db, dgm, K);
+        double uu[4];
+        uu[0] = c.W / al;
+        uu[1] = ((al * uu[0]) * c.vx) - (be[0] * uu[0]);
+        uu[2] = ((al * uu[0]) * c.vy) - (be[1] * uu[0]);
+        uu[3] = ((al * uu[0]) * c.vz) - (be[2] * uu[0]);
+        double T[16];
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) T[4 * i + j] = (((c.rho * c.h) * uu[i]) * uu[j]) + (c.p * gi[4 * i + j]);
         double S[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
         double vc[3];
 #pragma unroll

@@ -10,7 +10,10 @@
 // below 1e-7, after which quadratic convergence has put the root within 1e-14 -- the reference's
 // |step| < 1e-8 criterion holds on the next step.  The FP64 stage runs for every solve when
 // c2p64_above <= 0; otherwise only for states whose FP32 Lorentz factor exceeds c2p64_above (or
-// whose FP32 iteration did not converge).  Primitives are then formed in FP32.
+// whose FP32 iteration did not converge).  Primitives are then formed in FP32.  The iteration caps
+// are 100 (FP32) and 64 (FP64) instead of the reference's 1000: beyond them the state has no
+// physical root (on GB300 one FP64 iteration costs as much as a whole FP32 recovery), and the
+// result is the last iterate as in the reference, flagged in the status word.
 //
 // A sweep costs five primitive recoveries per cell (the two extrapolated states of the cell, the
 // two face states and the Richtmyer state of one face), against about two dozen in the reference,
@@ -72,7 +75,9 @@ CG_D SRPrim32 sr_c2p_fast(const SRFastParams& P, const float* u, int* flags) {
         const double et = 2.0 * dcd * grd;
         double xd = x;
         bool c64 = false;
-        for (int it = 0; it < 1000; it++) {
+        // from the FP32 iterate a solvable state converges in a few steps; a state without a
+        // physical root gives up after 64 (reported through the status word)
+        for (int it = 0; it < 64; it++) {
             const double x2 = xd * xd;
             const double f = k4 * x2 * xd * (xd - et) + k2 * x2 + k1 * xd + k0;
             const double fp = k1 + 2.0 * k2 * xd + 4.0 * k4 * x2 * xd - 3.0 * et * k4 * x2;

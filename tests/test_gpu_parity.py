@@ -212,7 +212,7 @@ def test_errors_are_reported(cg):
         cg.Grid(0, (1,), 0.1, 1.4)
     assert e.value.code == 1 and "2 cells" in str(e.value)
     with pytest.raises(cg.CosmosError):
-        cg.Grid(2, (8, 8), 0.1, 5 / 3, precision=1)
+        cg.Grid(2, (8, 8), 0.1, 5 / 3, precision=1, boundary=1)  # GR: transmissive boundaries only
     g = cg.Grid(0, (8,), 0.1, 1.4)
     with pytest.raises(ValueError):
         g.set_prim(np.zeros((7, 5)))
