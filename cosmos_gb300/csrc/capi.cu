@@ -1,4 +1,5 @@
 // C-ABI implementation: contexts, grids, solver runs (device-side dt, CUDA-graph replay).
+#include <algorithm>
 #include <atomic>
 #include <climits>
 #include <cstdarg>
@@ -56,6 +57,9 @@ void ctx_release(cosmos_ctx* c) {
     if (c->refs.fetch_sub(1) != 1) return;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    cudaStreamSynchronize(c->copy);
+    for (int k = 0; k < 2; k++) cudaEventDestroy(c->ev[k]);
+    cudaStreamDestroy(c->copy);
     cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -225,6 +229,8 @@ int cosmos_ctx_create(int device, cosmos_ctx** out) {
     c->device = device;
     c->refs.store(1);
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) e = cudaEventCreateWithFlags(&c->ev[k], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         delete c;
         return fail(COSMOS_ECUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
@@ -309,15 +315,54 @@ int cosmos_grid_destroy(cosmos_grid* g) {
     return COSMOS_OK;
 }
 
+namespace {
+// Rows per chunk of a host <-> device transfer: about eight chunks, at least 64 rows each.
+int chunk_rows(const Geom& G) { return std::max(64, (G.ny + 7) / 8); }
+
+cudaError_t convert_in(cosmos_grid* g, const double* staging, void* state, const Geom& G) {
+    if (g->p.precision == COSMOS_FP64) return launch_prim_in_exact(staging, state, G, g->ctx->stream);
+    if (g->p.system == COSMOS_GR) {
+        SweepArgs a = base_args(g);
+        a.G = G;
+        return launch_prim_in_gr_fast(a, staging, state);
+    }
+    return launch_prim_in_fast(staging, state, G, g->p.system, g->p.gamma, g->ctx->stream);
+}
+cudaError_t convert_out(cosmos_grid* g, const void* state, double* staging, const Geom& G) {
+    if (g->p.precision == COSMOS_FP64) return launch_prim_out_exact(state, staging, G, g->ctx->stream);
+    if (g->p.system == COSMOS_GR) {
+        SweepArgs a = base_args(g);
+        a.G = G;
+        return launch_prim_out_gr_fast(a, state, staging);
+    }
+    return launch_prim_out_fast(state, staging, G, g->p.system, g->p.gamma, g->ctx->stream);
+}
+}  // namespace
+
+// Uploads and downloads move row chunks on the context's copy stream while the conversion kernels
+// of the previous chunk run on its compute stream (two engines busy at once); events order them.
 int cosmos_grid_set_prim(cosmos_grid* g, const double* prim, size_t n) {
     if (!g || !prim) return fail(COSMOS_EINVAL, "null grid or buffer");
     const size_t want = (size_t)5 * g->G.nx * g->G.ny;
     if (n != want) return fail(COSMOS_EINVAL, "buffer holds %zu doubles, grid needs %zu", n, want);
     CK(cudaSetDevice(g->ctx->device));
-    CK(cudaMemcpyAsync(g->staging, prim, want * sizeof(double), cudaMemcpyHostToDevice, g->ctx->stream));
-    if (g->p.precision == COSMOS_FP64) CK(launch_prim_in_exact(g->staging, g->buf[g->cur], g->G, g->ctx->stream));
-    else if (g->p.system == COSMOS_GR) CK(launch_prim_in_gr_fast(base_args(g), g->staging, g->buf[g->cur]));
-    else CK(launch_prim_in_fast(g->staging, g->buf[g->cur], g->G, g->p.system, g->p.gamma, g->ctx->stream));
+    cosmos_ctx* c = g->ctx;
+    // the staging buffer may still be read by earlier work on the compute stream
+    CK(cudaEventRecord(c->ev[0], c->stream));
+    CK(cudaStreamWaitEvent(c->copy, c->ev[0], 0));
+    const int rows = chunk_rows(g->G);
+    for (int r0 = 0; r0 < g->G.ny; r0 += rows) {
+        Geom G = g->G;
+        G.ny = std::min(rows, g->G.ny - r0);
+        const size_t off = (size_t)5 * g->G.nx * r0;
+        CK(cudaMemcpyAsync(g->staging + off, prim + off, (size_t)5 * g->G.nx * G.ny * sizeof(double),
+                           cudaMemcpyHostToDevice, c->copy));
+        CK(cudaEventRecord(c->ev[1], c->copy));
+        CK(cudaStreamWaitEvent(c->stream, c->ev[1], 0));
+        CK(convert_in(g, g->staging + off, (char*)g->buf[g->cur] + (size_t)r0 * g->G.pitch * g->elem, G));
+    }
+    // the caller's buffer may be reused once this returns
+    CK(cudaStreamSynchronize(c->copy));
     return COSMOS_OK;
 }
 
@@ -326,11 +371,19 @@ int cosmos_grid_get_prim(cosmos_grid* g, double* prim, size_t n) {
     const size_t want = (size_t)5 * g->G.nx * g->G.ny;
     if (n != want) return fail(COSMOS_EINVAL, "buffer holds %zu doubles, grid needs %zu", n, want);
     CK(cudaSetDevice(g->ctx->device));
-    if (g->p.precision == COSMOS_FP64) CK(launch_prim_out_exact(g->buf[g->cur], g->staging, g->G, g->ctx->stream));
-    else if (g->p.system == COSMOS_GR) CK(launch_prim_out_gr_fast(base_args(g), g->buf[g->cur], g->staging));
-    else CK(launch_prim_out_fast(g->buf[g->cur], g->staging, g->G, g->p.system, g->p.gamma, g->ctx->stream));
-    CK(cudaMemcpyAsync(prim, g->staging, want * sizeof(double), cudaMemcpyDeviceToHost, g->ctx->stream));
-    CK(cudaStreamSynchronize(g->ctx->stream));
+    cosmos_ctx* c = g->ctx;
+    const int rows = chunk_rows(g->G);
+    for (int r0 = 0; r0 < g->G.ny; r0 += rows) {
+        Geom G = g->G;
+        G.ny = std::min(rows, g->G.ny - r0);
+        const size_t off = (size_t)5 * g->G.nx * r0;
+        CK(convert_out(g, (const char*)g->buf[g->cur] + (size_t)r0 * g->G.pitch * g->elem, g->staging + off, G));
+        CK(cudaEventRecord(c->ev[0], c->stream));
+        CK(cudaStreamWaitEvent(c->copy, c->ev[0], 0));
+        CK(cudaMemcpyAsync(prim + off, g->staging + off, (size_t)5 * g->G.nx * G.ny * sizeof(double),
+                           cudaMemcpyDeviceToHost, c->copy));
+    }
+    CK(cudaStreamSynchronize(c->copy));
     return COSMOS_OK;
 }
 

@@ -11,6 +11,10 @@ struct cosmos_ctx {
     int device;
     cudaStream_t stream;
     std::atomic<int> refs;
+    // host <-> device copies of set_prim / get_prim run here, chunk by chunk, overlapping the
+    // conversion kernels on `stream`; events order the two streams
+    cudaStream_t copy;
+    cudaEvent_t ev[2];
 };
 
 struct cosmos_grid {

@@ -88,28 +88,42 @@ cudaError_t launch_wavespeed_fast(const SweepArgs& a, unsigned long long* slot) 
     return cudaGetLastError();
 }
 
-// Primitive (double, AoS) -> conserved FP32 SoA.  The conserved state is formed in double with
-// the reference's formula (Euler/EulerStateVector.cpp:55-66) and rounded once.
+// Primitive (double, AoS) -> conserved FP32 SoA (Euler/EulerStateVector.cpp:55-66), formed in
+// FP64 and rounded once; E = rho v^2 / 2 + p / (gamma - 1) with the reciprocal hoisted (no
+// per-cell FP64 division: GB300's FP64 divide costs as much as the whole conversion).
 __global__ void prim_in_fast_kernel(const double* __restrict__ aos, float* __restrict__ soa, Geom G, double gamma) {
     const size_t n = (size_t)G.nx * G.ny;
-    NewtonExact<double> S{gamma};
+    const double igm1 = 1.0 / (gamma - 1.0);
     for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
-        const size_t i = c / G.nx, j = c % G.nx;
-        double u[5];
-        S.cons(aos + 5 * c, Pt{0, 0, 0}, u);
-#pragma unroll
-        for (int f = 0; f < 5; f++) soa[f * G.fstride + i * G.pitch + j] = (float)u[f];
+        const size_t i = c / G.nx, j = c % G.nx, k = i * G.pitch + j;
+        const double* p = aos + 5 * c;
+        const double rho = p[0], vx = p[1], vy = p[2], vz = p[3];
+        soa[k] = (float)rho;
+        soa[G.fstride + k] = (float)(rho * vx);
+        soa[2 * G.fstride + k] = (float)(rho * vy);
+        soa[3 * G.fstride + k] = (float)(rho * vz);
+        soa[4 * G.fstride + k] = (float)(0.5 * rho * (vx * vx + vy * vy + vz * vz) + p[4] * igm1);
     }
 }
+// Conserved FP32 -> primitives (double, AoS) (Euler/EulerStateVector.cpp:30-40): 1 / rho from an
+// FP32 reciprocal refined by one FP64 Newton step (relative error ~1e-14, no FP64 division).
 __global__ void prim_out_fast_kernel(const float* __restrict__ soa, double* __restrict__ aos, Geom G, double gamma) {
     const size_t n = (size_t)G.nx * G.ny;
-    NewtonExact<double> S{gamma};
+    const double gm1 = gamma - 1.0;
     for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
-        const size_t i = c / G.nx, j = c % G.nx;
-        double u[5];
-#pragma unroll
-        for (int f = 0; f < 5; f++) u[f] = (double)soa[f * G.fstride + i * G.pitch + j];
-        S.prim(u, Pt{0, 0, 0}, aos + 5 * c);
+        const size_t i = c / G.nx, j = c % G.nx, k = i * G.pitch + j;
+        const double rho = soa[k], m1 = soa[G.fstride + k], m2 = soa[2 * G.fstride + k], m3 = soa[3 * G.fstride + k];
+        const double E = soa[4 * G.fstride + k];
+        double ir = (double)__frcp_rn((float)rho);
+        ir = ir * (2.0 - rho * ir);
+        ir = ir * (2.0 - rho * ir);
+        const double vx = m1 * ir, vy = m2 * ir, vz = m3 * ir;
+        double* p = aos + 5 * c;
+        p[0] = rho;
+        p[1] = vx;
+        p[2] = vy;
+        p[3] = vz;
+        p[4] = gm1 * (E - 0.5 * (m1 * vx + m2 * vy + m3 * vz));
     }
 }
 static int grid_for(size_t n) {
