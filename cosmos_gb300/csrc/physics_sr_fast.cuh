@@ -11,9 +11,10 @@
 // |step| < 1e-8 criterion holds on the next step.  The FP64 stage runs for every solve when
 // c2p64_above <= 0; otherwise only for states whose FP32 Lorentz factor exceeds c2p64_above (or
 // whose FP32 iteration did not converge).  Primitives are then formed in FP32.  The iteration caps
-// are 100 (FP32) and 64 (FP64) instead of the reference's 1000: beyond them the state has no
-// physical root (on GB300 one FP64 iteration costs as much as a whole FP32 recovery), and the
-// result is the last iterate as in the reference, flagged in the status word.
+// are 40 (FP32, from xi = 1; physical states converge in well under 20) and 8 (FP64, from the FP32
+// iterate) instead of the reference's 1000: beyond them the state has no physical root (on GB300
+// one FP64 iteration costs as much as a whole FP32 recovery), and the result is the last iterate
+// as in the reference, flagged in the status word.
 //
 // A sweep costs five primitive recoveries per cell (the two extrapolated states of the cell, the
 // two face states and the Richtmyer state of one face), against about two dozen in the reference,
@@ -50,7 +51,7 @@ CG_D SRPrim32 sr_c2p_fast(const SRFastParams& P, const float* u, int* flags) {
     const float eta = 2.0f * dc * gr;
     float x = 1.0f;
     bool conv = false;
-    for (int it = 0; it < 100; it++) {
+    for (int it = 0; it < 40; it++) {
         const float x2 = x * x;
         const float f = c4 * x2 * x * (x - eta) + c2 * x2 + c1 * x + c0;
         const float fp = c1 + 2.0f * c2 * x + 4.0f * c4 * x2 * x - 3.0f * eta * c4 * x2;
@@ -75,9 +76,9 @@ CG_D SRPrim32 sr_c2p_fast(const SRFastParams& P, const float* u, int* flags) {
         const double et = 2.0 * dcd * grd;
         double xd = x;
         bool c64 = false;
-        // from the FP32 iterate a solvable state converges in a few steps; a state without a
-        // physical root gives up after 64 (reported through the status word)
-        for (int it = 0; it < 64; it++) {
+        // from the FP32 iterate a solvable state converges in one to three steps; a state without
+        // a physical root gives up after 8 (reported through the status word)
+        for (int it = 0; it < 8; it++) {
             const double x2 = xd * xd;
             const double f = k4 * x2 * xd * (xd - et) + k2 * x2 + k1 * xd + k0;
             const double fp = k1 + 2.0 * k2 * xd + 4.0 * k4 * x2 * xd - 3.0 * et * k4 * x2;
