@@ -197,9 +197,17 @@ CG_D void adj_force_vjp(const AdjFlux<T>& F, const T* L, const T* R, T c, T d, c
     F.template vjp<AX>(R, fRb, Rb);
 }
 
+// Coefficients of one sweep, formed on the host in both precisions (an FP64 divide per thread
+// would dominate the FP32 kernel: GB300's FP64 rate is 1/64 of FP32).
+template <class T>
+struct AdjCoef {
+    T g1, gam, w, d, c, hs;  // gamma - 1, gamma, bias, dt/dx, dx/dt, dt/(2 dx)
+};
 struct AdjSweepParams {
     Geom G;
     double dx, dt, bias, gamma;
+    AdjCoef<float> cf;
+    AdjCoef<double> cd;
     const void* state;     // sweep input in storage precision (FP64 primitives or FP32 conserved)
     const void* ubar_out;  // adjoint of the sweep output (T, conserved SoA, same layout)
     void* ubar_in;         // adjoint of the sweep input (written)
@@ -242,9 +250,11 @@ __global__ void __launch_bounds__(P * W, (sizeof(T) == 4 ? 3 : 1)) adjoint_sweep
     auto gi = [&](int pos) -> size_t {
         return AX == 0 ? (size_t)line * G.pitch + pos : (size_t)pos * G.pitch + line;
     };
-    const AdjFlux<T> F{T(a.gamma - 1.0)};
-    const T w = T(a.bias);
-    const T d = T(a.dt / a.dx), c = T(a.dx / a.dt), hs = T(0.5 * (a.dt / a.dx));
+    AdjCoef<T> K;
+    if constexpr (sizeof(T) == 4) K = a.cf;
+    else K = a.cd;
+    const AdjFlux<T> F{K.g1};
+    const T w = K.w, d = K.d, c = K.c, hs = K.hs;
     const S* st = (const S*)a.state;
     const T* ubo = (const T*)a.ubar_out;
     const int me = si(along);
@@ -264,7 +274,7 @@ __global__ void __launch_bounds__(P * W, (sizeof(T) == 4 ? 3 : 1)) adjoint_sweep
                 u[1] = v[0] * v[1];
                 u[2] = v[0] * v[2];
                 u[3] = v[0] * v[3];
-                u[4] = v[0] * (T(0.5) * ((v[1] * v[1] + v[2] * v[2]) + v[3] * v[3]) + v[4] / ((T(a.gamma) - T(1)) * v[0]));
+                u[4] = v[0] * (T(0.5) * ((v[1] * v[1] + v[2] * v[2]) + v[3] * v[3]) + v[4] / (K.g1 * v[0]));
             } else {
 #pragma unroll
                 for (int f = 0; f < 5; f++) u[f] = v[f];

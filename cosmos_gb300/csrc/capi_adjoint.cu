@@ -167,6 +167,12 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
             sweep_of(q, axis, dt);
             ap.G.axis = axis;
             ap.dt = dt;
+            {
+                const double gam = g->p.gamma, dx = g->p.dx;
+                ap.cd = AdjCoef<double>{gam - 1.0, gam, o->bias, dt / dx, dx / dt, 0.5 * (dt / dx)};
+                ap.cf = AdjCoef<float>{(float)ap.cd.g1, (float)ap.cd.gam, (float)ap.cd.w, (float)ap.cd.d, (float)ap.cd.c,
+                                       (float)ap.cd.hs};
+            }
             ap.state = slot(q);
             ap.ubar_out = adj + (size_t)cur * abytes;
             ap.ubar_in = adj + (size_t)(cur ^ 1) * abytes;

@@ -242,18 +242,27 @@ template <int LIM>
 __global__ void __launch_bounds__(128) gr_rk_kernel(SRFastParams P, NewtonFastParams NP, GRTables T, Geom G, double dx,
                                                     const float* __restrict__ src, float* __restrict__ dst, DtSrc ds,
                                                     int* status) {
+    // the step's dt (0.5 dt / subcycles from the controller) and dt/dx, once per block
+    __shared__ float s_dt, s_dtdx;
+    __shared__ int s_on;
+    if (threadIdx.x == 0) {
+        double d;
+        s_on = ds.get(d);
+        s_dt = (float)d;
+        s_dtdx = (float)(d / dx);
+    }
+    __syncthreads();
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y;
     if (j >= G.nx) return;
     const size_t idx = (size_t)i * G.pitch + j;
-    double dtd;
-    const bool on = ds.get(dtd) && (T.flags[(size_t)i * G.nx + j] & 4);
+    const bool on = s_on && (T.flags[(size_t)i * G.nx + j] & 4);
     if (!on) {
 #pragma unroll
         for (int f = 0; f < 5; f++) dst[f * G.fstride + idx] = src[f * G.fstride + idx];
         return;
     }
-    const float dtdx = (float)(dtd / dx);  // the sub-step's dt (0.5 dt / subcycles from the controller)
+    const float dtdx = s_dtdx;
     auto ld = [&](int ii, int jj, float* p) {
         const size_t k = (size_t)ghost_index(ii, G.ny, 0) * G.pitch + ghost_index(jj, G.nx, 0);
 #pragma unroll
@@ -287,7 +296,7 @@ __global__ void __launch_bounds__(128) gr_rk_kernel(SRFastParams P, NewtonFastPa
     GRSrc X;
     load_src(GRTab{T.src, T.cell_stride}, (size_t)i * G.nx + j, X);
     int flags = 0;
-    gr_rk_fast<LIM>(P, NP, G.dims, cl, cm, cr, ct, cb, Ml, Mc, Mr, Mt, Mb, X, (float)dtd, dtdx, out, &flags);
+    gr_rk_fast<LIM>(P, NP, G.dims, cl, cm, cr, ct, cb, Ml, Mc, Mr, Mt, Mb, X, s_dt, dtdx, out, &flags);
 #pragma unroll
     for (int f = 0; f < 5; f++) dst[f * G.fstride + idx] = out[f];
     if (flags && status) atomicOr(status, ST_NEWTON_CAP);

@@ -29,7 +29,7 @@ struct SRFastParams {
     float wa, wb, hom, hop;  // bias factors as in NewtonFastParams
     float gf;                // gamma
     double g;                // gamma (FP64 stage)
-    double c2p64_above;      // Lorentz factor above which the FP64 stage runs (<= 0: always)
+    float w64;               // Lorentz factor above which the FP64 stage runs (0: always)
 };
 
 struct SRPrim32 {
@@ -61,7 +61,7 @@ CG_D SRPrim32 sr_c2p_fast(const SRFastParams& P, const float* u, int* flags) {
         if (done) { conv = true; break; }
     }
     float W = 0.5f * ec * x * (1.0f + sqrtf(1.0f + 4.0f * gr * (1.0f - dc * x) / (ec * ec * x * x)));
-    if (P.c2p64_above <= 0.0 || !conv || W > (float)P.c2p64_above) {
+    if (!conv || W > P.w64) {
         // FP64 Newton from the FP32 root, coefficients in FP64
         const double Dd = D, td = tau;
         const double gd = P.g, grd = (gd - 1.0) / gd;

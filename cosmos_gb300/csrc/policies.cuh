@@ -255,7 +255,7 @@ inline SRFastPolicy<AXIS, LIM, MASKED> make_sr_fast(double gamma, double bias, i
     p.P.hop = p.NP.hop;
     p.P.gf = (float)gamma;
     p.P.g = gamma;
-    p.P.c2p64_above = c2p64_above;
+    p.P.w64 = c2p64_above > 0.0 ? (float)c2p64_above : 0.0f;  // W >= 1 > 0: threshold 0 always runs FP64
     p.lm.axis = AXIS;
     p.lm.nx = nx;
     p.dims = dims;

@@ -5,8 +5,9 @@
     python -m cosmos_gb300.profile --kernel adjoint --n 1024 --precision fp32 --launches 2
     python -m cosmos_gb300.profile --kernel batch --grids 64 --launches 2
 
-Creates one grid of the config-2 problem (four-quadrant data, periodic, MinBee) and launches the
-requested kernels a few times, so that a profiler can capture exactly those launches on a
+Creates one grid of the configuration's problem for the system (Newtonian: config-2 four-quadrant
+data, periodic; SR: config-3 Kelvin-Helmholtz layers, periodic; GR: config-4 accretion onto a
+Schwarzschild hole, transmissive; MinBee) and launches the requested kernels a few times, so that a profiler can capture exactly those launches on a
 bounded device footprint (two state buffers plus one staging buffer).  `adjoint` runs the
 gradient of `launches` SLIC steps (checkpoint every step: launches X and Y sweep adjoints per
 step); `batch` runs `launches` chunks of 10 steps of the first `grids` grids of the batched
@@ -48,20 +49,26 @@ def main():
         print(f"ok: {a.launches} x batch chunk ({len(shapes)} grids, {b.cells} cells)")
         return
     n = a.n
-    rng = np.random.default_rng(2)
-    q = np.zeros((4, 5))
-    q[:, 0] = rng.uniform(0.1, 1.5, 4)
-    q[:, 1] = rng.uniform(-1.0, 1.0, 4)
-    q[:, 2] = rng.uniform(-1.0, 1.0, 4)
-    q[:, 4] = rng.uniform(0.03, 1.5, 4)
-    s = np.zeros((n, n, 5))
-    h = n // 2
-    s[:h, :h], s[:h, h:], s[h:, :h], s[h:, h:] = q
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests"))
+    import cases
     prec = cg.FP32 if a.precision == "fp32" else cg.FP64
+    bh = None
+    dx = 1.0 / n
+    if a.system == cg.NEWTONIAN:  # config-2 four-quadrant data
+        s = cases.four_quadrant(n, 2)
+    elif a.system == cg.SR:  # config-3 Kelvin-Helmholtz layers
+        s = cases.kelvin_helmholtz(n, 3)
+    else:  # config-4 accretion: [-10, 10]^2 with the hole at the centre, M = 1
+        rng = np.random.default_rng(4)
+        s = np.zeros((n, n, 5))
+        s[..., 0] = np.exp(0.01 * rng.standard_normal((n, n)))
+        s[..., 4] = 0.01
+        dx = 20.0 / n
+        bh = cg.BlackHoleSpacetime(1.0, 0.0, 10.0, 10.0, 0.0)
     bc = cg.BC_PERIODIC if a.system != cg.GR else cg.BC_TRANSMISSIVE
-    g = cg.Grid(a.system, (n, n), 1.0 / n, 1.4 if a.system == 0 else 5.0 / 3.0, prec, bc)
+    g = cg.Grid(a.system, (n, n), dx, 1.4 if a.system == 0 else 5.0 / 3.0, prec, bc, bh)
     g.set_prim(s)
-    dt = 0.25 / n
+    dt = 0.25 * dx
     if a.kernel == "sweep":
         for _ in range(a.launches):
             g.sweep(a.axis, a.order, dt, 0.0, cg.MINBEE)
