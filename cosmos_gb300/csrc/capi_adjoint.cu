@@ -5,7 +5,8 @@
 // the state copied to a checkpoint store before every segment and each step's dt logged.
 // Backward, segment by segment from the last: the segment is recomputed from its checkpoint with
 // the same sweep kernels and the same dts, keeping every sweep's input; the sweep adjoints then
-// run in reverse order (X(dt/2) Y(dt) X(dt/2) per 2D step, X(dt) per 1D step).
+// run in reverse order (X(dt/2) Y(dt) X(dt/2) per 2D step, X(dt) per 1D step).  The next
+// segment's recomputation overlaps the current segment's adjoints on a second stream.
 #include <algorithm>
 #include <climits>
 #include <cstddef>
@@ -35,6 +36,7 @@ struct Scratch {
     cudaStream_t st = nullptr;
     std::vector<void*> ptrs;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t rec_done[2] = {nullptr, nullptr}, adj_done[2] = {nullptr, nullptr};
     StepCtl* patched = nullptr;  // controller whose dt pointers point into this scratch
     cudaError_t alloc(void** p, size_t bytes) {
         cudaError_t e = cudaMallocAsync(p, bytes, st);
@@ -53,6 +55,10 @@ struct Scratch {
         for (void* p : ptrs) cudaFreeAsync(p, st);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
+        for (int k = 0; k < 2; k++) {
+            if (rec_done[k]) cudaEventDestroy(rec_done[k]);
+            if (adj_done[k]) cudaEventDestroy(adj_done[k]);
+        }
     }
 };
 
@@ -84,13 +90,17 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
     char *ck, *seg, *adj;
     double *d_target, *d_dts, *d_rows, *d_loss;
     ACK(sc.alloc((void**)&ck, (size_t)nck * sbytes));
-    ACK(sc.alloc((void**)&seg, (size_t)K * spp * sbytes));
+    ACK(sc.alloc((void**)&seg, (size_t)2 * K * spp * sbytes));  // two segments: recompute one, reverse the other
     ACK(sc.alloc((void**)&adj, 2 * abytes));
     ACK(sc.alloc((void**)&d_target, ncell * sizeof(double)));
     ACK(sc.alloc((void**)&d_dts, nsteps * sizeof(double)));
     ACK(sc.alloc((void**)&d_rows, (size_t)G0.ny * sizeof(double)));
     ACK(sc.alloc((void**)&d_loss, sizeof(double)));
     for (auto& e : sc.ev) ACK(cudaEventCreate(&e));
+    for (int k = 0; k < 2; k++) {
+        ACK(cudaEventCreateWithFlags(&sc.rec_done[k], cudaEventDisableTiming));
+        ACK(cudaEventCreateWithFlags(&sc.adj_done[k], cudaEventDisableTiming));
+    }
     ACK(cudaMemcpyAsync(d_target, target, ncell * sizeof(double), cudaMemcpyHostToDevice, st));
     if (dts_in) ACK(cudaMemcpyAsync(d_dts, dts_in, nsteps * sizeof(double), cudaMemcpyHostToDevice, st));
 
@@ -139,32 +149,46 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
     ap.dx = g->p.dx;
     ap.bias = o->bias;
     ap.gamma = g->p.gamma;
-    auto slot = [&](int q) { return seg + (size_t)q * sbytes; };
-    for (int c = nck - 1; c >= 0; c--) {
-        const int s0 = c * K, s1 = std::min(nsteps, s0 + K);
-        const int nsw = (s1 - s0) * spp;  // sweeps in the segment; their inputs go to slots 0..nsw-1
-        ACK(cudaMemcpyAsync(slot(0), ck + (size_t)c * sbytes, sbytes, cudaMemcpyDeviceToDevice, st));
-        auto sweep_of = [&](int q, int& axis, double& dt) {
-            const double d = dts[s0 + q / spp];
-            const int m = q % spp;
-            axis = spp == 3 && m == 1 ? 1 : 0;
-            dt = spp == 3 && m != 1 ? 0.5 * d : d;
-        };
+    // The recomputation of segment c - 1 (forward sweeps, on the context's second stream) runs
+    // while the sweep adjoints of segment c run on the compute stream; the two segments use
+    // alternate halves of `seg`, and events order each half's writer and reader.
+    cudaStream_t rs = g->ctx->copy;
+    fa.stream = rs;
+    for (int k = 0; k < 2; k++) ACK(cudaEventRecord(sc.adj_done[k], st));  // after the forward pass and the loss
+    auto slot = [&](int c, int q) { return seg + ((size_t)(c & 1) * K * spp + q) * sbytes; };
+    auto sweep_of = [&](int c, int q, int& axis, double& dt) {
+        const double d = dts[c * K + q / spp];
+        const int m = q % spp;
+        axis = spp == 3 && m == 1 ? 1 : 0;
+        dt = spp == 3 && m != 1 ? 0.5 * d : d;
+    };
+    auto nsweeps = [&](int c) { return (std::min(nsteps, c * K + K) - c * K) * spp; };
+    auto recompute = [&](int c) -> int {
+        ACK(cudaStreamWaitEvent(rs, sc.adj_done[c & 1], 0));  // this half's previous reader is done
+        ACK(cudaMemcpyAsync(slot(c, 0), ck + (size_t)c * sbytes, sbytes, cudaMemcpyDeviceToDevice, rs));
+        const int nsw = nsweeps(c);
         for (int q = 0; q + 1 < nsw; q++) {  // the last sweep's output is not needed
             int axis;
             double dt;
-            sweep_of(q, axis, dt);
+            sweep_of(c, q, axis, dt);
             fa.G.axis = axis;
             fa.ds.fixed = dt;
             fa.ds.ffix = make_fast_coef(dt, g->p.dx);
-            fa.src = slot(q);
-            fa.dst = slot(q + 1);
+            fa.src = slot(c, q);
+            fa.dst = slot(c, q + 1);
             ACK(sweep_launch(g, fa));
         }
-        for (int q = nsw - 1; q >= 0; q--) {
+        ACK(cudaEventRecord(sc.rec_done[c & 1], rs));
+        return COSMOS_OK;
+    };
+    if ((rc = recompute(nck - 1))) return rc;
+    for (int c = nck - 1; c >= 0; c--) {
+        if (c > 0 && (rc = recompute(c - 1))) return rc;
+        ACK(cudaStreamWaitEvent(st, sc.rec_done[c & 1], 0));
+        for (int q = nsweeps(c) - 1; q >= 0; q--) {
             int axis;
             double dt;
-            sweep_of(q, axis, dt);
+            sweep_of(c, q, axis, dt);
             ap.G.axis = axis;
             ap.dt = dt;
             {
@@ -173,12 +197,13 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
                 ap.cf = AdjCoef<float>{(float)ap.cd.g1, (float)ap.cd.gam, (float)ap.cd.w, (float)ap.cd.d, (float)ap.cd.c,
                                        (float)ap.cd.hs};
             }
-            ap.state = slot(q);
+            ap.state = slot(c, q);
             ap.ubar_out = adj + (size_t)cur * abytes;
             ap.ubar_in = adj + (size_t)(cur ^ 1) * abytes;
             ACK(fp64 ? launch_adjoint_sweep_exact(ap, o->limiter, st) : launch_adjoint_sweep_fast(ap, o->limiter, st));
             cur ^= 1;
         }
+        ACK(cudaEventRecord(sc.adj_done[c & 1], st));
     }
     // ---- gradient with respect to the initial primitives
     ACK(fp64 ? launch_adjoint_grad_exact(G0, g->p.gamma, ck, adj + (size_t)cur * abytes, g->staging, st)
