@@ -24,174 +24,210 @@
 //   3 half-step reverse per cell   4 gather per updated cell.
 #pragma once
 #include "device_common.cuh"
+#include "physics_fast.cuh"
 #include "sweep_kernels.cuh"
 
 namespace cg {
 
-// Reciprocal: approximate (about 1 ulp) in FP32, where the derivative does not need IEEE division;
-// exact in FP64.
-CG_D float adj_rcp(float x) { return __fdividef(1.0f, x); }
-CG_D double adj_rcp(double x) { return 1.0 / x; }
+// ---- lane types: float (one line per thread), f2 (two lines per thread on paired FP32
+// instructions, physics_fast.cuh), double (the FP64 path; explicitly rounded like the others).
+CG_D double vadd(double a, double b) { return __dadd_rn(a, b); }
+CG_D double vsub(double a, double b) { return __dsub_rn(a, b); }
+CG_D double vmul(double a, double b) { return __dmul_rn(a, b); }
+CG_D double vfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+CG_D double vrcp(double a) { return 1.0 / a; }
+CG_D double vmin(double a, double b) { return fmin(a, b); }
+CG_D double vmax(double a, double b) { return fmax(a, b); }
+CG_D double vabs(double a) { return fabs(a); }
+CG_D double vsel_lt(double a, double b, double x, double y) { return a < b ? x : y; }
+
+template <class V> struct Lane;
+template <> struct Lane<float> {
+    using S = float;
+    static constexpr int N = 1;
+    static CG_D float bc(float s) { return s; }
+};
+template <> struct Lane<f2> {
+    using S = float;
+    static constexpr int N = 2;
+    static CG_D f2 bc(float s) { return f2{make_float2(s, s)}; }
+};
+template <> struct Lane<double> {
+    using S = double;
+    static constexpr int N = 1;
+    static CG_D double bc(double s) { return s; }
+};
+template <class V> CG_D V bcv(typename Lane<V>::S s) { return Lane<V>::bc(s); }
 
 // Newtonian flux along axis AX of a conserved state, and its transposed Jacobian.
-template <class T>
+template <class V>
 struct AdjFlux {
-    T g1;  // gamma - 1
+    V g1;  // gamma - 1
     template <int AX>
-    CG_D void flux(const T* u, T* f) const {
-        const T inv = adj_rcp(u[0]);
-        const T vn = u[1 + AX] * inv;
-        const T p = g1 * (u[4] - T(0.5) * ((u[1] * u[1] + u[2] * u[2]) + u[3] * u[3]) * inv);
+    CG_D void flux(const V* u, V* f) const {
+        const V inv = vrcp(u[0]);
+        const V vn = vmul(u[1 + AX], inv);
+        const V q = vfma(u[1], u[1], vfma(u[2], u[2], vmul(u[3], u[3])));
+        const V p = vmul(g1, vsub(u[4], vmul(bcv<V>(0.5), vmul(q, inv))));
         f[0] = u[1 + AX];
-        f[1] = u[1] * vn;
-        f[2] = u[2] * vn;
-        f[3] = u[3] * vn;
-        f[1 + AX] = f[1 + AX] + p;
-        f[4] = (u[4] + p) * vn;
+        f[1] = vmul(u[1], vn);
+        f[2] = vmul(u[2], vn);
+        f[3] = vmul(u[3], vn);
+        f[1 + AX] = vadd(f[1 + AX], p);
+        f[4] = vmul(vadd(u[4], p), vn);
     }
     // ub += (dF/du)^T gb
     template <int AX>
-    CG_D void vjp(const T* u, const T* gb, T* ub) const {
-        const T inv = adj_rcp(u[0]);
-        const T v0 = u[1] * inv, v1 = u[2] * inv, v2 = u[3] * inv;
-        const T vn = AX == 0 ? v0 : v1;
-        const T vv = (v0 * v0 + v1 * v1) + v2 * v2;
-        const T p = g1 * (u[4] - T(0.5) * u[0] * vv);
-        const T pb = gb[1 + AX] + gb[4] * vn;                                         // from F_n and F_E
-        const T vnb = ((gb[1] * u[1] + gb[2] * u[2]) + gb[3] * u[3]) + gb[4] * (u[4] + p);  // d/dv_n
-        const T gp = g1 * pb;
-        ub[0] += gp * T(0.5) * vv - vnb * vn * inv;
-        ub[1] += gb[1] * vn - gp * v0;
-        ub[2] += gb[2] * vn - gp * v1;
-        ub[3] += gb[3] * vn - gp * v2;
-        ub[1 + AX] += gb[0] + vnb * inv;
-        ub[4] += gb[4] * vn + gp;
+    CG_D void vjp(const V* u, const V* gb, V* ub) const {
+        const V inv = vrcp(u[0]);
+        const V v0 = vmul(u[1], inv), v1 = vmul(u[2], inv), v2 = vmul(u[3], inv);
+        const V vn = AX == 0 ? v0 : v1;
+        const V vv = vfma(v0, v0, vfma(v1, v1, vmul(v2, v2)));
+        const V p = vmul(g1, vsub(u[4], vmul(bcv<V>(0.5), vmul(u[0], vv))));
+        const V pb = vfma(gb[4], vn, gb[1 + AX]);                                         // from F_n and F_E
+        const V vnb = vfma(gb[4], vadd(u[4], p), vfma(gb[3], u[3], vfma(gb[2], u[2], vmul(gb[1], u[1]))));  // d/dv_n
+        const V gp = vmul(g1, pb);
+        ub[0] = vadd(ub[0], vsub(vmul(vmul(gp, bcv<V>(0.5)), vv), vmul(vmul(vnb, vn), inv)));
+        ub[1] = vadd(ub[1], vsub(vmul(gb[1], vn), vmul(gp, v0)));
+        ub[2] = vadd(ub[2], vsub(vmul(gb[2], vn), vmul(gp, v1)));
+        ub[3] = vadd(ub[3], vsub(vmul(gb[3], vn), vmul(gp, v2)));
+        ub[1 + AX] = vadd(ub[1 + AX], vfma(vnb, inv, gb[0]));
+        ub[4] = vadd(ub[4], vfma(gb[4], vn, gp));
     }
 };
 
+// Slope factors of one sweep: ca = (1 + w)/2, cb = (1 - w)/2 and the gradient ratio's 1 -+ w.
+template <class V>
+struct AdjSlope {
+    V ca, cb, w1m, w1p;
+};
+
 // Limiter value and derivative d(xi)/dr on the branch the forward evaluation takes
-// (Solvers/SlopeLimiters.cpp:8-69; min(a, b) picks b only when b < a).
-template <class T, int LIM>
-CG_D T limiter_d(T r, T w, T& d) {
-    if (r < T(0)) { d = T(0); return T(0); }
-    const T iden = adj_rcp((T(1) - w) + (T(1) + w) * r);
-    const T xr = T(2) * iden;
-    const T dxr = -T(2) * (T(1) + w) * iden * iden;
+// (Solvers/SlopeLimiters.cpp:8-69; min(a, b) picks b only when b < a), as select chains.
+template <class V, int LIM>
+CG_D V limiter_d(const AdjSlope<V>& A, V r, V& d) {
+    const V zero = bcv<V>(0), one = bcv<V>(1), two = bcv<V>(2);
+    const V iden = vrcp(vfma(A.w1p, r, A.w1m));
+    const V xr = vmul(two, iden);
+    const V dxr = vmul(vmul(bcv<V>(-2), A.w1p), vmul(iden, iden));
+    V val, der;
     if (LIM == 0) {  // SuperBee
-        if (r < T(0.5)) { d = T(2); return T(2) * r; }
-        if (r < T(1)) { d = T(0); return T(1); }
-        T m = r;
-        d = T(1);
-        if (xr < m) { m = xr; d = dxr; }
-        if (T(2) < m) { m = T(2); d = T(0); }
-        return m;
+        const V m1 = vsel_lt(xr, r, xr, r), d1 = vsel_lt(xr, r, dxr, one);
+        const V m2 = vsel_lt(two, m1, two, m1), d2 = vsel_lt(two, m1, zero, d1);
+        val = vsel_lt(r, bcv<V>(0.5), vmul(two, r), vsel_lt(r, one, one, m2));
+        der = vsel_lt(r, bcv<V>(0.5), two, vsel_lt(r, one, zero, d2));
     } else if (LIM == 1) {  // van Leer
-        const T iop = adj_rcp(T(1) + r);
-        const T vl = T(2) * r * iop;
-        if (xr < vl) { d = dxr; return xr; }
-        d = T(2) * iop * iop;
-        return vl;
+        const V iop = vrcp(vadd(one, r));
+        const V vl = vmul(vmul(two, r), iop);
+        val = vsel_lt(xr, vl, xr, vl);
+        der = vsel_lt(xr, vl, dxr, vmul(two, vmul(iop, iop)));
+    } else {  // MinBee
+        val = vsel_lt(r, one, r, vsel_lt(xr, one, xr, one));
+        der = vsel_lt(r, one, one, vsel_lt(xr, one, dxr, zero));
     }
-    // MinBee
-    if (r < T(1)) { d = T(1); return r; }
-    if (xr < T(1)) { d = dxr; return xr; }
-    d = T(0);
-    return T(1);
+    d = vsel_lt(r, zero, zero, der);
+    return vsel_lt(r, zero, zero, val);
 }
 
 // Half-step evolution of one cell: A (left-face) and B (right-face) states.
-template <class T, int AX, int LIM>
-CG_D void adj_evolve(const AdjFlux<T>& F, const T* ul, const T* uc, const T* ur, T w, T hs, T* A, T* B) {
-    const T ca = T(0.5) * (T(1) + w), cb = T(0.5) * (T(1) - w);
-    T UL[5], UR[5];
+template <class V, int AX, int LIM>
+CG_D void adj_evolve(const AdjFlux<V>& F, const AdjSlope<V>& Sl, const V* ul, const V* uc, const V* ur, V hs, V* A,
+                     V* B) {
+    const V eps = bcv<V>(1e-5);
+    V UL[5], UR[5];
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-        const T dl = uc[k] - ul[k], dr = ur[k] - uc[k];
-        const T s = ca * dl + cb * dr;
-        const T num = fabs(dl) < T(1e-5) ? T(1e-5) : dl;
-        const T den = fabs(dr) < T(1e-5) ? T(1e-5) : dr;
-        T dxi;
-        const T sl = s * limiter_d<T, LIM>(num * adj_rcp(den), w, dxi);
-        UL[k] = uc[k] - T(0.5) * sl;
-        UR[k] = uc[k] + T(0.5) * sl;
+        const V dl = vsub(uc[k], ul[k]), dr = vsub(ur[k], uc[k]);
+        const V s = vfma(Sl.ca, dl, vmul(Sl.cb, dr));
+        const V num = vsel_lt(vabs(dl), eps, eps, dl);
+        const V den = vsel_lt(vabs(dr), eps, eps, dr);
+        V dxi;
+        const V sl = vmul(s, limiter_d<V, LIM>(Sl, vmul(num, vrcp(den)), dxi));
+        UL[k] = vfma(bcv<V>(-0.5), sl, uc[k]);
+        UR[k] = vfma(bcv<V>(0.5), sl, uc[k]);
     }
-    T FL[5], FR[5];
+    V FL[5], FR[5];
     F.template flux<AX>(UL, FL);
     F.template flux<AX>(UR, FR);
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-        const T e = hs * (FL[k] - FR[k]);
-        A[k] = UL[k] + e;
-        B[k] = UR[k] + e;
+        const V e = vmul(hs, vsub(FL[k], FR[k]));
+        A[k] = vadd(UL[k], e);
+        B[k] = vadd(UR[k], e);
     }
 }
 
 // Reverse of adj_evolve: given Abar, Bbar, the contributions to the three stencil cells.
-template <class T, int AX, int LIM>
-CG_D void adj_evolve_vjp(const AdjFlux<T>& F, const T* ul, const T* uc, const T* ur, T w, T hs, const T* Ab,
-                         const T* Bb, T* gl, T* gc, T* gr) {
-    const T ca = T(0.5) * (T(1) + w), cb = T(0.5) * (T(1) - w);
-    T UL[5], UR[5], sv[5], xi[5], dxi[5], r[5], iden[5];
-    bool cn[5], cd[5];
+template <class V, int AX, int LIM>
+CG_D void adj_evolve_vjp(const AdjFlux<V>& F, const AdjSlope<V>& Sl, const V* ul, const V* uc, const V* ur, V hs,
+                         const V* Ab, const V* Bb, V* gl, V* gc, V* gr) {
+    const V eps = bcv<V>(1e-5), zero = bcv<V>(0);
+    V UL[5], UR[5], sv[5], xi[5], dxi[5], r[5], iden[5], adl[5], adr[5];
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-        const T dl = uc[k] - ul[k], dr = ur[k] - uc[k];
-        sv[k] = ca * dl + cb * dr;
-        cn[k] = fabs(dl) < T(1e-5);
-        cd[k] = fabs(dr) < T(1e-5);
-        const T num = cn[k] ? T(1e-5) : dl;
-        iden[k] = adj_rcp(cd[k] ? T(1e-5) : dr);
-        r[k] = num * iden[k];
-        xi[k] = limiter_d<T, LIM>(r[k], w, dxi[k]);
-        const T sl = sv[k] * xi[k];
-        UL[k] = uc[k] - T(0.5) * sl;
-        UR[k] = uc[k] + T(0.5) * sl;
+        const V dl = vsub(uc[k], ul[k]), dr = vsub(ur[k], uc[k]);
+        sv[k] = vfma(Sl.ca, dl, vmul(Sl.cb, dr));
+        adl[k] = vabs(dl);
+        adr[k] = vabs(dr);
+        const V num = vsel_lt(adl[k], eps, eps, dl);
+        iden[k] = vrcp(vsel_lt(adr[k], eps, eps, dr));
+        r[k] = vmul(num, iden[k]);
+        xi[k] = limiter_d<V, LIM>(Sl, r[k], dxi[k]);
+        const V sl = vmul(sv[k], xi[k]);
+        UL[k] = vfma(bcv<V>(-0.5), sl, uc[k]);
+        UR[k] = vfma(bcv<V>(0.5), sl, uc[k]);
     }
-    T ULb[5], URb[5], FLb[5], FRb[5];
+    V ULb[5], URb[5], FLb[5], FRb[5];
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-        const T eb = Ab[k] + Bb[k];
+        const V eb = vadd(Ab[k], Bb[k]);
         ULb[k] = Ab[k];
         URb[k] = Bb[k];
-        FLb[k] = hs * eb;
-        FRb[k] = -(hs * eb);
+        FLb[k] = vmul(hs, eb);
+        FRb[k] = vmul(bcv<V>(-1), vmul(hs, eb));
     }
     F.template vjp<AX>(UL, FLb, ULb);
     F.template vjp<AX>(UR, FRb, URb);
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-        const T slb = T(0.5) * (URb[k] - ULb[k]);
-        const T xib = slb * sv[k];
-        const T sb = slb * xi[k];
-        const T rb = xib * dxi[k];
-        const T dlb = ca * sb + (cn[k] ? T(0) : rb * iden[k]);
-        const T drb = cb * sb - (cd[k] ? T(0) : rb * r[k] * iden[k]);
-        gl[k] = -dlb;
-        gc[k] = (ULb[k] + URb[k]) + (dlb - drb);
+        const V slb = vmul(bcv<V>(0.5), vsub(URb[k], ULb[k]));
+        const V xib = vmul(slb, sv[k]);
+        const V sb = vmul(slb, xi[k]);
+        const V rb = vmul(xib, dxi[k]);
+        // the clamped differences carry no derivative
+        const V dlb = vfma(Sl.ca, sb, vsel_lt(adl[k], eps, zero, vmul(rb, iden[k])));
+        const V drb = vsub(vmul(Sl.cb, sb), vsel_lt(adr[k], eps, zero, vmul(vmul(rb, r[k]), iden[k])));
+        gl[k] = vmul(bcv<V>(-1), dlb);
+        gc[k] = vadd(vadd(ULb[k], URb[k]), vsub(dlb, drb));
         gr[k] = drb;
     }
 }
 
 // Reverse of the FORCE flux of (L, R): given Fbar, Lbar and Rbar.
-template <class T, int AX>
-CG_D void adj_force_vjp(const AdjFlux<T>& F, const T* L, const T* R, T c, T d, const T* Fb, T* Lb, T* Rb) {
-    T fL[5], fR[5], us[5];
+template <class V, int AX>
+CG_D void adj_force_vjp(const AdjFlux<V>& F, const V* L, const V* R, V c, V d, const V* Fb, V* Lb, V* Rb) {
+    const V h = bcv<V>(0.5);
+    V fL[5], fR[5], us[5];
     F.template flux<AX>(L, fL);
     F.template flux<AX>(R, fR);
 #pragma unroll
-    for (int k = 0; k < 5; k++) us[k] = T(0.5) * ((L[k] + R[k]) + d * (fL[k] - fR[k]));
-    T usb[5] = {T(0), T(0), T(0), T(0), T(0)}, fsb[5];
-#pragma unroll
-    for (int k = 0; k < 5; k++) fsb[k] = T(0.5) * Fb[k];
-    F.template vjp<AX>(us, fsb, usb);
-    T fLb[5], fRb[5];
+    for (int k = 0; k < 5; k++) us[k] = vmul(h, vfma(d, vsub(fL[k], fR[k]), vadd(L[k], R[k])));
+    V usb[5], fsb[5];
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-        const T lfb = T(0.5) * Fb[k];
-        Lb[k] = T(0.5) * usb[k] + T(0.5) * c * lfb;
-        Rb[k] = T(0.5) * usb[k] - T(0.5) * c * lfb;
-        fLb[k] = T(0.5) * d * usb[k] + T(0.5) * lfb;
-        fRb[k] = T(0.5) * lfb - T(0.5) * d * usb[k];
+        usb[k] = bcv<V>(0);
+        fsb[k] = vmul(h, Fb[k]);
+    }
+    F.template vjp<AX>(us, fsb, usb);
+    V fLb[5], fRb[5];
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const V lfb = vmul(h, Fb[k]);
+        const V a = vmul(h, usb[k]), b = vmul(vmul(h, c), lfb), e = vmul(vmul(h, d), usb[k]), f = vmul(h, lfb);
+        Lb[k] = vadd(a, b);
+        Rb[k] = vsub(a, b);
+        fLb[k] = vadd(e, f);
+        fRb[k] = vsub(f, e);
     }
     F.template vjp<AX>(L, fLb, Lb);
     F.template vjp<AX>(R, fRb, Rb);
@@ -202,6 +238,7 @@ CG_D void adj_force_vjp(const AdjFlux<T>& F, const T* L, const T* R, T c, T d, c
 template <class T>
 struct AdjCoef {
     T g1, gam, w, d, c, hs;  // gamma - 1, gamma, bias, dt/dx, dx/dt, dt/(2 dx)
+    T ca, cb, w1m, w1p;      // (1 + w)/2, (1 - w)/2, 1 - w, 1 + w
 };
 struct AdjSweepParams {
     Geom G;
@@ -226,50 +263,80 @@ CG_D int adj_map(int i, int n, bool per) {
     return m < 0 ? 0 : (m >= n ? n - 1 : m);
 }
 
-template <class T, class S, bool PRIM, int AX, int LIM, int P, int W>
-__global__ void __launch_bounds__(P * W, (sizeof(T) == 4 ? 3 : 1)) adjoint_sweep_kernel(AdjSweepParams a) {
+// Loads and stores of the lines a thread carries: one (float, double), or two (f2) -- adjacent rows
+// (X sweep, two scalar accesses) or adjacent columns (Y sweep, one 8-byte access when both exist).
+// q0/q1 are the offsets of the two lines; an incomplete pair repeats the first line and stores it once.
+CG_D float ld_lanes(const float* p, size_t q0, size_t, bool, float) { return p[q0]; }
+CG_D double ld_lanes(const double* p, size_t q0, size_t, bool, double) { return p[q0]; }
+CG_D f2 ld_lanes(const float* p, size_t q0, size_t q1, bool vec, f2) {
+    if (vec) return f2{*reinterpret_cast<const float2*>(p + q0)};
+    return f2{make_float2(p[q0], p[q1])};
+}
+CG_D void st_lanes(float* p, size_t q0, size_t, bool, bool, float v) { p[q0] = v; }
+CG_D void st_lanes(double* p, size_t q0, size_t, bool, bool, double v) { p[q0] = v; }
+CG_D void st_lanes(float* p, size_t q0, size_t q1, bool vec, bool two, f2 v) {
+    if (vec) {
+        *reinterpret_cast<float2*>(p + q0) = v.v;
+    } else {
+        p[q0] = v.v.x;
+        if (two) p[q1] = v.v.y;
+    }
+}
+
+template <class V, class S, bool PRIM, int AX, int LIM, int P, int W>
+__global__ void __launch_bounds__(P * W, (Lane<V>::N == 2 ? 2 : (sizeof(V) == 4 ? 3 : 1)))
+    adjoint_sweep_kernel(AdjSweepParams a) {
+    using T = typename Lane<V>::S;
+    constexpr int NL = Lane<V>::N;
+    static_assert(!PRIM || NL == 1, "primitive storage is the FP64 one-line path");
     constexpr int TS = P - 8;
     constexpr int NW = P * W;
     extern __shared__ __align__(16) unsigned char adj_smem[];
-    T* sA = (T*)adj_smem;   // [5]  state
-    T* sB = sA + 5 * NW;    // [5]  Ubar' (phase 0-2), then the contribution to the right neighbour
-    T* sC = sB + 5 * NW;    // [10] A,B evolved states (1-2), then contributions to self and left neighbour
-    T* sD = sC + 10 * NW;   // [10] Abar of the right state, Bbar of the left state per face
+    V* sA = (V*)adj_smem;   // [5]  state
+    V* sB = sA + 5 * NW;    // [5]  Ubar' (phase 0-2), then the contribution to the right neighbour
+    V* sC = sB + 5 * NW;    // [10] A,B evolved states (1-2), then contributions to self and left neighbour
+    V* sD = sC + 10 * NW;   // [10] Abar of the right state, Bbar of the left state per face
     const Geom& G = a.G;
     const int along = AX == 0 ? threadIdx.x : threadIdx.y;
     const int across = AX == 0 ? threadIdx.y : threadIdx.x;
     const int n = AX == 0 ? G.nx : G.ny;
     const int nl = AX == 0 ? G.ny : G.nx;
-    const int line = (AX == 0 ? blockIdx.y : blockIdx.x) * W + across;
+    const int l0 = ((AX == 0 ? blockIdx.y : blockIdx.x) * W + across) * NL;
+    const bool lok = l0 < nl;
+    const bool two = NL == 2 && l0 + 1 < nl;  // the second lane carries a line of its own
+    const bool vec = AX == 1 && two;           // adjacent columns: one 8-byte access
+    const int l1 = two ? l0 + 1 : l0;
     const int s0 = (AX == 0 ? blockIdx.x : blockIdx.y) * TS;
     const int k = s0 - 4 + along;
-    const bool lok = line < nl;
     const bool per = G.bc == 1;
     // shared index of (across, position): positions contiguous for X, lines contiguous for Y
     auto si = [&](int pos) { return AX == 0 ? across * P + pos : pos * W + across; };
-    auto gi = [&](int pos) -> size_t {
+    auto gq = [&](int line, int pos) -> size_t {
         return AX == 0 ? (size_t)line * G.pitch + pos : (size_t)pos * G.pitch + line;
     };
     AdjCoef<T> K;
     if constexpr (sizeof(T) == 4) K = a.cf;
     else K = a.cd;
-    const AdjFlux<T> F{K.g1};
-    const T w = K.w, d = K.d, c = K.c, hs = K.hs;
+    const AdjFlux<V> F{bcv<V>(K.g1)};
+    const AdjSlope<V> Sl{bcv<V>(K.ca), bcv<V>(K.cb), bcv<V>(K.w1m), bcv<V>(K.w1p)};
+    const V d = bcv<V>(K.d), c = bcv<V>(K.c), hs = bcv<V>(K.hs);
+    const V zero = bcv<V>(0);
     const S* st = (const S*)a.state;
     const T* ubo = (const T*)a.ubar_out;
     const int me = si(along);
 
     // ---- 0: state and Ubar' at this position
-    T ub_own[5];
+    V ub_own[5];
     {
-        T u[5] = {T(1), T(0), T(0), T(0), T(1)};
-        T b[5] = {T(0), T(0), T(0), T(0), T(0)};
+        V u[5] = {bcv<V>(1), zero, zero, zero, bcv<V>(1)};
+        V b[5] = {zero, zero, zero, zero, zero};
         if (lok) {
-            const size_t q = gi(adj_map(k, n, per));
-            T v[5];
+            const int m = adj_map(k, n, per);
+            const size_t q0 = gq(l0, m), q1 = gq(l1, m);
+            if constexpr (PRIM) {  // Euler/EulerStateVector.cpp:55-66
+                T v[5];
 #pragma unroll
-            for (int f = 0; f < 5; f++) v[f] = T(st[f * G.fstride + q]);
-            if (PRIM) {  // Euler/EulerStateVector.cpp:55-66
+                for (int f = 0; f < 5; f++) v[f] = T(st[f * G.fstride + q0]);
                 u[0] = v[0];
                 u[1] = v[0] * v[1];
                 u[2] = v[0] * v[2];
@@ -277,11 +344,11 @@ __global__ void __launch_bounds__(P * W, (sizeof(T) == 4 ? 3 : 1)) adjoint_sweep
                 u[4] = v[0] * (T(0.5) * ((v[1] * v[1] + v[2] * v[2]) + v[3] * v[3]) + v[4] / (K.g1 * v[0]));
             } else {
 #pragma unroll
-                for (int f = 0; f < 5; f++) u[f] = v[f];
+                for (int f = 0; f < 5; f++) u[f] = ld_lanes(st + f * G.fstride, q0, q1, vec, V{});
             }
             if (per || (k >= 0 && k < n)) {
 #pragma unroll
-                for (int f = 0; f < 5; f++) b[f] = ubo[f * G.fstride + q];
+                for (int f = 0; f < 5; f++) b[f] = ld_lanes(ubo + f * G.fstride, q0, q1, vec, V{});
             }
         }
 #pragma unroll
@@ -292,18 +359,18 @@ __global__ void __launch_bounds__(P * W, (sizeof(T) == 4 ? 3 : 1)) adjoint_sweep
         }
     }
     __syncthreads();
-    auto ld = [&](const T* arr, int pos, T* out) {
+    auto ld = [&](const V* arr, int pos, V* out) {
         const int x = si(pos);
 #pragma unroll
         for (int f = 0; f < 5; f++) out[f] = arr[f * NW + x];
     };
     // ---- 1: half-step evolution of every cell with both neighbours in the tile
     if (lok && along >= 1 && along < P - 1) {
-        T ul[5], uc[5], ur[5], A[5], B[5];
+        V ul[5], uc[5], ur[5], A[5], B[5];
         ld(sA, along - 1, ul);
         ld(sA, along, uc);
         ld(sA, along + 1, ur);
-        adj_evolve<T, AX, LIM>(F, ul, uc, ur, w, hs, A, B);
+        adj_evolve<V, AX, LIM>(F, Sl, ul, uc, ur, hs, A, B);
 #pragma unroll
         for (int f = 0; f < 5; f++) {
             sC[f * NW + me] = A[f];
@@ -313,31 +380,31 @@ __global__ void __launch_bounds__(P * W, (sizeof(T) == 4 ? 3 : 1)) adjoint_sweep
     __syncthreads();
     // ---- 2: FORCE reverse at the face between this cell (k) and the next (k + 1)
     if (along >= 1 && along < P - 2) {
-        T Lb[5] = {T(0), T(0), T(0), T(0), T(0)}, Rb[5] = {T(0), T(0), T(0), T(0), T(0)};
+        V Lb[5] = {zero, zero, zero, zero, zero}, Rb[5] = {zero, zero, zero, zero, zero};
         if (lok && (per || (k >= -1 && k <= n - 1))) {
-            T L[5], R[5], Fb[5];
+            V L[5], R[5], Fb[5];
             const int nx1 = si(along + 1);
 #pragma unroll
             for (int f = 0; f < 5; f++) {
                 L[f] = sC[(5 + f) * NW + me];
                 R[f] = sC[f * NW + nx1];
-                Fb[f] = d * (sB[f * NW + nx1] - sB[f * NW + me]);
+                Fb[f] = vmul(d, vsub(sB[f * NW + nx1], sB[f * NW + me]));
             }
-            adj_force_vjp<T, AX>(F, L, R, c, d, Fb, Lb, Rb);
+            adj_force_vjp<V, AX>(F, L, R, c, d, Fb, Lb, Rb);
         }
 #pragma unroll
         for (int f = 0; f < 5; f++) {
-            sD[f * NW + me] = Lb[f];       // adjoint of B_k
-            sD[(5 + f) * NW + me] = Rb[f]; // adjoint of A_{k+1}
+            sD[f * NW + me] = Lb[f];        // adjoint of B_k
+            sD[(5 + f) * NW + me] = Rb[f];  // adjoint of A_{k+1}
         }
     }
     __syncthreads();
     // ---- 3: half-step reverse of this cell; neither sB nor sC is read in this phase
     if (along >= 2 && along < P - 2) {
-        T gl[5] = {T(0), T(0), T(0), T(0), T(0)}, gc[5] = {T(0), T(0), T(0), T(0), T(0)},
-          gr[5] = {T(0), T(0), T(0), T(0), T(0)};
+        V gl[5] = {zero, zero, zero, zero, zero}, gc[5] = {zero, zero, zero, zero, zero},
+          gr[5] = {zero, zero, zero, zero, zero};
         if (lok && (per || (k >= -1 && k <= n))) {
-            T ul[5], uc[5], ur[5], Ab[5], Bb[5];
+            V ul[5], uc[5], ur[5], Ab[5], Bb[5];
             ld(sA, along - 1, ul);
             ld(sA, along, uc);
             ld(sA, along + 1, ur);
@@ -347,7 +414,7 @@ __global__ void __launch_bounds__(P * W, (sizeof(T) == 4 ? 3 : 1)) adjoint_sweep
                 Bb[f] = sD[f * NW + me];
                 Ab[f] = sD[(5 + f) * NW + pv];
             }
-            adj_evolve_vjp<T, AX, LIM>(F, ul, uc, ur, w, hs, Ab, Bb, gl, gc, gr);
+            adj_evolve_vjp<V, AX, LIM>(F, Sl, ul, uc, ur, hs, Ab, Bb, gl, gc, gr);
         }
 #pragma unroll
         for (int f = 0; f < 5; f++) {
@@ -359,14 +426,15 @@ __global__ void __launch_bounds__(P * W, (sizeof(T) == 4 ? 3 : 1)) adjoint_sweep
     __syncthreads();
     // ---- 4: gather for the updated cells
     if (lok && along >= 4 && along < 4 + TS && k < n) {
-        T acc[5];
+        V acc[5];
 #pragma unroll
         for (int f = 0; f < 5; f++) acc[f] = ub_own[f];
         if (k >= 2 && k <= n - 3) {
             // interior (n >= 5): the right neighbour of k - 1, k itself, the left neighbour of k + 1
             const int xl = si(along - 1), xr = si(along + 1);
 #pragma unroll
-            for (int f = 0; f < 5; f++) acc[f] += (sB[f * NW + xl] + sC[f * NW + me]) + sC[(5 + f) * NW + xr];
+            for (int f = 0; f < 5; f++)
+                acc[f] = vadd(acc[f], vadd(vadd(sB[f * NW + xl], sC[f * NW + me]), sC[(5 + f) * NW + xr]));
         } else
 #pragma unroll
         for (int dd = -2; dd <= 2; dd++) {
@@ -378,15 +446,15 @@ __global__ void __launch_bounds__(P * W, (sizeof(T) == 4 ? 3 : 1)) adjoint_sweep
             for (int q = -1; q <= 1; q++) {
                 const int tgt = per ? ((i + q) % n + n) % n : (i + q < 0 ? -1 - (i + q) : (i + q >= n ? 2 * n - 1 - (i + q) : i + q));
                 if (tgt != k) continue;
-                const T* src = q == -1 ? sC + 5 * NW : (q == 0 ? sC : sB);
+                const V* src = q == -1 ? sC + 5 * NW : (q == 0 ? sC : sB);
 #pragma unroll
-                for (int f = 0; f < 5; f++) acc[f] += src[f * NW + x];
+                for (int f = 0; f < 5; f++) acc[f] = vadd(acc[f], src[f * NW + x]);
             }
         }
         T* ubi = (T*)a.ubar_in;
-        const size_t q = gi(k);
+        const size_t q0 = gq(l0, k), q1 = gq(l1, k);
 #pragma unroll
-        for (int f = 0; f < 5; f++) ubi[f * G.fstride + q] = acc[f];
+        for (int f = 0; f < 5; f++) st_lanes(ubi + f * G.fstride, q0, q1, vec, two, acc[f]);
     }
 }
 
@@ -456,15 +524,17 @@ __global__ void adjoint_grad_kernel(Geom G, double gamma, const S* state, const 
 
 namespace cg {
 
-// Launch the sweep adjoint for one axis.  Tiles of 256 threads (three resident per SM in FP32): X lines of
-// 256 positions (248 updated cells); Y lines of 64 positions (56 cells) x 4 adjacent columns.
-template <class T, class S, bool PRIM, int AX, int LIM>
+// Launch the sweep adjoint for one axis.  Tiles of 256 threads: X lines of 256 positions (248
+// updated cells); Y lines of 64 positions (56 cells) x 4 threads across.  FP32 carries two lines per
+// thread (f2: two rows for X, two adjacent columns for Y), FP64 one.
+template <class V, class S, bool PRIM, int AX, int LIM>
 cudaError_t launch_adjoint_sweep_t(const AdjSweepParams& a, cudaStream_t st) {
     constexpr int P = AX == 0 ? 256 : 64;
     constexpr int W = AX == 0 ? 1 : 4;
     constexpr int TS = P - 8;
-    const size_t smem = (size_t)30 * P * W * sizeof(T);
-    auto kern = adjoint_sweep_kernel<T, S, PRIM, AX, LIM, P, W>;
+    constexpr int LB = W * Lane<V>::N;  // lines per block
+    const size_t smem = (size_t)30 * P * W * sizeof(V);
+    auto kern = adjoint_sweep_kernel<V, S, PRIM, AX, LIM, P, W>;
     static bool attr_set = false;  // per instantiation; the attribute is per function and device-independent here
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -473,22 +543,22 @@ cudaError_t launch_adjoint_sweep_t(const AdjSweepParams& a, cudaStream_t st) {
     }
     const Geom& G = a.G;
     dim3 block = AX == 0 ? dim3(P, W) : dim3(W, P);
-    dim3 grid = AX == 0 ? dim3((G.nx + TS - 1) / TS, (G.ny + W - 1) / W) : dim3((G.nx + W - 1) / W, (G.ny + TS - 1) / TS);
+    dim3 grid = AX == 0 ? dim3((G.nx + TS - 1) / TS, (G.ny + LB - 1) / LB) : dim3((G.nx + LB - 1) / LB, (G.ny + TS - 1) / TS);
     kern<<<grid, block, smem, st>>>(a);
     return cudaGetLastError();
 }
 
-template <class T, class S, bool PRIM>
+template <class V, class S, bool PRIM>
 cudaError_t launch_adjoint_sweep_any(const AdjSweepParams& a, int lim, cudaStream_t st) {
     const int ax = a.G.axis;
     if (ax == 0) {
-        if (lim == 0) return launch_adjoint_sweep_t<T, S, PRIM, 0, 0>(a, st);
-        if (lim == 1) return launch_adjoint_sweep_t<T, S, PRIM, 0, 1>(a, st);
-        return launch_adjoint_sweep_t<T, S, PRIM, 0, 2>(a, st);
+        if (lim == 0) return launch_adjoint_sweep_t<V, S, PRIM, 0, 0>(a, st);
+        if (lim == 1) return launch_adjoint_sweep_t<V, S, PRIM, 0, 1>(a, st);
+        return launch_adjoint_sweep_t<V, S, PRIM, 0, 2>(a, st);
     }
-    if (lim == 0) return launch_adjoint_sweep_t<T, S, PRIM, 1, 0>(a, st);
-    if (lim == 1) return launch_adjoint_sweep_t<T, S, PRIM, 1, 1>(a, st);
-    return launch_adjoint_sweep_t<T, S, PRIM, 1, 2>(a, st);
+    if (lim == 0) return launch_adjoint_sweep_t<V, S, PRIM, 1, 0>(a, st);
+    if (lim == 1) return launch_adjoint_sweep_t<V, S, PRIM, 1, 1>(a, st);
+    return launch_adjoint_sweep_t<V, S, PRIM, 1, 2>(a, st);
 }
 
 template <class T, class S, bool PRIM>

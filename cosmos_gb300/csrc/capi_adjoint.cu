@@ -193,9 +193,12 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
             ap.dt = dt;
             {
                 const double gam = g->p.gamma, dx = g->p.dx;
-                ap.cd = AdjCoef<double>{gam - 1.0, gam, o->bias, dt / dx, dx / dt, 0.5 * (dt / dx)};
-                ap.cf = AdjCoef<float>{(float)ap.cd.g1, (float)ap.cd.gam, (float)ap.cd.w, (float)ap.cd.d, (float)ap.cd.c,
-                                       (float)ap.cd.hs};
+                const double w = o->bias;
+                ap.cd = AdjCoef<double>{gam - 1.0, gam,          w,       dt / dx, dx / dt, 0.5 * (dt / dx),
+                                        0.5 * (1.0 + w), 0.5 * (1.0 - w), 1.0 - w, 1.0 + w};
+                const AdjCoef<double>& D = ap.cd;
+                ap.cf = AdjCoef<float>{(float)D.g1, (float)D.gam, (float)D.w,   (float)D.d,   (float)D.c,
+                                       (float)D.hs, (float)D.ca,  (float)D.cb,  (float)D.w1m, (float)D.w1p};
             }
             ap.state = slot(c, q);
             ap.ubar_out = adj + (size_t)cur * abytes;

@@ -8,7 +8,7 @@ namespace cg {
 
 cudaError_t launch_adjoint_sweep_fast(const AdjSweepParams& a, int lim, cudaStream_t st) {
     count_launch();
-    return launch_adjoint_sweep_any<float, float, false>(a, lim, st);
+    return launch_adjoint_sweep_any<f2, float, false>(a, lim, st);
 }
 cudaError_t launch_adjoint_loss_fast(const Geom& G, const void* state, const double* target, void* ubar,
                                      double* row_sums, double* loss, cudaStream_t st) {
