@@ -20,8 +20,8 @@
 //
 // Line tiles: P positions along the sweep axis (TS = P - 8 updated cells plus a 4-cell halo on each
 // side) times W lines; one thread per position, five barrier-separated phases in shared memory:
-//   0 load state and Ubar'   1 half-step evolution   2 FORCE reverse per face
-//   3 half-step reverse per cell   4 gather per updated cell.
+//   0 load state and Ubar'   1 half-step evolution (keeping each cell's slope and reverse factors)
+//   2 FORCE reverse per face   3 half-step reverse per cell   4 gather per updated cell.
 #pragma once
 #include "device_common.cuh"
 #include "physics_fast.cuh"
@@ -40,6 +40,9 @@ CG_D double vmin(double a, double b) { return fmin(a, b); }
 CG_D double vmax(double a, double b) { return fmax(a, b); }
 CG_D double vabs(double a) { return fabs(a); }
 CG_D double vsel_lt(double a, double b, double x, double y) { return a < b ? x : y; }
+
+CG_D float adj_div(float a, float b) { return __fdividef(a, b); }
+CG_D double adj_div(double a, double b) { return a / b; }
 
 template <class V> struct Lane;
 template <> struct Lane<float> {
@@ -129,22 +132,32 @@ CG_D V limiter_d(const AdjSlope<V>& A, V r, V& d) {
     return vsel_lt(r, zero, zero, val);
 }
 
-// Half-step evolution of one cell: A (left-face) and B (right-face) states.
+// Half-step evolution of one cell: A (left-face) and B (right-face) states, and per field the three
+// numbers its reverse needs: the limited slope sl = xi(r) s and the factors P, Q with which the
+// slope adjoint slb reaches the two differences, dlb = slb P and drb = slb Q:
+//   P = a xi + s xi'(r) / den   (0 for the derivative term where |dl| < 1e-5: the clamped numerator)
+//   Q = b xi - s xi'(r) r / den (0 for the derivative term where |dr| < 1e-5)
 template <class V, int AX, int LIM>
 CG_D void adj_evolve(const AdjFlux<V>& F, const AdjSlope<V>& Sl, const V* ul, const V* uc, const V* ur, V hs, V* A,
-                     V* B) {
-    const V eps = bcv<V>(1e-5);
+                     V* B, V* sl, V* Pf, V* Qf) {
+    const V eps = bcv<V>(1e-5), zero = bcv<V>(0);
     V UL[5], UR[5];
 #pragma unroll
     for (int k = 0; k < 5; k++) {
         const V dl = vsub(uc[k], ul[k]), dr = vsub(ur[k], uc[k]);
         const V s = vfma(Sl.ca, dl, vmul(Sl.cb, dr));
-        const V num = vsel_lt(vabs(dl), eps, eps, dl);
-        const V den = vsel_lt(vabs(dr), eps, eps, dr);
+        const V adl = vabs(dl), adr = vabs(dr);
+        const V num = vsel_lt(adl, eps, eps, dl);
+        const V iden = vrcp(vsel_lt(adr, eps, eps, dr));
+        const V r = vmul(num, iden);
         V dxi;
-        const V sl = vmul(s, limiter_d<V, LIM>(Sl, vmul(num, vrcp(den)), dxi));
-        UL[k] = vfma(bcv<V>(-0.5), sl, uc[k]);
-        UR[k] = vfma(bcv<V>(0.5), sl, uc[k]);
+        const V xi = limiter_d<V, LIM>(Sl, r, dxi);
+        const V t = vmul(vmul(s, dxi), iden);
+        sl[k] = vmul(s, xi);
+        Pf[k] = vfma(Sl.ca, xi, vsel_lt(adl, eps, zero, t));
+        Qf[k] = vsub(vmul(Sl.cb, xi), vsel_lt(adr, eps, zero, vmul(t, r)));
+        UL[k] = vfma(bcv<V>(-0.5), sl[k], uc[k]);
+        UR[k] = vfma(bcv<V>(0.5), sl[k], uc[k]);
     }
     V FL[5], FR[5];
     F.template flux<AX>(UL, FL);
@@ -157,46 +170,28 @@ CG_D void adj_evolve(const AdjFlux<V>& F, const AdjSlope<V>& Sl, const V* ul, co
     }
 }
 
-// Reverse of adj_evolve: given Abar, Bbar, the contributions to the three stencil cells.
-template <class V, int AX, int LIM>
-CG_D void adj_evolve_vjp(const AdjFlux<V>& F, const AdjSlope<V>& Sl, const V* ul, const V* uc, const V* ur, V hs,
-                         const V* Ab, const V* Bb, V* gl, V* gc, V* gr) {
-    const V eps = bcv<V>(1e-5), zero = bcv<V>(0);
-    V UL[5], UR[5], sv[5], xi[5], dxi[5], r[5], iden[5], adl[5], adr[5];
+// Reverse of adj_evolve: given Abar, Bbar and the cell's (sl, P, Q), the contributions to the three
+// stencil cells.
+template <class V, int AX>
+CG_D void adj_evolve_vjp(const AdjFlux<V>& F, const V* uc, const V* sl, const V* Pf, const V* Qf, V hs, const V* Ab,
+                         const V* Bb, V* gl, V* gc, V* gr) {
+    V UL[5], UR[5], ULb[5], URb[5], FLb[5], FRb[5];
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-        const V dl = vsub(uc[k], ul[k]), dr = vsub(ur[k], uc[k]);
-        sv[k] = vfma(Sl.ca, dl, vmul(Sl.cb, dr));
-        adl[k] = vabs(dl);
-        adr[k] = vabs(dr);
-        const V num = vsel_lt(adl[k], eps, eps, dl);
-        iden[k] = vrcp(vsel_lt(adr[k], eps, eps, dr));
-        r[k] = vmul(num, iden[k]);
-        xi[k] = limiter_d<V, LIM>(Sl, r[k], dxi[k]);
-        const V sl = vmul(sv[k], xi[k]);
-        UL[k] = vfma(bcv<V>(-0.5), sl, uc[k]);
-        UR[k] = vfma(bcv<V>(0.5), sl, uc[k]);
-    }
-    V ULb[5], URb[5], FLb[5], FRb[5];
-#pragma unroll
-    for (int k = 0; k < 5; k++) {
+        UL[k] = vfma(bcv<V>(-0.5), sl[k], uc[k]);
+        UR[k] = vfma(bcv<V>(0.5), sl[k], uc[k]);
         const V eb = vadd(Ab[k], Bb[k]);
         ULb[k] = Ab[k];
         URb[k] = Bb[k];
         FLb[k] = vmul(hs, eb);
-        FRb[k] = vmul(bcv<V>(-1), vmul(hs, eb));
+        FRb[k] = vmul(bcv<V>(-1), FLb[k]);
     }
     F.template vjp<AX>(UL, FLb, ULb);
     F.template vjp<AX>(UR, FRb, URb);
 #pragma unroll
     for (int k = 0; k < 5; k++) {
         const V slb = vmul(bcv<V>(0.5), vsub(URb[k], ULb[k]));
-        const V xib = vmul(slb, sv[k]);
-        const V sb = vmul(slb, xi[k]);
-        const V rb = vmul(xib, dxi[k]);
-        // the clamped differences carry no derivative
-        const V dlb = vfma(Sl.ca, sb, vsel_lt(adl[k], eps, zero, vmul(rb, iden[k])));
-        const V drb = vsub(vmul(Sl.cb, sb), vsel_lt(adr[k], eps, zero, vmul(vmul(rb, r[k]), iden[k])));
+        const V dlb = vmul(slb, Pf[k]), drb = vmul(slb, Qf[k]);
         gl[k] = vmul(bcv<V>(-1), dlb);
         gc[k] = vadd(vadd(ULb[k], URb[k]), vsub(dlb, drb));
         gr[k] = drb;
@@ -296,6 +291,7 @@ __global__ void __launch_bounds__(P * W, (Lane<V>::N == 2 ? 2 : (sizeof(V) == 4 
     V* sB = sA + 5 * NW;    // [5]  Ubar' (phase 0-2), then the contribution to the right neighbour
     V* sC = sB + 5 * NW;    // [10] A,B evolved states (1-2), then contributions to self and left neighbour
     V* sD = sC + 10 * NW;   // [10] Abar of the right state, Bbar of the left state per face
+    V* sE = sD + 10 * NW;   // [15] slope sl and reverse factors P, Q of each cell (phase 1 -> 3)
     const Geom& G = a.G;
     const int along = AX == 0 ? threadIdx.x : threadIdx.y;
     const int across = AX == 0 ? threadIdx.y : threadIdx.x;
@@ -366,15 +362,18 @@ __global__ void __launch_bounds__(P * W, (Lane<V>::N == 2 ? 2 : (sizeof(V) == 4 
     };
     // ---- 1: half-step evolution of every cell with both neighbours in the tile
     if (lok && along >= 1 && along < P - 1) {
-        V ul[5], uc[5], ur[5], A[5], B[5];
+        V ul[5], uc[5], ur[5], A[5], B[5], sl[5], Pf[5], Qf[5];
         ld(sA, along - 1, ul);
         ld(sA, along, uc);
         ld(sA, along + 1, ur);
-        adj_evolve<V, AX, LIM>(F, Sl, ul, uc, ur, hs, A, B);
+        adj_evolve<V, AX, LIM>(F, Sl, ul, uc, ur, hs, A, B, sl, Pf, Qf);
 #pragma unroll
         for (int f = 0; f < 5; f++) {
             sC[f * NW + me] = A[f];
             sC[(5 + f) * NW + me] = B[f];
+            sE[f * NW + me] = sl[f];
+            sE[(5 + f) * NW + me] = Pf[f];
+            sE[(10 + f) * NW + me] = Qf[f];
         }
     }
     __syncthreads();
@@ -404,17 +403,18 @@ __global__ void __launch_bounds__(P * W, (Lane<V>::N == 2 ? 2 : (sizeof(V) == 4 
         V gl[5] = {zero, zero, zero, zero, zero}, gc[5] = {zero, zero, zero, zero, zero},
           gr[5] = {zero, zero, zero, zero, zero};
         if (lok && (per || (k >= -1 && k <= n))) {
-            V ul[5], uc[5], ur[5], Ab[5], Bb[5];
-            ld(sA, along - 1, ul);
+            V uc[5], sl[5], Pf[5], Qf[5], Ab[5], Bb[5];
             ld(sA, along, uc);
-            ld(sA, along + 1, ur);
+            ld(sE, along, sl);
+            ld(sE + 5 * NW, along, Pf);
+            ld(sE + 10 * NW, along, Qf);
             const int pv = si(along - 1);
 #pragma unroll
             for (int f = 0; f < 5; f++) {
                 Bb[f] = sD[f * NW + me];
                 Ab[f] = sD[(5 + f) * NW + pv];
             }
-            adj_evolve_vjp<V, AX, LIM>(F, Sl, ul, uc, ur, hs, Ab, Bb, gl, gc, gr);
+            adj_evolve_vjp<V, AX>(F, uc, sl, Pf, Qf, hs, Ab, Bb, gl, gc, gr);
         }
 #pragma unroll
         for (int f = 0; f < 5; f++) {
@@ -483,40 +483,45 @@ __global__ void __launch_bounds__(256) adjoint_loss_kernel(Geom G, const S* stat
     if (threadIdx.x == 0) row_sums[i] = red[0];
 }
 
+// Fixed-order sum of the row sums: lane l adds rows l, l + 32, ... in order, then a fixed shuffle tree.
 static __global__ void __launch_bounds__(32) adjoint_loss_final_kernel(const double* row_sums, int n, double* loss) {
-    if (threadIdx.x != 0) return;
     double s = 0.0;
-    for (int i = 0; i < n; i++) s += row_sums[i];
-    *loss = s;
+    for (int i = threadIdx.x; i < n; i += 32) s += row_sums[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) *loss = s;
 }
 
 // Gradient with respect to the initial primitives: Pbar = (dU/dP)^T Ubar at the initial state,
-// written as AoS doubles (the layout of cosmos_grid_set_prim).
+// written as AoS doubles (the layout of cosmos_grid_set_prim), evaluated in the adjoint's precision T
+// (1/(gamma - 1) formed on the host for FP32).
 template <class T, class S, bool PRIM>
-__global__ void adjoint_grad_kernel(Geom G, double gamma, const S* state, const T* ubar, double* grad) {
+__global__ void adjoint_grad_kernel(Geom G, double gamma, T ig1, const S* state, const T* ubar, double* grad) {
     const size_t ncell = (size_t)G.nx * G.ny;
     for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x) {
         const int i = (int)(c / G.nx), j = (int)(c % G.nx);
         const size_t q = (size_t)i * G.pitch + j;
-        double v[5], u[5];
+        T v[5], u[5];
 #pragma unroll
         for (int f = 0; f < 5; f++) {
-            v[f] = (double)state[f * G.fstride + q];
-            u[f] = (double)ubar[f * G.fstride + q];
+            v[f] = (T)state[f * G.fstride + q];
+            u[f] = ubar[f * G.fstride + q];
         }
-        double rho, vx, vy, vz;
+        T rho, vx, vy, vz;
         if (PRIM) {
             rho = v[0]; vx = v[1]; vy = v[2]; vz = v[3];
         } else {
-            rho = v[0]; vx = v[1] / rho; vy = v[2] / rho; vz = v[3] / rho;
+            rho = v[0];
+            const T ir = adj_div(T(1), rho);
+            vx = v[1] * ir; vy = v[2] * ir; vz = v[3] * ir;
         }
-        const double vv = vx * vx + vy * vy + vz * vz;
+        const T vv = vx * vx + vy * vy + vz * vz;
         double* o = grad + 5 * c;
-        o[0] = u[0] + u[1] * vx + u[2] * vy + u[3] * vz + u[4] * 0.5 * vv;
-        o[1] = rho * (u[1] + u[4] * vx);
-        o[2] = rho * (u[2] + u[4] * vy);
-        o[3] = rho * (u[3] + u[4] * vz);
-        o[4] = u[4] / (gamma - 1.0);
+        o[0] = (double)(u[0] + u[1] * vx + u[2] * vy + u[3] * vz + u[4] * T(0.5) * vv);
+        o[1] = (double)(rho * (u[1] + u[4] * vx));
+        o[2] = (double)(rho * (u[2] + u[4] * vy));
+        o[3] = (double)(rho * (u[3] + u[4] * vz));
+        o[4] = sizeof(T) == 8 ? (double)u[4] / (gamma - 1.0) : (double)(u[4] * ig1);
     }
 }
 
@@ -533,7 +538,7 @@ cudaError_t launch_adjoint_sweep_t(const AdjSweepParams& a, cudaStream_t st) {
     constexpr int W = AX == 0 ? 1 : 4;
     constexpr int TS = P - 8;
     constexpr int LB = W * Lane<V>::N;  // lines per block
-    const size_t smem = (size_t)30 * P * W * sizeof(V);
+    const size_t smem = (size_t)45 * P * W * sizeof(V);
     auto kern = adjoint_sweep_kernel<V, S, PRIM, AX, LIM, P, W>;
     static bool attr_set = false;  // per instantiation; the attribute is per function and device-independent here
     if (!attr_set) {
@@ -574,7 +579,8 @@ cudaError_t launch_adjoint_grad_t(const Geom& G, double gamma, const void* state
                                   cudaStream_t st) {
     const size_t ncell = (size_t)G.nx * G.ny;
     const int blocks = (int)std::min<size_t>((ncell + 255) / 256, 152 * 16);
-    adjoint_grad_kernel<T, S, PRIM><<<blocks, 256, 0, st>>>(G, gamma, (const S*)state, (const T*)ubar, grad);
+    adjoint_grad_kernel<T, S, PRIM>
+        <<<blocks, 256, 0, st>>>(G, gamma, T(1.0 / (gamma - 1.0)), (const S*)state, (const T*)ubar, grad);
     return cudaGetLastError();
 }
 
