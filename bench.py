@@ -498,19 +498,35 @@ def adjoint_measure(cg, ctx, n=2048, nsteps=100, every=10):
     gq.set_prim(q0)
     _, grad, dts, _ = gq.adjoint(tq, nsteps, 0.9, 0.0, cg.MINBEE, checkpoint_every=every)
     d = np.random.default_rng(79).standard_normal(q0.shape)
-    h = 1e-8  # small: the map is piecewise smooth (limiter branches), FP64 round-off stays ~1e-8
-    ls = []
-    for sgn in (1.0, -1.0):
-        gq.set_prim(q0 + sgn * h * d)
-        ls.append(gq.adjoint(tq, nsteps, 0.9, 0.0, cg.MINBEE, checkpoint_every=every, dts=dts)[0])
+    # The step map is piecewise smooth (limiter branches): a central difference whose +-h stencil
+    # crosses a branch point measures neither one-sided derivative.  h shrinks by decades until two
+    # successive differences agree to 1e-5 (no crossing in either stencil, round-off still small);
+    # the larger h of that pair is reported.
+    def central(h):
+        ls = []
+        for sgn in (1.0, -1.0):
+            gq.set_prim(q0 + sgn * h * d)
+            ls.append(gq.adjoint(tq, nsteps, 0.9, 0.0, cg.MINBEE, checkpoint_every=every, dts=dts)[0])
+        return (ls[0] - ls[1]) / (2 * h)
+    hs = [1e-6, 1e-7, 1e-8, 1e-9, 1e-10]
+    fds = [central(hs[0])]
+    h, fd = hs[-1], None
+    for i in range(1, len(hs)):
+        fds.append(central(hs[i]))
+        if abs(fds[i] - fds[i - 1]) <= 1e-5 * abs(fds[i]):
+            h, fd = hs[i - 1], fds[i - 1]
+            break
+    if fd is None:
+        fd = fds[-1]
     gq.close()
-    fd = (ls[0] - ls[1]) / (2 * h)
     an = float(np.sum(grad * d))
     return {"grid": f"{n}x{n} FP32, seeded Riemann data", "steps": nsteps, "checkpoint_every": every,
             "forward_ms": fwd, "backward_ms": bwd, "adjoint_over_forward": bwd / fwd,
             "what": "backward = recomputation of each checkpoint segment + the sweep adjoints, per forward "
                     "pass of the same steps (graph-replayed, checkpoints stored)",
             "fd_check": {"grid": f"{m}x{m} FP64 smooth data", "steps": nsteps, "h": h,
+                         "rule": "h = 1e-6, 1e-7, ... until two successive central differences agree to 1e-5",
+                         "fd_by_h": {f"{x:.0e}": v for x, v in zip(hs, fds)},
                          "directional_adjoint": an, "directional_fd": fd, "rel_err": abs(fd - an) / abs(an)}}
 
 

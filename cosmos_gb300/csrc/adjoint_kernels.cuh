@@ -20,7 +20,8 @@
 //
 // Line tiles: P positions along the sweep axis (TS = P - 8 updated cells plus a 4-cell halo on each
 // side) times W lines; one thread per position, five barrier-separated phases in shared memory:
-//   0 load state and Ubar'   1 half-step evolution (keeping each cell's slope and reverse factors)
+//   0 store state and Ubar' (loaded while the previous tile was computed)
+//   1 half-step evolution (keeping each cell's slope and reverse factors)
 //   2 FORCE reverse per face   3 half-step reverse per cell   4 gather per updated cell.
 #pragma once
 #include "device_common.cuh"
@@ -41,7 +42,7 @@ CG_D double vmax(double a, double b) { return fmax(a, b); }
 CG_D double vabs(double a) { return fabs(a); }
 CG_D double vsel_lt(double a, double b, double x, double y) { return a < b ? x : y; }
 
-CG_D float adj_div(float a, float b) { return __fdividef(a, b); }
+CG_D float adj_div(float a, float b) { return fdiv(a, b); }
 CG_D double adj_div(double a, double b) { return a / b; }
 
 template <class V> struct Lane;
@@ -297,13 +298,8 @@ __global__ void __launch_bounds__(P * W, (Lane<V>::N == 2 ? 2 : (sizeof(V) == 4 
     const int across = AX == 0 ? threadIdx.y : threadIdx.x;
     const int n = AX == 0 ? G.nx : G.ny;
     const int nl = AX == 0 ? G.ny : G.nx;
-    const int l0 = ((AX == 0 ? blockIdx.y : blockIdx.x) * W + across) * NL;
-    const bool lok = l0 < nl;
-    const bool two = NL == 2 && l0 + 1 < nl;  // the second lane carries a line of its own
-    const bool vec = AX == 1 && two;           // adjacent columns: one 8-byte access
-    const int l1 = two ? l0 + 1 : l0;
-    const int s0 = (AX == 0 ? blockIdx.x : blockIdx.y) * TS;
-    const int k = s0 - 4 + along;
+    const int ntile_s = (n + TS - 1) / TS;             // tiles along the sweep axis
+    const int ntiles = ntile_s * ((nl + W * NL - 1) / (W * NL));
     const bool per = G.bc == 1;
     // shared index of (across, position): positions contiguous for X, lines contiguous for Y
     auto si = [&](int pos) { return AX == 0 ? across * P + pos : pos * W + across; };
@@ -321,18 +317,53 @@ __global__ void __launch_bounds__(P * W, (Lane<V>::N == 2 ? 2 : (sizeof(V) == 4 
     const T* ubo = (const T*)a.ubar_out;
     const int me = si(along);
 
-    // ---- 0: state and Ubar' at this position
-    V ub_own[5];
-    {
-        V u[5] = {bcv<V>(1), zero, zero, zero, bcv<V>(1)};
-        V b[5] = {zero, zero, zero, zero, zero};
-        if (lok) {
-            const int m = adj_map(k, n, per);
-            const size_t q0 = gq(l0, m), q1 = gq(l1, m);
-            if constexpr (PRIM) {  // Euler/EulerStateVector.cpp:55-66
-                T v[5];
+    // This thread's place in tile t: position k along the sweep, lines l0 and l1 (= l0 when the
+    // second lane has no line of its own).
+    struct Place {
+        int k, l0, l1;
+        bool lok, two, vec;
+    };
+    auto place = [&](int t) {
+        Place q;
+        q.l0 = ((t / ntile_s) * W + across) * NL;
+        q.lok = q.l0 < nl;
+        q.two = NL == 2 && q.l0 + 1 < nl;
+        q.vec = AX == 1 && q.two;  // adjacent columns: one 8-byte access
+        q.l1 = q.two ? q.l0 + 1 : q.l0;
+        q.k = (t % ntile_s) * TS - 4 + along;
+        return q;
+    };
+    // Inputs at a place, as stored (FP64: primitives), fetched one tile ahead into registers.
+    V ru[5], rb[5];
+    auto fetch = [&](const Place& q) {
+        ru[0] = ru[4] = bcv<V>(1);
+        ru[1] = ru[2] = ru[3] = zero;
 #pragma unroll
-                for (int f = 0; f < 5; f++) v[f] = T(st[f * G.fstride + q0]);
+        for (int f = 0; f < 5; f++) rb[f] = zero;
+        if (q.lok) {
+            const int m = adj_map(q.k, n, per);
+            const size_t q0 = gq(q.l0, m), q1 = gq(q.l1, m);
+#pragma unroll
+            for (int f = 0; f < 5; f++) ru[f] = ld_lanes(st + f * G.fstride, q0, q1, q.vec, V{});
+            if (per || (q.k >= 0 && q.k < n)) {
+#pragma unroll
+                for (int f = 0; f < 5; f++) rb[f] = ld_lanes(ubo + f * G.fstride, q0, q1, q.vec, V{});
+            }
+        }
+    };
+
+    int t = blockIdx.x;
+    if (t < ntiles) fetch(place(t));
+    for (; t < ntiles; t += gridDim.x) {
+        const Place q = place(t);
+        const int k = q.k;
+        const bool lok = q.lok;
+        // ---- 0: state and Ubar' at this position
+        V ub_own[5];
+        {
+            V u[5];
+            if constexpr (PRIM) {  // Euler/EulerStateVector.cpp:55-66
+                const T* v = ru;
                 u[0] = v[0];
                 u[1] = v[0] * v[1];
                 u[2] = v[0] * v[2];
@@ -340,121 +371,120 @@ __global__ void __launch_bounds__(P * W, (Lane<V>::N == 2 ? 2 : (sizeof(V) == 4 
                 u[4] = v[0] * (T(0.5) * ((v[1] * v[1] + v[2] * v[2]) + v[3] * v[3]) + v[4] / (K.g1 * v[0]));
             } else {
 #pragma unroll
-                for (int f = 0; f < 5; f++) u[f] = ld_lanes(st + f * G.fstride, q0, q1, vec, V{});
+                for (int f = 0; f < 5; f++) u[f] = ru[f];
             }
-            if (per || (k >= 0 && k < n)) {
-#pragma unroll
-                for (int f = 0; f < 5; f++) b[f] = ld_lanes(ubo + f * G.fstride, q0, q1, vec, V{});
-            }
-        }
-#pragma unroll
-        for (int f = 0; f < 5; f++) {
-            sA[f * NW + me] = u[f];
-            sB[f * NW + me] = b[f];
-            ub_own[f] = b[f];
-        }
-    }
-    __syncthreads();
-    auto ld = [&](const V* arr, int pos, V* out) {
-        const int x = si(pos);
-#pragma unroll
-        for (int f = 0; f < 5; f++) out[f] = arr[f * NW + x];
-    };
-    // ---- 1: half-step evolution of every cell with both neighbours in the tile
-    if (lok && along >= 1 && along < P - 1) {
-        V ul[5], uc[5], ur[5], A[5], B[5], sl[5], Pf[5], Qf[5];
-        ld(sA, along - 1, ul);
-        ld(sA, along, uc);
-        ld(sA, along + 1, ur);
-        adj_evolve<V, AX, LIM>(F, Sl, ul, uc, ur, hs, A, B, sl, Pf, Qf);
-#pragma unroll
-        for (int f = 0; f < 5; f++) {
-            sC[f * NW + me] = A[f];
-            sC[(5 + f) * NW + me] = B[f];
-            sE[f * NW + me] = sl[f];
-            sE[(5 + f) * NW + me] = Pf[f];
-            sE[(10 + f) * NW + me] = Qf[f];
-        }
-    }
-    __syncthreads();
-    // ---- 2: FORCE reverse at the face between this cell (k) and the next (k + 1)
-    if (along >= 1 && along < P - 2) {
-        V Lb[5] = {zero, zero, zero, zero, zero}, Rb[5] = {zero, zero, zero, zero, zero};
-        if (lok && (per || (k >= -1 && k <= n - 1))) {
-            V L[5], R[5], Fb[5];
-            const int nx1 = si(along + 1);
 #pragma unroll
             for (int f = 0; f < 5; f++) {
-                L[f] = sC[(5 + f) * NW + me];
-                R[f] = sC[f * NW + nx1];
-                Fb[f] = vmul(d, vsub(sB[f * NW + nx1], sB[f * NW + me]));
+                sA[f * NW + me] = u[f];
+                sB[f * NW + me] = rb[f];
+                ub_own[f] = rb[f];
             }
-            adj_force_vjp<V, AX>(F, L, R, c, d, Fb, Lb, Rb);
         }
+        __syncthreads();
+        // the next tile's inputs load while this one is computed
+        if (t + (int)gridDim.x < ntiles) fetch(place(t + gridDim.x));
+        auto ld = [&](const V* arr, int pos, V* out) {
+            const int x = si(pos);
 #pragma unroll
-        for (int f = 0; f < 5; f++) {
-            sD[f * NW + me] = Lb[f];        // adjoint of B_k
-            sD[(5 + f) * NW + me] = Rb[f];  // adjoint of A_{k+1}
-        }
-    }
-    __syncthreads();
-    // ---- 3: half-step reverse of this cell; neither sB nor sC is read in this phase
-    if (along >= 2 && along < P - 2) {
-        V gl[5] = {zero, zero, zero, zero, zero}, gc[5] = {zero, zero, zero, zero, zero},
-          gr[5] = {zero, zero, zero, zero, zero};
-        if (lok && (per || (k >= -1 && k <= n))) {
-            V uc[5], sl[5], Pf[5], Qf[5], Ab[5], Bb[5];
+            for (int f = 0; f < 5; f++) out[f] = arr[f * NW + x];
+        };
+        // ---- 1: half-step evolution of every cell with both neighbours in the tile
+        if (lok && along >= 1 && along < P - 1) {
+            V ul[5], uc[5], ur[5], A[5], B[5], sl[5], Pf[5], Qf[5];
+            ld(sA, along - 1, ul);
             ld(sA, along, uc);
-            ld(sE, along, sl);
-            ld(sE + 5 * NW, along, Pf);
-            ld(sE + 10 * NW, along, Qf);
-            const int pv = si(along - 1);
+            ld(sA, along + 1, ur);
+            adj_evolve<V, AX, LIM>(F, Sl, ul, uc, ur, hs, A, B, sl, Pf, Qf);
 #pragma unroll
             for (int f = 0; f < 5; f++) {
-                Bb[f] = sD[f * NW + me];
-                Ab[f] = sD[(5 + f) * NW + pv];
-            }
-            adj_evolve_vjp<V, AX>(F, uc, sl, Pf, Qf, hs, Ab, Bb, gl, gc, gr);
-        }
-#pragma unroll
-        for (int f = 0; f < 5; f++) {
-            sC[f * NW + me] = gc[f];
-            sC[(5 + f) * NW + me] = gl[f];
-            sB[f * NW + me] = gr[f];
-        }
-    }
-    __syncthreads();
-    // ---- 4: gather for the updated cells
-    if (lok && along >= 4 && along < 4 + TS && k < n) {
-        V acc[5];
-#pragma unroll
-        for (int f = 0; f < 5; f++) acc[f] = ub_own[f];
-        if (k >= 2 && k <= n - 3) {
-            // interior (n >= 5): the right neighbour of k - 1, k itself, the left neighbour of k + 1
-            const int xl = si(along - 1), xr = si(along + 1);
-#pragma unroll
-            for (int f = 0; f < 5; f++)
-                acc[f] = vadd(acc[f], vadd(vadd(sB[f * NW + xl], sC[f * NW + me]), sC[(5 + f) * NW + xr]));
-        } else
-#pragma unroll
-        for (int dd = -2; dd <= 2; dd++) {
-            const int i = k + dd;
-            if (!per && (i < -1 || i > n)) continue;
-            if (per && dd - n >= -2) continue;  // same physical cell as an earlier dd (n <= 4)
-            const int x = si(along + dd);
-#pragma unroll
-            for (int q = -1; q <= 1; q++) {
-                const int tgt = per ? ((i + q) % n + n) % n : (i + q < 0 ? -1 - (i + q) : (i + q >= n ? 2 * n - 1 - (i + q) : i + q));
-                if (tgt != k) continue;
-                const V* src = q == -1 ? sC + 5 * NW : (q == 0 ? sC : sB);
-#pragma unroll
-                for (int f = 0; f < 5; f++) acc[f] = vadd(acc[f], src[f * NW + x]);
+                sC[f * NW + me] = A[f];
+                sC[(5 + f) * NW + me] = B[f];
+                sE[f * NW + me] = sl[f];
+                sE[(5 + f) * NW + me] = Pf[f];
+                sE[(10 + f) * NW + me] = Qf[f];
             }
         }
-        T* ubi = (T*)a.ubar_in;
-        const size_t q0 = gq(l0, k), q1 = gq(l1, k);
+        __syncthreads();
+        // ---- 2: FORCE reverse at the face between this cell (k) and the next (k + 1)
+        if (along >= 1 && along < P - 2) {
+            V Lb[5] = {zero, zero, zero, zero, zero}, Rb[5] = {zero, zero, zero, zero, zero};
+            if (lok && (per || (k >= -1 && k <= n - 1))) {
+                V L[5], R[5], Fb[5];
+                const int nx1 = si(along + 1);
 #pragma unroll
-        for (int f = 0; f < 5; f++) st_lanes(ubi + f * G.fstride, q0, q1, vec, two, acc[f]);
+                for (int f = 0; f < 5; f++) {
+                    L[f] = sC[(5 + f) * NW + me];
+                    R[f] = sC[f * NW + nx1];
+                    Fb[f] = vmul(d, vsub(sB[f * NW + nx1], sB[f * NW + me]));
+                }
+                adj_force_vjp<V, AX>(F, L, R, c, d, Fb, Lb, Rb);
+            }
+#pragma unroll
+            for (int f = 0; f < 5; f++) {
+                sD[f * NW + me] = Lb[f];        // adjoint of B_k
+                sD[(5 + f) * NW + me] = Rb[f];  // adjoint of A_{k+1}
+            }
+        }
+        __syncthreads();
+        // ---- 3: half-step reverse of this cell; neither sB nor sC is read in this phase
+        if (along >= 2 && along < P - 2) {
+            V gl[5] = {zero, zero, zero, zero, zero}, gc[5] = {zero, zero, zero, zero, zero},
+              gr[5] = {zero, zero, zero, zero, zero};
+            if (lok && (per || (k >= -1 && k <= n))) {
+                V uc[5], sl[5], Pf[5], Qf[5], Ab[5], Bb[5];
+                ld(sA, along, uc);
+                ld(sE, along, sl);
+                ld(sE + 5 * NW, along, Pf);
+                ld(sE + 10 * NW, along, Qf);
+                const int pv = si(along - 1);
+#pragma unroll
+                for (int f = 0; f < 5; f++) {
+                    Bb[f] = sD[f * NW + me];
+                    Ab[f] = sD[(5 + f) * NW + pv];
+                }
+                adj_evolve_vjp<V, AX>(F, uc, sl, Pf, Qf, hs, Ab, Bb, gl, gc, gr);
+            }
+#pragma unroll
+            for (int f = 0; f < 5; f++) {
+                sC[f * NW + me] = gc[f];
+                sC[(5 + f) * NW + me] = gl[f];
+                sB[f * NW + me] = gr[f];
+            }
+        }
+        __syncthreads();
+        // ---- 4: gather for the updated cells
+        if (lok && along >= 4 && along < 4 + TS && k < n) {
+            V acc[5];
+#pragma unroll
+            for (int f = 0; f < 5; f++) acc[f] = ub_own[f];
+            if (k >= 2 && k <= n - 3) {
+                // interior (n >= 5): the right neighbour of k - 1, k itself, the left neighbour of k + 1
+                const int xl = si(along - 1), xr = si(along + 1);
+#pragma unroll
+                for (int f = 0; f < 5; f++)
+                    acc[f] = vadd(acc[f], vadd(vadd(sB[f * NW + xl], sC[f * NW + me]), sC[(5 + f) * NW + xr]));
+            } else
+#pragma unroll
+            for (int dd = -2; dd <= 2; dd++) {
+                const int i = k + dd;
+                if (!per && (i < -1 || i > n)) continue;
+                if (per && dd - n >= -2) continue;  // same physical cell as an earlier dd (n <= 4)
+                const int x = si(along + dd);
+#pragma unroll
+                for (int q = -1; q <= 1; q++) {
+                    const int tgt = per ? ((i + q) % n + n) % n : (i + q < 0 ? -1 - (i + q) : (i + q >= n ? 2 * n - 1 - (i + q) : i + q));
+                    if (tgt != k) continue;
+                    const V* src = q == -1 ? sC + 5 * NW : (q == 0 ? sC : sB);
+#pragma unroll
+                    for (int f = 0; f < 5; f++) acc[f] = vadd(acc[f], src[f * NW + x]);
+                }
+            }
+            T* ubi = (T*)a.ubar_in;
+            const size_t q0 = gq(q.l0, k), q1 = gq(q.l1, k);
+#pragma unroll
+            for (int f = 0; f < 5; f++) st_lanes(ubi + f * G.fstride, q0, q1, q.vec, q.two, acc[f]);
+        }
+        __syncthreads();  // phase 4 reads sB and sC, which the next tile's phases 0 and 1 overwrite
     }
 }
 
@@ -531,7 +561,8 @@ namespace cg {
 
 // Launch the sweep adjoint for one axis.  Tiles of 256 threads: X lines of 256 positions (248
 // updated cells); Y lines of 64 positions (56 cells) x 4 threads across.  FP32 carries two lines per
-// thread (f2: two rows for X, two adjacent columns for Y), FP64 one.
+// thread (f2: two rows for X, two adjacent columns for Y), FP64 one.  Persistent: as many blocks as
+// stay resident, each walking tiles t, t + gridDim.x, ... with the next tile's inputs in flight.
 template <class V, class S, bool PRIM, int AX, int LIM>
 cudaError_t launch_adjoint_sweep_t(const AdjSweepParams& a, cudaStream_t st) {
     constexpr int P = AX == 0 ? 256 : 64;
@@ -540,16 +571,23 @@ cudaError_t launch_adjoint_sweep_t(const AdjSweepParams& a, cudaStream_t st) {
     constexpr int LB = W * Lane<V>::N;  // lines per block
     const size_t smem = (size_t)45 * P * W * sizeof(V);
     auto kern = adjoint_sweep_kernel<V, S, PRIM, AX, LIM, P, W>;
-    static bool attr_set = false;  // per instantiation; the attribute is per function and device-independent here
-    if (!attr_set) {
+    // per instantiation: the attribute and the resident-block count (one GPU model per process)
+    static int resident = 0;
+    if (!resident) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        attr_set = true;
+        int dev = 0, sms = 0, per = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, P * W, smem)) != cudaSuccess) return e;
+        resident = sms * std::max(per, 1);
     }
     const Geom& G = a.G;
+    const int n = AX == 0 ? G.nx : G.ny, nl = AX == 0 ? G.ny : G.nx;
+    const long long ntiles = (long long)((n + TS - 1) / TS) * ((nl + LB - 1) / LB);
+    const int blocks = (int)std::min<long long>(ntiles, resident);
     dim3 block = AX == 0 ? dim3(P, W) : dim3(W, P);
-    dim3 grid = AX == 0 ? dim3((G.nx + TS - 1) / TS, (G.ny + LB - 1) / LB) : dim3((G.nx + LB - 1) / LB, (G.ny + TS - 1) / TS);
-    kern<<<grid, block, smem, st>>>(a);
+    kern<<<blocks, block, smem, st>>>(a);
     return cudaGetLastError();
 }
 

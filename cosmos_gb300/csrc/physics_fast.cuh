@@ -17,7 +17,26 @@
 
 namespace cg {
 
-CG_D float frcp(float x) { return __fdividef(1.0f, x); }
+// Single-instruction approximations used by every FP32 path: PTX rcp / sqrt / rsqrt .approx.ftz,
+// one MUFU operation each, within about 2 ulp of the rounded result; subnormal inputs and results
+// flush to zero, a range that physical states do not reach.  (Measured on GB300: a reciprocal
+// written as __fdividef(1, x) executes five instructions per lane; this form executes one.)
+CG_D float frcp(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+CG_D float fsqrt(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+CG_D float frsqrt(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+CG_D float fdiv(float a, float b) { return __fmul_rn(a, frcp(b)); }
 
 // ---- lane types and their arithmetic
 struct f2 {
@@ -31,24 +50,24 @@ CG_D float vadd(float a, float b) { return __fadd_rn(a, b); }
 CG_D float vsub(float a, float b) { return __fsub_rn(a, b); }
 CG_D float vmul(float a, float b) { return __fmul_rn(a, b); }
 CG_D float vfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-CG_D float vrcp(float a) { return __fdividef(1.0f, a); }
-CG_D float vdiv(float a, float b) { return __fdividef(a, b); }
+CG_D float vrcp(float a) { return frcp(a); }
+CG_D float vdiv(float a, float b) { return fdiv(a, b); }
 CG_D float vmin(float a, float b) { return fminf(a, b); }
 CG_D float vmax(float a, float b) { return fmaxf(a, b); }
 CG_D float vabs(float a) { return fabsf(a); }
-CG_D float vsqrt(float a) { return sqrtf(a); }
+CG_D float vsqrt(float a) { return fsqrt(a); }
 CG_D float vsel_lt(float a, float b, float x, float y) { return a < b ? x : y; }  // a < b ? x : y
 
 CG_D f2 vadd(f2 a, f2 b) { return f2{__fadd2_rn(a.v, b.v)}; }
 CG_D f2 vsub(f2 a, f2 b) { return f2{__ffma2_rn(b.v, make_float2(-1.0f, -1.0f), a.v)}; }
 CG_D f2 vmul(f2 a, f2 b) { return f2{__fmul2_rn(a.v, b.v)}; }
 CG_D f2 vfma(f2 a, f2 b, f2 c) { return f2{__ffma2_rn(a.v, b.v, c.v)}; }
-CG_D f2 vrcp(f2 a) { return f2{make_float2(__fdividef(1.0f, a.v.x), __fdividef(1.0f, a.v.y))}; }
-CG_D f2 vdiv(f2 a, f2 b) { return f2{make_float2(__fdividef(a.v.x, b.v.x), __fdividef(a.v.y, b.v.y))}; }
+CG_D f2 vrcp(f2 a) { return f2{make_float2(frcp(a.v.x), frcp(a.v.y))}; }
+CG_D f2 vdiv(f2 a, f2 b) { return vmul(a, vrcp(b)); }
 CG_D f2 vmin(f2 a, f2 b) { return f2{make_float2(fminf(a.v.x, b.v.x), fminf(a.v.y, b.v.y))}; }
 CG_D f2 vmax(f2 a, f2 b) { return f2{make_float2(fmaxf(a.v.x, b.v.x), fmaxf(a.v.y, b.v.y))}; }
 CG_D f2 vabs(f2 a) { return f2{make_float2(fabsf(a.v.x), fabsf(a.v.y))}; }
-CG_D f2 vsqrt(f2 a) { return f2{make_float2(sqrtf(a.v.x), sqrtf(a.v.y))}; }
+CG_D f2 vsqrt(f2 a) { return f2{make_float2(fsqrt(a.v.x), fsqrt(a.v.y))}; }
 CG_D f2 vsel_lt(f2 a, f2 b, f2 x, f2 y) {
     return f2{make_float2(a.v.x < b.v.x ? x.v.x : y.v.x, a.v.y < b.v.y ? x.v.y : y.v.y)};
 }

@@ -77,7 +77,7 @@ CG_D int g4sym(int m, int n) {
 // ---- state conversions and fluxes.  Primitives travel as float[5] (rho, vx, vy, vz, p), the
 // reference's stored state; conserved states are densitised.
 CG_D SRPrim32 gr_c2p_fast(const SRFastParams& P, const float* u, const GRMet& M, int* flags) {
-    const float is = __fdividef(1.0f, M.sg);
+    const float is = frcp(M.sg);
     float v[5];
 #pragma unroll
     for (int k = 0; k < 5; k++) v[k] = u[k] * is;
@@ -101,8 +101,8 @@ CG_D void gr_cons_fast(const SRFastParams& P, const float* p, const GRMet& M, fl
     for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int j = 0; j < 3; j++) v2 = fmaf(M.g[gsym(i, j)] * v[i], v[j], v2);
-    const float W = rsqrtf(1.0f - (v2 > 1.0f - 1e-8f ? 1.0f - 1e-8f : v2));
-    const float h = 1.0f + __fdividef(p[4], p[0]) * (P.gf / (P.gf - 1.0f));
+    const float W = frsqrt(1.0f - (v2 > 1.0f - 1e-8f ? 1.0f - 1e-8f : v2));
+    const float h = 1.0f + fdiv(p[4], p[0]) * P.hfac;
     const float sr = M.sg * p[0];
     u[0] = sr * W;
     const float m = sr * h * W * W;
@@ -120,7 +120,7 @@ CG_D void gr_flux_fast(const SRFastParams& P, const float* u, const GRMet& M, fl
     const float as = M.al * M.sg;
     const float rhw = c.rho * c.h * c.W * c.W;
     const float vn = AXIS == 0 ? c.vx : c.vy;
-    const float w = vn - __fdividef(M.be[AXIS], M.al);
+    const float w = vn - fdiv(M.be[AXIS], M.al);
     f[0] = as * (c.rho * c.W * w);
     f[1] = as * (rhw * c.vx * w + (AXIS == 0 ? c.p : 0.0f));
     f[2] = as * (rhw * c.vy * w + (AXIS == 1 ? c.p : 0.0f));
@@ -190,7 +190,7 @@ CG_D void gr_update_fast(const SRFastParams& P, const float* c, const float* FL,
 CG_D void gr_source_fast(const SRFastParams& P, const float* u, const GRMet& M, const GRSrc& X, float* s, int* flags) {
     const SRPrim32 c = gr_c2p_fast(P, u, M, flags);
     float uu[4];
-    uu[0] = __fdividef(c.W, M.al);
+    uu[0] = fdiv(c.W, M.al);
     uu[1] = (M.al * uu[0]) * c.vx - M.be[0] * uu[0];
     uu[2] = (M.al * uu[0]) * c.vy - M.be[1] * uu[0];
     uu[3] = (M.al * uu[0]) * c.vz - M.be[2] * uu[0];
@@ -203,7 +203,7 @@ CG_D void gr_source_fast(const SRFastParams& P, const float* u, const GRMet& M, 
     for (int i = 0; i < 3; i++) vc[i] = M.g[gsym(i, 0)] * v[0] + M.g[gsym(i, 1)] * v[1] + M.g[gsym(i, 2)] * v[2];
     const float rhw = rh * c.W * c.W;
     const float T00 = T(0, 0);
-    const float ial = __fdividef(1.0f, M.al);
+    const float ial = frcp(M.al);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
 #pragma unroll
@@ -310,9 +310,9 @@ CG_D void gr_rk_fast(const SRFastParams& P, const NewtonFastParams& NP, int dims
 // RelativisticEuler/RelativisticEulerEquationOfState.cpp:3-18).
 CG_D float gr_speed_fast(const SRFastParams& P, const float* p, const float* w) {
     const float al = w[0];
-    const float h = 1.0f + __fdividef(p[4], p[0]) * (P.gf / (P.gf - 1.0f));
-    const float cs2 = __fdividef(P.gf * p[4], p[0] * h);
-    const float cs = sqrtf(cs2);
+    const float h = 1.0f + fdiv(p[4], p[0]) * P.hfac;
+    const float cs2 = fdiv(P.gf * p[4], p[0] * h);
+    const float cs = fsqrt(cs2);
     const float v[3] = {p[1], p[2], p[3]};
     float v2 = 0.0f;
 #pragma unroll
@@ -324,8 +324,8 @@ CG_D float gr_speed_fast(const SRFastParams& P, const float* p, const float* w) 
     for (int i = 0; i < 3; i++) {
         const float be = w[1 + i];
         const float mat = al * v[i] - be;
-        const float rt = sqrtf((1.0f - v2) * (w[10 + i] * (1.0f - v2 * cs2) - v[i] * v[i] * (1.0f - cs2)));
-        const float pre = __fdividef(al, 1.0f - v2 * cs2);
+        const float rt = fsqrt((1.0f - v2) * (w[10 + i] * (1.0f - v2 * cs2) - v[i] * v[i] * (1.0f - cs2)));
+        const float pre = fdiv(al, 1.0f - v2 * cs2);
         const float fast = pre * (v[i] * (1.0f - cs2) + cs * rt) - be;
         const float slow = pre * (v[i] * (1.0f - cs2) - cs * rt) - be;
         s = mat > s ? mat : s;

@@ -30,7 +30,25 @@ struct SRFastParams {
     float gf;                // gamma
     double g;                // gamma (FP64 stage)
     float w64;               // Lorentz factor above which the FP64 stage runs (0: always)
+    // constants of gamma, formed on the host (sr_fast_constants): (g-1)/g, -1/g^2, (g-1)/g^2,
+    // (g-2)/g, g/(g-1), in FP32 and for the FP64 stage
+    float gr, c0, grg, g2g, hfac;
+    double grd, k0d, grgd, g2gd;
 };
+
+inline void sr_fast_constants(SRFastParams& P, double g) {
+    P.gf = (float)g;
+    P.g = g;
+    P.grd = (g - 1.0) / g;
+    P.k0d = -1.0 / (g * g);
+    P.grgd = P.grd / g;
+    P.g2gd = (g - 2.0) / g;
+    P.gr = (float)P.grd;
+    P.c0 = (float)P.k0d;
+    P.grg = (float)P.grgd;
+    P.g2g = (float)P.g2gd;
+    P.hfac = (float)(g / (g - 1.0));
+}
 
 struct SRPrim32 {
     float rho, vx, vy, vz, p, W, h;
@@ -39,14 +57,14 @@ struct SRPrim32 {
 // Primitive recovery of one FP32 conserved state; sets bit 0 of *flags when neither stage converged.
 CG_D SRPrim32 sr_c2p_fast(const SRFastParams& P, const float* u, int* flags) {
     const float D = u[0], Sx = u[1], Sy = u[2], Sz = u[3], tau = u[4];
-    const float g = P.gf, gr = (g - 1.0f) / g;
+    const float gr = P.gr;
     float q = (tau + D) * (tau + D) - (Sx * Sx + Sy * Sy + Sz * Sz);
     q = q < 1e-8f ? 1e-8f : q;
-    const float iq = rsqrtf(q);
+    const float iq = frsqrt(q);
     const float dc = D * iq, ec = (D + tau) * iq;
-    const float c0 = -1.0f / (g * g);
-    const float c1 = -2.0f * dc * (gr / g);
-    const float c2 = ((g - 2.0f) / g) * (ec * ec - 1.0f) + 1.0f - dc * dc * gr * gr;
+    const float c0 = P.c0;
+    const float c1 = -2.0f * dc * P.grg;
+    const float c2 = P.g2g * (ec * ec - 1.0f) + 1.0f - dc * dc * gr * gr;
     const float c4 = ec * ec - 1.0f;
     const float eta = 2.0f * dc * gr;
     float x = 1.0f;
@@ -55,23 +73,23 @@ CG_D SRPrim32 sr_c2p_fast(const SRFastParams& P, const float* u, int* flags) {
         const float x2 = x * x;
         const float f = c4 * x2 * x * (x - eta) + c2 * x2 + c1 * x + c0;
         const float fp = c1 + 2.0f * c2 * x + 4.0f * c4 * x2 * x - 3.0f * eta * c4 * x2;
-        const float nx = x - __fdividef(f, fp);
+        const float nx = x - fdiv(f, fp);
         const bool done = fabsf(nx - x) <= 1e-6f * fabsf(x);
         x = nx;
         if (done) { conv = true; break; }
     }
-    float W = 0.5f * ec * x * (1.0f + sqrtf(1.0f + 4.0f * gr * (1.0f - dc * x) / (ec * ec * x * x)));
+    float W = 0.5f * ec * x * (1.0f + fsqrt(1.0f + fdiv(4.0f * gr * (1.0f - dc * x), ec * ec * x * x)));
     if (!conv || W > P.w64) {
         // FP64 Newton from the FP32 root, coefficients in FP64
         const double Dd = D, td = tau;
-        const double gd = P.g, grd = (gd - 1.0) / gd;
+        const double grd = P.grd;
         double qd = (td + Dd) * (td + Dd) - ((double)Sx * Sx + (double)Sy * Sy + (double)Sz * Sz);
         qd = qd < 1e-8 ? 1e-8 : qd;
         const double iqd = rsqrt(qd);
         const double dcd = Dd * iqd, ecd = (Dd + td) * iqd;
-        const double k0 = -1.0 / (gd * gd);
-        const double k1 = -2.0 * dcd * (grd / gd);
-        const double k2 = ((gd - 2.0) / gd) * (ecd * ecd - 1.0) + 1.0 - dcd * dcd * grd * grd;
+        const double k0 = P.k0d;
+        const double k1 = -2.0 * dcd * P.grgd;
+        const double k2 = P.g2gd * (ecd * ecd - 1.0) + 1.0 - dcd * dcd * grd * grd;
         const double k4 = ecd * ecd - 1.0;
         const double et = 2.0 * dcd * grd;
         double xd = x;
@@ -88,15 +106,15 @@ CG_D SRPrim32 sr_c2p_fast(const SRFastParams& P, const float* u, int* flags) {
         }
         conv = c64;
         x = (float)xd;
-        W = 0.5f * ec * x * (1.0f + sqrtf(1.0f + 4.0f * gr * (1.0f - dc * x) / (ec * ec * x * x)));
+        W = 0.5f * ec * x * (1.0f + fsqrt(1.0f + fdiv(4.0f * gr * (1.0f - dc * x), ec * ec * x * x)));
     }
     if (!conv && flags) *flags |= 1;
     SRPrim32 r;
     r.W = W;
-    r.h = __fdividef(1.0f, dc * x);
-    r.rho = __fdividef(D, W);
+    r.h = frcp(dc * x);
+    r.rho = fdiv(D, W);
     const float rhw = r.rho * r.h * W * W;
-    const float irhw = __fdividef(1.0f, rhw);
+    const float irhw = frcp(rhw);
     r.vx = Sx * irhw;
     r.vy = Sy * irhw;
     r.vz = Sz * irhw;
@@ -128,8 +146,8 @@ CG_D void sr_flux_fast(const SRFastParams& P, const float* u, float* f, int* fla
 // v (clamped where v^2 > 1 - 1e-8), h from rho and p (RelativisticEulerEquationOfState.cpp:3-8)
 CG_D void sr_cons_of(const SRFastParams& P, const SRPrim32& c, float* u) {
     const float v2 = c.vx * c.vx + c.vy * c.vy + c.vz * c.vz;
-    const float W = rsqrtf(1.0f - (v2 > 1.0f - 1e-8f ? 1.0f - 1e-8f : v2));
-    const float h = 1.0f + __fdividef(c.p, c.rho) * (P.gf / (P.gf - 1.0f));
+    const float W = frsqrt(1.0f - (v2 > 1.0f - 1e-8f ? 1.0f - 1e-8f : v2));
+    const float h = 1.0f + fdiv(c.p, c.rho) * P.hfac;
     const float rhw = c.rho * h * W * W;
     u[0] = c.rho * W;
     u[1] = rhw * c.vx;
@@ -179,7 +197,7 @@ CG_D void sr_force_fast(const SRFastParams& P, const float* L, const float* R, f
 // RelativisticEuler/RelativisticEulerEquationOfState.cpp:3-18
 CG_D float sr_wavespeed_fast(const SRFastParams& P, const float* u, int dims, int* flags) {
     const SRPrim32 c = sr_c2p_fast(P, u, flags);
-    const float cs = sqrtf(__fdividef(P.gf * c.p, c.rho * c.h));
+    const float cs = fsqrt(fdiv(P.gf * c.p, c.rho * c.h));
     if (dims == 1) return fabsf(c.vx) + cs;
     return fmaxf(fabsf(c.vx), fabsf(c.vy)) + cs;
 }

@@ -253,8 +253,7 @@ inline SRFastPolicy<AXIS, LIM, MASKED> make_sr_fast(double gamma, double bias, i
     p.P.wb = p.NP.wb;
     p.P.hom = p.NP.hom;
     p.P.hop = p.NP.hop;
-    p.P.gf = (float)gamma;
-    p.P.g = gamma;
+    sr_fast_constants(p.P, gamma);
     p.P.w64 = c2p64_above > 0.0 ? (float)c2p64_above : 0.0f;  // W >= 1 > 0: threshold 0 always runs FP64
     p.lm.axis = AXIS;
     p.lm.nx = nx;
