@@ -66,37 +66,40 @@ template <class V> CG_D V bcv(typename Lane<V>::S s) { return Lane<V>::bc(s); }
 // Newtonian flux along axis AX of a conserved state, and its transposed Jacobian.
 template <class V>
 struct AdjFlux {
-    V g1;  // gamma - 1
+    V g1, ng1, ng1h;  // gamma - 1, -(gamma - 1), -(gamma - 1)/2
     template <int AX>
     CG_D void flux(const V* u, V* f) const {
         const V inv = vrcp(u[0]);
         const V vn = vmul(u[1 + AX], inv);
         const V q = vfma(u[1], u[1], vfma(u[2], u[2], vmul(u[3], u[3])));
-        const V p = vmul(g1, vsub(u[4], vmul(bcv<V>(0.5), vmul(q, inv))));
+        const V p = vfma(ng1h, vmul(q, inv), vmul(g1, u[4]));
         f[0] = u[1 + AX];
-        f[1] = vmul(u[1], vn);
-        f[2] = vmul(u[2], vn);
+        f[1] = AX == 0 ? vfma(u[1], vn, p) : vmul(u[1], vn);
+        f[2] = AX == 1 ? vfma(u[2], vn, p) : vmul(u[2], vn);
         f[3] = vmul(u[3], vn);
-        f[1 + AX] = vadd(f[1 + AX], p);
         f[4] = vmul(vadd(u[4], p), vn);
     }
-    // ub += (dF/du)^T gb
+    // ub += (dF/du)^T gb, with p = (gamma - 1)(E - rho |v|^2 / 2) and v = m / rho:
+    //   pb = gb_n + gb_E v_n (everything p multiplies), vnb = sum_k gb_k m_k + gb_E (E + p)
+    //   ub_rho += (gamma - 1) pb |v|^2 / 2 - vnb v_n / rho,  ub_mk += gb_k v_n - (gamma - 1) pb v_k,
+    //   ub_mn += gb_rho + vnb / rho,  ub_E += gb_E v_n + (gamma - 1) pb
     template <int AX>
     CG_D void vjp(const V* u, const V* gb, V* ub) const {
         const V inv = vrcp(u[0]);
         const V v0 = vmul(u[1], inv), v1 = vmul(u[2], inv), v2 = vmul(u[3], inv);
         const V vn = AX == 0 ? v0 : v1;
         const V vv = vfma(v0, v0, vfma(v1, v1, vmul(v2, v2)));
-        const V p = vmul(g1, vsub(u[4], vmul(bcv<V>(0.5), vmul(u[0], vv))));
-        const V pb = vfma(gb[4], vn, gb[1 + AX]);                                         // from F_n and F_E
-        const V vnb = vfma(gb[4], vadd(u[4], p), vfma(gb[3], u[3], vfma(gb[2], u[2], vmul(gb[1], u[1]))));  // d/dv_n
-        const V gp = vmul(g1, pb);
-        ub[0] = vadd(ub[0], vsub(vmul(vmul(gp, bcv<V>(0.5)), vv), vmul(vmul(vnb, vn), inv)));
-        ub[1] = vadd(ub[1], vsub(vmul(gb[1], vn), vmul(gp, v0)));
-        ub[2] = vadd(ub[2], vsub(vmul(gb[2], vn), vmul(gp, v1)));
-        ub[3] = vadd(ub[3], vsub(vmul(gb[3], vn), vmul(gp, v2)));
-        ub[1 + AX] = vadd(ub[1 + AX], vfma(vnb, inv, gb[0]));
-        ub[4] = vadd(ub[4], vfma(gb[4], vn, gp));
+        const V p = vfma(ng1h, vmul(u[0], vv), vmul(g1, u[4]));
+        const V pb = vfma(gb[4], vn, gb[1 + AX]);
+        const V vnb = vfma(gb[4], vadd(u[4], p), vfma(gb[3], u[3], vfma(gb[2], u[2], vmul(gb[1], u[1]))));
+        const V ngp = vmul(ng1, pb);    // -(gamma - 1) pb
+        const V ngh = vmul(ng1h, pb);   // -(gamma - 1) pb / 2
+        ub[0] = vsub(ub[0], vfma(ngh, vv, vmul(vmul(vnb, vn), inv)));
+        ub[1] = vfma(gb[1], vn, vfma(ngp, v0, ub[1]));
+        ub[2] = vfma(gb[2], vn, vfma(ngp, v1, ub[2]));
+        ub[3] = vfma(gb[3], vn, vfma(ngp, v2, ub[3]));
+        ub[1 + AX] = vfma(vnb, inv, vadd(ub[1 + AX], gb[0]));
+        ub[4] = vfma(gb[4], vn, vsub(ub[4], ngp));
     }
 };
 
@@ -280,7 +283,7 @@ CG_D void st_lanes(float* p, size_t q0, size_t q1, bool vec, bool two, f2 v) {
 }
 
 template <class V, class S, bool PRIM, int AX, int LIM, int P, int W>
-__global__ void __launch_bounds__(P * W, (Lane<V>::N == 2 ? 2 : (sizeof(V) == 4 ? 3 : 1)))
+__global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 2 : (sizeof(V) == 4 ? 3 : 1))))
     adjoint_sweep_kernel(AdjSweepParams a) {
     using T = typename Lane<V>::S;
     constexpr int NL = Lane<V>::N;
@@ -309,7 +312,7 @@ __global__ void __launch_bounds__(P * W, (Lane<V>::N == 2 ? 2 : (sizeof(V) == 4 
     AdjCoef<T> K;
     if constexpr (sizeof(T) == 4) K = a.cf;
     else K = a.cd;
-    const AdjFlux<V> F{bcv<V>(K.g1)};
+    const AdjFlux<V> F{bcv<V>(K.g1), bcv<V>(-K.g1), bcv<V>(T(-0.5) * K.g1)};
     const AdjSlope<V> Sl{bcv<V>(K.ca), bcv<V>(K.cb), bcv<V>(K.w1m), bcv<V>(K.w1p)};
     const V d = bcv<V>(K.d), c = bcv<V>(K.c), hs = bcv<V>(K.hs);
     const V zero = bcv<V>(0);
