@@ -14,6 +14,7 @@ constexpr int kXPairThreads = 32;  // one warp per block
 constexpr int kXPairSegs = 2;      // 60-cell segments per warp
 constexpr int kYPairThreads = 64;  // 128 columns per block (two per thread)
 constexpr int kYPairSeg = 32;
+constexpr int kYRingRows = 8;      // Y rows staged in shared memory per warp (up to 8 in flight)
 
 template <int AXIS, int LIM, bool MASKED>
 NewtonFastPolicy<AXIS, LIM, MASKED> make_fast(const SweepArgs& a) {
@@ -41,8 +42,8 @@ void run_fast(const SweepArgs& a) {
         else sweep_x_own_kernel<Pol, 1, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
     } else if (a.order == 2 && !MASKED) {
         dim3 grid((G.nx + 2 * kYPairThreads - 1) / (2 * kYPairThreads), (G.ny + kYPairSeg - 1) / kYPairSeg);
-        sweep_y_pair_kernel<LIM, kYPairThreads, kYPairSeg><<<grid, kYPairThreads, 0, a.stream>>>(pol.P, G.dims, G, src, dst,
-                                                                                              a.ds, a.out);
+        sweep_y_ring_kernel<LIM, kYPairThreads, kYPairSeg, kYRingRows><<<grid, kYPairThreads, 0, a.stream>>>(
+            pol.P, G.dims, G, src, dst, a.ds, a.out);
     } else {
         dim3 grid((G.nx + kYThreads - 1) / kYThreads, (G.ny + kYSeg - 1) / kYSeg);
         if (a.order == 2) sweep_y_kernel<Pol, 2, kYThreads, kYSeg><<<grid, kYThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);

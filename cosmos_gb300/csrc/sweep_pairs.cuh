@@ -5,6 +5,7 @@
 #pragma once
 #include "physics_fast.cuh"
 #include "sweep_kernels.cuh"
+#include "tma.cuh"
 
 namespace cg {
 
@@ -160,26 +161,139 @@ CG_D float x_pair_update(const NewtonFastParams& P, int dims, const Geom& G, flo
 
 // ---- single-grid kernels
 
-// Y sweep: threads march rows [y0, y0 + SEG) of column pairs.
-template <int LIM, int NT, int SEG>
-__global__ void __launch_bounds__(NT) sweep_y_pair_kernel(NewtonFastParams P, int dims, Geom G,
+// Y sweep with the rows staged in shared memory by bulk copies.  Each warp owns 64 columns (two per
+// lane) and a ring of R row slots in shared memory (five field rows each, one mbarrier per slot):
+// its rows y0 - 2 .. y1 + 1 arrive by cp.async.bulk, issued by lanes 0-4 (one field each) up to R
+// rows ahead of the row being consumed, so the loads overlap several rows of work where a register
+// prefetch covers one.  Warps never wait for each other (no block barrier after the set-up), and
+// each reduces its own CFL maximum.  The arithmetic is y_pair_march's.  A wait that runs out
+// (about a second) sets ST_TIMEOUT in the status word; the warp then waits, again bounded, for its
+// rows still in flight and leaves.
+template <int LIM, int NT, int SEG, int R>
+__global__ void __launch_bounds__(NT) sweep_y_ring_kernel(NewtonFastParams P, int dims, Geom G,
                                                           const float* __restrict__ src, float* __restrict__ dst,
                                                           DtSrc ds, SweepOut out) {
+    static_assert(R >= 5 && (R & (R - 1)) == 0, "a power of two above the four prologue rows");
+    static_assert(NT % 32 == 0, "whole warps");
+    constexpr int NWP = NT / 32;
+    constexpr unsigned FULL = 0xffffffffu;
+    __shared__ __align__(128) float ring[NWP][R][5][64];
+    __shared__ __align__(8) unsigned long long bar[NWP][R];
     __shared__ FastCoef s_coef;
     __shared__ int s_act;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const int jw = (blockIdx.x * NWP + wp) * 64;  // the warp's first column
+    const int j = jw + 2 * lane;
+    const bool live = j < G.nx, two = j + 1 < G.nx;
+    const int y0 = blockIdx.y * SEG, y1 = min(y0 + SEG, G.ny);
+    const int ylo = y0 - 2, yhi = y1 + 1;  // rows read
     if (threadIdx.x == 0) {
         double dt;
         s_act = ds.get(dt);
         if (s_act) s_coef = ds.fast_coef();
+        for (int w = 0; w < NWP; w++)
+            for (int q = 0; q < R; q++) mbar_init(&bar[w][q], 1);
+        mbar_init_fence();
     }
     __syncthreads();
-    const bool act = s_act != 0;
-    const int j = 2 * (blockIdx.x * NT + threadIdx.x);
-    const int y0 = blockIdx.y * SEG, y1 = min(y0 + SEG, G.ny);
-    unsigned long long* wslot = out.slot();
+    if (jw >= G.nx) return;  // warp-uniform: no column of this warp exists
+    if (!s_act) {            // inactive step: keep the ping-pong buffers consistent
+        if (live) y_pair_march<LIM>(P, dims, G, src, dst, j, y0, y1, false, s_coef, false);
+        return;
+    }
+    const FastCoef cf = s_coef;
+    const uint32_t bytes = ((uint32_t)min(64, G.nx - jw) * 4u + 15u) & ~15u;  // within the padded pitch
+    // Row r of the ring lives in slot (r - ylo) mod R; the slot's k-th use completes phase k mod 2.
+    // Lanes 0-4 each copy one field (lane 5+ hold a valid pointer they never use).
+    const float* fsrc = src + (size_t)min(lane, 4) * G.fstride + jw;
+    int inext = ylo;  // warp-uniform: next row to issue
+    auto issue_one = [&]() {
+        const int r = inext, q = (r - ylo) & (R - 1);
+        if (lane == 0) mbar_expect_tx(&bar[wp][q], 5 * bytes);
+        __syncwarp();
+        if (lane < 5) bulk_load(ring[wp][q][lane], fsrc + (size_t)ghost_index(r, G.ny, G.bc) * G.pitch, bytes, &bar[wp][q]);
+        ++inext;
+    };
+    for (int k = 0; k < R && inext <= yhi; k++) issue_one();
+    bool ok = true;
+    int tq = 0;          // slot of the next row to take
+    uint32_t tpar = 0;   // its phase parity
+    auto take = [&](Cell2& c) {
+        ok = ok && mbar_wait(&bar[wp][tq], tpar);
+#pragma unroll
+        for (int f = 0; f < 5; f++) {
+            const float2 v = *reinterpret_cast<const float2*>(&ring[wp][tq][f][2 * lane]);
+            c.v[f].v = make_float2(v.x, two ? v.y : v.x);  // a lone last column runs in both lanes
+        }
+        if (++tq == R) {
+            tq = 0;
+            tpar ^= 1u;
+        }
+    };
+    Cell2 cm2, cm1, c0, c1, c2;
+    take(cm2);
+    take(cm1);
+    take(c0);
+    take(c1);
+    ok = __all_sync(FULL, ok);
+    __syncwarp();  // every lane's reads of the freed slots are ordered before their refills
     float w = 0.0f;
-    if (j < G.nx) w = y_pair_march<LIM>(P, dims, G, src, dst, j, y0, y1, act, s_coef, wslot != nullptr);
-    if (wslot) block_max_to<NT>(wslot, w);
+    unsigned long long* wslot = out.slot();
+    const bool want_w = wslot != nullptr && live;
+    int consumed = ylo - 1;  // warp-uniform: last row every lane has copied out
+    if (ok) {
+        consumed = ylo + 3;
+        for (int k = 0; k < 4 && inext <= yhi; k++) issue_one();
+        f2 Lm1[5], Rm1[5], L0[5], R0[5], Fp[5], Fn[5];
+        nf_recon<1, LIM>(P, cm2.v, cm1.v, c0.v, cf.half_dtdx, Lm1, Rm1);
+        nf_recon<1, LIM>(P, cm1.v, c0.v, c1.v, cf.half_dtdx, L0, R0);
+        nf_force<1>(P, Rm1, L0, cf.half_dtdx, cf.q_dxdt, Fp);
+        for (int y = y0; y < y1; y++) {
+            take(c2);
+            ok = __all_sync(FULL, ok);
+            if (!ok) break;
+            __syncwarp();
+            consumed = y + 2;
+            if (inext <= yhi) issue_one();
+            f2 L1[5], R1[5];
+            nf_recon<1, LIM>(P, c0.v, c1.v, c2.v, cf.half_dtdx, L1, R1);
+            nf_force<1>(P, R0, L1, cf.half_dtdx, cf.q_dxdt, Fn);
+            Cell2 nc;
+            nf_update(cf.dtdx, c0.v, Fp, Fn, nc.v);
+            if (live) {
+                const size_t b = (size_t)y * G.pitch + j;
+#pragma unroll
+                for (int f = 0; f < 5; f++) {
+                    float* o = dst + f * G.fstride + b;
+                    if (two) *reinterpret_cast<float2*>(o) = nc.v[f].v;
+                    else *o = nc.v[f].v.x;
+                }
+                if (want_w) {
+                    const f2 ws = nf_wavespeed(P, nc.v, dims);
+                    w = fmaxf(w, fmaxf(ws.v.x, ws.v.y));  // a lone column's lanes are equal
+                }
+            }
+#pragma unroll
+            for (int f = 0; f < 5; f++) {
+                Fp[f] = Fn[f];
+                R0[f] = R1[f];
+            }
+            c0 = c1;
+            c1 = c2;
+        }
+    }
+    if (!ok) {  // warp-uniform
+        if (lane == 0) {
+            if (out.status) atomicOr(out.status, ST_TIMEOUT);
+            for (int r = consumed + 1; r < inext; r++)
+                mbar_wait(&bar[wp][(r - ylo) & (R - 1)], (uint32_t)((r - ylo) / R) & 1u, 100000000LL);
+        }
+        return;
+    }
+    if (wslot) {
+        w = warp_max(w);
+        if (lane == 0) atomic_max_nonneg(wslot, (double)w);
+    }
 }
 
 // X sweep: a warp walks SEGS consecutive 60-cell segments of its row, loading the next segment
