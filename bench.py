@@ -458,7 +458,7 @@ def run_batch(args):
                 "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms, "steps": e2e_steps,
                 "what": "per step: each grid's pinned host AoS FP64 primitives -> device, one batched step, "
                         "states -> host"},
-        "roofline": {"bound": "hbm", "kernel": "batch_step_kernel<NewtonFastPolicy> (whole step, FP32)",
+        "roofline": {"bound": "hbm", "kernel": "batch_pair_kernel (whole step, FP32 cell pairs)",
                      "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak, "peak_source": peak_kind,
                      "traffic": (traffic_per_launch("batch_step_fp32_ratio") or 0.0) * bytes_step or None,
                      "traffic_note": "per step; ncu ratio traffic/algorithmic of a 64-grid capture x this "

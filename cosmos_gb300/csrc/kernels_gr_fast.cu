@@ -208,7 +208,10 @@ GRFastPolicy<AXIS, LIM, MASKED> make_pol(const SweepArgs& a, double bias) {
 }
 
 constexpr int kXThreads = 256;
-constexpr int kYThreads = 128;
+// One warp of columns per Y block: the cells near the hole (FP64 recovery stage) make some column
+// segments several times costlier than the rest, and 32 blocks of 32 x 32 cells per 1024 columns
+// spread them over the SMs better than 8 blocks of 128 x 32.
+constexpr int kYThreads = 32;
 constexpr int kYSeg = 32;
 
 template <int AXIS, int LIM, bool MASKED>

@@ -6,9 +6,10 @@
 // 30-101): the quartic in xi built from dc = D / sqrt(q) and ec = (D + tau) / sqrt(q),
 // q = (tau + D)^2 - |S|^2 (guarded at 1e-8), solved by Newton from xi = 1, then W, h, rho, v, p,
 // with rho and p floored at 1e-8.  Here the iteration runs in FP32 to FP32 accuracy first; FP64
-// Newton steps from that root follow (the coefficients formed again in FP64) until a step is
-// below 1e-7, after which quadratic convergence has put the root within 1e-14 -- the reference's
-// |step| < 1e-8 criterion holds on the next step.  The FP64 stage runs for every solve when
+// Newton steps from that root follow (the coefficients formed again in FP64; square root and
+// division as refined FP32 estimates) until a step is below 1e-7, after which quadratic
+// convergence has put the root within 1e-14 -- the reference's |step| < 1e-8 criterion holds on
+// the next step.  The FP64 stage runs for every solve when
 // c2p64_above <= 0; otherwise only for states whose FP32 Lorentz factor exceeds c2p64_above (or
 // whose FP32 iteration did not converge).  Primitives are then formed in FP32.  The iteration caps
 // are 40 (FP32, from xi = 1; physical states converge in well under 20) and 8 (FP64, from the FP32
@@ -80,12 +81,16 @@ CG_D SRPrim32 sr_c2p_fast(const SRFastParams& P, const float* u, int* flags) {
     }
     float W = 0.5f * ec * x * (1.0f + fsqrt(1.0f + fdiv(4.0f * gr * (1.0f - dc * x), ec * ec * x * x)));
     if (!conv || W > P.w64) {
-        // FP64 Newton from the FP32 root, coefficients in FP64
+        // FP64 Newton from the FP32 root, coefficients in FP64 (they cancel at high Lorentz
+        // factor).  1/sqrt(q) and each step's 1/f' are FP32 estimates refined by one FP64 Newton
+        // step (relative error about 1e-14), so no FP64 square root or division runs: on GB300 the
+        // FP64 rate is 1/64 of FP32 and a lane in this stage holds its whole warp.
         const double Dd = D, td = tau;
         const double grd = P.grd;
         double qd = (td + Dd) * (td + Dd) - ((double)Sx * Sx + (double)Sy * Sy + (double)Sz * Sz);
         qd = qd < 1e-8 ? 1e-8 : qd;
-        const double iqd = rsqrt(qd);
+        double iqd = (double)frsqrt((float)qd);
+        iqd = iqd * fma(-0.5 * qd * iqd, iqd, 1.5);
         const double dcd = Dd * iqd, ecd = (Dd + td) * iqd;
         const double k0 = P.k0d;
         const double k1 = -2.0 * dcd * P.grgd;
@@ -100,7 +105,9 @@ CG_D SRPrim32 sr_c2p_fast(const SRFastParams& P, const float* u, int* flags) {
             const double x2 = xd * xd;
             const double f = k4 * x2 * xd * (xd - et) + k2 * x2 + k1 * xd + k0;
             const double fp = k1 + 2.0 * k2 * xd + 4.0 * k4 * x2 * xd - 3.0 * et * k4 * x2;
-            const double step = f / fp;
+            double ifp = (double)frcp((float)fp);
+            ifp = ifp * fma(-fp, ifp, 2.0);
+            const double step = f * ifp;
             xd -= step;
             if (fabs(step) < 1e-7) { c64 = true; break; }
         }
