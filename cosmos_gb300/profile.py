@@ -2,6 +2,7 @@
 
     python -m cosmos_gb300.profile --kernel sweep --n 4096 --precision fp32 --axis 0 --launches 3
     python -m cosmos_gb300.profile --kernel step --n 4096 --precision fp32 --launches 4
+    python -m cosmos_gb300.profile --kernel step --system 2 --n 1024 --warm 60 --launches 1
     python -m cosmos_gb300.profile --kernel adjoint --n 1024 --precision fp32 --launches 2
     python -m cosmos_gb300.profile --kernel batch --grids 64 --launches 2
 
@@ -30,6 +31,8 @@ def main():
     ap.add_argument("--axis", type=int, default=0)
     ap.add_argument("--order", type=int, default=2)
     ap.add_argument("--launches", type=int, default=3)
+    ap.add_argument("--warm", type=int, default=0,
+                    help="`step` only: steps run before the captured ones (evolved states)")
     a = ap.parse_args()
     sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
     import cosmos_gb300 as cg
@@ -78,8 +81,11 @@ def main():
     elif a.kernel == "rk":
         for _ in range(a.launches):
             g.rk_source(dt, 0.0, 1)
-    else:
-        g.run_begin(2, 0.9, 1e30, 0.0, cg.MINBEE)
+    else:  # the configuration's solve: MinBee (configs 2, 3); van Leer and the RK source (config 4)
+        lim = cg.VANLEER if a.system == cg.GR else cg.MINBEE
+        g.run_begin(2, 0.9, 1e30, 0.0, lim)
+        if a.warm:
+            g.run_steps(a.warm)
         g.run_steps(a.launches)
         g.run_end()
     g.ctx.synchronize()
