@@ -55,6 +55,44 @@ struct SRPrim32 {
     float rho, vx, vy, vz, p, W, h;
 };
 
+// FP64 Newton from the FP32 root, coefficients in FP64 (they cancel at high Lorentz factor).
+// 1/sqrt(q) and each step's 1/f' are FP32 estimates refined by one FP64 Newton step (relative
+// error about 1e-14), so no FP64 square root or division runs: on GB300 the FP64 rate is 1/64 of
+// FP32 and a lane in this stage holds its whole warp.  Out of line: kernels call the recovery at
+// dozens of sites (39 per GR source step) and this rarely taken stage would otherwise be inlined
+// at each, crowding the instruction cache.
+struct SRStage64 {
+    float x;
+    bool conv;
+};
+static __device__ __noinline__ SRStage64 sr_c2p_stage64(double grd, double k0, double grgd, double g2gd, float D, float Sx,
+                                                 float Sy, float Sz, float tau, float x) {
+    const double Dd = D, td = tau;
+    double qd = (td + Dd) * (td + Dd) - ((double)Sx * Sx + (double)Sy * Sy + (double)Sz * Sz);
+    qd = qd < 1e-8 ? 1e-8 : qd;
+    double iqd = (double)frsqrt((float)qd);
+    iqd = iqd * fma(-0.5 * qd * iqd, iqd, 1.5);
+    const double dcd = Dd * iqd, ecd = (Dd + td) * iqd;
+    const double k1 = -2.0 * dcd * grgd;
+    const double k2 = g2gd * (ecd * ecd - 1.0) + 1.0 - dcd * dcd * grd * grd;
+    const double k4 = ecd * ecd - 1.0;
+    const double et = 2.0 * dcd * grd;
+    double xd = x;
+    // from the FP32 iterate a solvable state converges in one to three steps; a state without a
+    // physical root gives up after 8 (reported through the status word)
+    for (int it = 0; it < 8; it++) {
+        const double x2 = xd * xd;
+        const double f = k4 * x2 * xd * (xd - et) + k2 * x2 + k1 * xd + k0;
+        const double fp = k1 + 2.0 * k2 * xd + 4.0 * k4 * x2 * xd - 3.0 * et * k4 * x2;
+        double ifp = (double)frcp((float)fp);
+        ifp = ifp * fma(-fp, ifp, 2.0);
+        const double step = f * ifp;
+        xd -= step;
+        if (fabs(step) < 1e-7) return SRStage64{(float)xd, true};
+    }
+    return SRStage64{(float)xd, false};
+}
+
 // Primitive recovery of one FP32 conserved state; sets bit 0 of *flags when neither stage converged.
 CG_D SRPrim32 sr_c2p_fast(const SRFastParams& P, const float* u, int* flags) {
     const float D = u[0], Sx = u[1], Sy = u[2], Sz = u[3], tau = u[4];
@@ -81,38 +119,9 @@ CG_D SRPrim32 sr_c2p_fast(const SRFastParams& P, const float* u, int* flags) {
     }
     float W = 0.5f * ec * x * (1.0f + fsqrt(1.0f + fdiv(4.0f * gr * (1.0f - dc * x), ec * ec * x * x)));
     if (!conv || W > P.w64) {
-        // FP64 Newton from the FP32 root, coefficients in FP64 (they cancel at high Lorentz
-        // factor).  1/sqrt(q) and each step's 1/f' are FP32 estimates refined by one FP64 Newton
-        // step (relative error about 1e-14), so no FP64 square root or division runs: on GB300 the
-        // FP64 rate is 1/64 of FP32 and a lane in this stage holds its whole warp.
-        const double Dd = D, td = tau;
-        const double grd = P.grd;
-        double qd = (td + Dd) * (td + Dd) - ((double)Sx * Sx + (double)Sy * Sy + (double)Sz * Sz);
-        qd = qd < 1e-8 ? 1e-8 : qd;
-        double iqd = (double)frsqrt((float)qd);
-        iqd = iqd * fma(-0.5 * qd * iqd, iqd, 1.5);
-        const double dcd = Dd * iqd, ecd = (Dd + td) * iqd;
-        const double k0 = P.k0d;
-        const double k1 = -2.0 * dcd * P.grgd;
-        const double k2 = P.g2gd * (ecd * ecd - 1.0) + 1.0 - dcd * dcd * grd * grd;
-        const double k4 = ecd * ecd - 1.0;
-        const double et = 2.0 * dcd * grd;
-        double xd = x;
-        bool c64 = false;
-        // from the FP32 iterate a solvable state converges in one to three steps; a state without
-        // a physical root gives up after 8 (reported through the status word)
-        for (int it = 0; it < 8; it++) {
-            const double x2 = xd * xd;
-            const double f = k4 * x2 * xd * (xd - et) + k2 * x2 + k1 * xd + k0;
-            const double fp = k1 + 2.0 * k2 * xd + 4.0 * k4 * x2 * xd - 3.0 * et * k4 * x2;
-            double ifp = (double)frcp((float)fp);
-            ifp = ifp * fma(-fp, ifp, 2.0);
-            const double step = f * ifp;
-            xd -= step;
-            if (fabs(step) < 1e-7) { c64 = true; break; }
-        }
-        conv = c64;
-        x = (float)xd;
+        const SRStage64 r = sr_c2p_stage64(P.grd, P.k0d, P.grgd, P.g2gd, D, Sx, Sy, Sz, tau, x);
+        conv = r.conv;
+        x = r.x;
         W = 0.5f * ec * x * (1.0f + fsqrt(1.0f + fdiv(4.0f * gr * (1.0f - dc * x), ec * ec * x * x)));
     }
     if (!conv && flags) *flags |= 1;
