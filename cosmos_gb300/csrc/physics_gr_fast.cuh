@@ -101,7 +101,10 @@ CG_D void gr_cons_fast(const SRFastParams& P, const float* p, const GRMet& M, fl
     for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int j = 0; j < 3; j++) v2 = fmaf(M.g[gsym(i, j)] * v[i], v[j], v2);
-    const float W = frsqrt(1.0f - (v2 > 1.0f - 1e-8f ? 1.0f - 1e-8f : v2));
+    // the reference's clamp of v^2 to 1 - 1e-8 (W <= 1e4), applied to 1 - v^2: in FP32, 1 - 1e-8
+    // rounds to 1, which would make W infinite
+    const float omv = 1.0f - v2;
+    const float W = frsqrt(omv < 1e-8f ? 1e-8f : omv);
     const float h = 1.0f + fdiv(p[4], p[0]) * P.hfac;
     const float sr = M.sg * p[0];
     u[0] = sr * W;
@@ -308,7 +311,35 @@ CG_D void gr_rk_fast(const SRFastParams& P, const NewtonFastParams& NP, int dims
 // BlackHoleEuler/BlackHoleEulerEigenvalues.cpp:3-96) of primitives c at a CFL point whose data are
 // w[0] lapse, w[1..3] shift, w[4..9] gamma_ij, w[10..12] diagonal of gamma^ij (sound speed from
 // RelativisticEuler/RelativisticEulerEquationOfState.cpp:3-18).
+// The same in FP64 (IEEE square roots and divisions), for the garbage states the recovery leaves at
+// the density floor near the horizon (velocities far above 1): their products overflow FP32, where
+// the reference's FP64 gives large finite speeds that limit the time step.
+static __device__ __noinline__ float gr_speed64(double gf, double hfac, const float* p, const float* w) {
+    const double al = w[0];
+    const double h = 1.0 + (double)p[4] / (double)p[0] * hfac;
+    const double cs2 = gf * p[4] / ((double)p[0] * h);
+    const double cs = sqrt(cs2);
+    const double v[3] = {p[1], p[2], p[3]};
+    double v2 = 0.0;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) v2 += (double)w[4 + gsym(i, j)] * v[i] * v[j];
+    double s = 0.0;
+    for (int i = 0; i < 3; i++) {
+        const double be = w[1 + i];
+        const double mat = al * v[i] - be;
+        const double rt = sqrt((1.0 - v2) * (w[10 + i] * (1.0 - v2 * cs2) - v[i] * v[i] * (1.0 - cs2)));
+        const double pre = al / (1.0 - v2 * cs2);
+        const double fast = pre * (v[i] * (1.0 - cs2) + cs * rt) - be;
+        const double slow = pre * (v[i] * (1.0 - cs2) - cs * rt) - be;
+        s = mat > s ? mat : s;
+        s = fast > s ? fast : s;
+        s = slow > s ? slow : s;
+    }
+    return (float)fabs(s);
+}
+
 CG_D float gr_speed_fast(const SRFastParams& P, const float* p, const float* w) {
+    if (!(fabsf(p[1]) < 1e6f && fabsf(p[2]) < 1e6f && fabsf(p[3]) < 1e6f)) return gr_speed64(P.g, 1.0 / P.grd, p, w);
     const float al = w[0];
     const float h = 1.0f + fdiv(p[4], p[0]) * P.hfac;
     const float cs2 = fdiv(P.gf * p[4], p[0] * h);

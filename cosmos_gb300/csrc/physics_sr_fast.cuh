@@ -55,42 +55,98 @@ struct SRPrim32 {
     float rho, vx, vy, vz, p, W, h;
 };
 
-// FP64 Newton from the FP32 root, coefficients in FP64 (they cancel at high Lorentz factor).
-// 1/sqrt(q) and each step's 1/f' are FP32 estimates refined by one FP64 Newton step (relative
-// error about 1e-14), so no FP64 square root or division runs: on GB300 the FP64 rate is 1/64 of
-// FP32 and a lane in this stage holds its whole warp.  Out of line: kernels call the recovery at
-// dozens of sites (39 per GR source step) and this rarely taken stage would otherwise be inlined
-// at each, crowding the instruction cache.
+// FP64 helpers of the recovery's FP64 stage: within FP32's normal range an FP32 estimate refined
+// by one FP64 Newton step (relative error about 1e-14; no FP64 division or square root -- on
+// GB300 the FP64 rate is 1/64 of FP32); outside it (states far beyond any physical range) IEEE.
+CG_D double rcp64(double a) {
+    const double m = fabs(a);
+    if (m > 1e-30 && m < 1e30) {
+        const double r = (double)frcp((float)a);
+        return r * fma(-a, r, 2.0);
+    }
+    return 1.0 / a;
+}
+CG_D double rsqrt64(double a) {
+    if (a > 1e-30 && a < 1e30) {
+        const double r = (double)frsqrt((float)a);
+        return r * fma(-0.5 * a * r, r, 1.5);
+    }
+    return 1.0 / sqrt(a);
+}
+
 struct SRStage64 {
-    float x;
+    SRPrim32 c;
     bool conv;
 };
-static __device__ __noinline__ SRStage64 sr_c2p_stage64(double grd, double k0, double grgd, double g2gd, float D, float Sx,
-                                                 float Sy, float Sz, float tau, float x) {
-    const double Dd = D, td = tau;
-    double qd = (td + Dd) * (td + Dd) - ((double)Sx * Sx + (double)Sy * Sy + (double)Sz * Sz);
+
+// The recovery's FP64 stage: Newton on the quartic with coefficients in FP64 (they cancel at high
+// Lorentz factor) from the FP32 iterate x0 (from the reference's start 1 when x0 is not finite),
+// then the primitives in FP64 with the reference's floors.  It takes the states the FP32 stage
+// cannot: Lorentz factor above the threshold, no FP32 convergence, or coefficients beyond FP32's
+// range -- near the horizon the reference's recovery meets states without a physical root whose
+// garbage primitives grow through the W cap and the fluxes to magnitudes (|S| ~ 1e30) that only
+// FP64 holds.  A state that is not finite, or whose primitives are not, becomes the floor state
+// (rho = p = 1e-8 at rest).  Out of line: kernels call the recovery at dozens of sites (39 per GR
+// source step) and this rarely taken stage would otherwise be inlined at each.
+static __device__ __noinline__ SRStage64 sr_c2p_stage64(double grd, double k0, double grgd, double g2gd, float D,
+                                                        float Sx, float Sy, float Sz, float tau, float x0) {
+    SRStage64 o;
+    o.conv = false;
+    o.c.rho = 1e-8f;
+    o.c.vx = o.c.vy = o.c.vz = 0.0f;
+    o.c.p = 1e-8f;
+    o.c.W = 1.0f;
+    o.c.h = (float)(1.0 + 1.0 / grd);  // 1 + (p / rho) gamma / (gamma - 1) at the floors
+    const float big = 3.0e38f;
+    if (!(fabsf(D) < big && fabsf(Sx) < big && fabsf(Sy) < big && fabsf(Sz) < big && fabsf(tau) < big)) return o;
+    const double Dd = D, td = tau, Sxd = Sx, Syd = Sy, Szd = Sz;
+    double qd = (td + Dd) * (td + Dd) - (Sxd * Sxd + Syd * Syd + Szd * Szd);
     qd = qd < 1e-8 ? 1e-8 : qd;
-    double iqd = (double)frsqrt((float)qd);
-    iqd = iqd * fma(-0.5 * qd * iqd, iqd, 1.5);
+    const double iqd = rsqrt64(qd);
     const double dcd = Dd * iqd, ecd = (Dd + td) * iqd;
     const double k1 = -2.0 * dcd * grgd;
     const double k2 = g2gd * (ecd * ecd - 1.0) + 1.0 - dcd * dcd * grd * grd;
     const double k4 = ecd * ecd - 1.0;
     const double et = 2.0 * dcd * grd;
-    double xd = x;
+    double xd = fabsf(x0) < big ? (double)x0 : 1.0;
     // from the FP32 iterate a solvable state converges in one to three steps; a state without a
     // physical root gives up after 8 (reported through the status word)
     for (int it = 0; it < 8; it++) {
         const double x2 = xd * xd;
         const double f = k4 * x2 * xd * (xd - et) + k2 * x2 + k1 * xd + k0;
         const double fp = k1 + 2.0 * k2 * xd + 4.0 * k4 * x2 * xd - 3.0 * et * k4 * x2;
-        double ifp = (double)frcp((float)fp);
-        ifp = ifp * fma(-fp, ifp, 2.0);
-        const double step = f * ifp;
+        const double step = f * rcp64(fp);
         xd -= step;
-        if (fabs(step) < 1e-7) return SRStage64{(float)xd, true};
+        if (fabs(step) < 1e-7) {
+            o.conv = true;
+            break;
+        }
     }
-    return SRStage64{(float)xd, false};
+    // RelativisticEuler/RelativisticEulerStateVector.cpp:82-101 in FP64
+    const double ex = ecd * xd;
+    const double a = 1.0 + 4.0 * grd * (1.0 - dcd * xd) * rcp64(ex * ex);
+    if (!(a >= 0.0 && fabs(xd) < 1e300)) return o;
+    const double W = 0.5 * ex * (1.0 + (a > 0.0 ? a * rsqrt64(a) : 0.0));
+    const double h = rcp64(dcd * xd);
+    double rho = Dd * rcp64(W);
+    const double rhw = rho * h * W * W;
+    const double irhw = rcp64(rhw);
+    double p = (rhw - Dd) - td;
+    rho = rho < 1e-8 ? 1e-8 : rho;
+    p = p < 1e-8 ? 1e-8 : p;
+    const double vx = Sxd * irhw, vy = Syd * irhw, vz = Szd * irhw;
+    const double lim = 1e30;
+    if (!(fabs(W) < lim && fabs(h) < lim && rho < lim && p < lim && fabs(vx) < lim && fabs(vy) < lim &&
+          fabs(vz) < lim))
+        return o;
+    o.c.W = (float)W;
+    o.c.h = (float)h;
+    o.c.rho = (float)rho;
+    o.c.p = (float)p;
+    o.c.vx = (float)vx;
+    o.c.vy = (float)vy;
+    o.c.vz = (float)vz;
+    return o;
 }
 
 // Primitive recovery of one FP32 conserved state; sets bit 0 of *flags when neither stage converged.
@@ -108,23 +164,26 @@ CG_D SRPrim32 sr_c2p_fast(const SRFastParams& P, const float* u, int* flags) {
     const float eta = 2.0f * dc * gr;
     float x = 1.0f;
     bool conv = false;
-    for (int it = 0; it < 40; it++) {
-        const float x2 = x * x;
-        const float f = c4 * x2 * x * (x - eta) + c2 * x2 + c1 * x + c0;
-        const float fp = c1 + 2.0f * c2 * x + 4.0f * c4 * x2 * x - 3.0f * eta * c4 * x2;
-        const float nx = x - fdiv(f, fp);
-        const bool done = fabsf(nx - x) <= 1e-6f * fabsf(x);
-        x = nx;
-        if (done) { conv = true; break; }
+    // coefficients beyond FP32's range (or a non-finite state) go to the FP64 stage directly
+    if (fabsf(c4) < 1e30f && fabsf(c2) < 1e30f && fabsf(c1) < 1e30f && fabsf(eta) < 1e30f) {
+        for (int it = 0; it < 40; it++) {
+            const float x2 = x * x;
+            const float f = c4 * x2 * x * (x - eta) + c2 * x2 + c1 * x + c0;
+            const float fp = c1 + 2.0f * c2 * x + 4.0f * c4 * x2 * x - 3.0f * eta * c4 * x2;
+            const float nx = x - fdiv(f, fp);
+            if (!(fabsf(nx) < 1e30f)) break;  // overflowing iterate: the FP64 stage takes over
+            const bool done = fabsf(nx - x) <= 1e-6f * fabsf(x);
+            x = nx;
+            if (done) { conv = true; break; }
+        }
     }
-    float W = 0.5f * ec * x * (1.0f + fsqrt(1.0f + fdiv(4.0f * gr * (1.0f - dc * x), ec * ec * x * x)));
-    if (!conv || W > P.w64) {
-        const SRStage64 r = sr_c2p_stage64(P.grd, P.k0d, P.grgd, P.g2gd, D, Sx, Sy, Sz, tau, x);
-        conv = r.conv;
-        x = r.x;
-        W = 0.5f * ec * x * (1.0f + fsqrt(1.0f + fdiv(4.0f * gr * (1.0f - dc * x), ec * ec * x * x)));
+    const float W = 0.5f * ec * x * (1.0f + fsqrt(1.0f + fdiv(4.0f * gr * (1.0f - dc * x), ec * ec * x * x)));
+    if (!conv || !(W <= P.w64)) {
+        // from the FP32 iterate unless it ran far off (then from the reference's start, 1)
+        const SRStage64 r = sr_c2p_stage64(P.grd, P.k0d, P.grgd, P.g2gd, D, Sx, Sy, Sz, tau, fabsf(x) < 1e3f ? x : 1.0f);
+        if (!r.conv && flags) *flags |= 1;
+        return r.c;
     }
-    if (!conv && flags) *flags |= 1;
     SRPrim32 r;
     r.W = W;
     r.h = frcp(dc * x);
@@ -162,7 +221,10 @@ CG_D void sr_flux_fast(const SRFastParams& P, const float* u, float* f, int* fla
 // v (clamped where v^2 > 1 - 1e-8), h from rho and p (RelativisticEulerEquationOfState.cpp:3-8)
 CG_D void sr_cons_of(const SRFastParams& P, const SRPrim32& c, float* u) {
     const float v2 = c.vx * c.vx + c.vy * c.vy + c.vz * c.vz;
-    const float W = frsqrt(1.0f - (v2 > 1.0f - 1e-8f ? 1.0f - 1e-8f : v2));
+    // the reference's clamp of v^2 to 1 - 1e-8 (W <= 1e4), applied to 1 - v^2: in FP32, 1 - 1e-8
+    // rounds to 1, which would make W infinite
+    const float omv = 1.0f - v2;
+    const float W = frsqrt(omv < 1e-8f ? 1e-8f : omv);
     const float h = 1.0f + fdiv(c.p, c.rho) * P.hfac;
     const float rhw = c.rho * h * W * W;
     u[0] = c.rho * W;

@@ -53,6 +53,45 @@ def test_gr_fp32_accretion_vs_oracle(cg, oracle, above):
     assert l1 < 1e-4, l1
 
 
+def test_gr_fp32_long_accretion_stays_finite(cg):
+    """Config-4 geometry at 256^2 for 40 steps: after about a dozen steps the inflow next to the
+    horizon reaches the reference's rootless recovery states (density floor, superluminal garbage
+    velocities whose conserved values outgrow FP32's range); the FP32 path hands those to its FP64
+    stage and keeps every cell and the CFL time step finite."""
+    n = 256
+    s = accretion(n, 4)
+    g = cg.Grid(2, (n, n), 20.0 / n, G53, 1, 0, cg.BlackHoleSpacetime(1.0, 0.0, 10.0, 10.0, 0.0))
+    g.set_prim(s)
+    r = g.solve(2, 0.9, 1e9, 0.0, 1, subcycles=1, max_steps=40)
+    assert r.steps == 40 and np.isfinite(r.t)
+    assert np.isfinite(g.get_prim()).all()
+
+
+def test_gr_fp32_lorentz_cap_keeps_states_finite(cg):
+    """Primitives with gamma_ij v^i v^j >= 1 (the density floor next to the horizon reaches them):
+    the conserved state caps W at 1e4 as the reference does (v^2 clamped to 1 - 1e-8).  In FP32 the
+    clamp value 1 - 1e-8 rounds to 1 (W would be infinite), so the cap is applied to 1 - v^2.  A
+    source step and both sweeps on such cells stay finite wherever the FP64 path does."""
+    n = 32
+    s = accretion(n, 5)
+    s[20, 10:20, 0] = 1e-8
+    s[20, 10:20, 1] = 1.5
+    s[20, 10:20, 4] = 1e-8
+    dx = 20.0 / n
+    out = {}
+    for prec in (0, 1):
+        g = cg.Grid(2, (n, n), dx, G53, prec, 0, cg.BlackHoleSpacetime(1.0, 0.0, 10.0, 10.0, 0.0))
+        g.set_prim(s)
+        g.rk_source(0.01, 0.0, 1)
+        g.sweep(0, 2, 0.01, 0.0, 1)
+        g.sweep(1, 2, 0.01, 0.0, 1)
+        out[prec] = g.get_prim()
+        g.close()
+    fin64 = np.isfinite(out[0]).all(axis=-1)
+    assert fin64[20, 10:20].all()
+    assert np.isfinite(out[1][fin64]).all()
+
+
 @pytest.mark.parametrize("bhname,bh", [("bh", cases.GR_BH), ("spin", cases.GR_BH_SPIN)])
 @pytest.mark.parametrize("dims", [1, 2])
 def test_gr_fp32_sweeps_and_source_vs_oracle(cg, oracle, bhname, bh, dims):
