@@ -75,32 +75,19 @@ CG_D double rsqrt64(double a) {
 }
 
 struct SRStage64 {
-    SRPrim32 c;
+    float x;
     bool conv;
 };
 
 // The recovery's FP64 stage: Newton on the quartic with coefficients in FP64 (they cancel at high
-// Lorentz factor) from the FP32 iterate x0 (from the reference's start 1 when x0 is not finite),
-// then the primitives in FP64 with the reference's floors.  It takes the states the FP32 stage
-// cannot: Lorentz factor above the threshold, no FP32 convergence, or coefficients beyond FP32's
-// range -- near the horizon the reference's recovery meets states without a physical root whose
-// garbage primitives grow through the W cap and the fluxes to magnitudes (|S| ~ 1e30) that only
-// FP64 holds.  A state that is not finite, or whose primitives are not, becomes the floor state
-// (rho = p = 1e-8 at rest).  Out of line: kernels call the recovery at dozens of sites (39 per GR
-// source step) and this rarely taken stage would otherwise be inlined at each.
+// Lorentz factor) from x0 (the FP32 iterate, or the reference's start 1), 1/sqrt(q) and each
+// step's 1/f' through rcp64 / rsqrt64.  Out of line: kernels call the recovery at dozens of sites
+// (39 per GR source step) and this rarely taken stage would otherwise be inlined at each; it is
+// kept small because its registers add to those live at every call site.
 static __device__ __noinline__ SRStage64 sr_c2p_stage64(double grd, double k0, double grgd, double g2gd, float D,
                                                         float Sx, float Sy, float Sz, float tau, float x0) {
-    SRStage64 o;
-    o.conv = false;
-    o.c.rho = 1e-8f;
-    o.c.vx = o.c.vy = o.c.vz = 0.0f;
-    o.c.p = 1e-8f;
-    o.c.W = 1.0f;
-    o.c.h = (float)(1.0 + 1.0 / grd);  // 1 + (p / rho) gamma / (gamma - 1) at the floors
-    const float big = 3.0e38f;
-    if (!(fabsf(D) < big && fabsf(Sx) < big && fabsf(Sy) < big && fabsf(Sz) < big && fabsf(tau) < big)) return o;
-    const double Dd = D, td = tau, Sxd = Sx, Syd = Sy, Szd = Sz;
-    double qd = (td + Dd) * (td + Dd) - (Sxd * Sxd + Syd * Syd + Szd * Szd);
+    const double Dd = D, td = tau;
+    double qd = (td + Dd) * (td + Dd) - ((double)Sx * Sx + (double)Sy * Sy + (double)Sz * Sz);
     qd = qd < 1e-8 ? 1e-8 : qd;
     const double iqd = rsqrt64(qd);
     const double dcd = Dd * iqd, ecd = (Dd + td) * iqd;
@@ -108,7 +95,7 @@ static __device__ __noinline__ SRStage64 sr_c2p_stage64(double grd, double k0, d
     const double k2 = g2gd * (ecd * ecd - 1.0) + 1.0 - dcd * dcd * grd * grd;
     const double k4 = ecd * ecd - 1.0;
     const double et = 2.0 * dcd * grd;
-    double xd = fabsf(x0) < big ? (double)x0 : 1.0;
+    double xd = x0;
     // from the FP32 iterate a solvable state converges in one to three steps; a state without a
     // physical root gives up after 8 (reported through the status word)
     for (int it = 0; it < 8; it++) {
@@ -117,39 +104,16 @@ static __device__ __noinline__ SRStage64 sr_c2p_stage64(double grd, double k0, d
         const double fp = k1 + 2.0 * k2 * xd + 4.0 * k4 * x2 * xd - 3.0 * et * k4 * x2;
         const double step = f * rcp64(fp);
         xd -= step;
-        if (fabs(step) < 1e-7) {
-            o.conv = true;
-            break;
-        }
+        if (fabs(step) < 1e-7) return SRStage64{(float)xd, true};
     }
-    // RelativisticEuler/RelativisticEulerStateVector.cpp:82-101 in FP64
-    const double ex = ecd * xd;
-    const double a = 1.0 + 4.0 * grd * (1.0 - dcd * xd) * rcp64(ex * ex);
-    if (!(a >= 0.0 && fabs(xd) < 1e300)) return o;
-    const double W = 0.5 * ex * (1.0 + (a > 0.0 ? a * rsqrt64(a) : 0.0));
-    const double h = rcp64(dcd * xd);
-    double rho = Dd * rcp64(W);
-    const double rhw = rho * h * W * W;
-    const double irhw = rcp64(rhw);
-    double p = (rhw - Dd) - td;
-    rho = rho < 1e-8 ? 1e-8 : rho;
-    p = p < 1e-8 ? 1e-8 : p;
-    const double vx = Sxd * irhw, vy = Syd * irhw, vz = Szd * irhw;
-    const double lim = 1e30;
-    if (!(fabs(W) < lim && fabs(h) < lim && rho < lim && p < lim && fabs(vx) < lim && fabs(vy) < lim &&
-          fabs(vz) < lim))
-        return o;
-    o.c.W = (float)W;
-    o.c.h = (float)h;
-    o.c.rho = (float)rho;
-    o.c.p = (float)p;
-    o.c.vx = (float)vx;
-    o.c.vy = (float)vy;
-    o.c.vz = (float)vz;
-    return o;
+    return SRStage64{(float)xd, false};
 }
 
 // Primitive recovery of one FP32 conserved state; sets bit 0 of *flags when neither stage converged.
+// Near the horizon the reference's recovery meets states without a physical root, whose garbage
+// primitives grow through the W cap and the fluxes to magnitudes beyond FP32's range (|S| ~ 1e30;
+// the reference's FP64 holds them, with garbage values of its own): where the coefficients or the
+// result leave FP32's range, the result is the floor state (rho = p = 1e-8 at rest).
 CG_D SRPrim32 sr_c2p_fast(const SRFastParams& P, const float* u, int* flags) {
     const float D = u[0], Sx = u[1], Sy = u[2], Sz = u[3], tau = u[4];
     const float gr = P.gr;
@@ -162,27 +126,26 @@ CG_D SRPrim32 sr_c2p_fast(const SRFastParams& P, const float* u, int* flags) {
     const float c2 = P.g2g * (ec * ec - 1.0f) + 1.0f - dc * dc * gr * gr;
     const float c4 = ec * ec - 1.0f;
     const float eta = 2.0f * dc * gr;
-    float x = 1.0f;
+    // coefficients beyond FP32's range (or a non-finite state): no iteration, the floor state below
+    const bool inrange = fabsf(c4) + fabsf(c2) + fabsf(c1) < 1e30f;
+    float x = inrange ? 1.0f : 0.0f;
     bool conv = false;
-    // coefficients beyond FP32's range (or a non-finite state) go to the FP64 stage directly
-    if (fabsf(c4) < 1e30f && fabsf(c2) < 1e30f && fabsf(c1) < 1e30f && fabsf(eta) < 1e30f) {
-        for (int it = 0; it < 40; it++) {
-            const float x2 = x * x;
-            const float f = c4 * x2 * x * (x - eta) + c2 * x2 + c1 * x + c0;
-            const float fp = c1 + 2.0f * c2 * x + 4.0f * c4 * x2 * x - 3.0f * eta * c4 * x2;
-            const float nx = x - fdiv(f, fp);
-            if (!(fabsf(nx) < 1e30f)) break;  // overflowing iterate: the FP64 stage takes over
-            const bool done = fabsf(nx - x) <= 1e-6f * fabsf(x);
-            x = nx;
-            if (done) { conv = true; break; }
-        }
+    for (int it = 0; inrange && it < 40; it++) {
+        const float x2 = x * x;
+        const float f = c4 * x2 * x * (x - eta) + c2 * x2 + c1 * x + c0;
+        const float fp = c1 + 2.0f * c2 * x + 4.0f * c4 * x2 * x - 3.0f * eta * c4 * x2;
+        const float nx = x - fdiv(f, fp);
+        const bool done = fabsf(nx - x) <= 1e-6f * fabsf(x);
+        x = nx;
+        if (done) { conv = true; break; }
     }
-    const float W = 0.5f * ec * x * (1.0f + fsqrt(1.0f + fdiv(4.0f * gr * (1.0f - dc * x), ec * ec * x * x)));
-    if (!conv || !(W <= P.w64)) {
-        // from the FP32 iterate unless it ran far off (then from the reference's start, 1)
+    float W = 0.5f * ec * x * (1.0f + fsqrt(1.0f + fdiv(4.0f * gr * (1.0f - dc * x), ec * ec * x * x)));
+    if (inrange && (!conv || !(W <= P.w64))) {  // also a non-finite iterate
+        // from the FP32 iterate unless it ran off (then from the reference's start, 1)
         const SRStage64 r = sr_c2p_stage64(P.grd, P.k0d, P.grgd, P.g2gd, D, Sx, Sy, Sz, tau, fabsf(x) < 1e3f ? x : 1.0f);
-        if (!r.conv && flags) *flags |= 1;
-        return r.c;
+        conv = r.conv;
+        x = r.x;
+        W = 0.5f * ec * x * (1.0f + fsqrt(1.0f + fdiv(4.0f * gr * (1.0f - dc * x), ec * ec * x * x)));
     }
     SRPrim32 r;
     r.W = W;
@@ -196,6 +159,15 @@ CG_D SRPrim32 sr_c2p_fast(const SRFastParams& P, const float* u, int* flags) {
     r.p = (rhw - D) - tau;
     r.rho = r.rho < 1e-8f ? 1e-8f : r.rho;
     r.p = r.p < 1e-8f ? 1e-8f : r.p;
+    // one test for every output: non-finite or beyond 1e30 (a NaN or an infinity carries through the sum)
+    if (!(fabsf(W) + fabsf(r.h) + r.rho + r.p + fabsf(r.vx) + fabsf(r.vy) + fabsf(r.vz) < 1e30f)) {
+        conv = false;
+        r.rho = r.p = 1e-8f;
+        r.vx = r.vy = r.vz = 0.0f;
+        r.W = 1.0f;
+        r.h = 1.0f + P.hfac;  // 1 + (p / rho) gamma / (gamma - 1) at the floors
+    }
+    if (!conv && flags) *flags |= 1;
     return r;
 }
 
