@@ -208,11 +208,11 @@ GRFastPolicy<AXIS, LIM, MASKED> make_pol(const SweepArgs& a, double bias) {
 }
 
 constexpr int kXThreads = 256;
-// One warp of columns per Y block: the cells near the hole (FP64 recovery stage) make some column
-// segments several times costlier than the rest, and 32 blocks of 32 x 32 cells per 1024 columns
-// spread them over the SMs better than 8 blocks of 128 x 32.
+// One warp of columns per Y block, 16 rows per segment: the cells near the hole (FP64 recovery
+// stage) make some column segments several times costlier than the rest, and many small blocks
+// spread them over the SMs (at 1024^2, 2048 blocks of 32 x 16 cells against 256 of 128 x 32).
 constexpr int kYThreads = 32;
-constexpr int kYSeg = 32;
+constexpr int kYSeg = 16;
 
 template <int AXIS, int LIM, bool MASKED>
 void run(const SweepArgs& a) {
