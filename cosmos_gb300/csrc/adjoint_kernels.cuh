@@ -283,7 +283,7 @@ CG_D void st_lanes(float* p, size_t q0, size_t q1, bool vec, bool two, f2 v) {
 }
 
 template <class V, class S, bool PRIM, int AX, int LIM, int P, int W>
-__global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 2 : (sizeof(V) == 4 ? 3 : 1))))
+__global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 512 / (P * W) : (sizeof(V) == 4 ? 3 : 1))))
     adjoint_sweep_kernel(AdjSweepParams a) {
     using T = typename Lane<V>::S;
     constexpr int NL = Lane<V>::N;
@@ -562,13 +562,15 @@ __global__ void adjoint_grad_kernel(Geom G, double gamma, T ig1, const S* state,
 
 namespace cg {
 
-// Launch the sweep adjoint for one axis.  Tiles of 256 threads: X lines of 256 positions (248
-// updated cells); Y lines of 64 positions (56 cells) x 4 threads across.  FP32 carries two lines per
-// thread (f2: two rows for X, two adjacent columns for Y), FP64 one.  Persistent: as many blocks as
+// Launch the sweep adjoint for one axis.  X tiles: lines of 128 positions (120 updated cells; 128
+// threads, four blocks per SM: smaller blocks wait less at the phase barriers) in FP32, of 256 in
+// FP64; Y tiles: 64 positions (56 cells) x 4 threads across (256 threads; four column pairs keep
+// each row access a whole 32-byte sector).  FP32 carries two lines per thread (f2: two rows for X,
+// two adjacent columns for Y), FP64 one.  Persistent: as many blocks as
 // stay resident, each walking tiles t, t + gridDim.x, ... with the next tile's inputs in flight.
 template <class V, class S, bool PRIM, int AX, int LIM>
 cudaError_t launch_adjoint_sweep_t(const AdjSweepParams& a, cudaStream_t st) {
-    constexpr int P = AX == 0 ? 256 : 64;
+    constexpr int P = AX == 0 ? (Lane<V>::N == 2 ? 128 : 256) : 64;
     constexpr int W = AX == 0 ? 1 : 4;
     constexpr int TS = P - 8;
     constexpr int LB = W * Lane<V>::N;  // lines per block

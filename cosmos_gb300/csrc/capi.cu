@@ -176,6 +176,36 @@ int enqueue_step(cosmos_grid* g, int cur, int* cur_out, unsigned* nk) {
 
 }  // namespace
 
+namespace cg {
+// One step of a Newtonian or SR run -- the launches enqueue_step records into the step graph, with
+// the same device time step -- on explicit buffers: the step reads `src` and its sweep k writes
+// dst[k] (three sweeps in 2D, one in 1D).
+int enqueue_step_into(cosmos_grid* g, const void* src, void* const* dst) {
+    if (g->p.system == COSMOS_GR) return fail(COSMOS_EUNSUPPORTED, "explicit-buffer steps cover the Newtonian and SR systems");
+    const cosmos_solve_opts& o = g->run;
+    CK(launch_dt_kernel(g->ctl, g->ctx->stream));
+    SweepArgs a = base_args(g);
+    a.order = o.order;
+    a.bias = o.bias;
+    a.lim = o.limiter;
+    a.out.status = &g->ctl->status;
+    a.ds.ctl = g->ctl;
+    const int ns = g->p.dims == 2 ? 3 : 1;
+    for (int k = 0; k < ns; k++) {
+        const double scale = ns == 3 && k != 1 ? 0.5 : 1.0;
+        a.G.axis = ns == 3 && k == 1 ? 1 : 0;
+        a.ds.scale = scale;
+        a.ds.nsub = 0;
+        a.ds.fsel = scale == 0.5 ? 1 : 0;
+        a.src = k == 0 ? src : dst[k - 1];
+        a.dst = dst[k];
+        a.out.ws_ctl = k == ns - 1 ? g->ctl : nullptr;  // the CFL reduction of the step's last sweep
+        CK(sweep_launch(g, a));
+    }
+    return COSMOS_OK;
+}
+}  // namespace cg
+
 extern "C" {
 
 const char* cosmos_version(void) { return "cosmos_gb300 0.1 (sm_103a)"; }

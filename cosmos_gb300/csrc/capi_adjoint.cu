@@ -4,9 +4,10 @@
 // Forward: the grid's own graph-replayed steps (device dt from the CFL rule, or the caller's dts),
 // the state copied to a checkpoint store before every segment and each step's dt logged.
 // Backward, segment by segment from the last: the segment is recomputed from its checkpoint with
-// the same sweep kernels and the same dts, keeping every sweep's input; the sweep adjoints then
-// run in reverse order (X(dt/2) Y(dt) X(dt/2) per 2D step, X(dt) per 1D step).  The next
-// segment's recomputation overlaps the current segment's adjoints on a second stream.
+// the same sweep kernels and the same dts, keeping every sweep's input (the last segment keeps
+// them during the forward pass); the sweep adjoints then run in reverse order (X(dt/2) Y(dt)
+// X(dt/2) per 2D step, X(dt) per 1D step).  The next segment's recomputation overlaps the current
+// segment's adjoints on a second stream.
 #include <algorithm>
 #include <climits>
 #include <cstddef>
@@ -119,9 +120,27 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
     const void* dtp[2] = {logp, fixp};
     sc.patched = g->ctl;
     ACK(cudaMemcpyAsync((char*)g->ctl + offsetof(StepCtl, dt_log), dtp, sizeof dtp, cudaMemcpyHostToDevice, st));
+    auto slot = [&](int c, int q) { return seg + ((size_t)(c & 1) * K * spp + q) * sbytes; };
     for (int c = 0; c < nck; c++) {
         ACK(cudaMemcpyAsync(ck + (size_t)c * sbytes, g->buf[g->cur], sbytes, cudaMemcpyDeviceToDevice, st));
-        if ((rc = cosmos_grid_run_steps(g, std::min(K, nsteps - c * K)))) return rc;
+        const int ns = std::min(K, nsteps - c * K);
+        if (c < nck - 1) {
+            if ((rc = cosmos_grid_run_steps(g, ns))) return rc;
+            continue;
+        }
+        // The last segment, reversed first, keeps every sweep's input in the segment store as it
+        // runs (same kernels and device time steps as the graph-replayed steps), so its reversal
+        // starts without a recomputation; the final state goes to the grid's other buffer.
+        ACK(cudaMemcpyAsync(slot(c, 0), g->buf[g->cur], sbytes, cudaMemcpyDeviceToDevice, st));
+        for (int s = 0; s < ns; s++) {
+            void* outs[3];
+            for (int k = 0; k < spp; k++) {
+                const int q = s * spp + k + 1;
+                outs[k] = q < ns * spp ? (void*)slot(c, q) : g->buf[g->cur ^ 1];
+            }
+            if ((rc = enqueue_step_into(g, slot(c, s * spp), outs))) return rc;
+        }
+        g->cur ^= 1;
     }
     ACK(cudaEventRecord(sc.ev[1], st));
     sc.unpatch();  // the controller's dt pointers point into this call's scratch
@@ -155,7 +174,6 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
     cudaStream_t rs = g->ctx->copy;
     fa.stream = rs;
     for (int k = 0; k < 2; k++) ACK(cudaEventRecord(sc.adj_done[k], st));  // after the forward pass and the loss
-    auto slot = [&](int c, int q) { return seg + ((size_t)(c & 1) * K * spp + q) * sbytes; };
     auto sweep_of = [&](int c, int q, int& axis, double& dt) {
         const double d = dts[c * K + q / spp];
         const int m = q % spp;
@@ -181,7 +199,7 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
         ACK(cudaEventRecord(sc.rec_done[c & 1], rs));
         return COSMOS_OK;
     };
-    if ((rc = recompute(nck - 1))) return rc;
+    ACK(cudaEventRecord(sc.rec_done[(nck - 1) & 1], st));  // the last segment is in the store already
     for (int c = nck - 1; c >= 0; c--) {
         if (c > 0 && (rc = recompute(c - 1))) return rc;
         ACK(cudaStreamWaitEvent(st, sc.rec_done[c & 1], 0));
