@@ -208,11 +208,13 @@ GRFastPolicy<AXIS, LIM, MASKED> make_pol(const SweepArgs& a, double bias) {
 }
 
 constexpr int kXThreads = 256;
-// One warp of columns per Y block, 16 rows per segment: the cells near the hole (FP64 recovery
+// One warp of columns per Y block, 8 rows per segment: the cells near the hole (FP64 recovery
 // stage) make some column segments several times costlier than the rest, and many small blocks
-// spread them over the SMs (at 1024^2, 2048 blocks of 32 x 16 cells against 256 of 128 x 32).
+// spread them over the SMs (at 1024^2, 4096 blocks of 32 x 8 cells against 256 of 128 x 32; the
+// 4-row halo of each segment costs less than the imbalance it removes: 2.49 vs 2.65 ms per step
+// against 32 x 16).
 constexpr int kYThreads = 32;
-constexpr int kYSeg = 16;
+constexpr int kYSeg = 8;
 
 template <int AXIS, int LIM, bool MASKED>
 void run(const SweepArgs& a) {
