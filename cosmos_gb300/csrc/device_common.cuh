@@ -51,7 +51,6 @@ struct StepCtl {
     int active;        // 1 while the current step runs, 0 once t >= t_final or it >= it_limit
     int status;        // sticky error bits, see COSMOS_STATUS_* in the public header
     unsigned long long smax[2];  // wavespeed maxima (bit patterns of non-negative doubles), ping-pong by it parity
-    unsigned long long newton_cap_hits;  // con2prim solves that reached the 1000-iteration cap
     FastCoef fc[2];    // FP32 coefficients of dt (fc[0]) and dt/2 (fc[1]), formed by the dt kernel
     double* dt_log;           // non-null: the dt kernel records each step's dt at dt_log[it]
     const double* dt_fixed;   // non-null: step `it` takes dt_fixed[it] instead of the CFL rule

@@ -37,7 +37,9 @@ extern "C" {
 
 /* ---- device status bits reported by cosmos_solve_result.status */
 #define COSMOS_STATUS_NONFINITE 1  /* non-finite or non-positive dt was produced */
-#define COSMOS_STATUS_NEWTON_CAP 2 /* a con2prim Newton solve stopped at its 1000-iteration cap */
+#define COSMOS_STATUS_NEWTON_CAP 2 /* a con2prim Newton solve stopped at its iteration cap (FP64 path: the
+                                      reference's 1000; FP32 path: 40 FP32 + 8 FP64), or (FP32 path) a state
+                                      beyond FP32's range was replaced by the floor state */
 
 /* ---- enumerations */
 enum { COSMOS_NEWTONIAN = 0, COSMOS_SR = 1, COSMOS_GR = 2 };
