@@ -1066,6 +1066,98 @@ void orc_amr_derefine(int sys, double* coarse_prim, const double* fine_prim, int
         }
 }
 
+// ---------------------------------------------------------------- AMR Level-1 driver
+// EulerAMR::solveLevel1AMR (AMR/EulerAMR.cpp:169-350) and solve2DLevel1AMR (:352-592); the SR
+// drivers (AMR/RelativisticEulerAMR.cpp) are the same loop with the SR state (their only other
+// difference, the 2D flag pass's bottom neighbour, is inside orc_amr_flags).  Per coarse step:
+// dt from the coarse grid with the TOTAL fine iteration count (:197-198); flag pass (:200-229);
+// masked coarse step with bias 0 and limiter 1 (:231-239); while any fine flag is set, fine steps
+// of dx/2 until the fine time passes (t + dt) - 1e-4, each dt from the whole fine grid (:253-277);
+// otherwise the fine count still advances (:279-282); restriction of flagged-off coarse cells and
+// injection into unflagged fine cells (:287-307); derefinement (:309-345).  coarse/fine receive
+// the final primitive grids, cflags/fflags the final flags; *fine_steps the fine step count.
+// Returns the number of coarse steps.
+int orc_amr_level1(int sys, const double* prim, int ny, int nx, int dims, double dx, double cfl, double tf,
+                   double tol, int order, double gamma, double* coarse, double* fine, unsigned char* cflags,
+                   unsigned char* fflags, int* fine_steps) {
+    if (dims == 1) ny = 1;
+    const int fny = dims == 1 ? 1 : 2 * ny, fnx = 2 * nx;
+    const size_t nc = (size_t)ny * nx;
+    auto kids = [&](int i, int j, size_t* k) -> int {
+        if (dims == 1) { k[0] = 2 * (size_t)j; k[1] = 2 * (size_t)j + 1; return 2; }
+        const size_t fw = (size_t)fnx;
+        k[0] = (2 * (size_t)i) * fw + 2 * j; k[1] = k[0] + 1;
+        k[2] = (2 * (size_t)i + 1) * fw + 2 * j; k[3] = k[2] + 1;
+        return 4;
+    };
+    auto cons_of = [&](const double* p, double* u) {
+        if (sys == 0) Newton<double>{gamma}.cons(p, Pt{0, 0, 0}, u); else SR{gamma}.cons(p, Pt{0, 0, 0}, u);
+    };
+    auto prim_of = [&](const double* u, double* p) {
+        if (sys == 0) Newton<double>{gamma}.prim(u, Pt{0, 0, 0}, p); else SR{gamma}.prim(u, Pt{0, 0, 0}, p);
+    };
+    std::memcpy(coarse, prim, nc * 5 * sizeof(double));
+    for (int i = 0; i < ny; i++)
+        for (int j = 0; j < nx; j++) {
+            size_t k[4];
+            const int nk = kids(i, j, k);
+            cflags[(size_t)i * nx + j] = 1;
+            for (int q = 0; q < nk; q++) {
+                fflags[k[q]] = 0;
+                std::memcpy(fine + 5 * k[q], coarse + 5 * ((size_t)i * nx + j), 5 * sizeof(double));
+            }
+        }
+    auto step = [&](double* p, int gy, int gx, double h, double dt, const unsigned char* m) {
+        if (dims == 1) {
+            orc_sweep(sys, p, 1, gx, 1, 0, order, h, dt, 0.0, 1, gamma, 0, m, nullptr);
+        } else {
+            orc_sweep(sys, p, gy, gx, 2, 0, order, h, dt * 0.5, 0.0, 1, gamma, 0, m, nullptr);
+            orc_sweep(sys, p, gy, gx, 2, 1, order, h, dt, 0.0, 1, gamma, 0, m, nullptr);
+            orc_sweep(sys, p, gy, gx, 2, 0, order, h, dt * 0.5, 0.0, 1, gamma, 0, m, nullptr);
+        }
+    };
+    double t = 0.0;
+    int it = 0, fit = 0;
+    while (t < tf) {
+        const double dt = orc_stable_dt(sys, coarse, ny, nx, dims, dx, cfl, t, tf, fit, gamma, nullptr);
+        orc_amr_flags(sys, coarse, ny, nx, dims, dx, tol, gamma, nullptr, cflags, fflags);
+        step(coarse, ny, nx, dx, dt, cflags);
+        bool refined = false;
+        for (size_t q = 0; q < (size_t)fny * fnx; q++) refined = refined || fflags[q];
+        if (refined) {
+            double ft = t;
+            while (ft < (t + dt - 1e-4)) {
+                const double fdt = orc_stable_dt(sys, fine, fny, fnx, dims, dx * 0.5, cfl, ft, t + dt, fit, gamma, nullptr);
+                step(fine, fny, fnx, dx * 0.5, fdt, fflags);
+                ft += fdt;
+                fit += 1;
+            }
+        } else {
+            fit += 1;
+        }
+        t += dt;
+        it += 1;
+        for (int i = 0; i < ny; i++)
+            for (int j = 0; j < nx; j++) {
+                size_t k[4];
+                const int nk = kids(i, j, k);
+                double* cp = coarse + 5 * ((size_t)i * nx + j);
+                if (!cflags[(size_t)i * nx + j]) {
+                    double u[4][5], avg[5];
+                    for (int q = 0; q < nk; q++) cons_of(fine + 5 * k[q], u[q]);
+                    for (int f = 0; f < 5; f++)
+                        avg[f] = nk == 2 ? 0.5 * (u[0][f] + u[1][f]) : 0.25 * (((u[0][f] + u[1][f]) + u[2][f]) + u[3][f]);
+                    prim_of(avg, cp);
+                }
+                for (int q = 0; q < nk; q++)
+                    if (!fflags[k[q]]) std::memcpy(fine + 5 * k[q], cp, 5 * sizeof(double));
+            }
+        orc_amr_derefine(sys, coarse, fine, ny, nx, dims, dx, tol, gamma, nullptr, cflags, fflags);
+    }
+    if (fine_steps) *fine_steps = fit;
+    return it;
+}
+
 // ---------------------------------------------------------------- tangent-linear (Newtonian)
 // Directional derivative of the SLIC loss L = 1/2 sum_cells (rho_T - rho_target)^2 after
 // `nsteps` steps with the step sizes dts[] held fixed (the adjoint's convention), along the

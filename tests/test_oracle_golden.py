@@ -126,3 +126,25 @@ def test_amr_flag_and_derefine_passes(oracle, golden, tag, system):
         assert bit_equal(cp.reshape(-1), golden[k + "_coarse"]) and bit_equal(fp.reshape(-1), golden[k + "_fine"]), k
         n += 1
     assert n == 6
+
+
+def amr_golden():
+    import os
+    return dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "amr_level1_golden.npz")))
+
+
+def test_amr_level1_driver(oracle):
+    """The oracle's Level-1 AMR driver against the reference's solveLevel1AMR / solve2DLevel1AMR runs
+    (Newtonian and SR, 1D and 2D, FORCE and SLIC; several coarse steps with fine sub-cycles)."""
+    G = amr_golden()
+    keys = _keys(G, "amr")
+    assert len(keys) == 8
+    for k in keys:
+        s = G[k + "_in"]
+        system, dims, T, order, tol, nsteps = G[k + "_args"]
+        system, order = int(system), int(order)
+        n, nf, cp, fp, cf, ff = oracle.amr_level1(system, s, 1.0 / s.shape[-2], 0.9, T, tol, order,
+                                                  cases.SYS_GAMMA[system])
+        assert n == int(nsteps) and nf > n, k
+        assert bit_equal(cp, G[k + "_coarse"]) and bit_equal(fp, G[k + "_fine"]), k
+        assert bit_equal(cf, G[k + "_cflags"]) and bit_equal(ff, G[k + "_fflags"]), k
