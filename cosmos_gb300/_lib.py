@@ -25,6 +25,11 @@ class Params(ctypes.Structure):
                 ("sr_c2p64_above", ctypes.c_double)]
 
 
+class AmrResult(ctypes.Structure):
+    _fields_ = [("coarse_steps", ctypes.c_int), ("fine_steps", ctypes.c_int), ("t", ctypes.c_double),
+                ("status", ctypes.c_int)]
+
+
 class SolveOpts(ctypes.Structure):
     _fields_ = [("order", ctypes.c_int), ("cfl", ctypes.c_double), ("t_final", ctypes.c_double),
                 ("bias", ctypes.c_double), ("limiter", ctypes.c_int), ("subcycles", ctypes.c_int),
@@ -68,6 +73,11 @@ SIGNATURES = {
                                ctypes.POINTER(SolveResult)]),
     "cosmos_field_sums_noalloc": (_i, [_p, _i, _i, _i, _i, _sz, _p, _p]),
     "cosmos_grid_adjoint": (_i, [_p, ctypes.POINTER(SolveOpts), _i, _i, _p, _p, _p, _p, _p, _p]),
+    "cosmos_amr_create": (_i, [_p, ctypes.POINTER(Params), ctypes.POINTER(_p)]),
+    "cosmos_amr_destroy": (_i, [_p]),
+    "cosmos_amr_set_prim": (_i, [_p, _p, _sz]),
+    "cosmos_amr_solve": (_i, [_p, _d, _d, _d, _i, ctypes.POINTER(AmrResult)]),
+    "cosmos_amr_get": (_i, [_p, _p, _p, _p, _p]),
     "cosmos_batch_create": (_i, [_p, _i, _p, _p, _p, _p, _d, _i, _i, ctypes.POINTER(_p)]),
     "cosmos_batch_destroy": (_i, [_p]),
     "cosmos_batch_size": (_i, [_p, ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_longlong)]),

@@ -38,6 +38,7 @@ UNITS = {
     "capi_batch.cu": [],
     "noalloc.cu": [],
     "capi_adjoint.cu": [],
+    "capi_amr.cu": [],
 }
 
 

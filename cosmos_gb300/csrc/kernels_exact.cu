@@ -401,6 +401,86 @@ cudaError_t launch_amr_derefine(const SweepArgs& a, int precision, const void* f
     return cudaGetLastError();
 }
 
+// End-of-step level exchange of the Level-1 drivers, AMR/EulerAMR.cpp:287-307 (1D) and :500-546
+// (2D): a coarse cell whose flag is off takes the conserved average of its fine children
+// (0.5 (a + b) in 1D, 0.25 (((a + b) + c) + d) in 2D, then the system's prim), and every fine
+// child whose flag is off takes its parent's state.  One thread per coarse cell touches only
+// that cell and its own children, in the reference's order (restriction, then injection).
+// FP64 storage holds primitives; FP32 Newtonian/SR storage holds conserved values, which are
+// averaged in FP64 and copied as stored.
+__global__ void amr_sync_kernel(ConsLoader F, Geom CG, void* coarse_state, void* fine_state,
+                                const unsigned char* coarse, const unsigned char* fine) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (j >= CG.nx) return;
+    const Geom& FG = F.G;
+    const int nk = CG.dims == 1 ? 2 : 4;
+    int ki[4], kj[4];
+    for (int q = 0; q < nk; q++) {
+        ki[q] = CG.dims == 1 ? 0 : 2 * i + (q >> 1);
+        kj[q] = 2 * j + (q & 1);
+    }
+    const size_t cidx = (size_t)i * CG.pitch + j;
+    const bool fp32 = F.precision == 1;
+    if (!coarse[(size_t)i * CG.nx + j]) {
+        double u[4][5], avg[5];
+        for (int q = 0; q < nk; q++) F.get(ki[q], kj[q], Pt{0.0, 0.0, 0.0}, u[q]);
+#pragma unroll
+        for (int k = 0; k < 5; k++)
+            avg[k] = nk == 2 ? 0.5 * (u[0][k] + u[1][k]) : 0.25 * (((u[0][k] + u[1][k]) + u[2][k]) + u[3][k]);
+        if (fp32) {
+#pragma unroll
+            for (int k = 0; k < 5; k++) ((float*)coarse_state)[k * CG.fstride + cidx] = (float)avg[k];
+        } else {
+            double p[5];
+            if (F.system == 0) F.nw.prim(avg, Pt{0.0, 0.0, 0.0}, p);
+            else F.sr.prim(avg, Pt{0.0, 0.0, 0.0}, p);
+#pragma unroll
+            for (int k = 0; k < 5; k++) ((double*)coarse_state)[k * CG.fstride + cidx] = p[k];
+        }
+    }
+    for (int q = 0; q < nk; q++) {
+        if (fine[(size_t)ki[q] * FG.nx + kj[q]]) continue;
+        const size_t fidx = (size_t)ki[q] * FG.pitch + kj[q];
+        if (fp32) {
+#pragma unroll
+            for (int k = 0; k < 5; k++)
+                ((float*)fine_state)[k * FG.fstride + fidx] = ((const float*)coarse_state)[k * CG.fstride + cidx];
+        } else {
+#pragma unroll
+            for (int k = 0; k < 5; k++)
+                ((double*)fine_state)[k * FG.fstride + fidx] = ((const double*)coarse_state)[k * CG.fstride + cidx];
+        }
+    }
+}
+
+cudaError_t launch_amr_sync(const SweepArgs& a, int precision, void* coarse_state, void* fine_state, const Geom& FG,
+                            const unsigned char* coarse, const unsigned char* fine) {
+    if (a.system == 2) return cudaErrorNotSupported;
+    dim3 grid((a.G.nx + 127) / 128, a.G.ny);
+    amr_sync_kernel<<<grid, 128, 0, a.stream>>>(make_loader(a, precision, fine_state, FG), a.G, coarse_state,
+                                                fine_state, coarse, fine);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// Whether any of n flag bytes is set (the drivers' `refined` test, AMR/EulerAMR.cpp:241-249):
+// ORs 1 into *out, which the caller zeroes first.
+__global__ void amr_any_kernel(const unsigned char* __restrict__ f, size_t n, unsigned long long* out) {
+    int hit = 0;
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        hit |= f[k];
+    if (__syncthreads_or(hit) && threadIdx.x == 0) atomicOr(out, 1ull);
+}
+
+cudaError_t launch_amr_any(const unsigned char* flags, size_t n, unsigned long long* out, cudaStream_t st) {
+    size_t b = (n + 255) / 256;
+    if (b > 152 * 4) b = 152 * 4;
+    amr_any_kernel<<<(int)(b ? b : 1), 256, 0, st>>>(flags, n, out);
+    count_launch();
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ conservation sums
 // Sum of each stored field over the grid with Kahan-Babuska (Neumaier) compensation per thread,
 // then compensated double atomics are avoided: per-block partials go to a small buffer summed by

@@ -51,6 +51,11 @@ cudaError_t launch_amr_flags(const SweepArgs& a, int precision, double tol, unsi
                              unsigned char* fine);
 cudaError_t launch_amr_derefine(const SweepArgs& a, int precision, const void* fine_state, const Geom& FG,
                                 double tol, unsigned char* coarse, unsigned char* fine, void* coarse_state);
+// Level-1 end-of-step exchange (restriction into unflagged coarse cells, injection into unflagged
+// fine cells; Newtonian and SR) and the any-flag test of n bytes (ORs 1 into *out).
+cudaError_t launch_amr_sync(const SweepArgs& a, int precision, void* coarse_state, void* fine_state, const Geom& FG,
+                            const unsigned char* coarse, const unsigned char* fine);
+cudaError_t launch_amr_any(const unsigned char* flags, size_t n, unsigned long long* out, cudaStream_t st);
 
 // FP32 bulk path (conserved SoA storage, float)
 cudaError_t launch_sweep_fast(const SweepArgs& a);

@@ -467,3 +467,84 @@ def solve_with_steps(system, cells, dx, cfl, t_final, bias, limiter, gamma, orde
     """solve() that also returns the step count (the reference prints it per step)."""
     return _solve(system, cells, dx, cfl, t_final, bias, limiter, EulerMaterialParameters(gamma), order, black_hole,
                   subcycles, precision, boundary, max_steps)
+
+
+class AMR:
+    """A device-resident Level-1 AMR pair (cosmos_amr): a coarse grid of `shape` and its 2x
+    refinement with one flag per cell (Newtonian or SR, transmissive boundaries)."""
+
+    def __init__(self, system, shape, dx, gamma, precision=FP64, ctx=None, sr_c2p64_above=2.0):
+        self.ctx = ctx or default_context()
+        p = Params()
+        load().cosmos_params_default(ctypes.byref(p))
+        p.sr_c2p64_above = float(sr_c2p64_above)
+        p.system = system
+        if len(shape) == 1:
+            p.dims, p.nx, p.ny = 1, shape[0], 1
+        else:
+            p.dims, p.ny, p.nx = 2, shape[0], shape[1]
+        p.precision, p.boundary, p.gamma, p.dx = precision, BC_TRANSMISSIVE, float(gamma), float(dx)
+        self.shape = tuple(shape)
+        self.fine_shape = tuple(2 * n for n in shape)
+        h = ctypes.c_void_p()
+        check(load().cosmos_amr_create(self.ctx.h, ctypes.byref(p), ctypes.byref(h)))
+        self.h = h
+
+    def set_prim(self, prim):
+        a = np.ascontiguousarray(prim, dtype=np.float64)
+        if a.shape != self.shape + (5,):
+            raise ValueError(f"expected shape {self.shape + (5,)}, got {a.shape}")
+        check(load().cosmos_amr_set_prim(self.h, a.ctypes.data, a.size))
+
+    def solve(self, cfl, t_final, tol, order):
+        """Runs the driver from t = 0; returns (coarse steps, fine steps, final time, status bits)."""
+        r = _lib.AmrResult()
+        check(load().cosmos_amr_solve(self.h, float(cfl), float(t_final), float(tol), int(order), ctypes.byref(r)))
+        return r.coarse_steps, r.fine_steps, r.t, r.status
+
+    def get(self):
+        """(coarse cells, fine cells, coarse flags, fine flags) as the reference's driver returns them."""
+        cp = np.empty(self.shape + (5,))
+        fp = np.empty(self.fine_shape + (5,))
+        cf = np.empty(self.shape, np.uint8)
+        ff = np.empty(self.fine_shape, np.uint8)
+        check(load().cosmos_amr_get(self.h, cp.ctypes.data, fp.ctypes.data, cf.ctypes.data, ff.ctypes.data))
+        return cp, fp, cf.astype(bool), ff.astype(bool)
+
+    def close(self):
+        if getattr(self, "h", None) and not sys.is_finalizing():
+            load().cosmos_amr_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _amr_family(system, name):
+    """The reference's AMR driver class of one system (AMR/EulerAMR.hpp, AMR/RelativisticEulerAMR.hpp):
+    solveLevel1AMR / solve2DLevel1AMR return (coarse cells, fine cells, coarse flags, fine flags)."""
+
+    class Driver:
+        __qualname__ = f"{name}AMR"
+
+        @staticmethod
+        def solveLevel1AMR(initialCells, cellSpacing, CFLCoefficient, finalTime, AMRTolerance, order,
+                           materialParameters, precision=FP64):
+            a = AMR(system, _shape(initialCells), cellSpacing, materialParameters.getAdiabaticIndex(), precision)
+            try:
+                a.set_prim(initialCells)
+                a.solve(CFLCoefficient, finalTime, AMRTolerance, order)
+                return a.get()
+            finally:
+                a.close()
+
+        solve2DLevel1AMR = solveLevel1AMR
+
+    return Driver
+
+
+EulerAMR = _amr_family(NEWTONIAN, "Euler")
+RelativisticEulerAMR = _amr_family(SR, "RelativisticEuler")

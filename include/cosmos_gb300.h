@@ -211,6 +211,36 @@ int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, int nsteps, 
                         const double* target, const double* dts_in, double* grad_prim, double* loss,
                         double* dts_out, double* ms);
 
+/* ---- Level-1 adaptive mesh refinement: EulerAMR::solveLevel1AMR / solve2DLevel1AMR
+ * (AMR/EulerAMR.cpp:169-592) and RelativisticEulerAMR::solveLevel1AMR / solve2DLevel1AMR
+ * (AMR/RelativisticEulerAMR.cpp:181-603), Newtonian and SR systems, transmissive boundaries.
+ * A coarse grid (described by the params) and its 2x refinement (2 nx, and 2 ny in 2D, spacing
+ * dx / 2) stay on the device with one flag byte per cell.  Each coarse step: the CFL time step of
+ * the coarse grid (its iteration count is the total fine step count, as in the reference), the
+ * refinement flag pass, a masked coarse step (bias 0, limiter 1, as the reference's drivers
+ * hard-code; 2D: X(dt/2) Y(dt) X(dt/2)), masked fine steps until the fine time reaches
+ * (t + dt) - 1e-4 when any fine flag is set, restriction and injection between the levels, and the
+ * derefinement pass.  FP64 grids give the reference's results bit for bit. */
+typedef struct cosmos_amr cosmos_amr;
+typedef struct cosmos_amr_result {
+    int coarse_steps;  /* the reference's coarseCurrentIteration at exit */
+    int fine_steps;    /* the reference's fineTotalIteration at exit */
+    double t;          /* coarseCurrentTime at exit */
+    int status;        /* COSMOS_STATUS_* bits of both levels' kernels */
+} cosmos_amr_result;
+int cosmos_amr_create(cosmos_ctx* ctx, const cosmos_params* coarse, cosmos_amr** out);
+int cosmos_amr_destroy(cosmos_amr* a);
+/* The coarse grid's initial cells (5 * nx * ny doubles, the layout of cosmos_grid_set_prim). */
+int cosmos_amr_set_prim(cosmos_amr* a, const double* prim, size_t n_doubles);
+/* Runs the driver from t = 0 on the current coarse cells: flags reset (coarse on, fine off), fine
+ * cells injected from their parents, then coarse steps until t >= t_final.  order 1: FORCE,
+ * 2: SLIC.  tol: the AMRTolerance argument. */
+int cosmos_amr_solve(cosmos_amr* a, double cfl, double t_final, double tol, int order, cosmos_amr_result* r);
+/* The driver's returned tuple: coarse cells (5 nx ny doubles), fine cells (4x or 2x as many),
+ * coarse and fine flags (1 byte per cell).  Any pointer may be NULL. */
+int cosmos_amr_get(cosmos_amr* a, double* coarse_prim, double* fine_prim, unsigned char* coarse_flags,
+                   unsigned char* fine_flags);
+
 /* Allocation-free conservation sums.  No counterpart in the reference: it exists for callers that
  * cannot allocate device memory where they need the sums -- code recorded into a CUDA graph
  * (allocation is not allowed during stream capture), host callbacks or foreign runtimes that own

@@ -15,6 +15,7 @@
 #include <cmath>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "cosmos_gb300.h"
@@ -398,3 +399,89 @@ public:
         cosmos_compat_detail::unpack2(a, c);
     }
 };
+
+// ----------------------------------------------------------------------------- Level-1 AMR drivers
+// AMR/EulerAMR.hpp and AMR/RelativisticEulerAMR.hpp: solveLevel1AMR / solve2DLevel1AMR return
+// (coarse cells, fine cells, coarse flags, fine flags).  The Level-2 drivers are not provided.
+namespace cosmos_compat_detail {
+
+struct Amr {
+    cosmos_amr* a = nullptr;
+    Amr(int system, int dims, int nx, int ny, double dx, double gamma) {
+        cosmos_params p;
+        cosmos_params_default(&p);
+        p.system = system;
+        p.dims = dims;
+        p.nx = nx;
+        p.ny = dims == 1 ? 1 : ny;
+        p.dx = dx;
+        p.gamma = gamma;
+        check(cosmos_amr_create(ctx(), &p, &a));
+    }
+    ~Amr() { cosmos_amr_destroy(a); }
+    // runs the driver and fills the host copies of both levels and their flags
+    void run(const std::vector<double>& prim, double cfl, double T, double tol, int order, std::vector<double>& c,
+             std::vector<double>& f, std::vector<unsigned char>& cf, std::vector<unsigned char>& ff) {
+        check(cosmos_amr_set_prim(a, prim.data(), prim.size()));
+        cosmos_amr_result r;
+        check(cosmos_amr_solve(a, cfl, T, tol, order, &r));
+        check(cosmos_amr_get(a, c.data(), f.data(), cf.data(), ff.data()));
+    }
+};
+
+template <class S>
+std::tuple<std::vector<S>, std::vector<S>, std::vector<bool>, std::vector<bool> >
+amr1(int sys, std::vector<S> cells, double dx, double cfl, double T, double tol, int order,
+     EulerMaterialParameters mp) {
+    const size_t n = cells.size();
+    Amr d(sys, 1, (int)n, 1, dx, mp.getAdiabaticIndex());
+    std::vector<double> c(5 * n), f(10 * n);
+    std::vector<unsigned char> cf(n), ff(2 * n);
+    d.run(pack1(cells), cfl, T, tol, order, c, f, cf, ff);
+    std::vector<S> coarse(n), fine(2 * n);
+    unpack1(c, coarse);
+    unpack1(f, fine);
+    return std::make_tuple(coarse, fine, std::vector<bool>(cf.begin(), cf.end()), std::vector<bool>(ff.begin(), ff.end()));
+}
+
+template <class S>
+std::tuple<std::vector<std::vector<S> >, std::vector<std::vector<S> >, std::vector<std::vector<bool> >,
+           std::vector<std::vector<bool> > >
+amr2(int sys, std::vector<std::vector<S> > cells, double dx, double cfl, double T, double tol, int order,
+     EulerMaterialParameters mp) {
+    const size_t ny = cells.size(), nx = cells[0].size();
+    Amr d(sys, 2, (int)nx, (int)ny, dx, mp.getAdiabaticIndex());
+    std::vector<double> c(5 * nx * ny), f(20 * nx * ny);
+    std::vector<unsigned char> cf(nx * ny), ff(4 * nx * ny);
+    d.run(pack2(cells), cfl, T, tol, order, c, f, cf, ff);
+    std::vector<std::vector<S> > coarse(ny, std::vector<S>(nx)), fine(2 * ny, std::vector<S>(2 * nx));
+    unpack2(c, coarse);
+    unpack2(f, fine);
+    std::vector<std::vector<bool> > cb(ny, std::vector<bool>(nx)), fb(2 * ny, std::vector<bool>(2 * nx));
+    for (size_t i = 0; i < ny; i++)
+        for (size_t j = 0; j < nx; j++) cb[i][j] = cf[i * nx + j] != 0;
+    for (size_t i = 0; i < 2 * ny; i++)
+        for (size_t j = 0; j < 2 * nx; j++) fb[i][j] = ff[i * 2 * nx + j] != 0;
+    return std::make_tuple(coarse, fine, cb, fb);
+}
+
+}  // namespace cosmos_compat_detail
+
+#define COSMOS_COMPAT_AMR(PREFIX, STATE, SYS)                                                                   \
+    class PREFIX##AMR {                                                                                        \
+    public:                                                                                                    \
+        static std::tuple<std::vector<STATE>, std::vector<STATE>, std::vector<bool>, std::vector<bool> >       \
+        solveLevel1AMR(std::vector<STATE> c, double dx, double cfl, double T, double tol, int order,          \
+                       EulerMaterialParameters mp) {                                                           \
+            return cosmos_compat_detail::amr1(SYS, c, dx, cfl, T, tol, order, mp);                             \
+        }                                                                                                      \
+        static std::tuple<std::vector<std::vector<STATE> >, std::vector<std::vector<STATE> >,                  \
+                          std::vector<std::vector<bool> >, std::vector<std::vector<bool> > >                   \
+        solve2DLevel1AMR(std::vector<std::vector<STATE> > c, double dx, double cfl, double T, double tol,      \
+                         int order, EulerMaterialParameters mp) {                                              \
+            return cosmos_compat_detail::amr2(SYS, c, dx, cfl, T, tol, order, mp);                             \
+        }                                                                                                      \
+    };
+COSMOS_COMPAT_AMR(Euler, EulerStateVector, COSMOS_NEWTONIAN)
+COSMOS_COMPAT_AMR(RelativisticEuler, RelativisticEulerStateVector, COSMOS_SR)
+#undef COSMOS_COMPAT_AMR

@@ -89,6 +89,26 @@ int main(int argc, char** argv) {
         dump(dir + "/bh_accretion.bin", flat1(BlackHoleEulerSecondOrderSolver::solve(
                                              initialCells, cellSpacing, 0.9, 0.02, 0.0, 1, 1, materialParameters, blackHole)));
     }
+    // Level-1 AMR (AMR/EulerAMR.cpp:352-592): the cylindrical explosion on 20x20 coarse cells, SLIC
+    {
+        int cellCount = 20;
+        double cellSpacing = 1.0 / cellCount;
+        std::vector<std::vector<EulerStateVector> > initialCells(cellCount, std::vector<EulerStateVector>(cellCount));
+        EulerMaterialParameters materialParameters(1.4);
+        for (int i = 0; i < cellCount; i++)
+            for (int j = 0; j < cellCount; j++) {
+                double r2 = ((i - (0.5 * cellCount)) * (i - (0.5 * cellCount))) + ((j - (0.5 * cellCount)) * (j - (0.5 * cellCount)));
+                if (r2 <= (0.2 * cellCount) * (0.2 * cellCount)) initialCells[i][j] = EulerStateVector(1.0, 0.0, 0.0, 0.0, 1.0);
+                else initialCells[i][j] = EulerStateVector(0.125, 0.0, 0.0, 0.0, 0.1);
+            }
+        auto r = EulerAMR::solve2DLevel1AMR(initialCells, cellSpacing, 0.9, 0.05, 4.0, 2, materialParameters);
+        dump(dir + "/amr_coarse.bin", flat2(std::get<0>(r)));
+        dump(dir + "/amr_fine.bin", flat2(std::get<1>(r)));
+        std::vector<double> flags;
+        for (auto& row : std::get<2>(r)) for (bool b : row) flags.push_back(b ? 1.0 : 0.0);
+        for (auto& row : std::get<3>(r)) for (bool b : row) flags.push_back(b ? 1.0 : 0.0);
+        dump(dir + "/amr_flags.bin", flags);
+    }
     std::printf("compat driver ok\n");
     return 0;
 }

@@ -22,7 +22,7 @@ def header_functions():
 def test_header_declares_the_abi():
     fns = header_functions()
     assert len(fns) >= 25
-    for must in ("cosmos_grid_sweep", "cosmos_grid_solve", "cosmos_grid_rk_source", "cosmos_grid_amr_flags",
+    for must in ("cosmos_grid_sweep", "cosmos_grid_solve", "cosmos_grid_rk_source", "cosmos_grid_amr_flags", "cosmos_amr_solve",
                  "cosmos_stable_dt_rule", "cosmos_last_error"):
         assert must in fns
 

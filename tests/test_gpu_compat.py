@@ -56,3 +56,14 @@ def test_compat_driver_matches_oracle(cosmos_lib, oracle, tmp_path):
     want, _, _, _ = oracle.solve(2, s, 2, 1.0 / k, 0.9, 0.02, 0.0, 1, 5.0 / 3.0, subcycles=1,
                                  bh=(0.05, 0.0, 0.5, 0.0, 0.0))
     assert bit_equal(load("bh_accretion.bin", (k, 5)), want)
+
+    n = 20
+    s = np.zeros((n, n, 5))
+    for i in range(n):
+        for j in range(n):
+            r2 = (i - 0.5 * n) ** 2 + (j - 0.5 * n) ** 2
+            s[i, j] = (1.0, 0, 0, 0, 1.0) if r2 <= (0.2 * n) ** 2 else (0.125, 0, 0, 0, 0.1)
+    _, _, cp, fp, cf, ff = oracle.amr_level1(0, s, 1.0 / n, 0.9, 0.05, 4.0, 2, 1.4)
+    assert bit_equal(load("amr_coarse.bin", (n * n * 5,)), cp)
+    assert bit_equal(load("amr_fine.bin", (4 * n * n * 5,)), fp)
+    assert bit_equal(load("amr_flags.bin", (5 * n * n,)), np.concatenate([cf, ff]).astype(np.float64))
