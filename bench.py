@@ -21,6 +21,7 @@ Our arm prints one JSON line with
 --impl reference times the CPU path alone (all host threads) on the same workload.
 """
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -744,11 +745,170 @@ def run_grid_reference(args, kind):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- Level-1 AMR (EulerAMR::solve2DLevel1AMR)
+AMR_WORKLOAD = "Level-1 AMR, EulerAMR::solve2DLevel1AMR: 2D Newtonian cylindrical explosion (rho, p = 1, 1 inside " \
+               "r <= 0.2, 0.125, 0.1 outside), 512x512 coarse cells on [0,1]^2 (1024x1024 fine), gamma 1.4, " \
+               "CFL 0.95, SLIC (bias 0, van Leer, as the driver fixes them), AMRTolerance 25.6, transmissive, " \
+               "t_final 0.125; one step = one whole driver run"
+AMR_N, AMR_T, AMR_TOL, AMR_CFL = 512, 0.125, 25.6, 0.95
+
+
+def amr_problem(n):
+    """The reference's 2D AMR test layout (Tests/EulerAMRTests.cpp:33-62) on n x n coarse cells."""
+    i, j = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    inside = np.sqrt((i - 0.5 * n) ** 2 + (j - 0.5 * n) ** 2) <= 0.2 * n
+    s = np.zeros((n, n, 5))
+    s[..., 0] = np.where(inside, 1.0, 0.125)
+    s[..., 4] = np.where(inside, 1.0, 0.1)
+    return s
+
+
+def amr_cpu_baseline(n, t_sample):
+    """The oracle's Level-1 driver (FP64 restatement, bit-identical to the reference's) on all host
+    cores, run to t_sample; cell-updates = coarse steps x coarse cells + fine steps taken x fine cells."""
+    from oracle.pyoracle import Oracle
+    O = Oracle()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    s = amr_problem(n)
+    fr = []
+    t0 = time.perf_counter()
+    nc, _, _, _, _, _ = O.amr_level1(0, s, 1.0 / n, AMR_CFL, t_sample, AMR_TOL * n / AMR_N, 2, 1.4, fine_run=fr)
+    el = time.perf_counter() - t0
+    cells = nc * n * n + fr[0] * 4 * n * n
+    return {"value": cells / el, "unit": METRIC, "cores": cores, "kind": "port", "sample_ms": el * 1e3,
+            "sample": f"the oracle's Level-1 AMR driver on the same {n}x{n} problem to t = {t_sample} "
+                      f"({nc} coarse and {fr[0]} fine steps, {cells / 1e6:.0f} M cell-updates) in {el:.1f} s "
+                      f"on {cores} host threads (sweeps line-parallel; flag, exchange and derefinement passes serial)"}
+
+
+def run_amr(args):
+    """Level-1 AMR runs (FP64, bit-identical to the reference's driver; FP32 beside it), state
+    resident in HBM between runs; e2e with host buffers through the C ABI."""
+    import torch
+    import cosmos_gb300 as cg
+    _, _, local = dist_env()
+    torch.cuda.set_device(local)
+    L = cg.load()
+    ctx = cg.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    n = args.n if args.n != 4096 else AMR_N
+    tol = AMR_TOL * n / AMR_N
+    s0 = amr_problem(n)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def timed(fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            fn()
+            b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    def measure(precision, runs, warm):
+        # every run starts from the initial cells (a run leaves its final cells in the coarse grid)
+        a = cg.AMR(cg.NEWTONIAN, (n, n), 1.0 / n, 1.4, precision, ctx=ctx)
+        for _ in range(warm):
+            a.set_prim(s0)
+            a.solve(AMR_CFL, AMR_T, tol, 2)
+        times, info = [], None
+        for _ in range(runs):
+            a.set_prim(s0)
+            flush.fill_(1)  # evict the previous run's state from L2
+            r = []
+            times.append(timed(lambda: r.append(a.solve(AMR_CFL, AMR_T, tol, 2))))
+            info = (r[0], a.fine_run)
+        cp, fp, cf, ff = a.get()
+        a.close()
+        return times, info, cp, cf
+
+    steps = args.steps if args.steps != 200 else 3
+    launches0 = L.cosmos_kernel_launches()
+    with Clocks(local) as clk:
+        t64, (r64, run64), cp64, cf64 = measure(cg.FP64, steps, args.warmup)
+    launches = (L.cosmos_kernel_launches() - launches0) // (steps + args.warmup)
+    ms = statistics.median(t64)
+    ncoarse, nfine = r64[0], run64
+    cells = ncoarse * n * n + nfine * 4 * n * n
+    value = cells / (ms * 1e-3)
+    t32, (r32, run32), cp32, cf32 = measure(cg.FP32, steps, 1)
+    ms32 = statistics.median(t32)
+    cells32 = r32[0] * n * n + run32 * 4 * n * n
+    # e2e: pinned host primitives -> device, one driver run, both levels and flags -> host
+    host = torch.empty((n, n, 5), dtype=torch.float64, pin_memory=True)
+    host.numpy()[...] = s0
+    hc = torch.empty((n, n, 5), dtype=torch.float64, pin_memory=True)
+    hf = torch.empty((2 * n, 2 * n, 5), dtype=torch.float64, pin_memory=True)
+    hcf = torch.empty((n, n), dtype=torch.uint8, pin_memory=True)
+    hff = torch.empty((2 * n, 2 * n), dtype=torch.uint8, pin_memory=True)
+    ae = cg.AMR(cg.NEWTONIAN, (n, n), 1.0 / n, 1.4, cg.FP64, ctx=ctx)
+    res = cg._lib.AmrResult()
+
+    def e2e_run():
+        cg._lib.check(L.cosmos_amr_set_prim(ae.h, host.data_ptr(), n * n * 5))
+        cg._lib.check(L.cosmos_amr_solve(ae.h, AMR_CFL, AMR_T, tol, 2, ctypes.byref(res)))
+        cg._lib.check(L.cosmos_amr_get(ae.h, hc.data_ptr(), hf.data_ptr(), hcf.data_ptr(), hff.data_ptr()))
+    e2e_run()
+    e2e_ms = timed(e2e_run)
+    ae.close()
+    h2d = n * n * 5 * 8
+    d2h = n * n * 5 * 8 + 4 * n * n * 5 * 8 + 5 * n * n
+    peak, peak_kind = peaks()
+    gbs = cells * 240 / (ms * 1e-3) / 1e9
+    base = None if args.no_cpu else amr_cpu_baseline(n, AMR_T / 4)
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": AMR_WORKLOAD, "n": n, "tolerance": tol, "coarse_steps": ncoarse, "fine_steps": nfine,
+                   "cell_updates_per_run": cells, "refined_coarse_cells_at_end": int((~cf64).sum()),
+                   "cell_updates": "coarse steps x coarse cells + fine steps taken x fine cells (every cell of a "
+                                   "level is swept; flagged-off cells are copied)",
+                   "l2": "256 MB buffer written between timed runs (the two levels' states, 105 MB, fit in L2)",
+                   "host_round_trips": "one per coarse step and one per fine step (time-step control stays on "
+                                       "the host, as in the reference)"},
+        "fp32": {"value": cells32 / (ms32 * 1e-3), "ms_per_step": ms32, "coarse_steps": r32[0], "fine_steps": run32,
+                 "l1_rho_vs_fp64": float(np.abs(cp32[..., 0] - cp64[..., 0]).sum() / np.abs(cp64[..., 0]).sum()),
+                 "coarse_flags_equal_fp64": float(np.mean(cf32 == cf64))},
+        "e2e": {"value": cells / (e2e_ms * 1e-3), "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_ms, "what": "pinned host primitives -> device, one driver run, both levels' "
+                                               "primitives and flags -> host"},
+        "roofline": {"bound": "hbm", "kernel": "whole driver run (masked sweeps, CFL reductions, flag, exchange "
+                                               "and derefinement passes)",
+                     "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak, "peak_source": peak_kind,
+                     "traffic": None, "bytes_per_cell_update": 240,
+                     "note": "FP64 sweeps in the reference's operation order are FP64-issue-bound on GB300; the "
+                             "run also waits on one host round trip per level step"},
+        "clocks": clk.summary(), "gpu_launches": int(launches), "status": r64[3],
+    }
+    if base:
+        line["cpu_baseline"] = base
+    print(json.dumps(line), flush=True)
+
+
+def run_amr_reference(args):
+    rank, _, _ = dist_env()
+    if rank != 0:
+        return
+    n = args.n if args.n != 4096 else AMR_N
+    base = amr_cpu_baseline(n, AMR_T / 4)
+    line = {"metric": METRIC, "value": base["value"], "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["sample_ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": AMR_WORKLOAD, "n": n},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="grid", choices=["grid", "batch", "sr", "gr"],
+    ap.add_argument("--workload", default="grid", choices=["grid", "batch", "sr", "gr", "amr"],
                     help="grid: one 4096^2 Newtonian grid (default); batch: 256 uneven grids in one persistent "
-                         "launch; sr: 2048^2 special-relativistic Kelvin-Helmholtz; gr: 1024^2 black-hole accretion")
+                         "launch; sr: 2048^2 special-relativistic Kelvin-Helmholtz; gr: 1024^2 black-hole accretion; "
+                         "amr: Level-1 AMR driver runs on a 512^2 cylindrical explosion")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
@@ -762,6 +922,8 @@ def main():
         args.warmup = 3
     if args.workload == "batch":
         run_batch_reference(args) if args.impl == "reference" else run_batch(args)
+    elif args.workload == "amr":
+        run_amr_reference(args) if args.impl == "reference" else run_amr(args)
     elif args.workload in ("sr", "gr"):
         run_grid_reference(args, args.workload) if args.impl == "reference" else run_grid(args, args.workload)
     elif args.impl == "reference":

@@ -27,7 +27,7 @@ class Params(ctypes.Structure):
 
 class AmrResult(ctypes.Structure):
     _fields_ = [("coarse_steps", ctypes.c_int), ("fine_steps", ctypes.c_int), ("t", ctypes.c_double),
-                ("status", ctypes.c_int)]
+                ("status", ctypes.c_int), ("fine_run", ctypes.c_int)]
 
 
 class SolveOpts(ctypes.Structure):

@@ -167,7 +167,7 @@ int cosmos_amr_solve(cosmos_amr* a, double cfl, double t_final, double tol, int 
     MCK(launch_amr_sync(ca, prec, C->buf[C->cur], F->buf[F->cur], F->G, cflags, fflags));
     const double dx = C->p.dx;
     double t = 0.0;
-    int it = 0, fit = 0;
+    int it = 0, fit = 0, run = 0;
     int rc = COSMOS_OK;
     while (t < t_final) {
         double smax = 0.0;
@@ -191,6 +191,7 @@ int cosmos_amr_solve(cosmos_amr* a, double cfl, double t_final, double tol, int 
                 if ((rc = masked_step(F, order, fdt, fflags))) break;
                 ft += fdt;
                 fit += 1;
+                run += 1;
             }
             if (rc) break;
         } else {
@@ -212,6 +213,7 @@ int cosmos_amr_solve(cosmos_amr* a, double cfl, double t_final, double tol, int 
         r->fine_steps = fit;
         r->t = t;
         r->status = st2[0] | st2[1] | (rc == COSMOS_ENONFINITE ? COSMOS_STATUS_NONFINITE : 0);
+        r->fine_run = run;
     }
     return rc;
 }

@@ -497,9 +497,11 @@ class AMR:
         check(load().cosmos_amr_set_prim(self.h, a.ctypes.data, a.size))
 
     def solve(self, cfl, t_final, tol, order):
-        """Runs the driver from t = 0; returns (coarse steps, fine steps, final time, status bits)."""
+        """Runs the driver from t = 0; returns (coarse steps, fine steps, final time, status bits) with
+        the reference's counters.  self.fine_run holds the number of fine steps actually taken."""
         r = _lib.AmrResult()
         check(load().cosmos_amr_solve(self.h, float(cfl), float(t_final), float(tol), int(order), ctypes.byref(r)))
+        self.fine_run = r.fine_run
         return r.coarse_steps, r.fine_steps, r.t, r.status
 
     def get(self):

@@ -227,6 +227,7 @@ typedef struct cosmos_amr_result {
     int fine_steps;    /* the reference's fineTotalIteration at exit */
     double t;          /* coarseCurrentTime at exit */
     int status;        /* COSMOS_STATUS_* bits of both levels' kernels */
+    int fine_run;      /* fine steps actually taken (fine_steps also counts coarse steps with no refinement) */
 } cosmos_amr_result;
 int cosmos_amr_create(cosmos_ctx* ctx, const cosmos_params* coarse, cosmos_amr** out);
 int cosmos_amr_destroy(cosmos_amr* a);

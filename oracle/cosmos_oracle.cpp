@@ -1075,11 +1075,12 @@ void orc_amr_derefine(int sys, double* coarse_prim, const double* fine_prim, int
 // of dx/2 until the fine time passes (t + dt) - 1e-4, each dt from the whole fine grid (:253-277);
 // otherwise the fine count still advances (:279-282); restriction of flagged-off coarse cells and
 // injection into unflagged fine cells (:287-307); derefinement (:309-345).  coarse/fine receive
-// the final primitive grids, cflags/fflags the final flags; *fine_steps the fine step count.
-// Returns the number of coarse steps.
+// the final primitive grids, cflags/fflags the final flags; *fine_steps the fine step count (the
+// reference's fineTotalIteration), *fine_run the fine steps actually taken (optional).  Returns
+// the number of coarse steps.
 int orc_amr_level1(int sys, const double* prim, int ny, int nx, int dims, double dx, double cfl, double tf,
                    double tol, int order, double gamma, double* coarse, double* fine, unsigned char* cflags,
-                   unsigned char* fflags, int* fine_steps) {
+                   unsigned char* fflags, int* fine_steps, int* fine_run) {
     if (dims == 1) ny = 1;
     const int fny = dims == 1 ? 1 : 2 * ny, fnx = 2 * nx;
     const size_t nc = (size_t)ny * nx;
@@ -1117,7 +1118,7 @@ int orc_amr_level1(int sys, const double* prim, int ny, int nx, int dims, double
         }
     };
     double t = 0.0;
-    int it = 0, fit = 0;
+    int it = 0, fit = 0, run = 0;
     while (t < tf) {
         const double dt = orc_stable_dt(sys, coarse, ny, nx, dims, dx, cfl, t, tf, fit, gamma, nullptr);
         orc_amr_flags(sys, coarse, ny, nx, dims, dx, tol, gamma, nullptr, cflags, fflags);
@@ -1131,6 +1132,7 @@ int orc_amr_level1(int sys, const double* prim, int ny, int nx, int dims, double
                 step(fine, fny, fnx, dx * 0.5, fdt, fflags);
                 ft += fdt;
                 fit += 1;
+                run += 1;
             }
         } else {
             fit += 1;
@@ -1155,6 +1157,7 @@ int orc_amr_level1(int sys, const double* prim, int ny, int nx, int dims, double
         orc_amr_derefine(sys, coarse, fine, ny, nx, dims, dx, tol, gamma, nullptr, cflags, fflags);
     }
     if (fine_steps) *fine_steps = fit;
+    if (fine_run) *fine_run = run;
     return it;
 }
 

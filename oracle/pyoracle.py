@@ -70,7 +70,7 @@ class Oracle:
         L.orc_gr_metric.argtypes = [_d, _d, _d, _d, _p, _p]
         L.orc_amr_flags.argtypes = [_i, _p, _i, _i, _i, _d, _d, _d, _p, _p, _p]
         L.orc_amr_derefine.argtypes = [_i, _p, _p, _i, _i, _i, _d, _d, _d, _p, _p, _p]
-        L.orc_amr_level1.argtypes = [_i, _p, _i, _i, _i, _d, _d, _d, _d, _i, _d, _p, _p, _p, _p, _p]
+        L.orc_amr_level1.argtypes = [_i, _p, _i, _i, _i, _d, _d, _d, _d, _i, _d, _p, _p, _p, _p, _p, _p]
         L.orc_amr_level1.restype = _i
         L.orc_tlm_newton.argtypes = [_p, _p, _p, _i, _i, _i, _d, _p, _i, _d, _i, _d, _i, _p]
         L.orc_tlm_newton.restype = _d
@@ -171,18 +171,21 @@ class Oracle:
                                 _ptr(c), _ptr(f))
         return cp, c, f
 
-    def amr_level1(self, system, prim, dx, cfl, tf, tol, order, gamma):
+    def amr_level1(self, system, prim, dx, cfl, tf, tol, order, gamma, fine_run=None):
         """The Level-1 AMR driver: (coarse steps, fine steps, coarse prims, fine prims, coarse flags,
-        fine flags), grids flattened like Reference.amr_level1."""
+        fine flags), grids flattened like Reference.amr_level1.  fine_run (a list) receives the number
+        of fine steps actually taken."""
         p = np.ascontiguousarray(prim, dtype=np.float64)
         ny, nx, dims = _shape(p)
         nc = nx * (ny if dims == 2 else 1)
         nf = nc * (4 if dims == 2 else 2)
         cp = np.zeros(nc * 5); fp = np.zeros(nf * 5)
         cf = np.zeros(nc, np.uint8); ff = np.zeros(nf, np.uint8)
-        fs = ctypes.c_int(0)
+        fs, fr = ctypes.c_int(0), ctypes.c_int(0)
         n = self.L.orc_amr_level1(_sys(system), _ptr(p), ny, nx, dims, dx, cfl, tf, tol, order, gamma, _ptr(cp),
-                                  _ptr(fp), _ptr(cf), _ptr(ff), ctypes.byref(fs))
+                                  _ptr(fp), _ptr(cf), _ptr(ff), ctypes.byref(fs), ctypes.byref(fr))
+        if fine_run is not None:
+            fine_run.append(fr.value)
         return n, fs.value, cp, fp, cf, ff
 
     # ---- tangent-linear of the Newtonian SLIC loss

@@ -49,6 +49,18 @@ def test_reference_arm_prints_one_contract_line(workload, n):
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
 
 
+def test_amr_reference_arm_prints_one_contract_line():
+    r = run_bench(["--workload", "amr", "--impl", "reference", "--n", "64", "--steps", "1"])
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.strip()]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert KEYS <= set(line) and line["impl"] == "reference" and line["value"] > 0
+    assert line["config"]["n"] == 64 and line["ms_per_step"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and "coarse" in line["cpu_baseline"]["sample"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+
+
 def test_reference_arm_other_ranks_exit_quietly():
     r = run_bench(["--impl", "reference", "--n", "64", "--steps", "1", "--gpus", "2"],
                   env={"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
