@@ -184,6 +184,7 @@ struct XTileSmem {
     X sc[5][NT + 2];  // cells s0-2 .. s0+NT-1 (own cell of thread t at t+1)
     X sl[5][NT];      // left face of the cell owned by thread t
     X sf[5][NT];      // flux at the right interface of the cell owned by thread t
+    unsigned char sa[NT + 1];  // masked sweeps: whether the cell owned by thread t updates
 };
 
 // One X tile: updates cells s0 .. min(s0 + NT - 2, nx) - 1 of `row`.  `act` and the policy's
@@ -226,13 +227,24 @@ CG_D typename Pol::W x_own_tile(Pol& pol, const Geom& G, const typename Pol::S* 
 #pragma unroll
         for (int f = 0; f < 5; f++) sc[f][t + 2] = e.v[f];
     }
+    // Masked sweeps (AMR levels) reconstruct only cells next to an updating cell and evaluate only
+    // the interfaces of updating cells; the skipped values are never read.
+    const bool msk = Pol::kMasked && out.mask != nullptr;
+    bool my_act = false;
+    if (msk) {
+        my_act = act && t >= 1 && c < send && pol.active(row, c, out.mask);
+        sm.sa[t] = my_act ? 1 : 0;
+        if (t == NT - 1) sm.sa[NT] = 0;  // cell s0 + NT - 1 belongs to the next tile
+    }
     __syncthreads();
     if (!act) {  // inactive step: keep the ping-pong buffers consistent
         if (t >= 1 && c < send) store_cell<Pol>(own, dst, G, row, c);
         return typename Pol::W(0);
     }
+    const bool need_recon = !msk || my_act || sm.sa[t + 1] || (t >= 1 && sm.sa[t - 1]);
+    const bool need_flux = !msk || my_act || sm.sa[t + 1];  // interface between c and c + 1
     Face L, R;
-    if (live) {
+    if (live && need_recon) {
         if (ORDER == 2) {
             Cell a, b;
 #pragma unroll
@@ -247,7 +259,7 @@ CG_D typename Pol::W x_own_tile(Pol& pol, const Geom& G, const typename Pol::S* 
     }
     __syncthreads();
     V5<X> Fr;
-    if (live && c < send && t < NT - 1) {  // right interface of c, between c and c + 1
+    if (live && c < send && t < NT - 1 && need_flux) {  // right interface of c, between c and c + 1
         Face Rn;
         if (ORDER == 2) {
 #pragma unroll
@@ -266,7 +278,7 @@ CG_D typename Pol::W x_own_tile(Pol& pol, const Geom& G, const typename Pol::S* 
     typename Pol::W w = 0;
     if (t >= 1 && c < send) {
         Cell nc = own;
-        if (pol.active(row, c, out.mask)) {
+        if (msk ? my_act : pol.active(row, c, out.mask)) {
             V5<X> Fl;
 #pragma unroll
             for (int f = 0; f < 5; f++) Fl.v[f] = sf[f][t - 1];
@@ -332,11 +344,15 @@ CG_D typename Pol::W y_march_seg(Pol& pol, const Geom& G, const typename Pol::S*
             const bool b = fi >= y0 && fi < y1 && pol.active(j, fi, out.mask);
             return a || b;
         };
+        // Masked sweeps (AMR levels) reconstruct a cell only when one of its two interfaces is
+        // needed; nf_next carries the next interface's need so each is evaluated once.
+        const bool msk = Pol::kMasked && out.mask != nullptr;
         // window: cm1 = y-1, c0 = y, c1 = y+1, c2 = y+2
         Cell cm2, cm1, c0, c1, c2;
         ld(y0 - 2, cm2); ld(y0 - 1, cm1); ld(y0, c0); ld(y0 + 1, c1);
         V5<X> Fp, Fn;
         Face R0;  // right face of the current cell (shared recon)
+        bool nf_next = msk ? need(y0 + 1) : true;
         if (ORDER == 1) {
             if (need(y0)) { Face L, R; pol.face_of(cm1, L); pol.face_of(c0, R); pol.flux(L, R, j, y0, Fp); }
         } else if (Pol::kShared) {
@@ -345,7 +361,7 @@ CG_D typename Pol::W y_march_seg(Pol& pol, const Geom& G, const typename Pol::S*
                 pol.recon(cm2, cm1, c0, j, y0 - 1, Lm1, Rm1);
                 pol.recon(cm1, c0, c1, j, y0, L0, R0);
                 pol.flux(Rm1, L0, j, y0, Fp);
-            } else {
+            } else if (nf_next) {
                 pol.recon(cm1, c0, c1, j, y0, L0, R0);
             }
         } else {
@@ -358,12 +374,13 @@ CG_D typename Pol::W y_march_seg(Pol& pol, const Geom& G, const typename Pol::S*
         }
         for (int y = y0; y < y1; y++) {
             ld(y + 2, c2);
-            const bool nf = need(y + 1);
+            const bool nf = msk ? nf_next : need(y + 1);
+            if (msk) nf_next = need(y + 2);
             if (ORDER == 1) {
                 if (nf) { Face L, R; pol.face_of(c0, L); pol.face_of(c1, R); pol.flux(L, R, j, y + 1, Fn); }
             } else if (Pol::kShared) {
                 Face L1, R1;
-                pol.recon(c0, c1, c2, j, y + 1, L1, R1);
+                if (nf || nf_next) pol.recon(c0, c1, c2, j, y + 1, L1, R1);  // R1 is read only if nf_next
                 if (nf) pol.flux(R0, L1, j, y + 1, Fn);
                 R0 = R1;
             } else {
