@@ -1161,6 +1161,194 @@ int orc_amr_level1(int sys, const double* prim, int ny, int nx, int dims, double
     return it;
 }
 
+// ---------------------------------------------------------------- AMR Level-2 driver
+// Pieces of the Level-2 drivers (Newtonian and SR), on primitive grids of gny x gnx cells (1D: gny = 1).
+namespace amr2 {
+
+struct Sys2 {
+    int sys;
+    double gamma;
+    void cons(const double* p, double* u) const {
+        if (sys == 0) Newton<double>{gamma}.cons(p, Pt{0, 0, 0}, u); else SR{gamma}.cons(p, Pt{0, 0, 0}, u);
+    }
+    void prim(const double* u, double* p) const {
+        if (sys == 0) Newton<double>{gamma}.prim(u, Pt{0, 0, 0}, p); else SR{gamma}.prim(u, Pt{0, 0, 0}, p);
+    }
+};
+
+// The drivers' gradient test of cell (ci, cj) against its 1-ghost transmissive neighbours:
+// |dU/dx| >= thr for any component on any side (top, bottom, left, right; 1D left, right).
+static bool hit(const Sys2& S, const double* g, int gny, int gnx, int dims, int ci, int cj, double dx, double thr) {
+    auto at = [&](int i, int j, double* u) { S.cons(g + 5 * ((size_t)ghost(i, gny, 0) * gnx + ghost(j, gnx, 0)), u); };
+    double c[5], l[5], r[5], t[5], b[5];
+    at(ci, cj, c);
+    at(ci, cj - 1, l);
+    at(ci, cj + 1, r);
+    if (dims == 2) { at(ci - 1, cj, t); at(ci + 1, cj, b); }
+    for (int k = 0; k < 5; k++) {
+        if (std::fabs((c[k] - l[k]) / dx) >= thr || std::fabs((r[k] - c[k]) / dx) >= thr) return true;
+        if (dims == 2 && (std::fabs((c[k] - t[k]) / dx) >= thr || std::fabs((b[k] - c[k]) / dx) >= thr)) return true;
+    }
+    return false;
+}
+
+// Children of parent cell (i, j) on a grid of child width cnx: 2 in 1D, 4 in 2D (tl, tr, bl, br).
+static int kids(int dims, int i, int j, int cnx, size_t* k) {
+    if (dims == 1) { k[0] = 2 * (size_t)j; k[1] = k[0] + 1; return 2; }
+    k[0] = (2 * (size_t)i) * cnx + 2 * j; k[1] = k[0] + 1;
+    k[2] = (2 * (size_t)i + 1) * cnx + 2 * j; k[3] = k[2] + 1;
+    return 4;
+}
+
+static void restrict_into(const Sys2& S, const double* child, const size_t* k, int nk, double* parent) {
+    double u[4][5], avg[5];
+    for (int q = 0; q < nk; q++) S.cons(child + 5 * k[q], u[q]);
+    for (int f = 0; f < 5; f++)
+        avg[f] = nk == 2 ? 0.5 * (u[0][f] + u[1][f]) : 0.25 * (((u[0][f] + u[1][f]) + u[2][f]) + u[3][f]);
+    S.prim(avg, parent);
+}
+
+// Refinement flags: a parent cell that passes the gradient test (and, with need_on, is itself on)
+// is switched off and its children on.
+static void flag(const Sys2& S, const double* g, int gny, int gnx, int dims, double dx, double thr, bool need_on,
+                 unsigned char* pf, unsigned char* cf) {
+    for (int i = 0; i < gny; i++)
+        for (int j = 0; j < gnx; j++) {
+            unsigned char& on = pf[(size_t)i * gnx + j];
+            if (need_on && !on) continue;
+            if (!hit(S, g, gny, gnx, dims, i, j, dx, thr)) continue;
+            on = 0;
+            size_t k[4];
+            const int nk = kids(dims, i, j, 2 * gnx, k);
+            for (int q = 0; q < nk; q++) cf[k[q]] = 1;
+        }
+}
+
+// Level exchange: restriction into an off parent (strict: only when every child is on), then
+// injection into each off child (strict: only when the parent is on).
+static void exchange(const Sys2& S, double* parent, double* child, int gny, int gnx, int dims, const unsigned char* pf,
+                     const unsigned char* cf, bool strict) {
+    for (int i = 0; i < gny; i++)
+        for (int j = 0; j < gnx; j++) {
+            size_t k[4];
+            const int nk = kids(dims, i, j, 2 * gnx, k);
+            const size_t pc = (size_t)i * gnx + j;
+            bool all = true;
+            for (int q = 0; q < nk; q++) all = all && cf[k[q]];
+            if (!pf[pc] && (!strict || all)) restrict_into(S, child, k, nk, parent + 5 * pc);
+            for (int q = 0; q < nk; q++)
+                if (!cf[k[q]] && (!strict || pf[pc])) std::memcpy(child + 5 * k[q], parent + 5 * pc, 5 * sizeof(double));
+        }
+}
+
+// Derefinement: the child-grid gradient test at cell (2i+1, 2j+1) (1D 2j+1) with divisor dx and
+// threshold thr; where nothing is marked and the children are on (strict: all of them; else the
+// first), the children go off, the parent on, and the parent is restricted from its children.
+static void derefine(const Sys2& S, double* parent, const double* child, int gny, int gnx, int dims, double dx,
+                     double thr, bool strict, unsigned char* pf, unsigned char* cf) {
+    const int cny = dims == 1 ? 1 : 2 * gny, cnx = 2 * gnx;
+    for (int i = 0; i < gny; i++)
+        for (int j = 0; j < gnx; j++) {
+            const bool marked = hit(S, child, cny, cnx, dims, dims == 1 ? 0 : 2 * i + 1, 2 * j + 1, dx, thr);
+            size_t k[4];
+            const int nk = kids(dims, i, j, cnx, k);
+            bool on = cf[k[0]] != 0;
+            if (strict)
+                for (int q = 1; q < nk; q++) on = on && cf[k[q]];
+            if (marked || !on) continue;
+            for (int q = 0; q < nk; q++) cf[k[q]] = 0;
+            pf[(size_t)i * gnx + j] = 1;
+            restrict_into(S, child, k, nk, parent + 5 * ((size_t)i * gnx + j));
+        }
+}
+
+}  // namespace amr2
+
+// EulerAMR::solveLevel2AMR (AMR/EulerAMR.cpp:593-917) and solve2DLevel2AMR (:918-1379); the SR
+// drivers (AMR/RelativisticEulerAMR.cpp:604-1392) are the same code with the SR state, including the
+// coarse flag pass's bottom neighbour [i+2][j+1] (:1008; the Level-1 SR driver reads [i+2][j+2]).
+// Three levels (coarse; intermediate at dx/2; fine at dx/4), each with flags.  Per coarse step: dt
+// (total fine count), coarse flags (tol), masked coarse step; while the intermediate level has a
+// flag on: intermediate dt, intermediate flags (tol * 2 * order with the coarse dx, only on cells
+// that are on), masked intermediate step, fine sub-steps while a fine flag is on (the total fine
+// count advances per fine step, or once when none runs), then once more per intermediate step;
+// strict exchange and derefinement (tol, coarse dx) between intermediate and fine; after the coarse
+// step: exchange and derefinement (tol * 0.5 / order) between coarse and intermediate.
+// counts (optional): [0] total fine count, [1] intermediate steps taken, [2] fine steps taken.
+int orc_amr_level2(int sys, const double* prim, int ny, int nx, int dims, double dx, double cfl, double tf,
+                   double tol, int order, double gamma, double* coarse, double* mid, double* fine, unsigned char* cflags,
+                   unsigned char* mflags, unsigned char* fflags, int* counts) {
+    if (dims == 1) ny = 1;
+    const amr2::Sys2 S{sys, gamma};
+    const int mny = dims == 1 ? 1 : 2 * ny, mnx = 2 * nx, fny = dims == 1 ? 1 : 4 * ny, fnx = 4 * nx;
+    const size_t nc = (size_t)ny * nx, nm = (size_t)mny * mnx, nf = (size_t)fny * fnx;
+    std::memcpy(coarse, prim, nc * 5 * sizeof(double));
+    std::memset(cflags, 1, nc);
+    std::memset(mflags, 0, nm);
+    std::memset(fflags, 0, nf);
+    for (int i = 0; i < mny; i++)
+        for (int j = 0; j < mnx; j++)
+            std::memcpy(mid + 5 * ((size_t)i * mnx + j), coarse + 5 * ((size_t)(i / 2) * nx + j / 2), 5 * sizeof(double));
+    for (int i = 0; i < fny; i++)
+        for (int j = 0; j < fnx; j++)
+            std::memcpy(fine + 5 * ((size_t)i * fnx + j), coarse + 5 * ((size_t)(i / 4) * nx + j / 4), 5 * sizeof(double));
+    auto step = [&](double* p, int gy, int gx, double h, double dt, const unsigned char* m) {
+        if (dims == 1) {
+            orc_sweep(sys, p, 1, gx, 1, 0, order, h, dt, 0.0, 1, gamma, 0, m, nullptr);
+        } else {
+            orc_sweep(sys, p, gy, gx, 2, 0, order, h, dt * 0.5, 0.0, 1, gamma, 0, m, nullptr);
+            orc_sweep(sys, p, gy, gx, 2, 1, order, h, dt, 0.0, 1, gamma, 0, m, nullptr);
+            orc_sweep(sys, p, gy, gx, 2, 0, order, h, dt * 0.5, 0.0, 1, gamma, 0, m, nullptr);
+        }
+    };
+    auto any = [](const unsigned char* f, size_t n) {
+        for (size_t q = 0; q < n; q++)
+            if (f[q]) return true;
+        return false;
+    };
+    double t = 0.0;
+    int it = 0, fit = 0, mrun = 0, frun = 0;
+    while (t < tf) {
+        const double dt = orc_stable_dt(sys, coarse, ny, nx, dims, dx, cfl, t, tf, fit, gamma, nullptr);
+        amr2::flag(S, coarse, ny, nx, dims, dx, tol, false, cflags, mflags);
+        step(coarse, ny, nx, dx, dt, cflags);
+        if (any(mflags, nm)) {
+            double mt = t;
+            while (mt < (t + dt - 1e-4)) {
+                const double mdt = orc_stable_dt(sys, mid, mny, mnx, dims, dx * 0.5, cfl, mt, t + dt, fit, gamma, nullptr);
+                amr2::flag(S, mid, mny, mnx, dims, dx, tol * 2.0 * order, true, mflags, fflags);
+                step(mid, mny, mnx, dx * 0.5, mdt, mflags);
+                if (any(fflags, nf)) {
+                    double ft = mt;
+                    while (ft < (mt + mdt - 1e-4)) {
+                        const double fdt = orc_stable_dt(sys, fine, fny, fnx, dims, dx * 0.25, cfl, ft, mt + mdt, fit, gamma,
+                                                         nullptr);
+                        step(fine, fny, fnx, dx * 0.25, fdt, fflags);
+                        ft += fdt;
+                        fit += 1;
+                        frun += 1;
+                    }
+                } else {
+                    fit += 1;
+                }
+                mt += mdt;
+                fit += 1;
+                mrun += 1;
+                amr2::exchange(S, mid, fine, mny, mnx, dims, mflags, fflags, true);
+                amr2::derefine(S, mid, fine, mny, mnx, dims, dx, tol, true, mflags, fflags);
+            }
+        } else {
+            fit += 1;
+        }
+        t += dt;
+        it += 1;
+        amr2::exchange(S, coarse, mid, ny, nx, dims, cflags, mflags, false);
+        amr2::derefine(S, coarse, mid, ny, nx, dims, dx, tol * 0.5 * (1.0 / order), true, cflags, mflags);
+    }
+    if (counts) { counts[0] = fit; counts[1] = mrun; counts[2] = frun; }
+    return it;
+}
+
 // ---------------------------------------------------------------- tangent-linear (Newtonian)
 // Directional derivative of the SLIC loss L = 1/2 sum_cells (rho_T - rho_target)^2 after
 // `nsteps` steps with the step sizes dts[] held fixed (the adjoint's convention), along the

@@ -72,6 +72,8 @@ class Oracle:
         L.orc_amr_derefine.argtypes = [_i, _p, _p, _i, _i, _i, _d, _d, _d, _p, _p, _p]
         L.orc_amr_level1.argtypes = [_i, _p, _i, _i, _i, _d, _d, _d, _d, _i, _d, _p, _p, _p, _p, _p, _p]
         L.orc_amr_level1.restype = _i
+        L.orc_amr_level2.argtypes = [_i, _p, _i, _i, _i, _d, _d, _d, _d, _i, _d, _p, _p, _p, _p, _p, _p, _p]
+        L.orc_amr_level2.restype = _i
         L.orc_tlm_newton.argtypes = [_p, _p, _p, _i, _i, _i, _d, _p, _i, _d, _i, _d, _i, _p]
         L.orc_tlm_newton.restype = _d
         L.orc_set_threads.argtypes = [_i]
@@ -188,6 +190,20 @@ class Oracle:
             fine_run.append(fr.value)
         return n, fs.value, cp, fp, cf, ff
 
+    def amr_level2(self, system, prim, dx, cfl, tf, tol, order, gamma):
+        """The Level-2 AMR driver: (coarse steps, [total fine count, intermediate steps taken, fine
+        steps taken], coarse, intermediate, fine prims, and the three flag sets), flattened."""
+        p = np.ascontiguousarray(prim, dtype=np.float64)
+        ny, nx, dims = _shape(p)
+        nc = nx * (ny if dims == 2 else 1)
+        r = 4 if dims == 2 else 2
+        cp, mp, fp = np.zeros(nc * 5), np.zeros(nc * r * 5), np.zeros(nc * r * r * 5)
+        cf, mf, ff = np.zeros(nc, np.uint8), np.zeros(nc * r, np.uint8), np.zeros(nc * r * r, np.uint8)
+        counts = np.zeros(3, np.int32)
+        n = self.L.orc_amr_level2(_sys(system), _ptr(p), ny, nx, dims, dx, cfl, tf, tol, order, gamma, _ptr(cp),
+                                  _ptr(mp), _ptr(fp), _ptr(cf), _ptr(mf), _ptr(ff), counts.ctypes.data)
+        return n, [int(c) for c in counts], cp, mp, fp, cf, mf, ff
+
     # ---- tangent-linear of the Newtonian SLIC loss
     def tlm_newton(self, prim0, dprim, target, dx, dts, bias, lim, gamma, bc=0):
         p = np.ascontiguousarray(prim0, dtype=np.float64)
@@ -239,6 +255,8 @@ class Reference:
         L.ref_gr_solve.restype = _i
         L.ref_amr_level1.argtypes = [_i, _p, _i, _i, _i, _d, _d, _d, _d, _i, _d, _p, _p, _p, _p, _p]
         L.ref_amr_level1.restype = _i
+        L.ref_amr_level2.argtypes = [_i, _p, _i, _i, _i, _d, _d, _d, _d, _i, _d, _p, _p, _p, _p, _p, _p]
+        L.ref_amr_level2.restype = _i
 
     def sweep(self, system, prim, axis, order, dx, dt, bias, lim, gamma, bc=0, bh=None):
         p = np.ascontiguousarray(prim, dtype=np.float64).copy()
@@ -326,3 +344,16 @@ class Reference:
         n = self.L.ref_amr_level1(_sys(system), _ptr(p), ny, nx, dims, dx, cfl, tf, tol, order, gamma,
                                   _ptr(_bh(bh)), _ptr(cp), _ptr(fp), _ptr(cf), _ptr(ff))
         return n, cp, fp, cf, ff
+
+    def amr_level2(self, system, prim, dx, cfl, tf, tol, order, gamma):
+        """The reference's Level-2 driver: (coarse steps, coarse, intermediate, fine prims, and the three
+        flag sets), flattened."""
+        p = np.ascontiguousarray(prim, dtype=np.float64)
+        ny, nx, dims = _shape(p)
+        nc = nx * (ny if dims == 2 else 1)
+        r = 4 if dims == 2 else 2
+        cp, mp, fp = np.zeros(nc * 5), np.zeros(nc * r * 5), np.zeros(nc * r * r * 5)
+        cf, mf, ff = np.zeros(nc, np.uint8), np.zeros(nc * r, np.uint8), np.zeros(nc * r * r, np.uint8)
+        n = self.L.ref_amr_level2(_sys(system), _ptr(p), ny, nx, dims, dx, cfl, tf, tol, order, gamma, _ptr(cp),
+                                  _ptr(mp), _ptr(fp), _ptr(cf), _ptr(mf), _ptr(ff))
+        return n, cp, mp, fp, cf, mf, ff

@@ -447,4 +447,48 @@ int ref_amr_level1(int sys, const double* prim, int ny, int nx, int dims, double
     return steps;
 }
 
+// ---------------------------------------------------------------- AMR (level 2)
+// Runs the reference's Level-2 AMR driver (three levels) and returns its final coarse,
+// intermediate and fine grids and flags.  sys: 0 Newtonian, 1 SR.  Returns the number of coarse
+// steps (status lines counted), -1 for other systems.
+int ref_amr_level2(int sys, const double* prim, int ny, int nx, int dims, double dx, double cfl, double tfinal,
+                   double tol, int order, double gamma, double* coarse_out, double* mid_out, double* fine_out,
+                   unsigned char* coarse_flags, unsigned char* mid_flags, unsigned char* fine_flags) {
+    EulerMaterialParameters mp(gamma);
+    Quiet q;
+    auto put_flags1 = [](const vector<bool>& f, unsigned char* o) { for (size_t i = 0; i < f.size(); i++) o[i] = f[i] ? 1 : 0; };
+    auto put_flags2 = [](const vector<vector<bool> >& f, unsigned char* o) {
+        size_t k = 0;
+        for (size_t i = 0; i < f.size(); i++) for (size_t j = 0; j < f[i].size(); j++) o[k++] = f[i][j] ? 1 : 0;
+    };
+#define AMR2_CASE(S, CALL1, CALL2)                                                                   \
+    if (dims == 1) {                                                                                 \
+        auto r = CALL1;                                                                              \
+        from1d(get<0>(r), coarse_out); from1d(get<1>(r), mid_out); from1d(get<2>(r), fine_out);      \
+        put_flags1(get<3>(r), coarse_flags); put_flags1(get<4>(r), mid_flags);                       \
+        put_flags1(get<5>(r), fine_flags);                                                           \
+    } else {                                                                                         \
+        auto r = CALL2;                                                                              \
+        from2d(get<0>(r), coarse_out); from2d(get<1>(r), mid_out); from2d(get<2>(r), fine_out);      \
+        put_flags2(get<3>(r), coarse_flags); put_flags2(get<4>(r), mid_flags);                       \
+        put_flags2(get<5>(r), fine_flags);                                                           \
+    }
+    if (sys == 0) {
+        typedef EulerStateVector S;
+        AMR2_CASE(S, EulerAMR::solveLevel2AMR(to1d<S>(prim, nx), dx, cfl, tfinal, tol, order, mp),
+                  EulerAMR::solve2DLevel2AMR(to2d<S>(prim, ny, nx), dx, cfl, tfinal, tol, order, mp))
+    } else if (sys == 1) {
+        typedef RelativisticEulerStateVector S;
+        AMR2_CASE(S, RelativisticEulerAMR::solveLevel2AMR(to1d<S>(prim, nx), dx, cfl, tfinal, tol, order, mp),
+                  RelativisticEulerAMR::solve2DLevel2AMR(to2d<S>(prim, ny, nx), dx, cfl, tfinal, tol, order, mp))
+    } else {
+        return -1;
+    }
+#undef AMR2_CASE
+    std::string s = q.sink.str();
+    int steps = 0;
+    for (size_t pos = 0; (pos = s.find("Coarse Grid Iteration", pos)) != std::string::npos; pos += 10) steps++;
+    return steps;
+}
+
 }  // extern "C"

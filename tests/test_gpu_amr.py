@@ -54,8 +54,8 @@ def check_invariants(cf, ff):
 
 
 def test_amr_level1_matches_reference_runs(cg):
-    G = dict(np.load(os.path.join(HERE, "golden", "amr_level1_golden.npz")))
-    keys = sorted(k[:-3] for k in G if k.endswith("_in"))
+    G = dict(np.load(os.path.join(HERE, "golden", "amr_golden.npz")))
+    keys = sorted(k[:-3] for k in G if k.endswith("_in") and k[3:-3].isdigit())  # Level-1 runs: amr<k>
     assert len(keys) == 8
     for k in keys:
         s = G[k + "_in"]

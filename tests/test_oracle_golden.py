@@ -130,14 +130,14 @@ def test_amr_flag_and_derefine_passes(oracle, golden, tag, system):
 
 def amr_golden():
     import os
-    return dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "amr_level1_golden.npz")))
+    return dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "amr_golden.npz")))
 
 
 def test_amr_level1_driver(oracle):
     """The oracle's Level-1 AMR driver against the reference's solveLevel1AMR / solve2DLevel1AMR runs
     (Newtonian and SR, 1D and 2D, FORCE and SLIC; several coarse steps with fine sub-cycles)."""
     G = amr_golden()
-    keys = _keys(G, "amr")
+    keys = [k for k in _keys(G, "amr") if k[3:].isdigit()]  # Level-1 runs: amr<k>
     assert len(keys) == 8
     for k in keys:
         s = G[k + "_in"]
@@ -148,3 +148,20 @@ def test_amr_level1_driver(oracle):
         assert n == int(nsteps) and nf > n, k
         assert bit_equal(cp, G[k + "_coarse"]) and bit_equal(fp, G[k + "_fine"]), k
         assert bit_equal(cf, G[k + "_cflags"]) and bit_equal(ff, G[k + "_fflags"]), k
+
+
+def test_amr_level2_driver(oracle):
+    """The oracle's Level-2 driver (three levels) against the reference's solveLevel2AMR /
+    solve2DLevel2AMR runs: every grid, flag set and the coarse step count, bit for bit."""
+    G = amr_golden()
+    keys = [k for k in _keys(G, "amr2_") if k[5:].isdigit()]  # Level-2 runs: amr2_<k>
+    assert len(keys) == 8
+    for k in keys:
+        s = G[k + "_in"]
+        system, dims, T, order, tol, nsteps = G[k + "_args"]
+        system, order = int(system), int(order)
+        n, counts, cp, mp, fp, cf, mf, ff = oracle.amr_level2(system, s, 1.0 / s.shape[-2], 0.9, T, tol, order,
+                                                              cases.SYS_GAMMA[system])
+        assert n == int(nsteps) and counts[1] > n, k
+        for name, got in (("coarse", cp), ("mid", mp), ("fine", fp), ("cflags", cf), ("mflags", mf), ("fflags", ff)):
+            assert bit_equal(got, G[f"{k}_{name}"]), (k, name)
