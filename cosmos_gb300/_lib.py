@@ -27,7 +27,7 @@ class Params(ctypes.Structure):
 
 class AmrResult(ctypes.Structure):
     _fields_ = [("coarse_steps", ctypes.c_int), ("fine_steps", ctypes.c_int), ("t", ctypes.c_double),
-                ("status", ctypes.c_int), ("fine_run", ctypes.c_int)]
+                ("status", ctypes.c_int), ("fine_run", ctypes.c_int), ("mid_run", ctypes.c_int)]
 
 
 class SolveOpts(ctypes.Structure):
@@ -74,6 +74,8 @@ SIGNATURES = {
     "cosmos_field_sums_noalloc": (_i, [_p, _i, _i, _i, _i, _sz, _p, _p]),
     "cosmos_grid_adjoint": (_i, [_p, ctypes.POINTER(SolveOpts), _i, _i, _p, _p, _p, _p, _p, _p]),
     "cosmos_amr_create": (_i, [_p, ctypes.POINTER(Params), ctypes.POINTER(_p)]),
+    "cosmos_amr_create_level2": (_i, [_p, ctypes.POINTER(Params), ctypes.POINTER(_p)]),
+    "cosmos_amr_get_level": (_i, [_p, _i, _p, _p]),
     "cosmos_amr_destroy": (_i, [_p]),
     "cosmos_amr_set_prim": (_i, [_p, _p, _sz]),
     "cosmos_amr_solve": (_i, [_p, _d, _d, _d, _i, ctypes.POINTER(AmrResult)]),

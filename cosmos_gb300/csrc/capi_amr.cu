@@ -1,13 +1,15 @@
-// C ABI of the Level-1 AMR drivers (EulerAMR::solveLevel1AMR / solve2DLevel1AMR,
-// AMR/EulerAMR.cpp:169-592; RelativisticEulerAMR twins, AMR/RelativisticEulerAMR.cpp:181-603).
+// C ABI of the AMR drivers: Level 1 (EulerAMR::solveLevel1AMR / solve2DLevel1AMR,
+// AMR/EulerAMR.cpp:169-592; RelativisticEulerAMR twins, AMR/RelativisticEulerAMR.cpp:181-603) and
+// Level 2 (solveLevel2AMR / solve2DLevel2AMR, AMR/EulerAMR.cpp:593-1379,
+// AMR/RelativisticEulerAMR.cpp:604-1392).
 //
-// Both levels are ordinary device grids (the fine one at 2x resolution and dx / 2) plus one flag
-// byte per cell.  The host keeps the reference's loop control (times, iteration counters, the
-// 1e-4 sub-cycling slack) in FP64 exactly as written; everything that touches cells runs on the
-// device: CFL reductions, the flag passes, masked sweeps (cells whose flag is off are copied),
-// the level exchange and the derefinement.  Each coarse step makes one host round trip (its CFL
-// maximum and the any-fine-flag word in one 16-byte read) plus one per fine step (its CFL
-// maximum); the masked sweeps take the host's dt as a launch argument.
+// Every level is an ordinary device grid (each at twice the previous resolution) plus one flag byte
+// per cell.  The host keeps the reference's loop control (times, iteration counters, the 1e-4
+// sub-cycling slack) in FP64 exactly as written; everything that touches cells runs on the device:
+// CFL reductions, the flag passes, masked sweeps (cells whose flag is off are copied), the level
+// exchanges and the derefinement passes.  Each level step makes one host round trip (its CFL
+// maximum, with the next level's any-flag word where the loop needs it, in one 16-byte read); the
+// masked sweeps take the host's dt as a launch argument.
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -18,10 +20,11 @@ using namespace cg;
 
 struct cosmos_amr {
     cosmos_ctx* ctx;
-    cosmos_grid* level[2];       // 0 coarse, 1 fine
-    unsigned char* flags;        // device: coarse flags (nc bytes), then fine flags (nf bytes)
-    size_t nc, nf;
-    unsigned long long* word;    // device: [0] CFL maximum (bits of a non-negative double), [1] any fine flag
+    int nlev;                    // 2: the Level-1 driver (coarse, fine); 3: Level 2 (coarse, intermediate, fine)
+    cosmos_grid* level[3];
+    unsigned char* flags;        // device: every level's flags, level after level
+    size_t n[3], off[3];         // cells and flag offset per level
+    unsigned long long* word;    // device: [0] CFL maximum (bits of a non-negative double), [1] any flag
     unsigned long long* host;    // page-locked copy of word
 };
 
@@ -70,15 +73,16 @@ int masked_step(cosmos_grid* g, int order, double dt, const unsigned char* mask)
     return masked_sweep(g, 0, order, dt * 0.5, mask);
 }
 
-// Enqueues the CFL maximum of a level into word[0] (and, with `any`, whether a fine flag is set into
-// word[1]), reads both back and returns them.
-int read_word(cosmos_amr* a, cosmos_grid* g, bool any, double* smax, bool* refined) {
+// Enqueues the CFL maximum of level l into word[0] (and, with any_level >= 0, whether a flag of that
+// level is set into word[1]), reads both back and returns them.
+int read_word(cosmos_amr* a, int l, int any_level, double* smax, bool* refined) {
     cudaStream_t st = a->ctx->stream;
+    cosmos_grid* g = a->level[l];
     MCK(cudaMemsetAsync(a->word, 0, 2 * sizeof(unsigned long long), st));
     SweepArgs w = base_args(g);
     w.src = g->buf[g->cur];
     MCK(g->p.precision == COSMOS_FP64 ? launch_wavespeed_exact(w, a->word) : launch_wavespeed_fast(w, a->word));
-    if (any) MCK(launch_amr_any(a->flags + a->nc, a->nf, a->word + 1, st));
+    if (any_level >= 0) MCK(launch_amr_any(a->flags + a->off[any_level], a->n[any_level], a->word + 1, st));
     MCK(cudaMemcpyAsync(a->host, a->word, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     MCK(cudaStreamSynchronize(st));
     memcpy(smax, &a->host[0], sizeof(double));
@@ -91,34 +95,47 @@ int bad_dt(double dt) {
     return afail(COSMOS_ENONFINITE, "AMR driver: non-finite or non-positive time step " + std::to_string(dt));
 }
 
-}  // namespace
+// Sweep arguments of level l reading its current state.
+SweepArgs level_args(cosmos_amr* a, int l) {
+    SweepArgs s = base_args(a->level[l]);
+    s.src = a->level[l]->buf[a->level[l]->cur];
+    return s;
+}
+void* state(cosmos_amr* a, int l) { return a->level[l]->buf[a->level[l]->cur]; }
+unsigned char* flags(cosmos_amr* a, int l) { return a->flags + a->off[l]; }
 
-extern "C" {
-
-int cosmos_amr_create(cosmos_ctx* ctx, const cosmos_params* p, cosmos_amr** out) {
+int create(cosmos_ctx* ctx, const cosmos_params* p, int nlev, cosmos_amr** out) {
     if (!ctx || !p || !out) return afail(COSMOS_EINVAL, "null context, params or output pointer");
     if (p->system == COSMOS_GR)
-        return afail(COSMOS_EUNSUPPORTED, "the AMR driver covers the Newtonian and SR systems (the reference's "
+        return afail(COSMOS_EUNSUPPORTED, "the AMR drivers cover the Newtonian and SR systems (the reference's "
                                           "black-hole AMR driver does not compile)");
     if (p->boundary != COSMOS_BC_TRANSMISSIVE)
-        return afail(COSMOS_EUNSUPPORTED, "the AMR driver uses the reference's transmissive boundaries");
+        return afail(COSMOS_EUNSUPPORTED, "the AMR drivers use the reference's transmissive boundaries");
     cosmos_amr* a = new cosmos_amr();
     memset((void*)a, 0, sizeof *a);
     a->ctx = ctx;
-    cosmos_params fp = *p;
-    fp.nx = 2 * p->nx;
-    fp.ny = p->dims == 2 ? 2 * p->ny : 1;
-    fp.dx = p->dx * 0.5;
-    int rc = cosmos_grid_create(ctx, p, &a->level[0]);
-    if (!rc) rc = cosmos_grid_create(ctx, &fp, &a->level[1]);
+    a->nlev = nlev;
+    int rc = COSMOS_OK;
+    size_t total = 0;
+    for (int l = 0; l < nlev && !rc; l++) {
+        cosmos_params q = *p;
+        const int s = 1 << l;
+        q.nx = s * p->nx;
+        q.ny = p->dims == 2 ? s * p->ny : 1;
+        q.dx = l == 0 ? p->dx : (l == 1 ? p->dx * 0.5 : p->dx * 0.25);  // the reference's cellSpacing * 0.5, * 0.25
+        rc = cosmos_grid_create(ctx, &q, &a->level[l]);
+        if (!rc) {
+            a->n[l] = (size_t)a->level[l]->G.nx * a->level[l]->G.ny;
+            a->off[l] = total;
+            total += a->n[l];
+        }
+    }
     if (rc) {
         cosmos_amr_destroy(a);
         return rc;
     }
-    a->nc = (size_t)a->level[0]->G.nx * a->level[0]->G.ny;
-    a->nf = (size_t)a->level[1]->G.nx * a->level[1]->G.ny;
     cudaError_t e = cudaSetDevice(ctx->device);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&a->flags, a->nc + a->nf);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&a->flags, total);
     if (e == cudaSuccess) e = cudaMalloc((void**)&a->word, 2 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMallocHost((void**)&a->host, 2 * sizeof(unsigned long long));
     if (e != cudaSuccess) {
@@ -129,14 +146,173 @@ int cosmos_amr_create(cosmos_ctx* ctx, const cosmos_params* p, cosmos_amr** out)
     return COSMOS_OK;
 }
 
+// Initial state of the drivers (AMR/EulerAMR.cpp:181-202, :606-636): every coarse flag on, every
+// other flag off, each finer level a copy of its parent.  The level exchange with the parent on
+// and the children off is exactly that copy; the intermediate flags are switched on for the
+// copy into the fine level and off again.
+int init_levels(cosmos_amr* a) {
+    cudaStream_t st = a->ctx->stream;
+    const int prec = a->level[0]->p.precision;
+    MCK(cudaMemsetAsync(flags(a, 0), 1, a->n[0], st));
+    for (int l = 1; l < a->nlev; l++) MCK(cudaMemsetAsync(flags(a, l), 0, a->n[l], st));
+    for (int l = 0; l + 1 < a->nlev; l++) {
+        if (l > 0) MCK(cudaMemsetAsync(flags(a, l), 1, a->n[l], st));
+        MCK(launch_amr_sync(level_args(a, l), prec, state(a, l), state(a, l + 1), a->level[l + 1]->G, flags(a, l),
+                            flags(a, l + 1)));
+        if (l > 0) MCK(cudaMemsetAsync(flags(a, l), 0, a->n[l], st));
+    }
+    return COSMOS_OK;
+}
+
+struct Counts {
+    int it = 0, fit = 0, mid_run = 0, fine_run = 0;
+};
+
+// Level-1 driver loop (AMR/EulerAMR.cpp:195-346).
+int run_level1(cosmos_amr* a, double cfl, double t_final, double tol, int order, double* t_out, Counts* c) {
+    cosmos_grid* C = a->level[0];
+    cosmos_grid* F = a->level[1];
+    const int prec = C->p.precision;
+    const double dx = C->p.dx;
+    double t = 0.0;
+    int rc = COSMOS_OK;
+    while (t < t_final) {
+        double smax = 0.0;
+        bool refined = false;
+        // the coarse time step is taken before the flag pass (AMR/EulerAMR.cpp:197-198); both read
+        // the same coarse state, so the flag pass is enqueued first and one read returns both
+        MCK(launch_amr_flags(level_args(a, 0), prec, tol, flags(a, 0), flags(a, 1)));
+        if ((rc = read_word(a, 0, 1, &smax, &refined))) break;
+        const double dt = cosmos_stable_dt_rule(cfl * (dx / smax), t, t_final, c->fit);
+        if ((rc = bad_dt(dt))) break;
+        if ((rc = masked_step(C, order, dt, flags(a, 0)))) break;
+        if (refined) {
+            double ft = t;
+            while (ft < (t + dt - 1e-4)) {
+                double fs = 0.0;
+                if ((rc = read_word(a, 1, -1, &fs, nullptr))) break;
+                const double fdt = cosmos_stable_dt_rule(cfl * ((dx * 0.5) / fs), ft, t + dt, c->fit);
+                if ((rc = bad_dt(fdt))) break;
+                if ((rc = masked_step(F, order, fdt, flags(a, 1)))) break;
+                ft += fdt;
+                c->fit += 1;
+                c->fine_run += 1;
+            }
+            if (rc) break;
+        } else {
+            c->fit += 1;
+        }
+        t += dt;
+        c->it += 1;
+        // restriction and injection (AMR/EulerAMR.cpp:287-307), then derefinement (:309-345)
+        SweepArgs sa = base_args(C);
+        MCK(launch_amr_sync(sa, prec, state(a, 0), state(a, 1), F->G, flags(a, 0), flags(a, 1)));
+        MCK(launch_amr_derefine(sa, prec, state(a, 1), F->G, tol, flags(a, 0), flags(a, 1), state(a, 0)));
+    }
+    *t_out = t;
+    return rc;
+}
+
+// Level-2 driver loop (AMR/EulerAMR.cpp:638-914; 2D :973-1376): coarse flags with the Newtonian
+// neighbours for both systems; intermediate steps while an intermediate flag is on, each with its
+// own flag pass (tol * 2 * order, coarse spacing, cells that are on), fine sub-steps while a fine
+// flag is on, the total fine count advancing per fine step (or once when none runs) and once more
+// per intermediate step, then the strict exchange and derefinement (tol) between intermediate and
+// fine; after the coarse step the exchange and derefinement (tol * 0.5 / order) between coarse and
+// intermediate.
+int run_level2(cosmos_amr* a, double cfl, double t_final, double tol, int order, double* t_out, Counts* c) {
+    cosmos_grid* C = a->level[0];
+    cosmos_grid* M = a->level[1];
+    cosmos_grid* F = a->level[2];
+    const int prec = C->p.precision;
+    const double dx = C->p.dx;
+    double t = 0.0;
+    int rc = COSMOS_OK;
+    while (t < t_final && !rc) {
+        double smax = 0.0;
+        bool refined = false;
+        MCK(launch_amr_flags_ex(level_args(a, 0), prec, tol, dx, true, false, flags(a, 0), flags(a, 1)));
+        if ((rc = read_word(a, 0, 1, &smax, &refined))) break;
+        const double dt = cosmos_stable_dt_rule(cfl * (dx / smax), t, t_final, c->fit);
+        if ((rc = bad_dt(dt))) break;
+        if ((rc = masked_step(C, order, dt, flags(a, 0)))) break;
+        if (refined) {
+            double mt = t;
+            while (mt < (t + dt - 1e-4)) {
+                double ms = 0.0;
+                bool refined2 = false;
+                // the intermediate time step precedes its flag pass; both read the same state
+                if ((rc = read_word(a, 1, -1, &ms, nullptr))) break;
+                const double mdt = cosmos_stable_dt_rule(cfl * ((dx * 0.5) / ms), mt, t + dt, c->fit);
+                if ((rc = bad_dt(mdt))) break;
+                MCK(launch_amr_flags_ex(level_args(a, 1), prec, tol * 2.0 * order, dx, true, true, flags(a, 1),
+                                        flags(a, 2)));
+                if ((rc = masked_step(M, order, mdt, flags(a, 1)))) break;
+                MCK(cudaMemsetAsync(a->word + 1, 0, sizeof(unsigned long long), a->ctx->stream));
+                MCK(launch_amr_any(flags(a, 2), a->n[2], a->word + 1, a->ctx->stream));
+                MCK(cudaMemcpyAsync(a->host + 1, a->word + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                    a->ctx->stream));
+                MCK(cudaStreamSynchronize(a->ctx->stream));
+                refined2 = a->host[1] != 0;
+                if (refined2) {
+                    double ft = mt;
+                    while (ft < (mt + mdt - 1e-4)) {
+                        double fs = 0.0;
+                        if ((rc = read_word(a, 2, -1, &fs, nullptr))) break;
+                        const double fdt = cosmos_stable_dt_rule(cfl * ((dx * 0.25) / fs), ft, mt + mdt, c->fit);
+                        if ((rc = bad_dt(fdt))) break;
+                        if ((rc = masked_step(F, order, fdt, flags(a, 2)))) break;
+                        ft += fdt;
+                        c->fit += 1;
+                        c->fine_run += 1;
+                    }
+                    if (rc) break;
+                } else {
+                    c->fit += 1;
+                }
+                mt += mdt;
+                c->fit += 1;
+                c->mid_run += 1;
+                SweepArgs ma = base_args(M);
+                MCK(launch_amr_sync(ma, prec, state(a, 1), state(a, 2), F->G, flags(a, 1), flags(a, 2), true));
+                MCK(launch_amr_derefine_ex(ma, prec, state(a, 2), F->G, tol, dx, true, flags(a, 1), flags(a, 2),
+                                           state(a, 1)));
+            }
+            if (rc) break;
+        } else {
+            c->fit += 1;
+        }
+        t += dt;
+        c->it += 1;
+        SweepArgs sa = base_args(C);
+        MCK(launch_amr_sync(sa, prec, state(a, 0), state(a, 1), M->G, flags(a, 0), flags(a, 1)));
+        MCK(launch_amr_derefine_ex(sa, prec, state(a, 1), M->G, tol * 0.5 * (1.0 / order), dx, true, flags(a, 0),
+                                   flags(a, 1), state(a, 0)));
+    }
+    *t_out = t;
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cosmos_amr_create(cosmos_ctx* ctx, const cosmos_params* p, cosmos_amr** out) { return create(ctx, p, 2, out); }
+
+int cosmos_amr_create_level2(cosmos_ctx* ctx, const cosmos_params* p, cosmos_amr** out) {
+    return create(ctx, p, 3, out);
+}
+
 int cosmos_amr_destroy(cosmos_amr* a) {
     if (!a) return COSMOS_OK;
-    if (a->level[0]) cudaSetDevice(a->level[0]->ctx->device);
-    if (a->ctx) cudaStreamSynchronize(a->ctx->stream);
+    if (a->ctx) {
+        cudaSetDevice(a->ctx->device);
+        cudaStreamSynchronize(a->ctx->stream);
+    }
     if (a->flags) cudaFree(a->flags);
     if (a->word) cudaFree(a->word);
     if (a->host) cudaFreeHost(a->host);
-    for (int l = 0; l < 2; l++) cosmos_grid_destroy(a->level[l]);
+    for (int l = 0; l < 3; l++) cosmos_grid_destroy(a->level[l]);
     delete a;
     return COSMOS_OK;
 }
@@ -150,85 +326,47 @@ int cosmos_amr_solve(cosmos_amr* a, double cfl, double t_final, double tol, int 
     if (!a) return afail(COSMOS_EINVAL, "null AMR handle");
     if (order != 1 && order != 2) return afail(COSMOS_EINVAL, "order must be 1 (FORCE) or 2 (SLIC)");
     if (!(cfl > 0.0)) return afail(COSMOS_EINVAL, "cfl must be positive");
-    cosmos_grid* C = a->level[0];
-    cosmos_grid* F = a->level[1];
-    const int prec = C->p.precision;
     MCK(cudaSetDevice(a->ctx->device));
     cudaStream_t st = a->ctx->stream;
-    unsigned char* cflags = a->flags;
-    unsigned char* fflags = a->flags + a->nc;
-    MCK(cudaMemsetAsync(C->status, 0, sizeof(int), st));
-    MCK(cudaMemsetAsync(F->status, 0, sizeof(int), st));
-    // initial flags (AMR/EulerAMR.cpp:181-190) and fine cells copied from their parents (:197-202):
-    // with every coarse flag on and every fine flag off, the level exchange is exactly that copy
-    MCK(cudaMemsetAsync(cflags, 1, a->nc, st));
-    MCK(cudaMemsetAsync(fflags, 0, a->nf, st));
-    SweepArgs ca = base_args(C);
-    MCK(launch_amr_sync(ca, prec, C->buf[C->cur], F->buf[F->cur], F->G, cflags, fflags));
-    const double dx = C->p.dx;
+    for (int l = 0; l < a->nlev; l++) MCK(cudaMemsetAsync(a->level[l]->status, 0, sizeof(int), st));
+    MRC(init_levels(a));
+    Counts c;
     double t = 0.0;
-    int it = 0, fit = 0, run = 0;
-    int rc = COSMOS_OK;
-    while (t < t_final) {
-        double smax = 0.0;
-        bool refined = false;
-        // the coarse time step is taken before the flag pass (AMR/EulerAMR.cpp:197-198); both read
-        // the same coarse state, so the flag pass is enqueued first and one read returns both
-        SweepArgs fa = base_args(C);
-        fa.src = C->buf[C->cur];
-        MCK(launch_amr_flags(fa, prec, tol, cflags, fflags));
-        if ((rc = read_word(a, C, true, &smax, &refined))) break;
-        const double dt = cosmos_stable_dt_rule(cfl * (dx / smax), t, t_final, fit);
-        if ((rc = bad_dt(dt))) break;
-        if ((rc = masked_step(C, order, dt, cflags))) break;
-        if (refined) {
-            double ft = t;
-            while (ft < (t + dt - 1e-4)) {
-                double fs = 0.0;
-                if ((rc = read_word(a, F, false, &fs, nullptr))) break;
-                const double fdt = cosmos_stable_dt_rule(cfl * ((dx * 0.5) / fs), ft, t + dt, fit);
-                if ((rc = bad_dt(fdt))) break;
-                if ((rc = masked_step(F, order, fdt, fflags))) break;
-                ft += fdt;
-                fit += 1;
-                run += 1;
-            }
-            if (rc) break;
-        } else {
-            fit += 1;
-        }
-        t += dt;
-        it += 1;
-        // restriction and injection (AMR/EulerAMR.cpp:287-307), then derefinement (:309-345)
-        SweepArgs sa = base_args(C);
-        MCK(launch_amr_sync(sa, prec, C->buf[C->cur], F->buf[F->cur], F->G, cflags, fflags));
-        MCK(launch_amr_derefine(sa, prec, F->buf[F->cur], F->G, tol, cflags, fflags, C->buf[C->cur]));
-    }
-    int st2[2] = {0, 0};
-    MCK(cudaMemcpyAsync(&st2[0], C->status, sizeof(int), cudaMemcpyDeviceToHost, st));
-    MCK(cudaMemcpyAsync(&st2[1], F->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    const int rc = a->nlev == 2 ? run_level1(a, cfl, t_final, tol, order, &t, &c)
+                                : run_level2(a, cfl, t_final, tol, order, &t, &c);
+    if (rc != COSMOS_OK && rc != COSMOS_ENONFINITE) return rc;
+    int sts[3] = {0, 0, 0};
+    for (int l = 0; l < a->nlev; l++)
+        MCK(cudaMemcpyAsync(&sts[l], a->level[l]->status, sizeof(int), cudaMemcpyDeviceToHost, st));
     MCK(cudaStreamSynchronize(st));
     if (r) {
-        r->coarse_steps = it;
-        r->fine_steps = fit;
+        r->coarse_steps = c.it;
+        r->fine_steps = c.fit;
         r->t = t;
-        r->status = st2[0] | st2[1] | (rc == COSMOS_ENONFINITE ? COSMOS_STATUS_NONFINITE : 0);
-        r->fine_run = run;
+        r->status = sts[0] | sts[1] | sts[2] | (rc == COSMOS_ENONFINITE ? COSMOS_STATUS_NONFINITE : 0);
+        r->fine_run = c.fine_run;
+        r->mid_run = c.mid_run;
     }
     return rc;
+}
+
+int cosmos_amr_get_level(cosmos_amr* a, int level, double* prim, unsigned char* level_flags) {
+    if (!a) return afail(COSMOS_EINVAL, "null AMR handle");
+    if (level < 0 || level >= a->nlev) return afail(COSMOS_EINVAL, "level out of range");
+    MCK(cudaSetDevice(a->ctx->device));
+    if (prim) MRC(cosmos_grid_get_prim(a->level[level], prim, 5 * a->n[level]));
+    if (level_flags) {
+        MCK(cudaMemcpyAsync(level_flags, flags(a, level), a->n[level], cudaMemcpyDeviceToHost, a->ctx->stream));
+        MCK(cudaStreamSynchronize(a->ctx->stream));
+    }
+    return COSMOS_OK;
 }
 
 int cosmos_amr_get(cosmos_amr* a, double* coarse_prim, double* fine_prim, unsigned char* coarse_flags,
                    unsigned char* fine_flags) {
     if (!a) return afail(COSMOS_EINVAL, "null AMR handle");
-    MCK(cudaSetDevice(a->ctx->device));
-    if (coarse_prim) MRC(cosmos_grid_get_prim(a->level[0], coarse_prim, 5 * a->nc));
-    if (fine_prim) MRC(cosmos_grid_get_prim(a->level[1], fine_prim, 5 * a->nf));
-    cudaStream_t st = a->ctx->stream;
-    if (coarse_flags) MCK(cudaMemcpyAsync(coarse_flags, a->flags, a->nc, cudaMemcpyDeviceToHost, st));
-    if (fine_flags) MCK(cudaMemcpyAsync(fine_flags, a->flags + a->nc, a->nf, cudaMemcpyDeviceToHost, st));
-    MCK(cudaStreamSynchronize(st));
-    return COSMOS_OK;
+    MRC(cosmos_amr_get_level(a, 0, coarse_prim, coarse_flags));
+    return cosmos_amr_get_level(a, a->nlev - 1, fine_prim, fine_flags);
 }
 
 }  // extern "C"

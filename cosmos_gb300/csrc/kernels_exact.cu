@@ -246,14 +246,21 @@ struct ConsLoader {
     }
 };
 
-// Refinement pass, AMR/EulerAMR.cpp:207-229 (1D) and :400-431 (2D); the SR and GR drivers read
-// the bottom neighbour at [i+2][j+2] (AMR/RelativisticEulerAMR.cpp:422,
+// Refinement pass, AMR/EulerAMR.cpp:207-229 (1D) and :400-431 (2D); the SR and GR Level-1 drivers
+// read the bottom neighbour at [i+2][j+2] (AMR/RelativisticEulerAMR.cpp:422,
 // AMR/BlackHoleEulerAMR.cpp:490), whose corner ghost keeps the default state (1,0,0,0,1).
-__global__ void amr_flags_kernel(ConsLoader L, double dx, double tol, unsigned char* coarse, unsigned char* fine) {
+// The Level-2 drivers' passes (AMR/EulerAMR.cpp:643-664 coarse, :699-722 intermediate, and the SR
+// twins, whose coarse pass reads [i+2][j+1], AMR/RelativisticEulerAMR.cpp:1008) use `plain` (the
+// Newtonian neighbours for every system), a threshold other than the tolerance, the coarse spacing
+// as the divisor on a finer grid (`div`) and, for the intermediate pass, `need_on` (only cells
+// whose own flag is on are tested).  dx places the cells (black-hole coordinates).
+__global__ void amr_flags_kernel(ConsLoader L, double dx, double tol, double div, int plain, int need_on,
+                                 unsigned char* coarse, unsigned char* fine) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y;
     const Geom& G = L.G;
     if (j >= G.nx) return;
+    if (need_on && !coarse[(size_t)i * G.nx + j]) return;
     double c[5], l[5], r[5], t[5], b[5];
     bool hit = false;
     if (G.dims == 1) {
@@ -262,13 +269,13 @@ __global__ void amr_flags_kernel(ConsLoader L, double dx, double tol, unsigned c
         L.get(0, j + 1, Pt{(j + 1) * dx, 0.0, 0.0}, r);
 #pragma unroll
         for (int k = 0; k < 5; k++)
-            if (fabs((c[k] - l[k]) / dx) >= tol || fabs((r[k] - c[k]) / dx) >= tol) hit = true;
+            if (fabs((c[k] - l[k]) / div) >= tol || fabs((r[k] - c[k]) / div) >= tol) hit = true;
     } else {
         L.get(i - 1, j, Pt{j * dx, (i - 1) * dx, 0.0}, t);
         L.get(i, j - 1, Pt{(j - 1) * dx, i * dx, 0.0}, l);
         L.get(i, j, Pt{j * dx, i * dx, 0.0}, c);
         L.get(i, j + 1, Pt{(j + 1) * dx, i * dx, 0.0}, r);
-        if (L.system == 0) L.get(i + 1, j, Pt{j * dx, (i + 1) * dx, 0.0}, b);
+        if (L.system == 0 || plain) L.get(i + 1, j, Pt{j * dx, (i + 1) * dx, 0.0}, b);
         else if (i == G.ny - 1 && j == G.nx - 1) {
             const double dflt[5] = {1.0, 0.0, 0.0, 0.0, 1.0};
             if (L.precision == 1) {
@@ -280,8 +287,8 @@ __global__ void amr_flags_kernel(ConsLoader L, double dx, double tol, unsigned c
         } else L.get(i + 1, j + 1, Pt{(j + 1) * dx, (i + 1) * dx, 0.0}, b);
 #pragma unroll
         for (int k = 0; k < 5; k++)
-            if (fabs((c[k] - t[k]) / dx) >= tol || fabs((b[k] - c[k]) / dx) >= tol ||
-                fabs((c[k] - l[k]) / dx) >= tol || fabs((r[k] - c[k]) / dx) >= tol)
+            if (fabs((c[k] - t[k]) / div) >= tol || fabs((b[k] - c[k]) / div) >= tol ||
+                fabs((c[k] - l[k]) / div) >= tol || fabs((r[k] - c[k]) / div) >= tol)
                 hit = true;
     }
     if (!hit) return;
@@ -312,8 +319,13 @@ static ConsLoader make_loader(const SweepArgs& a, int precision, const void* sta
 }
 
 cudaError_t launch_amr_flags(const SweepArgs& a, int precision, double tol, unsigned char* coarse, unsigned char* fine) {
+    return launch_amr_flags_ex(a, precision, tol, a.dx, false, false, coarse, fine);
+}
+cudaError_t launch_amr_flags_ex(const SweepArgs& a, int precision, double thr, double div, bool plain, bool need_on,
+                                unsigned char* coarse, unsigned char* fine) {
     dim3 grid((a.G.nx + 127) / 128, a.G.ny);
-    amr_flags_kernel<<<grid, 128, 0, a.stream>>>(make_loader(a, precision, a.src, a.G), a.dx, tol, coarse, fine);
+    amr_flags_kernel<<<grid, 128, 0, a.stream>>>(make_loader(a, precision, a.src, a.G), a.dx, thr, div, plain ? 1 : 0,
+                                                 need_on ? 1 : 0, coarse, fine);
     count_launch();
     return cudaGetLastError();
 }
@@ -322,12 +334,15 @@ cudaError_t launch_amr_flags(const SweepArgs& a, int precision, double tol, unsi
 // AMR/BlackHoleEulerAMR.cpp:388-421 (1D fine cells read one fine cell to the left) and :632-686.
 // Restriction writes the coarse state (FP64 storage only holds primitives, converted with the
 // system's exact prim; FP32 storage receives the averaged conserved state).
-__global__ void amr_derefine_kernel(ConsLoader F, Geom CG, double dx, double tol, unsigned char* coarse,
-                                    unsigned char* fine, void* coarse_state) {
+// The Level-2 drivers' passes (AMR/EulerAMR.cpp:804-838 on the fine grid, :875-911 on the
+// intermediate grid) take other thresholds and the coarse spacing as divisor (`div`), and are
+// `strict`: they derefine only where every child is flagged (Level-1 tests the first child).
+__global__ void amr_derefine_kernel(ConsLoader F, Geom CG, double dx, double half, double div, int strict,
+                                    unsigned char* coarse, unsigned char* fine, void* coarse_state) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y;
     if (j >= CG.nx) return;
-    const double half = tol * 0.5, fdx = dx * 0.5;
+    const double fdx = dx * 0.5;
     bool marked = false;
     double c[5], l[5], r[5], t[5], b[5], avg[5];
     Pt qc;
@@ -337,8 +352,8 @@ __global__ void amr_derefine_kernel(ConsLoader F, Geom CG, double dx, double tol
         F.get(0, 2 * j + 2, Pt{((j * 2) + 1) * fdx, 0.0, 0.0}, r);
 #pragma unroll
         for (int k = 0; k < 5; k++)
-            if (fabs((c[k] - l[k]) / dx) >= half || fabs((r[k] - c[k]) / dx) >= half) marked = true;
-        if (marked || !fine[2 * j]) return;
+            if (fabs((c[k] - l[k]) / div) >= half || fabs((r[k] - c[k]) / div) >= half) marked = true;
+        if (marked || !fine[2 * j] || (strict && !fine[2 * j + 1])) return;
         fine[2 * j] = 0;
         fine[2 * j + 1] = 0;
         coarse[j] = 1;
@@ -356,11 +371,14 @@ __global__ void amr_derefine_kernel(ConsLoader F, Geom CG, double dx, double tol
         F.get(2 * i + 2, 2 * j + 1, Pt{((j * 2) + 1) * fdx, ((i * 2) + 2) * fdx, 0.0}, b);
 #pragma unroll
         for (int k = 0; k < 5; k++)
-            if (fabs((c[k] - t[k]) / dx) >= half || fabs((b[k] - c[k]) / dx) >= half ||
-                fabs((c[k] - l[k]) / dx) >= half || fabs((r[k] - c[k]) / dx) >= half)
+            if (fabs((c[k] - t[k]) / div) >= half || fabs((b[k] - c[k]) / div) >= half ||
+                fabs((c[k] - l[k]) / div) >= half || fabs((r[k] - c[k]) / div) >= half)
                 marked = true;
         const size_t fw = 2 * (size_t)CG.nx;
         if (marked || !fine[(2 * i) * fw + 2 * j]) return;
+        if (strict && !(fine[(2 * i) * fw + 2 * j + 1] && fine[(2 * i + 1) * fw + 2 * j] &&
+                        fine[(2 * i + 1) * fw + 2 * j + 1]))
+            return;
         fine[(2 * i) * fw + 2 * j] = 0;
         fine[(2 * i) * fw + 2 * j + 1] = 0;
         fine[(2 * i + 1) * fw + 2 * j] = 0;
@@ -394,9 +412,14 @@ __global__ void amr_derefine_kernel(ConsLoader F, Geom CG, double dx, double tol
 
 cudaError_t launch_amr_derefine(const SweepArgs& a, int precision, const void* fine_state, const Geom& FG, double tol,
                                 unsigned char* coarse, unsigned char* fine, void* coarse_state) {
+    return launch_amr_derefine_ex(a, precision, fine_state, FG, tol * 0.5, a.dx, false, coarse, fine, coarse_state);
+}
+cudaError_t launch_amr_derefine_ex(const SweepArgs& a, int precision, const void* fine_state, const Geom& FG, double thr,
+                                   double div, bool strict, unsigned char* coarse, unsigned char* fine,
+                                   void* coarse_state) {
     dim3 grid((a.G.nx + 127) / 128, a.G.ny);
-    amr_derefine_kernel<<<grid, 128, 0, a.stream>>>(make_loader(a, precision, fine_state, FG), a.G, a.dx, tol, coarse,
-                                                    fine, coarse_state);
+    amr_derefine_kernel<<<grid, 128, 0, a.stream>>>(make_loader(a, precision, fine_state, FG), a.G, a.dx, thr, div,
+                                                    strict ? 1 : 0, coarse, fine, coarse_state);
     count_launch();
     return cudaGetLastError();
 }
@@ -405,11 +428,13 @@ cudaError_t launch_amr_derefine(const SweepArgs& a, int precision, const void* f
 // (2D): a coarse cell whose flag is off takes the conserved average of its fine children
 // (0.5 (a + b) in 1D, 0.25 (((a + b) + c) + d) in 2D, then the system's prim), and every fine
 // child whose flag is off takes its parent's state.  One thread per coarse cell touches only
-// that cell and its own children, in the reference's order (restriction, then injection).
+// that cell and its own children, in the reference's order (restriction, then injection).  The
+// Level-2 drivers' exchange between the intermediate and fine levels (AMR/EulerAMR.cpp:780-801) is
+// `strict`: restriction only where every child is flagged, injection only under a flagged parent.
 // FP64 storage holds primitives; FP32 Newtonian/SR storage holds conserved values, which are
 // averaged in FP64 and copied as stored.
 __global__ void amr_sync_kernel(ConsLoader F, Geom CG, void* coarse_state, void* fine_state,
-                                const unsigned char* coarse, const unsigned char* fine) {
+                                const unsigned char* coarse, const unsigned char* fine, int strict) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y;
     if (j >= CG.nx) return;
@@ -422,7 +447,10 @@ __global__ void amr_sync_kernel(ConsLoader F, Geom CG, void* coarse_state, void*
     }
     const size_t cidx = (size_t)i * CG.pitch + j;
     const bool fp32 = F.precision == 1;
-    if (!coarse[(size_t)i * CG.nx + j]) {
+    const bool on = coarse[(size_t)i * CG.nx + j] != 0;
+    bool all = true;
+    for (int q = 0; q < nk; q++) all = all && fine[(size_t)ki[q] * FG.nx + kj[q]];
+    if (!on && (!strict || all)) {
         double u[4][5], avg[5];
         for (int q = 0; q < nk; q++) F.get(ki[q], kj[q], Pt{0.0, 0.0, 0.0}, u[q]);
 #pragma unroll
@@ -440,7 +468,7 @@ __global__ void amr_sync_kernel(ConsLoader F, Geom CG, void* coarse_state, void*
         }
     }
     for (int q = 0; q < nk; q++) {
-        if (fine[(size_t)ki[q] * FG.nx + kj[q]]) continue;
+        if (fine[(size_t)ki[q] * FG.nx + kj[q]] || (strict && !on)) continue;
         const size_t fidx = (size_t)ki[q] * FG.pitch + kj[q];
         if (fp32) {
 #pragma unroll
@@ -455,11 +483,11 @@ __global__ void amr_sync_kernel(ConsLoader F, Geom CG, void* coarse_state, void*
 }
 
 cudaError_t launch_amr_sync(const SweepArgs& a, int precision, void* coarse_state, void* fine_state, const Geom& FG,
-                            const unsigned char* coarse, const unsigned char* fine) {
+                            const unsigned char* coarse, const unsigned char* fine, bool strict) {
     if (a.system == 2) return cudaErrorNotSupported;
     dim3 grid((a.G.nx + 127) / 128, a.G.ny);
     amr_sync_kernel<<<grid, 128, 0, a.stream>>>(make_loader(a, precision, fine_state, FG), a.G, coarse_state,
-                                                fine_state, coarse, fine);
+                                                fine_state, coarse, fine, strict ? 1 : 0);
     count_launch();
     return cudaGetLastError();
 }

@@ -51,10 +51,19 @@ cudaError_t launch_amr_flags(const SweepArgs& a, int precision, double tol, unsi
                              unsigned char* fine);
 cudaError_t launch_amr_derefine(const SweepArgs& a, int precision, const void* fine_state, const Geom& FG,
                                 double tol, unsigned char* coarse, unsigned char* fine, void* coarse_state);
-// Level-1 end-of-step exchange (restriction into unflagged coarse cells, injection into unflagged
-// fine cells; Newtonian and SR) and the any-flag test of n bytes (ORs 1 into *out).
+// The Level-2 drivers' forms: threshold `thr`, divisor `div` (the coarse spacing on a finer grid),
+// `plain` (Newtonian neighbours for every system), `need_on` (test only cells that are on), `strict`
+// (derefine only where every child is flagged).
+cudaError_t launch_amr_flags_ex(const SweepArgs& a, int precision, double thr, double div, bool plain, bool need_on,
+                                unsigned char* coarse, unsigned char* fine);
+cudaError_t launch_amr_derefine_ex(const SweepArgs& a, int precision, const void* fine_state, const Geom& FG, double thr,
+                                   double div, bool strict, unsigned char* coarse, unsigned char* fine,
+                                   void* coarse_state);
+// End-of-step level exchange (restriction into unflagged parent cells, injection into unflagged
+// children; strict: restriction only where every child is flagged, injection only under a flagged
+// parent; Newtonian and SR) and the any-flag test of n bytes (ORs 1 into *out).
 cudaError_t launch_amr_sync(const SweepArgs& a, int precision, void* coarse_state, void* fine_state, const Geom& FG,
-                            const unsigned char* coarse, const unsigned char* fine);
+                            const unsigned char* coarse, const unsigned char* fine, bool strict = false);
 cudaError_t launch_amr_any(const unsigned char* flags, size_t n, unsigned long long* out, cudaStream_t st);
 
 // FP32 bulk path (conserved SoA storage, float)

@@ -470,10 +470,11 @@ def solve_with_steps(system, cells, dx, cfl, t_final, bias, limiter, gamma, orde
 
 
 class AMR:
-    """A device-resident Level-1 AMR pair (cosmos_amr): a coarse grid of `shape` and its 2x
-    refinement with one flag per cell (Newtonian or SR, transmissive boundaries)."""
+    """A device-resident AMR hierarchy (cosmos_amr) with one flag per cell (Newtonian or SR,
+    transmissive boundaries): levels=1 is the Level-1 driver (a coarse grid of `shape` and its 2x
+    refinement), levels=2 the Level-2 driver (coarse, 2x intermediate, 4x fine)."""
 
-    def __init__(self, system, shape, dx, gamma, precision=FP64, ctx=None, sr_c2p64_above=2.0):
+    def __init__(self, system, shape, dx, gamma, precision=FP64, ctx=None, sr_c2p64_above=2.0, levels=1):
         self.ctx = ctx or default_context()
         p = Params()
         load().cosmos_params_default(ctypes.byref(p))
@@ -484,10 +485,15 @@ class AMR:
         else:
             p.dims, p.ny, p.nx = 2, shape[0], shape[1]
         p.precision, p.boundary, p.gamma, p.dx = precision, BC_TRANSMISSIVE, float(gamma), float(dx)
+        if levels not in (1, 2):
+            raise ValueError("levels must be 1 or 2")
+        self.levels = levels
         self.shape = tuple(shape)
-        self.fine_shape = tuple(2 * n for n in shape)
+        self.shapes = [tuple((1 << l) * n for n in shape) for l in range(levels + 1)]
+        self.fine_shape = self.shapes[-1]
         h = ctypes.c_void_p()
-        check(load().cosmos_amr_create(self.ctx.h, ctypes.byref(p), ctypes.byref(h)))
+        create = load().cosmos_amr_create if levels == 1 else load().cosmos_amr_create_level2
+        check(create(self.ctx.h, ctypes.byref(p), ctypes.byref(h)))
         self.h = h
 
     def set_prim(self, prim):
@@ -501,17 +507,22 @@ class AMR:
         the reference's counters.  self.fine_run holds the number of fine steps actually taken."""
         r = _lib.AmrResult()
         check(load().cosmos_amr_solve(self.h, float(cfl), float(t_final), float(tol), int(order), ctypes.byref(r)))
-        self.fine_run = r.fine_run
+        self.fine_run, self.mid_run = r.fine_run, r.mid_run
         return r.coarse_steps, r.fine_steps, r.t, r.status
 
+    def get_level(self, level):
+        """(cells, flags) of one level: 0 coarse, up to `levels` (the finest)."""
+        sh = self.shapes[level]
+        cells = np.empty(sh + (5,))
+        fl = np.empty(sh, np.uint8)
+        check(load().cosmos_amr_get_level(self.h, int(level), cells.ctypes.data, fl.ctypes.data))
+        return cells, fl.astype(bool)
+
     def get(self):
-        """(coarse cells, fine cells, coarse flags, fine flags) as the reference's driver returns them."""
-        cp = np.empty(self.shape + (5,))
-        fp = np.empty(self.fine_shape + (5,))
-        cf = np.empty(self.shape, np.uint8)
-        ff = np.empty(self.fine_shape, np.uint8)
-        check(load().cosmos_amr_get(self.h, cp.ctypes.data, fp.ctypes.data, cf.ctypes.data, ff.ctypes.data))
-        return cp, fp, cf.astype(bool), ff.astype(bool)
+        """The reference driver's tuple: Level 1 (coarse, fine cells, coarse, fine flags); Level 2
+        (coarse, intermediate, fine cells, coarse, intermediate, fine flags)."""
+        got = [self.get_level(l) for l in range(self.levels + 1)]
+        return tuple(c for c, _ in got) + tuple(f for _, f in got)
 
     def close(self):
         if getattr(self, "h", None) and not sys.is_finalizing():
@@ -527,7 +538,8 @@ class AMR:
 
 def _amr_family(system, name):
     """The reference's AMR driver class of one system (AMR/EulerAMR.hpp, AMR/RelativisticEulerAMR.hpp):
-    solveLevel1AMR / solve2DLevel1AMR return (coarse cells, fine cells, coarse flags, fine flags)."""
+    solveLevel1AMR / solve2DLevel1AMR return (coarse cells, fine cells, coarse flags, fine flags);
+    solveLevel2AMR / solve2DLevel2AMR (coarse, intermediate, fine cells, and their three flag sets)."""
 
     class Driver:
         __qualname__ = f"{name}AMR"
@@ -544,6 +556,20 @@ def _amr_family(system, name):
                 a.close()
 
         solve2DLevel1AMR = solveLevel1AMR
+
+        @staticmethod
+        def solveLevel2AMR(initialCells, cellSpacing, CFLCoefficient, finalTime, AMRTolerance, order,
+                           materialParameters, precision=FP64):
+            a = AMR(system, _shape(initialCells), cellSpacing, materialParameters.getAdiabaticIndex(), precision,
+                    levels=2)
+            try:
+                a.set_prim(initialCells)
+                a.solve(CFLCoefficient, finalTime, AMRTolerance, order)
+                return a.get()
+            finally:
+                a.close()
+
+        solve2DLevel2AMR = solveLevel2AMR
 
     return Driver
 

@@ -228,8 +228,16 @@ typedef struct cosmos_amr_result {
     double t;          /* coarseCurrentTime at exit */
     int status;        /* COSMOS_STATUS_* bits of both levels' kernels */
     int fine_run;      /* fine steps actually taken (fine_steps also counts coarse steps with no refinement) */
+    int mid_run;       /* Level-2 drivers: intermediate steps taken (0 for Level 1) */
 } cosmos_amr_result;
 int cosmos_amr_create(cosmos_ctx* ctx, const cosmos_params* coarse, cosmos_amr** out);
+/* Level-2 drivers: EulerAMR::solveLevel2AMR / solve2DLevel2AMR (AMR/EulerAMR.cpp:593-1379) and the
+ * RelativisticEulerAMR twins (AMR/RelativisticEulerAMR.cpp:604-1392): three levels (coarse,
+ * intermediate at dx / 2, fine at dx / 4).  The intermediate level sub-cycles inside each coarse
+ * step and the fine level inside each intermediate step, with the reference's thresholds
+ * (intermediate flags at tol * 2 * order, fine derefinement at tol, intermediate derefinement at
+ * tol * 0.5 / order, all with the coarse spacing) and its counters.  Same calls as Level 1. */
+int cosmos_amr_create_level2(cosmos_ctx* ctx, const cosmos_params* coarse, cosmos_amr** out);
 int cosmos_amr_destroy(cosmos_amr* a);
 /* The coarse grid's initial cells (5 * nx * ny doubles, the layout of cosmos_grid_set_prim). */
 int cosmos_amr_set_prim(cosmos_amr* a, const double* prim, size_t n_doubles);
@@ -237,10 +245,13 @@ int cosmos_amr_set_prim(cosmos_amr* a, const double* prim, size_t n_doubles);
  * cells injected from their parents, then coarse steps until t >= t_final.  order 1: FORCE,
  * 2: SLIC.  tol: the AMRTolerance argument. */
 int cosmos_amr_solve(cosmos_amr* a, double cfl, double t_final, double tol, int order, cosmos_amr_result* r);
-/* The driver's returned tuple: coarse cells (5 nx ny doubles), fine cells (4x or 2x as many),
- * coarse and fine flags (1 byte per cell).  Any pointer may be NULL. */
+/* The Level-1 driver's returned tuple: coarse cells (5 nx ny doubles), fine cells (4x or 2x as
+ * many), coarse and fine flags (1 byte per cell); for a Level-2 driver the fine level is the finest.
+ * Any pointer may be NULL. */
 int cosmos_amr_get(cosmos_amr* a, double* coarse_prim, double* fine_prim, unsigned char* coarse_flags,
                    unsigned char* fine_flags);
+/* One level's cells and flags: level 0 coarse, 1 the next finer, 2 the finest of a Level-2 driver. */
+int cosmos_amr_get_level(cosmos_amr* a, int level, double* prim, unsigned char* flags);
 
 /* Allocation-free conservation sums.  No counterpart in the reference: it exists for callers that
  * cannot allocate device memory where they need the sums -- code recorded into a CUDA graph

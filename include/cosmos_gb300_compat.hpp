@@ -400,14 +400,15 @@ public:
     }
 };
 
-// ----------------------------------------------------------------------------- Level-1 AMR drivers
+// ----------------------------------------------------------------------------- AMR drivers
 // AMR/EulerAMR.hpp and AMR/RelativisticEulerAMR.hpp: solveLevel1AMR / solve2DLevel1AMR return
-// (coarse cells, fine cells, coarse flags, fine flags).  The Level-2 drivers are not provided.
+// (coarse cells, fine cells, coarse flags, fine flags); solveLevel2AMR / solve2DLevel2AMR return
+// (coarse, intermediate, fine cells, and the three flag sets).
 namespace cosmos_compat_detail {
 
 struct Amr {
     cosmos_amr* a = nullptr;
-    Amr(int system, int dims, int nx, int ny, double dx, double gamma) {
+    Amr(int system, int dims, int nx, int ny, double dx, double gamma, int levels = 1) {
         cosmos_params p;
         cosmos_params_default(&p);
         p.system = system;
@@ -416,7 +417,7 @@ struct Amr {
         p.ny = dims == 1 ? 1 : ny;
         p.dx = dx;
         p.gamma = gamma;
-        check(cosmos_amr_create(ctx(), &p, &a));
+        check(levels == 1 ? cosmos_amr_create(ctx(), &p, &a) : cosmos_amr_create_level2(ctx(), &p, &a));
     }
     ~Amr() { cosmos_amr_destroy(a); }
     // runs the driver and fills the host copies of both levels and their flags
@@ -465,6 +466,60 @@ amr2(int sys, std::vector<std::vector<S> > cells, double dx, double cfl, double 
     return std::make_tuple(coarse, fine, cb, fb);
 }
 
+// Level-2 run: level l of the three, as primitives and flags.
+struct Amr2Out {
+    std::vector<double> c[3];
+    std::vector<unsigned char> f[3];
+};
+inline Amr2Out amr2_run(int sys, int dims, int nx, int ny, const std::vector<double>& prim, double dx, double cfl,
+                        double T, double tol, int order, double gamma) {
+    Amr d(sys, dims, nx, ny, dx, gamma, 2);
+    check(cosmos_amr_set_prim(d.a, prim.data(), prim.size()));
+    cosmos_amr_result r;
+    check(cosmos_amr_solve(d.a, cfl, T, tol, order, &r));
+    Amr2Out o;
+    const size_t n = (size_t)nx * (dims == 2 ? ny : 1);
+    for (int l = 0; l < 3; l++) {
+        const size_t m = n << (dims == 2 ? 2 * l : l);
+        o.c[l].resize(5 * m);
+        o.f[l].resize(m);
+        check(cosmos_amr_get_level(d.a, l, o.c[l].data(), o.f[l].data()));
+    }
+    return o;
+}
+
+template <class S>
+std::tuple<std::vector<S>, std::vector<S>, std::vector<S>, std::vector<bool>, std::vector<bool>, std::vector<bool> >
+amr1_level2(int sys, std::vector<S> cells, double dx, double cfl, double T, double tol, int order,
+            EulerMaterialParameters mp) {
+    const size_t n = cells.size();
+    Amr2Out o = amr2_run(sys, 1, (int)n, 1, pack1(cells), dx, cfl, T, tol, order, mp.getAdiabaticIndex());
+    std::vector<S> lv[3] = {std::vector<S>(n), std::vector<S>(2 * n), std::vector<S>(4 * n)};
+    for (int l = 0; l < 3; l++) unpack1(o.c[l], lv[l]);
+    auto b = [](const std::vector<unsigned char>& f) { return std::vector<bool>(f.begin(), f.end()); };
+    return std::make_tuple(lv[0], lv[1], lv[2], b(o.f[0]), b(o.f[1]), b(o.f[2]));
+}
+
+template <class S>
+std::tuple<std::vector<std::vector<S> >, std::vector<std::vector<S> >, std::vector<std::vector<S> >,
+           std::vector<std::vector<bool> >, std::vector<std::vector<bool> >, std::vector<std::vector<bool> > >
+amr2_level2(int sys, std::vector<std::vector<S> > cells, double dx, double cfl, double T, double tol, int order,
+            EulerMaterialParameters mp) {
+    const size_t ny = cells.size(), nx = cells[0].size();
+    Amr2Out o = amr2_run(sys, 2, (int)nx, (int)ny, pack2(cells), dx, cfl, T, tol, order, mp.getAdiabaticIndex());
+    std::vector<std::vector<S> > lv[3];
+    std::vector<std::vector<bool> > fb[3];
+    for (int l = 0; l < 3; l++) {
+        const size_t r = ny << l, c = nx << l;
+        lv[l].assign(r, std::vector<S>(c));
+        unpack2(o.c[l], lv[l]);
+        fb[l].assign(r, std::vector<bool>(c));
+        for (size_t i = 0; i < r; i++)
+            for (size_t j = 0; j < c; j++) fb[l][i][j] = o.f[l][i * c + j] != 0;
+    }
+    return std::make_tuple(lv[0], lv[1], lv[2], fb[0], fb[1], fb[2]);
+}
+
 }  // namespace cosmos_compat_detail
 
 #define COSMOS_COMPAT_AMR(PREFIX, STATE, SYS)                                                                   \
@@ -480,6 +535,19 @@ amr2(int sys, std::vector<std::vector<S> > cells, double dx, double cfl, double 
         solve2DLevel1AMR(std::vector<std::vector<STATE> > c, double dx, double cfl, double T, double tol,      \
                          int order, EulerMaterialParameters mp) {                                              \
             return cosmos_compat_detail::amr2(SYS, c, dx, cfl, T, tol, order, mp);                             \
+        }                                                                                                      \
+        static std::tuple<std::vector<STATE>, std::vector<STATE>, std::vector<STATE>, std::vector<bool>,       \
+                          std::vector<bool>, std::vector<bool> >                                               \
+        solveLevel2AMR(std::vector<STATE> c, double dx, double cfl, double T, double tol, int order,          \
+                       EulerMaterialParameters mp) {                                                           \
+            return cosmos_compat_detail::amr1_level2(SYS, c, dx, cfl, T, tol, order, mp);                      \
+        }                                                                                                      \
+        static std::tuple<std::vector<std::vector<STATE> >, std::vector<std::vector<STATE> >,                  \
+                          std::vector<std::vector<STATE> >, std::vector<std::vector<bool> >,                   \
+                          std::vector<std::vector<bool> >, std::vector<std::vector<bool> > >                   \
+        solve2DLevel2AMR(std::vector<std::vector<STATE> > c, double dx, double cfl, double T, double tol,      \
+                         int order, EulerMaterialParameters mp) {                                              \
+            return cosmos_compat_detail::amr2_level2(SYS, c, dx, cfl, T, tol, order, mp);                      \
         }                                                                                                      \
     };
 COSMOS_COMPAT_AMR(Euler, EulerStateVector, COSMOS_NEWTONIAN)

@@ -109,6 +109,25 @@ int main(int argc, char** argv) {
         for (auto& row : std::get<3>(r)) for (bool b : row) flags.push_back(b ? 1.0 : 0.0);
         dump(dir + "/amr_flags.bin", flags);
     }
+    // Level-2 AMR (AMR/RelativisticEulerAMR.cpp:604-929): the SR shock tube on 50 coarse cells, SLIC
+    {
+        int cellCount = 50;
+        double cellSpacing = 1.0 / cellCount;
+        std::vector<RelativisticEulerStateVector> initialCells(cellCount);
+        EulerMaterialParameters materialParameters(5.0 / 3.0);
+        for (int i = 0; i < cellCount; i++) {
+            if (i <= (0.5 * cellCount)) initialCells[i] = RelativisticEulerStateVector(10.0, 0.0, 0.0, 0.0, 13.3);
+            else initialCells[i] = RelativisticEulerStateVector(1.0, 0.0, 0.0, 0.0, 1e-6);
+        }
+        auto r = RelativisticEulerAMR::solveLevel2AMR(initialCells, cellSpacing, 0.8, 0.1, 20.0, 2, materialParameters);
+        std::vector<double> all = flat1(std::get<0>(r)), m = flat1(std::get<1>(r)), f = flat1(std::get<2>(r));
+        all.insert(all.end(), m.begin(), m.end());
+        all.insert(all.end(), f.begin(), f.end());
+        for (bool b : std::get<3>(r)) all.push_back(b ? 1.0 : 0.0);
+        for (bool b : std::get<4>(r)) all.push_back(b ? 1.0 : 0.0);
+        for (bool b : std::get<5>(r)) all.push_back(b ? 1.0 : 0.0);
+        dump(dir + "/amr2_sr.bin", all);
+    }
     std::printf("compat driver ok\n");
     return 0;
 }

@@ -123,3 +123,67 @@ def test_reference_named_amr_entry_points(cg, oracle):
     _, _, wcp, wfp, wcf, wff = oracle.amr_level1(1, s, 1.0 / 40, 0.9, 0.1, 2.0, 2, 5.0 / 3.0)
     assert bit_equal(cp.reshape(-1), wcp) and bit_equal(fp.reshape(-1), wfp)
     assert np.array_equal(cf, wcf.astype(bool)) and np.array_equal(ff, wff.astype(bool))
+
+
+def run_amr2(cg, system, s, T, tol, order, precision=0):
+    shape = s.shape[:-1]
+    a = cg.AMR(system, shape, 1.0 / shape[-1], cases.SYS_GAMMA[system], precision, levels=2)
+    try:
+        a.set_prim(s)
+        n, nf, t, status = a.solve(0.9, T, tol, order)
+        out = a.get()
+        runs = (a.mid_run, a.fine_run)
+    finally:
+        a.close()
+    return (n, nf, t, status, runs) + out
+
+
+def test_amr_level2_matches_reference_runs(cg):
+    """Level-2 drivers (three levels): the reference's own solveLevel2AMR / solve2DLevel2AMR runs."""
+    G = dict(np.load(os.path.join(HERE, "golden", "amr_golden.npz")))
+    keys = sorted(k[:-3] for k in G if k.startswith("amr2_") and k.endswith("_in") and k[5:-3].isdigit())
+    assert len(keys) == 8
+    for k in keys:
+        s = G[k + "_in"]
+        system, dims, T, order, tol, nsteps = G[k + "_args"]
+        n, nf, t, status, runs, cp, mp, fp, cf, mf, ff = run_amr2(cg, int(system), s, T, tol, int(order))
+        assert n == int(nsteps) and status == 0, k
+        for name, got in (("coarse", cp), ("mid", mp), ("fine", fp)):
+            assert bit_equal(got.reshape(-1), G[f"{k}_{name}"]), (k, name)
+        for name, got in (("cflags", cf), ("mflags", mf), ("fflags", ff)):
+            assert np.array_equal(got.reshape(-1), G[f"{k}_{name}"].astype(bool)), (k, name)
+
+
+@pytest.mark.parametrize("system", [0, 1])
+@pytest.mark.parametrize("shape,T,tol", [((37,), 0.1, 1.0), ((13, 11), 0.04, 1.0), ((9, 14), 0.04, 4.0)])
+@pytest.mark.parametrize("order", [1, 2])
+def test_amr_level2_matches_oracle(cg, oracle, system, shape, T, tol, order):
+    s = amr_state(shape, system, 51 + len(shape) + order)
+    n, nf, t, status, runs, cp, mp, fp, cf, mf, ff = run_amr2(cg, system, s, T, tol, order)
+    wn, counts, wcp, wmp, wfp, wcf, wmf, wff = oracle.amr_level2(system, s, 1.0 / shape[-1], 0.9, T, tol, order,
+                                                                 cases.SYS_GAMMA[system])
+    assert (n, nf, runs[0], runs[1]) == (wn, counts[0], counts[1], counts[2]) and t >= T
+    for got, want in ((cp, wcp), (mp, wmp), (fp, wfp)):
+        assert bit_equal(got.reshape(-1), want)
+    for got, want in ((cf, wcf), (mf, wmf), (ff, wff)):
+        assert np.array_equal(got.reshape(-1), want.astype(bool))
+
+
+@pytest.mark.parametrize("system", [0, 1])
+def test_amr_level2_fp32_stays_near_fp64(cg, system):
+    s = amr_state((24, 28), system, 78)
+    r64 = run_amr2(cg, system, s, 0.04, 1.0, 2, precision=0)
+    r32 = run_amr2(cg, system, s, 0.04, 1.0, 2, precision=1)
+    assert all(np.isfinite(x).all() for x in r32[5:8]) and r32[2] >= 0.04
+    rho64, rho32 = r64[5][..., 0], r32[5][..., 0]
+    assert np.abs(rho32 - rho64).sum() / np.abs(rho64).sum() < 2e-3
+
+
+def test_reference_named_level2_entry_points(cg, oracle):
+    s = amr_state((10, 12), 0, 19)
+    out = cg.EulerAMR.solve2DLevel2AMR(s, 1.0 / 12, 0.9, 0.03, 1.0, 2, cg.EulerMaterialParameters(1.4))
+    want = oracle.amr_level2(0, s, 1.0 / 12, 0.9, 0.03, 1.0, 2, 1.4)[2:]
+    for got, w in zip(out[:3], want[:3]):
+        assert bit_equal(got.reshape(-1), w)
+    for got, w in zip(out[3:], want[3:]):
+        assert np.array_equal(got.reshape(-1), w.astype(bool))

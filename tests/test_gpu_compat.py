@@ -67,3 +67,9 @@ def test_compat_driver_matches_oracle(cosmos_lib, oracle, tmp_path):
     assert bit_equal(load("amr_coarse.bin", (n * n * 5,)), cp)
     assert bit_equal(load("amr_fine.bin", (4 * n * n * 5,)), fp)
     assert bit_equal(load("amr_flags.bin", (5 * n * n,)), np.concatenate([cf, ff]).astype(np.float64))
+
+    m = 50
+    s = np.array([(10.0, 0, 0, 0, 13.3) if i <= 0.5 * m else (1.0, 0, 0, 0, 1e-6) for i in range(m)])
+    _, _, cp, mp, fp, cf, mf, ff = oracle.amr_level2(1, s, 1.0 / m, 0.8, 0.1, 20.0, 2, 5.0 / 3.0)
+    want = np.concatenate([cp, mp, fp, cf, mf, ff]).astype(np.float64)
+    assert bit_equal(load("amr2_sr.bin", want.shape), want)
