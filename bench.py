@@ -836,6 +836,24 @@ def run_amr(args):
     t32, (r32, run32), cp32, cf32 = measure(cg.FP32, steps, 1)
     ms32 = statistics.median(t32)
     cells32 = r32[0] * n * n + run32 * 4 * n * n
+
+    def measure_level2(precision):
+        """The Level-2 driver (three levels) on the same problem: one warm-up run, one timed run."""
+        a = cg.AMR(cg.NEWTONIAN, (n, n), 1.0 / n, 1.4, precision, ctx=ctx, levels=2)
+        a.set_prim(s0)
+        a.solve(AMR_CFL, AMR_T, tol, 2)
+        a.set_prim(s0)
+        flush.fill_(1)
+        r = []
+        ms2 = timed(lambda: r.append(a.solve(AMR_CFL, AMR_T, tol, 2)))
+        c2 = r[0][0] * n * n + a.mid_run * 4 * n * n + a.fine_run * 16 * n * n
+        out = {"value": c2 / (ms2 * 1e-3), "ms_per_run": ms2, "coarse_steps": r[0][0],
+               "intermediate_steps": a.mid_run, "fine_steps": a.fine_run, "cell_updates_per_run": c2}
+        a.close()
+        return out
+    level2 = {"fp64": measure_level2(cg.FP64), "fp32": measure_level2(cg.FP32),
+              "what": "EulerAMR::solve2DLevel2AMR on the same problem (coarse 512^2, intermediate 1024^2, fine "
+                      "2048^2); cell-updates count every level's steps taken"}
     # e2e: pinned host primitives -> device, one driver run, both levels and flags -> host
     host = torch.empty((n, n, 5), dtype=torch.float64, pin_memory=True)
     host.numpy()[...] = s0
@@ -872,6 +890,7 @@ def run_amr(args):
         "fp32": {"value": cells32 / (ms32 * 1e-3), "ms_per_step": ms32, "coarse_steps": r32[0], "fine_steps": run32,
                  "l1_rho_vs_fp64": float(np.abs(cp32[..., 0] - cp64[..., 0]).sum() / np.abs(cp64[..., 0]).sum()),
                  "coarse_flags_equal_fp64": float(np.mean(cf32 == cf64))},
+        "level2": level2,
         "e2e": {"value": cells / (e2e_ms * 1e-3), "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms, "what": "pinned host primitives -> device, one driver run, both levels' "
                                                "primitives and flags -> host"},
