@@ -111,6 +111,11 @@ public:
     double getBlackHoleXPosition() { return x; }
     double getBlackHoleYPosition() { return y; }
     double getBlackHoleZPosition() { return z; }
+    // BlackHoleEuler/BlackHoleSpacetime.cpp:372-386: Euclidean distance within M (1 + sqrt(1 - a^2))
+    bool inExcisionRegion(double X, double Y, double Z) const {
+        const double r = std::sqrt((((X - x) * (X - x)) + ((Y - y) * (Y - y))) + ((Z - z) * (Z - z)));
+        return r <= (m * (1.0 + std::sqrt(1.0 - (a * a))));
+    }
     void pack(double* o) const { o[0] = m; o[1] = a; o[2] = x; o[3] = y; o[4] = z; }
 private:
     double m, a, x, y, z;
