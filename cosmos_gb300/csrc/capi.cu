@@ -486,7 +486,9 @@ int cosmos_grid_run_begin(cosmos_grid* g, const cosmos_solve_opts* o) {
     if (!g || !o) return fail(COSMOS_EINVAL, "null grid or options");
     if (o->order != 1 && o->order != 2) return fail(COSMOS_EINVAL, "order must be 1 or 2");
     if (!(o->cfl > 0.0)) return fail(COSMOS_EINVAL, "cfl must be positive");
-    if (g->p.system == COSMOS_GR && o->subcycles < 1) return fail(COSMOS_EINVAL, "GR runs need subcycles >= 1");
+    // 0 subcycles: no source step, the flux sweeps alone (the reference's loops over
+    // subcyclingIterations run zero times, Solvers/BlackHoleEulerSecondOrderSolver.cpp:158-170)
+    if (g->p.system == COSMOS_GR && o->subcycles < 0) return fail(COSMOS_EINVAL, "GR runs need subcycles >= 0");
     CK(cudaSetDevice(g->ctx->device));
     cudaStream_t st = g->ctx->stream;
     const bool same = g->run_ready && g->run.order == o->order && g->run.bias == o->bias &&

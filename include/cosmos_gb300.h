@@ -80,7 +80,7 @@ typedef struct cosmos_solve_opts {
     double t_final;
     double bias;
     int limiter;
-    int subcycles;   /* GR only: RK source half-steps before and after the flux step */
+    int subcycles;   /* GR only: RK source half-steps before and after the flux step (0: none) */
     int max_steps;   /* < 0: run until t >= t_final; otherwise stop after max_steps steps */
 } cosmos_solve_opts;
 

@@ -45,6 +45,10 @@ for level in (1, 2):
     for fn in ("solve2DMildlyRelativisticShock", "solve2DStronglyRelativisticBlast", "solve2DPerturbedDensityTest"):
         SCENARIOS.append((f"RelativisticEulerAMRTests::{fn}", 8, 2, 1, 3.0, level))
 
+# the reference's own main.cpp runs the accretion tests with subcyclingIterations = 0 (no source step)
+SCENARIOS.append(("BlackHoleEulerTests::solve1DSphericalAccretionTest", 40, 2, 0, 0.0, 1))
+SCENARIOS.append(("BlackHoleEulerTests::solve2DSpinningSphericalAccretionTest", 10, 2, 0, 0.0, 1))
+
 # writer cases: (kind, system, dims, ny, nx); kind 0 plain, 1 Level-1 AMR, 2 Level-2 AMR
 WRITERS = [(0, 0, 1, 1, 23), (0, 1, 2, 7, 9), (0, 2, 1, 1, 31), (0, 2, 2, 9, 11), (1, 0, 1, 1, 29), (1, 0, 2, 6, 7),
            (1, 1, 2, 6, 7), (2, 0, 1, 1, 37), (2, 1, 1, 1, 37), (2, 0, 2, 7, 8), (2, 1, 2, 7, 8)]

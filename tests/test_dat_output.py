@@ -98,7 +98,7 @@ def test_scenario_problems_through_the_oracle_match_the_reference(golden, tool, 
     """Each scenario's problem data, solved by the oracle with the scenario's solver arguments and
     written by the writers, gives the reference's scenario files byte for byte."""
     cases = scenarios(golden)
-    assert len(cases) == 42
+    assert len(cases) == 44
     for key, name, n, order, sub, tol, level in cases:
         d = str(tmp_path / key)
         os.makedirs(d)
