@@ -36,7 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
-WORKLOAD = "config2: 2D Newtonian Euler SLIC MinBee, 4096x4096 on [0,1]^2, gamma 1.4, CFL 0.9, periodic, " \
+WORKLOAD = "2D Newtonian Euler SLIC MinBee, 4096x4096 on [0,1]^2, gamma 1.4, CFL 0.9, periodic, " \
            "four-quadrant Riemann data (seed 2)"
 METRIC = "cell-updates/s"
 
@@ -311,7 +311,7 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
-BATCH_WORKLOAD = "config5: 256 independent Newtonian Euler grids (1D and 2D), every side log-uniform in " \
+BATCH_WORKLOAD = "256 independent Newtonian Euler grids (1D and 2D), every side log-uniform in " \
                  "[128, 2048] cells (seed 5), seeded Riemann data, SLIC MinBee, CFL 0.9, transmissive, dx = 1/nx"
 
 
@@ -547,11 +547,11 @@ def run_batch_reference(args):
     print(json.dumps(line), flush=True)
 
 
-# ---------------------------------------------------------------- SR (config 3) and GR (config 4)
-SR_WORKLOAD = "config3: 2D special-relativistic Euler (gamma 5/3), SLIC MinBee, CFL 0.9, 2048x2048 on the periodic " \
+# ---------------------------------------------------------------- SR (2048^2 Kelvin-Helmholtz) and GR (1024^2 accretion)
+SR_WORKLOAD = "2D special-relativistic Euler (gamma 5/3), SLIC MinBee, CFL 0.9, 2048x2048 on the periodic " \
               "unit square, Kelvin-Helmholtz shear layers (vx = +-0.5 tanh profile, rho in {1, 2}, p = 1, " \
               "vy = 0.01 sin(4 pi x + phase), phase seed 3; Lorentz factor <= 1.16); 200 steps"
-GR_WORKLOAD = "config4: 2D black-hole Euler in Kerr-Schild Schwarzschild spacetime (M = 1), SLIC van Leer + " \
+GR_WORKLOAD = "2D black-hole Euler in Kerr-Schild Schwarzschild spacetime (M = 1), SLIC van Leer + " \
               "RK4 source (BlackHoleEulerForcingSolver, one subcycle), CFL 0.9, 1024x1024 on [-10, 10]^2 " \
               "(dx = 20/1024, hole at (10, 10) of the grid's coordinates), excision r <= 2M, rho = 1 with 1% " \
               "log-normal noise (seed 4), p = 0.01, transmissive; 100 steps"

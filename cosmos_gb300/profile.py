@@ -81,7 +81,7 @@ def main():
     elif a.kernel == "rk":
         for _ in range(a.launches):
             g.rk_source(dt, 0.0, 1)
-    else:  # the configuration's solve: MinBee (configs 2, 3); van Leer and the RK source (config 4)
+    else:  # the workload's solve: MinBee (Newtonian 4096^2, SR 2048^2); van Leer and the RK source (GR 1024^2)
         lim = cg.VANLEER if a.system == cg.GR else cg.MINBEE
         g.run_begin(2, 0.9, 1e30, 0.0, lim)
         if a.warm:

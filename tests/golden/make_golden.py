@@ -25,7 +25,7 @@ def main():
     rng = np.random.default_rng(20240611)
     out = {}
 
-    # config 1: Sod, SLIC van Leer, N=1000, CFL 0.9, t=0.25
+    # Sod shock tube: SLIC van Leer, N=1000, CFL 0.9, t=0.25
     p0 = cases.sod(1000)
     p, n = R.solve(0, p0, 2, 1.0 / 1000, 0.9, 0.25, 0.0, 1, 1.4)
     out["sod1000_final"] = p

@@ -24,8 +24,8 @@ def grid_from(cg, system, prim, dx, precision=0, bc=0, bh=None):
     return g
 
 
-def test_sod_config1_bit_exact(cg, golden):
-    """Config 1: Sod, SLIC van Leer, N=1000, CFL 0.9, t=0.25 (613 steps in the reference)."""
+def test_sod_1000_cells_bit_exact(cg, golden):
+    """Sod shock tube: SLIC van Leer, N=1000, CFL 0.9, t=0.25 (613 steps in the reference)."""
     g = grid_from(cg, 0, cases.sod(1000), 1.0 / 1000)
     r = g.solve(2, 0.9, 0.25, 0.0, 1)
     p = g.get_prim()
@@ -124,8 +124,8 @@ def test_gr_solve_golden(cg, golden):
 
 
 @pytest.mark.parametrize("sub", [0, 2])
-def test_gr_solve_vs_oracle_config4_shape(cg, oracle, sub):
-    """Config-4 geometry at reduced size: [-10,10]^2 as [0,20]^2 with the hole at (10,10), M=1,
+def test_gr_solve_vs_oracle_accretion_shape(cg, oracle, sub):
+    """The 1024^2 accretion geometry at reduced size: [-10,10]^2 as [0,20]^2 with the hole at (10,10), M=1,
     excision r <= 2M, rho = 1 + 1% log-normal noise, p = 0.01; two subcycles, or none (the flux
     sweeps alone, as the reference's own driver runs its accretion tests)."""
     n = 24
@@ -183,7 +183,7 @@ def test_amr_derefine_vs_oracle(cg, oracle, system, dims):
 
 
 def test_fp32_four_quadrant_error(cg, oracle):
-    """FP32 bulk path vs the FP64 oracle on config 2's problem at reduced size (128^2, 30 steps,
+    """FP32 bulk path vs the FP64 oracle on the 4096^2 four-quadrant problem at reduced size (128^2, 30 steps,
     MinBee, periodic): relative L1 density error and conservation drift stated here."""
     n = 128
     s = cases.four_quadrant(n, 2)

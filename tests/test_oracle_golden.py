@@ -23,7 +23,7 @@ def parse_sweep_key(k):
     return dict(zip(("d", "o", "l", "bc", "a"), map(int, m.groups())))
 
 
-def test_sod_config1(oracle, golden):
+def test_sod_1000_cells(oracle, golden):
     p, n, t, _ = oracle.solve(0, cases.sod(1000), 2, 1.0 / 1000, 0.9, 0.25, 0.0, 1, 1.4)
     assert n == int(golden["sod1000_steps"]) == 613
     assert bit_equal(p, golden["sod1000_final"])
