@@ -50,6 +50,43 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+class Ranks:
+    """The bookkeeping of a run launched one process per GPU (torchrun; RANK / WORLD_SIZE from the
+    environment): barriers around timed regions, the maximum of a time over ranks, and whole-job
+    throughput (units per rank x ranks / the slowest rank's time).  The ranks run independent
+    replicas; the process group carries only these scalars.  backend "nccl" with device "cuda" on
+    GPUs, "gloo" with "cpu" on hosts."""
+
+    def __init__(self, backend="nccl", device="cuda"):
+        self.rank, self.world, _ = dist_env()
+        self.device = device
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+            if not dist.is_initialized():
+                dist.init_process_group(backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+        if self.device == "cuda":
+            import torch
+            torch.cuda.synchronize()
+
+    def max(self, v):
+        if not self.dist:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def throughput(self, units_per_rank, ms):
+        """Whole-job units per second from this rank's time in ms (the slowest rank's time counts)."""
+        return units_per_rank * self.world / (self.max(ms) * 1e-3)
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -162,29 +199,14 @@ def run_ours(args):
     import cosmos_gb300 as cg
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    ranks = Ranks("nccl", "cuda")
     L = cg.load()
     ctx = cg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
     n = args.n
     s0 = four_quadrant(n, 2)
     cells = n * n
-
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(v):
-        if world == 1:
-            return v
-        import torch.distributed as dist
-        t = torch.tensor([v], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    barrier, max_over_ranks = ranks.barrier, ranks.max
 
     # ---------------- FP32 resident: value
     g = cg.Grid(cg.NEWTONIAN, (n, n), 1.0 / n, 1.4, cg.FP32, cg.BC_PERIODIC, ctx=ctx)
@@ -205,7 +227,7 @@ def run_ours(args):
     launches = L.cosmos_kernel_launches() - launches0
     ms = max_over_ranks(e0.elapsed_time(e1)) / args.steps
     r = g.run_end()
-    value = cells * world / (ms * 1e-3)
+    value = ranks.throughput(cells, ms)
 
     # ---------------- per-kernel durations for the roofline (individual launches, events between)
     dt_probe = 0.5 * 0.9 / n / 2.0
@@ -254,7 +276,7 @@ def run_ours(args):
         b.record(stream)
         b.synchronize()
     e2e_ms = max_over_ranks(a.elapsed_time(b)) / e2e_steps
-    e2e_value = cells * world / (e2e_ms * 1e-3)
+    e2e_value = ranks.throughput(cells, e2e_ms)
     ge.close()
 
     # ---------------- FP64 (reference-exact) on the same workload, and the FP32-vs-FP64 error
