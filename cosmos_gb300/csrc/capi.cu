@@ -98,6 +98,8 @@ bool valid_params(const cosmos_params* p, std::string& why) {
     if (p->nx < 2 || (p->dims == 2 && p->ny < 2)) { why = "need at least 2 cells per dimension (the reference's 2-cell ghost mirror reads c[1] and c[n-2])"; return false; }
     if (p->dims == 1 && p->ny != 1) { why = "1D grids have ny == 1"; return false; }
     if ((long long)p->nx * p->ny > (1ll << 31)) { why = "grid larger than 2^31 cells"; return false; }
+    // row-parallel kernels (X sweeps, source step, AMR passes) launch one block row per grid row
+    if (p->ny > 65535) { why = "at most 65535 rows (one launch row per grid row)"; return false; }
     if (p->precision != COSMOS_FP64 && p->precision != COSMOS_FP32) { why = "precision must be COSMOS_FP64 or COSMOS_FP32"; return false; }
     if (p->boundary != COSMOS_BC_TRANSMISSIVE && p->boundary != COSMOS_BC_PERIODIC) { why = "unknown boundary"; return false; }
     if (!(p->dx > 0.0)) { why = "dx must be positive"; return false; }

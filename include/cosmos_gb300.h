@@ -52,8 +52,9 @@ enum { COSMOS_SUPERBEE = 0, COSMOS_VANLEER = 1, COSMOS_MINBEE = 2 };
  * EulerMaterialParameters, BlackHoleSpacetime) arguments:
  *   gamma  -- EulerMaterialParameters adiabatic index (Euler/EulerMaterialParameters.cpp:3-21)
  *   bh_*   -- BlackHoleSpacetime(mass, spin, x, y, z) (BlackHoleEuler/BlackHoleSpacetime.cpp:3-52)
- * dims 1 uses ny = 1.  boundary: the reference only has transmissive ghost cells
- * (Solvers/EulerSolvers.cpp:3-85); periodic is an extension (Newtonian and SR only). */
+ * dims 1 uses ny = 1; 2D grids have at most 65535 rows and 2^31 cells.  boundary: the reference
+ * only has transmissive ghost cells (Solvers/EulerSolvers.cpp:3-85); periodic is an extension
+ * (Newtonian and SR only). */
 typedef struct cosmos_params {
     int system;
     int dims;
