@@ -117,39 +117,52 @@ template <class T> struct Newton {
 // (setConservedVariableVector), :138-220 / :227-309 (fluxes) and the densitised GR versions
 // BlackHoleEulerStateVector.cpp:30-103, :159-350, :359-430.  tol is 1e-8 everywhere except the
 // GR x-flux (BlackHoleEulerStateVector.cpp:205, 1e-10).  Results: rho, v, p, W, h.
-struct C2P { double rho, vx, vy, vz, p, W, h; };
-static C2P con2prim(double D, double Sx, double Sy, double Sz, double tau, double g, double tol) {
-    double q = ((tau + D) * (tau + D)) - (((Sx * Sx) + (Sy * Sy)) + (Sz * Sz));
-    double dc = D / std::sqrt(q);
-    double ec = (D + tau) / std::sqrt(q);
-    if (q < 1e-8) {
-        dc = D / std::sqrt(1e-8);
-        ec = (D + tau) / std::sqrt(1e-8);
+// Templated on the scalar: double for the restatement, Dual for the tangent-linear model (whose
+// comparisons act on values, so the iteration takes the FP64 run's path and the derivative
+// follows the iterates; the floors have derivative 0).
+template <class T> struct C2PT { T rho, vx, vy, vz, p, W, h; };
+template <class T>
+static C2PT<T> con2prim_t(T D, T Sx, T Sy, T Sz, T tau, double g, double tol) {
+    using std::sqrt;
+    using std::fabs;
+    T q = ((tau + D) * (tau + D)) - (((Sx * Sx) + (Sy * Sy)) + (Sz * Sz));
+    T dc = D / sqrt(q);
+    T ec = (D + tau) / sqrt(q);
+    if (q < T(1e-8)) {
+        dc = D / T(std::sqrt(1e-8));
+        ec = (D + tau) / T(std::sqrt(1e-8));
     }
-    double constant = -1.0 / (g * g);
-    double linear = (-2.0 * dc) * ((g - 1.0) / (g * g));
-    double quadratic = ((((g - 2.0) / g) * ((ec * ec) - 1.0)) + 1.0) - (((dc * dc) * ((g - 1.0) / g)) * ((g - 1.0) / g));
-    double quartic = (ec * ec) - 1.0;
-    double eta = (2.0 * dc) * ((g - 1.0) / g);
-    double x = 1.0;
+    const T constant = T(-1.0 / (g * g));
+    T linear = (T(-2.0) * dc) * T((g - 1.0) / (g * g));
+    T quadratic = (((T((g - 2.0) / g) * ((ec * ec) - T(1.0))) + T(1.0)) -
+                   (((dc * dc) * T((g - 1.0) / g)) * T((g - 1.0) / g)));
+    T quartic = (ec * ec) - T(1.0);
+    T eta = (T(2.0) * dc) * T((g - 1.0) / g);
+    T x = T(1.0);
     int it = 0;
     while (it < 1000) {
-        double f = ((((quartic * ((x * x) * x)) * (x - eta)) + (quadratic * (x * x))) + (linear * x)) + constant;
-        double fp = ((linear + ((2.0 * quadratic) * x)) + ((4.0 * quartic) * ((x * x) * x))) - (((3.0 * eta) * quartic) * (x * x));
-        double nx = x - (f / fp);
-        if (std::fabs(x - nx) < tol) it = 1000;
+        T f = ((((quartic * ((x * x) * x)) * (x - eta)) + (quadratic * (x * x))) + (linear * x)) + constant;
+        T fp = ((linear + ((T(2.0) * quadratic) * x)) + ((T(4.0) * quartic) * ((x * x) * x))) -
+               (((T(3.0) * eta) * quartic) * (x * x));
+        T nx = x - (f / fp);
+        if (fabs(x - nx) < T(tol)) it = 1000;
         else { it += 1; x = nx; }
     }
-    C2P r;
-    r.W = ((0.5 * ec) * x) * (1.0 + std::sqrt(1.0 + ((4.0 * ((g - 1.0) / g)) * ((1.0 - (dc * x)) / ((ec * ec) * (x * x))))));
-    r.h = 1.0 / (dc * x);
+    C2PT<T> r;
+    r.W = ((T(0.5) * ec) * x) *
+          (T(1.0) + sqrt(T(1.0) + ((T(4.0) * T((g - 1.0) / g)) * ((T(1.0) - (dc * x)) / ((ec * ec) * (x * x))))));
+    r.h = T(1.0) / (dc * x);
     r.rho = D / r.W;
-    double rhw = (r.rho * r.h) * (r.W * r.W);
+    T rhw = (r.rho * r.h) * (r.W * r.W);
     r.vx = Sx / rhw; r.vy = Sy / rhw; r.vz = Sz / rhw;
     r.p = (rhw - D) - tau;
-    if (r.rho < 1e-8) r.rho = 1e-8;
-    if (r.p < 1e-8) r.p = 1e-8;
+    if (r.rho < T(1e-8)) r.rho = T(1e-8);
+    if (r.p < T(1e-8)) r.p = T(1e-8);
     return r;
+}
+typedef C2PT<double> C2P;
+static C2P con2prim(double D, double Sx, double Sy, double Sz, double tau, double g, double tol) {
+    return con2prim_t<double>(D, Sx, Sy, Sz, tau, g, tol);
 }
 
 // RelativisticEuler/RelativisticEulerEquationOfState.cpp:3-8
@@ -161,30 +174,31 @@ static inline double sr_sound(double rho, double p, double g) {
     return std::sqrt(num / den);
 }
 
-struct SR {
+template <class T> struct SRT {
     double g;
     static constexpr bool coords = false;
     // RelativisticEuler/RelativisticEulerStateVector.cpp:116-136
-    void cons(const double* p, Pt, double* u) const {
-        double rho = p[0], vx = p[1], vy = p[2], vz = p[3], pr = p[4];
-        double v2 = ((vx * vx) + (vy * vy)) + (vz * vz);
-        double W = 1.0 / std::sqrt(1.0 - v2);
-        if (v2 > 1.0 - 1e-8) W = 1.0 / std::sqrt(1.0 - 1e-8);
-        double h = sr_enthalpy(rho, pr, g);
-        double rhw = (rho * h) * (W * W);
+    void cons(const T* p, Pt, T* u) const {
+        using std::sqrt;
+        T rho = p[0], vx = p[1], vy = p[2], vz = p[3], pr = p[4];
+        T v2 = ((vx * vx) + (vy * vy)) + (vz * vz);
+        T W = T(1.0) / sqrt(T(1.0) - v2);
+        if (v2 > T(1.0 - 1e-8)) W = T(1.0 / std::sqrt(1.0 - 1e-8));
+        T h = T(1.0) + ((pr / rho) * T(g / (g - 1.0)));  // sr_enthalpy
+        T rhw = (rho * h) * (W * W);
         u[0] = rho * W; u[1] = rhw * vx; u[2] = rhw * vy; u[3] = rhw * vz;
         u[4] = (rhw - pr) - (rho * W);
     }
     // RelativisticEuler/RelativisticEulerStateVector.cpp:30-101
-    void prim(const double* u, Pt, double* p) const {
-        C2P c = con2prim(u[0], u[1], u[2], u[3], u[4], g, 1e-8);
+    void prim(const T* u, Pt, T* p) const {
+        C2PT<T> c = con2prim_t<T>(u[0], u[1], u[2], u[3], u[4], g, 1e-8);
         p[0] = c.rho; p[1] = c.vx; p[2] = c.vy; p[3] = c.vz; p[4] = c.p;
     }
     // RelativisticEuler/RelativisticEulerStateVector.cpp:138-220 (x), :227-309 (y)
-    void flux(const double* u, int axis, Pt, double* f) const {
-        C2P c = con2prim(u[0], u[1], u[2], u[3], u[4], g, 1e-8);
-        double rhw = (c.rho * c.h) * (c.W * c.W);
-        double vn = axis == 0 ? c.vx : c.vy;
+    void flux(const T* u, int axis, Pt, T* f) const {
+        C2PT<T> c = con2prim_t<T>(u[0], u[1], u[2], u[3], u[4], g, 1e-8);
+        T rhw = (c.rho * c.h) * (c.W * c.W);
+        T vn = axis == 0 ? c.vx : c.vy;
         f[0] = (c.rho * c.W) * vn;
         if (axis == 0) {
             f[1] = (rhw * (c.vx * c.vx)) + c.p; f[2] = rhw * (c.vy * c.vx); f[3] = rhw * (c.vz * c.vx);
@@ -201,6 +215,7 @@ struct SR {
         return mx(std::fabs(p[1]), std::fabs(p[2])) + c;
     }
 };
+typedef SRT<double> SR;
 
 // ========================================================================= Kerr-Schild spacetime
 struct BH {
@@ -1354,13 +1369,13 @@ int orc_amr_level2(int sys, const double* prim, int ny, int nx, int dims, double
 // `nsteps` steps with the step sizes dts[] held fixed (the adjoint's convention), along the
 // initial-state direction dprim (primitive variables).  Runs the FP64 forward in dual numbers.
 // Strang splitting for 2D.  Returns L; *dL receives the directional derivative.
-double orc_tlm_newton(const double* prim0, const double* dprim, const double* target, int ny, int nx, int dims,
-                      double dx, const double* dts, int nsteps, double bias, int lim, double gamma, int bc,
-                      double* dL) {
+}  // extern "C"
+template <class Sys>
+static double tlm_run(const Sys& S, const double* prim0, const double* dprim, const double* target, int ny, int nx,
+                      int dims, double dx, const double* dts, int nsteps, double bias, int lim, int bc, double* dL) {
     size_t N = (size_t)(dims == 1 ? 1 : ny) * nx;
     std::vector<Dual> p(5 * N);
     for (size_t i = 0; i < 5 * N; i++) p[i] = Dual(prim0[i], dprim ? dprim[i] : 0.0);
-    Newton<Dual> S{gamma};
     for (int s = 0; s < nsteps; s++) {
         double dt = dts[s];
         if (dims == 1) sweep(S, p.data(), ny, nx, 1, 0, 2, dx, dt, bias, lim, bc, nullptr, nullptr);
@@ -1377,6 +1392,22 @@ double orc_tlm_newton(const double* prim0, const double* dprim, const double* ta
     }
     if (dL) *dL = L.d;
     return L.v;
+}
+extern "C" {
+
+double orc_tlm_newton(const double* prim0, const double* dprim, const double* target, int ny, int nx, int dims,
+                      double dx, const double* dts, int nsteps, double bias, int lim, double gamma, int bc,
+                      double* dL) {
+    return tlm_run(Newton<Dual>{gamma}, prim0, dprim, target, ny, nx, dims, dx, dts, nsteps, bias, lim, bc, dL);
+}
+
+// The same for the special-relativistic system (RelativisticEulerSecondOrderSolver's step,
+// Solvers/RelativisticEulerSecondOrderSolver.cpp:102-156): every primitive recovery runs its
+// Newton iteration on dual numbers, whose derivative part converges with the iterates to the
+// implicit-function derivative of the recovered primitives.
+double orc_tlm_sr(const double* prim0, const double* dprim, const double* target, int ny, int nx, int dims, double dx,
+                  const double* dts, int nsteps, double bias, int lim, double gamma, int bc, double* dL) {
+    return tlm_run(SRT<Dual>{gamma}, prim0, dprim, target, ny, nx, dims, dx, dts, nsteps, bias, lim, bc, dL);
 }
 
 }  // extern "C"

@@ -76,6 +76,8 @@ class Oracle:
         L.orc_amr_level2.restype = _i
         L.orc_tlm_newton.argtypes = [_p, _p, _p, _i, _i, _i, _d, _p, _i, _d, _i, _d, _i, _p]
         L.orc_tlm_newton.restype = _d
+        L.orc_tlm_sr.argtypes = [_p, _p, _p, _i, _i, _i, _d, _p, _i, _d, _i, _d, _i, _p]
+        L.orc_tlm_sr.restype = _d
         L.orc_set_threads.argtypes = [_i]
 
     def set_threads(self, n):
@@ -205,6 +207,18 @@ class Oracle:
         return n, [int(c) for c in counts], cp, mp, fp, cf, mf, ff
 
     # ---- tangent-linear of the Newtonian SLIC loss
+    def tlm_sr(self, prim0, dprim, target, dx, dts, bias, lim, gamma, bc=0):
+        """The SR tangent-linear model: (loss, directional derivative) like tlm_newton."""
+        p = np.ascontiguousarray(prim0, dtype=np.float64)
+        d = np.ascontiguousarray(dprim, dtype=np.float64)
+        t = np.ascontiguousarray(target, dtype=np.float64)
+        ds = np.ascontiguousarray(dts, dtype=np.float64)
+        ny, nx, dims = _shape(p)
+        out = _d(0.0)
+        L = self.L.orc_tlm_sr(_ptr(p), _ptr(d), _ptr(t), ny, nx, dims, dx, _ptr(ds), len(ds), bias, lim, gamma, bc,
+                              ctypes.byref(out))
+        return L, out.value
+
     def tlm_newton(self, prim0, dprim, target, dx, dts, bias, lim, gamma, bc=0):
         p = np.ascontiguousarray(prim0, dtype=np.float64)
         d = np.ascontiguousarray(dprim, dtype=np.float64)

@@ -45,3 +45,62 @@ def test_oracle_tlm_matches_finite_differences(oracle, dims, lim, bc):
         Lm, _ = oracle.tlm_newton(p0 - h * d, np.zeros_like(d), target, dx, dts, 0.0, lim, 1.4, bc)
         fd = (Lp - Lm) / (2 * h)
         assert abs(fd - dL) <= 1e-6 * abs(dL) + 1e-10, (fd, dL)
+
+
+def sr_smooth_state(shape, seed):
+    """Smooth periodic special-relativistic data (|v| <= 0.36, rho and p near 1)."""
+    rng = np.random.default_rng(seed)
+    x = np.linspace(0, 1, shape[-1], endpoint=False)
+    ph = rng.uniform(0, 2 * np.pi, 4)
+    s = np.zeros(shape + (5,))
+    s[..., 0] = 1.0 + 0.2 * np.sin(2 * np.pi * x + ph[0])
+    s[..., 1] = 0.3 * np.sin(2 * np.pi * x + ph[1])
+    s[..., 4] = 1.0 + 0.1 * np.cos(2 * np.pi * x + ph[3])
+    if len(shape) == 2:
+        y = np.linspace(0, 1, shape[0], endpoint=False)[:, None]
+        s[..., 2] = 0.2 * np.cos(2 * np.pi * y + ph[2]) + 0.0 * x
+        s[..., 0] += 0.1 * np.sin(2 * np.pi * y)
+    return s
+
+
+def sr_forward_loss(oracle, p, target, dx, dts, lim, bc, g):
+    q = p.copy()
+    for dt in dts:
+        if q.ndim == 2:
+            q = oracle.sweep(1, q, 0, 2, dx, dt, 0.0, lim, g, bc)
+        else:
+            q = oracle.sweep(1, q, 0, 2, dx, 0.5 * dt, 0.0, lim, g, bc)
+            q = oracle.sweep(1, q, 1, 2, dx, dt, 0.0, lim, g, bc)
+            q = oracle.sweep(1, q, 0, 2, dx, 0.5 * dt, 0.0, lim, g, bc)
+    e = (q[..., 0] - target).ravel()
+    L = 0.0
+    for v in 0.5 * (e * e):
+        L = L + float(v)
+    return L
+
+
+@pytest.mark.parametrize("dims", [1, 2])
+@pytest.mark.parametrize("lim", [0, 1, 2])
+@pytest.mark.parametrize("bc", [0, 1])
+def test_oracle_sr_tlm_matches_finite_differences(oracle, dims, lim, bc):
+    """The special-relativistic tangent-linear model (dual numbers through every primitive
+    recovery's Newton iteration): value part = the plain SR forward, derivative = central
+    differences (h = 1e-7: larger steps leave the reference's 1e-5 slope clamp on rows where a field
+    is constant)."""
+    g = 5.0 / 3.0
+    shape = (24,) if dims == 1 else (10, 12)
+    p0 = sr_smooth_state(shape, 3 + lim)
+    target = sr_smooth_state(shape, 11)[..., 0]
+    dx = 1.0 / shape[-1]
+    dts = np.full(5, 0.15 * dx)
+    L_plain = sr_forward_loss(oracle, p0, target, dx, dts, lim, bc, g)
+    rng = np.random.default_rng(dims * 10 + lim + 100 * bc)
+    for _ in range(2):
+        d = rng.standard_normal(p0.shape)
+        L0, dL = oracle.tlm_sr(p0, d, target, dx, dts, 0.0, lim, g, bc)
+        assert L0 == L_plain
+        h = 1e-7
+        Lp, _ = oracle.tlm_sr(p0 + h * d, np.zeros_like(d), target, dx, dts, 0.0, lim, g, bc)
+        Lm, _ = oracle.tlm_sr(p0 - h * d, np.zeros_like(d), target, dx, dts, 0.0, lim, g, bc)
+        fd = (Lp - Lm) / (2 * h)
+        assert abs(fd - dL) <= 1e-6 * abs(dL) + 1e-10, (fd, dL)
