@@ -15,6 +15,9 @@ NEWTONIAN, SR, GR = 0, 1, 2
 FP64, FP32 = 0, 1
 BC_TRANSMISSIVE, BC_PERIODIC = 0, 1
 SUPERBEE, VANLEER, MINBEE = 0, 1, 2
+(STATE_CONS, STATE_PRIM, STATE_FLUX_X, STATE_FLUX_Y, STATE_SOUND, STATE_INTERNAL_ENERGY, STATE_TOTAL_ENERGY,
+ STATE_PRESSURE, STATE_ENTHALPY, STATE_SOURCE, STATE_EIGENVALUES, STATE_GRADIENT_RATIO, STATE_LIMITER,
+ STATE_SLOPE) = range(14)
 
 
 class Params(ctypes.Structure):
@@ -80,6 +83,8 @@ SIGNATURES = {
     "cosmos_amr_set_prim": (_i, [_p, _p, _sz]),
     "cosmos_amr_solve": (_i, [_p, _d, _d, _d, _i, ctypes.POINTER(AmrResult)]),
     "cosmos_amr_get": (_i, [_p, _p, _p, _p, _p]),
+    "cosmos_state_width": (_i, [_i, ctypes.POINTER(_sz), ctypes.POINTER(_sz)]),
+    "cosmos_state_eval": (_i, [_p, ctypes.POINTER(Params), _i, _sz, _p, _p, _d, _i, _p]),
     "cosmos_batch_create": (_i, [_p, _i, _p, _p, _p, _p, _d, _i, _i, ctypes.POINTER(_p)]),
     "cosmos_batch_destroy": (_i, [_p]),
     "cosmos_batch_size": (_i, [_p, ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_longlong)]),

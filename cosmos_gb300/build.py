@@ -39,6 +39,7 @@ UNITS = {
     "noalloc.cu": [],
     "capi_adjoint.cu": [],
     "capi_amr.cu": [],
+    "capi_state.cu": [],
 }
 
 

@@ -509,6 +509,105 @@ cudaError_t launch_amr_any(const unsigned char* flags, size_t n, unsigned long l
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ state-level functions
+// The reference's per-state functions (state vectors, equations of state, slope limiters, the
+// black-hole eigenvalues) for n independent items, one thread per item, with the same arithmetic
+// as the sweeps.  Item k reads in_stride doubles at in + k in_stride (and, for the black-hole
+// system, its coordinates at xyz + 3k) and writes out_stride doubles at out + k out_stride.
+template <class Sys>
+CG_D void state_vector_op(const Sys& S, int op, const double* v, Pt q, double* o) {
+    if (op == kStateCons) S.cons(v, q, o);
+    else if (op == kStatePrim) S.prim(v, q, o);
+    else S.flux(v, op == kStateFluxX ? 0 : 1, q, o);
+}
+
+// BlackHoleEuler/BlackHoleEulerEigenvalues.cpp:3-96: material, fast and slow acoustic eigenvalues
+// along x, y, z (the terms whose largest value is GRExact::sound_speed).
+CG_D void gr_eigenvalues(const GRExact& S, const double* p, Pt q, double* o) {
+    double al, be[3];
+    S.bh.lapse_shift(q.x, q.y, q.z, al, be);
+    double gm[9], gs[9];
+    S.bh.gamma(q.x, q.y, q.z, gm);
+    inverse3(gm, gs);
+    const double cs = sr_sound(p[0], p[4], S.g);
+    const double v[3] = {p[1], p[2], p[3]};
+    double v2 = 0.0;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) v2 = v2 + ((gm[3 * i + j] * v[i]) * v[j]);
+    for (int i = 0; i < 3; i++) {
+        const double rt = sqrt((1.0 - v2) * ((gs[3 * i + i] * (1.0 - (v2 * (cs * cs)))) - ((v[i] * v[i]) * (1.0 - (cs * cs)))));
+        const double pre = al / (1.0 - (v2 * (cs * cs)));
+        o[i] = (al * v[i]) - be[i];
+        o[3 + i] = (pre * ((v[i] * (1.0 - (cs * cs))) + (cs * rt))) - be[i];
+        o[6 + i] = (pre * ((v[i] * (1.0 - (cs * cs))) - (cs * rt))) - be[i];
+    }
+}
+
+__global__ void state_eval_kernel(StateEvalArgs a, NewtonExact<double> nw, SRExact sr, GRExact gr) {
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < a.n; k += (size_t)gridDim.x * blockDim.x) {
+        const double* v = a.in + a.in_stride * k;
+        double* o = a.out + a.out_stride * k;
+        const Pt q = a.xyz ? Pt{a.xyz[3 * k], a.xyz[3 * k + 1], a.xyz[3 * k + 2]} : Pt{0.0, 0.0, 0.0};
+        const double g = a.gamma;
+        switch (a.op) {
+            case kStateCons:
+            case kStatePrim:
+            case kStateFluxX:
+            case kStateFluxY:
+                if (a.system == 0) state_vector_op(nw, a.op, v, q, o);
+                else if (a.system == 1) state_vector_op(sr, a.op, v, q, o);
+                else state_vector_op(gr, a.op, v, q, o);
+                break;
+            case kStateSound:  // Euler/EulerEquationOfState.cpp:17-22; SR :10-18; black hole :519-549
+                if (a.system == 0) o[0] = sqrt((g * v[4]) / v[0]);
+                else if (a.system == 1) o[0] = sr_sound(v[0], v[4], g);
+                else o[0] = gr.sound_speed(v, q);
+                break;
+            case kStateInternalEnergy:  // Euler/EulerEquationOfState.cpp:3-8
+                o[0] = v[4] / ((g - 1.0) * v[0]);
+                break;
+            case kStateTotalEnergy: {  // Euler/EulerStateVector.cpp:129-134 (the conserved energy)
+                double u[5];
+                nw.cons(v, q, u);
+                o[0] = u[4];
+                break;
+            }
+            case kStatePressure:  // Euler/EulerEquationOfState.cpp:10-15 from (rho, ., ., ., e)
+                o[0] = (v[4] * (g - 1.0)) * v[0];
+                break;
+            case kStateEnthalpy:  // RelativisticEuler/RelativisticEulerEquationOfState.cpp:3-8
+                o[0] = sr_enthalpy(v[0], v[4], g);
+                break;
+            case kStateSource:  // BlackHoleEuler/BlackHoleEulerStateVector.cpp:359-510
+                gr.source(v, q, o);
+                break;
+            case kStateEigenvalues:
+                gr_eigenvalues(gr, v, q, o);
+                break;
+            case kStateGradientRatio:  // Solvers/SlopeLimiters.cpp:3-6
+                o[0] = gradient_ratio(v[0], a.bias);
+                break;
+            case kStateLimiter:  // Solvers/SlopeLimiters.cpp:8-69
+                o[0] = limiter_exact(v[0], a.bias, a.lim);
+                break;
+            case kStateSlope:  // Solvers/SlopeLimiters.cpp:71-101 on three conserved vectors
+                slope_exact(v, v + 5, v + 10, a.bias, a.lim, o);
+                break;
+            default:
+                break;
+        }
+    }
+}
+
+cudaError_t launch_state_eval(const SweepArgs& s, const StateEvalArgs& a) {
+    size_t b = (a.n + 127) / 128;
+    if (b > 152 * 8) b = 152 * 8;
+    state_eval_kernel<<<(int)(b ? b : 1), 128, 0, s.stream>>>(a, NewtonExact<double>{s.gamma, nullptr},
+                                                                SRExact{s.gamma, nullptr}, make_gr(s));
+    count_launch();
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ conservation sums
 // Sum of each stored field over the grid with Kahan-Babuska (Neumaier) compensation per thread,
 // then compensated double atomics are avoided: per-block partials go to a small buffer summed by

@@ -66,6 +66,26 @@ cudaError_t launch_amr_sync(const SweepArgs& a, int precision, void* coarse_stat
                             const unsigned char* coarse, const unsigned char* fine, bool strict = false);
 cudaError_t launch_amr_any(const unsigned char* flags, size_t n, unsigned long long* out, cudaStream_t st);
 
+// State-level functions (kernels_exact.cu), the operations of cosmos_state_eval: values equal to
+// the public COSMOS_STATE_* constants.
+enum StateOp : int {
+    kStateCons = 0, kStatePrim = 1, kStateFluxX = 2, kStateFluxY = 3, kStateSound = 4, kStateInternalEnergy = 5,
+    kStateTotalEnergy = 6, kStatePressure = 7, kStateEnthalpy = 8, kStateSource = 9, kStateEigenvalues = 10,
+    kStateGradientRatio = 11, kStateLimiter = 12, kStateSlope = 13
+};
+struct StateEvalArgs {
+    int system, op;
+    size_t n;
+    const double* in;   // device, in_stride doubles per item
+    const double* xyz;  // device, 3 per item (black-hole system) or null
+    double* out;        // device, out_stride doubles per item
+    size_t in_stride, out_stride;
+    double gamma, bias;
+    int lim;
+};
+// s supplies gamma, the hole and dx (the metric derivatives' spacing) and the stream
+cudaError_t launch_state_eval(const SweepArgs& s, const StateEvalArgs& a);
+
 // FP32 bulk path (conserved SoA storage, float)
 cudaError_t launch_sweep_fast(const SweepArgs& a);
 cudaError_t launch_wavespeed_fast(const SweepArgs& a, unsigned long long* slot);

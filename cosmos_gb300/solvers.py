@@ -576,3 +576,27 @@ def _amr_family(system, name):
 
 EulerAMR = _amr_family(NEWTONIAN, "Euler")
 RelativisticEulerAMR = _amr_family(SR, "RelativisticEuler")
+
+
+def state_eval(op, items, system=NEWTONIAN, gamma=1.4, xyz=None, black_hole=None, dx=0.0, bias=0.0, limiter=1,
+               ctx=None):
+    """The reference's state-level functions for an array of items on the device (cosmos_state_eval):
+    op is a COSMOS_STATE_* code (cosmos_gb300._lib.STATE_*), items an array whose last axis holds
+    the op's input width (5 for states, 1 for ratios, 15 for slope triples); xyz (..., 3) holds the
+    black-hole items' coordinates.  Returns an array of the op's output width."""
+    ctx = ctx or default_context()
+    wi, wo = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    check(load().cosmos_state_width(int(op), ctypes.byref(wi), ctypes.byref(wo)))
+    a = np.ascontiguousarray(items, dtype=np.float64).reshape(-1, wi.value)
+    n = a.shape[0]
+    p = Params()
+    load().cosmos_params_default(ctypes.byref(p))
+    p.system, p.gamma, p.dx = int(system), float(gamma), float(dx)
+    if black_hole is not None:
+        p.bh_mass, p.bh_spin = black_hole.mass, black_hole.spin
+        p.bh_x, p.bh_y, p.bh_z = black_hole.x, black_hole.y, black_hole.z
+    q = None if xyz is None else np.ascontiguousarray(xyz, dtype=np.float64).reshape(n, 3)
+    out = np.empty((n, wo.value))
+    check(load().cosmos_state_eval(ctx.h, ctypes.byref(p), int(op), n, a.ctypes.data,
+                                   None if q is None else q.ctypes.data, float(bias), int(limiter), out.ctypes.data))
+    return out

@@ -254,6 +254,37 @@ int cosmos_amr_get(cosmos_amr* a, double* coarse_prim, double* fine_prim, unsign
 /* One level's cells and flags: level 0 coarse, 1 the next finer, 2 the finest of a Level-2 driver. */
 int cosmos_amr_get_level(cosmos_amr* a, int level, double* prim, unsigned char* flags);
 
+/* ---- state-level functions: the reference's per-state functions for arrays of n states, evaluated
+ * on the device with the sweeps' arithmetic (FP64, bit-identical to the reference).  p supplies the
+ * system, gamma and, for the black-hole system, the hole and dx (the spacing of the source term's
+ * metric derivatives).  in holds in_width doubles per item, out receives out_width doubles per item
+ * (cosmos_state_width); black-hole items take their coordinates from xyz (3 doubles per item).
+ *   COSMOS_STATE_CONS       prim -> conserved: StateVector::computeConservedVariableVector
+ *                           (Euler/EulerStateVector.cpp:55-66; SR and black-hole twins)
+ *   COSMOS_STATE_PRIM       conserved -> prim: setConservedVariableVector (:30-40; SR :30-101)
+ *   COSMOS_STATE_FLUX_X/_Y  conserved -> flux: static computeX/YFluxVector (:68-117; SR :138-309)
+ *   COSMOS_STATE_SOUND      prim -> sound speed (1): computeSoundSpeed / EquationOfState::computeSoundSpeed
+ *                           (the black-hole one is the largest signed eigenvalue, BlackHoleEulerStateVector.cpp:519-549)
+ *   COSMOS_STATE_INTERNAL_ENERGY, _TOTAL_ENERGY   Newtonian prim -> e, E (Euler/EulerEquationOfState.cpp:3-8,
+ *                           Euler/EulerStateVector.cpp:129-134)
+ *   COSMOS_STATE_PRESSURE   Newtonian (rho, -, -, -, e) -> p (Euler/EulerEquationOfState.cpp:10-15)
+ *   COSMOS_STATE_ENTHALPY   SR/black-hole prim -> h (RelativisticEuler/RelativisticEulerEquationOfState.cpp:3-8)
+ *   COSMOS_STATE_SOURCE     black-hole conserved -> source term: computeSourceTermVector (:359-510)
+ *   COSMOS_STATE_EIGENVALUES  black-hole prim -> 9 values: material, fast and slow acoustic eigenvalues
+ *                           along x, y, z (BlackHoleEuler/BlackHoleEulerEigenvalues.cpp:3-96)
+ *   COSMOS_STATE_GRADIENT_RATIO, _LIMITER   r -> SlopeLimiters::computeGradientRatio / computeSlopeLimiter
+ *                           (Solvers/SlopeLimiters.cpp:3-69; bias and limiter as given)
+ *   COSMOS_STATE_SLOPE      three conserved vectors (left, middle, right: 15 doubles) -> computeSlopeVector (:71-101) */
+enum {
+    COSMOS_STATE_CONS = 0, COSMOS_STATE_PRIM = 1, COSMOS_STATE_FLUX_X = 2, COSMOS_STATE_FLUX_Y = 3,
+    COSMOS_STATE_SOUND = 4, COSMOS_STATE_INTERNAL_ENERGY = 5, COSMOS_STATE_TOTAL_ENERGY = 6, COSMOS_STATE_PRESSURE = 7,
+    COSMOS_STATE_ENTHALPY = 8, COSMOS_STATE_SOURCE = 9, COSMOS_STATE_EIGENVALUES = 10, COSMOS_STATE_GRADIENT_RATIO = 11,
+    COSMOS_STATE_LIMITER = 12, COSMOS_STATE_SLOPE = 13
+};
+int cosmos_state_width(int op, size_t* in_width, size_t* out_width);
+int cosmos_state_eval(cosmos_ctx* ctx, const cosmos_params* p, int op, size_t n, const double* in, const double* xyz,
+                      double bias, int limiter, double* out);
+
 /* Allocation-free conservation sums.  No counterpart in the reference: it exists for callers that
  * cannot allocate device memory where they need the sums -- code recorded into a CUDA graph
  * (allocation is not allowed during stream capture), host callbacks or foreign runtimes that own

@@ -121,9 +121,34 @@ private:
     double m, a, x, y, z;
 };
 
+// ----------------------------------------------------------------------------- state-level functions
+// One state (or three, for slopes) through cosmos_state_eval: the device's reference-exact kernels.
+namespace cosmos_compat_detail {
+inline std::vector<double> state_op(int sys, int op, const std::vector<double>& in, double gamma,
+                                    const double* xyz = nullptr, const BlackHoleSpacetime* bh = nullptr,
+                                    double dx = 0.0, double bias = 0.0, int lim = 1) {
+    cosmos_params p;
+    cosmos_params_default(&p);
+    p.system = sys;
+    p.gamma = gamma;
+    p.dx = dx;
+    if (bh) {
+        double b[5];
+        bh->pack(b);
+        p.bh_mass = b[0]; p.bh_spin = b[1]; p.bh_x = b[2]; p.bh_y = b[3]; p.bh_z = b[4];
+    }
+    size_t wi = 0, wo = 0;
+    check(cosmos_state_width(op, &wi, &wo));
+    std::vector<double> out(wo);
+    check(cosmos_state_eval(ctx(), &p, op, 1, in.data(), xyz, bias, lim, out.data()));
+    return out;
+}
+}  // namespace cosmos_compat_detail
+
 // ----------------------------------------------------------------------------- state vectors
-// Primitive storage and accessors as in Euler/EulerStateVector.hpp:8-48 (and the SR/GR twins).
-#define COSMOS_COMPAT_STATE(NAME)                                                                          \
+// Primitive storage and accessors as in Euler/EulerStateVector.hpp:8-48 (and the SR/GR twins); the
+// physics methods (conserved variables, fluxes, sound speed, ...) evaluate on the GPU.
+#define COSMOS_COMPAT_STATE(NAME, METHODS)                                                                 \
     class NAME {                                                                                           \
     public:                                                                                                \
         NAME() : density(1.0), xVelocity(0.0), yVelocity(0.0), zVelocity(0.0), pressure(1.0) {}          \
@@ -145,13 +170,209 @@ private:
         double getYVelocity() { return yVelocity; }                                                        \
         double getZVelocity() { return zVelocity; }                                                        \
         double getPressure() { return pressure; }                                                          \
+        METHODS                                                                                            \
     private:                                                                                               \
         double density, xVelocity, yVelocity, zVelocity, pressure;                                         \
     };
-COSMOS_COMPAT_STATE(EulerStateVector)
-COSMOS_COMPAT_STATE(RelativisticEulerStateVector)
-COSMOS_COMPAT_STATE(BlackHoleEulerStateVector)
+
+// Newtonian and SR: Euler/EulerStateVector.hpp:14-28, RelativisticEuler/RelativisticEulerStateVector.hpp:14-26
+// (the member flux methods take the flux of the state's own conserved vector, as the reference's do).
+#define COSMOS_COMPAT_FLAT_METHODS(SYS)                                                                    \
+    std::vector<double> computeConservedVariableVector(EulerMaterialParameters mp) {                       \
+        return cosmos_compat_detail::state_op(SYS, COSMOS_STATE_CONS, computePrimitiveVariableVector(),    \
+                                              mp.getAdiabaticIndex());                                     \
+    }                                                                                                      \
+    void setConservedVariableVector(std::vector<double> u, EulerMaterialParameters mp) {                   \
+        setPrimitiveVariableVector(cosmos_compat_detail::state_op(SYS, COSMOS_STATE_PRIM, u, mp.getAdiabaticIndex())); \
+    }                                                                                                      \
+    static std::vector<double> computeXFluxVector(std::vector<double> u, EulerMaterialParameters mp) {     \
+        return cosmos_compat_detail::state_op(SYS, COSMOS_STATE_FLUX_X, u, mp.getAdiabaticIndex());        \
+    }                                                                                                      \
+    std::vector<double> computeXFluxVector(EulerMaterialParameters mp) {                                   \
+        return computeXFluxVector(computeConservedVariableVector(mp), mp);                                 \
+    }                                                                                                      \
+    static std::vector<double> computeYFluxVector(std::vector<double> u, EulerMaterialParameters mp) {     \
+        return cosmos_compat_detail::state_op(SYS, COSMOS_STATE_FLUX_Y, u, mp.getAdiabaticIndex());        \
+    }                                                                                                      \
+    std::vector<double> computeYFluxVector(EulerMaterialParameters mp) {                                   \
+        return computeYFluxVector(computeConservedVariableVector(mp), mp);                                 \
+    }                                                                                                      \
+    double computeSoundSpeed(EulerMaterialParameters mp) {                                                 \
+        return cosmos_compat_detail::state_op(SYS, COSMOS_STATE_SOUND, computePrimitiveVariableVector(),   \
+                                              mp.getAdiabaticIndex())[0];                                  \
+    }
+#define COSMOS_COMPAT_EULER_METHODS                                                                        \
+    COSMOS_COMPAT_FLAT_METHODS(COSMOS_NEWTONIAN)                                                           \
+    double computeSpecificInternalEnergy(EulerMaterialParameters mp) {                                     \
+        return cosmos_compat_detail::state_op(COSMOS_NEWTONIAN, COSMOS_STATE_INTERNAL_ENERGY,              \
+                                              computePrimitiveVariableVector(), mp.getAdiabaticIndex())[0]; \
+    }                                                                                                      \
+    double computeTotalEnergy(EulerMaterialParameters mp) {                                                \
+        return cosmos_compat_detail::state_op(COSMOS_NEWTONIAN, COSMOS_STATE_TOTAL_ENERGY,                 \
+                                              computePrimitiveVariableVector(), mp.getAdiabaticIndex())[0]; \
+    }
+// Black hole: BlackHoleEuler/BlackHoleEulerStateVector.hpp:14-37, functions of the coordinates.
+#define COSMOS_COMPAT_BH_METHODS                                                                           \
+    std::vector<double> computeConservedVariableVector(double x, double y, double z, EulerMaterialParameters mp, \
+                                                       BlackHoleSpacetime bh) {                            \
+        const double q[3] = {x, y, z};                                                                     \
+        return cosmos_compat_detail::state_op(COSMOS_GR, COSMOS_STATE_CONS, computePrimitiveVariableVector(), \
+                                              mp.getAdiabaticIndex(), q, &bh);                             \
+    }                                                                                                      \
+    void setConservedVariableVector(std::vector<double> u, double x, double y, double z, EulerMaterialParameters mp, \
+                                    BlackHoleSpacetime bh) {                                               \
+        const double q[3] = {x, y, z};                                                                     \
+        setPrimitiveVariableVector(cosmos_compat_detail::state_op(COSMOS_GR, COSMOS_STATE_PRIM, u,         \
+                                                                  mp.getAdiabaticIndex(), q, &bh));        \
+    }                                                                                                      \
+    static std::vector<double> computeXFluxVector(std::vector<double> u, double x, double y, double z,     \
+                                                  EulerMaterialParameters mp, BlackHoleSpacetime bh) {     \
+        const double q[3] = {x, y, z};                                                                     \
+        return cosmos_compat_detail::state_op(COSMOS_GR, COSMOS_STATE_FLUX_X, u, mp.getAdiabaticIndex(), q, &bh); \
+    }                                                                                                      \
+    std::vector<double> computeXFluxVector(double x, double y, double z, EulerMaterialParameters mp,       \
+                                           BlackHoleSpacetime bh) {                                        \
+        return computeXFluxVector(computeConservedVariableVector(x, y, z, mp, bh), x, y, z, mp, bh);       \
+    }                                                                                                      \
+    static std::vector<double> computeYFluxVector(std::vector<double> u, double x, double y, double z,     \
+                                                  EulerMaterialParameters mp, BlackHoleSpacetime bh) {     \
+        const double q[3] = {x, y, z};                                                                     \
+        return cosmos_compat_detail::state_op(COSMOS_GR, COSMOS_STATE_FLUX_Y, u, mp.getAdiabaticIndex(), q, &bh); \
+    }                                                                                                      \
+    std::vector<double> computeYFluxVector(double x, double y, double z, EulerMaterialParameters mp,       \
+                                           BlackHoleSpacetime bh) {                                        \
+        return computeYFluxVector(computeConservedVariableVector(x, y, z, mp, bh), x, y, z, mp, bh);       \
+    }                                                                                                      \
+    static std::vector<double> computeSourceTermVector(std::vector<double> u, double x, double y, double z, \
+                                                       double h, EulerMaterialParameters mp, BlackHoleSpacetime bh) { \
+        const double q[3] = {x, y, z};                                                                     \
+        return cosmos_compat_detail::state_op(COSMOS_GR, COSMOS_STATE_SOURCE, u, mp.getAdiabaticIndex(), q, &bh, h); \
+    }                                                                                                      \
+    std::vector<double> computeSourceTermVector(double x, double y, double z, double h, EulerMaterialParameters mp, \
+                                                BlackHoleSpacetime bh) {                                   \
+        return computeSourceTermVector(computeConservedVariableVector(x, y, z, mp, bh), x, y, z, h, mp, bh); \
+    }                                                                                                      \
+    double computeSoundSpeed(double x, double y, double z, EulerMaterialParameters mp, BlackHoleSpacetime bh) { \
+        const double q[3] = {x, y, z};                                                                     \
+        return cosmos_compat_detail::state_op(COSMOS_GR, COSMOS_STATE_SOUND, computePrimitiveVariableVector(), \
+                                              mp.getAdiabaticIndex(), q, &bh)[0];                          \
+    }
+
+COSMOS_COMPAT_STATE(EulerStateVector, COSMOS_COMPAT_EULER_METHODS)
+COSMOS_COMPAT_STATE(RelativisticEulerStateVector, COSMOS_COMPAT_FLAT_METHODS(COSMOS_SR))
+COSMOS_COMPAT_STATE(BlackHoleEulerStateVector, COSMOS_COMPAT_BH_METHODS)
 #undef COSMOS_COMPAT_STATE
+#undef COSMOS_COMPAT_FLAT_METHODS
+#undef COSMOS_COMPAT_EULER_METHODS
+#undef COSMOS_COMPAT_BH_METHODS
+
+// ----------------------------------------------------------------------------- equations of state
+class EulerEquationOfState {  // Euler/EulerEquationOfState.hpp
+public:
+    static double computeSpecificInternalEnergy(double rho, double p, EulerMaterialParameters mp) {
+        return cosmos_compat_detail::state_op(COSMOS_NEWTONIAN, COSMOS_STATE_INTERNAL_ENERGY, {rho, 0.0, 0.0, 0.0, p},
+                                              mp.getAdiabaticIndex())[0];
+    }
+    static double computePressure(double rho, double e, EulerMaterialParameters mp) {
+        return cosmos_compat_detail::state_op(COSMOS_NEWTONIAN, COSMOS_STATE_PRESSURE, {rho, 0.0, 0.0, 0.0, e},
+                                              mp.getAdiabaticIndex())[0];
+    }
+    static double computeSoundSpeed(double rho, double p, EulerMaterialParameters mp) {
+        return cosmos_compat_detail::state_op(COSMOS_NEWTONIAN, COSMOS_STATE_SOUND, {rho, 0.0, 0.0, 0.0, p},
+                                              mp.getAdiabaticIndex())[0];
+    }
+};
+
+class RelativisticEulerEquationOfState {  // RelativisticEuler/RelativisticEulerEquationOfState.hpp
+public:
+    static double computeSpecificEnthalpy(double rho, double p, EulerMaterialParameters mp) {
+        return cosmos_compat_detail::state_op(COSMOS_SR, COSMOS_STATE_ENTHALPY, {rho, 0.0, 0.0, 0.0, p},
+                                              mp.getAdiabaticIndex())[0];
+    }
+    static double computeSoundSpeed(double rho, double p, EulerMaterialParameters mp) {
+        return cosmos_compat_detail::state_op(COSMOS_SR, COSMOS_STATE_SOUND, {rho, 0.0, 0.0, 0.0, p},
+                                              mp.getAdiabaticIndex())[0];
+    }
+};
+
+// ----------------------------------------------------------------------------- slope limiters
+class SlopeLimiters {  // Solvers/SlopeLimiters.hpp (0 SuperBee, 1 van Leer, anything else MinBee)
+public:
+    static double computeGradientRatio(double r, double bias) {
+        return cosmos_compat_detail::state_op(COSMOS_NEWTONIAN, COSMOS_STATE_GRADIENT_RATIO, {r}, 1.4, nullptr, nullptr,
+                                              0.0, bias)[0];
+    }
+    static double computeSlopeLimiter(double r, double bias, int limiter) {
+        return cosmos_compat_detail::state_op(COSMOS_NEWTONIAN, COSMOS_STATE_LIMITER, {r}, 1.4, nullptr, nullptr, 0.0,
+                                              bias, limiter)[0];
+    }
+    static double computeSuperBeeSlopeLimiter(double r, double bias) { return computeSlopeLimiter(r, bias, 0); }
+    static double computeVanLeerSlopeLimiter(double r, double bias) { return computeSlopeLimiter(r, bias, 1); }
+    static double computeMinBeeSlopeLimiter(double r, double bias) { return computeSlopeLimiter(r, bias, 2); }
+    static std::vector<double> computeSlopeVector(std::vector<double> l, std::vector<double> m, std::vector<double> r,
+                                                  double bias, int limiter) {
+        std::vector<double> in(l);
+        in.insert(in.end(), m.begin(), m.end());
+        in.insert(in.end(), r.begin(), r.end());
+        return cosmos_compat_detail::state_op(COSMOS_NEWTONIAN, COSMOS_STATE_SLOPE, in, 1.4, nullptr, nullptr, 0.0, bias,
+                                              limiter);
+    }
+    static std::vector<double> computeSlopeVector(EulerStateVector l, EulerStateVector m, EulerStateVector r, double bias,
+                                                  int limiter, EulerMaterialParameters mp) {
+        return computeSlopeVector(l.computeConservedVariableVector(mp), m.computeConservedVariableVector(mp),
+                                  r.computeConservedVariableVector(mp), bias, limiter);
+    }
+    static std::vector<double> computeSlopeVector(RelativisticEulerStateVector l, RelativisticEulerStateVector m,
+                                                  RelativisticEulerStateVector r, double bias, int limiter,
+                                                  EulerMaterialParameters mp) {
+        return computeSlopeVector(l.computeConservedVariableVector(mp), m.computeConservedVariableVector(mp),
+                                  r.computeConservedVariableVector(mp), bias, limiter);
+    }
+    // Solvers/SlopeLimiters.cpp:103-147: neighbours evaluated one spacing away along the axis
+    static std::vector<double> computeSlopeVectorX(BlackHoleEulerStateVector l, BlackHoleEulerStateVector m,
+                                                   BlackHoleEulerStateVector r, double dx, double bias, int limiter,
+                                                   double x, double y, double z, EulerMaterialParameters mp,
+                                                   BlackHoleSpacetime bh) {
+        return computeSlopeVector(l.computeConservedVariableVector(x - dx, y, z, mp, bh),
+                                  m.computeConservedVariableVector(x, y, z, mp, bh),
+                                  r.computeConservedVariableVector(x + dx, y, z, mp, bh), bias, limiter);
+    }
+    static std::vector<double> computeSlopeVectorY(BlackHoleEulerStateVector t, BlackHoleEulerStateVector m,
+                                                   BlackHoleEulerStateVector b, double dx, double bias, int limiter,
+                                                   double x, double y, double z, EulerMaterialParameters mp,
+                                                   BlackHoleSpacetime bh) {
+        return computeSlopeVector(t.computeConservedVariableVector(x, y - dx, z, mp, bh),
+                                  m.computeConservedVariableVector(x, y, z, mp, bh),
+                                  b.computeConservedVariableVector(x, y + dx, z, mp, bh), bias, limiter);
+    }
+};
+
+// ----------------------------------------------------------------------------- black-hole eigenvalues
+class BlackHoleEulerEigenvalues {  // BlackHoleEuler/BlackHoleEulerEigenvalues.hpp
+public:
+    static std::vector<double> computeMaterialWaveEigenvalues(double x, double y, double z, double vx, double vy, double vz,
+                                                              EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        return part(x, y, z, 1.0, 1.0, vx, vy, vz, mp, bh, 0);
+    }
+    static std::vector<double> computeFastAcousticWaveEigenvalues(double x, double y, double z, double rho, double p,
+                                                                  double vx, double vy, double vz,
+                                                                  EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        return part(x, y, z, rho, p, vx, vy, vz, mp, bh, 1);
+    }
+    static std::vector<double> computeSlowAcousticWaveEigenvalues(double x, double y, double z, double rho, double p,
+                                                                  double vx, double vy, double vz,
+                                                                  EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        return part(x, y, z, rho, p, vx, vy, vz, mp, bh, 2);
+    }
+private:
+    static std::vector<double> part(double x, double y, double z, double rho, double p, double vx, double vy, double vz,
+                                    EulerMaterialParameters mp, BlackHoleSpacetime bh, int which) {
+        const double q[3] = {x, y, z};
+        std::vector<double> all = cosmos_compat_detail::state_op(COSMOS_GR, COSMOS_STATE_EIGENVALUES, {rho, vx, vy, vz, p},
+                                                                 mp.getAdiabaticIndex(), q, &bh);
+        return std::vector<double>(all.begin() + 3 * which, all.begin() + 3 * which + 3);
+    }
+};
 
 // ----------------------------------------------------------------------------- solvers
 namespace cosmos_compat_detail {

@@ -87,3 +87,20 @@ def test_python_api_names_mirror_reference():
             assert callable(getattr(cls, m)), (cls, m)
     assert cg.EulerMaterialParameters(1.4).getAdiabaticIndex() == 1.4
     assert cg.BlackHoleSpacetime(0.05, 0.5, 0.0, 0.0).mass == 0.05
+
+
+def test_state_operation_widths(cosmos_lib):
+    """cosmos_state_width: the input and output doubles per item of every state operation (host
+    only, no device)."""
+    from cosmos_gb300 import _lib
+    want = {_lib.STATE_CONS: (5, 5), _lib.STATE_PRIM: (5, 5), _lib.STATE_FLUX_X: (5, 5), _lib.STATE_FLUX_Y: (5, 5),
+            _lib.STATE_SOUND: (5, 1), _lib.STATE_INTERNAL_ENERGY: (5, 1), _lib.STATE_TOTAL_ENERGY: (5, 1),
+            _lib.STATE_PRESSURE: (5, 1), _lib.STATE_ENTHALPY: (5, 1), _lib.STATE_SOURCE: (5, 5),
+            _lib.STATE_EIGENVALUES: (5, 9), _lib.STATE_GRADIENT_RATIO: (1, 1), _lib.STATE_LIMITER: (1, 1),
+            _lib.STATE_SLOPE: (15, 5)}
+    for op, (wi, wo) in want.items():
+        a, b = ctypes.c_size_t(0), ctypes.c_size_t(0)
+        assert cosmos_lib.cosmos_state_width(op, ctypes.byref(a), ctypes.byref(b)) == 0
+        assert (a.value, b.value) == (wi, wo), op
+    assert cosmos_lib.cosmos_state_width(14, None, None) == _lib.EINVAL
+    assert cosmos_lib.cosmos_state_width(-1, None, None) == _lib.EINVAL
