@@ -13,6 +13,7 @@
 #pragma once
 
 #include <cmath>
+#include <iostream>
 #include <stdexcept>
 #include <string>
 #include <tuple>
@@ -462,11 +463,58 @@ double max_speed2(int sys, std::vector<std::vector<S> >& c, EulerMaterialParamet
     return s;
 }
 
+// EulerSolvers::insertBoundaryCells(2D) (Solvers/EulerSolvers.cpp:3-85; the SR and black-hole
+// twins are the same): a copy with 1 or 2 transmissive ghost cells per side (mirrored order for 2);
+// the 2D corners keep default-constructed states, as in the reference.
+template <class S> std::vector<S> insert_boundary(const std::vector<S>& c, int b) {
+    const long n = (long)c.size();
+    std::vector<S> o(n + 2 * b);
+    if (b == 1) {
+        o[0] = c[0];
+        o[n + 1] = c[n - 1];
+    } else if (b == 2) {
+        o[0] = c[1]; o[1] = c[0];
+        o[n + 2] = c[n - 1]; o[n + 3] = c[n - 2];
+    }
+    for (long i = 0; i < n; i++) o[i + b] = c[i];
+    return o;
+}
+template <class S> std::vector<std::vector<S> > insert_boundary_2d(const std::vector<std::vector<S> >& c, int b) {
+    const long rows = (long)c.size(), cols = (long)c[0].size();
+    std::vector<std::vector<S> > o(rows + 2 * b, std::vector<S>(cols + 2 * b));
+    if (b == 1) {
+        for (long i = 0; i < rows; i++) { o[i + 1][0] = c[i][0]; o[i + 1][cols + 1] = c[i][cols - 1]; }
+        for (long j = 0; j < cols; j++) { o[0][j + 1] = c[0][j]; o[rows + 1][j + 1] = c[rows - 1][j]; }
+    } else if (b == 2) {
+        for (long i = 0; i < rows; i++) {
+            o[i + 2][0] = c[i][1]; o[i + 2][1] = c[i][0];
+            o[i + 2][cols + 2] = c[i][cols - 1]; o[i + 2][cols + 3] = c[i][cols - 2];
+        }
+        for (long j = 0; j < cols; j++) {
+            o[0][j + 2] = c[1][j]; o[1][j + 2] = c[0][j];
+            o[rows + 2][j + 2] = c[rows - 1][j]; o[rows + 3][j + 2] = c[rows - 2][j];
+        }
+    }
+    for (long i = 0; i < rows; i++)
+        for (long j = 0; j < cols; j++) o[i + b][j + b] = c[i][j];
+    return o;
+}
+
 }  // namespace cosmos_compat_detail
 
 #define COSMOS_COMPAT_SOLVERS(PREFIX, STATE, SYS)                                                               \
     class PREFIX##Solvers {                                                                                    \
     public:                                                                                                    \
+        static std::vector<STATE> insertBoundaryCells(std::vector<STATE>& c, int b) {                          \
+            return cosmos_compat_detail::insert_boundary(c, b);                                                \
+        }                                                                                                      \
+        static std::vector<std::vector<STATE> > insertBoundaryCells2D(std::vector<std::vector<STATE> >& c, int b) { \
+            return cosmos_compat_detail::insert_boundary_2d(c, b);                                             \
+        }                                                                                                      \
+        /* Solvers/EulerSolvers.cpp:225-228 */                                                                 \
+        static void outputStatus(int it, double t, double dt) {                                                \
+            std::cout << "Iteration = " << it << "; Time = " << t << "; Timestep = " << dt << std::endl;       \
+        }                                                                                                      \
         static double computeMaximumWaveSpeed(std::vector<STATE>& c, EulerMaterialParameters mp) {             \
             return cosmos_compat_detail::max_speed1(SYS, c, mp);                                               \
         }                                                                                                      \
@@ -539,6 +587,21 @@ COSMOS_COMPAT_SOLVERS(RelativisticEuler, RelativisticEulerStateVector, COSMOS_SR
 // (Solvers/BlackHoleEulerSecondOrderSolver.hpp:10-32, Solvers/BlackHoleEulerForcingSolver.hpp:19-22).
 class BlackHoleEulerSolvers {
 public:
+    static std::vector<BlackHoleEulerStateVector> insertBoundaryCells(std::vector<BlackHoleEulerStateVector>& c, int b) {
+        return cosmos_compat_detail::insert_boundary(c, b);
+    }
+    static std::vector<std::vector<BlackHoleEulerStateVector> > insertBoundaryCells2D(
+        std::vector<std::vector<BlackHoleEulerStateVector> >& c, int b) {
+        return cosmos_compat_detail::insert_boundary_2d(c, b);
+    }
+    static double computeMaximumWaveSpeed(std::vector<BlackHoleEulerStateVector>& c, EulerMaterialParameters mp,
+                                          BlackHoleSpacetime bh) {
+        return cosmos_compat_detail::max_speed1(COSMOS_GR, c, mp, &bh);
+    }
+    static double computeMaximumWaveSpeed2D(std::vector<std::vector<BlackHoleEulerStateVector> >& c,
+                                            EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        return cosmos_compat_detail::max_speed2(COSMOS_GR, c, mp, &bh);
+    }
     static double computeStableTimeStep(std::vector<BlackHoleEulerStateVector> c, double dx, double cfl, double t,
                                         double T, int it, EulerMaterialParameters mp, BlackHoleSpacetime bh) {
         return cosmos_stable_dt_rule(cfl * (dx / cosmos_compat_detail::max_speed1(COSMOS_GR, c, mp, &bh)), t, T, it);
