@@ -11,6 +11,7 @@ from .solvers import (BlackHoleEulerFirstOrderSolver, BlackHoleEulerForcingSolve
                       EulerFirstOrderSolver, EulerMaterialParameters, EulerSecondOrderSolver, EulerSolvers, Grid,
                       RelativisticEulerFirstOrderSolver, RelativisticEulerSecondOrderSolver, RelativisticEulerSolvers,
                       default_context, solve_with_steps)
-from .solvers import AMR, Batch, EulerAMR, RelativisticEulerAMR, state_eval  # noqa: F401
+from .solvers import (AMR, Batch, EulerAMR, EulerEquationOfState, RelativisticEulerAMR,  # noqa: F401
+                      RelativisticEulerEquationOfState, SlopeLimiters, state_eval)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -600,3 +600,84 @@ def state_eval(op, items, system=NEWTONIAN, gamma=1.4, xyz=None, black_hole=None
     check(load().cosmos_state_eval(ctx.h, ctypes.byref(p), int(op), n, a.ctypes.data,
                                    None if q is None else q.ctypes.data, float(bias), int(limiter), out.ctypes.data))
     return out
+
+
+def _scalar_or_array(out, like):
+    return float(out[0, 0]) if np.ndim(like) == 0 else out[:, 0].reshape(np.shape(like))
+
+
+def _rho_p_items(rho, p):
+    r, q = np.broadcast_arrays(np.asarray(rho, dtype=np.float64), np.asarray(p, dtype=np.float64))
+    items = np.zeros(r.shape + (5,))
+    items[..., 0], items[..., 4] = r, q
+    return items, r
+
+
+class EulerEquationOfState:
+    """Euler/EulerEquationOfState.hpp on the device; scalars or arrays."""
+
+    @staticmethod
+    def computeSpecificInternalEnergy(density, pressure, materialParameters):
+        items, r = _rho_p_items(density, pressure)
+        return _scalar_or_array(state_eval(_lib.STATE_INTERNAL_ENERGY, items, NEWTONIAN,
+                                           materialParameters.getAdiabaticIndex()), r)
+
+    @staticmethod
+    def computePressure(density, specificInternalEnergy, materialParameters):
+        items, r = _rho_p_items(density, specificInternalEnergy)
+        return _scalar_or_array(state_eval(_lib.STATE_PRESSURE, items, NEWTONIAN,
+                                           materialParameters.getAdiabaticIndex()), r)
+
+    @staticmethod
+    def computeSoundSpeed(density, pressure, materialParameters):
+        items, r = _rho_p_items(density, pressure)
+        return _scalar_or_array(state_eval(_lib.STATE_SOUND, items, NEWTONIAN, materialParameters.getAdiabaticIndex()),
+                                r)
+
+
+class RelativisticEulerEquationOfState:
+    """RelativisticEuler/RelativisticEulerEquationOfState.hpp on the device; scalars or arrays."""
+
+    @staticmethod
+    def computeSpecificEnthalpy(density, pressure, materialParameters):
+        items, r = _rho_p_items(density, pressure)
+        return _scalar_or_array(state_eval(_lib.STATE_ENTHALPY, items, SR, materialParameters.getAdiabaticIndex()), r)
+
+    @staticmethod
+    def computeSoundSpeed(density, pressure, materialParameters):
+        items, r = _rho_p_items(density, pressure)
+        return _scalar_or_array(state_eval(_lib.STATE_SOUND, items, SR, materialParameters.getAdiabaticIndex()), r)
+
+
+class SlopeLimiters:
+    """Solvers/SlopeLimiters.hpp on the device: limiter functions of a steepness r (scalar or array)
+    and slope vectors of conserved (left, middle, right) vectors ((..., 5) arrays)."""
+
+    @staticmethod
+    def computeGradientRatio(steepness, bias):
+        r = np.asarray(steepness, dtype=np.float64)
+        return _scalar_or_array(state_eval(_lib.STATE_GRADIENT_RATIO, r.reshape(-1, 1), bias=bias), r)
+
+    @staticmethod
+    def computeSlopeLimiter(steepness, bias, slopeLimiter):
+        r = np.asarray(steepness, dtype=np.float64)
+        return _scalar_or_array(state_eval(_lib.STATE_LIMITER, r.reshape(-1, 1), bias=bias, limiter=slopeLimiter), r)
+
+    @staticmethod
+    def computeSuperBeeSlopeLimiter(steepness, bias):
+        return SlopeLimiters.computeSlopeLimiter(steepness, bias, 0)
+
+    @staticmethod
+    def computeVanLeerSlopeLimiter(steepness, bias):
+        return SlopeLimiters.computeSlopeLimiter(steepness, bias, 1)
+
+    @staticmethod
+    def computeMinBeeSlopeLimiter(steepness, bias):
+        return SlopeLimiters.computeSlopeLimiter(steepness, bias, 2)
+
+    @staticmethod
+    def computeSlopeVector(left, middle, right, bias, slopeLimiter):
+        l, m, r = np.broadcast_arrays(*(np.asarray(v, dtype=np.float64) for v in (left, middle, right)))
+        out = state_eval(_lib.STATE_SLOPE, np.concatenate([l.reshape(-1, 5), m.reshape(-1, 5), r.reshape(-1, 5)], axis=1),
+                         bias=bias, limiter=slopeLimiter)
+        return out.reshape(l.shape)

@@ -137,3 +137,20 @@ def test_state_eval_rejects_misuse(cg):
         cg.state_eval(_lib.STATE_SOURCE, states(0, 2, 1), system=0)
     with pytest.raises(CosmosError):
         cg.state_eval(_lib.STATE_CONS, states(2, 2, 1), system=2, gamma=5.0 / 3.0)  # no coordinates
+
+
+def test_reference_named_python_classes(cg, oracle):
+    mp = cg.EulerMaterialParameters(1.4)
+    assert cg.EulerEquationOfState.computeSoundSpeed(0.8, 0.6, mp) == math.sqrt((1.4 * 0.6) / 0.8)
+    e = cg.EulerEquationOfState.computeSpecificInternalEnergy(np.array([0.8, 1.2]), np.array([0.6, 0.3]), mp)
+    assert list(e) == [0.6 / ((1.4 - 1.0) * 0.8), 0.3 / ((1.4 - 1.0) * 1.2)]
+    assert cg.EulerEquationOfState.computePressure(0.8, e[0], mp) == (e[0] * (1.4 - 1.0)) * 0.8
+    r = np.linspace(-1, 3, 17)
+    assert list(cg.SlopeLimiters.computeVanLeerSlopeLimiter(r, 0.2)) == [oracle.limiter(v, 0.2, 1) for v in r]
+    u = np.random.default_rng(3).uniform(-1, 1, (3, 4, 5))
+    s = cg.SlopeLimiters.computeSlopeVector(u[0], u[1], u[2], 0.0, 2)
+    for k in range(4):
+        assert bit_equal(s[k], oracle.slope(u[0, k], u[1, k], u[2, k], 0.0, 2))
+    g = 5.0 / 3.0
+    h = cg.RelativisticEulerEquationOfState.computeSpecificEnthalpy(1.0, 2.0, cg.EulerMaterialParameters(g))
+    assert h == 1.0 + ((2.0 / 1.0) * (g / (g - 1.0)))
