@@ -128,22 +128,6 @@ int main(int argc, char** argv) {
         for (bool b : std::get<5>(r)) all.push_back(b ? 1.0 : 0.0);
         dump(dir + "/amr2_sr.bin", all);
     }
-    // state-level API (Euler/EulerStateVector.hpp, Solvers/SlopeLimiters.hpp, the equations of state)
-    {
-        EulerMaterialParameters mp(1.4);
-        EulerStateVector s(0.8, 0.3, -0.2, 0.1, 0.6);
-        std::vector<double> out = s.computeConservedVariableVector(mp);
-        std::vector<double> f = s.computeXFluxVector(mp);
-        out.insert(out.end(), f.begin(), f.end());
-        EulerStateVector t;
-        t.setConservedVariableVector(s.computeConservedVariableVector(mp), mp);
-        std::vector<double> tp = t.computePrimitiveVariableVector();
-        out.insert(out.end(), tp.begin(), tp.end());
-        out.push_back(SlopeLimiters::computeSlopeLimiter(0.7, 0.0, 1));
-        out.push_back(EulerEquationOfState::computeSoundSpeed(0.8, 0.6, mp));
-        out.push_back(RelativisticEulerEquationOfState::computeSoundSpeed(1.0, 1.0, EulerMaterialParameters(5.0 / 3.0)));
-        dump(dir + "/state.bin", out);
-    }
     std::printf("compat driver ok\n");
     return 0;
 }

@@ -154,3 +154,24 @@ def test_reference_named_python_classes(cg, oracle):
     g = 5.0 / 3.0
     h = cg.RelativisticEulerEquationOfState.computeSpecificEnthalpy(1.0, 2.0, cg.EulerMaterialParameters(g))
     assert h == 1.0 + ((2.0 / 1.0) * (g / (g - 1.0)))
+
+
+def test_compat_state_classes_from_cpp(cosmos_lib, oracle, tmp_path):
+    import os
+    import subprocess
+    from conftest import ROOT
+    exe, out = str(tmp_path / "state_driver"), str(tmp_path / "state.bin")
+    lib = os.path.join(ROOT, "cosmos_gb300")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "state_driver.cpp"), "-o", exe, "-L", lib, "-lcosmos_gb300",
+                    f"-Wl,-rpath,{lib}"], check=True)
+    subprocess.run([exe, out], check=True, timeout=120)
+    st = np.fromfile(out, dtype=np.float64)
+    assert st.shape == (18,)
+    prim = np.array([0.8, 0.3, -0.2, 0.1, 0.6])
+    u = oracle.cons(0, prim, 1.4)
+    assert bit_equal(st[:5], u) and bit_equal(st[5:10], oracle.flux(0, u, 0, 1.4))
+    assert bit_equal(st[10:15], oracle.prim(0, u, 1.4))
+    assert st[15] == oracle.limiter(0.7, 0.0, 1) and st[16] == math.sqrt((1.4 * 0.6) / 0.8)
+    g = 5.0 / 3.0
+    assert st[17] == math.sqrt(((g * 1.0) / 1.0) / (1.0 + ((1.0 / 1.0) * (g / (g - 1.0)))))
