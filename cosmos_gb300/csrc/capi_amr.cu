@@ -95,6 +95,14 @@ int bad_dt(double dt) {
     return afail(COSMOS_ENONFINITE, "AMR driver: non-finite or non-positive time step " + std::to_string(dt));
 }
 
+// A finer level takes about 2 steps per parent step; a run that needs this many has a collapsed
+// time step (the reference would keep looping), so the driver stops with an error instead.
+constexpr int kMaxSubSteps = 1 << 20;
+int too_many(int k) {
+    if (k < kMaxSubSteps) return COSMOS_OK;
+    return afail(COSMOS_ENONFINITE, "AMR driver: more than 2^20 sub-steps in one parent step (collapsed time step)");
+}
+
 // Sweep arguments of level l reading its current state.
 SweepArgs level_args(cosmos_amr* a, int l) {
     SweepArgs s = base_args(a->level[l]);
@@ -188,9 +196,9 @@ int run_level1(cosmos_amr* a, double cfl, double t_final, double tol, int order,
         if ((rc = masked_step(C, order, dt, flags(a, 0)))) break;
         if (refined) {
             double ft = t;
-            while (ft < (t + dt - 1e-4)) {
+            for (int sub = 0; ft < (t + dt - 1e-4); sub++) {
                 double fs = 0.0;
-                if ((rc = read_word(a, 1, -1, &fs, nullptr))) break;
+                if ((rc = too_many(sub)) || (rc = read_word(a, 1, -1, &fs, nullptr))) break;
                 const double fdt = cosmos_stable_dt_rule(cfl * ((dx * 0.5) / fs), ft, t + dt, c->fit);
                 if ((rc = bad_dt(fdt))) break;
                 if ((rc = masked_step(F, order, fdt, flags(a, 1)))) break;
@@ -238,11 +246,11 @@ int run_level2(cosmos_amr* a, double cfl, double t_final, double tol, int order,
         if ((rc = masked_step(C, order, dt, flags(a, 0)))) break;
         if (refined) {
             double mt = t;
-            while (mt < (t + dt - 1e-4)) {
+            for (int msub = 0; mt < (t + dt - 1e-4); msub++) {
                 double ms = 0.0;
                 bool refined2 = false;
                 // the intermediate time step precedes its flag pass; both read the same state
-                if ((rc = read_word(a, 1, -1, &ms, nullptr))) break;
+                if ((rc = too_many(msub)) || (rc = read_word(a, 1, -1, &ms, nullptr))) break;
                 const double mdt = cosmos_stable_dt_rule(cfl * ((dx * 0.5) / ms), mt, t + dt, c->fit);
                 if ((rc = bad_dt(mdt))) break;
                 MCK(launch_amr_flags_ex(level_args(a, 1), prec, tol * 2.0 * order, dx, true, true, flags(a, 1),
@@ -256,9 +264,9 @@ int run_level2(cosmos_amr* a, double cfl, double t_final, double tol, int order,
                 refined2 = a->host[1] != 0;
                 if (refined2) {
                     double ft = mt;
-                    while (ft < (mt + mdt - 1e-4)) {
+                    for (int fsub = 0; ft < (mt + mdt - 1e-4); fsub++) {
                         double fs = 0.0;
-                        if ((rc = read_word(a, 2, -1, &fs, nullptr))) break;
+                        if ((rc = too_many(fsub)) || (rc = read_word(a, 2, -1, &fs, nullptr))) break;
                         const double fdt = cosmos_stable_dt_rule(cfl * ((dx * 0.25) / fs), ft, mt + mdt, c->fit);
                         if ((rc = bad_dt(fdt))) break;
                         if ((rc = masked_step(F, order, fdt, flags(a, 2)))) break;
