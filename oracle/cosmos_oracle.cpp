@@ -332,7 +332,7 @@ static void inverse_n(const double* m, int n, double* o) {
     }
 }
 
-struct GR {
+template <class Num> struct GRT {
     double g;
     BH bh;
     double h;  // finite-difference spacing for metric derivatives (the grid's cell spacing)
@@ -340,43 +340,45 @@ struct GR {
 
     double detg(Pt p) const { double m[9]; bh.gamma(p.x, p.y, p.z, m); return det_n(m, 3); }  // :240-243
 
-    // BlackHoleEuler/BlackHoleEulerStateVector.cpp:118-157 (energy uses W, not W^2, at :154)
-    void cons(const double* p, Pt q, double* u) const {
+    // BlackHoleEuler/BlackHoleEulerStateVector.cpp:118-157 (energy uses W, not W^2, at :154).  The
+    // metric is FP64 data; the state may be a dual number (tangent-linear model).
+    void cons(const Num* p, Pt q, Num* u) const {
+        using std::sqrt;
         double m[9];
         bh.gamma(q.x, q.y, q.z, m);
         double dg = detg(q);
-        double v[3] = {p[1], p[2], p[3]};
-        double v2 = 0.0;
+        Num v[3] = {p[1], p[2], p[3]};
+        Num v2 = Num(0.0);
         for (int i = 0; i < 3; i++)
-            for (int j = 0; j < 3; j++) v2 = v2 + ((m[3 * i + j] * v[i]) * v[j]);
-        double W = 1.0 / std::sqrt(1.0 - v2);
-        if (v2 > 1.0 - 1e-8) W = 1.0 / std::sqrt(1.0 - 1e-8);
-        double hh = sr_enthalpy(p[0], p[4], g);
-        double sg = std::sqrt(dg);
+            for (int j = 0; j < 3; j++) v2 = v2 + ((Num(m[3 * i + j]) * v[i]) * v[j]);
+        Num W = Num(1.0) / sqrt(Num(1.0) - v2);
+        if (v2 > Num(1.0 - 1e-8)) W = Num(1.0 / std::sqrt(1.0 - 1e-8));
+        Num hh = Num(1.0) + ((p[4] / p[0]) * Num(g / (g - 1.0)));  // sr_enthalpy
+        Num sg = Num(std::sqrt(dg));
         u[0] = (sg * p[0]) * W;
         for (int k = 0; k < 3; k++) u[1 + k] = (((sg * p[0]) * hh) * (W * W)) * v[k];
         u[4] = sg * ((((p[0] * hh) * W) - p[4]) - (p[0] * W));
     }
-    C2P c2p(const double* u, Pt q, double tol) const {
-        double sg = std::sqrt(detg(q));
-        return con2prim(u[0] / sg, u[1] / sg, u[2] / sg, u[3] / sg, u[4] / sg, g, tol);
+    C2PT<Num> c2p(const Num* u, Pt q, double tol) const {
+        Num sg = Num(std::sqrt(detg(q)));
+        return con2prim_t<Num>(u[0] / sg, u[1] / sg, u[2] / sg, u[3] / sg, u[4] / sg, g, tol);
     }
     // BlackHoleEuler/BlackHoleEulerStateVector.cpp:30-103
-    void prim(const double* u, Pt q, double* p) const {
-        C2P c = c2p(u, q, 1e-8);
+    void prim(const Num* u, Pt q, Num* p) const {
+        C2PT<Num> c = c2p(u, q, 1e-8);
         p[0] = c.rho; p[1] = c.vx; p[2] = c.vy; p[3] = c.vz; p[4] = c.p;
     }
     // BlackHoleEuler/BlackHoleEulerStateVector.cpp:159-250 (x, Newton tol 1e-10) and :259-350 (y)
-    void flux(const double* u, int axis, Pt q, double* f) const {
+    void flux(const Num* u, int axis, Pt q, Num* f) const {
         double dg = detg(q);
         double al = bh.lapse(q.x, q.y, q.z);
         double be[3];
         bh.shiftv(q.x, q.y, q.z, be);
-        C2P c = c2p(u, q, axis == 0 ? 1e-10 : 1e-8);
-        double as = al * std::sqrt(dg);
-        double rhw = (c.rho * c.h) * (c.W * c.W);
-        double vn = axis == 0 ? c.vx : c.vy;
-        double w = vn - (be[axis] / al);
+        C2PT<Num> c = c2p(u, q, axis == 0 ? 1e-10 : 1e-8);
+        Num as = Num(al * std::sqrt(dg));
+        Num rhw = (c.rho * c.h) * (c.W * c.W);
+        Num vn = axis == 0 ? c.vx : c.vy;
+        Num w = vn - Num(be[axis] / al);
         f[0] = as * ((c.rho * c.W) * w);
         if (axis == 0) {
             f[1] = as * ((rhw * (c.vx * w)) + c.p);
@@ -528,6 +530,7 @@ struct GR {
         return s;
     }
 };
+typedef GRT<double> GR;
 
 // ========================================================================= generic sweep
 // Half-step evolution of the middle state, Solvers/EulerSolvers.cpp:174-223 (Newtonian),
@@ -1372,17 +1375,18 @@ int orc_amr_level2(int sys, const double* prim, int ny, int nx, int dims, double
 }  // extern "C"
 template <class Sys>
 static double tlm_run(const Sys& S, const double* prim0, const double* dprim, const double* target, int ny, int nx,
-                      int dims, double dx, const double* dts, int nsteps, double bias, int lim, int bc, double* dL) {
+                      int dims, double dx, const double* dts, int nsteps, double bias, int lim, int bc, double* dL,
+                      const BH* exc = nullptr) {
     size_t N = (size_t)(dims == 1 ? 1 : ny) * nx;
     std::vector<Dual> p(5 * N);
     for (size_t i = 0; i < 5 * N; i++) p[i] = Dual(prim0[i], dprim ? dprim[i] : 0.0);
     for (int s = 0; s < nsteps; s++) {
         double dt = dts[s];
-        if (dims == 1) sweep(S, p.data(), ny, nx, 1, 0, 2, dx, dt, bias, lim, bc, nullptr, nullptr);
+        if (dims == 1) sweep(S, p.data(), ny, nx, 1, 0, 2, dx, dt, bias, lim, bc, nullptr, exc);
         else {
-            sweep(S, p.data(), ny, nx, 2, 0, 2, dx, 0.5 * dt, bias, lim, bc, nullptr, nullptr);
-            sweep(S, p.data(), ny, nx, 2, 1, 2, dx, dt, bias, lim, bc, nullptr, nullptr);
-            sweep(S, p.data(), ny, nx, 2, 0, 2, dx, 0.5 * dt, bias, lim, bc, nullptr, nullptr);
+            sweep(S, p.data(), ny, nx, 2, 0, 2, dx, 0.5 * dt, bias, lim, bc, nullptr, exc);
+            sweep(S, p.data(), ny, nx, 2, 1, 2, dx, dt, bias, lim, bc, nullptr, exc);
+            sweep(S, p.data(), ny, nx, 2, 0, 2, dx, 0.5 * dt, bias, lim, bc, nullptr, exc);
         }
     }
     Dual L(0.0);
@@ -1408,6 +1412,16 @@ double orc_tlm_newton(const double* prim0, const double* dprim, const double* ta
 double orc_tlm_sr(const double* prim0, const double* dprim, const double* target, int ny, int nx, int dims, double dx,
                   const double* dts, int nsteps, double bias, int lim, double gamma, int bc, double* dL) {
     return tlm_run(SRT<Dual>{gamma}, prim0, dprim, target, ny, nx, dims, dx, dts, nsteps, bias, lim, bc, dL);
+}
+
+// The same for the black-hole flux step without source terms (BlackHoleEulerSecondOrderSolver's
+// step with zero subcycles, Solvers/BlackHoleEulerSecondOrderSolver.cpp:181-218): the metric enters as
+// FP64 data, cells whose stencil touches the excision region keep their state (derivative carried
+// through unchanged), transmissive boundaries.  bh = {M, a, x, y, z}.
+double orc_tlm_gr(const double* prim0, const double* dprim, const double* target, int ny, int nx, int dims, double dx,
+                  const double* dts, int nsteps, double bias, int lim, double gamma, const double* bh, double* dL) {
+    GRT<Dual> S{gamma, BH{bh[0], bh[1], bh[2], bh[3], bh[4]}, dx};
+    return tlm_run(S, prim0, dprim, target, ny, nx, dims, dx, dts, nsteps, bias, lim, 0, dL, &S.bh);
 }
 
 }  // extern "C"

@@ -78,6 +78,8 @@ class Oracle:
         L.orc_tlm_newton.restype = _d
         L.orc_tlm_sr.argtypes = [_p, _p, _p, _i, _i, _i, _d, _p, _i, _d, _i, _d, _i, _p]
         L.orc_tlm_sr.restype = _d
+        L.orc_tlm_gr.argtypes = [_p, _p, _p, _i, _i, _i, _d, _p, _i, _d, _i, _d, _p, _p]
+        L.orc_tlm_gr.restype = _d
         L.orc_set_threads.argtypes = [_i]
 
     def set_threads(self, n):
@@ -217,6 +219,18 @@ class Oracle:
         out = _d(0.0)
         L = self.L.orc_tlm_sr(_ptr(p), _ptr(d), _ptr(t), ny, nx, dims, dx, _ptr(ds), len(ds), bias, lim, gamma, bc,
                               ctypes.byref(out))
+        return L, out.value
+
+    def tlm_gr(self, prim0, dprim, target, dx, dts, bias, lim, gamma, bh):
+        """The black-hole flux-step tangent-linear model (no source terms): (loss, directional derivative)."""
+        p = np.ascontiguousarray(prim0, dtype=np.float64)
+        d = np.ascontiguousarray(dprim, dtype=np.float64)
+        t = np.ascontiguousarray(target, dtype=np.float64)
+        ds = np.ascontiguousarray(dts, dtype=np.float64)
+        ny, nx, dims = _shape(p)
+        out = _d(0.0)
+        L = self.L.orc_tlm_gr(_ptr(p), _ptr(d), _ptr(t), ny, nx, dims, dx, _ptr(ds), len(ds), bias, lim, gamma,
+                              _ptr(_bh(bh)), ctypes.byref(out))
         return L, out.value
 
     def tlm_newton(self, prim0, dprim, target, dx, dts, bias, lim, gamma, bc=0):

@@ -104,3 +104,64 @@ def test_oracle_sr_tlm_matches_finite_differences(oracle, dims, lim, bc):
         Lm, _ = oracle.tlm_sr(p0 - h * d, np.zeros_like(d), target, dx, dts, 0.0, lim, g, bc)
         fd = (Lp - Lm) / (2 * h)
         assert abs(fd - dL) <= 1e-6 * abs(dL) + 1e-10, (fd, dL)
+
+
+def gr_smooth_state(shape, seed):
+    """Gentle data for the black-hole scheme (|v| <= 0.15, p near 0.5, varying along both axes).  The
+    reference's GR half-step evolution drives faster flows superluminal at the grid edges within a
+    few steps; this stays physical over the test's steps."""
+    rng = np.random.default_rng(seed)
+    ph = rng.uniform(0, 2 * np.pi, 5)
+    x = np.linspace(0, 1, shape[-1], endpoint=False)
+    s = np.zeros(shape + (5,))
+    s[..., 0] = 1.0 + 0.2 * np.sin(2 * np.pi * x + ph[0])
+    s[..., 1] = 0.1 * np.cos(2 * np.pi * x + ph[1])
+    s[..., 4] = 0.5 + 0.05 * np.sin(4 * np.pi * x + ph[3])
+    if len(shape) == 2:
+        y = np.linspace(0, 1, shape[0], endpoint=False)[:, None]
+        s[..., 0] += 0.1 * np.sin(2 * np.pi * y + ph[4])
+        s[..., 2] = 0.05 * np.cos(2 * np.pi * y + ph[2]) + 0.0 * x
+        s[..., 4] += 0.03 * np.cos(2 * np.pi * y + ph[2])
+    return s
+
+
+def gr_forward_loss(oracle, p, target, dx, dts, lim, g, bh):
+    q = p.copy()
+    for dt in dts:
+        if q.ndim == 2:
+            q = oracle.sweep(2, q, 0, 2, dx, dt, 0.0, lim, g, bh=bh)
+        else:
+            q = oracle.sweep(2, q, 0, 2, dx, 0.5 * dt, 0.0, lim, g, bh=bh)
+            q = oracle.sweep(2, q, 1, 2, dx, dt, 0.0, lim, g, bh=bh)
+            q = oracle.sweep(2, q, 0, 2, dx, 0.5 * dt, 0.0, lim, g, bh=bh)
+    e = (q[..., 0] - target).ravel()
+    L = 0.0
+    for v in 0.5 * (e * e):
+        L = L + float(v)
+    return L
+
+
+@pytest.mark.parametrize("dims,bh", [(1, (0.05, 0.0, 0.5, 0.0, 0.0)), (2, (0.05, 0.0, 0.5, 0.5, 0.0)),
+                                     (2, (0.08, 0.6, 0.4, 0.6, 0.0))])
+@pytest.mark.parametrize("lim", [0, 1, 2])
+def test_oracle_gr_tlm_matches_finite_differences(oracle, dims, bh, lim):
+    """The black-hole flux step's tangent-linear model (no source terms; the hole excises cells on
+    the grid): value part = the plain GR sweeps, derivative = central differences (fields vary along
+    both axes, so no neighbour difference grows out of zero through the 1e-5 slope clamp)."""
+    g = 5.0 / 3.0
+    shape = (24,) if dims == 1 else (10, 12)
+    p0 = gr_smooth_state(shape, 5 + lim)
+    target = gr_smooth_state(shape, 13)[..., 0]
+    dx = 1.0 / shape[-1]
+    dts = np.full(4, 0.1 * dx)
+    L_plain = gr_forward_loss(oracle, p0, target, dx, dts, lim, g, bh)
+    rng = np.random.default_rng(dims * 10 + lim)
+    for _ in range(2):
+        d = rng.standard_normal(p0.shape)
+        L0, dL = oracle.tlm_gr(p0, d, target, dx, dts, 0.0, lim, g, bh)
+        assert L0 == L_plain
+        h = 1e-7
+        Lp, _ = oracle.tlm_gr(p0 + h * d, np.zeros_like(d), target, dx, dts, 0.0, lim, g, bh)
+        Lm, _ = oracle.tlm_gr(p0 - h * d, np.zeros_like(d), target, dx, dts, 0.0, lim, g, bh)
+        fd = (Lp - Lm) / (2 * h)
+        assert abs(fd - dL) <= 1e-6 * abs(dL) + 1e-10, (fd, dL)
