@@ -69,7 +69,13 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
                                    const double* target, const double* dts_in, double* grad_prim, double* loss,
                                    double* dts_out, double* ms) {
     if (!g || !o || !target || !grad_prim) return afail(COSMOS_EINVAL, "null grid, options, target or gradient");
-    if (g->p.system != COSMOS_NEWTONIAN) return afail(COSMOS_EUNSUPPORTED, "the adjoint covers the Newtonian system");
+    const bool sr = g->p.system == COSMOS_SR;
+    if (g->p.system != COSMOS_NEWTONIAN && !sr)
+        return afail(COSMOS_EUNSUPPORTED, "the adjoint covers the Newtonian and special-relativistic systems");
+    if (sr && g->p.precision != COSMOS_FP64)
+        return afail(COSMOS_EUNSUPPORTED, "the special-relativistic adjoint covers FP64 grids");
+    if (sr && (g->G.nx < 2 || (g->p.dims == 2 && g->G.ny < 2)))
+        return afail(COSMOS_EUNSUPPORTED, "the special-relativistic adjoint needs at least two cells per swept line");
     if (o->order != 2) return afail(COSMOS_EUNSUPPORTED, "the adjoint covers SLIC (order 2)");
     if (nsteps < 1 || checkpoint_every < 1) return afail(COSMOS_EINVAL, "nsteps and checkpoint_every must be >= 1");
     if (!dts_in && !(o->cfl > 0.0)) return afail(COSMOS_EINVAL, "cfl must be positive when no dts are given");
@@ -221,14 +227,21 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
             ap.state = slot(c, q);
             ap.ubar_out = adj + (size_t)cur * abytes;
             ap.ubar_in = adj + (size_t)(cur ^ 1) * abytes;
-            ACK(fp64 ? launch_adjoint_sweep_exact(ap, o->limiter, st) : launch_adjoint_sweep_fast(ap, o->limiter, st));
+            if (sr)
+                ACK(launch_adjoint_sr_sweep(ap.G, g->p.gamma, g->p.dx, dt, o->bias, o->limiter, ap.state, ap.ubar_out,
+                                            ap.ubar_in, st));
+            else
+                ACK(fp64 ? launch_adjoint_sweep_exact(ap, o->limiter, st) : launch_adjoint_sweep_fast(ap, o->limiter, st));
             cur ^= 1;
         }
         ACK(cudaEventRecord(sc.adj_done[c & 1], st));
     }
     // ---- gradient with respect to the initial primitives
-    ACK(fp64 ? launch_adjoint_grad_exact(G0, g->p.gamma, ck, adj + (size_t)cur * abytes, g->staging, st)
-             : launch_adjoint_grad_fast(G0, g->p.gamma, ck, adj + (size_t)cur * abytes, g->staging, st));
+    if (sr)  // the SR sweep adjoints carry primitive adjoints already
+        ACK(launch_adjoint_sr_grad(G0, adj + (size_t)cur * abytes, g->staging, st));
+    else
+        ACK(fp64 ? launch_adjoint_grad_exact(G0, g->p.gamma, ck, adj + (size_t)cur * abytes, g->staging, st)
+                 : launch_adjoint_grad_fast(G0, g->p.gamma, ck, adj + (size_t)cur * abytes, g->staging, st));
     ACK(cudaEventRecord(sc.ev[2], st));
     ACK(cudaMemcpyAsync(grad_prim, g->staging, ncell * 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
     double lv = 0.0;

@@ -145,5 +145,10 @@ cudaError_t launch_adjoint_grad_exact(const Geom& G, double gamma, const void* s
                                       cudaStream_t st);
 cudaError_t launch_adjoint_grad_fast(const Geom& G, double gamma, const void* state, const void* ubar, double* grad,
                                      cudaStream_t st);
+// Special-relativistic FP64 sweep adjoint on primitive adjoints (kernels_adjoint_sr.cu), and the
+// copy of the final primitive adjoint into AoS doubles.
+cudaError_t launch_adjoint_sr_sweep(const Geom& G, double gamma, double dx, double dt, double bias, int lim,
+                                    const void* state, const void* pbar_out, void* pbar_in, cudaStream_t st);
+cudaError_t launch_adjoint_sr_grad(const Geom& G, const void* pbar, double* grad, cudaStream_t st);
 
 }  // namespace cg

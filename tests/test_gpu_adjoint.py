@@ -127,7 +127,7 @@ def test_adjoint_errors(cg):
         g.adjoint(np.zeros((8, 8)), 0, 0.8, 0.0, 2)
     with pytest.raises(cg.CosmosError):
         g.adjoint(np.zeros((8, 8)), 3, 0.8, 0.0, 2, dts=np.array([0.01, -1.0, 0.01]))
-    sr = cg.Grid(1, (8,), 0.1, 5.0 / 3.0)
+    sr = cg.Grid(1, (8,), 0.1, 5.0 / 3.0, cg.FP32)  # the SR adjoint covers FP64 grids
     sr.set_prim(cases.sr_state(np.random.default_rng(0), (8,)))
     with pytest.raises(cg.CosmosError) as e:
         sr.adjoint(np.zeros(8), 3, 0.8, 0.0, 2)
