@@ -34,7 +34,7 @@ UNITS = {
     "kernels_batch_exact.cu": ["--fmad=false"],
     "kernels_adjoint.cu": ["--fmad=false"],
     "kernels_adjoint_fast.cu": [],
-    "kernels_adjoint_sr.cu": ["--fmad=false"],
+    "kernels_adjoint_rel.cu": ["--fmad=false"],
     "capi.cu": [],
     "capi_batch.cu": [],
     "noalloc.cu": [],

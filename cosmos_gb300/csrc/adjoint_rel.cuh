@@ -1,0 +1,458 @@
+// Adjoint (vector-Jacobian product) of one relativistic SLIC sweep, FP64, gather form: the
+// special-relativistic sweep and the black-hole flux sweep (excision, no source terms).
+//
+// Forward map of a sweep along a line of n cells (primitive states P, dt and dx fixed):
+//   SR  (Solvers/RelativisticEulerSecondOrderSolver.cpp:3-100, the half-step evolution of
+//        Solvers/RelativisticEulerSolvers.cpp:148-199): A_k, B_k = the left- and right-face
+//        primitives of cell k's half-step evolution from P_{k-1..k+1};  F_f = FORCE(B_{f-1}, A_f)
+//   GR  (Solvers/BlackHoleEulerSecondOrderSolver.cpp:3-179, Solvers/BlackHoleEulerSolvers.cpp:234-307):
+//        face f at x_f = (f - 1/2) dx gets F_f = FORCE(B, A) with B the right face of the evolution
+//        of P_{f-2..f} centred at x_f - dx/2 and A the left face of that of P_{f-1..f+1} centred at
+//        x_f + dx/2, every state converted with the Kerr-Schild metric at its own point
+//   P'_k = prim(cons(P_k) + (dt/dx) (F_k - F_{k+1})), or P'_k = P_k for a black-hole cell whose
+//   stencil touches the excision region;
+// with the FORCE flux of Solvers/EulerFirstOrderSolver.cpp:3-59 (BlackHoleEulerFirstOrderSolver.cpp:3-47),
+// the state functions of RelativisticEulerStateVector.cpp and BlackHoleEulerStateVector.cpp, and
+// the slope limiters of Solvers/SlopeLimiters.cpp:3-101.  So P'_k depends on P_{k-2} .. P_{k+2},
+// where positions outside the line read the interior cell they copy (transmissive mirror or
+// periodic wrap).  Given the adjoint Pbar' of the output, the adjoint of input cell j is
+//   Pbar_j = sum over the outputs k whose five-cell window holds j of (dP'_k / dP_j)^T Pbar'_k.
+// One thread owns one input cell: it evaluates the window of each such k in dual numbers whose
+// five tangent lanes are seeded on cell j's primitives, so the derivative is that of the arithmetic
+// the forward runs -- every primitive recovery's Newton iteration, the limiter branch taken, the
+// 1e-5 clamp and the floors (derivative 0) -- and no two threads write the same cell.
+//
+// Host and device code: the same cell function runs in the kernel and in host builds.
+#pragma once
+#include <cmath>
+#include <cstddef>
+
+#ifdef __CUDACC__
+#define RADJ_HD __host__ __device__ inline
+#else
+#define RADJ_HD inline
+#endif
+
+namespace cg {
+namespace radj {
+
+// ---- dual numbers: value and five tangent lanes; comparisons act on values
+struct D5 {
+    double v, d[5];
+    RADJ_HD D5() : v(0.0), d{0.0, 0.0, 0.0, 0.0, 0.0} {}
+    RADJ_HD D5(double x) : v(x), d{0.0, 0.0, 0.0, 0.0, 0.0} {}
+};
+RADJ_HD D5 operator+(const D5& a, const D5& b) {
+    D5 r(a.v + b.v);
+    for (int i = 0; i < 5; i++) r.d[i] = a.d[i] + b.d[i];
+    return r;
+}
+RADJ_HD D5 operator-(const D5& a, const D5& b) {
+    D5 r(a.v - b.v);
+    for (int i = 0; i < 5; i++) r.d[i] = a.d[i] - b.d[i];
+    return r;
+}
+RADJ_HD D5 operator-(const D5& a) {
+    D5 r(-a.v);
+    for (int i = 0; i < 5; i++) r.d[i] = -a.d[i];
+    return r;
+}
+RADJ_HD D5 operator*(const D5& a, const D5& b) {
+    D5 r(a.v * b.v);
+    for (int i = 0; i < 5; i++) r.d[i] = (a.d[i] * b.v) + (a.v * b.d[i]);
+    return r;
+}
+RADJ_HD D5 operator/(const D5& a, const D5& b) {
+    D5 r(a.v / b.v);
+    for (int i = 0; i < 5; i++) r.d[i] = (a.d[i] - (r.v * b.d[i])) / b.v;
+    return r;
+}
+RADJ_HD D5 sqrt(const D5& a) {
+    D5 r(::sqrt(a.v));
+    for (int i = 0; i < 5; i++) r.d[i] = a.d[i] / (2.0 * r.v);
+    return r;
+}
+RADJ_HD D5 fabs(const D5& a) { return a.v < 0.0 ? -a : a; }
+RADJ_HD bool operator<(const D5& a, const D5& b) { return a.v < b.v; }
+RADJ_HD bool operator>(const D5& a, const D5& b) { return a.v > b.v; }
+
+RADJ_HD D5 mn(const D5& a, const D5& b) { return (b < a) ? b : a; }
+
+// ---- slope limiters, Solvers/SlopeLimiters.cpp:3-101 (0 = SuperBee, 1 = van Leer, else MinBee)
+RADJ_HD D5 gradient_ratio(const D5& r, double w) { return D5(2.0) / (D5(1.0 - w) + (D5(1.0 + w) * r)); }
+RADJ_HD D5 limiter(const D5& r, double w, int lim) {
+    if (r < D5(0.0)) return D5(0.0);
+    if (lim == 0) {
+        if (r < D5(0.5)) return D5(2.0) * r;
+        if (r < D5(1.0)) return D5(1.0);
+        return mn(mn(r, gradient_ratio(r, w)), D5(2.0));
+    }
+    if (lim == 1) return mn((D5(2.0) * r) / (D5(1.0) + r), gradient_ratio(r, w));
+    if (r < D5(1.0)) return r;
+    return mn(D5(1.0), gradient_ratio(r, w));
+}
+RADJ_HD void slope_vector(const D5* ul, const D5* uc, const D5* ur, double w, int lim, D5* s) {
+    const D5 a = D5(0.5 * (1.0 + w)), b = D5(0.5 * (1.0 - w));
+    for (int k = 0; k < 5; k++) {
+        const D5 dl = uc[k] - ul[k], dr = ur[k] - uc[k];
+        s[k] = (a * dl) + (b * dr);
+        D5 num = dl, den = dr;
+        if (fabs(num) < D5(1e-5)) num = D5(1e-5);
+        if (fabs(den) < D5(1e-5)) den = D5(1e-5);
+        s[k] = s[k] * limiter(num / den, w, lim);
+    }
+}
+
+// ---- primitive recovery, RelativisticEulerStateVector.cpp:30-101 (BlackHoleEulerStateVector.cpp
+// divides the densitised state by sqrt(det gamma) first): the quartic in x = 1 / (h W) by Newton
+// from x = 1, stopping when a step moves x by less than tol; floors at 1e-8.
+struct Prim { D5 rho, vx, vy, vz, p, W, h; };
+RADJ_HD Prim con2prim(const D5* u, double g, double tol) {
+    const D5 D = u[0], Sx = u[1], Sy = u[2], Sz = u[3], tau = u[4];
+    const D5 q = ((tau + D) * (tau + D)) - (((Sx * Sx) + (Sy * Sy)) + (Sz * Sz));
+    D5 dc, ec;
+    if (q < D5(1e-8)) {
+        dc = D / D5(::sqrt(1e-8));
+        ec = (D + tau) / D5(::sqrt(1e-8));
+    } else {
+        dc = D / sqrt(q);
+        ec = (D + tau) / sqrt(q);
+    }
+    const double gm = (g - 1.0) / g;
+    const D5 cst = D5(-1.0 / (g * g));
+    const D5 lin = (D5(-2.0) * dc) * D5((g - 1.0) / (g * g));
+    const D5 quad = ((D5((g - 2.0) / g) * ((ec * ec) - D5(1.0))) + D5(1.0)) - (((dc * dc) * D5(gm)) * D5(gm));
+    const D5 quart = (ec * ec) - D5(1.0);
+    const D5 eta = (D5(2.0) * dc) * D5(gm);
+    D5 x = D5(1.0);
+    for (int it = 0; it < 1000; it++) {
+        const D5 f = ((((quart * ((x * x) * x)) * (x - eta)) + (quad * (x * x))) + (lin * x)) + cst;
+        const D5 fp = ((lin + ((D5(2.0) * quad) * x)) + ((D5(4.0) * quart) * ((x * x) * x))) -
+                      (((D5(3.0) * eta) * quart) * (x * x));
+        const D5 nx = x - (f / fp);
+        if (fabs(x - nx) < D5(tol)) break;
+        x = nx;
+    }
+    Prim r;
+    r.W = ((D5(0.5) * ec) * x) *
+          (D5(1.0) + sqrt(D5(1.0) + ((D5(4.0) * D5(gm)) * ((D5(1.0) - (dc * x)) / ((ec * ec) * (x * x))))));
+    r.h = D5(1.0) / (dc * x);
+    r.rho = D / r.W;
+    const D5 rhw = (r.rho * r.h) * (r.W * r.W);
+    r.vx = Sx / rhw;
+    r.vy = Sy / rhw;
+    r.vz = Sz / rhw;
+    r.p = (rhw - D) - tau;
+    if (r.rho < D5(1e-8)) r.rho = D5(1e-8);
+    if (r.p < D5(1e-8)) r.p = D5(1e-8);
+    return r;
+}
+// RelativisticEulerEquationOfState.cpp:3-8
+RADJ_HD D5 enthalpy(const D5& rho, const D5& p, double g) { return D5(1.0) + ((p / rho) * D5(g / (g - 1.0))); }
+
+struct Pt { double x, y, z; };
+RADJ_HD Pt shift(Pt p, int axis, double d) {
+    if (axis == 0) p.x = p.x + d;
+    else p.y = p.y + d;
+    return p;
+}
+
+// ---- special-relativistic state, RelativisticEulerStateVector.cpp:116-309
+struct SRSys {
+    double g;
+    static constexpr bool coords = false;
+    RADJ_HD void cons(const D5* p, Pt, D5* u) const {
+        const D5 v2 = ((p[1] * p[1]) + (p[2] * p[2])) + (p[3] * p[3]);
+        D5 W = D5(1.0 / ::sqrt(1.0 - 1e-8));
+        if (!(v2 > D5(1.0 - 1e-8))) W = D5(1.0) / sqrt(D5(1.0) - v2);
+        const D5 rhw = (p[0] * enthalpy(p[0], p[4], g)) * (W * W);
+        u[0] = p[0] * W;
+        u[1] = rhw * p[1];
+        u[2] = rhw * p[2];
+        u[3] = rhw * p[3];
+        u[4] = (rhw - p[4]) - (p[0] * W);
+    }
+    RADJ_HD void prim(const D5* u, Pt, D5* p) const {
+        const Prim c = con2prim(u, g, 1e-8);
+        p[0] = c.rho; p[1] = c.vx; p[2] = c.vy; p[3] = c.vz; p[4] = c.p;
+    }
+    RADJ_HD void flux(const D5* u, int axis, Pt, D5* f) const {
+        const Prim c = con2prim(u, g, 1e-8);
+        const D5 rhw = (c.rho * c.h) * (c.W * c.W);
+        const D5 vn = axis == 0 ? c.vx : c.vy;
+        f[0] = (c.rho * c.W) * vn;
+        f[1] = (rhw * (c.vx * vn)) + (axis == 0 ? c.p : D5(0.0));
+        f[2] = (rhw * (c.vy * vn)) + (axis == 1 ? c.p : D5(0.0));
+        f[3] = rhw * (c.vz * vn);
+        f[4] = (((rhw - c.p) - (c.rho * c.W)) * vn) + (c.p * vn);
+    }
+    RADJ_HD bool active(int, int, int, int, double) const { return true; }
+};
+
+// ---- Kerr-Schild spacetime (BlackHoleSpacetime.cpp:54-186, :372-386), the arithmetic of the
+// sweeps' FP64 metric: mass M, spin a, position (bx, by, bz).
+struct KerrSchild {
+    double M, a, bx, by, bz;
+    RADJ_HD void Hl(double x, double y, double z, double& h, double* l) const {
+        const double dx = x - bx, dy = y - by, dz = z - bz;
+        const double n2 = ((dx * dx) + (dy * dy)) + (dz * dz);
+        const double ma2 = (M * M) * (a * a);
+        const double r = ::sqrt(0.5 * ((n2 - ma2) + ::sqrt(((n2 - ma2) * (n2 - ma2)) + (4.0 * (ma2 * (dz * dz))))));
+        h = -(M * ((r * r) * r)) / ((((r * r) * r) * r) + (ma2 * (dz * dz)));
+        l[0] = -((r * dx) + ((a * M) * dy)) / ((r * r) + ma2);
+        l[1] = -((r * dy) - ((a * M) * dx)) / ((r * r) + ma2);
+        l[2] = -dz / r;
+    }
+    RADJ_HD void gamma(Pt q, double* m) const {
+        double h, l[3];
+        Hl(q.x, q.y, q.z, h, l);
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) m[3 * i + j] = (i == j ? 1.0 : 0.0) - (((2.0 * h) * l[i]) * l[j]);
+    }
+    RADJ_HD void lapse_shift(Pt q, double& al, double* b) const {
+        double h, l[3];
+        Hl(q.x, q.y, q.z, h, l);
+        al = 1.0 / ::sqrt(1.0 - (2.0 * h));
+        for (int i = 0; i < 3; i++) b[i] = ((2.0 * h) / (1.0 - (2.0 * h))) * l[i];
+    }
+    // Mathematics/MatrixAlgebra.cpp:106-149, cofactor expansion along row 0
+    RADJ_HD static double det3(const double* m) {
+        double d = 0.0;
+        d = d + (m[0] * ((m[4] * m[8]) - (m[7] * m[5])));
+        d = d - (m[1] * ((m[3] * m[8]) - (m[6] * m[5])));
+        d = d + (m[2] * ((m[3] * m[7]) - (m[6] * m[4])));
+        return d;
+    }
+    RADJ_HD double sqrt_det(Pt q) const {
+        double m[9];
+        gamma(q, m);
+        return ::sqrt(det3(m));
+    }
+    RADJ_HD bool excised(double x, double y, double z) const {
+        const double r = ::sqrt((((x - bx) * (x - bx)) + ((y - by) * (y - by))) + ((z - bz) * (z - bz)));
+        return r <= (M * (1.0 + ::sqrt(1.0 - (a * a))));
+    }
+};
+
+// ---- black-hole state, BlackHoleEulerStateVector.cpp:30-350 (energy with W, not W^2, at :154;
+// x-flux Newton tolerance 1e-10 at :205)
+struct GRSys {
+    double g;
+    KerrSchild bh;
+    int dims;
+    static constexpr bool coords = true;
+    RADJ_HD void cons(const D5* p, Pt q, D5* u) const {
+        double m[9];
+        bh.gamma(q, m);
+        const double sg = ::sqrt(KerrSchild::det3(m));
+        D5 v2 = D5(0.0);
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) v2 = v2 + ((D5(m[3 * i + j]) * p[1 + i]) * p[1 + j]);
+        D5 W = D5(1.0 / ::sqrt(1.0 - 1e-8));
+        if (!(v2 > D5(1.0 - 1e-8))) W = D5(1.0) / sqrt(D5(1.0) - v2);
+        const D5 hh = enthalpy(p[0], p[4], g);
+        const D5 sr = D5(sg) * p[0];
+        u[0] = sr * W;
+        for (int k = 0; k < 3; k++) u[1 + k] = ((sr * hh) * (W * W)) * p[1 + k];
+        u[4] = D5(sg) * ((((p[0] * hh) * W) - p[4]) - (p[0] * W));
+    }
+    RADJ_HD Prim c2p(const D5* u, Pt q, double tol) const {
+        const D5 sg = D5(bh.sqrt_det(q));
+        const D5 us[5] = {u[0] / sg, u[1] / sg, u[2] / sg, u[3] / sg, u[4] / sg};
+        return con2prim(us, g, tol);
+    }
+    RADJ_HD void prim(const D5* u, Pt q, D5* p) const {
+        const Prim c = c2p(u, q, 1e-8);
+        p[0] = c.rho; p[1] = c.vx; p[2] = c.vy; p[3] = c.vz; p[4] = c.p;
+    }
+    RADJ_HD void flux(const D5* u, int axis, Pt q, D5* f) const {
+        const double sg = bh.sqrt_det(q);
+        double al, be[3];
+        bh.lapse_shift(q, al, be);
+        const Prim c = c2p(u, q, axis == 0 ? 1e-10 : 1e-8);
+        const D5 as = D5(al * sg);
+        const D5 rhw = (c.rho * c.h) * (c.W * c.W);
+        const D5 vn = axis == 0 ? c.vx : c.vy;
+        const D5 w = vn - D5(be[axis] / al);
+        f[0] = as * ((c.rho * c.W) * w);
+        f[1] = as * ((rhw * (c.vx * w)) + (axis == 0 ? c.p : D5(0.0)));
+        f[2] = as * ((rhw * (c.vy * w)) + (axis == 1 ? c.p : D5(0.0)));
+        f[3] = as * (rhw * (c.vz * w));
+        f[4] = as * ((((rhw - c.p) - (c.rho * c.W)) * w) + (c.p * vn));
+    }
+    // Cell k of line L is updated unless a cell of its stencil (two cells out along the line in
+    // 1D; the cell and two cells out along both axes in 2D, Solvers/BlackHoleEulerSecondOrderSolver.cpp:39-100)
+    // lies in the excision region, tested at the unmirrored positions x = j dx, y = i dx.
+    RADJ_HD bool active(int axis, int L, int k, int, double dx) const {
+        if (dims == 1) {
+            for (int d = -2; d <= 2; d++)
+                if (bh.excised((k + d) * dx, 0.0, 0.0)) return false;
+            return true;
+        }
+        const int i = axis == 0 ? L : k, j = axis == 0 ? k : L;
+        if (bh.excised(j * dx, i * dx, 0.0)) return false;
+        for (int d = 1; d <= 2; d++)
+            if (bh.excised((j - d) * dx, i * dx, 0.0) || bh.excised((j + d) * dx, i * dx, 0.0) ||
+                bh.excised(j * dx, (i - d) * dx, 0.0) || bh.excised(j * dx, (i + d) * dx, 0.0))
+                return false;
+        return true;
+    }
+};
+
+struct Step {
+    double dx, dt, w;
+    int lim, axis;
+};
+
+// Half-step evolution of the middle state centred at xc to its two face primitives (either may be
+// null); the faces sit at xc -/+ dx/2.
+template <class Sys>
+RADJ_HD void evolve(const Sys& S, const Step& s, const D5* l, const D5* m, const D5* r, Pt xc, D5* left, D5* right) {
+    D5 ul[5], um[5], ur[5], sl[5];
+    S.cons(l, shift(xc, s.axis, -s.dx), ul);
+    S.cons(m, xc, um);
+    S.cons(r, shift(xc, s.axis, s.dx), ur);
+    slope_vector(ul, um, ur, s.w, s.lim, sl);
+    D5 UL[5], UR[5], FL[5], FR[5];
+    for (int k = 0; k < 5; k++) {
+        UL[k] = um[k] - (D5(0.5) * sl[k]);
+        UR[k] = um[k] + (D5(0.5) * sl[k]);
+    }
+    const Pt pl = shift(xc, s.axis, -(s.dx * 0.5)), pr = shift(xc, s.axis, s.dx * 0.5);
+    S.flux(UL, s.axis, pl, FL);
+    S.flux(UR, s.axis, pr, FR);
+    const D5 hs = D5(0.5 * (s.dt / s.dx));
+    D5 a[5], b[5];
+    for (int k = 0; k < 5; k++) {
+        const D5 ev = hs * (FL[k] - FR[k]);
+        a[k] = UL[k] + ev;
+        b[k] = UR[k] + ev;
+    }
+    if (left) S.prim(a, pl, left);
+    if (right) S.prim(b, pr, right);
+}
+
+// FORCE flux at face point xf between face primitives L (at xf - dx/2) and R (at xf + dx/2): the
+// mean of the Lax-Friedrichs flux and the flux of the Richtmyer state (at xf).
+template <class Sys> RADJ_HD void force(const Sys& S, const Step& s, const D5* L, const D5* R, Pt xf, D5* F) {
+    D5 uL[5], uR[5], fL[5], fR[5], us[5], fs[5];
+    const Pt pl = shift(xf, s.axis, -(s.dx * 0.5)), pr = shift(xf, s.axis, s.dx * 0.5);
+    S.cons(L, pl, uL);
+    S.cons(R, pr, uR);
+    S.flux(uL, s.axis, pl, fL);
+    S.flux(uR, s.axis, pr, fR);
+    const D5 c = D5(s.dx / s.dt), d = D5(s.dt / s.dx);
+    for (int k = 0; k < 5; k++) us[k] = D5(0.5) * ((uL[k] + uR[k]) + (d * (fL[k] - fR[k])));
+    S.flux(us, s.axis, xf, fs);
+    for (int k = 0; k < 5; k++) F[k] = D5(0.5) * ((D5(0.5) * ((fL[k] + fR[k]) + (c * (uL[k] - uR[k])))) + fs[k]);
+}
+
+// Position k of a line of n cells that a stencil position reads: transmissive mirror
+// (g[-1] = c[0], g[-2] = c[1], g[n] = c[n-1], g[n+1] = c[n-2]) or periodic wrap.  n >= 2.
+RADJ_HD int ghost(int k, int n, bool periodic) {
+    if (periodic) return ((k % n) + n) % n;
+    if (k < 0) return -1 - k;
+    if (k >= n) return 2 * n - 1 - k;
+    return k;
+}
+
+// One sweep's adjoint over a grid in structure-of-arrays storage: field f of cell (i, j) at
+// f * fstride + i * pitch + j, for the state (the sweep's input primitives), the output adjoint
+// and the input adjoint alike.  system 1 = SR, 2 = black hole (bh = M, a, x, y, z).
+struct Params {
+    int system, dims, nx, ny, pitch, periodic;
+    size_t fstride;
+    double gamma, bh[5];
+    Step s;
+    const double* state;
+    const double* pbar_out;
+    double* pbar_in;
+};
+
+// The input adjoint of cell c = i * nx + j.
+template <class Sys> RADJ_HD void cell_adjoint_sys(const Sys& S, const Params& P, size_t c) {
+    const int i = (int)(c / (size_t)P.nx), j = (int)(c % (size_t)P.nx);
+    const int axis = P.s.axis;
+    const bool per = P.periodic != 0;
+    const int n = axis == 0 ? P.nx : P.ny;
+    const int me = axis == 0 ? j : i, line = axis == 0 ? i : j;
+    const double dx = P.s.dx;
+    // storage offset of line position k: base + k * step
+    const size_t base = axis == 0 ? (size_t)i * P.pitch : (size_t)j;
+    const size_t step = axis == 0 ? 1 : (size_t)P.pitch;
+    int ks[5], nk = 0;
+    for (int t = -2; t <= 2; t++) {
+        int k = me + t;
+        if (per) k = ghost(k, n, true);
+        else if (k < 0 || k >= n) continue;
+        bool dup = false;
+        for (int q = 0; q < nk; q++) dup = dup || ks[q] == k;
+        if (!dup) ks[nk++] = k;
+    }
+    double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int q = 0; q < nk; q++) {
+        const int k = ks[q];
+        const size_t ok = base + (size_t)k * step;
+        if (!S.active(axis, line, k, n, dx)) {  // P'_k = P_k
+            if (k == me)
+                for (int f = 0; f < 5; f++) acc[f] = acc[f] + P.pbar_out[f * P.fstride + ok];
+            continue;
+        }
+        D5 win[5][5];
+        bool hit = false;
+        for (int p = 0; p < 5; p++) {
+            const int src = ghost(k - 2 + p, n, per);
+            const size_t off = base + (size_t)src * step;
+            for (int f = 0; f < 5; f++) win[p][f] = D5(P.state[f * P.fstride + off]);
+            if (src == me) {
+                hit = true;
+                for (int f = 0; f < 5; f++) win[p][f].d[f] = 1.0;
+            }
+        }
+        if (!hit) continue;
+        // face f at x = (f - 1/2) dx along the line, the line's coordinate across it
+        auto face_pt = [&](int f) -> Pt {
+            return axis == 0 ? Pt{(f - 0.5) * dx, line * dx, 0.0} : Pt{line * dx, (f - 0.5) * dx, 0.0};
+        };
+        const Pt ck = axis == 0 ? Pt{k * dx, line * dx, 0.0} : Pt{line * dx, k * dx, 0.0};
+        D5 F0[5], F1[5];
+        if (Sys::coords) {
+            D5 er[5], el[5];
+            const Pt x0 = face_pt(k), x1 = face_pt(k + 1);
+            evolve(S, P.s, win[0], win[1], win[2], shift(x0, axis, -(dx * 0.5)), (D5*)nullptr, er);
+            evolve(S, P.s, win[1], win[2], win[3], shift(x0, axis, dx * 0.5), el, (D5*)nullptr);
+            force(S, P.s, er, el, x0, F0);
+            evolve(S, P.s, win[1], win[2], win[3], shift(x1, axis, -(dx * 0.5)), (D5*)nullptr, er);
+            evolve(S, P.s, win[2], win[3], win[4], shift(x1, axis, dx * 0.5), el, (D5*)nullptr);
+            force(S, P.s, er, el, x1, F1);
+        } else {
+            D5 Bm[5], A0[5], B0[5], A1[5];
+            evolve(S, P.s, win[0], win[1], win[2], ck, (D5*)nullptr, Bm);
+            evolve(S, P.s, win[1], win[2], win[3], ck, A0, B0);
+            evolve(S, P.s, win[2], win[3], win[4], ck, A1, (D5*)nullptr);
+            force(S, P.s, Bm, A0, ck, F0);
+            force(S, P.s, B0, A1, ck, F1);
+        }
+        D5 u[5], nu[5], o[5];
+        S.cons(win[2], ck, u);
+        const D5 d = D5(P.s.dt / dx);
+        for (int f = 0; f < 5; f++) nu[f] = u[f] + (d * (F0[f] - F1[f]));
+        S.prim(nu, ck, o);
+        for (int f = 0; f < 5; f++) {
+            const double pb = P.pbar_out[f * P.fstride + ok];
+            for (int l = 0; l < 5; l++) acc[l] = acc[l] + (o[f].d[l] * pb);
+        }
+    }
+    const size_t me_off = base + (size_t)me * step;
+    for (int f = 0; f < 5; f++) P.pbar_in[f * P.fstride + me_off] = acc[f];
+}
+
+RADJ_HD void cell_adjoint(const Params& P, size_t c) {
+    if (P.system == 2)
+        cell_adjoint_sys(GRSys{P.gamma, KerrSchild{P.bh[0], P.bh[1], P.bh[2], P.bh[3], P.bh[4]}, P.dims}, P, c);
+    else
+        cell_adjoint_sys(SRSys{P.gamma}, P, c);
+}
+
+}  // namespace radj
+}  // namespace cg

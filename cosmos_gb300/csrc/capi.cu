@@ -183,8 +183,10 @@ namespace cg {
 // the same device time step -- on explicit buffers: the step reads `src` and its sweep k writes
 // dst[k] (three sweeps in 2D, one in 1D).
 int enqueue_step_into(cosmos_grid* g, const void* src, void* const* dst) {
-    if (g->p.system == COSMOS_GR) return fail(COSMOS_EUNSUPPORTED, "explicit-buffer steps cover the Newtonian and SR systems");
+    const bool gr = g->p.system == COSMOS_GR;
     const cosmos_solve_opts& o = g->run;
+    if (gr && o.subcycles != 0)
+        return fail(COSMOS_EUNSUPPORTED, "explicit-buffer steps of a black-hole grid cover the flux step (zero subcycles)");
     CK(launch_dt_kernel(g->ctl, g->ctx->stream));
     SweepArgs a = base_args(g);
     a.order = o.order;
@@ -201,8 +203,14 @@ int enqueue_step_into(cosmos_grid* g, const void* src, void* const* dst) {
         a.ds.fsel = scale == 0.5 ? 1 : 0;
         a.src = k == 0 ? src : dst[k - 1];
         a.dst = dst[k];
-        a.out.ws_ctl = k == ns - 1 ? g->ctl : nullptr;  // the CFL reduction of the step's last sweep
+        a.out.ws_ctl = k == ns - 1 && !gr ? g->ctl : nullptr;  // the CFL reduction of the step's last sweep
         CK(sweep_launch(g, a));
+    }
+    if (gr) {  // the black-hole CFL reduction runs on the step's final state, as in enqueue_step
+        SweepArgs w = base_args(g);
+        w.src = dst[ns - 1];
+        w.out.ws_ctl = g->ctl;
+        CK(g->p.precision == COSMOS_FP64 ? launch_wavespeed_exact(w, nullptr) : launch_wavespeed_gr_fast(w, nullptr));
     }
     return COSMOS_OK;
 }

@@ -1,5 +1,6 @@
 // C ABI of the hand-written adjoint: reverse-mode gradient of a final-density misfit through
-// nsteps SLIC steps of a Newtonian grid, with checkpoints every `checkpoint_every` steps.
+// nsteps SLIC steps of a Newtonian grid (or an FP64 SR grid, or the flux steps of an FP64
+// black-hole grid), with checkpoints every `checkpoint_every` steps.
 //
 // Forward: the grid's own graph-replayed steps (device dt from the CFL rule, or the caller's dts),
 // the state copied to a checkpoint store before every segment and each step's dt logged.
@@ -69,13 +70,13 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
                                    const double* target, const double* dts_in, double* grad_prim, double* loss,
                                    double* dts_out, double* ms) {
     if (!g || !o || !target || !grad_prim) return afail(COSMOS_EINVAL, "null grid, options, target or gradient");
-    const bool sr = g->p.system == COSMOS_SR;
-    if (g->p.system != COSMOS_NEWTONIAN && !sr)
-        return afail(COSMOS_EUNSUPPORTED, "the adjoint covers the Newtonian and special-relativistic systems");
-    if (sr && g->p.precision != COSMOS_FP64)
-        return afail(COSMOS_EUNSUPPORTED, "the special-relativistic adjoint covers FP64 grids");
-    if (sr && (g->G.nx < 2 || (g->p.dims == 2 && g->G.ny < 2)))
-        return afail(COSMOS_EUNSUPPORTED, "the special-relativistic adjoint needs at least two cells per swept line");
+    // SR and black-hole grids (FP64) run the relativistic sweep adjoints on primitive adjoints; the
+    // black-hole step is differentiated without its source terms (the forward runs zero subcycles)
+    const bool rel = g->p.system == COSMOS_SR || g->p.system == COSMOS_GR;
+    if (rel && g->p.precision != COSMOS_FP64)
+        return afail(COSMOS_EUNSUPPORTED, "the relativistic adjoints cover FP64 grids");
+    if (rel && (g->G.nx < 2 || (g->p.dims == 2 && g->G.ny < 2)))
+        return afail(COSMOS_EUNSUPPORTED, "the relativistic adjoints need at least two cells per swept line");
     if (o->order != 2) return afail(COSMOS_EUNSUPPORTED, "the adjoint covers SLIC (order 2)");
     if (nsteps < 1 || checkpoint_every < 1) return afail(COSMOS_EINVAL, "nsteps and checkpoint_every must be >= 1");
     if (!dts_in && !(o->cfl > 0.0)) return afail(COSMOS_EINVAL, "cfl must be positive when no dts are given");
@@ -116,7 +117,7 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
     cosmos_solve_opts fo = *o;
     fo.t_final = 1e300;  // exactly nsteps steps
     fo.max_steps = nsteps;
-    fo.subcycles = 1;
+    fo.subcycles = g->p.system == COSMOS_GR ? 0 : 1;
     if (dts_in) fo.cfl = 1.0;
     int rc = cosmos_grid_run_begin(g, &fo);
     if (rc) return rc;
@@ -174,6 +175,7 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
     ap.dx = g->p.dx;
     ap.bias = o->bias;
     ap.gamma = g->p.gamma;
+    const double bh[5] = {g->p.bh_mass, g->p.bh_spin, g->p.bh_x, g->p.bh_y, g->p.bh_z};
     // The recomputation of segment c - 1 (forward sweeps, on the context's second stream) runs
     // while the sweep adjoints of segment c run on the compute stream; the two segments use
     // alternate halves of `seg`, and events order each half's writer and reader.
@@ -227,9 +229,9 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
             ap.state = slot(c, q);
             ap.ubar_out = adj + (size_t)cur * abytes;
             ap.ubar_in = adj + (size_t)(cur ^ 1) * abytes;
-            if (sr)
-                ACK(launch_adjoint_sr_sweep(ap.G, g->p.gamma, g->p.dx, dt, o->bias, o->limiter, ap.state, ap.ubar_out,
-                                            ap.ubar_in, st));
+            if (rel)
+                ACK(launch_adjoint_rel_sweep(ap.G, g->p.system, g->p.gamma, bh, g->p.dx, dt, o->bias, o->limiter, ap.state,
+                                             ap.ubar_out, ap.ubar_in, st));
             else
                 ACK(fp64 ? launch_adjoint_sweep_exact(ap, o->limiter, st) : launch_adjoint_sweep_fast(ap, o->limiter, st));
             cur ^= 1;
@@ -237,8 +239,8 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
         ACK(cudaEventRecord(sc.adj_done[c & 1], st));
     }
     // ---- gradient with respect to the initial primitives
-    if (sr)  // the SR sweep adjoints carry primitive adjoints already
-        ACK(launch_adjoint_sr_grad(G0, adj + (size_t)cur * abytes, g->staging, st));
+    if (rel)  // the relativistic sweep adjoints carry primitive adjoints already
+        ACK(launch_adjoint_rel_grad(G0, adj + (size_t)cur * abytes, g->staging, st));
     else
         ACK(fp64 ? launch_adjoint_grad_exact(G0, g->p.gamma, ck, adj + (size_t)cur * abytes, g->staging, st)
                  : launch_adjoint_grad_fast(G0, g->p.gamma, ck, adj + (size_t)cur * abytes, g->staging, st));

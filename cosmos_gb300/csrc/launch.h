@@ -145,10 +145,11 @@ cudaError_t launch_adjoint_grad_exact(const Geom& G, double gamma, const void* s
                                       cudaStream_t st);
 cudaError_t launch_adjoint_grad_fast(const Geom& G, double gamma, const void* state, const void* ubar, double* grad,
                                      cudaStream_t st);
-// Special-relativistic FP64 sweep adjoint on primitive adjoints (kernels_adjoint_sr.cu), and the
-// copy of the final primitive adjoint into AoS doubles.
-cudaError_t launch_adjoint_sr_sweep(const Geom& G, double gamma, double dx, double dt, double bias, int lim,
-                                    const void* state, const void* pbar_out, void* pbar_in, cudaStream_t st);
-cudaError_t launch_adjoint_sr_grad(const Geom& G, const void* pbar, double* grad, cudaStream_t st);
+// Relativistic FP64 sweep adjoints on primitive adjoints (kernels_adjoint_rel.cu; system 1 SR,
+// 2 black hole with bh = M, a, x, y, z), and the copy of the final primitive adjoint into AoS doubles.
+cudaError_t launch_adjoint_rel_sweep(const Geom& G, int system, double gamma, const double* bh, double dx, double dt,
+                                     double bias, int lim, const void* state, const void* pbar_out, void* pbar_in,
+                                     cudaStream_t st);
+cudaError_t launch_adjoint_rel_grad(const Geom& G, const void* pbar, double* grad, cudaStream_t st);
 
 }  // namespace cg

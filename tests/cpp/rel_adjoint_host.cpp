@@ -1,16 +1,17 @@
-// Host build of the special-relativistic sweep adjoint's cell function (the body of
-// sr_adjoint_sweep_kernel) for the CPU tests.  AoS (ny, nx, 5) doubles in and out; in between a
+// Host build of the relativistic sweep adjoint's cell function (the body of
+// rel_adjoint_sweep_kernel) for the CPU tests.  AoS (ny, nx, 5) doubles in and out; in between a
 // structure-of-arrays copy with the device grid's kind of padding (row pitch nx + 3, field stride
 // ny * pitch + 5) whose padding holds NaN, so a read outside the cells it should touch shows up
-// in the result.
+// in the result.  system 1 = SR, 2 = black hole (bh = M, a, x, y, z; dims 1 or 2).
 #include <cstddef>
 #include <limits>
 #include <vector>
 
-#include "../../cosmos_gb300/csrc/adjoint_sr.cuh"
+#include "../../cosmos_gb300/csrc/adjoint_rel.cuh"
 
-extern "C" int sra_host_sweep_adjoint(const double* state, const double* pbar_out, double* pbar_in, int ny, int nx,
-                                      int axis, int bc, double gamma, double dx, double dt, double bias, int lim) {
+extern "C" int rel_host_sweep_adjoint(int system, int dims, const double* state, const double* pbar_out,
+                                      double* pbar_in, int ny, int nx, int axis, int bc, double gamma, const double* bh,
+                                      double dx, double dt, double bias, int lim) {
     if (nx < 2 || ny < 1 || (axis == 1 && ny < 2)) return 1;
     const int pitch = nx + 3;
     const size_t fstride = (size_t)ny * pitch + 5;
@@ -22,18 +23,21 @@ extern "C" int sra_host_sweep_adjoint(const double* state, const double* pbar_ou
                 s[f * fstride + (size_t)i * pitch + j] = state[((size_t)i * nx + j) * 5 + f];
                 po[f * fstride + (size_t)i * pitch + j] = pbar_out[((size_t)i * nx + j) * 5 + f];
             }
-    cg::sra::Params P;
+    cg::radj::Params P;
+    P.system = system;
+    P.dims = dims;
     P.nx = nx;
     P.ny = ny;
     P.pitch = pitch;
-    P.axis = axis;
     P.periodic = bc == 1;
     P.fstride = fstride;
-    P.s = cg::sra::Step{gamma, dx, dt, bias, lim, axis};
+    P.gamma = gamma;
+    for (int k = 0; k < 5; k++) P.bh[k] = bh ? bh[k] : 0.0;
+    P.s = cg::radj::Step{dx, dt, bias, lim, axis};
     P.state = s.data();
     P.pbar_out = po.data();
     P.pbar_in = pi.data();
-    for (size_t c = 0; c < (size_t)nx * ny; c++) cg::sra::cell_adjoint(P, c);
+    for (size_t c = 0; c < (size_t)nx * ny; c++) cg::radj::cell_adjoint(P, c);
     for (int i = 0; i < ny; i++)
         for (int j = 0; j < nx; j++)
             for (int f = 0; f < 5; f++) pbar_in[((size_t)i * nx + j) * 5 + f] = pi[f * fstride + (size_t)i * pitch + j];
