@@ -453,54 +453,55 @@ template <class Num> struct GRT {
             }
     }
     // BlackHoleEuler/BlackHoleEulerStateVector.cpp:359-510
-    void source(const double* u, Pt q, double* s) const {
+    // State-dependent parts in Num (the tangent-linear model's dual numbers), the metric in FP64.
+    void source(const Num* u, Pt q, Num* s) const {
         double dg = detg(q);
         double al = bh.lapse(q.x, q.y, q.z), be[3];
         bh.shiftv(q.x, q.y, q.z, be);
-        C2P c = c2p(u, q, 1e-8);
+        C2PT<Num> c = c2p(u, q, 1e-8);
         double g4m[16], gi[16];
         bh.g4(q.x, q.y, q.z, g4m);
         inverse_n(g4m, 4, gi);
-        double uu[4];
-        uu[0] = c.W / al;
-        uu[1] = ((al * uu[0]) * c.vx) - (be[0] * uu[0]);
-        uu[2] = ((al * uu[0]) * c.vy) - (be[1] * uu[0]);
-        uu[3] = ((al * uu[0]) * c.vz) - (be[2] * uu[0]);
-        double T[16];
+        Num uu[4];
+        uu[0] = c.W / Num(al);
+        uu[1] = ((Num(al) * uu[0]) * c.vx) - (Num(be[0]) * uu[0]);
+        uu[2] = ((Num(al) * uu[0]) * c.vy) - (Num(be[1]) * uu[0]);
+        uu[3] = ((Num(al) * uu[0]) * c.vz) - (Num(be[2]) * uu[0]);
+        Num T[16];
         for (int i = 0; i < 4; i++)
-            for (int j = 0; j < 4; j++) T[4 * i + j] = (((c.rho * c.h) * uu[i]) * uu[j]) + (c.p * gi[4 * i + j]);
+            for (int j = 0; j < 4; j++) T[4 * i + j] = (((c.rho * c.h) * uu[i]) * uu[j]) + (c.p * Num(gi[4 * i + j]));
         double da[3], db[9], gm[9], dgm[27], K[9];
         dalpha(q, da);
         dbeta(q, db);
         bh.gamma(q.x, q.y, q.z, gm);
         dgamma(q, dgm);
         Kij(q, K);
-        double S[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-        double vc[3];
-        for (int i = 0; i < 3; i++) vc[i] = ((gm[3 * i + 0] * c.vx) + (gm[3 * i + 1] * c.vy)) + (gm[3 * i + 2] * c.vz);
-        double rhw = (c.rho * c.h) * (c.W * c.W);
+        Num S[5] = {Num(0.0), Num(0.0), Num(0.0), Num(0.0), Num(0.0)};
+        Num vc[3];
+        for (int i = 0; i < 3; i++) vc[i] = ((Num(gm[3 * i + 0]) * c.vx) + (Num(gm[3 * i + 1]) * c.vy)) + (Num(gm[3 * i + 2]) * c.vz);
+        Num rhw = (c.rho * c.h) * (c.W * c.W);
         for (int i = 0; i < 3; i++) {
             for (int j = 0; j < 3; j++) {
                 for (int k = 0; k < 3; k++) {
                     double dgijk = dgm[9 * i + 3 * j + k];
-                    S[i + 1] = S[i + 1] + (T[0] * (((0.5 * be[j]) * be[k]) * dgijk));
-                    S[i + 1] = S[i + 1] + ((T[j + 1] * be[k]) * dgijk);
-                    S[i + 1] = S[i + 1] + (0.5 * (T[4 * (j + 1) + (k + 1)] * dgijk));
+                    S[i + 1] = S[i + 1] + (T[0] * Num(((0.5 * be[j]) * be[k]) * dgijk));
+                    S[i + 1] = S[i + 1] + ((T[j + 1] * Num(be[k])) * Num(dgijk));
+                    S[i + 1] = S[i + 1] + (Num(0.5) * (T[4 * (j + 1) + (k + 1)] * Num(dgijk)));
                 }
-                S[i + 1] = S[i + 1] + (((rhw * vc[j]) / al) * db[3 * i + j]);
+                S[i + 1] = S[i + 1] + (((rhw * vc[j]) / Num(al)) * Num(db[3 * i + j]));
             }
-            S[i + 1] = S[i + 1] - ((T[0] * al) * da[i]);
+            S[i + 1] = S[i + 1] - ((T[0] * Num(al)) * Num(da[i]));
         }
         for (int i = 0; i < 3; i++) {
             for (int j = 0; j < 3; j++) {
-                S[4] = S[4] + (T[0] * ((be[i] * be[j]) * K[3 * i + j]));
-                S[4] = S[4] + (T[i + 1] * ((2.0 * be[j]) * K[3 * i + j]));
-                S[4] = S[4] + (T[4 * (i + 1) + (j + 1)] * K[3 * i + j]);
+                S[4] = S[4] + (T[0] * Num((be[i] * be[j]) * K[3 * i + j]));
+                S[4] = S[4] + (T[i + 1] * Num((2.0 * be[j]) * K[3 * i + j]));
+                S[4] = S[4] + (T[4 * (i + 1) + (j + 1)] * Num(K[3 * i + j]));
             }
-            S[4] = S[4] - (T[0] * (be[i] * da[i]));
-            S[4] = S[4] - (T[i + 1] * da[i]);
+            S[4] = S[4] - (T[0] * Num(be[i] * da[i]));
+            S[4] = S[4] - (T[i + 1] * Num(da[i]));
         }
-        double f = al * std::sqrt(dg);
+        Num f = Num(al * std::sqrt(dg));
         for (int k = 0; k < 5; k++) s[k] = f * S[k];
     }
     // BlackHoleEuler/BlackHoleEulerStateVector.cpp:519-549 with
@@ -740,46 +741,47 @@ static double gr_max_wavespeed(const GR& S, const double* prim, int ny, int nx, 
 
 // ---------------------------------------------------------------- GR source RK step
 // Solvers/BlackHoleEulerSolvers.cpp:159-232: fractional evolution with face fluxes at xc -/+ dx
-template <class P>
-static void evolve_fraction(const GR& S, double frac, const double* l, const double* m, const double* r, P xc, int axis,
-                            double dx, double dt, double w, int lim, double* out) {
-    double ul[5], um[5], ur[5], sl[5];
+template <class Sys, class T, class P>
+static void evolve_fraction(const Sys& S, double frac, const T* l, const T* m, const T* r, P xc, int axis, double dx,
+                            double dt, double w, int lim, T* out) {
+    T ul[5], um[5], ur[5], sl[5];
     S.cons(l, shift(xc, axis, -dx), ul);
     S.cons(m, xc, um);
     S.cons(r, shift(xc, axis, dx), ur);
     slope_vector(ul, um, ur, w, lim, sl);
-    double UL[5], UR[5], FL[5], FR[5];
-    for (int k = 0; k < 5; k++) { UL[k] = um[k] - (0.5 * sl[k]); UR[k] = um[k] + (0.5 * sl[k]); }
+    T UL[5], UR[5], FL[5], FR[5];
+    for (int k = 0; k < 5; k++) { UL[k] = um[k] - (T(0.5) * sl[k]); UR[k] = um[k] + (T(0.5) * sl[k]); }
     S.flux(UL, axis, shift(xc, axis, -dx), FL);
     S.flux(UR, axis, shift(xc, axis, dx), FR);
-    const double s = frac * (dt / dx);
-    double nu[5];
+    const T s = T(frac * (dt / dx));
+    T nu[5];
     for (int k = 0; k < 5; k++) nu[k] = um[k] + (s * (FL[k] - FR[k]));
     S.prim(nu, xc, out);
 }
 
 // Solvers/BlackHoleEulerForcingSolver.cpp:3-70 (1D) and :72-185 (2D): classical RK4 on the
 // source with interleaved fractional flux sweeps on frozen neighbours.
-static void rk_cell(const GR& S, int dims, const double* cl, const double* cm, const double* cr, const double* ct,
-                    const double* cb, Pt q, double dx, double dt, double w, int lim, double* out_cons) {
-    double L[5], R[5], Tp[5], B[5], Mp[5], E1[5], E2[5], E[5];
+template <class Sys, class T>
+static void rk_cell(const Sys& S, int dims, const T* cl, const T* cm, const T* cr, const T* ct, const T* cb, Pt q,
+                    double dx, double dt, double w, int lim, T* out_cons) {
+    T L[5], R[5], Tp[5], B[5], Mp[5], E1[5], E2[5], E[5];
     S.prim(cl, shift(q, 0, -dx), L);
     S.prim(cr, shift(q, 0, dx), R);
     if (dims == 2) {
         S.prim(ct, shift(q, 1, -dx), Tp);
         S.prim(cb, shift(q, 1, dx), B);
     }
-    double k[4][5], st[5], c[5];
-    auto src = [&](const double* u, double* o) {
-        double s[5];
+    T k[4][5], st[5], c[5];
+    auto src = [&](const T* u, T* o) {
+        T s[5];
         S.source(u, q, s);
-        for (int i = 0; i < 5; i++) o[i] = dt * s[i];
+        for (int i = 0; i < 5; i++) o[i] = T(dt) * s[i];
     };
     src(cm, k[0]);
     const double fx1[3] = {0.5, 0.5, 1.0};                                     // 1D fractions
     const double fx2[3] = {0.25, 0.25, 0.5}, fy2[3] = {0.5, 0.5, 1.0};        // 2D fractions
     for (int stage = 0; stage < 3; stage++) {
-        for (int i = 0; i < 5; i++) st[i] = stage < 2 ? (cm[i] + (0.5 * k[stage][i])) : (cm[i] + k[stage][i]);
+        for (int i = 0; i < 5; i++) st[i] = stage < 2 ? (cm[i] + (T(0.5) * k[stage][i])) : (cm[i] + k[stage][i]);
         S.prim(st, q, Mp);
         if (dims == 1) {
             evolve_fraction(S, fx1[stage], L, Mp, R, q, 0, dx, dt, w, lim, E);
@@ -792,14 +794,15 @@ static void rk_cell(const GR& S, int dims, const double* cl, const double* cm, c
         src(c, k[stage + 1]);
     }
     for (int i = 0; i < 5; i++)
-        out_cons[i] = cm[i] + ((1.0 / 6.0) * (k[0][i] + ((2.0 * k[1][i]) + ((2.0 * k[2][i]) + k[3][i]))));
+        out_cons[i] = cm[i] + (T(1.0 / 6.0) * (k[0][i] + ((T(2.0) * k[1][i]) + ((T(2.0) * k[2][i]) + k[3][i]))));
 }
 
 // Solvers/BlackHoleEulerForcingSolver.cpp:187-250 (transmissive 1-ghost neighbours)
-static void rk_source(const GR& S, double* prim, int ny, int nx, int dims, double dx, double dt, double w, int lim) {
+template <class Sys, class T>
+static void rk_source(const Sys& S, T* prim, int ny, int nx, int dims, double dx, double dt, double w, int lim) {
     if (dims == 1) ny = 1;
-    std::vector<double> out((size_t)ny * nx * 5);
-    std::memcpy(out.data(), prim, out.size() * sizeof(double));
+    std::vector<T> out((size_t)ny * nx * 5);
+    std::memcpy(out.data(), prim, out.size() * sizeof(T));
     for (int i = 0; i < ny; i++)
         for (int j = 0; j < nx; j++) {
             bool on;
@@ -811,11 +814,11 @@ static void rk_source(const GR& S, double* prim, int ny, int nx, int dims, doubl
                      !S.bh.excised((j + 1) * dx, i * dx, 0.0) && !S.bh.excised(j * dx, (i - 1) * dx, 0.0) &&
                      !S.bh.excised(j * dx, (i + 1) * dx, 0.0);
             if (!on) continue;
-            auto P = [&](int ii, int jj) -> const double* {
+            auto P = [&](int ii, int jj) -> const T* {
                 return prim + 5 * ((size_t)ghost(ii, ny, 0) * nx + ghost(jj, nx, 0));
             };
             Pt q = dims == 1 ? Pt{j * dx, 0.0, 0.0} : Pt{j * dx, i * dx, 0.0};
-            double cl[5], cm[5], cr[5], ct[5], cb[5], nc[5];
+            T cl[5], cm[5], cr[5], ct[5], cb[5], nc[5];
             S.cons(P(i, j - 1), dims == 1 ? Pt{(j - 1) * dx, 0.0, 0.0} : Pt{(j - 1) * dx, i * dx, 0.0}, cl);
             S.cons(P(i, j), q, cm);
             S.cons(P(i, j + 1), dims == 1 ? Pt{(j + 1) * dx, 0.0, 0.0} : Pt{(j + 1) * dx, i * dx, 0.0}, cr);
@@ -826,7 +829,7 @@ static void rk_source(const GR& S, double* prim, int ny, int nx, int dims, doubl
             rk_cell(S, dims, cl, cm, cr, ct, cb, q, dx, dt, w, lim, nc);
             S.prim(nc, q, &out[5 * ((size_t)i * nx + j)]);
         }
-    std::memcpy(prim, out.data(), out.size() * sizeof(double));
+    std::memcpy(prim, out.data(), out.size() * sizeof(T));
 }
 
 }  // namespace orc
@@ -1376,18 +1379,25 @@ int orc_amr_level2(int sys, const double* prim, int ny, int nx, int dims, double
 template <class Sys>
 static double tlm_run(const Sys& S, const double* prim0, const double* dprim, const double* target, int ny, int nx,
                       int dims, double dx, const double* dts, int nsteps, double bias, int lim, int bc, double* dL,
-                      const BH* exc = nullptr) {
+                      const BH* exc = nullptr, int subcycles = 0) {
     size_t N = (size_t)(dims == 1 ? 1 : ny) * nx;
     std::vector<Dual> p(5 * N);
     for (size_t i = 0; i < 5 * N; i++) p[i] = Dual(prim0[i], dprim ? dprim[i] : 0.0);
     for (int s = 0; s < nsteps; s++) {
         double dt = dts[s];
+        // black hole: `subcycles` RK source half-steps (bias 0, limiter 1) around the flux step
+        auto source_steps = [&]() {
+            if constexpr (Sys::coords)
+                for (int c = 0; c < subcycles; c++) rk_source(S, p.data(), ny, nx, dims, dx, 0.5 * (dt / subcycles), 0.0, 1);
+        };
+        source_steps();
         if (dims == 1) sweep(S, p.data(), ny, nx, 1, 0, 2, dx, dt, bias, lim, bc, nullptr, exc);
         else {
             sweep(S, p.data(), ny, nx, 2, 0, 2, dx, 0.5 * dt, bias, lim, bc, nullptr, exc);
             sweep(S, p.data(), ny, nx, 2, 1, 2, dx, dt, bias, lim, bc, nullptr, exc);
             sweep(S, p.data(), ny, nx, 2, 0, 2, dx, 0.5 * dt, bias, lim, bc, nullptr, exc);
         }
+        source_steps();
     }
     Dual L(0.0);
     for (size_t c = 0; c < N; c++) {
@@ -1414,14 +1424,18 @@ double orc_tlm_sr(const double* prim0, const double* dprim, const double* target
     return tlm_run(SRT<Dual>{gamma}, prim0, dprim, target, ny, nx, dims, dx, dts, nsteps, bias, lim, bc, dL);
 }
 
-// The same for the black-hole flux step without source terms (BlackHoleEulerSecondOrderSolver's
-// step with zero subcycles, Solvers/BlackHoleEulerSecondOrderSolver.cpp:181-218): the metric enters as
-// FP64 data, cells whose stencil touches the excision region keep their state (derivative carried
-// through unchanged), transmissive boundaries.  bh = {M, a, x, y, z}.
+// The same for the black-hole step (BlackHoleEulerSecondOrderSolver's step,
+// Solvers/BlackHoleEulerSecondOrderSolver.cpp:181-218): `subcycles` RK source half-steps
+// (Solvers/BlackHoleEulerForcingSolver.cpp:3-250, the source term of
+// BlackHoleEulerStateVector.cpp:359-510 in dual numbers) before and after the flux step; 0 gives
+// the flux step alone.  The metric and its derivatives enter as FP64 data, cells whose stencil
+// touches the excision region keep their state (derivative carried through unchanged),
+// transmissive boundaries.  bh = {M, a, x, y, z}.
 double orc_tlm_gr(const double* prim0, const double* dprim, const double* target, int ny, int nx, int dims, double dx,
-                  const double* dts, int nsteps, double bias, int lim, double gamma, const double* bh, double* dL) {
+                  const double* dts, int nsteps, double bias, int lim, double gamma, const double* bh, int subcycles,
+                  double* dL) {
     GRT<Dual> S{gamma, BH{bh[0], bh[1], bh[2], bh[3], bh[4]}, dx};
-    return tlm_run(S, prim0, dprim, target, ny, nx, dims, dx, dts, nsteps, bias, lim, 0, dL, &S.bh);
+    return tlm_run(S, prim0, dprim, target, ny, nx, dims, dx, dts, nsteps, bias, lim, 0, dL, &S.bh, subcycles);
 }
 
 }  // extern "C"

@@ -78,7 +78,7 @@ class Oracle:
         L.orc_tlm_newton.restype = _d
         L.orc_tlm_sr.argtypes = [_p, _p, _p, _i, _i, _i, _d, _p, _i, _d, _i, _d, _i, _p]
         L.orc_tlm_sr.restype = _d
-        L.orc_tlm_gr.argtypes = [_p, _p, _p, _i, _i, _i, _d, _p, _i, _d, _i, _d, _p, _p]
+        L.orc_tlm_gr.argtypes = [_p, _p, _p, _i, _i, _i, _d, _p, _i, _d, _i, _d, _p, _i, _p]
         L.orc_tlm_gr.restype = _d
         L.orc_set_threads.argtypes = [_i]
 
@@ -221,8 +221,9 @@ class Oracle:
                               ctypes.byref(out))
         return L, out.value
 
-    def tlm_gr(self, prim0, dprim, target, dx, dts, bias, lim, gamma, bh):
-        """The black-hole flux-step tangent-linear model (no source terms): (loss, directional derivative)."""
+    def tlm_gr(self, prim0, dprim, target, dx, dts, bias, lim, gamma, bh, subcycles=0):
+        """The black-hole step's tangent-linear model (`subcycles` RK source half-steps around the flux
+        step; 0: the flux step alone): (loss, directional derivative)."""
         p = np.ascontiguousarray(prim0, dtype=np.float64)
         d = np.ascontiguousarray(dprim, dtype=np.float64)
         t = np.ascontiguousarray(target, dtype=np.float64)
@@ -230,7 +231,7 @@ class Oracle:
         ny, nx, dims = _shape(p)
         out = _d(0.0)
         L = self.L.orc_tlm_gr(_ptr(p), _ptr(d), _ptr(t), ny, nx, dims, dx, _ptr(ds), len(ds), bias, lim, gamma,
-                              _ptr(_bh(bh)), ctypes.byref(out))
+                              _ptr(_bh(bh)), int(subcycles), ctypes.byref(out))
         return L, out.value
 
     def tlm_newton(self, prim0, dprim, target, dx, dts, bias, lim, gamma, bc=0):
