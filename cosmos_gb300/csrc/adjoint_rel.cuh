@@ -1,5 +1,6 @@
 // Adjoint (vector-Jacobian product) of one relativistic SLIC sweep, FP64, gather form: the
-// special-relativistic sweep and the black-hole flux sweep (excision, no source terms).
+// special-relativistic sweep and the black-hole flux sweep (excision); and of one black-hole RK
+// source step (rk_cell_adjoint, at the end).
 //
 // Forward map of a sweep along a line of n cells (primitive states P, dt and dx fixed):
 //   SR  (Solvers/RelativisticEulerSecondOrderSolver.cpp:3-100, the half-step evolution of
@@ -232,6 +233,58 @@ struct KerrSchild {
         const double r = ::sqrt((((x - bx) * (x - bx)) + ((y - by) * (y - by))) + ((z - bz) * (z - bz)));
         return r <= (M * (1.0 + ::sqrt(1.0 - (a * a))));
     }
+    // BlackHoleSpacetime.cpp:92-113 with "r + (y - y_BH)" of :108 as written, and :188-228
+    RADJ_HD void g4(Pt q, double* m) const {
+        const double dx = q.x - bx, dy = q.y - by, dz = q.z - bz;
+        const double n2 = ((dx * dx) + (dy * dy)) + (dz * dz);
+        const double ma2 = (M * M) * (a * a);
+        const double r = ::sqrt(0.5 * ((n2 - ma2) + ::sqrt(((n2 - ma2) * (n2 - ma2)) + (4.0 * (ma2 * (dz * dz))))));
+        const double h = -(M * ((r * r) * r)) / ((((r * r) * r) * r) + (ma2 * (dz * dz)));
+        const double l[4] = {-1.0, -((r * dx) + ((a * M) * dy)) / ((r * r) + ma2),
+                             -((r + dy) - ((a * M) * dx)) / ((r * r) + ma2), -dz / r};
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) {
+                const double eta = (i == j) ? ((i == 0) ? -1.0 : 1.0) : 0.0;
+                m[4 * i + j] = eta - (((2.0 * h) * l[i]) * l[j]);
+            }
+    }
+    // Mathematics/MatrixAlgebra.cpp:106-194: cofactor determinant, Cayley-Hamilton inverse
+    RADJ_HD static double det4(const double* m) {
+        double d = 0.0;
+        for (int i = 0; i < 4; i++) {
+            double c[9];
+            for (int j = 0; j < 3; j++)
+                for (int k = 0; k < 3; k++) c[3 * j + k] = (k < i) ? m[4 * (j + 1) + k] : m[4 * (j + 1) + k + 1];
+            if (i % 2 == 0) d = d + (m[i] * det3(c));
+            else d = d - (m[i] * det3(c));
+        }
+        return d;
+    }
+    RADJ_HD static void inverse4(const double* m, double* o) {
+        double m2[16], m3[16];
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) {
+                double s = 0.0;
+                for (int k = 0; k < 4; k++) s = s + (m[4 * i + k] * m[4 * k + j]);
+                m2[4 * i + j] = s;
+            }
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) {
+                double s = 0.0;
+                for (int k = 0; k < 4; k++) s = s + (m2[4 * i + k] * m[4 * k + j]);
+                m3[4 * i + j] = s;
+            }
+        double tr = 0.0, tr2 = 0.0, tr3 = 0.0;
+        for (int i = 0; i < 4; i++) tr = tr + m[5 * i];
+        for (int i = 0; i < 4; i++) tr2 = tr2 + m2[5 * i];
+        for (int i = 0; i < 4; i++) tr3 = tr3 + m3[5 * i];
+        const double c0 = (1.0 / 6.0) * ((((tr * tr) * tr) - ((3.0 * tr) * tr2)) + (2.0 * tr3));
+        const double c1 = 0.5 * ((tr * tr) - tr2);
+        const double inv = 1.0 / det4(m);
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++)
+                o[4 * i + j] = inv * ((((c0 * (i == j ? 1.0 : 0.0)) - (c1 * m[4 * i + j])) + (tr * m2[4 * i + j])) - m3[4 * i + j]);
+    }
 };
 
 // ---- black-hole state, BlackHoleEulerStateVector.cpp:30-350 (energy with W, not W^2, at :154;
@@ -240,6 +293,7 @@ struct GRSys {
     double g;
     KerrSchild bh;
     int dims;
+    double h;  // spacing of the metric's centred derivatives (the cell spacing)
     static constexpr bool coords = true;
     RADJ_HD void cons(const D5* p, Pt q, D5* u) const {
         double m[9];
@@ -279,6 +333,98 @@ struct GRSys {
         f[2] = as * ((rhw * (c.vy * w)) + (axis == 1 ? c.p : D5(0.0)));
         f[3] = as * (rhw * (c.vz * w));
         f[4] = as * ((((rhw - c.p) - (c.rho * c.W)) * w) + (c.p * vn));
+    }
+    // ---- the source term, BlackHoleEuler/BlackHoleEulerStateVector.cpp:359-510, with the metric's
+    // centred derivatives (spacing h) and extrinsic curvature, BlackHoleSpacetime.cpp:115-151, :230-370
+    RADJ_HD static Pt off(Pt q, int d, double s) {
+        if (d == 0) q.x = q.x + s;
+        else if (d == 1) q.y = q.y + s;
+        else q.z = q.z + s;
+        return q;
+    }
+    RADJ_HD void Kij(Pt q, double al, double* K) const {
+        double Hs, v[3], dh[3], dv[9];
+        bh.Hl(q.x, q.y, q.z, Hs, v);
+        const double hs = 0.5 * h;
+        for (int d = 0; d < 3; d++) {
+            const Pt p1 = off(q, d, hs), p0 = off(q, d, -hs);
+            double h1, h0, a1[3], a0[3];
+            bh.Hl(p1.x, p1.y, p1.z, h1, a1);
+            bh.Hl(p0.x, p0.y, p0.z, h0, a0);
+            dh[d] = (h1 - h0) / h;
+            for (int c = 0; c < 3; c++) dv[3 * d + c] = (1.0 / h) * (a1[c] - a0[c]);
+        }
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double k = al * ((((-(v[i] * dh[j])) - (v[j] * dh[i])) - (Hs * dv[3 * j + i])) - (Hs * dv[3 * i + j]));
+                for (int c = 0; c < 3; c++) {
+                    k = k + (((al * 2.0) * (Hs * Hs)) * (((v[i] * v[c]) * dv[3 * c + j]) + ((v[j] * v[c]) * dv[3 * c + i])));
+                    k = k + ((((((al * 2.0) * Hs) * v[i]) * v[j]) * v[c]) * dh[c]);
+                }
+                K[3 * i + j] = k;
+            }
+    }
+    RADJ_HD void source(const D5* u, Pt q, D5* s) const {
+        double gm[9];
+        bh.gamma(q, gm);
+        const double dg = KerrSchild::det3(gm);
+        double al, be[3];
+        bh.lapse_shift(q, al, be);
+        const D5 sg = D5(::sqrt(dg));
+        const D5 us[5] = {u[0] / sg, u[1] / sg, u[2] / sg, u[3] / sg, u[4] / sg};
+        const Prim c = con2prim(us, g, 1e-8);
+        double g4m[16], gi[16], da[3], db[9], dgm[27], K[9];
+        bh.g4(q, g4m);
+        KerrSchild::inverse4(g4m, gi);
+        const double hs = 0.5 * h;
+        for (int d = 0; d < 3; d++) {
+            const Pt p1 = off(q, d, hs), p0 = off(q, d, -hs);
+            double a1, a0, b1[3], b0[3], g1[9], g0[9];
+            bh.lapse_shift(p1, a1, b1);
+            bh.lapse_shift(p0, a0, b0);
+            bh.gamma(p1, g1);
+            bh.gamma(p0, g0);
+            da[d] = (a1 - a0) / h;
+            for (int k = 0; k < 3; k++) db[3 * d + k] = (1.0 / h) * (b1[k] - b0[k]);
+            for (int k = 0; k < 9; k++) dgm[9 * d + k] = (1.0 / h) * (g1[k] - g0[k]);
+        }
+        Kij(q, al, K);
+        D5 uu[4];
+        uu[0] = c.W / D5(al);
+        uu[1] = ((D5(al) * uu[0]) * c.vx) - (D5(be[0]) * uu[0]);
+        uu[2] = ((D5(al) * uu[0]) * c.vy) - (D5(be[1]) * uu[0]);
+        uu[3] = ((D5(al) * uu[0]) * c.vz) - (D5(be[2]) * uu[0]);
+        D5 T[16];
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) T[4 * i + j] = (((c.rho * c.h) * uu[i]) * uu[j]) + (c.p * D5(gi[4 * i + j]));
+        D5 S[5];
+        D5 vc[3];
+        for (int i = 0; i < 3; i++)
+            vc[i] = ((D5(gm[3 * i + 0]) * c.vx) + (D5(gm[3 * i + 1]) * c.vy)) + (D5(gm[3 * i + 2]) * c.vz);
+        const D5 rhw = (c.rho * c.h) * (c.W * c.W);
+        for (int i = 0; i < 3; i++) {
+            for (int j = 0; j < 3; j++) {
+                for (int k = 0; k < 3; k++) {
+                    const double dgijk = dgm[9 * i + 3 * j + k];
+                    S[i + 1] = S[i + 1] + (T[0] * D5(((0.5 * be[j]) * be[k]) * dgijk));
+                    S[i + 1] = S[i + 1] + ((T[j + 1] * D5(be[k])) * D5(dgijk));
+                    S[i + 1] = S[i + 1] + (D5(0.5) * (T[4 * (j + 1) + (k + 1)] * D5(dgijk)));
+                }
+                S[i + 1] = S[i + 1] + (((rhw * vc[j]) / D5(al)) * D5(db[3 * i + j]));
+            }
+            S[i + 1] = S[i + 1] - ((T[0] * D5(al)) * D5(da[i]));
+        }
+        for (int i = 0; i < 3; i++) {
+            for (int j = 0; j < 3; j++) {
+                S[4] = S[4] + (T[0] * D5((be[i] * be[j]) * K[3 * i + j]));
+                S[4] = S[4] + (T[i + 1] * D5((2.0 * be[j]) * K[3 * i + j]));
+                S[4] = S[4] + (T[4 * (i + 1) + (j + 1)] * D5(K[3 * i + j]));
+            }
+            S[4] = S[4] - (T[0] * D5(be[i] * da[i]));
+            S[4] = S[4] - (T[i + 1] * D5(da[i]));
+        }
+        const D5 f = D5(al * ::sqrt(dg));
+        for (int k = 0; k < 5; k++) s[k] = f * S[k];
     }
     // Cell k of line L is updated unless a cell of its stencil (two cells out along the line in
     // 1D; the cell and two cells out along both axes in 2D, Solvers/BlackHoleEulerSecondOrderSolver.cpp:39-100)
@@ -447,9 +593,123 @@ template <class Sys> RADJ_HD void cell_adjoint_sys(const Sys& S, const Params& P
     for (int f = 0; f < 5; f++) P.pbar_in[f * P.fstride + me_off] = acc[f];
 }
 
+// ---- the black-hole RK source step, Solvers/BlackHoleEulerForcingSolver.cpp:3-250: classical RK4 on
+// the source term with interleaved fractional evolutions on frozen neighbours
+// (Solvers/BlackHoleEulerSolvers.cpp:159-232: face fluxes at xc -/+ dx, as written).
+RADJ_HD void evolve_fraction(const GRSys& S, double frac, const D5* l, const D5* m, const D5* r, Pt xc, int axis,
+                             double dx, double dt, double w, int lim, D5* out) {
+    D5 ul[5], um[5], ur[5], sl[5];
+    S.cons(l, shift(xc, axis, -dx), ul);
+    S.cons(m, xc, um);
+    S.cons(r, shift(xc, axis, dx), ur);
+    slope_vector(ul, um, ur, w, lim, sl);
+    D5 UL[5], UR[5], FL[5], FR[5];
+    for (int k = 0; k < 5; k++) {
+        UL[k] = um[k] - (D5(0.5) * sl[k]);
+        UR[k] = um[k] + (D5(0.5) * sl[k]);
+    }
+    S.flux(UL, axis, shift(xc, axis, -dx), FL);
+    S.flux(UR, axis, shift(xc, axis, dx), FR);
+    const D5 s = D5(frac * (dt / dx));
+    D5 nu[5];
+    for (int k = 0; k < 5; k++) nu[k] = um[k] + (s * (FL[k] - FR[k]));
+    S.prim(nu, xc, out);
+}
+RADJ_HD void rk_cell(const GRSys& S, int dims, const D5* cl, const D5* cm, const D5* cr, const D5* ct, const D5* cb,
+                     Pt q, double dx, double dt, double w, int lim, D5* out_cons) {
+    D5 L[5], R[5], Tp[5], B[5], Mp[5], E1[5], E2[5], E[5];
+    S.prim(cl, shift(q, 0, -dx), L);
+    S.prim(cr, shift(q, 0, dx), R);
+    if (dims == 2) {
+        S.prim(ct, shift(q, 1, -dx), Tp);
+        S.prim(cb, shift(q, 1, dx), B);
+    }
+    D5 k[4][5], st[5], c[5], sv[5];
+    S.source(cm, q, sv);
+    for (int i = 0; i < 5; i++) k[0][i] = D5(dt) * sv[i];
+    const double fx1[3] = {0.5, 0.5, 1.0};                               // 1D fractions
+    const double fx2[3] = {0.25, 0.25, 0.5}, fy2[3] = {0.5, 0.5, 1.0};  // 2D fractions
+    for (int stage = 0; stage < 3; stage++) {
+        for (int i = 0; i < 5; i++) st[i] = stage < 2 ? (cm[i] + (D5(0.5) * k[stage][i])) : (cm[i] + k[stage][i]);
+        S.prim(st, q, Mp);
+        if (dims == 1) {
+            evolve_fraction(S, fx1[stage], L, Mp, R, q, 0, dx, dt, w, lim, E);
+        } else {
+            evolve_fraction(S, fx2[stage], L, Mp, R, q, 0, dx, dt, w, lim, E1);
+            evolve_fraction(S, fy2[stage], Tp, E1, B, q, 1, dx, dt, w, lim, E2);
+            evolve_fraction(S, fx2[stage], L, E2, R, q, 0, dx, dt, w, lim, E);
+        }
+        S.cons(E, q, c);
+        S.source(c, q, sv);
+        for (int i = 0; i < 5; i++) k[stage + 1][i] = D5(dt) * sv[i];
+    }
+    for (int i = 0; i < 5; i++)
+        out_cons[i] = cm[i] + (D5(1.0 / 6.0) * (k[0][i] + ((D5(2.0) * k[1][i]) + ((D5(2.0) * k[2][i]) + k[3][i]))));
+}
+
+// The input adjoint of cell c = i * nx + j for one RK source step (time step P.s.dt, slopes P.s.w and
+// P.s.lim).  Output cell (i', j') reads itself and its 2 (1D) or 4 (2D) direct neighbours through a
+// transmissive one-ghost copy (Solvers/BlackHoleEulerForcingSolver.cpp:187-250); an output whose
+// point or a neighbour's lies in the excision region keeps its state.
+RADJ_HD void rk_cell_adjoint(const Params& P, size_t c) {
+    const GRSys S{P.gamma, KerrSchild{P.bh[0], P.bh[1], P.bh[2], P.bh[3], P.bh[4]}, P.dims, P.s.dx};
+    const int i = (int)(c / (size_t)P.nx), j = (int)(c % (size_t)P.nx);
+    const int dims = P.dims, ny = dims == 1 ? 1 : P.ny;
+    const double dx = P.s.dx;
+    auto active = [&](int ii, int jj) -> bool {
+        const KerrSchild& b = S.bh;
+        if (dims == 1) return !b.excised(jj * dx, 0.0, 0.0) && !b.excised((jj - 1) * dx, 0.0, 0.0) && !b.excised((jj + 1) * dx, 0.0, 0.0);
+        return !b.excised(jj * dx, ii * dx, 0.0) && !b.excised((jj - 1) * dx, ii * dx, 0.0) &&
+               !b.excised((jj + 1) * dx, ii * dx, 0.0) && !b.excised(jj * dx, (ii - 1) * dx, 0.0) &&
+               !b.excised(jj * dx, (ii + 1) * dx, 0.0);
+    };
+    const int oi_[5] = {i, i, i, i - 1, i + 1}, oj_[5] = {j, j - 1, j + 1, j, j};
+    double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int q = 0; q < (dims == 1 ? 3 : 5); q++) {
+        const int oi = oi_[q], oj = oj_[q];
+        if (oi < 0 || oi >= ny || oj < 0 || oj >= P.nx) continue;
+        const size_t ok = (size_t)oi * P.pitch + oj;
+        if (!active(oi, oj)) {  // P'(i', j') = P(i', j')
+            if (q == 0)
+                for (int f = 0; f < 5; f++) acc[f] = acc[f] + P.pbar_out[f * P.fstride + ok];
+            continue;
+        }
+        auto ld = [&](int ii, int jj, D5* p) {
+            const int gi = ghost(ii, ny, false), gj = ghost(jj, P.nx, false);
+            const size_t k = (size_t)gi * P.pitch + gj;
+            for (int f = 0; f < 5; f++) p[f] = D5(P.state[f * P.fstride + k]);
+            if (gi == i && gj == j)
+                for (int f = 0; f < 5; f++) p[f].d[f] = 1.0;
+        };
+        const double y = dims == 1 ? 0.0 : oi * dx;
+        const Pt pq{oj * dx, y, 0.0};
+        D5 p[5], cl[5], cm[5], cr[5], ct[5], cb[5], nc[5], o[5];
+        ld(oi, oj - 1, p);
+        S.cons(p, Pt{(oj - 1) * dx, y, 0.0}, cl);
+        ld(oi, oj, p);
+        S.cons(p, pq, cm);
+        ld(oi, oj + 1, p);
+        S.cons(p, Pt{(oj + 1) * dx, y, 0.0}, cr);
+        if (dims == 2) {
+            ld(oi - 1, oj, p);
+            S.cons(p, Pt{oj * dx, (oi - 1) * dx, 0.0}, ct);
+            ld(oi + 1, oj, p);
+            S.cons(p, Pt{oj * dx, (oi + 1) * dx, 0.0}, cb);
+        }
+        rk_cell(S, dims, cl, cm, cr, ct, cb, pq, dx, P.s.dt, P.s.w, P.s.lim, nc);
+        S.prim(nc, pq, o);
+        for (int f = 0; f < 5; f++) {
+            const double pb = P.pbar_out[f * P.fstride + ok];
+            for (int l = 0; l < 5; l++) acc[l] = acc[l] + (o[f].d[l] * pb);
+        }
+    }
+    const size_t me = (size_t)i * P.pitch + j;
+    for (int f = 0; f < 5; f++) P.pbar_in[f * P.fstride + me] = acc[f];
+}
+
 RADJ_HD void cell_adjoint(const Params& P, size_t c) {
     if (P.system == 2)
-        cell_adjoint_sys(GRSys{P.gamma, KerrSchild{P.bh[0], P.bh[1], P.bh[2], P.bh[3], P.bh[4]}, P.dims}, P, c);
+        cell_adjoint_sys(GRSys{P.gamma, KerrSchild{P.bh[0], P.bh[1], P.bh[2], P.bh[3], P.bh[4]}, P.dims, P.s.dx}, P, c);
     else
         cell_adjoint_sys(SRSys{P.gamma}, P, c);
 }

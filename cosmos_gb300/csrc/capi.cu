@@ -185,8 +185,7 @@ namespace cg {
 int enqueue_step_into(cosmos_grid* g, const void* src, void* const* dst) {
     const bool gr = g->p.system == COSMOS_GR;
     const cosmos_solve_opts& o = g->run;
-    if (gr && o.subcycles != 0)
-        return fail(COSMOS_EUNSUPPORTED, "explicit-buffer steps of a black-hole grid cover the flux step (zero subcycles)");
+    const int nsub = gr ? o.subcycles : 0;  // RK source half-steps before and after the flux sweeps
     CK(launch_dt_kernel(g->ctl, g->ctx->stream));
     SweepArgs a = base_args(g);
     a.order = o.order;
@@ -195,20 +194,33 @@ int enqueue_step_into(cosmos_grid* g, const void* src, void* const* dst) {
     a.out.status = &g->ctl->status;
     a.ds.ctl = g->ctl;
     const int ns = g->p.dims == 2 ? 3 : 1;
-    for (int k = 0; k < ns; k++) {
-        const double scale = ns == 3 && k != 1 ? 0.5 : 1.0;
-        a.G.axis = ns == 3 && k == 1 ? 1 : 0;
-        a.ds.scale = scale;
-        a.ds.nsub = 0;
-        a.ds.fsel = scale == 0.5 ? 1 : 0;
-        a.src = k == 0 ? src : dst[k - 1];
-        a.dst = dst[k];
-        a.out.ws_ctl = k == ns - 1 && !gr ? g->ctl : nullptr;  // the CFL reduction of the step's last sweep
-        CK(sweep_launch(g, a));
+    int k = 0;  // operations done; operation k reads dst[k - 1] (src for k = 0) and writes dst[k]
+    for (int half = 0; half < 2; half++) {
+        for (int s = 0; s < nsub; s++, k++) {  // as enqueue_step's RK half-steps: bias 0, limiter 1
+            SweepArgs r = a;
+            r.bias = 0.0;
+            r.lim = 1;
+            r.ds.nsub = nsub;
+            r.src = k == 0 ? src : dst[k - 1];
+            r.dst = dst[k];
+            CK(g->p.precision == COSMOS_FP64 ? launch_rk_source_exact(r) : launch_rk_source_gr_fast(r));
+        }
+        if (half == 1) break;
+        for (int m = 0; m < ns; m++, k++) {
+            const double scale = ns == 3 && m != 1 ? 0.5 : 1.0;
+            a.G.axis = ns == 3 && m == 1 ? 1 : 0;
+            a.ds.scale = scale;
+            a.ds.nsub = 0;
+            a.ds.fsel = scale == 0.5 ? 1 : 0;
+            a.src = k == 0 ? src : dst[k - 1];
+            a.dst = dst[k];
+            a.out.ws_ctl = m == ns - 1 && !gr ? g->ctl : nullptr;  // the CFL reduction of the step's last sweep
+            CK(sweep_launch(g, a));
+        }
     }
     if (gr) {  // the black-hole CFL reduction runs on the step's final state, as in enqueue_step
         SweepArgs w = base_args(g);
-        w.src = dst[ns - 1];
+        w.src = dst[k - 1];
         w.out.ws_ctl = g->ctl;
         CK(g->p.precision == COSMOS_FP64 ? launch_wavespeed_exact(w, nullptr) : launch_wavespeed_gr_fast(w, nullptr));
     }

@@ -1,6 +1,6 @@
 // C ABI of the hand-written adjoint: reverse-mode gradient of a final-density misfit through
-// nsteps SLIC steps of a Newtonian grid (or an FP64 SR grid, or the flux steps of an FP64
-// black-hole grid), with checkpoints every `checkpoint_every` steps.
+// nsteps SLIC steps of a Newtonian grid (or an FP64 SR grid, or an FP64 black-hole grid with its RK
+// source half-steps), with checkpoints every `checkpoint_every` steps.
 //
 // Forward: the grid's own graph-replayed steps (device dt from the CFL rule, or the caller's dts),
 // the state copied to a checkpoint store before every segment and each step's dt logged.
@@ -70,14 +70,15 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
                                    const double* target, const double* dts_in, double* grad_prim, double* loss,
                                    double* dts_out, double* ms) {
     if (!g || !o || !target || !grad_prim) return afail(COSMOS_EINVAL, "null grid, options, target or gradient");
-    // SR and black-hole grids (FP64) run the relativistic sweep adjoints on primitive adjoints; the
-    // black-hole step is differentiated without its source terms (the forward runs zero subcycles)
+    // SR and black-hole grids (FP64) run the relativistic adjoints on primitive adjoints; a black-hole
+    // step is o->subcycles RK source half-steps, the flux sweeps, o->subcycles more
     const bool rel = g->p.system == COSMOS_SR || g->p.system == COSMOS_GR;
     if (rel && g->p.precision != COSMOS_FP64)
         return afail(COSMOS_EUNSUPPORTED, "the relativistic adjoints cover FP64 grids");
     if (rel && (g->G.nx < 2 || (g->p.dims == 2 && g->G.ny < 2)))
         return afail(COSMOS_EUNSUPPORTED, "the relativistic adjoints need at least two cells per swept line");
     if (o->order != 2) return afail(COSMOS_EUNSUPPORTED, "the adjoint covers SLIC (order 2)");
+    if (g->p.system == COSMOS_GR && o->subcycles < 0) return afail(COSMOS_EINVAL, "subcycles must be >= 0");
     if (nsteps < 1 || checkpoint_every < 1) return afail(COSMOS_EINVAL, "nsteps and checkpoint_every must be >= 1");
     if (!dts_in && !(o->cfl > 0.0)) return afail(COSMOS_EINVAL, "cfl must be positive when no dts are given");
     if (dts_in)
@@ -91,7 +92,10 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
     const size_t abytes = G0.fstride * 5 * (fp64 ? sizeof(double) : sizeof(float));  // one adjoint state
     const int K = std::min(checkpoint_every, nsteps);
     const int nck = (nsteps + K - 1) / K;
-    const int spp = g->p.dims == 2 ? 3 : 1;  // sweeps per step
+    // operations per step: the sweeps, and around them a black-hole grid's RK source half-steps
+    const int nsw = g->p.dims == 2 ? 3 : 1;
+    const int nsub = g->p.system == COSMOS_GR ? o->subcycles : 0;
+    const int spp = nsw + 2 * nsub;
     Scratch sc;
     sc.st = g->ctx->stream;
     cudaStream_t st = sc.st;
@@ -117,7 +121,7 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
     cosmos_solve_opts fo = *o;
     fo.t_final = 1e300;  // exactly nsteps steps
     fo.max_steps = nsteps;
-    fo.subcycles = g->p.system == COSMOS_GR ? 0 : 1;
+    fo.subcycles = g->p.system == COSMOS_GR ? nsub : 1;
     if (dts_in) fo.cfl = 1.0;
     int rc = cosmos_grid_run_begin(g, &fo);
     if (rc) return rc;
@@ -140,12 +144,12 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
         // starts without a recomputation; the final state goes to the grid's other buffer.
         ACK(cudaMemcpyAsync(slot(c, 0), g->buf[g->cur], sbytes, cudaMemcpyDeviceToDevice, st));
         for (int s = 0; s < ns; s++) {
-            void* outs[3];
+            std::vector<void*> outs(spp);
             for (int k = 0; k < spp; k++) {
                 const int q = s * spp + k + 1;
                 outs[k] = q < ns * spp ? (void*)slot(c, q) : g->buf[g->cur ^ 1];
             }
-            if ((rc = enqueue_step_into(g, slot(c, s * spp), outs))) return rc;
+            if ((rc = enqueue_step_into(g, slot(c, s * spp), outs.data()))) return rc;
         }
         g->cur ^= 1;
     }
@@ -182,21 +186,38 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
     cudaStream_t rs = g->ctx->copy;
     fa.stream = rs;
     for (int k = 0; k < 2; k++) ACK(cudaEventRecord(sc.adj_done[k], st));  // after the forward pass and the loss
-    auto sweep_of = [&](int c, int q, int& axis, double& dt) {
+    // operation q of segment c: its axis and dt; true for an RK source half-step (dt / (2 nsub))
+    auto op_of = [&](int c, int q, int& axis, double& dt) -> bool {
         const double d = dts[c * K + q / spp];
-        const int m = q % spp;
-        axis = spp == 3 && m == 1 ? 1 : 0;
-        dt = spp == 3 && m != 1 ? 0.5 * d : d;
+        int m = q % spp;
+        if (m < nsub || m >= nsub + nsw) {
+            axis = 0;
+            dt = 0.5 * (d / nsub);
+            return true;
+        }
+        m -= nsub;
+        axis = nsw == 3 && m == 1 ? 1 : 0;
+        dt = nsw == 3 && m != 1 ? 0.5 * d : d;
+        return false;
     };
-    auto nsweeps = [&](int c) { return (std::min(nsteps, c * K + K) - c * K) * spp; };
+    auto nops_of = [&](int c) { return (std::min(nsteps, c * K + K) - c * K) * spp; };
     auto recompute = [&](int c) -> int {
         ACK(cudaStreamWaitEvent(rs, sc.adj_done[c & 1], 0));  // this half's previous reader is done
         ACK(cudaMemcpyAsync(slot(c, 0), ck + (size_t)c * sbytes, sbytes, cudaMemcpyDeviceToDevice, rs));
-        const int nsw = nsweeps(c);
-        for (int q = 0; q + 1 < nsw; q++) {  // the last sweep's output is not needed
+        const int nops = nops_of(c);
+        for (int q = 0; q + 1 < nops; q++) {  // the last operation's output is not needed
             int axis;
             double dt;
-            sweep_of(c, q, axis, dt);
+            if (op_of(c, q, axis, dt)) {  // RK source half-step: bias 0, limiter 1, as in the forward
+                SweepArgs r = fa;
+                r.bias = 0.0;
+                r.lim = 1;
+                r.ds.fixed = dt;
+                r.src = slot(c, q);
+                r.dst = slot(c, q + 1);
+                ACK(launch_rk_source_exact(r));
+                continue;
+            }
             fa.G.axis = axis;
             fa.ds.fixed = dt;
             fa.ds.ffix = make_fast_coef(dt, g->p.dx);
@@ -211,10 +232,15 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
     for (int c = nck - 1; c >= 0; c--) {
         if (c > 0 && (rc = recompute(c - 1))) return rc;
         ACK(cudaStreamWaitEvent(st, sc.rec_done[c & 1], 0));
-        for (int q = nsweeps(c) - 1; q >= 0; q--) {
+        for (int q = nops_of(c) - 1; q >= 0; q--) {
             int axis;
             double dt;
-            sweep_of(c, q, axis, dt);
+            if (op_of(c, q, axis, dt)) {
+                ACK(launch_adjoint_rel_rk(G0, g->p.gamma, bh, g->p.dx, dt, slot(c, q), adj + (size_t)cur * abytes,
+                                          adj + (size_t)(cur ^ 1) * abytes, st));
+                cur ^= 1;
+                continue;
+            }
             ap.G.axis = axis;
             ap.dt = dt;
             {

@@ -47,7 +47,8 @@ void set_capturing(bool on);
 SweepArgs base_args(cosmos_grid* g);
 // the sweep kernel of the grid's precision
 cudaError_t sweep_launch(cosmos_grid* g, const SweepArgs& a);
-// one step of a running (cosmos_grid_run_begin) Newtonian or SR grid reading `src`, sweep k writing
-// dst[k]; returns a cosmos status code
+// one step of a running (cosmos_grid_run_begin) grid reading `src`, its k-th operation writing dst[k]:
+// the sweeps, and for a black-hole grid `subcycles` RK source half-steps before and after them;
+// returns a cosmos status code
 int enqueue_step_into(cosmos_grid* g, const void* src, void* const* dst);
 }  // namespace cg

@@ -150,6 +150,9 @@ cudaError_t launch_adjoint_grad_fast(const Geom& G, double gamma, const void* st
 cudaError_t launch_adjoint_rel_sweep(const Geom& G, int system, double gamma, const double* bh, double dx, double dt,
                                      double bias, int lim, const void* state, const void* pbar_out, void* pbar_in,
                                      cudaStream_t st);
+// One black-hole RK source step's adjoint (dt the step's, bias 0, limiter 1, transmissive).
+cudaError_t launch_adjoint_rel_rk(const Geom& G, double gamma, const double* bh, double dx, double dt, const void* state,
+                                  const void* pbar_out, void* pbar_in, cudaStream_t st);
 cudaError_t launch_adjoint_rel_grad(const Geom& G, const void* pbar, double* grad, cudaStream_t st);
 
 }  // namespace cg

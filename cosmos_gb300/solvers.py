@@ -184,15 +184,16 @@ class Grid:
         check(load().cosmos_grid_field_sums(self.h, o.ctypes.data))
         return o
 
-    def adjoint(self, target, nsteps, cfl, bias, limiter, checkpoint_every=10, dts=None):
+    def adjoint(self, target, nsteps, cfl, bias, limiter, checkpoint_every=10, dts=None, subcycles=1):
         """Gradient of L = 1/2 sum (rho_T - target)^2 after `nsteps` SLIC steps from the current
         state with respect to its primitives (dt of each step held fixed: `dts` if given, else the
-        CFL rule's).  Returns (loss, grad with the shape of get_prim(), dts, (forward_ms, backward_ms)).
-        The grid holds the final state afterwards."""
+        CFL rule's).  Black-hole grids take `subcycles` RK source half-steps before and after each
+        flux step (0: the flux step alone).  Returns (loss, grad with the shape of get_prim(), dts,
+        (forward_ms, backward_ms)).  The grid holds the final state afterwards."""
         tgt = np.ascontiguousarray(target, dtype=np.float64)
         if tgt.shape != self.shape:
             raise ValueError(f"target must have shape {self.shape}, got {tgt.shape}")
-        o = self.opts(2, cfl, 1e300, bias, limiter, 1, nsteps)
+        o = self.opts(2, cfl, 1e300, bias, limiter, int(subcycles), nsteps)
         grad = np.empty(self.shape + (5,), dtype=np.float64)
         dts_out = np.empty(int(nsteps), dtype=np.float64)
         din = None if dts is None else np.ascontiguousarray(dts, dtype=np.float64)

@@ -201,10 +201,10 @@ int cosmos_batch_autotune(cosmos_batch* b, const char* cache_path, int* nt, int*
  * Newtonian grid, or of a special-relativistic or black-hole FP64 grid, from its current state,
  * with respect to that initial state's primitives.  No counterpart in the reference (it has no
  * derivatives); it differentiates the reference's EulerSecondOrderSolver::solve / solve2D step
- * (Solvers/EulerSecondOrderSolver.cpp:102-147; RelativisticEulerSecondOrderSolver for SR grids and
- * BlackHoleEulerSecondOrderSolver's flux step without the source terms for black-hole grids, whose
- * forward run then takes zero subcycles; through every primitive recovery's Newton iteration;
- * lines of at least two cells) with
+ * (Solvers/EulerSecondOrderSolver.cpp:102-147; RelativisticEulerSecondOrderSolver for SR grids;
+ * BlackHoleEulerSecondOrderSolver's step for black-hole grids, with o->subcycles RK source
+ * half-steps before and after each flux step, 0 for the flux step alone; through every primitive
+ * recovery's Newton iteration; lines of at least two cells) with
  * each step's dt held fixed: the caller's dts_in[nsteps] if non-NULL, else the CFL rule's dts
  * (o->cfl) of the forward run, which are returned in dts_out[nsteps] if non-NULL.  Checkpoints
  * every `checkpoint_every` steps; each segment is recomputed once.  target: ny*nx doubles (row

@@ -1,5 +1,5 @@
 """GPU adjoints of the relativistic SLIC steps (cosmos_grid_adjoint on FP64 SR grids, and on FP64
-black-hole grids for the flux step without source terms) against the host build of the same
+black-hole grids for the flux step alone and with its RK source half-steps) against the host build of the same
 sweep-adjoint cell function and against the oracle's tangent-linear models (dual numbers through
 every primitive recovery's Newton iteration, same fixed time steps).
 
@@ -29,15 +29,15 @@ def rel_grid(cg, system, p0, bc=0, precision=0, bh=None):
     return g
 
 
-def check(cg, oracle, host_adjoint, system, p0, target, dts, lim, bc, bh, bias=0.0, seed=0):
+def check(cg, oracle, host_adjoint, system, p0, target, dts, lim, bc, bh, bias=0.0, seed=0, sub=0):
     dx = 1.0 / p0.shape[-2]
     g = rel_grid(cg, system, p0, bc, bh=bh)
     loss, grad, dts_out, _ = g.adjoint(target, len(dts) if dts is not None else 5, 0.6, bias, lim, checkpoint_every=3,
-                                       dts=dts)
+                                       dts=dts, subcycles=sub)
     if dts is None:
         assert (dts_out > 0).all()
         dts = dts_out
-    host = reverse_gradient(oracle, host_adjoint, system, p0, target, dx, dts, bias, lim, bc, bh)
+    host = reverse_gradient(oracle, host_adjoint, system, p0, target, dx, dts, bias, lim, bc, bh, sub)
     assert np.abs(grad - host).max() <= 1e-12 * np.abs(host).max()
     rng = np.random.default_rng(seed)
     for _ in range(2):
@@ -45,7 +45,7 @@ def check(cg, oracle, host_adjoint, system, p0, target, dts, lim, bc, bh, bias=0
         if system == 1:
             L0, dL = oracle.tlm_sr(p0, d, target, dx, dts, bias, lim, G, bc)
         else:
-            L0, dL = oracle.tlm_gr(p0, d, target, dx, dts, bias, lim, G, bh)
+            L0, dL = oracle.tlm_gr(p0, d, target, dx, dts, bias, lim, G, bh, sub)
         assert abs(loss - L0) <= 1e-13 * abs(L0), (loss, L0)
         got = float(np.sum(grad * d))
         assert abs(got - dL) <= 1e-10 * max(1.0, abs(dL)), (got, dL)
@@ -76,6 +76,18 @@ def test_gr_adjoint_matches_host_build_and_tangent_model(cg, oracle, host_adjoin
     target = gr_smooth_state(shape, 13)[..., 0]
     dts = np.full(4, 0.1 / shape[-1])
     check(cg, oracle, host_adjoint, 2, p0, target, dts, lim, 0, bh, seed=dims * 10 + lim)
+
+
+@pytest.mark.parametrize("dims,bh", [(1, (0.05, 0.0, 0.5, 0.0, 0.0)), (2, HOLES[1])])
+@pytest.mark.parametrize("sub", [1, 2])
+def test_gr_adjoint_with_source_steps(cg, oracle, host_adjoint, dims, bh, sub):
+    """The whole black-hole step: `sub` RK source half-steps before and after each flux step; four
+    steps with checkpoints every three, so the first segment is recomputed (RK steps included)."""
+    shape = (24,) if dims == 1 else (10, 12)
+    p0 = gr_smooth_state(shape, 7 + sub)
+    target = gr_smooth_state(shape, 13)[..., 0]
+    dts = np.full(4, 0.1 / shape[-1])
+    check(cg, oracle, host_adjoint, 2, p0, target, dts, 1, 0, bh, seed=dims * 10 + sub, sub=sub)
 
 
 def test_relativistic_adjoint_rejects_fp32_grids(cg):

@@ -27,6 +27,8 @@ def host_adjoint(tmp_path_factory):
     d, i, p = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
     lib.rel_host_sweep_adjoint.argtypes = [i, i, p, p, p, i, i, i, i, d, p, d, d, d, i]
     lib.rel_host_sweep_adjoint.restype = i
+    lib.rel_host_rk_adjoint.argtypes = [i, p, p, p, i, i, d, p, d, d]
+    lib.rel_host_rk_adjoint.restype = i
 
     def run(system, state, pbar_out, axis, bc, dx, dt, bias, lim, bh=None):
         s = np.ascontiguousarray(state, dtype=np.float64)
@@ -38,27 +40,46 @@ def host_adjoint(tmp_path_factory):
                                         axis, bc, G, None if hole is None else hole.ctypes.data, dx, dt, bias, lim)
         assert rc == 0
         return out
+
+    def rk(state, pbar_out, dx, dt, bh):
+        s = np.ascontiguousarray(state, dtype=np.float64)
+        po = np.ascontiguousarray(pbar_out, dtype=np.float64)
+        out = np.empty_like(s)
+        ny, nx = (1, s.shape[0]) if s.ndim == 2 else s.shape[:2]
+        hole = np.ascontiguousarray(bh, dtype=np.float64)
+        assert lib.rel_host_rk_adjoint(s.ndim - 1, s.ctypes.data, po.ctypes.data, out.ctypes.data, ny, nx, G,
+                                       hole.ctypes.data, dx, dt) == 0
+        return out
+    run.rk = rk
     return run
 
 
-def sweeps_of(dims, dts):
-    """(axis, dt) of every sweep in order: X(dt) per 1D step, X(dt/2) Y(dt) X(dt/2) per 2D step."""
+def ops_of(dims, dts, sub=0):
+    """(axis, dt) of every operation in order: X(dt) per 1D step, X(dt/2) Y(dt) X(dt/2) per 2D step,
+    with `sub` black-hole RK source half-steps (axis None, dt / (2 sub)) before and after."""
     out = []
     for dt in dts:
-        out += [(0, dt)] if dims == 1 else [(0, 0.5 * dt), (1, dt), (0, 0.5 * dt)]
+        rk = [(None, 0.5 * (dt / sub))] * sub if sub else []
+        out += rk + ([(0, dt)] if dims == 1 else [(0, 0.5 * dt), (1, dt), (0, 0.5 * dt)]) + rk
     return out
 
 
-def reverse_gradient(oracle, adj, system, p0, target, dx, dts, bias, lim, bc, bh=None):
-    seq = sweeps_of(p0.ndim - 1, dts)
+def reverse_gradient(oracle, adj, system, p0, target, dx, dts, bias, lim, bc, bh=None, sub=0):
+    seq = ops_of(p0.ndim - 1, dts, sub)
     inputs, q = [], p0.copy()
     for axis, dt in seq:
         inputs.append(q)
-        q = oracle.sweep(system, q, axis, 2, dx, dt, bias, lim, G, bc, bh=bh)
+        if axis is None:
+            q = oracle.rk_source(q, dx, dt, 0.0, 1, G, bh)
+        else:
+            q = oracle.sweep(system, q, axis, 2, dx, dt, bias, lim, G, bc, bh=bh)
     pbar = np.zeros_like(q)
     pbar[..., 0] = q[..., 0] - target
     for (axis, dt), s in zip(reversed(seq), reversed(inputs)):
-        pbar = adj(system, s, pbar, axis, bc, dx, dt, bias, lim, bh)
+        if axis is None:
+            pbar = adj.rk(s, pbar, dx, dt, bh)
+        else:
+            pbar = adj(system, s, pbar, axis, bc, dx, dt, bias, lim, bh)
     return pbar
 
 
@@ -114,6 +135,23 @@ def test_gr_sweep_adjoint_matches_tangent_model(oracle, host_adjoint, dims, bh, 
     assert np.isfinite(grad).all()
     check_directions(grad, lambda d: oracle.tlm_gr(p0, d, target, dx, dts, 0.0, lim, G, bh)[1], p0.shape,
                      dims * 10 + lim)
+
+
+@pytest.mark.parametrize("dims,bh", [(1, (0.05, 0.0, 0.5, 0.0, 0.0))] + [(2, h) for h in HOLES])
+@pytest.mark.parametrize("sub", [1, 2])
+@pytest.mark.parametrize("lim", [0, 1])
+def test_gr_step_adjoint_with_source_matches_tangent_model(oracle, host_adjoint, dims, bh, sub, lim):
+    """The whole black-hole step: `sub` RK source half-steps (source term, fractional evolutions in
+    each RK stage, excision) around the flux sweeps."""
+    shape = (24,) if dims == 1 else (10, 12)
+    p0 = gr_smooth_state(shape, 5 + lim)
+    target = gr_smooth_state(shape, 13)[..., 0]
+    dx = 1.0 / shape[-1]
+    dts = np.full(2, 0.1 * dx)
+    grad = reverse_gradient(oracle, host_adjoint, 2, p0, target, dx, dts, 0.0, lim, 0, bh, sub)
+    assert np.isfinite(grad).all()
+    check_directions(grad, lambda d: oracle.tlm_gr(p0, d, target, dx, dts, 0.0, lim, G, bh, sub)[1], p0.shape,
+                     dims * 10 + sub * 3 + lim, n=2)
 
 
 def test_gr_sweep_adjoint_passes_excised_cells_through(oracle, host_adjoint):
