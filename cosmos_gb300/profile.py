@@ -4,6 +4,7 @@
     python -m cosmos_gb300.profile --kernel step --n 4096 --precision fp32 --launches 4
     python -m cosmos_gb300.profile --kernel step --system 2 --n 1024 --warm 60 --launches 1
     python -m cosmos_gb300.profile --kernel adjoint --n 1024 --precision fp32 --launches 2
+    python -m cosmos_gb300.profile --kernel adjoint --system 2 --n 256 --precision fp64 --subcycles 1 --launches 1
     python -m cosmos_gb300.profile --kernel batch --grids 64 --launches 2
 
 Creates one grid of the configuration's problem for the system (Newtonian: config-2 four-quadrant
@@ -11,7 +12,8 @@ data, periodic; SR: config-3 Kelvin-Helmholtz layers, periodic; GR: config-4 acc
 Schwarzschild hole, transmissive; MinBee) and launches the requested kernels a few times, so that a profiler can capture exactly those launches on a
 bounded device footprint (two state buffers plus one staging buffer).  `adjoint` runs the
 gradient of `launches` SLIC steps (checkpoint every step: launches X and Y sweep adjoints per
-step); `batch` runs `launches` chunks of 10 steps of the first `grids` grids of the batched
+step; FP64 SR and black-hole grids run the relativistic adjoints, the latter with `subcycles` RK
+source half-steps around each flux step); `batch` runs `launches` chunks of 10 steps of the first `grids` grids of the batched
 workload (256 grids, sides log-uniform in [128, 2048]).
 """
 import argparse
@@ -31,6 +33,7 @@ def main():
     ap.add_argument("--axis", type=int, default=0)
     ap.add_argument("--order", type=int, default=2)
     ap.add_argument("--launches", type=int, default=3)
+    ap.add_argument("--subcycles", type=int, default=1, help="`adjoint` on a black-hole grid: RK source half-steps")
     ap.add_argument("--warm", type=int, default=0,
                     help="`step` only: steps run before the captured ones (evolved states)")
     a = ap.parse_args()
@@ -77,7 +80,7 @@ def main():
             g.sweep(a.axis, a.order, dt, 0.0, cg.MINBEE)
     elif a.kernel == "adjoint":
         tgt = s[..., 0] * 0.9
-        g.adjoint(tgt, a.launches, 0.8, 0.0, cg.MINBEE, checkpoint_every=1)
+        g.adjoint(tgt, a.launches, 0.8, 0.0, cg.MINBEE, checkpoint_every=1, subcycles=a.subcycles)
     elif a.kernel == "rk":
         for _ in range(a.launches):
             g.rk_source(dt, 0.0, 1)
