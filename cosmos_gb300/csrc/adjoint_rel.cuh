@@ -515,7 +515,10 @@ struct Params {
     double* pbar_in;
 };
 
-// The input adjoint of cell c = i * nx + j.
+// The input adjoint of cell c = i * nx + j.  The output windows of one input cell overlap, and every
+// half-step evolution and face flux in them carries the same seeds whichever window uses it, so
+// each is evaluated once: the states at line positions [kmin - 2, kmax + 2] for the outputs
+// kmin..kmax, the evolutions and fluxes of the faces that an updated output reads.
 template <class Sys> RADJ_HD void cell_adjoint_sys(const Sys& S, const Params& P, size_t c) {
     const int i = (int)(c / (size_t)P.nx), j = (int)(c % (size_t)P.nx);
     const int axis = P.s.axis;
@@ -523,66 +526,79 @@ template <class Sys> RADJ_HD void cell_adjoint_sys(const Sys& S, const Params& P
     const int n = axis == 0 ? P.nx : P.ny;
     const int me = axis == 0 ? j : i, line = axis == 0 ? i : j;
     const double dx = P.s.dx;
-    // storage offset of line position k: base + k * step
+    // storage offset of line cell k: base + k * step
     const size_t base = axis == 0 ? (size_t)i * P.pitch : (size_t)j;
     const size_t step = axis == 0 ? 1 : (size_t)P.pitch;
-    int ks[5], nk = 0;
+    // outputs: line positions me - 2 .. me + 2 inside the line (periodic: each distinct cell once)
+    int kpos[5], nk = 0;
+    bool act[5];
     for (int t = -2; t <= 2; t++) {
-        int k = me + t;
-        if (per) k = ghost(k, n, true);
-        else if (k < 0 || k >= n) continue;
+        const int k = me + t;
+        if (!per && (k < 0 || k >= n)) continue;
         bool dup = false;
-        for (int q = 0; q < nk; q++) dup = dup || ks[q] == k;
-        if (!dup) ks[nk++] = k;
+        for (int q = 0; q < nk; q++) dup = dup || ghost(kpos[q], n, per) == ghost(k, n, per);
+        if (dup) continue;
+        act[nk] = S.active(axis, line, ghost(k, n, per), n, dx);
+        kpos[nk++] = k;
+    }
+    const int kmin = kpos[0], kmax = kpos[nk - 1];
+    const int lo = kmin - 2;  // states at positions lo .. kmax + 2 (at most 9)
+    D5 W[9][5];
+    for (int p = lo; p <= kmax + 2; p++) {
+        const int src = ghost(p, n, per);
+        const size_t off = base + (size_t)src * step;
+        for (int f = 0; f < 5; f++) W[p - lo][f] = D5(P.state[f * P.fstride + off]);
+        if (src == me)
+            for (int f = 0; f < 5; f++) W[p - lo][f].d[f] = 1.0;
+    }
+    auto at = [&](int p) -> const D5* { return W[p - lo]; };
+    // faces kmin .. kmax + 1 (face f between positions f - 1 and f); a face is needed when an
+    // updated output reads it
+    bool need[6] = {false, false, false, false, false, false};
+    for (int q = 0; q < nk; q++)
+        if (act[q]) {
+            need[kpos[q] - kmin] = true;
+            need[kpos[q] + 1 - kmin] = true;
+        }
+    auto face_pt = [&](int f) -> Pt {
+        return axis == 0 ? Pt{(f - 0.5) * dx, line * dx, 0.0} : Pt{line * dx, (f - 0.5) * dx, 0.0};
+    };
+    auto cell_pt = [&](int k) -> Pt { return axis == 0 ? Pt{k * dx, line * dx, 0.0} : Pt{line * dx, k * dx, 0.0}; };
+    D5 F[6][5];
+    if (Sys::coords) {  // each face evolves its two cells at its own points
+        for (int f = kmin; f <= kmax + 1; f++) {
+            if (!need[f - kmin]) continue;
+            D5 er[5], el[5];
+            const Pt xf = face_pt(f);
+            evolve(S, P.s, at(f - 2), at(f - 1), at(f), shift(xf, axis, -(dx * 0.5)), (D5*)nullptr, er);
+            evolve(S, P.s, at(f - 1), at(f), at(f + 1), shift(xf, axis, dx * 0.5), el, (D5*)nullptr);
+            force(S, P.s, er, el, xf, F[f - kmin]);
+        }
+    } else {  // each cell's evolution gives both its faces
+        D5 A[7][5], B[7][5];  // cells kmin - 1 .. kmax + 1
+        for (int k = kmin - 1; k <= kmax + 1; k++) {
+            const bool left = k >= kmin && need[k - kmin], right = k + 1 <= kmax + 1 && need[k + 1 - kmin];
+            if (!left && !right) continue;
+            evolve(S, P.s, at(k - 1), at(k), at(k + 1), cell_pt(k), left ? A[k - kmin + 1] : (D5*)nullptr,
+                   right ? B[k - kmin + 1] : (D5*)nullptr);
+        }
+        for (int f = kmin; f <= kmax + 1; f++)
+            if (need[f - kmin]) force(S, P.s, B[f - kmin], A[f - kmin + 1], face_pt(f), F[f - kmin]);
     }
     double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     for (int q = 0; q < nk; q++) {
-        const int k = ks[q];
-        const size_t ok = base + (size_t)k * step;
-        if (!S.active(axis, line, k, n, dx)) {  // P'_k = P_k
-            if (k == me)
+        const int k = kpos[q], cell = ghost(k, n, per);
+        const size_t ok = base + (size_t)cell * step;
+        if (!act[q]) {  // P'_k = P_k
+            if (cell == me)
                 for (int f = 0; f < 5; f++) acc[f] = acc[f] + P.pbar_out[f * P.fstride + ok];
             continue;
         }
-        D5 win[5][5];
-        bool hit = false;
-        for (int p = 0; p < 5; p++) {
-            const int src = ghost(k - 2 + p, n, per);
-            const size_t off = base + (size_t)src * step;
-            for (int f = 0; f < 5; f++) win[p][f] = D5(P.state[f * P.fstride + off]);
-            if (src == me) {
-                hit = true;
-                for (int f = 0; f < 5; f++) win[p][f].d[f] = 1.0;
-            }
-        }
-        if (!hit) continue;
-        // face f at x = (f - 1/2) dx along the line, the line's coordinate across it
-        auto face_pt = [&](int f) -> Pt {
-            return axis == 0 ? Pt{(f - 0.5) * dx, line * dx, 0.0} : Pt{line * dx, (f - 0.5) * dx, 0.0};
-        };
-        const Pt ck = axis == 0 ? Pt{k * dx, line * dx, 0.0} : Pt{line * dx, k * dx, 0.0};
-        D5 F0[5], F1[5];
-        if (Sys::coords) {
-            D5 er[5], el[5];
-            const Pt x0 = face_pt(k), x1 = face_pt(k + 1);
-            evolve(S, P.s, win[0], win[1], win[2], shift(x0, axis, -(dx * 0.5)), (D5*)nullptr, er);
-            evolve(S, P.s, win[1], win[2], win[3], shift(x0, axis, dx * 0.5), el, (D5*)nullptr);
-            force(S, P.s, er, el, x0, F0);
-            evolve(S, P.s, win[1], win[2], win[3], shift(x1, axis, -(dx * 0.5)), (D5*)nullptr, er);
-            evolve(S, P.s, win[2], win[3], win[4], shift(x1, axis, dx * 0.5), el, (D5*)nullptr);
-            force(S, P.s, er, el, x1, F1);
-        } else {
-            D5 Bm[5], A0[5], B0[5], A1[5];
-            evolve(S, P.s, win[0], win[1], win[2], ck, (D5*)nullptr, Bm);
-            evolve(S, P.s, win[1], win[2], win[3], ck, A0, B0);
-            evolve(S, P.s, win[2], win[3], win[4], ck, A1, (D5*)nullptr);
-            force(S, P.s, Bm, A0, ck, F0);
-            force(S, P.s, B0, A1, ck, F1);
-        }
+        const Pt ck = cell_pt(cell);
         D5 u[5], nu[5], o[5];
-        S.cons(win[2], ck, u);
+        S.cons(at(k), ck, u);
         const D5 d = D5(P.s.dt / dx);
-        for (int f = 0; f < 5; f++) nu[f] = u[f] + (d * (F0[f] - F1[f]));
+        for (int f = 0; f < 5; f++) nu[f] = u[f] + (d * (F[k - kmin][f] - F[k + 1 - kmin][f]));
         S.prim(nu, ck, o);
         for (int f = 0; f < 5; f++) {
             const double pb = P.pbar_out[f * P.fstride + ok];
