@@ -1,24 +1,35 @@
-"""Benchmark: 2D Newtonian SLIC (MinBee), FP32 bulk vs FP64, 4096 x 4096 cells, periodic.
+"""Benchmark: 2D Newtonian SLIC (MinBee), FP32 bulk vs FP64, 4096 x 4096 cells, periodic -- and,
+in the same default run, every other configuration of the solver's workload set.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 4096]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--no-extras]
+    python bench.py --workload {grid,sod,batch,sr,gr,adjoint,amr} ...   (one configuration per line)
 
 One "step" is one Strang step X(dt/2) Y(dt) X(dt/2) of the whole grid with the time step computed
 on the device from the previous step's CFL reduction (the reference's solve2D loop body,
 Solvers/EulerSecondOrderSolver.cpp:131-146).  Metric: cell-updates per second.
 
-Our arm prints one JSON line with
+The default line (our arm) carries
   value           FP32 cell-updates/s with the state resident in HBM (CUDA events on the library's
                   stream around K graph-replayed steps; the 335 MB state exceeds the 129 MB L2, so no
                   flush is needed between steps),
-  e2e             the same steps through the C ABI with pinned host buffers: every step copies the
-                  grid's primitive state (5 doubles per cell) host->device, runs the step and copies
-                  the state back (the reference-facing per-step call, whose grids live on the host),
-  fp64            the plain FP64 (reference-exact) path on the same workload,
-  l1_rho_fp32_vs_fp64  relative L1 density error of the FP32 run against the FP64 run,
-  roofline        per-kernel achieved HBM GB/s for the dominant kernel (the X sweep) against the
-                  measured copy bandwidth in MEASURED_PEAKS.json,
-  cpu_baseline    the CPU oracle (FP64 restatement of the reference) on the host cores, bounded sample.
---impl reference times the CPU path alone (all host threads) on the same workload.
+  e2e             the same K steps through the C ABI with one pinned host buffer: every step copies
+                  the grid's primitive state (5 doubles per cell) host->device, runs the step and
+                  copies the state back into the same buffer, which the next step reads (the
+                  reference-facing per-step call, whose grids live on the host); split into the
+                  upload, the step and the download,
+  roofline        per-kernel achieved HBM GB/s of the dominant kernel (the X sweep) against the
+                  measured copy bandwidth in MEASURED_PEAKS.json, with the Y sweep and the whole step,
+  cpu_baseline    the CPU oracle (FP64 restatement of the reference) on the host cores, bounded sample,
+  configs         the other configurations, each with its own value, the FP64 path on the same
+                  steps, the FP32-vs-FP64 density error over the configuration's full step count,
+                  conservation drift, an e2e over the same steps and the roofline fraction:
+                  sod (1000-cell shock tube, FP64), grid_parity (this workload at 200 steps in FP32
+                  and FP64), sr (2048^2 Kelvin-Helmholtz), gr (1024^2 black-hole accretion), batch
+                  (256 uneven grids in one persistent launch), adjoint (Newtonian 2048^2, 100 steps,
+                  checkpoint every 10, finite-difference check) and rel_adjoint (special-relativistic
+                  and black-hole adjoints, bounded step counts).
+--impl reference times the CPU path alone (all host threads) on the same workload, W untimed and
+K timed full-size steps.
 """
 import argparse
 import ctypes
@@ -29,6 +40,7 @@ import subprocess
 import sys
 import threading
 import time
+import traceback
 
 import numpy as np
 
@@ -88,7 +100,7 @@ class Ranks:
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling while the GPU works."""
 
     def __init__(self, gpu):
         self.gpu, self.samples, self.proc = gpu, [], None
@@ -157,6 +169,92 @@ def traffic_per_launch(kernel):
         return None
 
 
+def grid_config(n, gpus):
+    """The headline workload's config; both arms print exactly this dict."""
+    return {"workload": WORKLOAD, "n": n, "cells_per_gpu": n * n, "precision": "fp32 bulk (reference arm: fp64)",
+            "l2": "state 335 MB > 129 MB L2 (no flush needed)" if n >= 4096 else "state size n^2 x 20 B",
+            "parallelism": f"replicas x{gpus}", "step": "X(dt/2) Y(dt) X(dt/2), dt from the CFL rule"}
+
+
+def rel_l1(a, b):
+    """Relative L1 difference of a against the reference values b."""
+    return float(np.abs(a - b).sum() / np.abs(b).sum())
+
+
+def newton_totals(prim, gamma):
+    """Total mass and total energy (the reference's conserved density and energy, in FP64)."""
+    rho, vx, vy, vz, p = (prim[..., k] for k in range(5))
+    e = rho * (0.5 * (vx * vx + vy * vy + vz * vz)) + p / (gamma - 1.0)
+    return float(np.sum(rho, dtype=np.float64)), float(np.sum(e, dtype=np.float64))
+
+
+def sr_totals(prim, gamma):
+    """Total conserved density D = rho W and energy tau = rho h W^2 - p - rho W (FP64)."""
+    rho, vx, vy, vz, p = (prim[..., k] for k in range(5))
+    W = 1.0 / np.sqrt(1.0 - (vx * vx + vy * vy + vz * vz))
+    h = 1.0 + p / rho * gamma / (gamma - 1.0)
+    return float(np.sum(rho * W)), float(np.sum(rho * h * W * W - p - rho * W))
+
+
+def drift(t0, t1):
+    return {"mass": abs(t1[0] - t0[0]) / abs(t0[0]), "energy": abs(t1[1] - t0[1]) / abs(t0[1])}
+
+
+class Clock:
+    """CUDA-event timing on one stream (the library context's)."""
+
+    def __init__(self, stream):
+        self.stream = stream
+
+    def __call__(self, fn):
+        import torch
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(self.stream):
+            a.record(self.stream)
+            fn()
+            b.record(self.stream)
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    def event(self):
+        import torch
+        e = torch.cuda.Event(enable_timing=True)
+        e.record(self.stream)
+        return e
+
+
+def e2e_chain(cg, L, g, clock, nsteps, host):
+    """nsteps steps through the C ABI, each: the pinned host buffer `host` (primitives) -> device,
+    one step of the run begun on g, the state -> the same buffer (which the next step reads).
+    Returns (total ms, upload ms, step ms, download ms) summed over the steps."""
+    import torch
+    n = host.numel()
+    ev = []
+    with torch.cuda.stream(clock.stream):
+        for _ in range(nsteps):
+            e0 = clock.event()
+            cg._lib.check(L.cosmos_grid_set_prim(g.h, host.data_ptr(), n))
+            e1 = clock.event()
+            g.run_steps(1)
+            e2 = clock.event()
+            cg._lib.check(L.cosmos_grid_get_prim(g.h, host.data_ptr(), n))
+            e3 = clock.event()
+            ev.append((e0, e1, e2, e3))
+    ev[-1][3].synchronize()
+    up = sum(a.elapsed_time(b) for a, b, _, _ in ev)
+    st = sum(b.elapsed_time(c) for _, b, c, _ in ev)
+    dn = sum(c.elapsed_time(d) for _, _, c, d in ev)
+    return ev[0][0].elapsed_time(ev[-1][3]), up, st, dn
+
+
+def guarded(fn):
+    """Runs one configuration's measurement; an exception becomes an error entry of the line."""
+    try:
+        return fn()
+    except Exception as e:  # the headline line still prints
+        return {"error": f"{type(e).__name__}: {e}", "trace": traceback.format_exc(limit=3)[-600:]}
+
+
 def cpu_baseline(n, seconds=12.0, threads=None):
     """Time the CPU oracle (FP64 restatement of the reference, line-parallel on all host cores) on
     the same workload: as many full-size Strang steps as fit in `seconds` (at least one)."""
@@ -180,20 +278,34 @@ def cpu_baseline(n, seconds=12.0, threads=None):
 
 
 def run_reference(args):
+    """The CPU arm: the oracle (bit-identical restatement of the reference) on all host threads, W
+    untimed and K timed full-size Strang steps of the headline workload."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    from oracle.pyoracle import Oracle
+    O = Oracle()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
     n = args.n
-    base = cpu_baseline(n, seconds=max(8.0, 2.0 * args.steps))
-    line = {"metric": METRIC, "value": base["value"], "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": n * n / base["value"] * 1e3,
+    s = four_quadrant(n, 2)
+    s, _, _, _ = O.solve(0, s, 2, 1.0 / n, 0.9, 1e9, 0.0, 2, 1.4, 1, max_steps=args.warmup)
+    t0 = time.perf_counter()
+    s, k, _, _ = O.solve(0, s, 2, 1.0 / n, 0.9, 1e9, 0.0, 2, 1.4, 1, max_steps=args.steps)
+    el = time.perf_counter() - t0
+    value = k * n * n / el
+    base = {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"{args.warmup} untimed and {k} timed full {n}x{n} Strang steps of the FP64 oracle "
+                      f"(restatement of the reference, bit-identical to it) in {el:.1f} s on {cores} host threads"}
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / k * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "n": n, "cells": n * n},
-            "cpu_baseline": base,
-            "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "data": "synthetic", "config": grid_config(n, args.gpus), "cpu_baseline": base,
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- the headline workload
 def run_ours(args):
     import torch
     import cosmos_gb300 as cg
@@ -203,29 +315,29 @@ def run_ours(args):
     L = cg.load()
     ctx = cg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
+    clock = Clock(stream)
     n = args.n
     s0 = four_quadrant(n, 2)
     cells = n * n
-    barrier, max_over_ranks = ranks.barrier, ranks.max
 
     # ---------------- FP32 resident: value
     g = cg.Grid(cg.NEWTONIAN, (n, n), 1.0 / n, 1.4, cg.FP32, cg.BC_PERIODIC, ctx=ctx)
     g.set_prim(s0)
     g.run_begin(2, 0.9, 1e30, 0.0, cg.MINBEE)
-    g.run_steps(args.warmup)
-    ctx.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    launches0 = L.cosmos_kernel_launches()
-    barrier()
-    with Clocks(local) as clk:
+    with Clocks(local) as clk:  # sampled over the warm-up and the timed steps
+        g.run_steps(args.warmup)
+        ctx.synchronize()
+        launches0 = L.cosmos_kernel_launches()
+        ranks.barrier()
         with torch.cuda.stream(stream):
             e0.record(stream)
             g.run_steps(args.steps)
             e1.record(stream)
         e1.synchronize()
-    barrier()
+        ranks.barrier()
     launches = L.cosmos_kernel_launches() - launches0
-    ms = max_over_ranks(e0.elapsed_time(e1)) / args.steps
+    ms = ranks.max(e0.elapsed_time(e1)) / args.steps
     r = g.run_end()
     value = ranks.throughput(cells, ms)
 
@@ -238,12 +350,11 @@ def run_ours(args):
             g.sweep(1, 2, dt_probe, 0.0, cg.MINBEE)
         for _ in range(max(4, args.steps // 2)):
             for ax, key in ((0, "x"), (1, "y")):
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record(stream)
+                a = clock.event()
                 g.sweep(ax, 2, dt_probe, 0.0, cg.MINBEE)
-                b.record(stream)
-                kern[key].append((a, b))
+                kern[key].append((a, clock.event()))
     torch.cuda.synchronize()
+    g.close()
     kx = statistics.mean(a.elapsed_time(b) for a, b in kern["x"])
     ky = statistics.mean(a.elapsed_time(b) for a, b in kern["y"])
     peak, peak_kind = peaks()
@@ -252,54 +363,19 @@ def run_ours(args):
     y_gbs = bytes_sweep / (ky * 1e-3) / 1e9
     step_gbs = cells * 120 / (ms * 1e-3) / 1e9
 
-    # ---------------- e2e: per step, host state in -> step -> host state out (pinned buffers)
-    host_in = torch.empty((n, n, 5), dtype=torch.float64, pin_memory=True)
-    host_out = torch.empty((n, n, 5), dtype=torch.float64, pin_memory=True)
-    host_in.numpy()[...] = s0
+    # ---------------- e2e: K steps chained through one pinned host buffer
+    host = torch.empty((n, n, 5), dtype=torch.float64, pin_memory=True)
+    host.numpy()[...] = s0
     ge = cg.Grid(cg.NEWTONIAN, (n, n), 1.0 / n, 1.4, cg.FP32, cg.BC_PERIODIC, ctx=ctx)
     ge.set_prim(s0)
     ge.run_begin(2, 0.9, 1e30, 0.0, cg.MINBEE)
-    nbytes = cells * 5 * 8
-    e2e_steps = max(3, min(args.steps, 10))
-    for _ in range(2):
-        L.cosmos_grid_set_prim(ge.h, host_in.data_ptr(), cells * 5)
-        ge.run_steps(1)
-        L.cosmos_grid_get_prim(ge.h, host_out.data_ptr(), cells * 5)
-    barrier()
-    with torch.cuda.stream(stream):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        for _ in range(e2e_steps):
-            cg._lib.check(L.cosmos_grid_set_prim(ge.h, host_in.data_ptr(), cells * 5))
-            ge.run_steps(1)
-            cg._lib.check(L.cosmos_grid_get_prim(ge.h, host_out.data_ptr(), cells * 5))
-        b.record(stream)
-        b.synchronize()
-    e2e_ms = max_over_ranks(a.elapsed_time(b)) / e2e_steps
-    e2e_value = ranks.throughput(cells, e2e_ms)
+    e2e_chain(cg, L, ge, clock, 2, host)  # warm-up (staging, conversion kernels)
+    host.numpy()[...] = s0
+    ranks.barrier()
+    tot, up, st, dn = e2e_chain(cg, L, ge, clock, args.steps, host)
     ge.close()
-
-    # ---------------- FP64 (reference-exact) on the same workload, and the FP32-vs-FP64 error
-    nerr = args.err_steps
-    g32 = cg.Grid(cg.NEWTONIAN, (n, n), 1.0 / n, 1.4, cg.FP32, cg.BC_PERIODIC, ctx=ctx)
-    g32.set_prim(s0)
-    g32.solve(2, 0.9, 1e30, 0.0, cg.MINBEE, max_steps=nerr)
-    rho32 = g32.get_prim()[..., 0].copy()
-    g32.close()
-    g64 = cg.Grid(cg.NEWTONIAN, (n, n), 1.0 / n, 1.4, cg.FP64, cg.BC_PERIODIC, ctx=ctx)
-    g64.set_prim(s0)
-    g64.run_begin(2, 0.9, 1e30, 0.0, cg.MINBEE, max_steps=nerr)
-    with torch.cuda.stream(stream):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        g64.run_steps(nerr)
-        b.record(stream)
-        b.synchronize()
-    ms64 = max_over_ranks(a.elapsed_time(b)) / nerr
-    g64.run_end()
-    rho64 = g64.get_prim()[..., 0]
-    g64.close()
-    l1 = float(np.abs(rho32 - rho64).mean() / np.abs(rho64).mean())
+    e2e_ms = ranks.max(tot) / args.steps
+    nbytes = cells * 5 * 8
 
     if rank != 0:
         return
@@ -308,16 +384,14 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n": n, "cells_per_gpu": cells, "precision": "fp32 bulk",
-                   "l2": "state 335 MB > 129 MB L2 (no flush needed)", "parallelism": f"replicas x{world}",
-                   "device_dt": True, "graph_replay": True, "steps_completed": r.steps},
-        "fp64": {"value": cells * world / (ms64 * 1e-3), "ms_per_step": ms64, "steps": nerr,
-                 "path": "plain FP64, bit-identical to the reference"},
-        "l1_rho_fp32_vs_fp64": l1, "l1_steps": nerr,
-        "fp32_over_fp64": ms64 / ms,
-        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                "ms_per_step": e2e_ms, "steps": e2e_steps,
-                "what": "per step: pinned host AoS FP64 primitives -> device, one Strang step, state -> host"},
+        "config": grid_config(n, args.gpus),
+        "run": {"device_dt": True, "graph_replay": True, "steps_completed": r.steps, "status": r.status},
+        "e2e": {"value": ranks.throughput(cells, e2e_ms), "unit": METRIC, "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms, "steps": args.steps,
+                "h2d_ms": up / args.steps, "compute_ms": st / args.steps, "d2h_ms": dn / args.steps,
+                "h2d_gbs": nbytes / (up / args.steps * 1e-3) / 1e9, "d2h_gbs": nbytes / (dn / args.steps * 1e-3) / 1e9,
+                "what": "per step: pinned host AoS FP64 primitives -> device (copy + conversion to FP32 conserved), "
+                        "one Strang step, state -> the same host buffer, which the next step reads"},
         "roofline": {"bound": "hbm", "kernel": "sweep_x_pair_kernel (X sweep, FP32 cell pairs)",
                      "achieved": x_gbs, "peak": peak, "unit": "GB/s", "frac": x_gbs / peak,
                      "peak_source": peak_kind, "traffic": traffic_per_launch("sweep_x_fp32"),
@@ -326,13 +400,259 @@ def run_ours(args):
                      "step": {"achieved": step_gbs, "frac": step_gbs / peak, "bytes_per_cell_update": 120}},
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
-        "status": r.status,
     }
     if base:
         line["cpu_baseline"] = base
+    if not args.no_extras:
+        with Clocks(local) as clk2:
+            line["configs"] = all_configs(cg, L, ctx, stream, args)
+        line["clocks_configs"] = clk2.summary()
     print(json.dumps(line), flush=True)
 
 
+def all_configs(cg, L, ctx, stream, args):
+    """Every other configuration, measured in this process after the headline (state resident in
+    HBM unless an e2e says otherwise); an exception in one becomes that entry's error."""
+    out = {}
+    steps = [("sod", lambda: measure_sod(cg, ctx, stream)),
+             ("grid_parity", lambda: measure_grid_parity(cg, ctx, stream, args.n, args.parity_steps)),
+             ("sr", lambda: measure_sr(cg, L, ctx, stream, 2048, args.sr_steps, args.warmup)),
+             ("gr", lambda: measure_gr(cg, L, ctx, stream, 1024, args.gr_steps, args.warmup)),
+             ("batch", lambda: measure_batch(cg, L, ctx, stream, max(args.steps, 20), args.warmup)),
+             ("adjoint", lambda: adjoint_measure(cg, ctx)),
+             ("rel_adjoint", lambda: measure_rel_adjoint(cg, ctx))]
+    for name, fn in steps:
+        t0 = time.perf_counter()
+        out[name] = guarded(fn)
+        out[name]["wall_s"] = time.perf_counter() - t0
+    return out
+
+
+# ---------------------------------------------------------------- configuration 1: Sod, FP64
+SOD_WORKLOAD = "1D Newtonian Euler Sod shock tube, SLIC van Leer, FP64, 1000 cells on [0,1], gamma 1.4, CFL 0.9, " \
+               "transmissive, t = 0.25"
+# The reference's own run of this problem (built from its sources): 613 steps, rho[500] at t = 0.25.
+SOD_STEPS, SOD_RHO500 = 613, 0.42639270172959448
+
+
+def measure_sod(cg, ctx, stream):
+    import cases
+    import torch
+    clock = Clock(torch.cuda.ExternalStream(ctx.stream))
+    s = cases.sod(1000)
+    g = cg.Grid(cg.NEWTONIAN, (1000,), 1.0 / 1000, 1.4, cg.FP64, ctx=ctx)
+    res = []
+    for _ in range(2):  # the first solve captures the step graph
+        g.set_prim(s)
+        ms = clock(lambda: res.append(g.solve(2, 0.9, 0.25, 0.0, cg.VANLEER)))
+    r = res[-1]
+    rho = g.get_prim()[..., 0]
+    g.close()
+    return {"workload": SOD_WORKLOAD, "dtype": "f64", "value": r.steps * 1000 / (ms * 1e-3), "unit": METRIC,
+            "ms_per_run": ms, "steps": r.steps, "t": r.t, "rho500": float(rho[500]),
+            "matches_reference_run": bool(r.steps == SOD_STEPS and float(rho[500]) == SOD_RHO500),
+            "note": "1000 cells: launch-bound (one host round trip per solve, 613 graph-replayed steps)"}
+
+
+# ---------------------------------------------------------------- configuration 2 at full length
+def measure_grid_parity(cg, ctx, stream, n, steps):
+    """The headline workload run `steps` steps in FP32 and in the FP64 (reference-exact) path, each
+    with its own CFL time steps: the FP64 path's rate, the FP32-vs-FP64 relative L1 density error,
+    and both runs' mass and energy drift (periodic boundaries conserve both exactly)."""
+    clock = Clock(stream)
+    s0 = four_quadrant(n, 2)
+    tot0 = newton_totals(s0, 1.4)
+    out = {"workload": WORKLOAD, "steps": steps}
+    prims = {}
+    for prec, tag in ((cg.FP32, "fp32"), (cg.FP64, "fp64")):
+        g = cg.Grid(cg.NEWTONIAN, (n, n), 1.0 / n, 1.4, prec, cg.BC_PERIODIC, ctx=ctx)
+        g.set_prim(s0)
+        g.run_begin(2, 0.9, 1e30, 0.0, cg.MINBEE, max_steps=steps)
+        ms = clock(lambda: g.run_steps(steps)) / steps
+        r = g.run_end()
+        p = g.get_prim()
+        sums = g.field_sums() if prec == cg.FP32 else None
+        g.close()
+        prims[tag] = p
+        out[tag] = {"value": n * n / (ms * 1e-3), "ms_per_step": ms, "t": r.t, "steps_completed": r.steps,
+                    "status": r.status, "drift": drift(tot0, newton_totals(p, 1.4))}
+        if sums is not None:  # the stored FP32 conserved totals, compensated on the device
+            out[tag]["drift_stored"] = {"mass": abs(sums[0] - tot0[0]) / tot0[0],
+                                        "energy": abs(sums[4] - tot0[1]) / tot0[1]}
+    out["l1_rho_fp32_vs_fp64"] = rel_l1(prims["fp32"][..., 0], prims["fp64"][..., 0])
+    out["l1_bound"] = 1e-5
+    out["fp32_over_fp64"] = out["fp64"]["ms_per_step"] / out["fp32"]["ms_per_step"]
+    return out
+
+
+# ---------------------------------------------------------------- configuration 3: SR Kelvin-Helmholtz
+SR_WORKLOAD = "2D special-relativistic Euler (gamma 5/3), SLIC MinBee, CFL 0.9, 2048x2048 on the periodic " \
+              "unit square, Kelvin-Helmholtz shear layers (vx = +-0.5 tanh profile, rho in {1, 2}, p = 1, " \
+              "vy = 0.01 sin(4 pi x + phase), phase seed 3; Lorentz factor <= 1.16); 200 steps"
+
+
+def measure_sr(cg, L, ctx, stream, n, steps, warmup):
+    """Configuration 3 as stated (FP32 bulk, every primitive recovery's Newton iterations finished
+    in FP64), the FP32-Newton variant (FP64 stage only above a Lorentz factor of 2), and the FP64
+    reference-exact path, all over the same `steps` steps from the same data."""
+    import cases
+    import torch
+    clock = Clock(stream)
+    s0 = cases.kelvin_helmholtz(n, 3)
+    gam = 5.0 / 3.0
+    tot0 = sr_totals(s0, gam)
+    peak, peak_kind = peaks()
+
+    def make(prec, above):
+        g = cg.Grid(cg.SR, (n, n), 1.0 / n, gam, prec, cg.BC_PERIODIC, ctx=ctx, sr_c2p64_above=above)
+        g.set_prim(s0)
+        return g
+
+    out = {"workload": SR_WORKLOAD, "steps": steps}
+    prims = {}
+    for tag, prec, above in (("fp32_c2p_fp64", cg.FP32, 0.0), ("fp32_newton_variant", cg.FP32, 2.0),
+                             ("fp64", cg.FP64, 2.0)):
+        g = make(prec, above)
+        if prec == cg.FP32:  # warm-up run (graph capture), then the timed run from the same data
+            g.run_begin(2, 0.9, 1e30, 0.0, cg.MINBEE, max_steps=warmup)
+            g.run_steps(warmup)
+            g.run_end()
+            g.set_prim(s0)
+        g.run_begin(2, 0.9, 1e30, 0.0, cg.MINBEE, max_steps=steps)
+        ms = clock(lambda: g.run_steps(steps)) / steps
+        r = g.run_end()
+        prims[tag] = g.get_prim()
+        g.close()
+        bpc = 120 if prec == cg.FP32 else 240
+        out[tag] = {"value": n * n / (ms * 1e-3), "ms_per_step": ms, "t": r.t, "steps_completed": r.steps,
+                    "status": r.status, "drift": drift(tot0, sr_totals(prims[tag], gam)),
+                    "roofline_frac": n * n * bpc / (ms * 1e-3) / 1e9 / peak}
+    for tag in ("fp32_c2p_fp64", "fp32_newton_variant"):
+        out[tag]["l1_rho_vs_fp64"] = rel_l1(prims[tag][..., 0], prims["fp64"][..., 0])
+    out["fp32_c2p_fp64"]["what"] = "config 3 as stated: FP32 bulk, FP64 Newton iterations in every primitive recovery"
+    out["fp32_newton_variant"]["what"] = "variant: FP32 Newton iterations, FP64 only above Lorentz factor 2 " \
+                                         "(not reached here) or on FP32 non-convergence"
+    out["value"] = out["fp32_c2p_fp64"]["value"]
+    # e2e of the as-stated path over the same steps, chained through one pinned host buffer
+    host = torch.empty((n, n, 5), dtype=torch.float64, pin_memory=True)
+    host.numpy()[...] = s0
+    ge = make(cg.FP32, 0.0)
+    ge.run_begin(2, 0.9, 1e30, 0.0, cg.MINBEE, max_steps=steps)
+    tot, up, st, dn = e2e_chain(cg, L, ge, clock, steps, host)
+    ge.close()
+    nb = n * n * 40
+    out["e2e"] = {"value": n * n * steps / (tot * 1e-3), "ms_per_step": tot / steps, "steps": steps,
+                  "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb, "h2d_ms": up / steps,
+                  "compute_ms": st / steps, "d2h_ms": dn / steps}
+    out["roofline_note"] = "compute-bound: five primitive recoveries per cell per sweep"
+    return out
+
+
+# ---------------------------------------------------------------- configuration 4: black-hole accretion
+GR_WORKLOAD = "2D black-hole Euler in Kerr-Schild Schwarzschild spacetime (M = 1), SLIC van Leer + " \
+              "RK4 source (BlackHoleEulerForcingSolver, one subcycle), CFL 0.9, 1024x1024 on [-10, 10]^2 " \
+              "(dx = 20/1024, hole at (10, 10) of the grid's coordinates), excision r <= 2M, rho = 1 with 1% " \
+              "log-normal noise (seed 4), p = 0.01, transmissive; 100 steps"
+GR_HOLE = (1.0, 0.0, 10.0, 10.0, 0.0)
+
+
+def gr_state(n, seed=4):
+    rng = np.random.default_rng(seed)
+    s = np.zeros((n, n, 5))
+    s[..., 0] = np.exp(0.01 * rng.standard_normal((n, n)))
+    s[..., 4] = 0.01
+    return s
+
+
+def gr_step_fixed(g, dt, nsub=1, lim=1):
+    """One solver step with a given dt, as the library's run enqueues it: the RK source half-steps,
+    X(dt/2) Y(dt) X(dt/2), the RK source half-steps (Solvers/BlackHoleEulerSecondOrderSolver.cpp:181-218)."""
+    for _ in range(nsub):
+        g.rk_source(0.5 * (dt / nsub), 0.0, 1)
+    g.sweep(0, 2, 0.5 * dt, 0.0, lim)
+    g.sweep(1, 2, dt, 0.0, lim)
+    g.sweep(0, 2, 0.5 * dt, 0.0, lim)
+    for _ in range(nsub):
+        g.rk_source(0.5 * (dt / nsub), 0.0, 1)
+
+
+def measure_gr(cg, L, ctx, stream, n, steps, warmup, r_cut=5.0):
+    """Configuration 4: the FP32 bulk path's own run (CFL time steps), the FP64 reference-exact path
+    over the same number of steps driven by its own CFL rule, and the FP32 path driven by the FP64
+    run's time-step sequence, so that the density error over r > r_cut M compares the solutions at
+    equal times (the free-running runs' time steps part where the horizon cells' speeds differ)."""
+    import torch
+    clock = Clock(stream)
+    s0 = gr_state(n)
+    dx = 20.0 / n
+    bh = cg.BlackHoleSpacetime(*GR_HOLE)
+    x = np.arange(n) * dx
+    X, Y = np.meshgrid(x, x)
+    rr = np.sqrt((X - GR_HOLE[2]) ** 2 + (Y - GR_HOLE[3]) ** 2)
+    far = rr > r_cut * GR_HOLE[0]
+    peak, peak_kind = peaks()
+
+    def make(prec):
+        g = cg.Grid(cg.GR, (n, n), dx, 5.0 / 3.0, prec, cg.BC_TRANSMISSIVE, bh, ctx=ctx)
+        g.set_prim(s0)
+        return g
+
+    out = {"workload": GR_WORKLOAD, "steps": steps}
+    # FP32 free-running (own CFL steps): the configuration's value
+    g = make(cg.FP32)
+    g.run_begin(2, 0.9, 1e30, 0.0, cg.VANLEER, max_steps=warmup)
+    g.run_steps(warmup)
+    g.run_end()
+    g.set_prim(s0)
+    g.run_begin(2, 0.9, 1e30, 0.0, cg.VANLEER, max_steps=steps)
+    ms = clock(lambda: g.run_steps(steps)) / steps
+    r = g.run_end()
+    free32 = g.get_prim()
+    g.close()
+    out["fp32"] = {"value": n * n / (ms * 1e-3), "ms_per_step": ms, "t": r.t, "steps_completed": r.steps,
+                   "status": r.status, "roofline_frac": n * n * 200 / (ms * 1e-3) / 1e9 / peak,
+                   "what": "FP32 bulk; metric from FP64 tables; primitive recovery finished in FP64 above W = 2 "
+                           "or on FP32 non-convergence"}
+    out["value"] = out["fp32"]["value"]
+    # FP64 driven by its own CFL rule, and FP32 driven by the FP64 run's dts
+    g64, g32 = make(cg.FP64), make(cg.FP32)
+    t, ms64, dts = 0.0, 0.0, []
+    for it in range(steps):
+        dt = g64.stable_dt(0.9, t, 1e30, it)
+        ms64 += clock(lambda: gr_step_fixed(g64, dt))
+        gr_step_fixed(g32, dt)
+        dts.append(dt)
+        t += dt
+    p64, p32 = g64.get_prim(), g32.get_prim()
+    g64.close()
+    g32.close()
+    out["fp64"] = {"value": n * n * steps / (ms64 * 1e-3), "ms_per_step": ms64 / steps, "t": t,
+                   "path": "plain FP64, bit-identical to the reference; its CFL time steps (host-driven loop)"}
+    out["l1_rho_fp32_vs_fp64_same_dts"] = rel_l1(p32[..., 0][far], p64[..., 0][far])
+    out["l1_rho_fp32_vs_fp64_free_running"] = rel_l1(free32[..., 0][far], p64[..., 0][far])
+    out["l1_cells"] = f"r > {r_cut} M ({int(far.sum())} cells)"
+    out["t_free_running_fp32"] = r.t
+    out["dt_first_last"] = [dts[0], dts[-1]]
+    out["density_total_diff_same_dts"] = abs(float(p32[..., 0][far].sum() - p64[..., 0][far].sum())) / \
+        float(p64[..., 0][far].sum())
+    out["drift_note"] = "no conserved total here (inflow through the boundary and into the excised hole): " \
+                        "the FP32-vs-FP64 difference of the density total over the same cells is given"
+    # e2e of the FP32 path over the same steps
+    host = torch.empty((n, n, 5), dtype=torch.float64, pin_memory=True)
+    host.numpy()[...] = s0
+    ge = make(cg.FP32)
+    ge.run_begin(2, 0.9, 1e30, 0.0, cg.VANLEER, max_steps=steps)
+    tot, up, st, dn = e2e_chain(cg, L, ge, clock, steps, host)
+    ge.close()
+    nb = n * n * 40
+    out["e2e"] = {"value": n * n * steps / (tot * 1e-3), "ms_per_step": tot / steps, "steps": steps,
+                  "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb, "h2d_ms": up / steps,
+                  "compute_ms": st / steps, "d2h_ms": dn / steps}
+    out["fp32_over_fp64"] = out["fp64"]["ms_per_step"] / ms
+    return out
+
+
+# ---------------------------------------------------------------- configuration 5: batched uneven grids
 BATCH_WORKLOAD = "256 independent Newtonian Euler grids (1D and 2D), every side log-uniform in " \
                  "[128, 2048] cells (seed 5), seeded Riemann data, SLIC MinBee, CFL 0.9, transmissive, dx = 1/nx"
 
@@ -345,67 +665,40 @@ def batch_problem():
     return shapes, states, dxs
 
 
-def batch_cpu_baseline(shapes, states, dxs, seconds=12.0):
-    """The CPU oracle on the batched workload: one step of each grid in turn (the grids are
-    independent) until `seconds` have passed; cell-updates per second."""
-    from oracle.pyoracle import Oracle
-    O = Oracle()
-    cores = os.cpu_count() or 1
-    O.set_threads(cores)
-    t0 = time.perf_counter()
-    cells = grids = 0
-    for k in range(len(shapes)):
-        O.solve(0, states[k], 2, dxs[k], 0.9, 1e9, 0.0, 2, 1.4, 0, max_steps=1)
-        cells += int(np.prod(shapes[k]))
-        grids += 1
-        if time.perf_counter() - t0 >= seconds:
-            break
-    el = time.perf_counter() - t0
-    return {"value": cells / el, "unit": METRIC, "cores": cores, "kind": "port",
-            "sample": f"one FP64 oracle step of each of the first {grids} grids ({cells} cells) in {el:.1f} s "
-                      f"on {cores} host threads"}
-
-
-def run_batch(args):
+def measure_batch(cg, L, ctx, stream, steps, warmup, l1_steps=20, tiles=False):
+    """Configuration 5: the FP32 batch in one persistent graph-replayed launch (tile shape from the
+    autotuner), the same grids stepped one by one, the FP64 batch and the FP32-vs-FP64 density
+    error over `l1_steps` steps, and an e2e over the value's steps."""
     import torch
-    import cosmos_gb300 as cg
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    L = cg.load()
-    ctx = cg.Context(local)
-    stream = torch.cuda.ExternalStream(ctx.stream)
+    clock = Clock(stream)
     shapes, states, dxs = batch_problem()
     cells = sum(int(np.prod(sh)) for sh in shapes)
     bytes_step = sum(int(np.prod(sh)) * (120 if len(sh) == 2 else 40) for sh in shapes)
-
-    def timed(fn):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        with torch.cuda.stream(stream):
-            a.record(stream)
-            fn()
-            b.record(stream)
-        b.synchronize()
-        return a.elapsed_time(b)
-
+    peak, peak_kind = peaks()
     b = cg.Batch(shapes, dxs, 1.4, cg.FP32, cg.BC_TRANSMISSIVE, ctx=ctx)
     for k, s in enumerate(states):
         b.set_prim(k, s)
     b.run_begin(0.9, 1e30, 0.0, cg.MINBEE)
     tile_ms = {f"{nt}x{seg}{'c' if cap else ''}": b.time_shape(nt, seg, cap, steps=5)
-               for nt in (128, 256) for seg in (32, 64) for cap in (0, 1)}
+               for nt in (128, 256) for seg in (32, 64) for cap in (0, 1)} if tiles else None
     tuned, _ = b.autotune(None)
-    b.run_steps(args.warmup)
+    b.run_steps(warmup)
     launches0 = L.cosmos_kernel_launches()
-    with Clocks(local) as clk:
-        ms = timed(lambda: b.run_steps(args.steps)) / args.steps
+    ms = clock(lambda: b.run_steps(steps)) / steps
     launches = L.cosmos_kernel_launches() - launches0
     res = b.run_end()
-    value = cells / (ms * 1e-3)
-    peak, peak_kind = peaks()
-    gbs = bytes_step / (ms * 1e-3) / 1e9
-
-    # the same grids advanced one by one (each its own graph-replayed steps), for comparison
+    b.close()
+    out = {"workload": BATCH_WORKLOAD, "grids": len(shapes), "grids_2d": sum(len(s) == 2 for s in shapes),
+           "cells": cells, "tile_shape": list(tuned), "steps": steps,
+           "value": cells / (ms * 1e-3), "ms_per_step": ms, "gpu_launches": int(launches),
+           "roofline": {"bound": "hbm", "kernel": "batch_pair_kernel (whole step)",
+                        "achieved": bytes_step / (ms * 1e-3) / 1e9, "peak": peak,
+                        "frac": bytes_step / (ms * 1e-3) / 1e9 / peak,
+                        "bytes_per_cell_update": "40 (1D), 120 (2D)"},
+           "status": [x.status for x in res if x.status][:8]}
+    if tile_ms:
+        out["tile_ms_per_step"] = tile_ms
+    # the same grids advanced one by one (each its own graph-replayed steps)
     ku = 5
     singles = []
     for k, sh in enumerate(shapes):
@@ -414,33 +707,41 @@ def run_batch(args):
         g.run_begin(2, 0.9, 1e30, 0.0, cg.MINBEE)
         g.run_steps(3)
         singles.append(g)
-    ms_u = timed(lambda: [g.run_steps(ku) for g in singles]) / ku
+    ms_u = clock(lambda: [g.run_steps(ku) for g in singles]) / ku
     for g in singles:
         g.close()
-
+    out["unbatched"] = {"value": cells / (ms_u * 1e-3), "ms_per_step": ms_u}
     # FP64 batch (bit-identical to the reference per grid) and the FP32-vs-FP64 density error
-    nerr = 10
     b64 = cg.Batch(shapes, dxs, 1.4, cg.FP64, cg.BC_TRANSMISSIVE, ctx=ctx)
     b32 = cg.Batch(shapes, dxs, 1.4, cg.FP32, cg.BC_TRANSMISSIVE, ctx=ctx)
     for k, s in enumerate(states):
         b64.set_prim(k, s)
         b32.set_prim(k, s)
-    b64.run_begin(0.9, 1e30, 0.0, cg.MINBEE, max_steps=nerr)
+    b64.run_begin(0.9, 1e30, 0.0, cg.MINBEE, max_steps=l1_steps)
     b64.autotune(None)
-    ms64 = timed(lambda: b64.run_steps(nerr)) / nerr
+    ms64 = clock(lambda: b64.run_steps(l1_steps)) / l1_steps
     b64.run_end()
-    b32.run_begin(0.9, 1e30, 0.0, cg.MINBEE, max_steps=nerr)
+    b32.run_begin(0.9, 1e30, 0.0, cg.MINBEE, max_steps=l1_steps)
     b32.set_shape(*tuned)
-    b32.run_steps(nerr)
+    b32.run_steps(l1_steps)
     b32.run_end()
     num = den = 0.0
+    m32 = m64 = 0.0
     for k in range(len(shapes)):
         r64 = b64.get_prim(k)[..., 0]
-        num += float(np.abs(b32.get_prim(k)[..., 0] - r64).sum())
+        r32 = b32.get_prim(k)[..., 0]
+        num += float(np.abs(r32 - r64).sum())
         den += float(np.abs(r64).sum())
+        m32 += float(r32.sum())
+        m64 += float(r64.sum())
     b64.close()
     b32.close()
-
+    out["fp64"] = {"value": cells / (ms64 * 1e-3), "ms_per_step": ms64, "steps": l1_steps,
+                   "path": "FP64 batch, bit-identical to the reference per grid"}
+    out["l1_rho_fp32_vs_fp64"] = num / den
+    out["l1_steps"] = l1_steps
+    out["density_total_diff"] = abs(m32 - m64) / m64
+    out["drift_note"] = "transmissive boundaries exchange mass; the FP32-vs-FP64 difference of the density total"
     # e2e: per step, every grid's primitive state host -> device, one batched step, state -> host
     hosts = [torch.empty(sh + (5,), dtype=torch.float64, pin_memory=True) for sh in shapes]
     for h, s in zip(hosts, states):
@@ -456,47 +757,18 @@ def run_batch(args):
         for k, h in enumerate(hosts):
             cg._lib.check(L.cosmos_batch_get_prim(be.h, k, h.data_ptr(), h.numel()))
     e2e_step()
-    e2e_steps = 3
-    e2e_ms = timed(lambda: [e2e_step() for _ in range(e2e_steps)]) / e2e_steps
+    e2e_steps = min(steps, 10)
+    e2e_ms = clock(lambda: [e2e_step() for _ in range(e2e_steps)]) / e2e_steps
     be.close()
     nbytes = cells * 5 * 8
-
-    adj = adjoint_measure(cg, ctx)
-    base = None if args.no_cpu else batch_cpu_baseline(shapes, states, dxs, args.cpu_seconds)
-    line = {
-        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": BATCH_WORKLOAD, "grids": len(shapes), "grids_2d": sum(len(s) == 2 for s in shapes),
-                   "cells": cells, "precision": "fp32 bulk", "tile_shape": list(tuned),
-                   "l2": f"state {cells * 40 / 1e9:.2f} GB > 129 MB L2 (no flush needed)",
-                   "launch": "one persistent cooperative kernel per 10 steps, replayed from a CUDA graph"},
-        "tile_ms_per_step": tile_ms,
-        "unbatched": {"value": cells / (ms_u * 1e-3), "ms_per_step": ms_u,
-                      "what": "the same grids stepped one after another, each by its own graph-replayed steps"},
-        "fp64": {"value": cells / (ms64 * 1e-3), "ms_per_step": ms64, "steps": nerr,
-                 "path": "FP64 batch, bit-identical to the reference per grid"},
-        "l1_rho_fp32_vs_fp64": num / den, "l1_steps": nerr,
-        "e2e": {"value": cells / (e2e_ms * 1e-3), "unit": METRIC, "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms, "steps": e2e_steps,
-                "what": "per step: each grid's pinned host AoS FP64 primitives -> device, one batched step, "
-                        "states -> host"},
-        "roofline": {"bound": "hbm", "kernel": "batch_pair_kernel (whole step, FP32 cell pairs)",
-                     "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak, "peak_source": peak_kind,
-                     "traffic": (traffic_per_launch("batch_step_fp32_ratio") or 0.0) * bytes_step or None,
-                     "traffic_note": "per step; ncu ratio traffic/algorithmic of a 64-grid capture x this "
-                                     "workload's algorithmic bytes", "algorithmic_bytes_per_step": bytes_step,
-                     "bytes_per_cell_update": "40 (1D), 120 (2D)"},
-        "adjoint": adj,
-        "clocks": clk.summary(),
-        "gpu_launches": int(launches),
-        "status": [r.status for r in res if r.status][:8],
-    }
-    if base:
-        line["cpu_baseline"] = base
-    print(json.dumps(line), flush=True)
+    out["e2e"] = {"value": cells / (e2e_ms * 1e-3), "unit": METRIC, "h2d_bytes_per_step": nbytes,
+                  "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms, "steps": e2e_steps,
+                  "what": "per step: each grid's pinned host AoS FP64 primitives -> device, one batched step, "
+                          "states -> host (256 calls each way)"}
+    return out
 
 
+# ---------------------------------------------------------------- adjoints
 def adjoint_measure(cg, ctx, n=2048, nsteps=100, every=10):
     """Adjoint of `nsteps` SLIC steps (checkpoint every `every`) of the loss 1/2 |rho_T - target|^2 on
     the batch's largest grid size (n x n, FP32, seeded Riemann data, seeded target), timed against
@@ -544,81 +816,57 @@ def adjoint_measure(cg, ctx, n=2048, nsteps=100, every=10):
     gq.close()
     an = float(np.sum(grad * d))
     return {"grid": f"{n}x{n} FP32, seeded Riemann data", "steps": nsteps, "checkpoint_every": every,
-            "forward_ms": fwd, "backward_ms": bwd, "adjoint_over_forward": bwd / fwd,
+            "forward_ms": fwd, "backward_ms": bwd, "adjoint_over_forward": bwd / fwd, "target": 3.0,
             "what": "backward = recomputation of each checkpoint segment + the sweep adjoints, per forward "
                     "pass of the same steps (graph-replayed, checkpoints stored)",
             "fd_check": {"grid": f"{m}x{m} FP64 smooth data", "steps": nsteps, "h": h,
                          "rule": "h = 1e-6, 1e-7, ... until two successive central differences agree to 1e-5",
                          "fd_by_h": {f"{x:.0e}": v for x, v in zip(hs, fds)},
-                         "directional_adjoint": an, "directional_fd": fd, "rel_err": abs(fd - an) / abs(an)}}
+                         "directional_adjoint": an, "directional_fd": fd, "rel_err": abs(fd - an) / abs(an),
+                         "bound": 1e-4}}
 
 
-def run_batch_reference(args):
-    rank, _, _ = dist_env()
-    if rank != 0:
-        return
-    shapes, states, dxs = batch_problem()
-    cells = sum(int(np.prod(sh)) for sh in shapes)
-    base = batch_cpu_baseline(shapes, states, dxs, max(8.0, 2.0 * args.steps))
-    line = {"metric": METRIC, "value": base["value"], "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": cells / base["value"] * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": BATCH_WORKLOAD, "grids": len(shapes), "cells": cells},
-            "cpu_baseline": base,
-            "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
-
-
-# ---------------------------------------------------------------- SR (2048^2 Kelvin-Helmholtz) and GR (1024^2 accretion)
-SR_WORKLOAD = "2D special-relativistic Euler (gamma 5/3), SLIC MinBee, CFL 0.9, 2048x2048 on the periodic " \
-              "unit square, Kelvin-Helmholtz shear layers (vx = +-0.5 tanh profile, rho in {1, 2}, p = 1, " \
-              "vy = 0.01 sin(4 pi x + phase), phase seed 3; Lorentz factor <= 1.16); 200 steps"
-GR_WORKLOAD = "2D black-hole Euler in Kerr-Schild Schwarzschild spacetime (M = 1), SLIC van Leer + " \
-              "RK4 source (BlackHoleEulerForcingSolver, one subcycle), CFL 0.9, 1024x1024 on [-10, 10]^2 " \
-              "(dx = 20/1024, hole at (10, 10) of the grid's coordinates), excision r <= 2M, rho = 1 with 1% " \
-              "log-normal noise (seed 4), p = 0.01, transmissive; 100 steps"
-
-
-def gr_state(n, seed=4):
-    rng = np.random.default_rng(seed)
-    s = np.zeros((n, n, 5))
-    s[..., 0] = np.exp(0.01 * rng.standard_normal((n, n)))
-    s[..., 4] = 0.01
-    return s
-
-
-def grid_problem(kind, n):
-    """(system, state, dx, gamma, boundary, limiter, black hole, subcycles)"""
+def measure_rel_adjoint(cg, ctx, sr_n=2048, sr_steps=2, gr_n=1024, gr_steps=1):
+    """Adjoint-to-forward cost of the special-relativistic (Kelvin-Helmholtz, FP64) and black-hole
+    (accretion, FP64, one RK source half-step on each side of the flux step) adjoints at their
+    configurations' sizes, over a bounded number of steps (checkpoint every step)."""
     import cases
-    if kind == "sr":
-        return 1, cases.kelvin_helmholtz(n, 3), 1.0 / n, 5.0 / 3.0, 1, 2, None, 1
-    return 2, gr_state(n), 20.0 / n, 5.0 / 3.0, 0, 1, (1.0, 0.0, 10.0, 10.0, 0.0), 1
+    out = {}
+    s = cases.kelvin_helmholtz(sr_n, 3)
+    g = cg.Grid(cg.SR, (sr_n, sr_n), 1.0 / sr_n, 5.0 / 3.0, cg.FP64, cg.BC_PERIODIC, ctx=ctx)
+    g.set_prim(s)
+    _, grad, _, ms = g.adjoint(s[..., 0] * 0.99, sr_steps, 0.9, 0.0, cg.MINBEE, checkpoint_every=1)
+    g.close()
+    out["sr"] = {"grid": f"{sr_n}x{sr_n} FP64 Kelvin-Helmholtz", "steps": sr_steps, "forward_ms": ms[0],
+                 "backward_ms": ms[1], "adjoint_over_forward": ms[1] / ms[0], "finite": bool(np.isfinite(grad).all())}
+    a = gr_state(gr_n)
+    g = cg.Grid(cg.GR, (gr_n, gr_n), 20.0 / gr_n, 5.0 / 3.0, cg.FP64, cg.BC_TRANSMISSIVE,
+                cg.BlackHoleSpacetime(*GR_HOLE), ctx=ctx)
+    g.set_prim(a)
+    _, grad, _, ms = g.adjoint(a[..., 0] * 0.99, gr_steps, 0.9, 0.0, cg.VANLEER, checkpoint_every=1, subcycles=1)
+    g.close()
+    out["gr"] = {"grid": f"{gr_n}x{gr_n} FP64 accretion, 1 subcycle", "steps": gr_steps, "forward_ms": ms[0],
+                 "backward_ms": ms[1], "adjoint_over_forward": ms[1] / ms[0], "finite": bool(np.isfinite(grad).all())}
+    out["what"] = "gather-form vector-Jacobian products in dual numbers (FP64), recomputation per checkpoint"
+    return out
 
 
-def grid_cpu_baseline(kind, n, seconds):
-    """The CPU oracle (FP64 restatement of the reference, line-parallel on all host cores) on the
-    full-size grid: whole steps until `seconds` have passed (at least one)."""
-    from oracle.pyoracle import Oracle
-    O = Oracle()
-    cores = os.cpu_count() or 1
-    O.set_threads(cores)
-    system, s, dx, gam, bc, lim, bh, sub = grid_problem(kind, n)
-    t0 = time.perf_counter()
-    steps = 0
-    while True:
-        s, k, _, _ = O.solve(system, s, 2, dx, 0.9, 1e9, 0.0, lim, gam, bc, subcycles=sub, bh=bh, max_steps=1)
-        steps += k
-        el = time.perf_counter() - t0
-        if el >= seconds or steps >= 20:
-            break
-    return {"value": steps * n * n / el, "unit": METRIC, "cores": cores, "kind": "port",
-            "sample": f"{steps} full {n}x{n} steps of the FP64 oracle (bit-identical restatement of the reference) "
-                      f"in {el:.1f} s on {cores} host threads"}
+# ---------------------------------------------------------------- single-configuration lines
+def config_line(args, workload, entry, dtype="f32", extra_config=None):
+    """A contract line for one configuration measured by the functions above."""
+    v = entry["value"]
+    ms = entry.get("ms_per_step") or entry.get("fp32", entry.get("fp32_c2p_fp64", {})).get("ms_per_step")
+    e = entry.get("e2e", {})
+    line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": 1, "steps": entry.get("steps", args.steps),
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+            "config": dict({"workload": workload}, **(extra_config or {})), "result": entry}
+    if e:
+        line["e2e"] = dict({"unit": METRIC}, **e)
+    return line
 
 
-def run_grid(args, kind):
-    """One SR or GR grid: FP32 (SR) or FP64 (GR) steps resident in HBM, e2e through the C ABI with
-    host buffers, the FP64 path and the FP32-vs-FP64 density error (SR)."""
+def run_single(args):
     import torch
     import cosmos_gb300 as cg
     _, _, local = dist_env()
@@ -626,144 +874,88 @@ def run_grid(args, kind):
     L = cg.load()
     ctx = cg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
-    n = args.n if args.n != 4096 else (2048 if kind == "sr" else 1024)
-    system, s0, dx, gam, bc, lim, bh, sub = grid_problem(kind, n)
-    cells = n * n
-    bhs = cg.BlackHoleSpacetime(*bh) if bh else None
-    prec = cg.FP32
-
-    def timed(fn):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        with torch.cuda.stream(stream):
-            a.record(stream)
-            fn()
-            b.record(stream)
-        b.synchronize()
-        return a.elapsed_time(b)
-
-    def make(precision, above=2.0):
-        g = cg.Grid(system, (n, n), dx, gam, precision, bc, bhs, ctx=ctx, sr_c2p64_above=above)
-        g.set_prim(s0)
-        g.run_begin(2, 0.9, 1e30, 0.0, lim, subcycles=sub)
-        return g
-
-    steps = args.steps if args.steps != 200 or kind == "sr" else 100
-    g = make(prec)
-    g.run_steps(args.warmup)
-    launches0 = L.cosmos_kernel_launches()
+    w = args.workload
     with Clocks(local) as clk:
-        ms = timed(lambda: g.run_steps(steps)) / steps
-    launches = L.cosmos_kernel_launches() - launches0
-    r = g.run_end()
-    g.close()
-    value = cells / (ms * 1e-3)
-    extra = {}
-    nerr = 10 if kind == "sr" else 5
-    if kind == "gr":
-        # FP64 over the same window as the FP32 value (the per-step cost grows as the inflow reaches
-        # the horizon, where the recovery meets states without a physical root)
-        g64 = make(cg.FP64)
-        g64.run_steps(args.warmup)
-        ms64 = timed(lambda: g64.run_steps(steps)) / steps
-        g64.close()
-        g64 = make(cg.FP64)
-        g64.run_steps(nerr)
-        rho64 = g64.get_prim()[..., 0]
-        g64.close()
-        g32 = make(cg.FP32)
-        g32.run_steps(nerr)
-        rho32 = g32.get_prim()[..., 0]
-        g32.close()
-        x = np.arange(n) * dx
-        X, Y = np.meshgrid(x, x)
-        outside = np.sqrt((X - bh[2]) ** 2 + (Y - bh[3]) ** 2) > 2.0 * bh[0] + 3 * dx
-        extra = {"fp64": {"value": cells / (ms64 * 1e-3), "ms_per_step": ms64, "steps": steps,
-                          "path": "plain FP64, bit-identical to the reference (same steps as value)"},
-                 "l1_rho_vs_fp64": float(np.abs(rho32[outside] - rho64[outside]).mean() / np.abs(rho64[outside]).mean()),
-                 "l1_cells": "outside r > 2M + 3 dx (the excised region keeps its initial state in both)",
-                 "l1_steps": nerr, "fp32_over_fp64": ms64 / ms}
-    if kind == "sr":
-        # FP32 with the FP64 Newton stage in every primitive recovery
-        ga = make(cg.FP32, 0.0)
-        ga.run_steps(args.warmup)
-        ms_a = timed(lambda: ga.run_steps(steps)) / steps
-        ga.close()
-        # the FP64 (reference-exact) path and the density errors after nerr steps
-        g64 = make(cg.FP64)
-        ms64 = timed(lambda: g64.run_steps(nerr)) / nerr
-        rho64 = g64.get_prim()[..., 0]
-        g64.close()
-        errs = {}
-        for tag, above in (("fp32", 2.0), ("fp32_c2p64_always", 0.0)):
-            gg = make(cg.FP32, above)
-            gg.run_steps(nerr)
-            rr = gg.get_prim()[..., 0]
-            gg.close()
-            errs[tag] = float(np.abs(rr - rho64).mean() / np.abs(rho64).mean())
-        extra = {"fp64": {"value": cells / (ms64 * 1e-3), "ms_per_step": ms64, "steps": nerr,
-                          "path": "plain FP64, bit-identical to the reference"},
-                 "fp32_c2p64_always": {"value": cells / (ms_a * 1e-3), "ms_per_step": ms_a,
-                                       "what": "FP32 with the FP64 Newton stage in every primitive recovery"},
-                 "l1_rho_vs_fp64": errs, "l1_steps": nerr, "fp32_over_fp64": ms64 / ms}
-    # e2e: per step, host primitives -> device, one step, state -> host (pinned buffers)
-    host = torch.empty((n, n, 5), dtype=torch.float64, pin_memory=True)
-    host.numpy()[...] = s0
-    ge = make(prec)
-    nbytes = cells * 5 * 8
-
-    def e2e_step():
-        cg._lib.check(L.cosmos_grid_set_prim(ge.h, host.data_ptr(), cells * 5))
-        ge.run_steps(1)
-        cg._lib.check(L.cosmos_grid_get_prim(ge.h, host.data_ptr(), cells * 5))
-    e2e_step()
-    e2e_steps = 3
-    e2e_ms = timed(lambda: [e2e_step() for _ in range(e2e_steps)]) / e2e_steps
-    ge.close()
-    peak, peak_kind = peaks()
-    word = 4 if prec == cg.FP32 else 8
-    bpc = (30 if kind == "sr" else 50) * word  # 3 sweeps x 10 words (+ 2 RK source passes for GR)
-    gbs = cells * bpc / (ms * 1e-3) / 1e9
-    base = None if args.no_cpu else grid_cpu_baseline(kind, n, args.cpu_seconds)
-    line = {
-        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": steps, "warmup": args.warmup,
-        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32" if prec == cg.FP32 else "f64", "data": "synthetic",
-        "config": {"workload": SR_WORKLOAD if kind == "sr" else GR_WORKLOAD, "n": n, "cells": cells,
-                   "precision": "fp32 bulk; primitive recovery finishes in FP64 for W > 2 or when the FP32 "
-                                "Newton iteration does not converge" + ("" if kind == "sr" else
-                                "; metric, its derivatives and inverses from FP64 tables built once"),
-                   "l2": f"state {cells * 10 * word / 1e6:.0f} MB (two buffers) > 129 MB L2 (no flush needed)"
-                   if cells * 10 * word > 129e6 else "state fits in L2",
-                   "device_dt": True, "graph_replay": True, "steps_completed": r.steps},
-        **extra,
-        "e2e": {"value": cells / (e2e_ms * 1e-3), "unit": METRIC, "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_ms, "steps": e2e_steps,
-                "what": "per step: pinned host AoS FP64 primitives -> device, one step, state -> host"},
-        "roofline": {"bound": "hbm", "kernel": "whole step (X, Y, X sweeps" + (", RK source" if kind == "gr" else "") + ")",
-                     "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak, "peak_source": peak_kind,
-                     "traffic": None, "bytes_per_cell_update": bpc,
-                     "note": "compute-bound: primitive recovery (FP32 Newton, FP64 stage above W = 2)" +
-                             ("; RK4 source: 38 recoveries per cell per source step" if kind == "gr" else "")},
-        "clocks": clk.summary(), "gpu_launches": int(launches), "status": r.status,
-    }
-    if base:
-        line["cpu_baseline"] = base
+        if w == "sod":
+            e, wl, dt = measure_sod(cg, ctx, stream), SOD_WORKLOAD, "f64"
+        elif w == "sr":
+            e, wl, dt = measure_sr(cg, L, ctx, stream, args.n if args.n != 4096 else 2048, args.sr_steps,
+                                   args.warmup), SR_WORKLOAD, "f32"
+        elif w == "gr":
+            e, wl, dt = measure_gr(cg, L, ctx, stream, args.n if args.n != 4096 else 1024, args.gr_steps,
+                                   args.warmup), GR_WORKLOAD, "f32"
+        elif w == "batch":
+            e, wl, dt = measure_batch(cg, L, ctx, stream, args.steps, args.warmup, tiles=True), BATCH_WORKLOAD, "f32"
+        elif w == "adjoint":
+            e = adjoint_measure(cg, ctx)
+            e["value"] = 2048 * 2048 * e["steps"] / ((e["forward_ms"] + e["backward_ms"]) * 1e-3)
+            e["rel"] = measure_rel_adjoint(cg, ctx)
+            wl, dt = "adjoint of 100 SLIC steps (checkpoint every 10), Newtonian 2048^2 FP32", "f32"
+        else:
+            raise ValueError(w)
+    line = config_line(args, wl, e, dt)
+    line["clocks"] = clk.summary()
     print(json.dumps(line), flush=True)
 
 
-def run_grid_reference(args, kind):
+def run_single_reference(args):
+    """CPU arm of a single-configuration line: the oracle on the configuration's full-size data."""
     rank, _, _ = dist_env()
     if rank != 0:
         return
-    n = args.n if args.n != 4096 else (2048 if kind == "sr" else 1024)
-    base = grid_cpu_baseline(kind, n, max(8.0, 2.0 * args.steps))
-    line = {"metric": METRIC, "value": base["value"], "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": n * n / base["value"] * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": SR_WORKLOAD if kind == "sr" else GR_WORKLOAD, "n": n},
-            "cpu_baseline": base,
-            "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    from oracle.pyoracle import Oracle
+    import cases
+    O = Oracle()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    w = args.workload
+    if w in ("sr", "gr"):
+        n = args.n if args.n != 4096 else (2048 if w == "sr" else 1024)
+        if w == "sr":
+            sysid, s, dx, gam, bc, lim, bh, wl = 1, cases.kelvin_helmholtz(n, 3), 1.0 / n, 5 / 3, 1, 2, None, SR_WORKLOAD
+        else:
+            sysid, s, dx, gam, bc, lim, bh, wl = 2, gr_state(n), 20.0 / n, 5 / 3, 0, 1, GR_HOLE, GR_WORKLOAD
+        t0 = time.perf_counter()
+        steps = 0
+        while True:
+            s, k, _, _ = O.solve(sysid, s, 2, dx, 0.9, 1e9, 0.0, lim, gam, bc, subcycles=1, bh=bh, max_steps=1)
+            steps += k
+            el = time.perf_counter() - t0
+            if el >= max(8.0, 2.0 * args.steps) or steps >= max(1, args.steps):
+                break
+        value, cells, sample = steps * n * n / el, n * n, f"{steps} full {n}x{n} steps"
+    elif w == "batch":
+        shapes, states, dxs = batch_problem()
+        t0 = time.perf_counter()
+        cells = grids = 0
+        for k in range(len(shapes)):
+            O.solve(0, states[k], 2, dxs[k], 0.9, 1e9, 0.0, 2, 1.4, 0, max_steps=1)
+            cells += int(np.prod(shapes[k]))
+            grids += 1
+            if time.perf_counter() - t0 >= max(8.0, 2.0 * args.steps):
+                break
+        el = time.perf_counter() - t0
+        value, sample, wl = cells / el, f"one step of each of the first {grids} grids ({cells} cells)", BATCH_WORKLOAD
+    elif w == "sod":
+        s = cases.sod(1000)
+        t0 = time.perf_counter()
+        _, k, _, _ = O.solve(0, s, 2, 1e-3, 0.9, 0.25, 0.0, 1, 1.4)
+        el = time.perf_counter() - t0
+        value, sample, wl = k * 1000 / el, f"the whole {k}-step solve", SOD_WORKLOAD
+    else:
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no adjoint"}), flush=True)
+        return
+    base = {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"{sample} of the FP64 oracle (restatement of the reference, bit-identical to it) in "
+                      f"{el:.1f} s on {cores} host threads"}
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl}, "cpu_baseline": base,
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if w in ("sr", "gr"):
+        line["ms_per_step"] = n * n / value * 1e3
+        line["config"]["n"] = n
     print(json.dumps(line), flush=True)
 
 
@@ -944,33 +1136,35 @@ def run_amr_reference(args):
     print(json.dumps(line), flush=True)
 
 
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="grid", choices=["grid", "batch", "sr", "gr", "amr"],
-                    help="grid: one 4096^2 Newtonian grid (default); batch: 256 uneven grids in one persistent "
-                         "launch; sr: 2048^2 special-relativistic Kelvin-Helmholtz; gr: 1024^2 black-hole accretion; "
-                         "amr: Level-1 AMR driver runs on a 512^2 cylindrical explosion")
+    ap.add_argument("--workload", default="grid", choices=["grid", "sod", "batch", "sr", "gr", "adjoint", "amr"],
+                    help="grid: one 4096^2 Newtonian grid plus every other configuration as `configs` (default); "
+                         "sod: the 1000-cell FP64 shock tube; batch: 256 uneven grids in one persistent launch; "
+                         "sr: 2048^2 special-relativistic Kelvin-Helmholtz; gr: 1024^2 black-hole accretion; "
+                         "adjoint: the adjoints; amr: Level-1 AMR driver runs on a 512^2 cylindrical explosion")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=4096)
-    ap.add_argument("--err-steps", type=int, default=10)
+    ap.add_argument("--parity-steps", "--err-steps", dest="parity_steps", type=int, default=200,
+                    help="steps of the FP32-vs-FP64 comparison of the headline workload")
+    ap.add_argument("--sr-steps", type=int, default=200)
+    ap.add_argument("--gr-steps", type=int, default=100)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="the headline workload alone (no `configs`)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.workload == "batch":
-        run_batch_reference(args) if args.impl == "reference" else run_batch(args)
+    if args.workload == "grid":
+        run_reference(args) if args.impl == "reference" else run_ours(args)
     elif args.workload == "amr":
         run_amr_reference(args) if args.impl == "reference" else run_amr(args)
-    elif args.workload in ("sr", "gr"):
-        run_grid_reference(args, args.workload) if args.impl == "reference" else run_grid(args, args.workload)
-    elif args.impl == "reference":
-        run_reference(args)
     else:
-        run_ours(args)
+        run_single_reference(args) if args.impl == "reference" else run_single(args)
 
 
 if __name__ == "__main__":

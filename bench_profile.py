@@ -1,11 +1,11 @@
 """Minimal launch driver for profiler captures of single kernels.
 
-    python -m cosmos_gb300.profile --kernel sweep --n 4096 --precision fp32 --axis 0 --launches 3
-    python -m cosmos_gb300.profile --kernel step --n 4096 --precision fp32 --launches 4
-    python -m cosmos_gb300.profile --kernel step --system 2 --n 1024 --warm 60 --launches 1
-    python -m cosmos_gb300.profile --kernel adjoint --n 1024 --precision fp32 --launches 2
-    python -m cosmos_gb300.profile --kernel adjoint --system 2 --n 256 --precision fp64 --subcycles 1 --launches 1
-    python -m cosmos_gb300.profile --kernel batch --grids 64 --launches 2
+    python bench_profile.py --kernel sweep --n 4096 --precision fp32 --axis 0 --launches 3
+    python bench_profile.py --kernel step --n 4096 --precision fp32 --launches 4
+    python bench_profile.py --kernel step --system 2 --n 1024 --warm 60 --launches 1
+    python bench_profile.py --kernel adjoint --n 1024 --precision fp32 --launches 2
+    python bench_profile.py --kernel adjoint --system 2 --n 256 --precision fp64 --subcycles 1 --launches 1
+    python bench_profile.py --kernel batch --grids 64 --launches 2
 
 Creates one grid of the configuration's problem for the system (Newtonian: config-2 four-quadrant
 data, periodic; SR: config-3 Kelvin-Helmholtz layers, periodic; GR: config-4 accretion onto a
@@ -37,11 +37,11 @@ def main():
     ap.add_argument("--warm", type=int, default=0,
                     help="`step` only: steps run before the captured ones (evolved states)")
     a = ap.parse_args()
-    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
     import cosmos_gb300 as cg
 
     if a.kernel == "batch":
-        sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests"))
+        sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests"))
         import cases
         shapes = cases.batch_shapes()[:a.grids]
         b = cg.Batch(shapes, [1.0 / sh[-1] for sh in shapes], 1.4, cg.FP32, cg.BC_TRANSMISSIVE)
@@ -55,7 +55,7 @@ def main():
         print(f"ok: {a.launches} x batch chunk ({len(shapes)} grids, {b.cells} cells)")
         return
     n = a.n
-    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests"))
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests"))
     import cases
     prec = cg.FP32 if a.precision == "fp32" else cg.FP64
     bh = None

@@ -621,7 +621,7 @@ template <class T, class S, bool PRIM>
 cudaError_t launch_adjoint_grad_t(const Geom& G, double gamma, const void* state, const void* ubar, double* grad,
                                   cudaStream_t st) {
     const size_t ncell = (size_t)G.nx * G.ny;
-    const int blocks = (int)std::min<size_t>((ncell + 255) / 256, 152 * 16);
+    const int blocks = (int)std::min<size_t>((ncell + 255) / 256, (size_t)device_sm_count() * 16);
     adjoint_grad_kernel<T, S, PRIM>
         <<<blocks, 256, 0, st>>>(G, gamma, T(1.0 / (gamma - 1.0)), (const S*)state, (const T*)ubar, grad);
     return cudaGetLastError();

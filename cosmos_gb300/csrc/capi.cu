@@ -17,6 +17,17 @@ static thread_local bool t_capturing = false;  // launches recorded into a graph
 void count_launch(unsigned n) {
     if (!t_capturing) g_launches.fetch_add(n, std::memory_order_relaxed);
 }
+int device_sm_count() {
+    static std::atomic<int> counts[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    int c = counts[dev].load(std::memory_order_relaxed);
+    if (c <= 0) {
+        if (cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || c <= 0) c = 152;
+        counts[dev].store(c, std::memory_order_relaxed);
+    }
+    return c;
+}
 }  // namespace cg
 
 using namespace cg;

@@ -10,6 +10,10 @@ namespace cg {
 
 struct Pt { double x, y, z; };
 
+// Streaming multiprocessors of the current device (host code; cached per device): grid-stride
+// launches size their grids as a multiple of it.
+int device_sm_count();
+
 CG_HD Pt shift_pt(Pt p, int axis, double d) {
     if (axis == 0) p.x = p.x + d; else p.y = p.y + d;
     return p;

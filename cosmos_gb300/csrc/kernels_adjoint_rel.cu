@@ -48,7 +48,7 @@ cudaError_t launch_adjoint_rel_sweep(const Geom& G, int system, double gamma, co
     p.pbar_out = (const double*)pbar_out;
     p.pbar_in = (double*)pbar_in;
     const size_t n = (size_t)G.nx * G.ny;
-    const int blocks = (int)std::max<size_t>(1, std::min<size_t>((n + 127) / 128, 152 * 16));
+    const int blocks = (int)std::max<size_t>(1, std::min<size_t>((n + 127) / 128, device_sm_count() * 16));
     rel_adjoint_sweep_kernel<<<blocks, 128, 0, st>>>(p);
     count_launch();
     return cudaGetLastError();
@@ -71,7 +71,7 @@ cudaError_t launch_adjoint_rel_rk(const Geom& G, double gamma, const double* bh,
     p.pbar_out = (const double*)pbar_out;
     p.pbar_in = (double*)pbar_in;
     const size_t n = (size_t)G.nx * G.ny;
-    const int blocks = (int)std::max<size_t>(1, std::min<size_t>((n + 127) / 128, 152 * 16));
+    const int blocks = (int)std::max<size_t>(1, std::min<size_t>((n + 127) / 128, device_sm_count() * 16));
     rel_adjoint_rk_kernel<<<blocks, 128, 0, st>>>(p);
     count_launch();
     return cudaGetLastError();
@@ -79,7 +79,7 @@ cudaError_t launch_adjoint_rel_rk(const Geom& G, double gamma, const double* bh,
 
 cudaError_t launch_adjoint_rel_grad(const Geom& G, const void* pbar, double* grad, cudaStream_t st) {
     const size_t n = (size_t)G.nx * G.ny;
-    const int blocks = (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 152 * 16));
+    const int blocks = (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, device_sm_count() * 16));
     rel_adjoint_grad_kernel<<<blocks, 256, 0, st>>>(G, (const double*)pbar, grad);
     count_launch();
     return cudaGetLastError();

@@ -77,7 +77,7 @@ cudaError_t launch_wavespeed_exact(const SweepArgs& a, unsigned long long* slot)
     if (slot) { o.smax = slot; o.ws_ctl = nullptr; }
     const size_t n = (size_t)G.nx * G.ny;
     int blocks = (int)((n + NT - 1) / NT);
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks > device_sm_count() * 16) blocks = device_sm_count() * 16;
     const double* src = (const double*)a.src;
     if (a.system == 0) wavespeed_kernel<ExactPolicy<NewtonExact<double>>, NT><<<blocks, NT, 0, a.stream>>>(make_policy(b, NewtonExact<double>{a.gamma}), b.G, src, o);
     else if (a.system == 1) wavespeed_kernel<ExactPolicy<SRExact>, NT><<<blocks, NT, 0, a.stream>>>(make_policy(b, SRExact{a.gamma, nullptr}), b.G, src, o);
@@ -164,7 +164,7 @@ __global__ void prim_out_exact_kernel(const double* __restrict__ soa, double* __
 }
 static int grid_for(size_t n) {
     size_t b = (n + 255) / 256;
-    return (int)(b > 152 * 32 ? 152 * 32 : (b ? b : 1));
+    return (int)(b > device_sm_count() * 32 ? device_sm_count() * 32 : (b ? b : 1));
 }
 cudaError_t launch_prim_in_exact(const double* aos, void* soa, const Geom& G, cudaStream_t st) {
     prim_in_exact_kernel<<<grid_for((size_t)G.nx * G.ny), 256, 0, st>>>(aos, (double*)soa, G);
@@ -503,7 +503,7 @@ __global__ void amr_any_kernel(const unsigned char* __restrict__ f, size_t n, un
 
 cudaError_t launch_amr_any(const unsigned char* flags, size_t n, unsigned long long* out, cudaStream_t st) {
     size_t b = (n + 255) / 256;
-    if (b > 152 * 4) b = 152 * 4;
+    if (b > device_sm_count() * 4) b = device_sm_count() * 4;
     amr_any_kernel<<<(int)(b ? b : 1), 256, 0, st>>>(flags, n, out);
     count_launch();
     return cudaGetLastError();
@@ -601,7 +601,7 @@ __global__ void state_eval_kernel(StateEvalArgs a, NewtonExact<double> nw, SRExa
 
 cudaError_t launch_state_eval(const SweepArgs& s, const StateEvalArgs& a) {
     size_t b = (a.n + 127) / 128;
-    if (b > 152 * 8) b = 152 * 8;
+    if (b > device_sm_count() * 8) b = device_sm_count() * 8;
     state_eval_kernel<<<(int)(b ? b : 1), 128, 0, s.stream>>>(a, NewtonExact<double>{s.gamma, nullptr},
                                                                 SRExact{s.gamma, nullptr}, make_gr(s));
     count_launch();

@@ -82,7 +82,7 @@ cudaError_t launch_wavespeed_fast(const SweepArgs& a, unsigned long long* slot) 
     if (slot) { o.smax = slot; o.ws_ctl = nullptr; }
     const size_t n = (size_t)a.G.nx * a.G.ny;
     int blocks = (int)((n + NT - 1) / NT);
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks > device_sm_count() * 16) blocks = device_sm_count() * 16;
     auto pol = make_fast<0, 2, false>(b);
     wavespeed_kernel<decltype(pol), NT><<<blocks, NT, 0, a.stream>>>(pol, b.G, (const float*)a.src, o);
     count_launch();
@@ -129,7 +129,7 @@ __global__ void prim_out_fast_kernel(const float* __restrict__ soa, double* __re
 }
 static int grid_for(size_t n) {
     size_t b = (n + 255) / 256;
-    return (int)(b > 152 * 32 ? 152 * 32 : (b ? b : 1));
+    return (int)(b > device_sm_count() * 32 ? device_sm_count() * 32 : (b ? b : 1));
 }
 cudaError_t launch_prim_in_fast(const double* aos, void* soa, const Geom& G, int system, double gamma, cudaStream_t st) {
     if (system == 1) return launch_prim_in_sr_fast(aos, soa, G, gamma, st);

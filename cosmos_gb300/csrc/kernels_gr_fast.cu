@@ -110,7 +110,7 @@ __global__ void gr_cell_table_kernel(GRExact sys, int dims, int order, double dx
     }
 }
 
-int blocks_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
+int blocks_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, device_sm_count() * 16); }
 
 // ---------------------------------------------------------------- sweep policy
 // Plugs into the one-cell tile functions (sweep_x_own_kernel, sweep_y_kernel) on primitive cells:

@@ -68,7 +68,7 @@ __global__ void sr_prim_out_kernel(const float* __restrict__ soa, double* __rest
 }
 int grid_for(size_t n) {
     size_t b = (n + 255) / 256;
-    return (int)(b > 152 * 32 ? 152 * 32 : (b ? b : 1));
+    return (int)(b > device_sm_count() * 32 ? device_sm_count() * 32 : (b ? b : 1));
 }
 
 }  // namespace
@@ -89,7 +89,7 @@ cudaError_t launch_wavespeed_sr_fast(const SweepArgs& a, unsigned long long* slo
     if (slot) { o.smax = slot; o.ws_ctl = nullptr; }
     const size_t n = (size_t)a.G.nx * a.G.ny;
     int blocks = (int)((n + NT - 1) / NT);
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks > device_sm_count() * 16) blocks = device_sm_count() * 16;
     auto pol = make_pol<0, 2, false>(b);
     wavespeed_kernel<decltype(pol), NT><<<blocks, NT, 0, a.stream>>>(pol, b.G, (const float*)a.src, o);
     count_launch();

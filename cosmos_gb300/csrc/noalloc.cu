@@ -1,18 +1,22 @@
 // Allocation-free conservation sums.
 //
-// Some callers cannot allocate device memory at the point where they need the sums: code that
-// runs while a stream is being captured into a CUDA graph (allocation calls are not allowed
-// there), code inside a host callback or a foreign runtime that owns the device allocator, and
-// embedded callers with a fixed memory budget.  cosmos_field_sums_noalloc serves them: it takes
-// the caller's device state and output pointers and keeps its reduction scratch in a file-scope
-// device array instead of calling cudaMalloc.
+// Some callers cannot allocate device memory at the point where they need the sums: a foreign
+// runtime or framework that owns the device allocator and its memory pool (a cudaMalloc beside
+// it fragments or overdraws the pool it manages), an embedded caller with a fixed memory budget
+// set at start-up, and a pipeline that must not stall (cudaMalloc and cudaFree can synchronise
+// the device).  cosmos_field_sums_noalloc serves them: it takes the caller's device state and
+// output pointers and keeps its reduction scratch in a file-scope device array instead of
+// calling cudaMalloc.
 //
 // Limits and sharing: the scratch holds one row of partial sums per grid row, so grids taller
 // than COSMOS_NOALLOC_MAX_ROWS rows are rejected.  The array lives as long as the library is
 // loaded, on every device that loads it (640 KB each).  All calls share it, so calls whose
 // kernels overlap on the GPU (concurrent streams, several host threads) race and must be
-// serialised by the caller.
+// serialised by the caller.  The scratch's device address is looked up on the first call on each
+// device and kept; a cudaDeviceReset invalidates it, so do not call this entry point again in a
+// process after resetting the device.
 #include <mutex>
+#include <string>
 
 #include "../../include/cosmos_gb300.h"
 #include "launch.h"
@@ -125,6 +129,13 @@ extern "C" int cosmos_field_sums_noalloc(const void* state, int precision, int n
         a = g_addr[dev];
     }
     cudaStream_t st = (cudaStream_t)stream;
+    // an error left pending by earlier, unrelated work is reported as such, not as this call's
+    const cudaError_t pending = cudaGetLastError();
+    if (pending != cudaSuccess) {
+        set_error((std::string("cosmos_field_sums_noalloc: a CUDA error was already pending before the call: ") +
+                   cudaGetErrorString(pending)).c_str());
+        return COSMOS_ECUDA;
+    }
     // the completion counter must start at zero on every call
     if (cudaMemsetAsync(a.done, 0, sizeof(unsigned int), st) != cudaSuccess) {
         set_error("cosmos_field_sums_noalloc: clearing the completion counter failed");

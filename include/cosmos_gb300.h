@@ -290,9 +290,9 @@ int cosmos_state_eval(cosmos_ctx* ctx, const cosmos_params* p, int op, size_t n,
                       double bias, int limiter, double* out);
 
 /* Allocation-free conservation sums.  No counterpart in the reference: it exists for callers that
- * cannot allocate device memory where they need the sums -- code recorded into a CUDA graph
- * (allocation is not allowed during stream capture), host callbacks or foreign runtimes that own
- * the device allocator, fixed-budget embedded callers.  Same sums as cosmos_grid_field_sums, on a
+ * cannot allocate device memory where they need the sums -- runtimes that own the device
+ * allocator and its pool, embedded callers with a fixed memory budget, pipelines that must not
+ * stall on cudaMalloc's device synchronisation.  Same sums as cosmos_grid_field_sums, on a
  * caller-owned structure-of-arrays state: field f of cell (i, j) at
  * state[f * field_stride + i * pitch + j], doubles (COSMOS_FP64) or floats (COSMOS_FP32).
  * out5 is caller-owned device memory for 5 doubles; the work is enqueued on `stream` (a
@@ -300,7 +300,9 @@ int cosmos_state_eval(cosmos_ctx* ctx, const cosmos_params* p, int op, size_t n,
  * reduction scratch is a fixed device array of COSMOS_NOALLOC_MAX_ROWS rows (640 KB, held on
  * every device that loads the library), so grids with more rows are rejected (COSMOS_EINVAL).
  * The first call on a device looks up that array's device address (make it before any stream
- * capture).  All calls share the array: calls whose kernels overlap on the GPU race. */
+ * capture); the address is kept, so do not call it again after a cudaDeviceReset.  All calls
+ * share the array: calls whose kernels overlap on the GPU race.  A CUDA error already pending
+ * when it is called is returned (COSMOS_ECUDA) before anything is enqueued. */
 #define COSMOS_NOALLOC_MAX_ROWS 16384
 int cosmos_field_sums_noalloc(const void* state, int precision, int nx, int ny, int pitch, size_t field_stride,
                               double* out5, void* stream);

@@ -7,6 +7,7 @@ import os
 import subprocess
 import sys
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -47,6 +48,41 @@ def test_reference_arm_prints_one_contract_line(workload, n):
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    if workload == "grid":  # both arms print the same config dict for the headline workload
+        sys.path.insert(0, ROOT)
+        import bench
+        assert line["config"] == bench.grid_config(n, 1)
+        assert "1 timed" in base["sample"] and "3 untimed" in base["sample"]
+
+
+@pytest.mark.parametrize("workload", ["sod", "batch"])
+def test_single_config_reference_arms(workload):
+    r = run_bench(["--workload", workload, "--impl", "reference", "--steps", "1", "--warmup", "3"])
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.strip()]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert KEYS <= set(line) and line["impl"] == "reference" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_conservation_totals():
+    sys.path.insert(0, ROOT)
+    import bench
+    rng = np.random.default_rng(3)
+    p = np.stack([rng.uniform(0.5, 1.5, (8, 9)), rng.uniform(-0.3, 0.3, (8, 9)), rng.uniform(-0.3, 0.3, (8, 9)),
+                  np.zeros((8, 9)), rng.uniform(0.1, 1.0, (8, 9))], axis=-1)
+    m, e = bench.newton_totals(p, 1.4)
+    assert m == pytest.approx(p[..., 0].sum(), rel=1e-15)
+    v2 = (p[..., 1:4] ** 2).sum(-1)
+    assert e == pytest.approx((0.5 * p[..., 0] * v2 + p[..., 4] / 0.4).sum(), rel=1e-14)
+    d, tau = bench.sr_totals(p, 5.0 / 3.0)
+    W = 1.0 / np.sqrt(1.0 - v2)
+    h = 1.0 + p[..., 4] / p[..., 0] * 2.5
+    assert d == pytest.approx((p[..., 0] * W).sum(), rel=1e-14)
+    assert tau == pytest.approx((p[..., 0] * h * W * W - p[..., 4] - p[..., 0] * W).sum(), rel=1e-14)
+    assert bench.drift((2.0, 4.0), (2.0 + 2e-7, 4.0 - 4e-6)) == pytest.approx({"mass": 1e-7, "energy": 1e-6})
+    assert bench.rel_l1(np.array([1.0, 2.0]), np.array([1.0, 1.0])) == pytest.approx(0.5)
 
 
 def test_amr_reference_arm_prints_one_contract_line():

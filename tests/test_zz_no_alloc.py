@@ -1,7 +1,8 @@
 """cosmos_field_sums_noalloc: the allocation-free conservation sums.
 
-Callers that cannot allocate device memory (code recorded into a CUDA graph, host callbacks,
-runtimes that own the allocator) use this entry point; its scratch is a fixed device array.  The
+Callers that cannot allocate device memory (runtimes that own the device allocator and its pool,
+embedded callers with a fixed memory budget, pipelines that must not stall on cudaMalloc's device
+synchronisation) use this entry point; its scratch is a fixed device array.  The
 test calls it through the C ABI on caller-owned device buffers, twice in a row (the second call
 runs on the scratch left by the first), and checks both results against cosmos_grid_field_sums on
 a grid holding the same state.  It lives in its own file, collected last, and also passes alone.
