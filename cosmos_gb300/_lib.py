@@ -94,6 +94,7 @@ SIGNATURES = {
     "cosmos_batch_run_steps": (_i, [_p, _i]),
     "cosmos_batch_run_end": (_i, [_p, _p]),
     "cosmos_batch_set_shape": (_i, [_p, _i, _i, _i]),
+    "cosmos_batch_set_wait_limit": (_i, [_p, ctypes.c_longlong]),
     "cosmos_batch_time_shape": (_i, [_p, _i, _i, _i, _i, ctypes.POINTER(_d)]),
     "cosmos_batch_autotune": (_i, [_p, ctypes.c_char_p, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i),
                                    ctypes.POINTER(_d)]),

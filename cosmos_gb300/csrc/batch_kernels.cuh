@@ -32,6 +32,8 @@ struct GridBarrier {
     unsigned int count;
     unsigned int gen;
     int err;
+    int pad;
+    long long limit;  // polls before a waiting block gives up (0: 2^26, about 4 s)
 };
 
 struct BatchDev {
@@ -67,8 +69,9 @@ CG_D void step_ctl_advance(StepCtl* c) {
     c->it = c->it + 1;
 }
 
-// Grid-wide barrier for a cooperative launch.  Waits are bounded (about 4 s); a block that gives
-// up sets err, and every block returns at its next barrier.
+// Grid-wide barrier for a cooperative launch.  Waits are bounded (b->limit polls of about 64 ns,
+// by default 2^26, about 4 s); a block that gives up sets err, and every block returns at its next
+// barrier (a block that is last to arrive passes, sees err and returns too).
 CG_D bool grid_sync(GridBarrier* b) {
     __shared__ int s_ok;
     __syncthreads();
@@ -83,11 +86,12 @@ CG_D bool grid_sync(GridBarrier* b) {
             __threadfence();
             atomicAdd(&b->gen, 1u);
         } else {
+            const long long limit = b->limit > 0 ? b->limit : (1ll << 26);
             long long spins = 0;
             while (*vgen == g) {
                 if (*verr) { ok = 0; break; }
                 __nanosleep(64);
-                if (++spins > (1ll << 26)) { atomicOr(&b->err, ST_TIMEOUT); ok = 0; break; }
+                if (++spins > limit) { atomicOr(&b->err, ST_TIMEOUT); ok = 0; break; }
             }
         }
         __threadfence();

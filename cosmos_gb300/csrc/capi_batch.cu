@@ -66,6 +66,8 @@ struct cosmos_batch {
     int chunk;
     cudaGraphExec_t graph;
     bool graph_ok;
+    long long wait_limit;  // grid-barrier polls before a wait gives up (0: the default)
+    GridBarrier h_bar;     // staging for the barrier's initial state
 };
 
 namespace {
@@ -158,7 +160,15 @@ int reset_controllers(cosmos_batch* b) {
         h[g].active = 1;
     }
     BCK(cudaMemcpyAsync(b->d_ctl, h.data(), n * sizeof(StepCtl), cudaMemcpyHostToDevice, b->stream));
-    BCK(cudaMemsetAsync(b->d_bar, 0, sizeof(GridBarrier), b->stream));
+    {
+        // the barrier's counters start at zero; its wait limit comes from cosmos_batch_set_wait_limit
+        static_assert(sizeof(GridBarrier) == 24, "barrier layout");
+        GridBarrier* hb = &b->h_bar;
+        memset(hb, 0, sizeof *hb);
+        hb->limit = b->wait_limit;
+        BCK(cudaMemcpyAsync(b->d_bar, hb, sizeof *hb, cudaMemcpyHostToDevice, b->stream));
+        BCK(cudaStreamSynchronize(b->stream));  // hb is host memory read by the copy
+    }
     const int cur = (int)(b->steps_done & 1);
     for (int g = 0; g < n; g++) {
         SweepArgs a;
@@ -471,6 +481,13 @@ int cosmos_batch_autotune(cosmos_batch* b, const char* cache_path, int* nt_out, 
     if (seg_out) *seg_out = best_seg;
     if (cap_out) *cap_out = best_cap;
     if (ms_out) *ms_out = best;
+    return COSMOS_OK;
+}
+
+int cosmos_batch_set_wait_limit(cosmos_batch* b, long long polls) {
+    if (!b) return bfail(COSMOS_EINVAL, "null batch");
+    if (polls < 0) return bfail(COSMOS_EINVAL, "the wait limit must be >= 0 (0 restores the default)");
+    b->wait_limit = polls;
     return COSMOS_OK;
 }
 

@@ -31,6 +31,13 @@ CG_HD int ghost_index(int k, int n, int bc) {
     return k;
 }
 
+// A cell whose density or energy (FP64 grids: pressure) is not finite gets an infinite CFL speed:
+// the step's time step becomes zero and the run reports a non-finite time step
+// (COSMOS_STATUS_NONFINITE / COSMOS_ENONFINITE), where the reference carries the NaN on (its
+// `if (w > max)` drops a NaN speed).  Finite states keep the reference's speed bit for bit.
+CG_HD double speed_or_inf(double a, double b, double ws) { return isfinite(a + b) ? ws : (double)INFINITY; }
+CG_HD float speed_or_inf(float a, float b, float ws) { return fabsf(a + b) < INFINITY ? ws : INFINITY; }
+
 // std::min / std::max semantics as used by the reference.
 template <class T> CG_HD T mn(T a, T b) { return (b < a) ? b : a; }
 template <class T> CG_HD T mx(T a, T b) { return (a < b) ? b : a; }

@@ -183,7 +183,7 @@ struct GRFastPolicy {
         float w[kWsFields];
 #pragma unroll
         for (int t = 0; t < kWsFields; t++) w[t] = T.ws[t * T.cell_stride + q];
-        return gr_speed_fast(P, c.v, w);
+        return speed_or_inf(c.v[0], c.v[4], gr_speed_fast(P, c.v, w));
     }
     CG_D void flush_status(int* st) const {
         if (st && flags) atomicOr(st, ST_NEWTON_CAP);

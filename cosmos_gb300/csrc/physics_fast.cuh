@@ -170,6 +170,12 @@ CG_D void nf_update(float dtdx, const V* c, const V* FL, const V* FR, V* o) {
     for (int f = 0; f < 5; f++) o[f] = vfma(splat_v<V>(dtdx), vsub(FL[f], FR[f]), c[f]);
 }
 
+// speed_or_inf (device_common.cuh) per lane
+CG_D float nf_speed_or_inf(float a, float b, float s) { return speed_or_inf(a, b, s); }
+CG_D f2 nf_speed_or_inf(f2 a, f2 b, f2 s) {
+    return f2{make_float2(speed_or_inf(a.v.x, b.v.x, s.v.x), speed_or_inf(a.v.y, b.v.y, s.v.y))};
+}
+
 // Solvers/EulerSolvers.cpp:87-128 (2D: max(|vx|, |vy| + c) as written in the reference)
 template <class V>
 CG_D V nf_wavespeed(const NewtonFastParams& P, const V* u, int dims) {
@@ -178,8 +184,8 @@ CG_D V nf_wavespeed(const NewtonFastParams& P, const V* u, int dims) {
     const V q = vfma(u[1], u[1], vfma(u[2], u[2], vmul(u[3], u[3])));
     const V p = vfma(splat_v<V>(P.g1), u[4], vmul(splat_v<V>(-P.hg1), vmul(q, ir)));
     const V c = vsqrt(vmul(vmul(splat_v<V>(P.gam), p), ir));  // NaN for p < 0 is dropped by the max, as in the reference
-    if (dims == 1) return vadd(vabs(vx), c);
-    return vmax(vabs(vx), vadd(vabs(vy), c));
+    const V s = dims == 1 ? vadd(vabs(vx), c) : vmax(vabs(vx), vadd(vabs(vy), c));
+    return nf_speed_or_inf(u[0], u[4], s);
 }
 
 }  // namespace cg

@@ -248,8 +248,8 @@ CG_D void sr_force_fast(const SRFastParams& P, const float* L, const float* R, f
 CG_D float sr_wavespeed_fast(const SRFastParams& P, const float* u, int dims, int* flags) {
     const SRPrim32 c = sr_c2p_fast(P, u, flags);
     const float cs = fsqrt(fdiv(P.gf * c.p, c.rho * c.h));
-    if (dims == 1) return fabsf(c.vx) + cs;
-    return fmaxf(fabsf(c.vx), fabsf(c.vy)) + cs;
+    if (dims == 1) return speed_or_inf(u[0], u[4], fabsf(c.vx) + cs);
+    return speed_or_inf(u[0], u[4], fmaxf(fabsf(c.vx), fabsf(c.vy)) + cs);
 }
 
 }  // namespace cg

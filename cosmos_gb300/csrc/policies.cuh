@@ -103,7 +103,9 @@ struct ExactPolicy {
 template <class Sys>
 CG_D bool ExactPolicy<Sys>::excised_stencil(int, int) const { return false; }
 template <class Sys>
-CG_D double ExactPolicy<Sys>::wavespeed(const Cell& c, int, int) const { return sys.wavespeed(c.v, dims, Pt{0, 0, 0}); }
+CG_D double ExactPolicy<Sys>::wavespeed(const Cell& c, int, int) const {
+    return speed_or_inf(c.v[0], c.v[4], sys.wavespeed(c.v, dims, Pt{0, 0, 0}));
+}
 
 // GR excision: the updated cell and its stencil along both axes must lie outside the horizon
 // (Solvers/BlackHoleEulerSecondOrderSolver.cpp:44-46 in 1D, :81-85 in 2D; reach 1 for FORCE,
@@ -137,11 +139,11 @@ CG_D double ExactPolicy<GRExact>::wavespeed(const Cell& c, int line, int k) cons
     if (dims == 1) {
         const double cs = 1.0 / lm.nx;
         if (sys.bh.excised(j * cs, 0.0, 0.0)) return 0.0;
-        return fabs(sys.sound_speed(c.v, Pt{j * cs, 0.0, 0.0}));
+        return speed_or_inf(c.v[0], c.v[4], fabs(sys.sound_speed(c.v, Pt{j * cs, 0.0, 0.0})));
     }
     const double rs = 1.0 / ny, cs = 1.0 / lm.nx;
     if (sys.bh.excised(j * cs, i * rs, 0.0)) return 0.0;
-    return fabs(sys.sound_speed(c.v, Pt{i * rs, j * cs, 0.0}));
+    return speed_or_inf(c.v[0], c.v[4], fabs(sys.sound_speed(c.v, Pt{i * rs, j * cs, 0.0})));
 }
 
 // ------------------------------------------------------------------ Newtonian FP32 bulk

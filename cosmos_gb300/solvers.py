@@ -285,6 +285,11 @@ class Batch:
         check(load().cosmos_batch_run_end(self.h, r))
         return list(r)
 
+    def set_wait_limit(self, polls):
+        """Bound each grid-barrier wait to `polls` polls of about 64 ns (0: the default, about 4 s);
+        takes effect at the next run_begin."""
+        check(load().cosmos_batch_set_wait_limit(self.h, int(polls)))
+
     def set_shape(self, threads, rows, cap=0):
         check(load().cosmos_batch_set_shape(self.h, int(threads), int(rows), int(cap)))
 

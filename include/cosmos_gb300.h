@@ -36,10 +36,14 @@ extern "C" {
 #define COSMOS_ESTATE 5       /* call order violated */
 
 /* ---- device status bits reported by cosmos_solve_result.status */
-#define COSMOS_STATUS_NONFINITE 1  /* non-finite or non-positive dt was produced */
+#define COSMOS_STATUS_NONFINITE 1  /* a non-finite or non-positive dt was produced; a cell whose density
+                                      or energy (FP64 grids: pressure) is not finite has an infinite CFL
+                                      speed and so yields a zero dt (the reference carries NaNs on) */
 #define COSMOS_STATUS_NEWTON_CAP 2 /* a con2prim Newton solve stopped at its iteration cap (FP64 path: the
                                       reference's 1000; FP32 path: 40 FP32 + 8 FP64), or (FP32 path) a state
                                       beyond FP32's range was replaced by the floor state */
+#define COSMOS_STATUS_TIMEOUT 4    /* a bounded device wait gave up (the Y sweep's bulk-copy waits, about
+                                      a second of SM clocks) */
 
 /* ---- enumerations */
 enum { COSMOS_NEWTONIAN = 0, COSMOS_SR = 1, COSMOS_GR = 2 };
@@ -192,6 +196,13 @@ int cosmos_batch_run_end(cosmos_batch* b, cosmos_solve_result* results);
  * restores the state; cosmos_batch_autotune times every shape, keeps the fastest, and caches the
  * choice in cache_path (one line per device and batch signature; NULL for no cache). */
 int cosmos_batch_set_shape(cosmos_batch* b, int nt, int seg, int cap);
+/* Bound on each grid-barrier wait of the persistent launch, in polls of about 64 ns (0: the
+ * default 2^26, about 4 s), taking effect at the next cosmos_batch_run_begin.  A wait that runs
+ * out ends the launch (every block leaves at its next barrier) and cosmos_batch_run_end returns
+ * COSMOS_ECUDA ("a grid barrier wait timed out"); the grids' states are then partly advanced.
+ * No counterpart in the reference (which has no batched launch): it exists so that the timeout
+ * path can be exercised without a hung device. */
+int cosmos_batch_set_wait_limit(cosmos_batch* b, long long polls);
 int cosmos_batch_time_shape(cosmos_batch* b, int nt, int seg, int cap, int steps, double* ms_per_step);
 int cosmos_batch_autotune(cosmos_batch* b, const char* cache_path, int* nt, int* seg, int* cap, double* ms_per_step);
 
