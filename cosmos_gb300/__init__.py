@@ -12,6 +12,6 @@ from .solvers import (BlackHoleEulerFirstOrderSolver, BlackHoleEulerForcingSolve
                       RelativisticEulerFirstOrderSolver, RelativisticEulerSecondOrderSolver, RelativisticEulerSolvers,
                       default_context, solve_with_steps)
 from .solvers import (AMR, Batch, EulerAMR, EulerEquationOfState, RelativisticEulerAMR,  # noqa: F401
-                      RelativisticEulerEquationOfState, SlopeLimiters, state_eval)
+                      RelativisticEulerEquationOfState, SlopeLimiters, interface_eval, state_eval)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

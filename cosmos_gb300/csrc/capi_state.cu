@@ -111,4 +111,71 @@ int cosmos_state_eval(cosmos_ctx* ctx, const cosmos_params* p, int op, size_t n,
     return COSMOS_OK;
 }
 
+static_assert(COSMOS_IF_LAX_FRIEDRICHS == 0 && COSMOS_IF_EVOLUTION == 5 && COSMOS_IF_X_LAX_FRIEDRICHS_FLUX == 6 &&
+                  COSMOS_IF_Y_FORCE_FLUX == 11 && COSMOS_IF_X_SLIC_FLUX == 12 && COSMOS_IF_EVOLVE_HALF_X == 14 &&
+                  COSMOS_IF_EVOLVE_HALF_VECTOR_Y == 17 && COSMOS_IF_EVOLVE_FRACTION_X == 18 &&
+                  COSMOS_IF_EVOLVE_FRACTION_VECTOR == 20 && COSMOS_IF_RK_CELL_2D == 22 && kIfaceOps == 23,
+              "interface operation codes of the public header and the kernels differ");
+
+int cosmos_interface_width(int op, size_t* in_width, size_t* out_width) {
+    if (op < 0 || op >= kIfaceOps) return sfail(COSMOS_EINVAL, "unknown interface operation " + std::to_string(op));
+    if (in_width) *in_width = (size_t)kIfaceWidth[op];
+    if (out_width) *out_width = 5;
+    return COSMOS_OK;
+}
+
+int cosmos_interface_eval(cosmos_ctx* ctx, const cosmos_params* p, int op, size_t n, const double* in, const double* xyz,
+                          double dt, double bias, int limiter, double frac, int side, double* out) {
+    size_t wi = 0;
+    int rc = cosmos_interface_width(op, &wi, nullptr);
+    if (rc) return rc;
+    if (!ctx || !p) return sfail(COSMOS_EINVAL, "null context or params");
+    if (n == 0) return COSMOS_OK;
+    if (!in || !out) return sfail(COSMOS_EINVAL, "null input or output array");
+    if (p->system < COSMOS_NEWTONIAN || p->system > COSMOS_GR) return sfail(COSMOS_EINVAL, "unknown system");
+    if (!(p->gamma > 1.0)) return sfail(COSMOS_EINVAL, "gamma must exceed 1");
+    if (!(p->dx > 0.0) || !(dt > 0.0)) return sfail(COSMOS_EINVAL, "cellSpacing (params dx) and timeStep must be positive");
+    if (op >= COSMOS_IF_EVOLVE_FRACTION_X && p->system != COSMOS_GR)
+        return sfail(COSMOS_EUNSUPPORTED, "fractional evolutions and the forcing solver's cell update belong to the "
+                                          "black-hole system");
+    if ((op >= COSMOS_IF_EVOLVE_HALF_X && op <= COSMOS_IF_EVOLVE_HALF_VECTOR_Y) && side != 0 && side != 1)
+        return sfail(COSMOS_EINVAL, "side must be 0 (left / top face) or 1 (right / bottom face)");
+    const bool coords = p->system == COSMOS_GR && op >= COSMOS_IF_X_LAX_FRIEDRICHS_FLUX;
+    if (coords && !xyz) return sfail(COSMOS_EINVAL, "black-hole functions need the coordinate arguments (xyz)");
+    SCK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const size_t bin = n * wi * sizeof(double), bout = n * 5 * sizeof(double), bxyz = coords ? n * 3 * sizeof(double) : 0;
+    char* d = nullptr;
+    SCK(cudaMallocAsync((void**)&d, bin + bout + bxyz, st));
+    SweepArgs s;
+    memset(&s, 0, sizeof s);
+    s.system = p->system;
+    s.gamma = p->gamma;
+    s.dx = p->dx;
+    s.bh[0] = p->bh_mass; s.bh[1] = p->bh_spin; s.bh[2] = p->bh_x; s.bh[3] = p->bh_y; s.bh[4] = p->bh_z;
+    s.stream = st;
+    IfaceArgs a;
+    a.system = p->system;
+    a.op = op;
+    a.n = n;
+    a.in = (const double*)d;
+    a.out = (double*)(d + bin);
+    a.xyz = coords ? (const double*)(d + bin + bout) : nullptr;
+    a.dx = p->dx;
+    a.dt = dt;
+    a.bias = bias;
+    a.frac = frac;
+    a.lim = limiter;
+    a.side = side;
+    a.width = (int)wi;
+    cudaError_t e = cudaMemcpyAsync(d, in, bin, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && coords) e = cudaMemcpyAsync(d + bin + bout, xyz, bxyz, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launch_interface_eval(s, a);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d + bin, bout, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return sfail(COSMOS_ECUDA, std::string("interface evaluation: ") + cudaGetErrorString(e));
+    return COSMOS_OK;
+}
+
 }  // extern "C"

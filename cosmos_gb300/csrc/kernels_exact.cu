@@ -608,6 +608,114 @@ cudaError_t launch_state_eval(const SweepArgs& s, const StateEvalArgs& a) {
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ per-interface functions
+// The reference's static building blocks, one item per thread, in the reference's operation order
+// (this unit is compiled without FMA contraction):
+//   0 computeLaxFriedrichsFlux, 1 computeRichtmyerFlux (the intermediate state), 2 computeFORCEFlux,
+//   3 computeFORCEUpdate (Solvers/EulerFirstOrderSolver.cpp:3-24, :96-101), 4 computeFractional-
+//   EvolutionVector, 5 computeEvolutionVector (Solvers/EulerSolvers.cpp:163-172);
+//   6..11 computeX/Y{LaxFriedrichs,Richtmyer,FORCE}Flux of primitive states
+//   (Solvers/EulerFirstOrderSolver.cpp:26-94 and the SR and black-hole twins; black hole: states
+//   at x -/+ dx/2, the intermediate state's flux at x);
+//   12/13 computeX/YSLICFlux (Solvers/EulerSecondOrderSolver.cpp:3-25; black hole
+//   Solvers/BlackHoleEulerSecondOrderSolver.cpp:3-39: evolutions at x -/+ dx/2);
+//   14/15 evolveStateByHalfX/YTimeStep of states, 16/17 evolveStateByHalfTimeStep of vectors
+//   (Solvers/EulerSolvers.cpp:174-223; black hole Solvers/BlackHoleEulerSolvers.cpp:234-307);
+//   black hole only: 18/19 evolveStateByFractionalX/YTimeStep, 20 evolveStateByFractionalTimeStep
+//   (Solvers/BlackHoleEulerSolvers.cpp:159-232), 21/22 the forcing solver's
+//   evolveConservedVariableVector / ...2D (Solvers/BlackHoleEulerForcingSolver.cpp:3-185).
+template <class Sys>
+CG_D void iface_item(const Sys& S, bool gr, const IfaceArgs& A, const double* a, Pt q, double* o) {
+    const double* b = a + 5;
+    const double* c = a + 10;
+    const double* d = a + 15;
+    const int op = A.op;
+    const int axis = (op & 1) ? 1 : 0;
+    const double dx = A.dx, dt = A.dt;
+    switch (op) {
+        case 0: { const double r = dx / dt; for (int k = 0; k < 5; k++) o[k] = 0.5 * ((c[k] + d[k]) + (r * (a[k] - b[k]))); break; }
+        case 1: { const double r = dt / dx; for (int k = 0; k < 5; k++) o[k] = 0.5 * ((a[k] + b[k]) + (r * (c[k] - d[k]))); break; }
+        case 2: for (int k = 0; k < 5; k++) o[k] = 0.5 * (a[k] + b[k]); break;
+        case 3: { const double r = dt / dx; for (int k = 0; k < 5; k++) o[k] = a[k] + (r * (b[k] - c[k])); break; }
+        case 4: case 5: {
+            const double r = (op == 4 ? A.frac : 0.5) * (dt / dx);
+            for (int k = 0; k < 5; k++) o[k] = r * (a[k] - b[k]);
+            break;
+        }
+        case 6: case 7: case 8: case 9: {
+            double uL[5], uR[5], fL[5], fR[5];
+            const Pt pl = shift_pt(q, axis, -(dx * 0.5)), pr = shift_pt(q, axis, dx * 0.5);
+            S.cons(a, pl, uL);
+            S.cons(b, pr, uR);
+            S.flux(uL, axis, pl, fL);
+            S.flux(uR, axis, pr, fR);
+            if (op <= 7) {
+                const double r = dx / dt;
+                for (int k = 0; k < 5; k++) o[k] = 0.5 * ((fL[k] + fR[k]) + (r * (uL[k] - uR[k])));
+                break;
+            }
+            const double r = dt / dx;
+            double us[5];
+            for (int k = 0; k < 5; k++) us[k] = 0.5 * ((uL[k] + uR[k]) + (r * (fL[k] - fR[k])));
+            S.flux(us, axis, q, o);
+            break;
+        }
+        case 10: case 11: force_exact(S, a, b, q, axis, dx, dt, o); break;
+        case 12: case 13: {
+            double eR[5], eL[5];
+            evolve_half_exact(S, a, b, c, shift_pt(q, axis, -(dx * 0.5)), axis, dx, dt, A.bias, A.lim, (double*)nullptr, eR);
+            evolve_half_exact(S, b, c, d, shift_pt(q, axis, dx * 0.5), axis, dx, dt, A.bias, A.lim, eL, (double*)nullptr);
+            force_exact(S, eR, eL, q, axis, dx, dt, o);
+            break;
+        }
+        case 14: case 15:
+            evolve_half_exact(S, a, b, c, q, axis, dx, dt, A.bias, A.lim, A.side == 0 ? o : nullptr,
+                              A.side == 0 ? nullptr : o);
+            break;
+        case 16: case 17: {
+            double u[5];
+            const double* x = A.side == 0 ? a : b;
+            for (int k = 0; k < 5; k++) u[k] = x[k] + c[k];
+            S.prim(u, gr ? shift_pt(q, axis, A.side == 0 ? -(dx * 0.5) : dx * 0.5) : q, o);
+            break;
+        }
+        default: break;
+    }
+}
+
+__global__ void iface_kernel(IfaceArgs A, NewtonExact<double> nw, SRExact sr, GRExact gr) {
+    const int w = A.width;
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < A.n; k += (size_t)gridDim.x * blockDim.x) {
+        const double* a = A.in + (size_t)w * k;
+        double* o = A.out + 5 * k;
+        const Pt q = A.xyz ? Pt{A.xyz[3 * k], A.xyz[3 * k + 1], A.xyz[3 * k + 2]} : Pt{0.0, 0.0, 0.0};
+        if (A.system == 0) iface_item(nw, false, A, a, q, o);
+        else if (A.system == 1) iface_item(sr, false, A, a, q, o);
+        else if (A.op <= 17) iface_item(gr, true, A, a, q, o);
+        else if (A.op <= 19) evolve_fraction_exact(gr, A.frac, a, a + 5, a + 10, q, A.op - 18, A.dx, A.dt, A.bias, A.lim, o);
+        else if (A.op == 20) {
+            double u[5];
+            for (int f = 0; f < 5; f++) u[f] = a[f] + a[5 + f];
+            gr.prim(u, q, o);
+        } else if (A.op == 21) {
+            rk_cell_exact(gr, 1, a, a + 5, a + 10, a, a, q, A.dx, A.dt, A.bias, A.lim, o);
+        } else {
+            rk_cell_exact(gr, 2, a, a + 5, a + 10, a + 15, a + 20, q, A.dx, A.dt, A.bias, A.lim, o);
+        }
+    }
+}
+
+cudaError_t launch_interface_eval(const SweepArgs& s, const IfaceArgs& a) {
+    size_t b = (a.n + 127) / 128;
+    if (b > (size_t)device_sm_count() * 8) b = (size_t)device_sm_count() * 8;
+    SweepArgs g = s;
+    g.dx = a.dx;  // the black-hole metric derivatives take the cell spacing (the reference's h)
+    iface_kernel<<<(int)(b ? b : 1), 128, 0, s.stream>>>(a, NewtonExact<double>{s.gamma, nullptr}, SRExact{s.gamma, nullptr},
+                                                         make_gr(g));
+    count_launch();
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ conservation sums
 // Sum of each stored field over the grid with Kahan-Babuska (Neumaier) compensation per thread,
 // then compensated double atomics are avoided: per-block partials go to a small buffer summed by

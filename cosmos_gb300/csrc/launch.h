@@ -86,6 +86,24 @@ struct StateEvalArgs {
 // s supplies gamma, the hole and dx (the metric derivatives' spacing) and the stream
 cudaError_t launch_state_eval(const SweepArgs& s, const StateEvalArgs& a);
 
+// Per-interface solver functions (kernels_exact.cu), the operations of cosmos_interface_eval
+// (op numbers: the public COSMOS_IF_* values; input widths kIfaceWidth).
+constexpr int kIfaceOps = 23;
+constexpr int kIfaceWidth[kIfaceOps] = {20, 20, 10, 15, 10, 10, 10, 10, 10, 10, 10, 10,
+                                        20, 20, 15, 15, 15, 15, 15, 15, 10, 15, 25};
+struct IfaceArgs {
+    int system, op;
+    size_t n;
+    const double* in;   // device, kIfaceWidth[op] doubles per item
+    const double* xyz;  // device, 3 per item (black-hole system) or null
+    double* out;        // device, 5 per item
+    double dx, dt, bias, frac;
+    int lim, side;
+    int width;          // kIfaceWidth[op]
+};
+// s supplies gamma, the hole and the stream
+cudaError_t launch_interface_eval(const SweepArgs& s, const IfaceArgs& a);
+
 // FP32 bulk path (conserved SoA storage, float)
 cudaError_t launch_sweep_fast(const SweepArgs& a);
 cudaError_t launch_wavespeed_fast(const SweepArgs& a, unsigned long long* slot);

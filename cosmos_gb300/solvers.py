@@ -608,6 +608,34 @@ def state_eval(op, items, system=NEWTONIAN, gamma=1.4, xyz=None, black_hole=None
     return out
 
 
+def interface_eval(op, items, system=NEWTONIAN, gamma=1.4, dx=1.0, dt=1.0, xyz=None, black_hole=None, bias=0.0,
+                   limiter=1, frac=0.5, side=0, ctx=None):
+    """The reference's per-interface solver functions (computeXSLICFlux, computeLaxFriedrichsFlux,
+    evolveStateByHalfXTimeStep, ..., cosmos_interface_eval) for an array of items on the device,
+    bit for bit with the reference: op is a COSMOS_IF_* code (cosmos_gb300._lib.IF_*), items an
+    array whose last axis holds the op's inputs back to back (5-vectors: conserved vectors, flux
+    vectors or primitive states), dx the cellSpacing, dt the timeStep; xyz (..., 3) holds the
+    black-hole items' coordinate arguments.  Returns (n, 5): the vectors, or the primitives of the
+    returned states."""
+    ctx = ctx or default_context()
+    wi = ctypes.c_size_t(0)
+    check(load().cosmos_interface_width(int(op), ctypes.byref(wi), None))
+    a = np.ascontiguousarray(items, dtype=np.float64).reshape(-1, wi.value)
+    n = a.shape[0]
+    p = Params()
+    load().cosmos_params_default(ctypes.byref(p))
+    p.system, p.gamma, p.dx = int(system), float(gamma), float(dx)
+    if black_hole is not None:
+        p.bh_mass, p.bh_spin = black_hole.mass, black_hole.spin
+        p.bh_x, p.bh_y, p.bh_z = black_hole.x, black_hole.y, black_hole.z
+    q = None if xyz is None else np.ascontiguousarray(xyz, dtype=np.float64).reshape(n, 3)
+    out = np.empty((n, 5))
+    check(load().cosmos_interface_eval(ctx.h, ctypes.byref(p), int(op), n, a.ctypes.data,
+                                       None if q is None else q.ctypes.data, float(dt), float(bias), int(limiter),
+                                       float(frac), int(side), out.ctypes.data))
+    return out
+
+
 def _scalar_or_array(out, like):
     return float(out[0, 0]) if np.ndim(like) == 0 else out[:, 0].reshape(np.shape(like))
 

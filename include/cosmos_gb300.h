@@ -300,6 +300,53 @@ int cosmos_state_width(int op, size_t* in_width, size_t* out_width);
 int cosmos_state_eval(cosmos_ctx* ctx, const cosmos_params* p, int op, size_t n, const double* in, const double* xyz,
                       double bias, int limiter, double* out);
 
+/* ---- per-interface solver functions: the reference's static building blocks of the sweeps for
+ * arrays of items, evaluated on the device in the reference's operation order (bit for bit).
+ * in: n items of cosmos_interface_width(op) doubles (5-vectors back to back: conserved vectors,
+ * flux vectors or primitive states (rho, vx, vy, vz, p), in the reference function's argument
+ * order); out: n items of 5 doubles (a vector, or the primitives of the returned state).
+ * p supplies the system, gamma (materialParameters), dx (cellSpacing) and, for the black-hole
+ * system, the hole; xyz: 3 doubles per item, the (xCoordinate, yCoordinate, zCoordinate)
+ * arguments of the black-hole functions (NULL otherwise).  dt is timeStep; bias, limiter, frac
+ * (stepFraction) and side are the functions' arguments of those names where they have them. */
+enum {
+    COSMOS_IF_LAX_FRIEDRICHS = 0,   /* EulerFirstOrderSolver::computeLaxFriedrichsFlux (UL, UR, FL, FR)
+                                       Solvers/EulerFirstOrderSolver.hpp:11 */
+    COSMOS_IF_RICHTMYER = 1,        /* ::computeRichtmyerFlux (UL, UR, FL, FR) -> intermediate state, :13 */
+    COSMOS_IF_FORCE = 2,            /* ::computeFORCEFlux (LF flux, Richtmyer flux), :15 */
+    COSMOS_IF_FORCE_UPDATE = 3,     /* ::computeFORCEUpdate (U, FL, FR), :31 */
+    COSMOS_IF_FRACTIONAL_EVOLUTION = 4, /* EulerSolvers::computeFractionalEvolutionVector (FL, FR; frac),
+                                           Solvers/EulerSolvers.hpp:25 */
+    COSMOS_IF_EVOLUTION = 5,        /* EulerSolvers::computeEvolutionVector (FL, FR), :27 */
+    COSMOS_IF_X_LAX_FRIEDRICHS_FLUX = 6, /* *FirstOrderSolver::computeXLaxFriedrichsFlux (L, R states),
+                                            Solvers/EulerFirstOrderSolver.hpp:18, SR and black-hole twins */
+    COSMOS_IF_Y_LAX_FRIEDRICHS_FLUX = 7,
+    COSMOS_IF_X_RICHTMYER_FLUX = 8,
+    COSMOS_IF_Y_RICHTMYER_FLUX = 9,
+    COSMOS_IF_X_FORCE_FLUX = 10,
+    COSMOS_IF_Y_FORCE_FLUX = 11,
+    COSMOS_IF_X_SLIC_FLUX = 12,     /* *SecondOrderSolver::computeXSLICFlux (LL, L, R, RR states; bias, limiter),
+                                       Solvers/EulerSecondOrderSolver.hpp:9-14, SR and black-hole twins */
+    COSMOS_IF_Y_SLIC_FLUX = 13,
+    COSMOS_IF_EVOLVE_HALF_X = 14,   /* *Solvers::evolveStateByHalfXTimeStep (l, m, r states; bias, limiter, side),
+                                       Solvers/EulerSolvers.hpp:30-34, SR and black-hole twins */
+    COSMOS_IF_EVOLVE_HALF_Y = 15,
+    COSMOS_IF_EVOLVE_HALF_VECTOR_X = 16, /* *Solvers::evolveStateByHalfTimeStep (UL, UR, evolution; side),
+                                            Solvers/EulerSolvers.hpp:29; black hole: the vector form of
+                                            evolveStateByHalfXTimeStep, Solvers/BlackHoleEulerSolvers.hpp:37 */
+    COSMOS_IF_EVOLVE_HALF_VECTOR_Y = 17, /* the same (Newtonian, SR); black hole: evolveStateByHalfYTimeStep's :45 */
+    COSMOS_IF_EVOLVE_FRACTION_X = 18, /* black hole: evolveStateByFractionalXTimeStep (l, m, r; frac, bias, limiter),
+                                         Solvers/BlackHoleEulerSolvers.hpp:26 */
+    COSMOS_IF_EVOLVE_FRACTION_Y = 19,
+    COSMOS_IF_EVOLVE_FRACTION_VECTOR = 20, /* black hole: evolveStateByFractionalTimeStep (U, evolution), :22 */
+    COSMOS_IF_RK_CELL_1D = 21,      /* BlackHoleEulerForcingSolver::evolveConservedVariableVector (conserved l, m, r),
+                                       Solvers/BlackHoleEulerForcingSolver.hpp:9 */
+    COSMOS_IF_RK_CELL_2D = 22       /* ::evolveConservedVariableVector2D (conserved l, m, r, t, b), :13 */
+};
+int cosmos_interface_width(int op, size_t* in_width, size_t* out_width);
+int cosmos_interface_eval(cosmos_ctx* ctx, const cosmos_params* p, int op, size_t n, const double* in, const double* xyz,
+                          double dt, double bias, int limiter, double frac, int side, double* out);
+
 /* Allocation-free conservation sums.  No counterpart in the reference: it exists for callers that
  * cannot allocate device memory where they need the sums -- runtimes that own the device
  * allocator and its pool, embedded callers with a fixed memory budget, pipelines that must not

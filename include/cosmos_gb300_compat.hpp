@@ -144,6 +144,39 @@ inline std::vector<double> state_op(int sys, int op, const std::vector<double>& 
     check(cosmos_state_eval(ctx(), &p, op, 1, in.data(), xyz, bias, lim, out.data()));
     return out;
 }
+
+// One item of a per-interface solver function (cosmos_interface_eval): `in` holds the function's
+// vector and state arguments back to back (states as primitive vectors).
+inline std::vector<double> iface_op(int sys, int op, const std::vector<double>& in, double gamma, double dx, double dt,
+                                    double bias = 0.0, int lim = 1, double frac = 0.5, int side = 0,
+                                    const double* xyz = nullptr, const BlackHoleSpacetime* bh = nullptr) {
+    cosmos_params p;
+    cosmos_params_default(&p);
+    p.system = sys;
+    p.gamma = gamma;
+    p.dx = dx;
+    if (bh) {
+        double b[5];
+        bh->pack(b);
+        p.bh_mass = b[0]; p.bh_spin = b[1]; p.bh_x = b[2]; p.bh_y = b[3]; p.bh_z = b[4];
+    }
+    std::vector<double> out(5);
+    check(cosmos_interface_eval(ctx(), &p, op, 1, in.data(), xyz, dt, bias, lim, frac, side, out.data()));
+    return out;
+}
+inline void cat_into(std::vector<double>&) {}
+template <class... R>
+inline void cat_into(std::vector<double>& o, const std::vector<double>& v, const R&... rest) {
+    o.insert(o.end(), v.begin(), v.end());
+    cat_into(o, rest...);
+}
+template <class... V> inline std::vector<double> cat(const V&... v) {
+    std::vector<double> o;
+    cat_into(o, v...);
+    return o;
+}
+template <class S> inline std::vector<double> pv(S s) { return s.computePrimitiveVariableVector(); }
+template <class S> inline S from_prim(const std::vector<double>& p) { return S(p[0], p[1], p[2], p[3], p[4]); }
 }  // namespace cosmos_compat_detail
 
 // ----------------------------------------------------------------------------- state vectors
@@ -502,9 +535,63 @@ template <class S> std::vector<std::vector<S> > insert_boundary_2d(const std::ve
 
 }  // namespace cosmos_compat_detail
 
-#define COSMOS_COMPAT_SOLVERS(PREFIX, STATE, SYS)                                                               \
+// Per-interface building blocks (evolveStateByHalf*, compute*Flux): one item each through
+// cosmos_interface_eval, bit for bit with the reference.  VEC_SOLVERS / VEC_FIRST add the vector
+// forms the Newtonian classes declare (Solvers/EulerSolvers.hpp:25-27, EulerFirstOrderSolver.hpp:11-15, :31).
+#define COSMOS_COMPAT_EULER_VEC_SOLVERS                                                                        \
+    static std::vector<double> computeFractionalEvolutionVector(double f, std::vector<double> FL, std::vector<double> FR, \
+                                                                double dx, double dt) {                        \
+        using namespace cosmos_compat_detail;                                                                  \
+        return iface_op(COSMOS_NEWTONIAN, COSMOS_IF_FRACTIONAL_EVOLUTION, cat(FL, FR), 1.4, dx, dt, 0.0, 1, f); \
+    }                                                                                                          \
+    static std::vector<double> computeEvolutionVector(std::vector<double> FL, std::vector<double> FR, double dx,  \
+                                                      double dt) {                                             \
+        using namespace cosmos_compat_detail;                                                                  \
+        return iface_op(COSMOS_NEWTONIAN, COSMOS_IF_EVOLUTION, cat(FL, FR), 1.4, dx, dt);                      \
+    }
+#define COSMOS_COMPAT_EULER_VEC_FIRST                                                                          \
+    static std::vector<double> computeLaxFriedrichsFlux(std::vector<double> UL, std::vector<double> UR,        \
+                                                        std::vector<double> FL, std::vector<double> FR, double dx, \
+                                                        double dt) {                                           \
+        using namespace cosmos_compat_detail;                                                                  \
+        return iface_op(COSMOS_NEWTONIAN, COSMOS_IF_LAX_FRIEDRICHS, cat(UL, UR, FL, FR), 1.4, dx, dt);         \
+    }                                                                                                          \
+    static std::vector<double> computeRichtmyerFlux(std::vector<double> UL, std::vector<double> UR,            \
+                                                    std::vector<double> FL, std::vector<double> FR, double dx, double dt) { \
+        using namespace cosmos_compat_detail;                                                                  \
+        return iface_op(COSMOS_NEWTONIAN, COSMOS_IF_RICHTMYER, cat(UL, UR, FL, FR), 1.4, dx, dt);              \
+    }                                                                                                          \
+    static std::vector<double> computeFORCEFlux(std::vector<double> LF, std::vector<double> RI) {              \
+        using namespace cosmos_compat_detail;                                                                  \
+        return iface_op(COSMOS_NEWTONIAN, COSMOS_IF_FORCE, cat(LF, RI), 1.4, 1.0, 1.0);                        \
+    }                                                                                                          \
+    static std::vector<double> computeFORCEUpdate(std::vector<double> U, std::vector<double> FL,               \
+                                                  std::vector<double> FR, double dx, double dt) {              \
+        using namespace cosmos_compat_detail;                                                                  \
+        return iface_op(COSMOS_NEWTONIAN, COSMOS_IF_FORCE_UPDATE, cat(U, FL, FR), 1.4, dx, dt);                \
+    }
+#define COSMOS_COMPAT_SOLVERS(PREFIX, STATE, SYS, VEC_SOLVERS, VEC_FIRST)                                      \
     class PREFIX##Solvers {                                                                                    \
     public:                                                                                                    \
+        VEC_SOLVERS                                                                                            \
+        static STATE evolveStateByHalfTimeStep(std::vector<double> UL, std::vector<double> UR, std::vector<double> ev, \
+                                               int side, EulerMaterialParameters mp) {                         \
+            using namespace cosmos_compat_detail;                                                              \
+            return from_prim<STATE>(iface_op(SYS, COSMOS_IF_EVOLVE_HALF_VECTOR_X, cat(UL, UR, ev),             \
+                                             mp.getAdiabaticIndex(), 1.0, 1.0, 0.0, 1, 0.5, side));            \
+        }                                                                                                      \
+        static STATE evolveStateByHalfXTimeStep(STATE l, STATE m, STATE r, double dx, double dt, double bias,   \
+                                                int lim, int side, EulerMaterialParameters mp) {               \
+            using namespace cosmos_compat_detail;                                                              \
+            return from_prim<STATE>(iface_op(SYS, COSMOS_IF_EVOLVE_HALF_X, cat(pv(l), pv(m), pv(r)),           \
+                                             mp.getAdiabaticIndex(), dx, dt, bias, lim, 0.5, side));           \
+        }                                                                                                      \
+        static STATE evolveStateByHalfYTimeStep(STATE t, STATE m, STATE b, double dx, double dt, double bias,   \
+                                                int lim, int side, EulerMaterialParameters mp) {               \
+            using namespace cosmos_compat_detail;                                                              \
+            return from_prim<STATE>(iface_op(SYS, COSMOS_IF_EVOLVE_HALF_Y, cat(pv(t), pv(m), pv(b)),           \
+                                             mp.getAdiabaticIndex(), dx, dt, bias, lim, 0.5, side));           \
+        }                                                                                                      \
         static std::vector<STATE> insertBoundaryCells(std::vector<STATE>& c, int b) {                          \
             return cosmos_compat_detail::insert_boundary(c, b);                                                \
         }                                                                                                      \
@@ -535,6 +622,37 @@ template <class S> std::vector<std::vector<S> > insert_boundary_2d(const std::ve
     };                                                                                                         \
     class PREFIX##FirstOrderSolver {                                                                           \
     public:                                                                                                    \
+        VEC_FIRST                                                                                              \
+        static std::vector<double> computeXLaxFriedrichsFlux(STATE L, STATE R, double dx, double dt,           \
+                                                             EulerMaterialParameters mp) {                     \
+            using namespace cosmos_compat_detail;                                                              \
+            return iface_op(SYS, COSMOS_IF_X_LAX_FRIEDRICHS_FLUX, cat(pv(L), pv(R)), mp.getAdiabaticIndex(), dx, dt); \
+        }                                                                                                      \
+        static std::vector<double> computeYLaxFriedrichsFlux(STATE T, STATE B, double dx, double dt,           \
+                                                             EulerMaterialParameters mp) {                     \
+            using namespace cosmos_compat_detail;                                                              \
+            return iface_op(SYS, COSMOS_IF_Y_LAX_FRIEDRICHS_FLUX, cat(pv(T), pv(B)), mp.getAdiabaticIndex(), dx, dt); \
+        }                                                                                                      \
+        static std::vector<double> computeXRichtmyerFlux(STATE L, STATE R, double dx, double dt,               \
+                                                         EulerMaterialParameters mp) {                         \
+            using namespace cosmos_compat_detail;                                                              \
+            return iface_op(SYS, COSMOS_IF_X_RICHTMYER_FLUX, cat(pv(L), pv(R)), mp.getAdiabaticIndex(), dx, dt); \
+        }                                                                                                      \
+        static std::vector<double> computeYRichtmyerFlux(STATE T, STATE B, double dx, double dt,               \
+                                                         EulerMaterialParameters mp) {                         \
+            using namespace cosmos_compat_detail;                                                              \
+            return iface_op(SYS, COSMOS_IF_Y_RICHTMYER_FLUX, cat(pv(T), pv(B)), mp.getAdiabaticIndex(), dx, dt); \
+        }                                                                                                      \
+        static std::vector<double> computeXFORCEFlux(STATE L, STATE R, double dx, double dt,                   \
+                                                     EulerMaterialParameters mp) {                             \
+            using namespace cosmos_compat_detail;                                                              \
+            return iface_op(SYS, COSMOS_IF_X_FORCE_FLUX, cat(pv(L), pv(R)), mp.getAdiabaticIndex(), dx, dt);   \
+        }                                                                                                      \
+        static std::vector<double> computeYFORCEFlux(STATE T, STATE B, double dx, double dt,                   \
+                                                     EulerMaterialParameters mp) {                             \
+            using namespace cosmos_compat_detail;                                                              \
+            return iface_op(SYS, COSMOS_IF_Y_FORCE_FLUX, cat(pv(T), pv(B)), mp.getAdiabaticIndex(), dx, dt);   \
+        }                                                                                                      \
         static void computeFORCETimeStep(std::vector<STATE>& c, double dx, double dt, EulerMaterialParameters mp) { \
             cosmos_compat_detail::sweep1(SYS, c, dx, dt, 1, 0.0, 1, mp);                                       \
         }                                                                                                      \
@@ -557,6 +675,18 @@ template <class S> std::vector<std::vector<S> > insert_boundary_2d(const std::ve
     };                                                                                                         \
     class PREFIX##SecondOrderSolver {                                                                          \
     public:                                                                                                    \
+        static std::vector<double> computeXSLICFlux(STATE ll, STATE l, STATE r, STATE rr, double dx, double dt, \
+                                                    double bias, int lim, EulerMaterialParameters mp) {        \
+            using namespace cosmos_compat_detail;                                                              \
+            return iface_op(SYS, COSMOS_IF_X_SLIC_FLUX, cat(pv(ll), pv(l), pv(r), pv(rr)), mp.getAdiabaticIndex(), \
+                            dx, dt, bias, lim);                                                                \
+        }                                                                                                      \
+        static std::vector<double> computeYSLICFlux(STATE tt, STATE t, STATE b, STATE bb, double dx, double dt, \
+                                                    double bias, int lim, EulerMaterialParameters mp) {        \
+            using namespace cosmos_compat_detail;                                                              \
+            return iface_op(SYS, COSMOS_IF_Y_SLIC_FLUX, cat(pv(tt), pv(t), pv(b), pv(bb)), mp.getAdiabaticIndex(), \
+                            dx, dt, bias, lim);                                                                \
+        }                                                                                                      \
         static void computeSLICTimeStep(std::vector<STATE>& c, double dx, double dt, double bias, int lim,      \
                                         EulerMaterialParameters mp) {                                          \
             cosmos_compat_detail::sweep1(SYS, c, dx, dt, 2, bias, lim, mp);                                    \
@@ -579,14 +709,78 @@ template <class S> std::vector<std::vector<S> > insert_boundary_2d(const std::ve
             return cosmos_compat_detail::solve2(SYS, c, dx, cfl, T, 2, bias, lim, mp);                         \
         }                                                                                                      \
     };
-COSMOS_COMPAT_SOLVERS(Euler, EulerStateVector, COSMOS_NEWTONIAN)
-COSMOS_COMPAT_SOLVERS(RelativisticEuler, RelativisticEulerStateVector, COSMOS_SR)
+COSMOS_COMPAT_SOLVERS(Euler, EulerStateVector, COSMOS_NEWTONIAN, COSMOS_COMPAT_EULER_VEC_SOLVERS,
+                      COSMOS_COMPAT_EULER_VEC_FIRST)
+COSMOS_COMPAT_SOLVERS(RelativisticEuler, RelativisticEulerStateVector, COSMOS_SR, , )
 #undef COSMOS_COMPAT_SOLVERS
+#undef COSMOS_COMPAT_EULER_VEC_SOLVERS
+#undef COSMOS_COMPAT_EULER_VEC_FIRST
 
 // GR solvers take (..., subcyclingIterations, EulerMaterialParameters, BlackHoleSpacetime)
 // (Solvers/BlackHoleEulerSecondOrderSolver.hpp:10-32, Solvers/BlackHoleEulerForcingSolver.hpp:19-22).
+namespace cosmos_compat_detail {
+typedef BlackHoleEulerStateVector BHS;
+inline std::vector<double> bh_op(int op, const std::vector<double>& in, double x, double y, double z, double dx,
+                                 double dt, EulerMaterialParameters mp, const BlackHoleSpacetime& bh, double bias = 0.0,
+                                 int lim = 1, double frac = 0.5, int side = 0) {
+    const double q[3] = {x, y, z};
+    return iface_op(COSMOS_GR, op, in, mp.getAdiabaticIndex(), dx, dt, bias, lim, frac, side, q, &bh);
+}
+}  // namespace cosmos_compat_detail
+
 class BlackHoleEulerSolvers {
 public:
+    // Solvers/BlackHoleEulerSolvers.hpp:22-49: evolutions at (x, y, z), one item through cosmos_interface_eval
+    static BlackHoleEulerStateVector evolveStateByFractionalTimeStep(std::vector<double> U, std::vector<double> ev, double x,
+                                                                     double y, double z, EulerMaterialParameters mp,
+                                                                     BlackHoleSpacetime bh) {
+        using namespace cosmos_compat_detail;
+        return from_prim<BHS>(bh_op(COSMOS_IF_EVOLVE_FRACTION_VECTOR, cat(U, ev), x, y, z, 1.0, 1.0, mp, bh));
+    }
+    static BlackHoleEulerStateVector evolveStateByFractionalXTimeStep(double f, BlackHoleEulerStateVector l,
+                                                                      BlackHoleEulerStateVector m, BlackHoleEulerStateVector r,
+                                                                      double dx, double dt, double bias, int lim, double x,
+                                                                      double y, double z, EulerMaterialParameters mp,
+                                                                      BlackHoleSpacetime bh) {
+        using namespace cosmos_compat_detail;
+        return from_prim<BHS>(bh_op(COSMOS_IF_EVOLVE_FRACTION_X, cat(pv(l), pv(m), pv(r)), x, y, z, dx, dt, mp, bh, bias, lim, f));
+    }
+    static BlackHoleEulerStateVector evolveStateByFractionalYTimeStep(double f, BlackHoleEulerStateVector t,
+                                                                      BlackHoleEulerStateVector m, BlackHoleEulerStateVector b,
+                                                                      double dx, double dt, double bias, int lim, double x,
+                                                                      double y, double z, EulerMaterialParameters mp,
+                                                                      BlackHoleSpacetime bh) {
+        using namespace cosmos_compat_detail;
+        return from_prim<BHS>(bh_op(COSMOS_IF_EVOLVE_FRACTION_Y, cat(pv(t), pv(m), pv(b)), x, y, z, dx, dt, mp, bh, bias, lim, f));
+    }
+    static BlackHoleEulerStateVector evolveStateByHalfXTimeStep(std::vector<double> UL, std::vector<double> UR,
+                                                                std::vector<double> ev, int side, double dx, double x,
+                                                                double y, double z, EulerMaterialParameters mp,
+                                                                BlackHoleSpacetime bh) {
+        using namespace cosmos_compat_detail;
+        return from_prim<BHS>(bh_op(COSMOS_IF_EVOLVE_HALF_VECTOR_X, cat(UL, UR, ev), x, y, z, dx, 1.0, mp, bh, 0.0, 1, 0.5, side));
+    }
+    static BlackHoleEulerStateVector evolveStateByHalfXTimeStep(BlackHoleEulerStateVector l, BlackHoleEulerStateVector m,
+                                                                BlackHoleEulerStateVector r, double dx, double dt, double bias,
+                                                                int lim, int side, double x, double y, double z,
+                                                                EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        using namespace cosmos_compat_detail;
+        return from_prim<BHS>(bh_op(COSMOS_IF_EVOLVE_HALF_X, cat(pv(l), pv(m), pv(r)), x, y, z, dx, dt, mp, bh, bias, lim, 0.5, side));
+    }
+    static BlackHoleEulerStateVector evolveStateByHalfYTimeStep(std::vector<double> UT, std::vector<double> UB,
+                                                                std::vector<double> ev, int side, double dx, double x,
+                                                                double y, double z, EulerMaterialParameters mp,
+                                                                BlackHoleSpacetime bh) {
+        using namespace cosmos_compat_detail;
+        return from_prim<BHS>(bh_op(COSMOS_IF_EVOLVE_HALF_VECTOR_Y, cat(UT, UB, ev), x, y, z, dx, 1.0, mp, bh, 0.0, 1, 0.5, side));
+    }
+    static BlackHoleEulerStateVector evolveStateByHalfYTimeStep(BlackHoleEulerStateVector t, BlackHoleEulerStateVector m,
+                                                                BlackHoleEulerStateVector b, double dx, double dt, double bias,
+                                                                int lim, int side, double x, double y, double z,
+                                                                EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        using namespace cosmos_compat_detail;
+        return from_prim<BHS>(bh_op(COSMOS_IF_EVOLVE_HALF_Y, cat(pv(t), pv(m), pv(b)), x, y, z, dx, dt, mp, bh, bias, lim, 0.5, side));
+    }
     static std::vector<BlackHoleEulerStateVector> insertBoundaryCells(std::vector<BlackHoleEulerStateVector>& c, int b) {
         return cosmos_compat_detail::insert_boundary(c, b);
     }
@@ -612,8 +806,21 @@ public:
         return cosmos_stable_dt_rule(cfl * (dx / cosmos_compat_detail::max_speed2(COSMOS_GR, c, mp, &bh)), t, T, it);
     }
 };
+#define COSMOS_COMPAT_BH_FLUX(NAME, OP)                                                                         \
+    static std::vector<double> NAME(BlackHoleEulerStateVector a, BlackHoleEulerStateVector b, double x, double y, \
+                                    double z, double dx, double dt, EulerMaterialParameters mp, BlackHoleSpacetime bh) { \
+        using namespace cosmos_compat_detail;                                                                  \
+        return bh_op(OP, cat(pv(a), pv(b)), x, y, z, dx, dt, mp, bh);                                          \
+    }
 class BlackHoleEulerFirstOrderSolver {
 public:
+    // Solvers/BlackHoleEulerFirstOrderSolver.hpp:11-28: fluxes at the interface point (x, y, z)
+    COSMOS_COMPAT_BH_FLUX(computeXLaxFriedrichsFlux, COSMOS_IF_X_LAX_FRIEDRICHS_FLUX)
+    COSMOS_COMPAT_BH_FLUX(computeYLaxFriedrichsFlux, COSMOS_IF_Y_LAX_FRIEDRICHS_FLUX)
+    COSMOS_COMPAT_BH_FLUX(computeXRichtmyerFlux, COSMOS_IF_X_RICHTMYER_FLUX)
+    COSMOS_COMPAT_BH_FLUX(computeYRichtmyerFlux, COSMOS_IF_Y_RICHTMYER_FLUX)
+    COSMOS_COMPAT_BH_FLUX(computeXFORCEFlux, COSMOS_IF_X_FORCE_FLUX)
+    COSMOS_COMPAT_BH_FLUX(computeYFORCEFlux, COSMOS_IF_Y_FORCE_FLUX)
     static void computeFORCETimeStep(std::vector<BlackHoleEulerStateVector>& c, double dx, double dt,
                                      EulerMaterialParameters mp, BlackHoleSpacetime bh) {
         cosmos_compat_detail::sweep1(COSMOS_GR, c, dx, dt, 1, 0.0, 1, mp, &bh);
@@ -637,8 +844,24 @@ public:
         return cosmos_compat_detail::solve2(COSMOS_GR, c, dx, cfl, T, 1, 0.0, 1, mp, sub, &bh);
     }
 };
+#undef COSMOS_COMPAT_BH_FLUX
 class BlackHoleEulerSecondOrderSolver {
 public:
+    // Solvers/BlackHoleEulerSecondOrderSolver.hpp:9-16
+    static std::vector<double> computeXSLICFlux(BlackHoleEulerStateVector ll, BlackHoleEulerStateVector l,
+                                                BlackHoleEulerStateVector r, BlackHoleEulerStateVector rr, double dx, double dt,
+                                                double bias, int lim, double x, double y, double z, EulerMaterialParameters mp,
+                                                BlackHoleSpacetime bh) {
+        using namespace cosmos_compat_detail;
+        return bh_op(COSMOS_IF_X_SLIC_FLUX, cat(pv(ll), pv(l), pv(r), pv(rr)), x, y, z, dx, dt, mp, bh, bias, lim);
+    }
+    static std::vector<double> computeYSLICFlux(BlackHoleEulerStateVector tt, BlackHoleEulerStateVector t,
+                                                BlackHoleEulerStateVector b, BlackHoleEulerStateVector bb, double dx, double dt,
+                                                double bias, int lim, double x, double y, double z, EulerMaterialParameters mp,
+                                                BlackHoleSpacetime bh) {
+        using namespace cosmos_compat_detail;
+        return bh_op(COSMOS_IF_Y_SLIC_FLUX, cat(pv(tt), pv(t), pv(b), pv(bb)), x, y, z, dx, dt, mp, bh, bias, lim);
+    }
     static void computeSLICTimeStep(std::vector<BlackHoleEulerStateVector>& c, double dx, double dt, double bias,
                                     int lim, EulerMaterialParameters mp, BlackHoleSpacetime bh) {
         cosmos_compat_detail::sweep1(COSMOS_GR, c, dx, dt, 2, bias, lim, mp, &bh);
@@ -664,6 +887,22 @@ public:
 };
 class BlackHoleEulerForcingSolver {
 public:
+    // Solvers/BlackHoleEulerForcingSolver.hpp:9-17: one cell's RK4 source update (conserved vectors)
+    static std::vector<double> evolveConservedVariableVector(std::vector<double> l, std::vector<double> m,
+                                                             std::vector<double> r, double x, double y, double z, double dx,
+                                                             double dt, double bias, int lim, EulerMaterialParameters mp,
+                                                             BlackHoleSpacetime bh) {
+        using namespace cosmos_compat_detail;
+        return bh_op(COSMOS_IF_RK_CELL_1D, cat(l, m, r), x, y, z, dx, dt, mp, bh, bias, lim);
+    }
+    static std::vector<double> evolveConservedVariableVector2D(std::vector<double> l, std::vector<double> m,
+                                                               std::vector<double> r, std::vector<double> t,
+                                                               std::vector<double> b, double x, double y, double z,
+                                                               double dx, double dt, double bias, int lim,
+                                                               EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+        using namespace cosmos_compat_detail;
+        return bh_op(COSMOS_IF_RK_CELL_2D, cat(l, m, r, t, b), x, y, z, dx, dt, mp, bh, bias, lim);
+    }
     static void computeRungeKuttaTimeStep(std::vector<BlackHoleEulerStateVector>& c, double dx, double dt, double bias,
                                           int lim, EulerMaterialParameters mp, BlackHoleSpacetime bh) {
         double b[5];

@@ -931,6 +931,131 @@ double orc_limiter(double r, double bias, int lim) { return limiter(r, bias, lim
 void orc_slope(const double* ul, const double* uc, const double* ur, double bias, int lim, double* s) {
     slope_vector(ul, uc, ur, bias, lim, s);
 }
+// ---------------------------------------------------------------- per-interface solver functions
+// One reference building block per op, applied to n items (in: in_width doubles per item, out: 5
+// per item; xyz: the reference's coordinate arguments per item, black-hole system only).  The op
+// numbers are the public COSMOS_IF_* values.  Vector forms restate the reference's VectorAlgebra
+// compositions in its operation order:
+//   0 computeLaxFriedrichsFlux  Solvers/EulerFirstOrderSolver.cpp:3-11   (UL, UR, FL, FR)
+//   1 computeRichtmyerFlux      :13-19 (the intermediate state)          (UL, UR, FL, FR)
+//   2 computeFORCEFlux          :21-24                                   (LF, RI)
+//   3 computeFORCEUpdate        :96-101                                  (U, FL, FR)
+//   4 computeFractionalEvolutionVector  Solvers/EulerSolvers.cpp:163-167 (FL, FR; frac)
+//   5 computeEvolutionVector    Solvers/EulerSolvers.cpp:169-172         (FL, FR)
+// State forms (primitive states in, flux or primitive state out):
+//   6/7 computeX/YLaxFriedrichsFlux, 8/9 computeX/YRichtmyerFlux, 10/11 computeX/YFORCEFlux
+//       Solvers/EulerFirstOrderSolver.cpp:26-94; SR Solvers/RelativisticEulerFirstOrderSolver.cpp;
+//       black hole Solvers/BlackHoleEulerFirstOrderSolver.cpp:3-94 (states at x -/+ dx/2, the
+//       Richtmyer state's flux at x)                                   (L, R)
+//   12/13 computeX/YSLICFlux  Solvers/EulerSecondOrderSolver.cpp:3-25, SR twin, black hole
+//       Solvers/BlackHoleEulerSecondOrderSolver.cpp:3-39                 (LL, L, R, RR)
+//   14/15 evolveStateByHalfX/YTimeStep (states; side)  Solvers/EulerSolvers.cpp:190-223, SR
+//       Solvers/RelativisticEulerSolvers.cpp:166-199, black hole Solvers/BlackHoleEulerSolvers.cpp:250-307
+//                                                                      (l, m, r)
+//   16/17 evolveStateByHalfTimeStep (vector form; side)  Solvers/EulerSolvers.cpp:174-188, SR :148-164;
+//       black hole evolveStateByHalfX/YTimeStep vector forms Solvers/BlackHoleEulerSolvers.cpp:234-248,
+//       :281-295 (the evolved state converted at x -/+ dx/2)           (UL, UR, evolution)
+// Black hole only:
+//   18/19 evolveStateByFractionalX/YTimeStep  Solvers/BlackHoleEulerSolvers.cpp:171-232 (l, m, r; frac)
+//   20 evolveStateByFractionalTimeStep  Solvers/BlackHoleEulerSolvers.cpp:159-169       (U, evolution)
+//   21 BlackHoleEulerForcingSolver::evolveConservedVariableVector    :3-70  (conserved l, m, r)
+//   22 BlackHoleEulerForcingSolver::evolveConservedVariableVector2D  :72-185 (conserved l, m, r, t, b)
+// Returns 0, or -1 for an op this system does not have.
+int orc_interface_width(int op, int* in_w) {
+    static const int w[23] = {20, 20, 10, 15, 10, 10, 10, 10, 10, 10, 10, 10, 20, 20, 15, 15, 15, 15, 15, 15, 10, 15, 25};
+    if (op < 0 || op > 22) return -1;
+    *in_w = w[op];
+    return 0;
+}
+
+}  // extern "C"
+
+template <class Sys>
+static int interface_item(const Sys& S, bool gr, int op, const double* a, Pt q, double dx, double dt, double w, int lim,
+                          double frac, int side, double* o) {
+    const double* b = a + 5;
+    const double* c = a + 10;
+    const double* d = a + 15;
+    const int axis = (op & 1) ? 1 : 0;  // ops 6..19 alternate X (even) and Y (odd)
+    switch (op) {
+        case 0: { const double r = dx / dt; for (int k = 0; k < 5; k++) o[k] = 0.5 * ((c[k] + d[k]) + (r * (a[k] - b[k]))); return 0; }
+        case 1: { const double r = dt / dx; for (int k = 0; k < 5; k++) o[k] = 0.5 * ((a[k] + b[k]) + (r * (c[k] - d[k]))); return 0; }
+        case 2: for (int k = 0; k < 5; k++) o[k] = 0.5 * (a[k] + b[k]); return 0;
+        case 3: { const double r = dt / dx; for (int k = 0; k < 5; k++) o[k] = a[k] + (r * (b[k] - c[k])); return 0; }
+        case 4: case 5: {
+            const double r = (op == 4 ? frac : 0.5) * (dt / dx);
+            for (int k = 0; k < 5; k++) o[k] = r * (a[k] - b[k]);
+            return 0;
+        }
+        case 6: case 7: case 8: case 9: {
+            double uL[5], uR[5], fL[5], fR[5], us[5];
+            const Pt pl = shift(q, axis, -(dx * 0.5)), pr = shift(q, axis, dx * 0.5);
+            S.cons(a, pl, uL);
+            S.cons(b, pr, uR);
+            S.flux(uL, axis, pl, fL);
+            S.flux(uR, axis, pr, fR);
+            if (op <= 7) {
+                const double r = dx / dt;
+                for (int k = 0; k < 5; k++) o[k] = 0.5 * ((fL[k] + fR[k]) + (r * (uL[k] - uR[k])));
+                return 0;
+            }
+            const double r = dt / dx;
+            for (int k = 0; k < 5; k++) us[k] = 0.5 * ((uL[k] + uR[k]) + (r * (fL[k] - fR[k])));
+            S.flux(us, axis, q, o);
+            return 0;
+        }
+        case 10: case 11: force_flux(S, a, b, q, axis, dx, dt, o); return 0;
+        case 12: case 13: {
+            double eR[5], eL[5];
+            evolve_half(S, a, b, c, shift(q, axis, -(dx * 0.5)), axis, dx, dt, w, lim, (double*)nullptr, eR);
+            evolve_half(S, b, c, d, shift(q, axis, dx * 0.5), axis, dx, dt, w, lim, eL, (double*)nullptr);
+            force_flux(S, eR, eL, q, axis, dx, dt, o);
+            return 0;
+        }
+        case 14: case 15:
+            evolve_half(S, a, b, c, q, axis, dx, dt, w, lim, side == 0 ? o : nullptr, side == 0 ? nullptr : o);
+            return 0;
+        case 16: case 17: {
+            double u[5];
+            const double* x = side == 0 ? a : b;
+            for (int k = 0; k < 5; k++) u[k] = x[k] + c[k];
+            S.prim(u, gr ? shift(q, axis, side == 0 ? -(dx * 0.5) : dx * 0.5) : q, o);
+            return 0;
+        }
+        default: return -1;
+    }
+}
+
+extern "C" {
+
+int orc_interface_eval(int op, int sys, size_t n, const double* in, const double* xyz, double gamma, const double* bh,
+                       double dx, double dt, double bias, int lim, double frac, int side, double* out) {
+    int iw = 0;
+    if (orc_interface_width(op, &iw)) return -1;
+    for (size_t i = 0; i < n; i++) {
+        const double* a = in + iw * i;
+        double* o = out + 5 * i;
+        Pt q = xyz ? Pt{xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]} : Pt{0.0, 0.0, 0.0};
+        int rc;
+        if (sys == 0) rc = op > 17 ? -1 : interface_item(Newton<double>{gamma}, false, op, a, q, dx, dt, bias, lim, frac, side, o);
+        else if (sys == 1) rc = op > 17 ? -1 : interface_item(SR{gamma}, false, op, a, q, dx, dt, bias, lim, frac, side, o);
+        else {
+            GR S{gamma, BH{bh[0], bh[1], bh[2], bh[3], bh[4]}, dx};
+            if (op <= 17) rc = interface_item(S, true, op, a, q, dx, dt, bias, lim, frac, side, o);
+            else if (op <= 19) { evolve_fraction(S, frac, a, a + 5, a + 10, q, op - 18, dx, dt, bias, lim, o); rc = 0; }
+            else if (op == 20) {
+                double u[5];
+                for (int k = 0; k < 5; k++) u[k] = a[k] + a[5 + k];
+                S.prim(u, q, o);
+                rc = 0;
+            } else if (op == 21) { rk_cell(S, 1, a, a + 5, a + 10, a, a, q, dx, dt, bias, lim, o); rc = 0; }
+            else { rk_cell(S, 2, a, a + 5, a + 10, a + 15, a + 20, q, dx, dt, bias, lim, o); rc = 0; }
+        }
+        if (rc) return rc;
+    }
+    return 0;
+}
+
 // metric probe with the same layout as the reference harness's ref_gr_metric
 void orc_gr_metric(double x, double y, double z, double h, const double* bhp, double* out) {
     BH b{bhp[0], bhp[1], bhp[2], bhp[3], bhp[4]};

@@ -41,6 +41,22 @@ def _bh(bh):
     return np.ascontiguousarray(np.asarray(bh if bh is not None else (1.0, 0.0, 0.5, 0.5, 0.0), dtype=np.float64))
 
 
+IFACE_WIDTH = (20, 20, 10, 15, 10, 10, 10, 10, 10, 10, 10, 10, 20, 20, 15, 15, 15, 15, 15, 15, 10, 15, 25)
+
+
+def _iface(fn, op, system, items, xyz, gamma, bh, dx, dt, bias, lim, frac, side):
+    """Shared driver of orc_interface_eval / ref_interface_eval: items (n, in_width), xyz (n, 3) or
+    None; returns (n, 5)."""
+    a = np.ascontiguousarray(items, dtype=np.float64).reshape(-1, IFACE_WIDTH[op])
+    n = a.shape[0]
+    q = None if xyz is None else np.ascontiguousarray(xyz, dtype=np.float64).reshape(n, 3)
+    o = np.zeros((n, 5))
+    rc = fn(op, _sys(system), n, _ptr(a), _ptr(q), gamma, _ptr(_bh(bh)), dx, dt, bias, lim, frac, side, _ptr(o))
+    if rc:
+        raise ValueError(f"interface op {op} is not defined for system {system}")
+    return o
+
+
 class Oracle:
     """The FP64 restatement (always available once built)."""
 
@@ -53,6 +69,8 @@ class Oracle:
         L.orc_max_wavespeed.restype = _d
         L.orc_stable_dt.argtypes = [_i, _p, _i, _i, _i, _d, _d, _d, _d, _i, _d, _p]
         L.orc_stable_dt.restype = _d
+        L.orc_interface_eval.argtypes = [_i, _i, ctypes.c_size_t, _p, _p, _d, _p, _d, _d, _d, _i, _d, _i, _p]
+        L.orc_interface_eval.restype = _i
         L.orc_stable_dt_rule.argtypes = [_d, _d, _d, _i]
         L.orc_stable_dt_rule.restype = _d
         L.orc_rk_source.argtypes = [_p, _i, _i, _i, _d, _d, _d, _i, _d, _p]
@@ -151,6 +169,11 @@ class Oracle:
 
     def limiter(self, r, bias, lim):
         return self.L.orc_limiter(r, bias, lim)
+
+    def interface(self, op, system, items, xyz=None, gamma=1.4, bh=None, dx=0.01, dt=0.004, bias=0.0, lim=1,
+                  frac=0.5, side=0):
+        """The per-interface solver function `op` (orc_interface_eval) on each item."""
+        return _iface(self.L.orc_interface_eval, op, system, items, xyz, gamma, bh, dx, dt, bias, lim, frac, side)
 
     def slope(self, ul, uc, ur, bias, lim):
         a, b, c = (np.ascontiguousarray(v, dtype=np.float64) for v in (ul, uc, ur)); o = np.zeros(5)
@@ -266,6 +289,8 @@ class Reference:
             getattr(L, n).argtypes = [_p, _d, _p]
         for n in ("ref_euler_flux", "ref_sr_flux"):
             getattr(L, n).argtypes = [_p, _i, _d, _p]
+        L.ref_interface_eval.argtypes = [_i, _i, ctypes.c_size_t, _p, _p, _d, _p, _d, _d, _d, _i, _d, _i, _p]
+        L.ref_interface_eval.restype = _i
         L.ref_limiter.argtypes = [_d, _d, _i]
         L.ref_limiter.restype = _d
         L.ref_slope.argtypes = [_p, _p, _p, _d, _i, _p]
@@ -358,6 +383,11 @@ class Reference:
 
     def limiter(self, r, bias, lim):
         return self.L.ref_limiter(r, bias, lim)
+
+    def interface(self, op, system, items, xyz=None, gamma=1.4, bh=None, dx=0.01, dt=0.004, bias=0.0, lim=1,
+                  frac=0.5, side=0):
+        """The reference's own static function for `op` (ref_interface_eval) on each item."""
+        return _iface(self.L.ref_interface_eval, op, system, items, xyz, gamma, bh, dx, dt, bias, lim, frac, side)
 
     def slope(self, ul, uc, ur, bias, lim):
         a, b, c = (np.ascontiguousarray(v, dtype=np.float64) for v in (ul, uc, ur)); o = np.zeros(5)

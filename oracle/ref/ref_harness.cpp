@@ -334,6 +334,108 @@ double ref_gr_sound_speed(const double* prim, double x, double y, double z, doub
     return make_state<BlackHoleEulerStateVector>(prim).computeSoundSpeed(x, y, z, mp, mkbh(bh));
 }
 
+// ---------------------------------------------------------------- per-interface solver functions
+// The reference's static building blocks applied to n items: in holds the op's inputs per item
+// (vectors of 5 doubles: conserved vectors, flux vectors or primitive states, see
+// orc_interface_eval in oracle/cosmos_oracle.cpp for the op list), xyz the coordinate arguments
+// (black hole only), out 5 doubles per item (a vector, or the primitives of the returned state).
+}  // extern "C"
+
+namespace {
+const int kIfaceWidth[23] = {20, 20, 10, 15, 10, 10, 10, 10, 10, 10, 10, 10, 20, 20, 15, 15, 15, 15, 15, 15, 10, 15, 25};
+
+// ops 0..5: system-independent vector forms
+bool vector_op(int op, const double* a, double dx, double dt, double frac, double* o) {
+    auto v = [&](int k) { return mk5(a + 5 * k); };
+    switch (op) {
+        case 0: vec5(EulerFirstOrderSolver::computeLaxFriedrichsFlux(v(0), v(1), v(2), v(3), dx, dt), o); return true;
+        case 1: vec5(EulerFirstOrderSolver::computeRichtmyerFlux(v(0), v(1), v(2), v(3), dx, dt), o); return true;
+        case 2: vec5(EulerFirstOrderSolver::computeFORCEFlux(v(0), v(1)), o); return true;
+        case 3: vec5(EulerFirstOrderSolver::computeFORCEUpdate(v(0), v(1), v(2), dx, dt), o); return true;
+        case 4: vec5(EulerSolvers::computeFractionalEvolutionVector(frac, v(0), v(1), dx, dt), o); return true;
+        case 5: vec5(EulerSolvers::computeEvolutionVector(v(0), v(1), dx, dt), o); return true;
+        default: return false;
+    }
+}
+
+// Newtonian and special-relativistic state forms (the same signatures in both families)
+template <class S, class First, class Second, class Solvers>
+int flat_op(int op, const double* a, double dx, double dt, double bias, int lim, int side, double gamma, double* o) {
+    EulerMaterialParameters mp(gamma);
+    auto st = [&](int k) { return make_state<S>(a + 5 * k); };
+    auto v = [&](int k) { return mk5(a + 5 * k); };
+    switch (op) {
+        case 6: vec5(First::computeXLaxFriedrichsFlux(st(0), st(1), dx, dt, mp), o); return 0;
+        case 7: vec5(First::computeYLaxFriedrichsFlux(st(0), st(1), dx, dt, mp), o); return 0;
+        case 8: vec5(First::computeXRichtmyerFlux(st(0), st(1), dx, dt, mp), o); return 0;
+        case 9: vec5(First::computeYRichtmyerFlux(st(0), st(1), dx, dt, mp), o); return 0;
+        case 10: vec5(First::computeXFORCEFlux(st(0), st(1), dx, dt, mp), o); return 0;
+        case 11: vec5(First::computeYFORCEFlux(st(0), st(1), dx, dt, mp), o); return 0;
+        case 12: vec5(Second::computeXSLICFlux(st(0), st(1), st(2), st(3), dx, dt, bias, lim, mp), o); return 0;
+        case 13: vec5(Second::computeYSLICFlux(st(0), st(1), st(2), st(3), dx, dt, bias, lim, mp), o); return 0;
+        case 14: put_state(Solvers::evolveStateByHalfXTimeStep(st(0), st(1), st(2), dx, dt, bias, lim, side, mp), o); return 0;
+        case 15: put_state(Solvers::evolveStateByHalfYTimeStep(st(0), st(1), st(2), dx, dt, bias, lim, side, mp), o); return 0;
+        case 16: case 17: put_state(Solvers::evolveStateByHalfTimeStep(v(0), v(1), v(2), side, mp), o); return 0;
+        default: return -1;
+    }
+}
+
+int gr_op(int op, const double* a, const double* q, double dx, double dt, double bias, int lim, double frac, int side,
+          double gamma, const double* bhp, double* o) {
+    typedef BlackHoleEulerStateVector S;
+    EulerMaterialParameters mp(gamma);
+    BlackHoleSpacetime bh = mkbh(bhp);
+    const double x = q[0], y = q[1], z = q[2];
+    auto st = [&](int k) { return make_state<S>(a + 5 * k); };
+    auto v = [&](int k) { return mk5(a + 5 * k); };
+    typedef BlackHoleEulerFirstOrderSolver F;
+    typedef BlackHoleEulerSolvers V;
+    switch (op) {
+        case 6: vec5(F::computeXLaxFriedrichsFlux(st(0), st(1), x, y, z, dx, dt, mp, bh), o); return 0;
+        case 7: vec5(F::computeYLaxFriedrichsFlux(st(0), st(1), x, y, z, dx, dt, mp, bh), o); return 0;
+        case 8: vec5(F::computeXRichtmyerFlux(st(0), st(1), x, y, z, dx, dt, mp, bh), o); return 0;
+        case 9: vec5(F::computeYRichtmyerFlux(st(0), st(1), x, y, z, dx, dt, mp, bh), o); return 0;
+        case 10: vec5(F::computeXFORCEFlux(st(0), st(1), x, y, z, dx, dt, mp, bh), o); return 0;
+        case 11: vec5(F::computeYFORCEFlux(st(0), st(1), x, y, z, dx, dt, mp, bh), o); return 0;
+        case 12: vec5(BlackHoleEulerSecondOrderSolver::computeXSLICFlux(st(0), st(1), st(2), st(3), dx, dt, bias, lim, x, y, z, mp, bh), o); return 0;
+        case 13: vec5(BlackHoleEulerSecondOrderSolver::computeYSLICFlux(st(0), st(1), st(2), st(3), dx, dt, bias, lim, x, y, z, mp, bh), o); return 0;
+        case 14: put_state(V::evolveStateByHalfXTimeStep(st(0), st(1), st(2), dx, dt, bias, lim, side, x, y, z, mp, bh), o); return 0;
+        case 15: put_state(V::evolveStateByHalfYTimeStep(st(0), st(1), st(2), dx, dt, bias, lim, side, x, y, z, mp, bh), o); return 0;
+        case 16: put_state(V::evolveStateByHalfXTimeStep(v(0), v(1), v(2), side, dx, x, y, z, mp, bh), o); return 0;
+        case 17: put_state(V::evolveStateByHalfYTimeStep(v(0), v(1), v(2), side, dx, x, y, z, mp, bh), o); return 0;
+        case 18: put_state(V::evolveStateByFractionalXTimeStep(frac, st(0), st(1), st(2), dx, dt, bias, lim, x, y, z, mp, bh), o); return 0;
+        case 19: put_state(V::evolveStateByFractionalYTimeStep(frac, st(0), st(1), st(2), dx, dt, bias, lim, x, y, z, mp, bh), o); return 0;
+        case 20: put_state(V::evolveStateByFractionalTimeStep(v(0), v(1), x, y, z, mp, bh), o); return 0;
+        case 21: vec5(BlackHoleEulerForcingSolver::evolveConservedVariableVector(v(0), v(1), v(2), x, y, z, dx, dt, bias, lim, mp, bh), o); return 0;
+        case 22: vec5(BlackHoleEulerForcingSolver::evolveConservedVariableVector2D(v(0), v(1), v(2), v(3), v(4), x, y, z, dx, dt, bias, lim, mp, bh), o); return 0;
+        default: return -1;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int ref_interface_eval(int op, int sys, size_t n, const double* in, const double* xyz, double gamma, const double* bh,
+                       double dx, double dt, double bias, int lim, double frac, int side, double* out) {
+    if (op < 0 || op > 22) return -1;
+    const int iw = kIfaceWidth[op];
+    for (size_t i = 0; i < n; i++) {
+        const double* a = in + (size_t)iw * i;
+        double* o = out + 5 * i;
+        if (vector_op(op, a, dx, dt, frac, o)) continue;
+        int rc;
+        if (sys == 0)
+            rc = flat_op<EulerStateVector, EulerFirstOrderSolver, EulerSecondOrderSolver, EulerSolvers>(op, a, dx, dt, bias, lim, side, gamma, o);
+        else if (sys == 1)
+            rc = flat_op<RelativisticEulerStateVector, RelativisticEulerFirstOrderSolver, RelativisticEulerSecondOrderSolver,
+                         RelativisticEulerSolvers>(op, a, dx, dt, bias, lim, side, gamma, o);
+        else
+            rc = gr_op(op, a, xyz + 3 * i, dx, dt, bias, lim, frac, side, gamma, bh, o);
+        if (rc) return rc;
+    }
+    return 0;
+}
+
 void ref_gr_sweep(double* prim, int ny, int nx, int dims, int axis, int order, double dx, double dt,
                   double bias, int lim, double gamma, const double* bh) {
     typedef BlackHoleEulerStateVector S;
