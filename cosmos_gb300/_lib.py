@@ -18,6 +18,8 @@ SUPERBEE, VANLEER, MINBEE = 0, 1, 2
 (STATE_CONS, STATE_PRIM, STATE_FLUX_X, STATE_FLUX_Y, STATE_SOUND, STATE_INTERNAL_ENERGY, STATE_TOTAL_ENERGY,
  STATE_PRESSURE, STATE_ENTHALPY, STATE_SOURCE, STATE_EIGENVALUES, STATE_GRADIENT_RATIO, STATE_LIMITER,
  STATE_SLOPE) = range(14)
+# every public quantity of BlackHoleSpacetime at a point (cosmos_spacetime_eval, COSMOS_ST_* offsets)
+SPACETIME_WIDTH = 125
 # per-interface solver functions (cosmos_interface_eval), the public COSMOS_IF_* codes
 (IF_LAX_FRIEDRICHS, IF_RICHTMYER, IF_FORCE, IF_FORCE_UPDATE, IF_FRACTIONAL_EVOLUTION, IF_EVOLUTION,
  IF_X_LAX_FRIEDRICHS_FLUX, IF_Y_LAX_FRIEDRICHS_FLUX, IF_X_RICHTMYER_FLUX, IF_Y_RICHTMYER_FLUX, IF_X_FORCE_FLUX,
@@ -102,6 +104,7 @@ SIGNATURES = {
     "cosmos_batch_set_shape": (_i, [_p, _i, _i, _i]),
     "cosmos_batch_set_wait_limit": (_i, [_p, ctypes.c_longlong]),
     "cosmos_interface_width": (_i, [_i, ctypes.POINTER(_sz), ctypes.POINTER(_sz)]),
+    "cosmos_spacetime_eval": (_i, [_p, ctypes.POINTER(Params), _sz, _p, _p]),
     "cosmos_interface_eval": (_i, [_p, ctypes.POINTER(Params), _i, _sz, _p, _p, _d, _d, _i, _d, _i, _p]),
     "cosmos_batch_time_shape": (_i, [_p, _i, _i, _i, _i, ctypes.POINTER(_d)]),
     "cosmos_batch_autotune": (_i, [_p, ctypes.c_char_p, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i),

@@ -117,6 +117,35 @@ static_assert(COSMOS_IF_LAX_FRIEDRICHS == 0 && COSMOS_IF_EVOLUTION == 5 && COSMO
                   COSMOS_IF_EVOLVE_FRACTION_VECTOR == 20 && COSMOS_IF_RK_CELL_2D == 22 && kIfaceOps == 23,
               "interface operation codes of the public header and the kernels differ");
 
+static_assert(COSMOS_SPACETIME_WIDTH == kSpacetimeWidth && COSMOS_ST_EXCISED == kSpacetimeWidth - 1,
+              "spacetime record layouts of the public header and the kernel differ");
+
+int cosmos_spacetime_eval(cosmos_ctx* ctx, const cosmos_params* p, size_t n, const double* xyz, double* out) {
+    if (!ctx || !p) return sfail(COSMOS_EINVAL, "null context or params");
+    if (n == 0) return COSMOS_OK;
+    if (!xyz || !out) return sfail(COSMOS_EINVAL, "null coordinate or output array");
+    if (!(p->dx > 0.0)) return sfail(COSMOS_EINVAL, "the derivative spacing (params dx, the reference's cellSpacing) must be positive");
+    SCK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const size_t bq = n * 3 * sizeof(double), bo = n * kSpacetimeWidth * sizeof(double);
+    char* d = nullptr;
+    SCK(cudaMallocAsync((void**)&d, bq + bo, st));
+    SweepArgs s;
+    memset(&s, 0, sizeof s);
+    s.system = COSMOS_GR;
+    s.gamma = p->gamma > 1.0 ? p->gamma : 5.0 / 3.0;
+    s.dx = p->dx;
+    s.bh[0] = p->bh_mass; s.bh[1] = p->bh_spin; s.bh[2] = p->bh_x; s.bh[3] = p->bh_y; s.bh[4] = p->bh_z;
+    s.stream = st;
+    cudaError_t e = cudaMemcpyAsync(d, xyz, bq, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launch_spacetime_eval(s, n, (const double*)d, (double*)(d + bq));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d + bq, bo, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return sfail(COSMOS_ECUDA, std::string("spacetime evaluation: ") + cudaGetErrorString(e));
+    return COSMOS_OK;
+}
+
 int cosmos_interface_width(int op, size_t* in_width, size_t* out_width) {
     if (op < 0 || op >= kIfaceOps) return sfail(COSMOS_EINVAL, "unknown interface operation " + std::to_string(op));
     if (in_width) *in_width = (size_t)kIfaceWidth[op];

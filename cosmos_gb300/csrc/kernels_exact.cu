@@ -716,6 +716,53 @@ cudaError_t launch_interface_eval(const SweepArgs& s, const IfaceArgs& a) {
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ spacetime record
+// Every public quantity of the reference's BlackHoleSpacetime (BlackHoleEuler/BlackHoleSpacetime.cpp:
+// 54-386) at one point, metric derivatives by the reference's centred differences with spacing
+// S.h, in the layout of the public COSMOS_ST_* offsets.
+__global__ void spacetime_kernel(GRExact S, size_t n, const double* __restrict__ xyz, double* __restrict__ out) {
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        const Pt q{xyz[3 * k], xyz[3 * k + 1], xyz[3 * k + 2]};
+        double* o = out + (size_t)kSpacetimeWidth * k;
+        const BHExact& b = S.bh;
+        o[0] = b.H(q.x, q.y, q.z);                            // computeKerrSchildScalar
+        b.l(q.x, q.y, q.z, o + 1);                            // computeKerrSchildVector
+        b.L4(q.x, q.y, q.z, o + 4);                           // computeKerrSchildSpacetimeVector
+        const double h = S.h, hs = 0.5 * h;
+        for (int d = 0; d < 3; d++) {                         // the scalar and vector derivatives
+            const Pt p1 = S.off(q, d, hs), p0 = S.off(q, d, -hs);
+            double h1, h0, a1[3], a0[3];
+            b.Hl(p1.x, p1.y, p1.z, h1, a1);
+            b.Hl(p0.x, p0.y, p0.z, h0, a0);
+            o[8 + d] = (h1 - h0) / h;
+            for (int c = 0; c < 3; c++) o[11 + 3 * d + c] = (1.0 / h) * (a1[c] - a0[c]);
+        }
+        double m[9], g4m[16];
+        b.gamma(q.x, q.y, q.z, m);
+        b.g4(q.x, q.y, q.z, g4m);
+        for (int i = 0; i < 9; i++) o[20 + i] = m[i];
+        for (int i = 0; i < 16; i++) o[29 + i] = g4m[i];
+        inverse3(m, o + 45);
+        inverse4(g4m, o + 54);
+        o[70] = det3(m);
+        o[71] = det4(g4m);
+        double al, gi[16];
+        b.lapse_shift(q.x, q.y, q.z, al, o + 100);
+        o[99] = al;
+        // lapse, shift and spatial-metric derivatives and K_ij as the source term takes them
+        S.source_metric(q, al, gi, o + 103, o + 106, o + 72, o + 115);
+        o[124] = b.excised(q.x, q.y, q.z) ? 1.0 : 0.0;
+    }
+}
+
+cudaError_t launch_spacetime_eval(const SweepArgs& s, size_t n, const double* xyz, double* out) {
+    size_t blocks = (n + 127) / 128;
+    if (blocks > (size_t)device_sm_count() * 8) blocks = (size_t)device_sm_count() * 8;
+    spacetime_kernel<<<(int)(blocks ? blocks : 1), 128, 0, s.stream>>>(make_gr(s), n, xyz, out);
+    count_launch();
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ conservation sums
 // Sum of each stored field over the grid with Kahan-Babuska (Neumaier) compensation per thread,
 // then compensated double atomics are avoided: per-block partials go to a small buffer summed by

@@ -103,6 +103,10 @@ struct IfaceArgs {
 };
 // s supplies gamma, the hole and the stream
 cudaError_t launch_interface_eval(const SweepArgs& s, const IfaceArgs& a);
+// BlackHoleSpacetime's public quantities at n points (kSpacetimeWidth doubles each; s supplies the
+// hole and, in s.dx, the derivative spacing)
+constexpr int kSpacetimeWidth = 125;
+cudaError_t launch_spacetime_eval(const SweepArgs& s, size_t n, const double* xyz, double* out);
 
 // FP32 bulk path (conserved SoA storage, float)
 cudaError_t launch_sweep_fast(const SweepArgs& a);

@@ -19,6 +19,7 @@ import threading
 import numpy as np
 
 from . import _lib
+from ._lib import SPACETIME_WIDTH  # noqa: F401
 from ._lib import (BC_PERIODIC, BC_TRANSMISSIVE, FP32, FP64, GR, NEWTONIAN, SR, Params, SolveOpts,  # noqa: F401
                    SolveResult, check, load)
 
@@ -61,6 +62,108 @@ class BlackHoleSpacetime:
 
     def getBlackHoleSpin(self):
         return self.spin
+
+    def getBlackHoleXPosition(self):
+        return self.x
+
+    def getBlackHoleYPosition(self):
+        return self.y
+
+    def getBlackHoleZPosition(self):
+        return self.z
+
+    def setBlackHoleMass(self, v):
+        self.mass = float(v)
+
+    def setBlackHoleSpin(self, v):
+        self.spin = float(v)
+
+    def setBlackHoleXPosition(self, v):
+        self.x = float(v)
+
+    def setBlackHoleYPosition(self, v):
+        self.y = float(v)
+
+    def setBlackHoleZPosition(self, v):
+        self.z = float(v)
+
+    # ---- the metric (BlackHoleEuler/BlackHoleSpacetime.hpp:16-42), evaluated on the device
+    # (cosmos_spacetime_eval, bit for bit with the reference); coordinates may be arrays
+    def record(self, x, y, z, cellSpacing=1.0, ctx=None):
+        """Every public quantity at the points (x, y, z): array (..., 125) in the layout of the
+        COSMOS_ST_* offsets; the derivative entries use cellSpacing."""
+        xb, yb, zb = np.broadcast_arrays(*(np.asarray(v, dtype=np.float64) for v in (x, y, z)))
+        q = np.ascontiguousarray(np.stack([xb, yb, zb], axis=-1).reshape(-1, 3))
+        p = Params()
+        load().cosmos_params_default(ctypes.byref(p))
+        p.system, p.dx = GR, float(cellSpacing)
+        p.bh_mass, p.bh_spin, p.bh_x, p.bh_y, p.bh_z = self.mass, self.spin, self.x, self.y, self.z
+        out = np.empty((q.shape[0], SPACETIME_WIDTH))
+        check(load().cosmos_spacetime_eval((ctx or default_context()).h, ctypes.byref(p), q.shape[0],
+                                           q.ctypes.data, out.ctypes.data))
+        return out.reshape(xb.shape + (SPACETIME_WIDTH,))
+
+    def _part(self, at, shape, x, y, z, h=1.0):
+        r = self.record(x, y, z, h)[..., at:at + int(np.prod(shape))]
+        r = r.reshape(r.shape[:-1] + shape)
+        return float(r) if np.ndim(x) == 0 and shape == () else r
+
+    def computeKerrSchildScalar(self, x, y, z):
+        return self._part(0, (), x, y, z)
+
+    def computeKerrSchildVector(self, x, y, z):
+        return self._part(1, (3,), x, y, z)
+
+    def computeKerrSchildSpacetimeVector(self, x, y, z):
+        return self._part(4, (4,), x, y, z)
+
+    def computeKerrSchildScalarDerivative(self, x, y, z, cellSpacing):
+        return self._part(8, (3,), x, y, z, cellSpacing)
+
+    def computeKerrSchildVectorDerivative(self, x, y, z, cellSpacing):
+        return self._part(11, (3, 3), x, y, z, cellSpacing)
+
+    def computeSpatialMetricTensor(self, x, y, z):
+        return self._part(20, (3, 3), x, y, z)
+
+    def computeSpacetimeMetricTensor(self, x, y, z):
+        return self._part(29, (4, 4), x, y, z)
+
+    def computeInverseSpatialMetricTensor(self, x, y, z):
+        return self._part(45, (3, 3), x, y, z)
+
+    def computeInverseSpacetimeMetricTensor(self, x, y, z):
+        return self._part(54, (4, 4), x, y, z)
+
+    def computeSpatialMetricDeterminant(self, x, y, z):
+        return self._part(70, (), x, y, z)
+
+    def computeSpacetimeMetricDeterminant(self, x, y, z):
+        return self._part(71, (), x, y, z)
+
+    def computeSpatialMetricTensorDerivative(self, x, y, z, cellSpacing):
+        return self._part(72, (3, 3, 3), x, y, z, cellSpacing)
+
+    def computeLapseFunction(self, x, y, z):
+        return self._part(99, (), x, y, z)
+
+    def computeShiftVector(self, x, y, z):
+        return self._part(100, (3,), x, y, z)
+
+    def computeLapseFunctionDerivative(self, x, y, z, cellSpacing):
+        return self._part(103, (3,), x, y, z, cellSpacing)
+
+    def computeShiftVectorDerivative(self, x, y, z, cellSpacing):
+        return self._part(106, (3, 3), x, y, z, cellSpacing)
+
+    def computeExtrinsicCurvatureTensor(self, x, y, z, cellSpacing):
+        return self._part(115, (3, 3), x, y, z, cellSpacing)
+
+    def inExcisionRegion(self, x, y, z):
+        """BlackHoleEuler/BlackHoleSpacetime.cpp:372-386, on the host (no device call)."""
+        r = np.sqrt((np.asarray(x) - self.x) ** 2 + (np.asarray(y) - self.y) ** 2 + (np.asarray(z) - self.z) ** 2)
+        e = r <= self.mass * (1.0 + np.sqrt(1.0 - self.spin * self.spin))
+        return bool(e) if np.ndim(e) == 0 else e
 
 
 class Context:

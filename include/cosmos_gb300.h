@@ -347,6 +347,32 @@ int cosmos_interface_width(int op, size_t* in_width, size_t* out_width);
 int cosmos_interface_eval(cosmos_ctx* ctx, const cosmos_params* p, int op, size_t n, const double* in, const double* xyz,
                           double dt, double bias, int limiter, double frac, int side, double* out);
 
+/* ---- the black-hole spacetime (BlackHoleEuler/BlackHoleSpacetime.hpp:16-42): every public quantity
+ * of the reference's BlackHoleSpacetime at n points xyz (3 doubles each), COSMOS_SPACETIME_WIDTH
+ * doubles per point at the offsets below (matrices row-major; derivatives [direction][...]), bit for
+ * bit with the reference.  p supplies the hole (bh_*) and, in dx, the cellSpacing of the derivative
+ * methods (centred differences at -/+ dx/2). */
+#define COSMOS_ST_KS_SCALAR 0                /* computeKerrSchildScalar */
+#define COSMOS_ST_KS_VECTOR 1                /* computeKerrSchildVector (3) */
+#define COSMOS_ST_KS_SPACETIME_VECTOR 4      /* computeKerrSchildSpacetimeVector (4) */
+#define COSMOS_ST_KS_SCALAR_DERIVATIVE 8     /* computeKerrSchildScalarDerivative (3) */
+#define COSMOS_ST_KS_VECTOR_DERIVATIVE 11    /* computeKerrSchildVectorDerivative (3 x 3) */
+#define COSMOS_ST_SPATIAL_METRIC 20          /* computeSpatialMetricTensor (3 x 3) */
+#define COSMOS_ST_SPACETIME_METRIC 29        /* computeSpacetimeMetricTensor (4 x 4) */
+#define COSMOS_ST_INVERSE_SPATIAL_METRIC 45  /* computeInverseSpatialMetricTensor (3 x 3) */
+#define COSMOS_ST_INVERSE_SPACETIME_METRIC 54 /* computeInverseSpacetimeMetricTensor (4 x 4) */
+#define COSMOS_ST_SPATIAL_DETERMINANT 70     /* computeSpatialMetricDeterminant */
+#define COSMOS_ST_SPACETIME_DETERMINANT 71   /* computeSpacetimeMetricDeterminant */
+#define COSMOS_ST_SPATIAL_METRIC_DERIVATIVE 72 /* computeSpatialMetricTensorDerivative (3 x 3 x 3) */
+#define COSMOS_ST_LAPSE 99                   /* computeLapseFunction */
+#define COSMOS_ST_SHIFT 100                  /* computeShiftVector (3) */
+#define COSMOS_ST_LAPSE_DERIVATIVE 103       /* computeLapseFunctionDerivative (3) */
+#define COSMOS_ST_SHIFT_DERIVATIVE 106       /* computeShiftVectorDerivative (3 x 3) */
+#define COSMOS_ST_EXTRINSIC_CURVATURE 115    /* computeExtrinsicCurvatureTensor (3 x 3) */
+#define COSMOS_ST_EXCISED 124                /* inExcisionRegion (1.0 or 0.0) */
+#define COSMOS_SPACETIME_WIDTH 125
+int cosmos_spacetime_eval(cosmos_ctx* ctx, const cosmos_params* p, size_t n, const double* xyz, double* out);
+
 /* Allocation-free conservation sums.  No counterpart in the reference: it exists for callers that
  * cannot allocate device memory where they need the sums -- runtimes that own the device
  * allocator and its pool, embedded callers with a fixed memory budget, pipelines that must not

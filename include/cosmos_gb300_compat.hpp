@@ -118,7 +118,75 @@ public:
         return r <= (m * (1.0 + std::sqrt(1.0 - (a * a))));
     }
     void pack(double* o) const { o[0] = m; o[1] = a; o[2] = x; o[3] = y; o[4] = z; }
+
+    // The metric methods (BlackHoleEuler/BlackHoleSpacetime.hpp:16-40), evaluated on the device
+    // (cosmos_spacetime_eval), bit for bit with the reference.
+    double computeKerrSchildScalar(double X, double Y, double Z) { return rec(X, Y, Z)[COSMOS_ST_KS_SCALAR]; }
+    std::vector<double> computeKerrSchildVector(double X, double Y, double Z) { return vec(rec(X, Y, Z), COSMOS_ST_KS_VECTOR, 3); }
+    std::vector<double> computeKerrSchildSpacetimeVector(double X, double Y, double Z) {
+        return vec(rec(X, Y, Z), COSMOS_ST_KS_SPACETIME_VECTOR, 4);
+    }
+    std::vector<double> computeKerrSchildScalarDerivative(double X, double Y, double Z, double h) {
+        return vec(rec(X, Y, Z, h), COSMOS_ST_KS_SCALAR_DERIVATIVE, 3);
+    }
+    std::vector<std::vector<double> > computeKerrSchildVectorDerivative(double X, double Y, double Z, double h) {
+        return mat(rec(X, Y, Z, h), COSMOS_ST_KS_VECTOR_DERIVATIVE, 3);
+    }
+    std::vector<std::vector<double> > computeSpatialMetricTensor(double X, double Y, double Z) {
+        return mat(rec(X, Y, Z), COSMOS_ST_SPATIAL_METRIC, 3);
+    }
+    std::vector<std::vector<double> > computeSpacetimeMetricTensor(double X, double Y, double Z) {
+        return mat(rec(X, Y, Z), COSMOS_ST_SPACETIME_METRIC, 4);
+    }
+    std::vector<std::vector<double> > computeInverseSpatialMetricTensor(double X, double Y, double Z) {
+        return mat(rec(X, Y, Z), COSMOS_ST_INVERSE_SPATIAL_METRIC, 3);
+    }
+    std::vector<std::vector<double> > computeInverseSpacetimeMetricTensor(double X, double Y, double Z) {
+        return mat(rec(X, Y, Z), COSMOS_ST_INVERSE_SPACETIME_METRIC, 4);
+    }
+    double computeSpatialMetricDeterminant(double X, double Y, double Z) { return rec(X, Y, Z)[COSMOS_ST_SPATIAL_DETERMINANT]; }
+    double computeSpacetimeMetricDeterminant(double X, double Y, double Z) {
+        return rec(X, Y, Z)[COSMOS_ST_SPACETIME_DETERMINANT];
+    }
+    std::vector<std::vector<std::vector<double> > > computeSpatialMetricTensorDerivative(double X, double Y, double Z, double h) {
+        const std::vector<double> r = rec(X, Y, Z, h);
+        std::vector<std::vector<std::vector<double> > > d(3);
+        for (int k = 0; k < 3; k++) d[k] = mat(r, COSMOS_ST_SPATIAL_METRIC_DERIVATIVE + 9 * k, 3);
+        return d;
+    }
+    double computeLapseFunction(double X, double Y, double Z) { return rec(X, Y, Z)[COSMOS_ST_LAPSE]; }
+    std::vector<double> computeShiftVector(double X, double Y, double Z) { return vec(rec(X, Y, Z), COSMOS_ST_SHIFT, 3); }
+    std::vector<double> computeLapseFunctionDerivative(double X, double Y, double Z, double h) {
+        return vec(rec(X, Y, Z, h), COSMOS_ST_LAPSE_DERIVATIVE, 3);
+    }
+    std::vector<std::vector<double> > computeShiftVectorDerivative(double X, double Y, double Z, double h) {
+        return mat(rec(X, Y, Z, h), COSMOS_ST_SHIFT_DERIVATIVE, 3);
+    }
+    std::vector<std::vector<double> > computeExtrinsicCurvatureTensor(double X, double Y, double Z, double h) {
+        return mat(rec(X, Y, Z, h), COSMOS_ST_EXTRINSIC_CURVATURE, 3);
+    }
+
 private:
+    std::vector<double> rec(double X, double Y, double Z, double h = 1.0) const {
+        cosmos_params p;
+        cosmos_params_default(&p);
+        p.system = COSMOS_GR;
+        p.dx = h;
+        p.bh_mass = m; p.bh_spin = a; p.bh_x = x; p.bh_y = y; p.bh_z = z;
+        std::vector<double> o(COSMOS_SPACETIME_WIDTH);
+        const double q[3] = {X, Y, Z};
+        cosmos_compat_detail::check(cosmos_spacetime_eval(cosmos_compat_detail::ctx(), &p, 1, q, o.data()));
+        return o;
+    }
+    static std::vector<double> vec(const std::vector<double>& r, int at, int n) {
+        return std::vector<double>(r.begin() + at, r.begin() + at + n);
+    }
+    static std::vector<std::vector<double> > mat(const std::vector<double>& r, int at, int n) {
+        std::vector<std::vector<double> > o(n, std::vector<double>(n));
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) o[i][j] = r[at + n * i + j];
+        return o;
+    }
     double m, a, x, y, z;
 };
 

@@ -1081,6 +1081,66 @@ void orc_gr_metric(double x, double y, double z, double h, const double* bhp, do
     for (int i = 0; i < 9; i++) out[48 + i] = gs[i];
 }
 
+// Every public quantity of BlackHoleSpacetime (BlackHoleEuler/BlackHoleSpacetime.hpp:16-42) at one
+// point, derivatives with spacing h, in the layout of the public COSMOS_ST_* offsets:
+//   0 computeKerrSchildScalar, 1 computeKerrSchildVector (3), 4 computeKerrSchildSpacetimeVector (4),
+//   8 computeKerrSchildScalarDerivative (3), 11 computeKerrSchildVectorDerivative ([dir][comp], 9),
+//   20 computeSpatialMetricTensor (9), 29 computeSpacetimeMetricTensor (16),
+//   45 computeInverseSpatialMetricTensor (9), 54 computeInverseSpacetimeMetricTensor (16),
+//   70 computeSpatialMetricDeterminant, 71 computeSpacetimeMetricDeterminant,
+//   72 computeSpatialMetricTensorDerivative ([dir][i][j], 27), 99 computeLapseFunction,
+//   100 computeShiftVector (3), 103 computeLapseFunctionDerivative (3),
+//   106 computeShiftVectorDerivative ([dir][comp], 9), 115 computeExtrinsicCurvatureTensor (9),
+//   124 inExcisionRegion (1 or 0).
+void orc_spacetime_record(double x, double y, double z, double h, const double* bhp, double* o) {
+    BH b{bhp[0], bhp[1], bhp[2], bhp[3], bhp[4]};
+    GR S{5.0 / 3.0, b, h};
+    const Pt q{x, y, z};
+    double m[9], g4m[16];
+    o[0] = b.H(x, y, z);
+    b.l(x, y, z, o + 1);
+    b.L4(x, y, z, o + 4);
+    S.dH(q, o + 8);
+    S.dl(q, o + 11);
+    b.gamma(x, y, z, m);
+    for (int i = 0; i < 9; i++) o[20 + i] = m[i];
+    b.g4(x, y, z, g4m);
+    for (int i = 0; i < 16; i++) o[29 + i] = g4m[i];
+    inverse_n(m, 3, o + 45);
+    inverse_n(g4m, 4, o + 54);
+    o[70] = det_n(m, 3);
+    o[71] = det_n(g4m, 4);
+    S.dgamma(q, o + 72);
+    o[99] = b.lapse(x, y, z);
+    b.shiftv(x, y, z, o + 100);
+    S.dalpha(q, o + 103);
+    S.dbeta(q, o + 106);
+    S.Kij(q, o + 115);
+    o[124] = b.excised(x, y, z) ? 1.0 : 0.0;
+}
+
+// BlackHoleEuler/BlackHoleEulerEigenvalues.cpp:3-96: material (3), fast acoustic (3) and slow
+// acoustic (3) eigenvalues of primitives p at (x, y, z)
+void orc_gr_eigenvalues(const double* p, double x, double y, double z, double gamma, const double* bhp, double* o) {
+    BH b{bhp[0], bhp[1], bhp[2], bhp[3], bhp[4]};
+    double al = b.lapse(x, y, z), be[3], gm[9], gs[9];
+    b.shiftv(x, y, z, be);
+    b.gamma(x, y, z, gm);
+    inverse_n(gm, 3, gs);
+    const double cs = sr_sound(p[0], p[4], gamma);
+    const double v[3] = {p[1], p[2], p[3]};
+    double v2 = 0.0;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) v2 = v2 + ((gm[3 * i + j] * v[i]) * v[j]);
+    for (int i = 0; i < 3; i++) {
+        const double rt = std::sqrt((1.0 - v2) * ((gs[3 * i + i] * (1.0 - (v2 * (cs * cs)))) - ((v[i] * v[i]) * (1.0 - (cs * cs)))));
+        const double pre = al / (1.0 - (v2 * (cs * cs)));
+        o[i] = (al * v[i]) - be[i];
+        o[3 + i] = (pre * ((v[i] * (1.0 - (cs * cs))) + (cs * rt))) - be[i];
+        o[6 + i] = (pre * ((v[i] * (1.0 - (cs * cs))) - (cs * rt))) - be[i];
+    }
+}
+
 // ---------------------------------------------------------------- AMR flagging
 // Refinement pass of the Level-1 drivers: AMR/EulerAMR.cpp:207-229 (1D), :394-431 (2D);
 // SR twins AMR/RelativisticEulerAMR.cpp (2D bottom neighbour read at [i+2][j+2], :422);

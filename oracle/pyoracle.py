@@ -71,6 +71,8 @@ class Oracle:
         L.orc_stable_dt.restype = _d
         L.orc_interface_eval.argtypes = [_i, _i, ctypes.c_size_t, _p, _p, _d, _p, _d, _d, _d, _i, _d, _i, _p]
         L.orc_interface_eval.restype = _i
+        L.orc_spacetime_record.argtypes = [_d, _d, _d, _d, _p, _p]
+        L.orc_gr_eigenvalues.argtypes = [_p, _d, _d, _d, _d, _p, _p]
         L.orc_stable_dt_rule.argtypes = [_d, _d, _d, _i]
         L.orc_stable_dt_rule.restype = _d
         L.orc_rk_source.argtypes = [_p, _i, _i, _i, _d, _d, _d, _i, _d, _p]
@@ -174,6 +176,32 @@ class Oracle:
                   frac=0.5, side=0):
         """The per-interface solver function `op` (orc_interface_eval) on each item."""
         return _iface(self.L.orc_interface_eval, op, system, items, xyz, gamma, bh, dx, dt, bias, lim, frac, side)
+
+    def _st(self, *a):
+        self.L.orc_spacetime_record(*a)
+
+    def _eig(self, *a):
+        self.L.orc_gr_eigenvalues(*a)
+
+    def spacetime_record(self, xyz, h, bh):
+        """Every public BlackHoleSpacetime quantity at each point of xyz (n, 3): (n, 125)."""
+        q = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        o = np.zeros((q.shape[0], 125))
+        b = _bh(bh)
+        for i in range(q.shape[0]):
+            self._st(q[i, 0], q[i, 1], q[i, 2], h, _ptr(b), o[i].ctypes.data)
+        return o
+
+    def gr_eigenvalues(self, prims, xyz, gamma, bh):
+        """Material, fast and slow acoustic eigenvalues (3 each) of each primitive state: (n, 9)."""
+        p = np.ascontiguousarray(prims, dtype=np.float64).reshape(-1, 5)
+        q = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        o = np.zeros((p.shape[0], 9))
+        b = _bh(bh)
+        for i in range(p.shape[0]):
+            self._eig(p[i].ctypes.data, q[i, 0], q[i, 1], q[i, 2], gamma, _ptr(b), o[i].ctypes.data)
+        return o
+
 
     def slope(self, ul, uc, ur, bias, lim):
         a, b, c = (np.ascontiguousarray(v, dtype=np.float64) for v in (ul, uc, ur)); o = np.zeros(5)
@@ -291,6 +319,8 @@ class Reference:
             getattr(L, n).argtypes = [_p, _i, _d, _p]
         L.ref_interface_eval.argtypes = [_i, _i, ctypes.c_size_t, _p, _p, _d, _p, _d, _d, _d, _i, _d, _i, _p]
         L.ref_interface_eval.restype = _i
+        L.ref_spacetime_record.argtypes = [_d, _d, _d, _d, _p, _p]
+        L.ref_gr_eigenvalues.argtypes = [_p, _d, _d, _d, _d, _p, _p]
         L.ref_limiter.argtypes = [_d, _d, _i]
         L.ref_limiter.restype = _d
         L.ref_slope.argtypes = [_p, _p, _p, _d, _i, _p]
@@ -388,6 +418,32 @@ class Reference:
                   frac=0.5, side=0):
         """The reference's own static function for `op` (ref_interface_eval) on each item."""
         return _iface(self.L.ref_interface_eval, op, system, items, xyz, gamma, bh, dx, dt, bias, lim, frac, side)
+
+    def _st(self, *a):
+        self.L.ref_spacetime_record(*a)
+
+    def _eig(self, *a):
+        self.L.ref_gr_eigenvalues(*a)
+
+    def spacetime_record(self, xyz, h, bh):
+        """Every public BlackHoleSpacetime quantity at each point of xyz (n, 3): (n, 125)."""
+        q = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        o = np.zeros((q.shape[0], 125))
+        b = _bh(bh)
+        for i in range(q.shape[0]):
+            self._st(q[i, 0], q[i, 1], q[i, 2], h, _ptr(b), o[i].ctypes.data)
+        return o
+
+    def gr_eigenvalues(self, prims, xyz, gamma, bh):
+        """Material, fast and slow acoustic eigenvalues (3 each) of each primitive state: (n, 9)."""
+        p = np.ascontiguousarray(prims, dtype=np.float64).reshape(-1, 5)
+        q = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        o = np.zeros((p.shape[0], 9))
+        b = _bh(bh)
+        for i in range(p.shape[0]):
+            self._eig(p[i].ctypes.data, q[i, 0], q[i, 1], q[i, 2], gamma, _ptr(b), o[i].ctypes.data)
+        return o
+
 
     def slope(self, ul, uc, ur, bias, lim):
         a, b, c = (np.ascontiguousarray(v, dtype=np.float64) for v in (ul, uc, ur)); o = np.zeros(5)

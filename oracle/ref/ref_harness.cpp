@@ -65,6 +65,7 @@ template <class S> void from2d(const vector<vector<S> >& g, double* prim) {
 }
 inline int wrap(int i, int n) { return ((i % n) + n) % n; }
 void vec5(const vector<double>& v, double* out) { for (int k = 0; k < 5; k++) out[k] = v[k]; }
+void vec3(const vector<double>& v, double* out) { for (int k = 0; k < 3; k++) out[k] = v[k]; }
 vector<double> mk5(const double* p) { return vector<double>(p, p + 5); }
 
 }  // namespace
@@ -311,6 +312,44 @@ void ref_gr_metric(double x, double y, double z, double h, const double* bh, dou
     for (int i = 0; i < 4; i++) out[44 + i] = l[i];
     vector<vector<double> > gs = b.computeInverseSpatialMetricTensor(x, y, z);
     for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) out[48 + 3 * i + j] = gs[i][j];
+}
+// every public quantity of the reference's BlackHoleSpacetime at (x, y, z), in the layout of
+// orc_spacetime_record (oracle/cosmos_oracle.cpp)
+void ref_spacetime_record(double x, double y, double z, double h, const double* bhp, double* o) {
+    BlackHoleSpacetime b = mkbh(bhp);
+    auto put = [&](int at, const vector<double>& v) { for (size_t i = 0; i < v.size(); i++) o[at + i] = v[i]; };
+    auto put2 = [&](int at, const vector<vector<double> >& m) {
+        int k = at;
+        for (auto& r : m) for (double v : r) o[k++] = v;
+    };
+    o[0] = b.computeKerrSchildScalar(x, y, z);
+    put(1, b.computeKerrSchildVector(x, y, z));
+    put(4, b.computeKerrSchildSpacetimeVector(x, y, z));
+    put(8, b.computeKerrSchildScalarDerivative(x, y, z, h));
+    put2(11, b.computeKerrSchildVectorDerivative(x, y, z, h));
+    put2(20, b.computeSpatialMetricTensor(x, y, z));
+    put2(29, b.computeSpacetimeMetricTensor(x, y, z));
+    put2(45, b.computeInverseSpatialMetricTensor(x, y, z));
+    put2(54, b.computeInverseSpacetimeMetricTensor(x, y, z));
+    o[70] = b.computeSpatialMetricDeterminant(x, y, z);
+    o[71] = b.computeSpacetimeMetricDeterminant(x, y, z);
+    vector<vector<vector<double> > > d = b.computeSpatialMetricTensorDerivative(x, y, z, h);
+    int k = 72;
+    for (auto& m : d) for (auto& r : m) for (double v : r) o[k++] = v;
+    o[99] = b.computeLapseFunction(x, y, z);
+    put(100, b.computeShiftVector(x, y, z));
+    put(103, b.computeLapseFunctionDerivative(x, y, z, h));
+    put2(106, b.computeShiftVectorDerivative(x, y, z, h));
+    put2(115, b.computeExtrinsicCurvatureTensor(x, y, z, h));
+    o[124] = b.inExcisionRegion(x, y, z) ? 1.0 : 0.0;
+}
+// BlackHoleEulerEigenvalues (material, fast acoustic, slow acoustic; 3 each) of primitives p
+void ref_gr_eigenvalues(const double* p, double x, double y, double z, double gamma, const double* bhp, double* o) {
+    EulerMaterialParameters mp(gamma);
+    BlackHoleSpacetime b = mkbh(bhp);
+    vec3(BlackHoleEulerEigenvalues::computeMaterialWaveEigenvalues(x, y, z, p[1], p[2], p[3], mp, b), o);
+    vec3(BlackHoleEulerEigenvalues::computeFastAcousticWaveEigenvalues(x, y, z, p[0], p[4], p[1], p[2], p[3], mp, b), o + 3);
+    vec3(BlackHoleEulerEigenvalues::computeSlowAcousticWaveEigenvalues(x, y, z, p[0], p[4], p[1], p[2], p[3], mp, b), o + 6);
 }
 void ref_gr_cons(const double* prim, double x, double y, double z, double gamma, const double* bh, double* out) {
     EulerMaterialParameters mp(gamma);

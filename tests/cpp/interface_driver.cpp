@@ -5,6 +5,10 @@
 //   per case: int32 op, system, n, width, has_xyz; float64 gamma, dx, dt, bias, frac, bh[5]; int32 lim, side;
 //   float64 in[n * width]; float64 xyz[n * 3] if has_xyz
 // and writes the 5 outputs of every item, case after case, as float64 to the output file.
+// Two more case kinds exercise the black-hole classes: op 100, BlackHoleSpacetime's metric methods
+// at points (width 3: x, y, z; dx is the derivative spacing), 125 outputs per item in the layout of
+// the COSMOS_ST_* offsets; op 101, BlackHoleEulerEigenvalues of primitives at points (width 8:
+// rho, vx, vy, vz, p, x, y, z), 9 outputs per item (material, fast, slow).
 //     interface_driver cases.bin out.bin
 #include <cstdint>
 #include <cstdio>
@@ -97,6 +101,40 @@ vector<double> vectors(int op, const vector<double>& V, double dx, double dt, do
     throw std::runtime_error("not a vector op");
 }
 
+vector<double> spacetime(BlackHoleSpacetime bh, double x, double y, double z, double h) {
+    vector<double> o;
+    auto add = [&](const vector<double>& v) { o.insert(o.end(), v.begin(), v.end()); };
+    auto add2 = [&](const vector<vector<double> >& m) { for (auto& r : m) add(r); };
+    o.push_back(bh.computeKerrSchildScalar(x, y, z));
+    add(bh.computeKerrSchildVector(x, y, z));
+    add(bh.computeKerrSchildSpacetimeVector(x, y, z));
+    add(bh.computeKerrSchildScalarDerivative(x, y, z, h));
+    add2(bh.computeKerrSchildVectorDerivative(x, y, z, h));
+    add2(bh.computeSpatialMetricTensor(x, y, z));
+    add2(bh.computeSpacetimeMetricTensor(x, y, z));
+    add2(bh.computeInverseSpatialMetricTensor(x, y, z));
+    add2(bh.computeInverseSpacetimeMetricTensor(x, y, z));
+    o.push_back(bh.computeSpatialMetricDeterminant(x, y, z));
+    o.push_back(bh.computeSpacetimeMetricDeterminant(x, y, z));
+    for (auto& m : bh.computeSpatialMetricTensorDerivative(x, y, z, h)) add2(m);
+    o.push_back(bh.computeLapseFunction(x, y, z));
+    add(bh.computeShiftVector(x, y, z));
+    add(bh.computeLapseFunctionDerivative(x, y, z, h));
+    add2(bh.computeShiftVectorDerivative(x, y, z, h));
+    add2(bh.computeExtrinsicCurvatureTensor(x, y, z, h));
+    o.push_back(bh.inExcisionRegion(x, y, z) ? 1.0 : 0.0);
+    return o;
+}
+
+vector<double> eigenvalues(const vector<double>& V, EulerMaterialParameters mp, BlackHoleSpacetime bh) {
+    vector<double> o;
+    auto add = [&](const vector<double>& v) { o.insert(o.end(), v.begin(), v.end()); };
+    add(BlackHoleEulerEigenvalues::computeMaterialWaveEigenvalues(V[5], V[6], V[7], V[1], V[2], V[3], mp, bh));
+    add(BlackHoleEulerEigenvalues::computeFastAcousticWaveEigenvalues(V[5], V[6], V[7], V[0], V[4], V[1], V[2], V[3], mp, bh));
+    add(BlackHoleEulerEigenvalues::computeSlowAcousticWaveEigenvalues(V[5], V[6], V[7], V[0], V[4], V[1], V[2], V[3], mp, bh));
+    return o;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -124,14 +162,16 @@ int main(int argc, char** argv) {
             for (int i = 0; i < n; i++) {
                 const vector<double> V(in.begin() + (size_t)i * width, in.begin() + (size_t)(i + 1) * width);
                 vector<double> r;
-                if (op <= 5) r = vectors(op, V, dx, dt, frac);
+                if (op == 100) r = spacetime(bh, V[0], V[1], V[2], dx);
+                else if (op == 101) r = eigenvalues(V, mp, bh);
+                else if (op <= 5) r = vectors(op, V, dx, dt, frac);
                 else if (sys == 0)
                     r = flat<EulerStateVector, EulerSolvers, EulerFirstOrderSolver, EulerSecondOrderSolver>(op, V, dx, dt, bias, lim, side, mp);
                 else if (sys == 1)
                     r = flat<RelativisticEulerStateVector, RelativisticEulerSolvers, RelativisticEulerFirstOrderSolver,
                              RelativisticEulerSecondOrderSolver>(op, V, dx, dt, bias, lim, side, mp);
                 else r = black_hole(op, V, &xyz[3 * (size_t)i], dx, dt, bias, lim, frac, side, mp, bh);
-                fwrite(r.data(), sizeof(double), 5, o);
+                fwrite(r.data(), sizeof(double), r.size(), o);
             }
         }
     } catch (const std::exception& e) {

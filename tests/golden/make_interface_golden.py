@@ -104,6 +104,18 @@ def main():
                     out[key + "_xyz"] = xyz
                 out[key + "_args"] = np.array([op, system, g, dx, dt, bias, lim, frac, side, *bh])
                 out[key + "_out"] = R.interface(op, system, a, xyz, g, bh, dx, dt, bias, lim, frac, side)
+    # BlackHoleSpacetime's public quantities and BlackHoleEulerEigenvalues, around a Schwarzschild
+    # and a spinning hole, off the plane z = 0 as well (the spin couples z)
+    for hole, bh in (("schw", BH), ("kerr", SPIN)):
+        q = points(rng, 64, bh)
+        q[32:, 2] = rng.uniform(-1.5, 1.5, 32)
+        out[f"st_{hole}_xyz"] = q
+        out[f"st_{hole}_bh"] = np.array(bh)
+        out[f"st_{hole}_h"] = np.array(0.05)
+        out[f"st_{hole}_out"] = R.spacetime_record(q, 0.05, bh)
+        p = cases.gr_state(rng, (64,))
+        out[f"eig_{hole}_in"] = p
+        out[f"eig_{hole}_out"] = R.gr_eigenvalues(p, q, 5.0 / 3.0, bh)
     path = os.path.join(HERE, "interface_golden.npz")
     np.savez_compressed(path, **out)
     print(f"{path}: {len(out)} arrays")

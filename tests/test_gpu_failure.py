@@ -137,8 +137,9 @@ def test_negative_pressure_runs_as_the_reference(cg, oracle):
 
 def test_superluminal_sr_input_runs_as_the_reference(cg, oracle):
     """|v| >= 1 in the primitives: the reference clamps v^2 to 1 - 1e-8 when it forms the conserved
-    state (W = 1e4) and recovers a subluminal state; the FP64 path does the same bit for bit, the
-    FP32 path stays finite and subluminal."""
+    state (W = 1e4), whose primitive recovery then has no physical root; it leaves the density at
+    its 1e-8 floor and superluminal velocities (|v| about 3.5 here) and carries on.  The FP64 path
+    does the same bit for bit; the FP32 path stays finite."""
     rng = np.random.default_rng(6)
     s = cases.sr_state(rng, (40,))
     s[17, 1] = 1.2
@@ -152,8 +153,7 @@ def test_superluminal_sr_input_runs_as_the_reference(cg, oracle):
     g32 = cg.Grid(cg.SR, (40,), 1.0 / 40, 5.0 / 3.0, cg.FP32)
     g32.set_prim(s)
     g32.solve(2, 0.5, 1e9, 0.0, cg.MINBEE, max_steps=3)
-    p = g32.get_prim()
-    assert np.isfinite(p).all() and (np.abs(p[:, 1:4]).max() < 1.0)
+    assert np.isfinite(g32.get_prim()).all()
 
 
 @pytest.mark.parametrize("precision", [0, 1])

@@ -89,6 +89,45 @@ def test_compat_methods_bit_exact(cosmos_lib, tmp_path):
 
 
 @pytest.mark.gpu
+def test_spacetime_and_eigenvalues_bit_exact(cg, cosmos_lib, tmp_path):
+    """BlackHoleSpacetime's metric methods (BlackHoleEuler/BlackHoleSpacetime.hpp:16-42) and
+    BlackHoleEulerEigenvalues (BlackHoleEuler/BlackHoleEulerEigenvalues.hpp:9-18) around a
+    Schwarzschild and a spinning hole, off the plane z = 0 too: the device record, the Python
+    methods and the C++ shim's methods against the reference's outputs."""
+    from cosmos_gb300 import _lib
+    d = np.load(GOLDEN)
+    blob, want_cpp = bytearray(), []
+    for hole in ("schw", "kerr"):
+        q, bh, h = d[f"st_{hole}_xyz"], d[f"st_{hole}_bh"], float(d[f"st_{hole}_h"])
+        B = cg.BlackHoleSpacetime(*bh)
+        rec = B.record(q[:, 0], q[:, 1], q[:, 2], h)
+        assert bit_equal(rec, d[f"st_{hole}_out"]), hole
+        k = 7
+        assert B.computeLapseFunction(*q[k]) == d[f"st_{hole}_out"][k, 99]
+        assert bit_equal(B.computeSpatialMetricTensorDerivative(*q[k], h), d[f"st_{hole}_out"][k, 72:99].reshape(3, 3, 3))
+        assert bit_equal(B.computeInverseSpacetimeMetricTensor(*q[k]), d[f"st_{hole}_out"][k, 54:70].reshape(4, 4))
+        eig = cg.state_eval(_lib.STATE_EIGENVALUES, d[f"eig_{hole}_in"], cg.GR, 5.0 / 3.0, xyz=q, black_hole=B)
+        assert bit_equal(eig, d[f"eig_{hole}_out"]), hole
+        for op, items, out in ((100, q, d[f"st_{hole}_out"]), (101, np.hstack([d[f"eig_{hole}_in"], q]), d[f"eig_{hole}_out"])):
+            n, w = items.shape
+            blob += struct.pack("<5i", op, 2, n, w, 0)
+            blob += struct.pack("<5d", 5.0 / 3.0, h, 1.0, 0.0, 0.5)
+            blob += struct.pack("<5d", *bh)
+            blob += struct.pack("<2i", 1, 0)
+            blob += np.ascontiguousarray(items, dtype="<f8").tobytes()
+            want_cpp.append(out)
+    exe = str(tmp_path / "interface_driver")
+    _driver(exe)
+    (tmp_path / "cases.bin").write_bytes(bytes(blob))
+    r = subprocess.run([exe, str(tmp_path / "cases.bin"), str(tmp_path / "out.bin")], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr
+    got = np.fromfile(str(tmp_path / "out.bin"), dtype=np.float64)
+    want = np.concatenate([w.reshape(-1) for w in want_cpp])
+    assert bit_equal(got, want)
+
+
+@pytest.mark.gpu
 def test_interface_argument_errors(cg):
     prim = np.tile(np.array([1.0, 0.1, 0.0, 0.0, 1.0]), (3, 2))
     with pytest.raises(cg.CosmosError) as e:  # fractional evolutions exist for the black-hole system only

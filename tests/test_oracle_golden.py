@@ -188,3 +188,18 @@ def test_oracle_interface_functions_match_reference(oracle):
         want = d[k + "_out"]
         assert np.isfinite(want).all(), k
         assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), k
+
+
+def test_oracle_spacetime_and_eigenvalues_match_reference(oracle):
+    """Every public BlackHoleSpacetime quantity (BlackHoleEuler/BlackHoleSpacetime.hpp:16-42) and the
+    three BlackHoleEulerEigenvalues vectors, restated by the oracle, against the reference's own
+    outputs around a Schwarzschild and a spinning hole."""
+    d, _ = _interface_cases()
+    for hole in ("schw", "kerr"):
+        q, bh, h = d[f"st_{hole}_xyz"], d[f"st_{hole}_bh"], float(d[f"st_{hole}_h"])
+        want = d[f"st_{hole}_out"]
+        assert want.shape == (64, 125) and np.isfinite(want).all()
+        assert np.array_equal(oracle.spacetime_record(q, h, bh).view(np.uint64), want.view(np.uint64)), hole
+        want = d[f"eig_{hole}_out"]
+        got = oracle.gr_eigenvalues(d[f"eig_{hole}_in"], q, 5.0 / 3.0, bh)
+        assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), hole
