@@ -192,18 +192,11 @@ __global__ void __launch_bounds__(NT, MINB) batch_step_kernel(PolX polx0, PolY p
     if (blockIdx.x == 0 && threadIdx.x == 0) *B.gstep = step0 + nsteps;
 }
 
-// The pair sweeps as the batched kernel calls them (one Y column pair; one X row segment).
+// The Y pair sweep as the batched kernel calls it (one column pair, a run of rows).
 template <int LIM>
 __device__ __forceinline__ float batch_y_pair(const NewtonFastParams& P, int dims, const Geom& G, const float* src,
                                            float* dst, int j, int y0, int y1, bool act, const FastCoef& cf, bool ws) {
     return y_pair_march<LIM>(P, dims, G, src, dst, j, y0, y1, act, cf, ws);
-}
-template <int LIM>
-__device__ __forceinline__ float batch_x_pair(const NewtonFastParams& P, int dims, const Geom& G, const float* src,
-                                           float* dst, int row, int s0, bool act, const FastCoef& cf, bool ws) {
-    Cell2 m;
-    x_pair_load(G, src, row, s0, m);
-    return x_pair_update<LIM>(P, dims, G, dst, row, s0, m, act, cf, ws);
 }
 
 // FP32 batch on cell pairs (sweep_pairs.cuh): X items are whole rows of one grid, dealt to the
@@ -259,9 +252,15 @@ __global__ void __launch_bounds__(NT, MINB) batch_pair_kernel(NewtonFastParams P
                 } else {
                     const int spr = (G.nx + TSW - 1) / TSW;
                     const int total = (it.b - it.a) * spr;
+                    // the warp's next segment is loaded while the current one is computed
+                    Cell2 ahead;
+                    if (warp < total) x_pair_load(G, sg, it.a + warp / spr, (warp % spr) * TSW, ahead);
                     for (int q = warp; q < total; q += W) {  // warp-uniform
                         const int row = it.a + q / spr, s0 = (q % spr) * TSW;
-                        w = fmaxf(w, batch_x_pair<LIM>(P, G.dims, G, sg, dg, row, s0, act, cf, ws));
+                        const Cell2 m = ahead;
+                        const int qn = q + W;
+                        if (qn < total) x_pair_load(G, sg, it.a + qn / spr, (qn % spr) * TSW, ahead);
+                        w = fmaxf(w, x_pair_update<LIM>(P, G.dims, G, dg, row, s0, m, act, cf, ws));
                     }
                 }
                 if (ws && act) block_max_to<NT>(&ctl->smax[ctl->it & 1], w);

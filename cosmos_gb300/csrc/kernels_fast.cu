@@ -11,10 +11,12 @@ constexpr int kXThreads = 256;  // X sweep tile: 256 evolutions, 255 fluxes, 254
 constexpr int kYThreads = 128;
 constexpr int kYSeg = 32;
 constexpr int kXPairThreads = 32;  // one warp per block
-constexpr int kXPairSegs = 2;      // 60-cell segments per warp
-constexpr int kYPairThreads = 64;  // 128 columns per block (two per thread)
+constexpr int kXPairSegs = 3;      // 60-cell segments per warp (4096^2: 0.145 ms against 0.149 with 2)
+constexpr int kYPairThreads = 32;  // one warp (64 columns, two per thread) per block: 0.154 ms at 4096^2
+                                   // against 0.168 with two warps per block at the same registers
 constexpr int kYPairSeg = 32;
 constexpr int kYRingRows = 8;      // Y rows staged in shared memory per warp (up to 8 in flight)
+constexpr int kYRingMinBlocks = 16;  // at most 128 registers: 16 one-warp blocks per SM
 
 template <int AXIS, int LIM, bool MASKED>
 NewtonFastPolicy<AXIS, LIM, MASKED> make_fast(const SweepArgs& a) {
@@ -42,7 +44,7 @@ void run_fast(const SweepArgs& a) {
         else sweep_x_own_kernel<Pol, 1, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
     } else if (a.order == 2 && !MASKED) {
         dim3 grid((G.nx + 2 * kYPairThreads - 1) / (2 * kYPairThreads), (G.ny + kYPairSeg - 1) / kYPairSeg);
-        sweep_y_ring_kernel<LIM, kYPairThreads, kYPairSeg, kYRingRows><<<grid, kYPairThreads, 0, a.stream>>>(
+        sweep_y_ring_kernel<LIM, kYPairThreads, kYPairSeg, kYRingRows, kYRingMinBlocks><<<grid, kYPairThreads, 0, a.stream>>>(
             pol.P, G.dims, G, src, dst, a.ds, a.out);
     } else {
         dim3 grid((G.nx + kYThreads - 1) / kYThreads, (G.ny + kYSeg - 1) / kYSeg);

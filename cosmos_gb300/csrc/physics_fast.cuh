@@ -107,8 +107,9 @@ CG_D V nf_limiter(const NewtonFastParams& P, V r) {
         const V v = vmin(vdiv(vmul(two, r), vadd(one, r)), xi);
         return vsel_lt(r, zero, zero, v);
     }
-    // MinBee: r for 0 <= r < 1, min(1, xi) above (xi > 1 > r whenever r < 1)
-    return vmax(vmin(vmin(r, one), xi), zero);
+    // MinBee: r for 0 <= r <= 1, min(1, xi) = xi above; min(r, xi) is both (xi >= 1 >= r below
+    // r = 1, xi < 1 < r above)
+    return vmax(vmin(r, xi), zero);
 }
 
 // Solvers/SlopeLimiters.cpp:71-101 with the +1e-5 clamps of numerator and denominator
@@ -140,9 +141,9 @@ CG_D void nf_recon(const NewtonFastParams& P, const V* ul, const V* um, const V*
     nf_flux<AXIS>(P, b, Fb);
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-        const V ev = vmul(splat_v<V>(half_dtdx), vsub(Fa[k], Fb[k]));
-        fl[k] = vadd(a[k], ev);
-        fr[k] = vadd(b[k], ev);
+        const V d = vsub(Fa[k], Fb[k]);
+        fl[k] = vfma(splat_v<V>(half_dtdx), d, a[k]);
+        fr[k] = vfma(splat_v<V>(half_dtdx), d, b[k]);
     }
 }
 
@@ -162,6 +163,28 @@ CG_D void nf_force(const NewtonFastParams& P, const V* L, const V* R, float half
         F[k] = vfma(splat_v<V>(0.25f), vadd(fL[k], fR[k]),
                     vfma(splat_v<V>(q_dxdt), vsub(L[k], R[k]), vmul(splat_v<V>(0.5f), fs[k])));
 }
+
+// Four times the FORCE flux, from the flux's homogeneity F(2u) = 2 F(u) (exact in floating point:
+// doubling is exact): 4F = (fL + fR) + (dx/dt)(L - R) + F((L + R) + (dt/dx)(fL - fR)) -- two
+// operations per field fewer than nf_force.  Callers update with nf_update and dt/(4 dx).
+template <int AXIS, class V>
+CG_D void nf_force4(const NewtonFastParams& P, const V* L, const V* R, float dtdx, float dxdt, V* F4) {
+    V fL[5], fR[5], us[5], fs[5];
+    nf_flux<AXIS>(P, L, fL);
+    nf_flux<AXIS>(P, R, fR);
+#pragma unroll
+    for (int k = 0; k < 5; k++) us[k] = vfma(splat_v<V>(dtdx), vsub(fL[k], fR[k]), vadd(L[k], R[k]));
+    nf_flux<AXIS>(P, us, fs);
+#pragma unroll
+    for (int k = 0; k < 5; k++) F4[k] = vfma(splat_v<V>(dxdt), vsub(L[k], R[k]), vadd(vadd(fL[k], fR[k]), fs[k]));
+}
+
+// The coefficients nf_force4 and its update take: dt/dx, dx/dt, dt/(4 dx) (exact scalings of the
+// step's FP32 coefficients), and 0.5 dt/dx for the half-step evolution.
+struct Force4Coef {
+    float half_dtdx, dtdx, dxdt, q_dtdx;
+};
+CG_D Force4Coef force4_coef(const FastCoef& c) { return Force4Coef{c.half_dtdx, c.dtdx, 4.0f * c.q_dxdt, 0.25f * c.dtdx}; }
 
 // Conservative update U + (dt/dx)(F_left - F_right)
 template <class V>

@@ -1,7 +1,7 @@
 // FP32 Newtonian sweeps on cell pairs: every thread carries two cells through Blackwell's paired
 // FP32 instructions (FFMA2 / FADD2 / FMUL2) and moves them with 8-byte loads and stores.  The
-// arithmetic is physics_fast.cuh's, instantiated on the pair type, so the results equal the
-// one-cell kernels' bit for bit.
+// arithmetic is physics_fast.cuh's, instantiated on the pair type; the FORCE flux is taken as four
+// times itself (nf_force4), so the results agree with the one-cell kernels' to FP32 rounding.
 #pragma once
 #include "physics_fast.cuh"
 #include "sweep_kernels.cuh"
@@ -55,6 +55,7 @@ CG_D float y_pair_march(const NewtonFastParams& P, int dims, const Geom& G, cons
         }
         return w;
     }
+    const Force4Coef c4 = force4_coef(cf);
     Cell2 cm2, cm1, c0, c1, c2, ahead;
     ld(y0 - 2, cm2);
     ld(y0 - 1, cm1);
@@ -64,16 +65,16 @@ CG_D float y_pair_march(const NewtonFastParams& P, int dims, const Geom& G, cons
     f2 Lm1[5], Rm1[5], L0[5], R0[5], Fp[5], Fn[5];
     nf_recon<1, LIM>(P, cm2.v, cm1.v, c0.v, cf.half_dtdx, Lm1, Rm1);
     nf_recon<1, LIM>(P, cm1.v, c0.v, c1.v, cf.half_dtdx, L0, R0);
-    nf_force<1>(P, Rm1, L0, cf.half_dtdx, cf.q_dxdt, Fp);
+    nf_force4<1>(P, Rm1, L0, c4.dtdx, c4.dxdt, Fp);
     for (int y = y0; y < y1; y++) {
         // the next row is loaded one iteration ahead, so its latency overlaps this row's work
         c2 = ahead;
         if (y + 1 < y1) ld(y + 3, ahead);
         f2 L1[5], R1[5];
         nf_recon<1, LIM>(P, c0.v, c1.v, c2.v, cf.half_dtdx, L1, R1);
-        nf_force<1>(P, R0, L1, cf.half_dtdx, cf.q_dxdt, Fn);
+        nf_force4<1>(P, R0, L1, c4.dtdx, c4.dxdt, Fn);
         Cell2 nc;
-        nf_update(cf.dtdx, c0.v, Fp, Fn, nc.v);
+        nf_update(c4.q_dtdx, c0.v, Fp, Fn, nc.v);
         st(y, nc);
         if (want_w) {
             const f2 ws = nf_wavespeed(P, nc.v, dims);
@@ -137,10 +138,11 @@ CG_D float x_pair_update(const NewtonFastParams& P, int dims, const Geom& G, flo
 #pragma unroll
         for (int f = 0; f < 5; f++) Rn[f].v = make_float2(L[f].v.y, __shfl_down_sync(FULL, L[f].v.x, 1));
         f2 Fr[5], Fl[5];
-        nf_force<0>(P, R, Rn, cf.half_dtdx, cf.q_dxdt, Fr);
+        const Force4Coef c4 = force4_coef(cf);
+        nf_force4<0>(P, R, Rn, c4.dtdx, c4.dxdt, Fr);
 #pragma unroll
         for (int f = 0; f < 5; f++) Fl[f].v = make_float2(__shfl_up_sync(FULL, Fr[f].v.y, 1), Fr[f].v.x);
-        nf_update(cf.dtdx, m.v, Fl, Fr, nc.v);
+        nf_update(c4.q_dtdx, m.v, Fl, Fr, nc.v);
     }
     float w = 0.0f;
     if (lane >= 1 && lane <= 30 && p0 < n) {
@@ -169,8 +171,8 @@ CG_D float x_pair_update(const NewtonFastParams& P, int dims, const Geom& G, flo
 // each reduces its own CFL maximum.  The arithmetic is y_pair_march's.  A wait that runs out
 // (about a second) sets ST_TIMEOUT in the status word; the warp then waits, again bounded, for its
 // rows still in flight and leaves.
-template <int LIM, int NT, int SEG, int R>
-__global__ void __launch_bounds__(NT) sweep_y_ring_kernel(NewtonFastParams P, int dims, Geom G,
+template <int LIM, int NT, int SEG, int R, int MINB>
+__global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams P, int dims, Geom G,
                                                           const float* __restrict__ src, float* __restrict__ dst,
                                                           DtSrc ds, SweepOut out) {
     static_assert(R >= 5 && (R & (R - 1)) == 0, "a power of two above the four prologue rows");
@@ -202,6 +204,7 @@ __global__ void __launch_bounds__(NT) sweep_y_ring_kernel(NewtonFastParams P, in
         return;
     }
     const FastCoef cf = s_coef;
+    const Force4Coef c4 = force4_coef(cf);
     const uint32_t bytes = ((uint32_t)min(64, G.nx - jw) * 4u + 15u) & ~15u;  // within the padded pitch
     // Row r of the ring lives in slot (r - ylo) mod R; the slot's k-th use completes phase k mod 2.
     // Lanes 0-4 each copy one field (lane 5+ hold a valid pointer they never use).
@@ -247,7 +250,7 @@ __global__ void __launch_bounds__(NT) sweep_y_ring_kernel(NewtonFastParams P, in
         f2 Lm1[5], Rm1[5], L0[5], R0[5], Fp[5], Fn[5];
         nf_recon<1, LIM>(P, cm2.v, cm1.v, c0.v, cf.half_dtdx, Lm1, Rm1);
         nf_recon<1, LIM>(P, cm1.v, c0.v, c1.v, cf.half_dtdx, L0, R0);
-        nf_force<1>(P, Rm1, L0, cf.half_dtdx, cf.q_dxdt, Fp);
+        nf_force4<1>(P, Rm1, L0, c4.dtdx, c4.dxdt, Fp);
         for (int y = y0; y < y1; y++) {
             take(c2);
             ok = __all_sync(FULL, ok);
@@ -257,9 +260,9 @@ __global__ void __launch_bounds__(NT) sweep_y_ring_kernel(NewtonFastParams P, in
             if (inext <= yhi) issue_one();
             f2 L1[5], R1[5];
             nf_recon<1, LIM>(P, c0.v, c1.v, c2.v, cf.half_dtdx, L1, R1);
-            nf_force<1>(P, R0, L1, cf.half_dtdx, cf.q_dxdt, Fn);
+            nf_force4<1>(P, R0, L1, c4.dtdx, c4.dxdt, Fn);
             Cell2 nc;
-            nf_update(cf.dtdx, c0.v, Fp, Fn, nc.v);
+            nf_update(c4.q_dtdx, c0.v, Fp, Fn, nc.v);
             if (live) {
                 const size_t b = (size_t)y * G.pitch + j;
 #pragma unroll
