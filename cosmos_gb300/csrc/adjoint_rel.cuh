@@ -63,14 +63,61 @@ RADJ_HD D5 operator*(const D5& a, const D5& b) {
     for (int i = 0; i < 5; i++) r.d[i] = (a.d[i] * b.v) + (a.v * b.d[i]);
     return r;
 }
+// The value part of a quotient is the IEEE quotient (the forward's arithmetic); the tangents take
+// one reciprocal instead of five divisions (an FP64 division is a long instruction sequence).
 RADJ_HD D5 operator/(const D5& a, const D5& b) {
     D5 r(a.v / b.v);
-    for (int i = 0; i < 5; i++) r.d[i] = (a.d[i] - (r.v * b.d[i])) / b.v;
+    const double ib = 1.0 / b.v;
+    for (int i = 0; i < 5; i++) r.d[i] = (a.d[i] - (r.v * b.d[i])) * ib;
     return r;
 }
 RADJ_HD D5 sqrt(const D5& a) {
     D5 r(::sqrt(a.v));
-    for (int i = 0; i < 5; i++) r.d[i] = a.d[i] / (2.0 * r.v);
+    const double ih = 1.0 / (2.0 * r.v);
+    for (int i = 0; i < 5; i++) r.d[i] = a.d[i] * ih;
+    return r;
+}
+// A constant operand (no tangents): the product and sum of the dual forms without the zero lanes.
+RADJ_HD D5 operator*(double a, const D5& b) {
+    D5 r(a * b.v);
+    for (int i = 0; i < 5; i++) r.d[i] = a * b.d[i];
+    return r;
+}
+RADJ_HD D5 operator*(const D5& a, double b) {
+    D5 r(a.v * b);
+    for (int i = 0; i < 5; i++) r.d[i] = a.d[i] * b;
+    return r;
+}
+RADJ_HD D5 operator+(double a, const D5& b) {
+    D5 r(a + b.v);
+    for (int i = 0; i < 5; i++) r.d[i] = b.d[i];
+    return r;
+}
+RADJ_HD D5 operator+(const D5& a, double b) {
+    D5 r(a.v + b);
+    for (int i = 0; i < 5; i++) r.d[i] = a.d[i];
+    return r;
+}
+RADJ_HD D5 operator-(const D5& a, double b) {
+    D5 r(a.v - b);
+    for (int i = 0; i < 5; i++) r.d[i] = a.d[i];
+    return r;
+}
+RADJ_HD D5 operator-(double a, const D5& b) {
+    D5 r(a - b.v);
+    for (int i = 0; i < 5; i++) r.d[i] = -b.d[i];
+    return r;
+}
+RADJ_HD D5 operator/(double a, const D5& b) {
+    D5 r(a / b.v);
+    const double ib = 1.0 / b.v;
+    for (int i = 0; i < 5; i++) r.d[i] = -(r.v * b.d[i]) * ib;
+    return r;
+}
+RADJ_HD D5 operator/(const D5& a, double b) {
+    D5 r(a.v / b);
+    const double ib = 1.0 / b;
+    for (int i = 0; i < 5; i++) r.d[i] = a.d[i] * ib;
     return r;
 }
 RADJ_HD D5 fabs(const D5& a) { return a.v < 0.0 ? -a : a; }
@@ -80,20 +127,20 @@ RADJ_HD bool operator>(const D5& a, const D5& b) { return a.v > b.v; }
 RADJ_HD D5 mn(const D5& a, const D5& b) { return (b < a) ? b : a; }
 
 // ---- slope limiters, Solvers/SlopeLimiters.cpp:3-101 (0 = SuperBee, 1 = van Leer, else MinBee)
-RADJ_HD D5 gradient_ratio(const D5& r, double w) { return D5(2.0) / (D5(1.0 - w) + (D5(1.0 + w) * r)); }
+RADJ_HD D5 gradient_ratio(const D5& r, double w) { return 2.0 / ((1.0 - w) + ((1.0 + w) * r)); }
 RADJ_HD D5 limiter(const D5& r, double w, int lim) {
     if (r < D5(0.0)) return D5(0.0);
     if (lim == 0) {
-        if (r < D5(0.5)) return D5(2.0) * r;
+        if (r < D5(0.5)) return 2.0 * r;
         if (r < D5(1.0)) return D5(1.0);
         return mn(mn(r, gradient_ratio(r, w)), D5(2.0));
     }
-    if (lim == 1) return mn((D5(2.0) * r) / (D5(1.0) + r), gradient_ratio(r, w));
+    if (lim == 1) return mn((2.0 * r) / (1.0 + r), gradient_ratio(r, w));
     if (r < D5(1.0)) return r;
     return mn(D5(1.0), gradient_ratio(r, w));
 }
 RADJ_HD void slope_vector(const D5* ul, const D5* uc, const D5* ur, double w, int lim, D5* s) {
-    const D5 a = D5(0.5 * (1.0 + w)), b = D5(0.5 * (1.0 - w));
+    const double a = 0.5 * (1.0 + w), b = 0.5 * (1.0 - w);
     for (int k = 0; k < 5; k++) {
         const D5 dl = uc[k] - ul[k], dr = ur[k] - uc[k];
         s[k] = (a * dl) + (b * dr);
@@ -113,31 +160,30 @@ RADJ_HD Prim con2prim(const D5* u, double g, double tol) {
     const D5 q = ((tau + D) * (tau + D)) - (((Sx * Sx) + (Sy * Sy)) + (Sz * Sz));
     D5 dc, ec;
     if (q < D5(1e-8)) {
-        dc = D / D5(::sqrt(1e-8));
-        ec = (D + tau) / D5(::sqrt(1e-8));
+        dc = D / ::sqrt(1e-8);
+        ec = (D + tau) / ::sqrt(1e-8);
     } else {
         dc = D / sqrt(q);
         ec = (D + tau) / sqrt(q);
     }
     const double gm = (g - 1.0) / g;
     const D5 cst = D5(-1.0 / (g * g));
-    const D5 lin = (D5(-2.0) * dc) * D5((g - 1.0) / (g * g));
-    const D5 quad = ((D5((g - 2.0) / g) * ((ec * ec) - D5(1.0))) + D5(1.0)) - (((dc * dc) * D5(gm)) * D5(gm));
-    const D5 quart = (ec * ec) - D5(1.0);
-    const D5 eta = (D5(2.0) * dc) * D5(gm);
+    const D5 lin = (-2.0 * dc) * ((g - 1.0) / (g * g));
+    const D5 quad = ((((g - 2.0) / g) * ((ec * ec) - 1.0)) + 1.0) - (((dc * dc) * gm) * gm);
+    const D5 quart = (ec * ec) - 1.0;
+    const D5 eta = (2.0 * dc) * gm;
     D5 x = D5(1.0);
     for (int it = 0; it < 1000; it++) {
         const D5 f = ((((quart * ((x * x) * x)) * (x - eta)) + (quad * (x * x))) + (lin * x)) + cst;
-        const D5 fp = ((lin + ((D5(2.0) * quad) * x)) + ((D5(4.0) * quart) * ((x * x) * x))) -
-                      (((D5(3.0) * eta) * quart) * (x * x));
+        const D5 fp = ((lin + ((2.0 * quad) * x)) + ((4.0 * quart) * ((x * x) * x))) -
+                      (((3.0 * eta) * quart) * (x * x));
         const D5 nx = x - (f / fp);
         if (fabs(x - nx) < D5(tol)) break;
         x = nx;
     }
     Prim r;
-    r.W = ((D5(0.5) * ec) * x) *
-          (D5(1.0) + sqrt(D5(1.0) + ((D5(4.0) * D5(gm)) * ((D5(1.0) - (dc * x)) / ((ec * ec) * (x * x))))));
-    r.h = D5(1.0) / (dc * x);
+    r.W = ((0.5 * ec) * x) * (1.0 + sqrt(1.0 + ((4.0 * gm) * ((1.0 - (dc * x)) / ((ec * ec) * (x * x))))));
+    r.h = 1.0 / (dc * x);
     r.rho = D / r.W;
     const D5 rhw = (r.rho * r.h) * (r.W * r.W);
     r.vx = Sx / rhw;
@@ -149,7 +195,7 @@ RADJ_HD Prim con2prim(const D5* u, double g, double tol) {
     return r;
 }
 // RelativisticEulerEquationOfState.cpp:3-8
-RADJ_HD D5 enthalpy(const D5& rho, const D5& p, double g) { return D5(1.0) + ((p / rho) * D5(g / (g - 1.0))); }
+RADJ_HD D5 enthalpy(const D5& rho, const D5& p, double g) { return 1.0 + ((p / rho) * (g / (g - 1.0))); }
 
 struct Pt { double x, y, z; };
 RADJ_HD Pt shift(Pt p, int axis, double d) {
@@ -165,7 +211,7 @@ struct SRSys {
     RADJ_HD void cons(const D5* p, Pt, D5* u) const {
         const D5 v2 = ((p[1] * p[1]) + (p[2] * p[2])) + (p[3] * p[3]);
         D5 W = D5(1.0 / ::sqrt(1.0 - 1e-8));
-        if (!(v2 > D5(1.0 - 1e-8))) W = D5(1.0) / sqrt(D5(1.0) - v2);
+        if (!(v2 > D5(1.0 - 1e-8))) W = 1.0 / sqrt(1.0 - v2);
         const D5 rhw = (p[0] * enthalpy(p[0], p[4], g)) * (W * W);
         u[0] = p[0] * W;
         u[1] = rhw * p[1];
@@ -301,17 +347,17 @@ struct GRSys {
         const double sg = ::sqrt(KerrSchild::det3(m));
         D5 v2 = D5(0.0);
         for (int i = 0; i < 3; i++)
-            for (int j = 0; j < 3; j++) v2 = v2 + ((D5(m[3 * i + j]) * p[1 + i]) * p[1 + j]);
+            for (int j = 0; j < 3; j++) v2 = v2 + ((m[3 * i + j] * p[1 + i]) * p[1 + j]);
         D5 W = D5(1.0 / ::sqrt(1.0 - 1e-8));
-        if (!(v2 > D5(1.0 - 1e-8))) W = D5(1.0) / sqrt(D5(1.0) - v2);
+        if (!(v2 > D5(1.0 - 1e-8))) W = 1.0 / sqrt(1.0 - v2);
         const D5 hh = enthalpy(p[0], p[4], g);
-        const D5 sr = D5(sg) * p[0];
+        const D5 sr = sg * p[0];
         u[0] = sr * W;
         for (int k = 0; k < 3; k++) u[1 + k] = ((sr * hh) * (W * W)) * p[1 + k];
-        u[4] = D5(sg) * ((((p[0] * hh) * W) - p[4]) - (p[0] * W));
+        u[4] = sg * ((((p[0] * hh) * W) - p[4]) - (p[0] * W));
     }
     RADJ_HD Prim c2p(const D5* u, Pt q, double tol) const {
-        const D5 sg = D5(bh.sqrt_det(q));
+        const double sg = bh.sqrt_det(q);
         const D5 us[5] = {u[0] / sg, u[1] / sg, u[2] / sg, u[3] / sg, u[4] / sg};
         return con2prim(us, g, tol);
     }
@@ -324,10 +370,10 @@ struct GRSys {
         double al, be[3];
         bh.lapse_shift(q, al, be);
         const Prim c = c2p(u, q, axis == 0 ? 1e-10 : 1e-8);
-        const D5 as = D5(al * sg);
+        const double as = al * sg;
         const D5 rhw = (c.rho * c.h) * (c.W * c.W);
         const D5 vn = axis == 0 ? c.vx : c.vy;
-        const D5 w = vn - D5(be[axis] / al);
+        const D5 w = vn - (be[axis] / al);
         f[0] = as * ((c.rho * c.W) * w);
         f[1] = as * ((rhw * (c.vx * w)) + (axis == 0 ? c.p : D5(0.0)));
         f[2] = as * ((rhw * (c.vy * w)) + (axis == 1 ? c.p : D5(0.0)));
@@ -370,7 +416,7 @@ struct GRSys {
         const double dg = KerrSchild::det3(gm);
         double al, be[3];
         bh.lapse_shift(q, al, be);
-        const D5 sg = D5(::sqrt(dg));
+        const double sg = ::sqrt(dg);
         const D5 us[5] = {u[0] / sg, u[1] / sg, u[2] / sg, u[3] / sg, u[4] / sg};
         const Prim c = con2prim(us, g, 1e-8);
         double g4m[16], gi[16], da[3], db[9], dgm[27], K[9];
@@ -390,40 +436,40 @@ struct GRSys {
         }
         Kij(q, al, K);
         D5 uu[4];
-        uu[0] = c.W / D5(al);
-        uu[1] = ((D5(al) * uu[0]) * c.vx) - (D5(be[0]) * uu[0]);
-        uu[2] = ((D5(al) * uu[0]) * c.vy) - (D5(be[1]) * uu[0]);
-        uu[3] = ((D5(al) * uu[0]) * c.vz) - (D5(be[2]) * uu[0]);
+        uu[0] = c.W / al;
+        uu[1] = ((al * uu[0]) * c.vx) - (be[0] * uu[0]);
+        uu[2] = ((al * uu[0]) * c.vy) - (be[1] * uu[0]);
+        uu[3] = ((al * uu[0]) * c.vz) - (be[2] * uu[0]);
         D5 T[16];
         for (int i = 0; i < 4; i++)
-            for (int j = 0; j < 4; j++) T[4 * i + j] = (((c.rho * c.h) * uu[i]) * uu[j]) + (c.p * D5(gi[4 * i + j]));
+            for (int j = 0; j < 4; j++) T[4 * i + j] = (((c.rho * c.h) * uu[i]) * uu[j]) + (c.p * gi[4 * i + j]);
         D5 S[5];
         D5 vc[3];
         for (int i = 0; i < 3; i++)
-            vc[i] = ((D5(gm[3 * i + 0]) * c.vx) + (D5(gm[3 * i + 1]) * c.vy)) + (D5(gm[3 * i + 2]) * c.vz);
+            vc[i] = ((gm[3 * i + 0] * c.vx) + (gm[3 * i + 1] * c.vy)) + (gm[3 * i + 2] * c.vz);
         const D5 rhw = (c.rho * c.h) * (c.W * c.W);
         for (int i = 0; i < 3; i++) {
             for (int j = 0; j < 3; j++) {
                 for (int k = 0; k < 3; k++) {
                     const double dgijk = dgm[9 * i + 3 * j + k];
-                    S[i + 1] = S[i + 1] + (T[0] * D5(((0.5 * be[j]) * be[k]) * dgijk));
-                    S[i + 1] = S[i + 1] + ((T[j + 1] * D5(be[k])) * D5(dgijk));
-                    S[i + 1] = S[i + 1] + (D5(0.5) * (T[4 * (j + 1) + (k + 1)] * D5(dgijk)));
+                    S[i + 1] = S[i + 1] + (T[0] * (((0.5 * be[j]) * be[k]) * dgijk));
+                    S[i + 1] = S[i + 1] + ((T[j + 1] * be[k]) * dgijk);
+                    S[i + 1] = S[i + 1] + (0.5 * (T[4 * (j + 1) + (k + 1)] * dgijk));
                 }
-                S[i + 1] = S[i + 1] + (((rhw * vc[j]) / D5(al)) * D5(db[3 * i + j]));
+                S[i + 1] = S[i + 1] + (((rhw * vc[j]) / al) * db[3 * i + j]);
             }
-            S[i + 1] = S[i + 1] - ((T[0] * D5(al)) * D5(da[i]));
+            S[i + 1] = S[i + 1] - ((T[0] * al) * da[i]);
         }
         for (int i = 0; i < 3; i++) {
             for (int j = 0; j < 3; j++) {
-                S[4] = S[4] + (T[0] * D5((be[i] * be[j]) * K[3 * i + j]));
-                S[4] = S[4] + (T[i + 1] * D5((2.0 * be[j]) * K[3 * i + j]));
-                S[4] = S[4] + (T[4 * (i + 1) + (j + 1)] * D5(K[3 * i + j]));
+                S[4] = S[4] + (T[0] * ((be[i] * be[j]) * K[3 * i + j]));
+                S[4] = S[4] + (T[i + 1] * ((2.0 * be[j]) * K[3 * i + j]));
+                S[4] = S[4] + (T[4 * (i + 1) + (j + 1)] * K[3 * i + j]);
             }
-            S[4] = S[4] - (T[0] * D5(be[i] * da[i]));
-            S[4] = S[4] - (T[i + 1] * D5(da[i]));
+            S[4] = S[4] - (T[0] * (be[i] * da[i]));
+            S[4] = S[4] - (T[i + 1] * da[i]);
         }
-        const D5 f = D5(al * ::sqrt(dg));
+        const double f = al * ::sqrt(dg);
         for (int k = 0; k < 5; k++) s[k] = f * S[k];
     }
     // Cell k of line L is updated unless a cell of its stencil (two cells out along the line in
@@ -461,13 +507,13 @@ RADJ_HD void evolve(const Sys& S, const Step& s, const D5* l, const D5* m, const
     slope_vector(ul, um, ur, s.w, s.lim, sl);
     D5 UL[5], UR[5], FL[5], FR[5];
     for (int k = 0; k < 5; k++) {
-        UL[k] = um[k] - (D5(0.5) * sl[k]);
-        UR[k] = um[k] + (D5(0.5) * sl[k]);
+        UL[k] = um[k] - (0.5 * sl[k]);
+        UR[k] = um[k] + (0.5 * sl[k]);
     }
     const Pt pl = shift(xc, s.axis, -(s.dx * 0.5)), pr = shift(xc, s.axis, s.dx * 0.5);
     S.flux(UL, s.axis, pl, FL);
     S.flux(UR, s.axis, pr, FR);
-    const D5 hs = D5(0.5 * (s.dt / s.dx));
+    const double hs = 0.5 * (s.dt / s.dx);
     D5 a[5], b[5];
     for (int k = 0; k < 5; k++) {
         const D5 ev = hs * (FL[k] - FR[k]);
@@ -487,10 +533,10 @@ template <class Sys> RADJ_HD void force(const Sys& S, const Step& s, const D5* L
     S.cons(R, pr, uR);
     S.flux(uL, s.axis, pl, fL);
     S.flux(uR, s.axis, pr, fR);
-    const D5 c = D5(s.dx / s.dt), d = D5(s.dt / s.dx);
-    for (int k = 0; k < 5; k++) us[k] = D5(0.5) * ((uL[k] + uR[k]) + (d * (fL[k] - fR[k])));
+    const double c = s.dx / s.dt, d = s.dt / s.dx;
+    for (int k = 0; k < 5; k++) us[k] = 0.5 * ((uL[k] + uR[k]) + (d * (fL[k] - fR[k])));
     S.flux(us, s.axis, xf, fs);
-    for (int k = 0; k < 5; k++) F[k] = D5(0.5) * ((D5(0.5) * ((fL[k] + fR[k]) + (c * (uL[k] - uR[k])))) + fs[k]);
+    for (int k = 0; k < 5; k++) F[k] = 0.5 * ((0.5 * ((fL[k] + fR[k]) + (c * (uL[k] - uR[k])))) + fs[k]);
 }
 
 // Position k of a line of n cells that a stencil position reads: transmissive mirror
@@ -597,7 +643,7 @@ template <class Sys> RADJ_HD void cell_adjoint_sys(const Sys& S, const Params& P
         const Pt ck = cell_pt(cell);
         D5 u[5], nu[5], o[5];
         S.cons(at(k), ck, u);
-        const D5 d = D5(P.s.dt / dx);
+        const double d = P.s.dt / dx;
         for (int f = 0; f < 5; f++) nu[f] = u[f] + (d * (F[k - kmin][f] - F[k + 1 - kmin][f]));
         S.prim(nu, ck, o);
         for (int f = 0; f < 5; f++) {
@@ -621,12 +667,12 @@ RADJ_HD void evolve_fraction(const GRSys& S, double frac, const D5* l, const D5*
     slope_vector(ul, um, ur, w, lim, sl);
     D5 UL[5], UR[5], FL[5], FR[5];
     for (int k = 0; k < 5; k++) {
-        UL[k] = um[k] - (D5(0.5) * sl[k]);
-        UR[k] = um[k] + (D5(0.5) * sl[k]);
+        UL[k] = um[k] - (0.5 * sl[k]);
+        UR[k] = um[k] + (0.5 * sl[k]);
     }
     S.flux(UL, axis, shift(xc, axis, -dx), FL);
     S.flux(UR, axis, shift(xc, axis, dx), FR);
-    const D5 s = D5(frac * (dt / dx));
+    const double s = frac * (dt / dx);
     D5 nu[5];
     for (int k = 0; k < 5; k++) nu[k] = um[k] + (s * (FL[k] - FR[k]));
     S.prim(nu, xc, out);
@@ -642,11 +688,11 @@ RADJ_HD void rk_cell(const GRSys& S, int dims, const D5* cl, const D5* cm, const
     }
     D5 k[4][5], st[5], c[5], sv[5];
     S.source(cm, q, sv);
-    for (int i = 0; i < 5; i++) k[0][i] = D5(dt) * sv[i];
+    for (int i = 0; i < 5; i++) k[0][i] = dt * sv[i];
     const double fx1[3] = {0.5, 0.5, 1.0};                               // 1D fractions
     const double fx2[3] = {0.25, 0.25, 0.5}, fy2[3] = {0.5, 0.5, 1.0};  // 2D fractions
     for (int stage = 0; stage < 3; stage++) {
-        for (int i = 0; i < 5; i++) st[i] = stage < 2 ? (cm[i] + (D5(0.5) * k[stage][i])) : (cm[i] + k[stage][i]);
+        for (int i = 0; i < 5; i++) st[i] = stage < 2 ? (cm[i] + (0.5 * k[stage][i])) : (cm[i] + k[stage][i]);
         S.prim(st, q, Mp);
         if (dims == 1) {
             evolve_fraction(S, fx1[stage], L, Mp, R, q, 0, dx, dt, w, lim, E);
@@ -657,10 +703,10 @@ RADJ_HD void rk_cell(const GRSys& S, int dims, const D5* cl, const D5* cm, const
         }
         S.cons(E, q, c);
         S.source(c, q, sv);
-        for (int i = 0; i < 5; i++) k[stage + 1][i] = D5(dt) * sv[i];
+        for (int i = 0; i < 5; i++) k[stage + 1][i] = dt * sv[i];
     }
     for (int i = 0; i < 5; i++)
-        out_cons[i] = cm[i] + (D5(1.0 / 6.0) * (k[0][i] + ((D5(2.0) * k[1][i]) + ((D5(2.0) * k[2][i]) + k[3][i]))));
+        out_cons[i] = cm[i] + ((1.0 / 6.0) * (k[0][i] + ((2.0 * k[1][i]) + ((2.0 * k[2][i]) + k[3][i]))));
 }
 
 // The input adjoint of cell c = i * nx + j for one RK source step (time step P.s.dt, slopes P.s.w and
