@@ -392,7 +392,7 @@ def run_ours(args):
                 "h2d_gbs": nbytes / (up / args.steps * 1e-3) / 1e9, "d2h_gbs": nbytes / (dn / args.steps * 1e-3) / 1e9,
                 "what": "per step: pinned host AoS FP64 primitives -> device (copy + conversion to FP32 conserved), "
                         "one Strang step, state -> the same host buffer, which the next step reads"},
-        "roofline": {"bound": "hbm", "kernel": "sweep_x_pair_kernel (X sweep, FP32 cell pairs)",
+        "roofline": {"bound": "hbm", "kernel": "sweep_x_ring_kernel (X sweep, FP32 cell pairs staged by bulk copies)",
                      "achieved": x_gbs, "peak": peak, "unit": "GB/s", "frac": x_gbs / peak,
                      "peak_source": peak_kind, "traffic": traffic_per_launch("sweep_x_fp32"),
                      "algorithmic_bytes_per_launch": bytes_sweep, "ms_per_launch": kx,
@@ -428,7 +428,7 @@ def all_configs(cg, L, ctx, stream, args):
     return out
 
 
-# ---------------------------------------------------------------- configuration 1: Sod, FP64
+# ---------------------------------------------------------------- Sod shock tube, 1000 cells, FP64
 SOD_WORKLOAD = "1D Newtonian Euler Sod shock tube, SLIC van Leer, FP64, 1000 cells on [0,1], gamma 1.4, CFL 0.9, " \
                "transmissive, t = 0.25"
 # The reference's own run of this problem (built from its sources): 613 steps, rho[500] at t = 0.25.
@@ -454,7 +454,7 @@ def measure_sod(cg, ctx, stream):
             "note": "1000 cells: launch-bound (one host round trip per solve, 613 graph-replayed steps)"}
 
 
-# ---------------------------------------------------------------- configuration 2 at full length
+# ---------------------------------------------------------------- the 4096^2 grid at full length
 def measure_grid_parity(cg, ctx, stream, n, steps):
     """The headline workload run `steps` steps in FP32 and in the FP64 (reference-exact) path, each
     with its own CFL time steps: the FP64 path's rate, the FP32-vs-FP64 relative L1 density error,
@@ -485,14 +485,14 @@ def measure_grid_parity(cg, ctx, stream, n, steps):
     return out
 
 
-# ---------------------------------------------------------------- configuration 3: SR Kelvin-Helmholtz
+# ---------------------------------------------------------------- SR Kelvin-Helmholtz, 2048^2
 SR_WORKLOAD = "2D special-relativistic Euler (gamma 5/3), SLIC MinBee, CFL 0.9, 2048x2048 on the periodic " \
               "unit square, Kelvin-Helmholtz shear layers (vx = +-0.5 tanh profile, rho in {1, 2}, p = 1, " \
               "vy = 0.01 sin(4 pi x + phase), phase seed 3; Lorentz factor <= 1.16); 200 steps"
 
 
 def measure_sr(cg, L, ctx, stream, n, steps, warmup):
-    """Configuration 3 as stated (FP32 bulk, every primitive recovery's Newton iterations finished
+    """The SR Kelvin-Helmholtz workload as stated (FP32 bulk, every primitive recovery's Newton iterations finished
     in FP64), the FP32-Newton variant (FP64 stage only above a Lorentz factor of 2), and the FP64
     reference-exact path, all over the same `steps` steps from the same data."""
     import cases
@@ -529,7 +529,7 @@ def measure_sr(cg, L, ctx, stream, n, steps, warmup):
                     "roofline_frac": n * n * bpc / (ms * 1e-3) / 1e9 / peak}
     for tag in ("fp32_c2p_fp64", "fp32_newton_variant"):
         out[tag]["l1_rho_vs_fp64"] = rel_l1(prims[tag][..., 0], prims["fp64"][..., 0])
-    out["fp32_c2p_fp64"]["what"] = "config 3 as stated: FP32 bulk, FP64 Newton iterations in every primitive recovery"
+    out["fp32_c2p_fp64"]["what"] = "as stated: FP32 bulk, FP64 Newton iterations in every primitive recovery"
     out["fp32_newton_variant"]["what"] = "variant: FP32 Newton iterations, FP64 only above Lorentz factor 2 " \
                                          "(not reached here) or on FP32 non-convergence"
     out["value"] = out["fp32_c2p_fp64"]["value"]
@@ -548,7 +548,7 @@ def measure_sr(cg, L, ctx, stream, n, steps, warmup):
     return out
 
 
-# ---------------------------------------------------------------- configuration 4: black-hole accretion
+# ---------------------------------------------------------------- black-hole accretion, 1024^2
 GR_WORKLOAD = "2D black-hole Euler in Kerr-Schild Schwarzschild spacetime (M = 1), SLIC van Leer + " \
               "RK4 source (BlackHoleEulerForcingSolver, one subcycle), CFL 0.9, 1024x1024 on [-10, 10]^2 " \
               "(dx = 20/1024, hole at (10, 10) of the grid's coordinates), excision r <= 2M, rho = 1 with 1% " \
@@ -577,7 +577,7 @@ def gr_step_fixed(g, dt, nsub=1, lim=1):
 
 
 def measure_gr(cg, L, ctx, stream, n, steps, warmup, r_cut=5.0):
-    """Configuration 4: the FP32 bulk path's own run (CFL time steps), the FP64 reference-exact path
+    """Black-hole accretion: the FP32 bulk path's own run (CFL time steps), the FP64 reference-exact path
     over the same number of steps driven by its own CFL rule, and the FP32 path driven by the FP64
     run's time-step sequence, so that the density error over r > r_cut M compares the solutions at
     equal times (the free-running runs' time steps part where the horizon cells' speeds differ)."""
@@ -667,7 +667,7 @@ def measure_gr(cg, L, ctx, stream, n, steps, warmup, r_cut=5.0):
     return out
 
 
-# ---------------------------------------------------------------- configuration 5: batched uneven grids
+# ---------------------------------------------------------------- 256 batched uneven grids
 BATCH_WORKLOAD = "256 independent Newtonian Euler grids (1D and 2D), every side log-uniform in " \
                  "[128, 2048] cells (seed 5), seeded Riemann data, SLIC MinBee, CFL 0.9, transmissive, dx = 1/nx"
 
@@ -681,7 +681,7 @@ def batch_problem():
 
 
 def measure_batch(cg, L, ctx, stream, steps, warmup, l1_steps=20, tiles=False):
-    """Configuration 5: the FP32 batch in one persistent graph-replayed launch (tile shape from the
+    """The 256-grid batch: the FP32 batch in one persistent graph-replayed launch (tile shape from the
     autotuner), the same grids stepped one by one, the FP64 batch and the FP32-vs-FP64 density
     error over `l1_steps` steps, and an e2e over the value's steps."""
     import torch

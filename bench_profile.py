@@ -7,8 +7,8 @@
     python bench_profile.py --kernel adjoint --system 2 --n 256 --precision fp64 --subcycles 1 --launches 1
     python bench_profile.py --kernel batch --grids 64 --launches 2
 
-Creates one grid of the configuration's problem for the system (Newtonian: config-2 four-quadrant
-data, periodic; SR: config-3 Kelvin-Helmholtz layers, periodic; GR: config-4 accretion onto a
+Creates one grid of the system's benchmark problem (Newtonian: four-quadrant Riemann
+data, periodic; SR: Kelvin-Helmholtz layers, periodic; GR: accretion onto a
 Schwarzschild hole, transmissive; MinBee) and launches the requested kernels a few times, so that a profiler can capture exactly those launches on a
 bounded device footprint (two state buffers plus one staging buffer).  `adjoint` runs the
 gradient of `launches` SLIC steps (checkpoint every step: launches X and Y sweep adjoints per
@@ -60,11 +60,11 @@ def main():
     prec = cg.FP32 if a.precision == "fp32" else cg.FP64
     bh = None
     dx = 1.0 / n
-    if a.system == cg.NEWTONIAN:  # config-2 four-quadrant data
+    if a.system == cg.NEWTONIAN:  # four-quadrant Riemann data
         s = cases.four_quadrant(n, 2)
-    elif a.system == cg.SR:  # config-3 Kelvin-Helmholtz layers
+    elif a.system == cg.SR:  # Kelvin-Helmholtz layers
         s = cases.kelvin_helmholtz(n, 3)
-    else:  # config-4 accretion: [-10, 10]^2 with the hole at the centre, M = 1
+    else:  # accretion: [-10, 10]^2 with the hole at the centre, M = 1
         rng = np.random.default_rng(4)
         s = np.zeros((n, n, 5))
         s[..., 0] = np.exp(0.01 * rng.standard_normal((n, n)))

@@ -9,8 +9,9 @@
 //   C  the Y sweep of every 2D grid (dt);
 //   D  the second X sweep of every 2D grid (dt/2), with each grid's CFL reduction fused in.
 // Work is a list of items per phase (X: a few rows of one grid, tiled; Y: a block of columns
-// times a run of rows), dealt to the resident blocks round-robin.  The barrier needs co-residency, so the
-// launch is cooperative; every wait is bounded and reports a timeout instead of hanging.
+// times a run of rows), dealt on the host to the workers (resident blocks, or their warps) so that
+// their loads by cells swept are even.  The barrier needs co-residency, so the launch is
+// cooperative; every wait is bounded and reports a timeout instead of hanging.
 #pragma once
 #include "policies.cuh"
 #include "sweep_pairs.cuh"
@@ -23,10 +24,15 @@ struct BatchGrid {
     double dx;
 };
 
-// X item: rows [a, b) of grid g, each row in tiles of NT - 2 cells; Y item: columns [a, a + NT)
-// and rows [b, c) of grid g.  Items hold several tiles so that the per-item set-up (descriptor
-// loads, time step, two barriers) and the CFL reduction are paid once per few thousand cells.
+// One-cell tiles (FP64): X item rows [a, b) of grid g, each row in tiles of NT - 2 cells; Y item
+// columns [a, a + NT) and rows [b, c) of grid g.  Cell pairs (FP32): X item the grid's 60-cell
+// segments a .. b - 1, numbered row by row; Y item columns [a, a + 64) and rows [b, c).  Items
+// hold several tiles so that the per-item set-up (descriptor loads, time step) and the CFL
+// reduction are paid once per few thousand cells.
 struct BatchItem { int g, a, b, c; };
+
+// Rows' worth of 60-cell segments in one FP32 X item.
+constexpr int kBatchXSegs = 8;
 
 struct GridBarrier {
     unsigned int count;
@@ -40,8 +46,8 @@ struct BatchDev {
     const BatchGrid* grids;
     StepCtl* ctl;
     int ngrids;
-    const BatchItem* items[3];  // phases B, C, D
-    int nitems[3];
+    const BatchItem* items[3];  // phases B, C, D, worker by worker
+    const int* offs[3];         // worker w's items: items[offs[w]] .. items[offs[w + 1] - 1]
     void* buf[2];
     GridBarrier* bar;
     int* gstep;                 // steps completed by the batch (buffer parity)
@@ -134,8 +140,9 @@ __global__ void __launch_bounds__(NT, MINB) batch_step_kernel(PolX polx0, PolY p
             const S* src = (const S*)(ph == 1 ? b1 : b0);
             S* dst = (S*)(ph == 1 ? b0 : b1);
             const BatchItem* items = ph == 0 ? B.items[0] : (ph == 1 ? B.items[1] : B.items[2]);
-            const int n = ph == 0 ? B.nitems[0] : (ph == 1 ? B.nitems[1] : B.nitems[2]);
-            for (int k = blockIdx.x; k < n; k += gridDim.x) {
+            const int* offs = ph == 0 ? B.offs[0] : (ph == 1 ? B.offs[1] : B.offs[2]);
+            const int k1 = offs[blockIdx.x + 1];
+            for (int k = offs[blockIdx.x]; k < k1; k++) {
                 const BatchItem it = items[k];
                 const BatchGrid bg = B.grids[it.g];
                 StepCtl* ctl = &B.ctl[it.g];
@@ -192,23 +199,36 @@ __global__ void __launch_bounds__(NT, MINB) batch_step_kernel(PolX polx0, PolY p
     if (blockIdx.x == 0 && threadIdx.x == 0) *B.gstep = step0 + nsteps;
 }
 
-// The Y pair sweep as the batched kernel calls it (one column pair, a run of rows).
-template <int LIM>
-__device__ __forceinline__ float batch_y_pair(const NewtonFastParams& P, int dims, const Geom& G, const float* src,
-                                           float* dst, int j, int y0, int y1, bool act, const FastCoef& cf, bool ws) {
-    return y_pair_march<LIM>(P, dims, G, src, dst, j, y0, y1, act, cf, ws);
+// Rows of each warp's Y ring in the FP32 batched launch, and the launch's dynamic shared memory
+// (the rings and their mbarriers) for NT threads.
+constexpr int kBatchRingRows = 8;
+constexpr size_t batch_pair_smem(int nt) {
+    return (size_t)(nt / 32) * kBatchRingRows * (5 * 64 * sizeof(float) + sizeof(unsigned long long));
 }
 
-// FP32 batch on cell pairs (sweep_pairs.cuh): X items are whole rows of one grid, dealt to the
-// block's warps one 60-cell segment at a time; Y items are 2 NT columns (a pair per thread) x a
-// run of rows.  Same phases, barriers and per-grid controllers as batch_step_kernel.
+// FP32 batch on cell pairs (sweep_pairs.cuh), one warp per item and no block barrier inside a
+// phase: X items are runs of 60-cell segments of one grid (the next segment loaded while the
+// current one is computed); Y items are 64 columns (a pair per lane) x a run of rows, marched
+// through the warp's ring of rows staged by bulk copies (y_ring_march), its barriers initialised
+// again before each item.  Each warp reads its item's time step and reduces its own CFL maximum.
+// Same phases, grid barriers and per-grid controllers as batch_step_kernel.  A ring wait that runs
+// out sets ST_TIMEOUT in the grid's status and in the barrier's error word, so every block leaves
+// at the next barrier.
 template <int LIM, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) batch_pair_kernel(NewtonFastParams P, BatchDev B, int nsteps) {
     constexpr int W = NT / 32;
     constexpr int TSW = 60;
-    __shared__ FastCoef s_cf;
-    __shared__ int s_act;
-    const int warp = threadIdx.x >> 5;
+    constexpr int R = kBatchRingRows;
+    constexpr unsigned FULL = 0xffffffffu;
+    extern __shared__ __align__(128) unsigned char batch_smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int worker = blockIdx.x * W + warp;
+    float(*ring)[R][5][64] = reinterpret_cast<float(*)[R][5][64]>(batch_smem);
+    unsigned long long* rbar = reinterpret_cast<unsigned long long*>(batch_smem + W * sizeof(float[R][5][64]));
+    unsigned long long* wbar = rbar + warp * R;
+    ring_init<R>(wbar, false);
+    bool ring_ok = true;     // warp-uniform
+    bool ring_used = false;  // warp-uniform: the ring's barriers have been used since their initialisation
     const int step0 = *B.gstep;
     for (int s = 0; s < nsteps; s++) {
         const int p = (step0 + s) & 1;
@@ -220,8 +240,9 @@ __global__ void __launch_bounds__(NT, MINB) batch_pair_kernel(NewtonFastParams P
             const float* src = (const float*)(ph == 1 ? b1 : b0);
             float* dst = (float*)(ph == 1 ? b0 : b1);
             const BatchItem* items = ph == 0 ? B.items[0] : (ph == 1 ? B.items[1] : B.items[2]);
-            const int n = ph == 0 ? B.nitems[0] : (ph == 1 ? B.nitems[1] : B.nitems[2]);
-            for (int k = blockIdx.x; k < n; k += gridDim.x) {
+            const int* offs = ph == 0 ? B.offs[0] : (ph == 1 ? B.offs[1] : B.offs[2]);
+            const int k1 = offs[worker + 1];
+            for (int k = offs[worker]; k < k1; k++) {  // warp-uniform
                 const BatchItem it = items[k];
                 const BatchGrid bg = B.grids[it.g];
                 StepCtl* ctl = &B.ctl[it.g];
@@ -233,37 +254,48 @@ __global__ void __launch_bounds__(NT, MINB) batch_pair_kernel(NewtonFastParams P
                 ds.scale = (ph == 1 || one_d) ? 1.0 : 0.5;
                 ds.fsel = (ph == 1 || one_d) ? 0 : 1;
                 const bool ws = (ph == 0 && one_d) || ph == 2;
-                __syncthreads();  // the previous item's coefficients and reduction are no longer read
-                if (threadIdx.x == 0) {
+                int act = 0;
+                FastCoef cf{0.0f, 0.0f, 0.0f};
+                if (lane == 0) {
                     double dt;
-                    s_act = ds.get(dt);
-                    if (s_act) s_cf = ds.fast_coef();
+                    act = ds.get(dt);
+                    if (act) cf = ds.fast_coef();
                 }
-                __syncthreads();
-                const bool act = s_act != 0;
-                const FastCoef cf = s_cf;
+                act = __shfl_sync(FULL, act, 0);
+                cf.dtdx = __shfl_sync(FULL, cf.dtdx, 0);
+                cf.half_dtdx = __shfl_sync(FULL, cf.half_dtdx, 0);
+                cf.q_dxdt = __shfl_sync(FULL, cf.q_dxdt, 0);
                 const Geom& G = bg.G;
                 const float* sg = src + bg.off;
                 float* dg = dst + bg.off;
                 float w = 0.0f;
                 if (ph == 1) {
-                    const int j = it.a + 2 * threadIdx.x;
-                    if (j < G.nx) w = batch_y_pair<LIM>(P, G.dims, G, sg, dg, j, it.b, it.c, act, cf, ws);
+                    if (!act) {
+                        const int j = it.a + 2 * lane;
+                        if (j < G.nx) y_pair_march<LIM>(P, G.dims, G, sg, dg, j, it.b, it.c, false, cf, false);
+                    } else if (ring_ok) {
+                        if (ring_used) ring_init<R>(wbar, true);
+                        ring_used = true;
+                        w = y_ring_march<LIM, R>(P, G.dims, G, sg, dg, it.a, it.b, it.c, cf, ws, ring[warp], wbar, ring_ok);
+                        if (!ring_ok && lane == 0) {
+                            atomicOr(&ctl->status, ST_TIMEOUT);
+                            atomicOr(&B.bar->err, ST_TIMEOUT);
+                        }
+                    }
                 } else {
                     const int spr = (G.nx + TSW - 1) / TSW;
-                    const int total = (it.b - it.a) * spr;
-                    // the warp's next segment is loaded while the current one is computed
                     Cell2 ahead;
-                    if (warp < total) x_pair_load(G, sg, it.a + warp / spr, (warp % spr) * TSW, ahead);
-                    for (int q = warp; q < total; q += W) {  // warp-uniform
-                        const int row = it.a + q / spr, s0 = (q % spr) * TSW;
+                    x_pair_load(G, sg, it.a / spr, (it.a % spr) * TSW, ahead);
+                    for (int q = it.a; q < it.b; q++) {
                         const Cell2 m = ahead;
-                        const int qn = q + W;
-                        if (qn < total) x_pair_load(G, sg, it.a + qn / spr, (qn % spr) * TSW, ahead);
-                        w = fmaxf(w, x_pair_update<LIM>(P, G.dims, G, dg, row, s0, m, act, cf, ws));
+                        if (q + 1 < it.b) x_pair_load(G, sg, (q + 1) / spr, ((q + 1) % spr) * TSW, ahead);
+                        w = fmaxf(w, x_pair_update<LIM>(P, G.dims, G, dg, q / spr, (q % spr) * TSW, m, act, cf, ws));
                     }
                 }
-                if (ws && act) block_max_to<NT>(&ctl->smax[ctl->it & 1], w);
+                if (ws && act) {
+                    w = warp_max(w);
+                    if (lane == 0) atomic_max_nonneg(&ctl->smax[ctl->it & 1], (double)w);
+                }
             }
             if (!grid_sync(B.bar)) return;
         }

@@ -7,6 +7,7 @@
 #include <cstring>
 #include <fstream>
 #include <iomanip>
+#include <queue>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -17,6 +18,7 @@
 
 namespace cg {
 void* batch_fast_fn(int nt, int cap, int lim);
+size_t batch_fast_smem(int nt);
 void* batch_exact_fn(int nt, int cap);
 }  // namespace cg
 
@@ -57,7 +59,8 @@ struct cosmos_batch {
     size_t max_cells;
     // work lists for the current tile shape
     int nt, seg, cap, blocks;
-    BatchItem* d_items[3];
+    BatchItem* d_items[3];  // per phase, worker by worker
+    int* d_offs[3];         // per phase: worker w's items are d_items[off[w] .. off[w + 1] - 1]
     int nitems[3];
     // run state
     cosmos_solve_opts run;
@@ -77,7 +80,7 @@ BatchDev dev_desc(cosmos_batch* b) {
     B.grids = b->d_grids;
     B.ctl = b->d_ctl;
     B.ngrids = (int)b->grids.size();
-    for (int k = 0; k < 3; k++) { B.items[k] = b->d_items[k]; B.nitems[k] = b->nitems[k]; }
+    for (int k = 0; k < 3; k++) { B.items[k] = b->d_items[k]; B.offs[k] = b->d_offs[k]; }
     B.buf[0] = b->buf[0];
     B.buf[1] = b->buf[1];
     B.bar = b->d_bar;
@@ -90,44 +93,95 @@ void* kernel_fn(cosmos_batch* b, int nt, int seg, int cap, int lim) {
     return b->precision == COSMOS_FP32 ? batch_fast_fn(nt, cap, lim) : batch_exact_fn(nt, cap);
 }
 
-// Work lists for a tile shape.  FP64 (one-cell tiles): X items are whole rows of one grid, as many
-// as make about 8 tiles of nt - 2 cells; Y items nt columns x seg rows.  FP32 (cell pairs): X items
-// are whole rows making about two 60-cell segments per warp; Y items 2 nt columns x seg rows.
+// Work lists for a tile shape, one per phase.  FP64 (one-cell tiles, one block per item): X items
+// are whole rows of one grid, as many as make about 8 tiles of nt - 2 cells; Y items nt columns x
+// seg rows.  FP32 (cell pairs, one warp per item): X items are runs of kBatchXSegs 60-cell segments
+// of one grid, numbered row by row (a = first, b = one past the last); Y items 64 columns x seg rows.
+// Each list is dealt to the workers (FP64: the resident blocks; FP32: their warps) longest item
+// first, each onto the least-loaded worker, by a cost of cells swept (Y counting its four halo
+// rows) plus a per-item overhead; worker w's items are stored at off[w] .. off[w + 1] - 1.
 int build_items(cosmos_batch* b, int nt, int seg, int cap) {
     void* fn = kernel_fn(b, nt, seg, cap, b->run.limiter);
     if (!fn) return bfail(COSMOS_EUNSUPPORTED, "batch tile shape not provided for this precision");
-    std::vector<BatchItem> ph[3];
-    for (int g = 0; g < (int)b->grids.size(); g++) {
-        const Geom& G = b->grids[g].G;
-        const bool pairs = b->precision == COSMOS_FP32;
-        const int tiles = pairs ? (G.nx + 59) / 60 : (G.nx + nt - 3) / (nt - 2);
-        const int rows = std::max(1, (pairs ? 2 * (nt / 32) : 8) / tiles);
-        const int ycols = pairs ? 2 * nt : nt;
-        for (int r = 0; r < G.ny; r += rows) {
-            const BatchItem it{g, r, std::min(r + rows, G.ny), 0};
-            ph[0].push_back(it);
-            if (G.dims == 2) ph[2].push_back(it);
-        }
-        if (G.dims == 2)
-            for (int j0 = 0; j0 < G.nx; j0 += ycols)
-                for (int y0 = 0; y0 < G.ny; y0 += seg) ph[1].push_back(BatchItem{g, j0, y0, std::min(y0 + seg, G.ny)});
-    }
-    for (int k = 0; k < 3; k++) {
-        if (b->d_items[k]) cudaFree(b->d_items[k]);
-        b->d_items[k] = nullptr;
-        b->nitems[k] = (int)ph[k].size();
-        if (ph[k].empty()) continue;
-        BCK(cudaMalloc(&b->d_items[k], ph[k].size() * sizeof(BatchItem)));
-        BCK(cudaMemcpy(b->d_items[k], ph[k].data(), ph[k].size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
-    }
     int per_sm = 0, sms = 0;
-    BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, nt, 0));
+    const size_t smem = b->precision == COSMOS_FP32 ? batch_fast_smem(nt) : 0;
+    BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, nt, smem));
     BCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
     if (per_sm < 1) return bfail(COSMOS_EUNSUPPORTED, "batch kernel does not fit on an SM");
+    const bool pairs = b->precision == COSMOS_FP32;
+    const int blocks = per_sm * sms;
+    const int workers = pairs ? blocks * (nt / 32) : blocks;
+    struct Costed { long long cost; BatchItem it; };
+    std::vector<Costed> ph[3];
+    const long long overhead = 32;
+    for (int g = 0; g < (int)b->grids.size(); g++) {
+        const Geom& G = b->grids[g].G;
+        if (pairs) {
+            const int spr = (G.nx + 59) / 60, total = spr * G.ny;
+            for (int q = 0; q < total; q += kBatchXSegs) {
+                const BatchItem it{g, q, std::min(q + kBatchXSegs, total), 0};
+                const long long c = 64ll * (it.b - it.a) + overhead;
+                ph[0].push_back({c, it});
+                if (G.dims == 2) ph[2].push_back({c, it});
+            }
+            if (G.dims == 2)
+                for (int j0 = 0; j0 < G.nx; j0 += 64)
+                    for (int y0 = 0; y0 < G.ny; y0 += seg) {
+                        const int y1 = std::min(y0 + seg, G.ny);
+                        ph[1].push_back({64ll * (y1 - y0 + 4) + overhead, BatchItem{g, j0, y0, y1}});
+                    }
+        } else {
+            const int tiles = (G.nx + nt - 3) / (nt - 2);
+            const int rows = std::max(1, 8 / tiles);
+            for (int r = 0; r < G.ny; r += rows) {
+                const BatchItem it{g, r, std::min(r + rows, G.ny), 0};
+                const long long c = (long long)nt * tiles * (it.b - it.a) + overhead;
+                ph[0].push_back({c, it});
+                if (G.dims == 2) ph[2].push_back({c, it});
+            }
+            if (G.dims == 2)
+                for (int j0 = 0; j0 < G.nx; j0 += nt)
+                    for (int y0 = 0; y0 < G.ny; y0 += seg) {
+                        const int y1 = std::min(y0 + seg, G.ny);
+                        ph[1].push_back({(long long)nt * (y1 - y0 + 4) + overhead, BatchItem{g, j0, y0, y1}});
+                    }
+        }
+    }
+    for (int k = 0; k < 3; k++) {
+        // longest processing time first onto the least-loaded worker (ties: the lower index)
+        std::stable_sort(ph[k].begin(), ph[k].end(), [](const Costed& x, const Costed& y) { return x.cost > y.cost; });
+        using Load = std::pair<long long, int>;
+        std::priority_queue<Load, std::vector<Load>, std::greater<Load>> pq;
+        for (int w = 0; w < workers; w++) pq.push({0ll, w});
+        std::vector<std::vector<BatchItem>> per(workers);
+        for (const Costed& c : ph[k]) {
+            Load l = pq.top();
+            pq.pop();
+            per[l.second].push_back(c.it);
+            pq.push({l.first + c.cost, l.second});
+        }
+        std::vector<BatchItem> flat;
+        std::vector<int> off(workers + 1, 0);
+        flat.reserve(ph[k].size());
+        for (int w = 0; w < workers; w++) {
+            flat.insert(flat.end(), per[w].begin(), per[w].end());
+            off[w + 1] = (int)flat.size();
+        }
+        if (b->d_items[k]) cudaFree(b->d_items[k]);
+        if (b->d_offs[k]) cudaFree(b->d_offs[k]);
+        b->d_items[k] = nullptr;
+        b->d_offs[k] = nullptr;
+        b->nitems[k] = (int)flat.size();
+        BCK(cudaMalloc(&b->d_offs[k], off.size() * sizeof(int)));
+        BCK(cudaMemcpy(b->d_offs[k], off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice));
+        if (flat.empty()) continue;
+        BCK(cudaMalloc(&b->d_items[k], flat.size() * sizeof(BatchItem)));
+        BCK(cudaMemcpy(b->d_items[k], flat.data(), flat.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
+    }
     b->nt = nt;
     b->seg = seg;
     b->cap = cap;
-    b->blocks = per_sm * sms;
+    b->blocks = blocks;
     return COSMOS_OK;
 }
 
@@ -282,7 +336,10 @@ int cosmos_batch_destroy(cosmos_batch* b) {
     cudaStreamSynchronize(b->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     for (int k = 0; k < 2; k++) if (b->buf[k]) cudaFree(b->buf[k]);
-    for (int k = 0; k < 3; k++) if (b->d_items[k]) cudaFree(b->d_items[k]);
+    for (int k = 0; k < 3; k++) {
+        if (b->d_items[k]) cudaFree(b->d_items[k]);
+        if (b->d_offs[k]) cudaFree(b->d_offs[k]);
+    }
     if (b->d_grids) cudaFree(b->d_grids);
     if (b->d_ctl) cudaFree(b->d_ctl);
     if (b->d_bar) cudaFree(b->d_bar);

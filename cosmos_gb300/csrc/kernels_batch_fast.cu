@@ -9,12 +9,20 @@ namespace {
 template <int LIM, int NT, int CAP>
 struct FastBatch {
     static constexpr int MINB = CAP ? 512 / NT : 1;  // cap: at most 128 registers
-    static void* fn() { return (void*)batch_pair_kernel<LIM, NT, MINB>; }
+    // the rings' dynamic shared memory (above the 48 KB default for 256 threads)
+    static void* fn() {
+        auto k = batch_pair_kernel<LIM, NT, MINB>;
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)batch_pair_smem(NT)) != cudaSuccess)
+            return nullptr;
+        return (void*)k;
+    }
     static cudaError_t launch(const BatchLaunch& L) {
+        if (!fn()) return cudaErrorInvalidValue;
         const NewtonFastParams P = make_newton_fast<0, LIM, false>(L.gamma, L.bias, 0, 2).P;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(L.blocks);
         cfg.blockDim = dim3(NT);
+        cfg.dynamicSmemBytes = batch_pair_smem(NT);
         cfg.stream = L.stream;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeCooperative;
@@ -47,6 +55,8 @@ cudaError_t launch_batch_fast(const BatchLaunch& L) {
     count_launch();
     return e;
 }
+
+size_t batch_fast_smem(int nt) { return batch_pair_smem(nt); }
 
 void* batch_fast_fn(int nt, int cap, int lim) {
     if (nt != 128 && nt != 256) return nullptr;

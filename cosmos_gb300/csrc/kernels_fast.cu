@@ -10,13 +10,30 @@ namespace {
 constexpr int kXThreads = 256;  // X sweep tile: 256 evolutions, 255 fluxes, 254 updates
 constexpr int kYThreads = 128;
 constexpr int kYSeg = 32;
-constexpr int kXPairThreads = 32;  // one warp per block
-constexpr int kXPairSegs = 3;      // 60-cell segments per warp (4096^2: 0.145 ms against 0.149 with 2)
+constexpr int kXPairSegs = 3;      // 60-cell segments per one-warp block (4096^2: 0.145 ms against 0.149 with 2)
+constexpr int kXRingMinBlocks = 32;  // at most 64 registers: 32 one-warp blocks per SM
 constexpr int kYPairThreads = 32;  // one warp (64 columns, two per thread) per block: 0.154 ms at 4096^2
                                    // against 0.168 with two warps per block at the same registers
-constexpr int kYPairSeg = 32;
 constexpr int kYRingRows = 8;      // Y rows staged in shared memory per warp (up to 8 in flight)
 constexpr int kYRingMinBlocks = 16;  // at most 128 registers: 16 one-warp blocks per SM
+
+// Rows per Y-sweep block: about 32 (each block re-reads four halo rows), adjusted so that the
+// blocks fill whole waves of the resident slots.  At 4096^2, 32-row segments make 8192 one-warp
+// blocks for 152 x 16 slots (3.37 waves, the last a third full); 36-row segments make 7296, three
+// full waves.
+int y_ring_seg(const void* kernel, int nx, int ny) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kYPairThreads, 0) != cudaSuccess || per_sm < 1)
+        per_sm = kYRingMinBlocks;
+    const long long slots = (long long)per_sm * device_sm_count();
+    const long long cols = (nx + 2 * kYPairThreads - 1) / (2 * kYPairThreads);
+    const long long blocks32 = cols * ((ny + 31) / 32);
+    const long long waves = blocks32 / slots > 1 ? blocks32 / slots : 1;
+    long long rows = waves * slots / cols;  // block rows that fill `waves` whole waves
+    if (rows < 1) rows = 1;
+    int seg = (int)((ny + rows - 1) / rows);
+    return seg < 8 ? 8 : (seg > 64 ? 64 : seg);
+}
 
 template <int AXIS, int LIM, bool MASKED>
 NewtonFastPolicy<AXIS, LIM, MASKED> make_fast(const SweepArgs& a) {
@@ -24,7 +41,7 @@ NewtonFastPolicy<AXIS, LIM, MASKED> make_fast(const SweepArgs& a) {
 }
 
 template <int AXIS, int LIM, bool MASKED>
-void run_fast(const SweepArgs& a) {
+cudaError_t run_fast(const SweepArgs& a) {
     const Geom& G = a.G;
     const float* src = (const float*)a.src;
     float* dst = (float*)a.dst;
@@ -33,31 +50,33 @@ void run_fast(const SweepArgs& a) {
     if constexpr (AXIS == 0) {
         if (a.order == 2 && !MASKED) {
             const int segs = (G.nx + 59) / 60;
-            const int per_block = (kXPairThreads / 32) * kXPairSegs;
-            dim3 grid((segs + per_block - 1) / per_block, G.ny);
-            sweep_x_pair_kernel<LIM, kXPairThreads, kXPairSegs><<<grid, kXPairThreads, 0, a.stream>>>(
-                pol.P, G.dims, G, src, dst, a.ds, a.out);
-            return;
+            dim3 grid((segs + kXPairSegs - 1) / kXPairSegs, G.ny);
+            sweep_x_ring_kernel<LIM, kXPairSegs, kXRingMinBlocks><<<grid, 32, 0, a.stream>>>(pol.P, G.dims, G, src, dst,
+                                                                                        a.ds, a.out);
+            return cudaSuccess;
         }
         dim3 grid((G.nx + kXThreads - 3) / (kXThreads - 2), G.ny);
         if (a.order == 2) sweep_x_own_kernel<Pol, 2, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
         else sweep_x_own_kernel<Pol, 1, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
     } else if (a.order == 2 && !MASKED) {
-        dim3 grid((G.nx + 2 * kYPairThreads - 1) / (2 * kYPairThreads), (G.ny + kYPairSeg - 1) / kYPairSeg);
-        sweep_y_ring_kernel<LIM, kYPairThreads, kYPairSeg, kYRingRows, kYRingMinBlocks><<<grid, kYPairThreads, 0, a.stream>>>(
-            pol.P, G.dims, G, src, dst, a.ds, a.out);
+        auto kernel = sweep_y_ring_kernel<LIM, kYPairThreads, kYRingRows, kYRingMinBlocks>;
+        const int seg = y_ring_seg((const void*)kernel, G.nx, G.ny);
+        dim3 grid((G.nx + 2 * kYPairThreads - 1) / (2 * kYPairThreads), (G.ny + seg - 1) / seg);
+        kernel<<<grid, kYPairThreads, 0, a.stream>>>(pol.P, G.dims, G, src, dst, a.ds, a.out, seg);
+        return cudaSuccess;
     } else {
         dim3 grid((G.nx + kYThreads - 1) / kYThreads, (G.ny + kYSeg - 1) / kYSeg);
         if (a.order == 2) sweep_y_kernel<Pol, 2, kYThreads, kYSeg><<<grid, kYThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
         else sweep_y_kernel<Pol, 1, kYThreads, kYSeg><<<grid, kYThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
     }
+    return cudaSuccess;
 }
 
 template <int AXIS, bool MASKED>
-void run_fast_lim(const SweepArgs& a) {
-    if (a.lim == 0) run_fast<AXIS, 0, MASKED>(a);
-    else if (a.lim == 1) run_fast<AXIS, 1, MASKED>(a);
-    else run_fast<AXIS, 2, MASKED>(a);  // Solvers/SlopeLimiters.cpp:66: any other id is MinBee
+cudaError_t run_fast_lim(const SweepArgs& a) {
+    if (a.lim == 0) return run_fast<AXIS, 0, MASKED>(a);
+    if (a.lim == 1) return run_fast<AXIS, 1, MASKED>(a);
+    return run_fast<AXIS, 2, MASKED>(a);  // Solvers/SlopeLimiters.cpp:66: any other id is MinBee
 }
 
 }  // namespace
@@ -67,10 +86,11 @@ cudaError_t launch_sweep_fast(const SweepArgs& a) {
     if (a.system == 2) return launch_sweep_gr_fast(a);
     if (a.system != 0) return cudaErrorNotSupported;
     const bool masked = a.out.mask != nullptr;
-    if (a.G.axis == 0) masked ? run_fast_lim<0, true>(a) : run_fast_lim<0, false>(a);
-    else masked ? run_fast_lim<1, true>(a) : run_fast_lim<1, false>(a);
+    cudaError_t e;
+    if (a.G.axis == 0) e = masked ? run_fast_lim<0, true>(a) : run_fast_lim<0, false>(a);
+    else e = masked ? run_fast_lim<1, true>(a) : run_fast_lim<1, false>(a);
     count_launch();
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_wavespeed_fast(const SweepArgs& a, unsigned long long* slot) {

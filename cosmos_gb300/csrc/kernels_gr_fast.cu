@@ -244,7 +244,7 @@ void run_lim(const SweepArgs& a) {
 // ---------------------------------------------------------------- source step
 // One cell per thread; cells whose five-point stencil touches the excised region keep their state.
 // Capped at three blocks of 128 threads per SM (168 registers, a small L1-resident spill): on the
-// evolved config-4 grid that beat 205 registers at two blocks (2.65 vs 2.81 ms per step).
+// evolved 1024^2 accretion grid that beat 205 registers at two blocks (2.65 vs 2.81 ms per step).
 template <int LIM>
 __global__ void __launch_bounds__(128, 3) gr_rk_kernel(SRFastParams P, NewtonFastParams NP, GRTables T, Geom G, double dx,
                                                     const float* __restrict__ src, float* __restrict__ dst, DtSrc ds,

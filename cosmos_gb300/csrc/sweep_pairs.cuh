@@ -163,69 +163,63 @@ CG_D float x_pair_update(const NewtonFastParams& P, int dims, const Geom& G, flo
 
 // ---- single-grid kernels
 
-// Y sweep with the rows staged in shared memory by bulk copies.  Each warp owns 64 columns (two per
-// lane) and a ring of R row slots in shared memory (five field rows each, one mbarrier per slot):
-// its rows y0 - 2 .. y1 + 1 arrive by cp.async.bulk, issued by lanes 0-4 (one field each) up to R
-// rows ahead of the row being consumed, so the loads overlap several rows of work where a register
-// prefetch covers one.  Warps never wait for each other (no block barrier after the set-up), and
-// each reduces its own CFL maximum.  The arithmetic is y_pair_march's.  A wait that runs out
-// (about a second) sets ST_TIMEOUT in the status word; the warp then waits, again bounded, for its
-// rows still in flight and leaves.
-template <int LIM, int NT, int SEG, int R, int MINB>
-__global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams P, int dims, Geom G,
-                                                          const float* __restrict__ src, float* __restrict__ dst,
-                                                          DtSrc ds, SweepOut out) {
-    static_assert(R >= 5 && (R & (R - 1)) == 0, "a power of two above the four prologue rows");
-    static_assert(NT % 32 == 0, "whole warps");
-    constexpr int NWP = NT / 32;
-    constexpr unsigned FULL = 0xffffffffu;
-    __shared__ __align__(128) float ring[NWP][R][5][64];
-    __shared__ __align__(8) unsigned long long bar[NWP][R];
-    __shared__ FastCoef s_coef;
-    __shared__ int s_act;
-    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    const int jw = (blockIdx.x * NWP + wp) * 64;  // the warp's first column
-    const int j = jw + 2 * lane;
-    const bool live = j < G.nx, two = j + 1 < G.nx;
-    const int y0 = blockIdx.y * SEG, y1 = min(y0 + SEG, G.ny);
-    const int ylo = y0 - 2, yhi = y1 + 1;  // rows read
-    if (threadIdx.x == 0) {
-        double dt;
-        s_act = ds.get(dt);
-        if (s_act) s_coef = ds.fast_coef();
-        for (int w = 0; w < NWP; w++)
-            for (int q = 0; q < R; q++) mbar_init(&bar[w][q], 1);
+// (Re)initialise one warp's R ring mbarriers; lane 0 works, the whole warp calls it.  A ring is
+// drained between marches (every copy it issued has been waited for), so its barriers can be
+// invalidated and initialised again: each march then starts at slot 0, phase 0, whose fixed
+// slot and parity sequence compiles into cheaper code than a ring state carried in registers
+// (measured 3 % on the 4096^2 Y sweep).
+template <int R>
+CG_D void ring_init(unsigned long long* bar, bool reinit) {
+    if ((threadIdx.x & 31) == 0) {
+        for (int q = 0; q < R; q++) {
+            if (reinit) mbar_inval(&bar[q]);
+            mbar_init(&bar[q], 1);
+        }
         mbar_init_fence();
     }
-    __syncthreads();
-    if (jw >= G.nx) return;  // warp-uniform: no column of this warp exists
-    if (!s_act) {            // inactive step: keep the ping-pong buffers consistent
-        if (live) y_pair_march<LIM>(P, dims, G, src, dst, j, y0, y1, false, s_coef, false);
-        return;
-    }
-    const FastCoef cf = s_coef;
+    __syncwarp();
+}
+
+// Y march of one warp over rows [y0, y1) of the 64 columns from jw (two per lane), the rows
+// arriving through the warp's ring of R row slots in shared memory (five field rows of 64 floats
+// each, one mbarrier per slot, freshly initialised) by cp.async.bulk: lanes 0-4 copy one field
+// each, up to R rows ahead of the row being consumed, so the loads overlap several rows of work
+// where a register prefetch covers one.  The arithmetic is y_pair_march's.  All 32 lanes call it
+// together, with jw < G.nx.  Returns the lane's wavespeed maximum over its updated cells when
+// want_w.  A wait that runs out (about a second) makes `ok` false (warp-uniform); the warp then
+// waits, again bounded, for its rows still in flight and returns.  On success the ring is drained.
+template <int LIM, int R>
+CG_D float y_ring_march(const NewtonFastParams& P, int dims, const Geom& G, const float* __restrict__ src,
+                        float* __restrict__ dst, int jw, int y0, int y1, const FastCoef cf, bool want_w,
+                        float (*ring)[5][64], unsigned long long* bar, bool& ok) {
+    static_assert(R >= 5 && (R & (R - 1)) == 0, "a power of two above the four prologue rows");
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int j = jw + 2 * lane;
+    const bool live = j < G.nx, two = j + 1 < G.nx;
     const Force4Coef c4 = force4_coef(cf);
     const uint32_t bytes = ((uint32_t)min(64, G.nx - jw) * 4u + 15u) & ~15u;  // within the padded pitch
+    const int ylo = y0 - 2, yhi = y1 + 1;  // rows read
     // Row r of the ring lives in slot (r - ylo) mod R; the slot's k-th use completes phase k mod 2.
-    // Lanes 0-4 each copy one field (lane 5+ hold a valid pointer they never use).
+    // Lanes 0-4 each copy one field (lanes 5+ hold a valid pointer they never use).
     const float* fsrc = src + (size_t)min(lane, 4) * G.fstride + jw;
     int inext = ylo;  // warp-uniform: next row to issue
     auto issue_one = [&]() {
         const int r = inext, q = (r - ylo) & (R - 1);
-        if (lane == 0) mbar_expect_tx(&bar[wp][q], 5 * bytes);
+        if (lane == 0) mbar_expect_tx(&bar[q], 5 * bytes);
         __syncwarp();
-        if (lane < 5) bulk_load(ring[wp][q][lane], fsrc + (size_t)ghost_index(r, G.ny, G.bc) * G.pitch, bytes, &bar[wp][q]);
+        if (lane < 5) bulk_load(ring[q][lane], fsrc + (size_t)ghost_index(r, G.ny, G.bc) * G.pitch, bytes, &bar[q]);
         ++inext;
     };
     for (int k = 0; k < R && inext <= yhi; k++) issue_one();
-    bool ok = true;
-    int tq = 0;          // slot of the next row to take
-    uint32_t tpar = 0;   // its phase parity
+    bool mine = true;
+    int tq = 0;         // slot of the next row to take
+    uint32_t tpar = 0;  // its phase parity
     auto take = [&](Cell2& c) {
-        ok = ok && mbar_wait(&bar[wp][tq], tpar);
+        mine = mine && mbar_wait(&bar[tq], tpar);
 #pragma unroll
         for (int f = 0; f < 5; f++) {
-            const float2 v = *reinterpret_cast<const float2*>(&ring[wp][tq][f][2 * lane]);
+            const float2 v = *reinterpret_cast<const float2*>(&ring[tq][f][2 * lane]);
             c.v[f].v = make_float2(v.x, two ? v.y : v.x);  // a lone last column runs in both lanes
         }
         if (++tq == R) {
@@ -238,11 +232,9 @@ __global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams
     take(cm1);
     take(c0);
     take(c1);
-    ok = __all_sync(FULL, ok);
+    ok = __all_sync(FULL, mine);
     __syncwarp();  // every lane's reads of the freed slots are ordered before their refills
     float w = 0.0f;
-    unsigned long long* wslot = out.slot();
-    const bool want_w = wslot != nullptr && live;
     int consumed = ylo - 1;  // warp-uniform: last row every lane has copied out
     if (ok) {
         consumed = ylo + 3;
@@ -253,7 +245,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams
         nf_force4<1>(P, Rm1, L0, c4.dtdx, c4.dxdt, Fp);
         for (int y = y0; y < y1; y++) {
             take(c2);
-            ok = __all_sync(FULL, ok);
+            ok = __all_sync(FULL, mine);
             if (!ok) break;
             __syncwarp();
             consumed = y + 2;
@@ -285,12 +277,52 @@ __global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams
             c1 = c2;
         }
     }
-    if (!ok) {  // warp-uniform
-        if (lane == 0) {
-            if (out.status) atomicOr(out.status, ST_TIMEOUT);
+    if (!ok) {  // warp-uniform: rows consumed + 1 .. inext - 1 may still be in flight
+        if (lane == 0)
             for (int r = consumed + 1; r < inext; r++)
-                mbar_wait(&bar[wp][(r - ylo) & (R - 1)], (uint32_t)((r - ylo) / R) & 1u, 100000000LL);
-        }
+                mbar_wait(&bar[(r - ylo) & (R - 1)], (uint32_t)((r - ylo) / R) & 1u, 100000000LL);
+        __syncwarp();
+    }
+    return w;
+}
+
+// Y sweep with the rows staged in shared memory by bulk copies (y_ring_march).  Block row b covers
+// grid rows b seg .. (b + 1) seg - 1; each warp owns 64 columns and its own ring, never waits for
+// the other warps (no block barrier after the set-up) and reduces its own CFL maximum.  A ring
+// wait that runs out sets ST_TIMEOUT in the status word.
+template <int LIM, int NT, int R, int MINB>
+__global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams P, int dims, Geom G,
+                                                          const float* __restrict__ src, float* __restrict__ dst,
+                                                          DtSrc ds, SweepOut out, int seg) {
+    static_assert(NT % 32 == 0, "whole warps");
+    constexpr int NWP = NT / 32;
+    __shared__ __align__(128) float ring[NWP][R][5][64];
+    __shared__ __align__(8) unsigned long long bar[NWP][R];
+    __shared__ FastCoef s_coef;
+    __shared__ int s_act;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const int jw = (blockIdx.x * NWP + wp) * 64;  // the warp's first column
+    const int y0 = blockIdx.y * seg, y1 = min(y0 + seg, G.ny);
+    if (threadIdx.x == 0) {
+        double dt;
+        s_act = ds.get(dt);
+        if (s_act) s_coef = ds.fast_coef();
+        for (int w = 0; w < NWP; w++)
+            for (int q = 0; q < R; q++) mbar_init(&bar[w][q], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    if (jw >= G.nx) return;  // warp-uniform: no column of this warp exists
+    if (!s_act) {            // inactive step: keep the ping-pong buffers consistent
+        if (jw + 2 * lane < G.nx) y_pair_march<LIM>(P, dims, G, src, dst, jw + 2 * lane, y0, y1, false, s_coef, false);
+        return;
+    }
+    unsigned long long* wslot = out.slot();
+    bool ok = true;
+    const FastCoef cf = s_coef;  // in registers: the ring's waits would make every use re-read shared memory
+    float w = y_ring_march<LIM, R>(P, dims, G, src, dst, jw, y0, y1, cf, wslot != nullptr, ring[wp], bar[wp], ok);
+    if (!ok) {
+        if (lane == 0 && out.status) atomicOr(out.status, ST_TIMEOUT);
         return;
     }
     if (wslot) {
@@ -299,37 +331,73 @@ __global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams
     }
 }
 
-// X sweep: a warp walks SEGS consecutive 60-cell segments of its row, loading the next segment
-// while it computes the current one.
-template <int LIM, int NT, int SEGS>
-__global__ void __launch_bounds__(NT) sweep_x_pair_kernel(NewtonFastParams P, int dims, Geom G,
-                                                          const float* __restrict__ src, float* __restrict__ dst,
-                                                          DtSrc ds, SweepOut out) {
-    constexpr int TSW = 60;
+// X sweep with each warp's segments staged in shared memory by bulk copies: a one-warp block
+// takes SEGS consecutive 60-cell segments of its row and, at its start, copies every segment whose
+// 64-cell window lies inside the row (cells s0 - 4 .. s0 + 63, a 16-byte aligned run of 272 bytes
+// per field) into its own slot, so all of them are in flight while the first is computed; the
+// row's first segment and its last ones (whose windows reach ghost cells) load through
+// x_pair_load.  No registers hold a prefetched segment.  A wait that runs out (about a second)
+// sets ST_TIMEOUT; the warp then waits, again bounded, for its copies still in flight and leaves.
+template <int LIM, int SEGS, int MINB>
+__global__ void __launch_bounds__(32, MINB) sweep_x_ring_kernel(NewtonFastParams P, int dims, Geom G,
+                                                               const float* __restrict__ src, float* __restrict__ dst,
+                                                               DtSrc ds, SweepOut out) {
+    constexpr int TSW = 60, W = 68;
+    __shared__ __align__(128) float xr[SEGS][5][W];
+    __shared__ __align__(8) unsigned long long xb[SEGS];
     __shared__ FastCoef s_coef;
     __shared__ int s_act;
-    if (threadIdx.x == 0) {
+    const int lane = threadIdx.x;
+    if (lane == 0) {
         double dt;
         s_act = ds.get(dt);
         if (s_act) s_coef = ds.fast_coef();
+        for (int q = 0; q < SEGS; q++) mbar_init(&xb[q], 1);
+        mbar_init_fence();
     }
     __syncthreads();
     const bool act = s_act != 0;
-    const int seg0 = (blockIdx.x * (NT / 32) + (threadIdx.x >> 5)) * SEGS;
-    const int row = blockIdx.y;
-    const int n = G.nx;
-    unsigned long long* wslot = out.slot();
-    float w = 0.0f;
-    Cell2 ahead;
-    if (seg0 * TSW < n) x_pair_load(G, src, row, seg0 * TSW, ahead);
-    for (int k = 0; k < SEGS; k++) {
-        const int s0 = (seg0 + k) * TSW;
-        if (s0 >= n) break;  // warp-uniform
-        const Cell2 m = ahead;
-        if (k + 1 < SEGS && s0 + TSW < n) x_pair_load(G, src, row, s0 + TSW, ahead);
-        w = fmaxf(w, x_pair_update<LIM>(P, dims, G, dst, row, s0, m, act, s_coef, wslot != nullptr));
+    const int n = G.nx, row = blockIdx.y;
+    const int k0 = blockIdx.x * SEGS;
+    const int kn = min(SEGS, (n + TSW - 1) / TSW - k0);  // segments of this warp (k0 < segments per row)
+    // segment k's window s0 - 2 .. s0 + 61 lies inside the row and its copy s0 - 4 .. s0 + 63 too
+    auto inside = [&](int k) { return k >= 1 && k * TSW + 64 <= n; };
+    const size_t rb = (size_t)row * G.pitch;
+    for (int i = 0; i < kn; i++) {
+        if (!inside(k0 + i)) continue;
+        if (lane == 0) mbar_expect_tx(&xb[i], 5 * W * 4);
+        __syncwarp();
+        if (lane < 5) bulk_load(xr[i][lane], src + (size_t)lane * G.fstride + rb + (k0 + i) * TSW - 4, W * 4, &xb[i]);
     }
-    if (wslot) block_max_to<NT>(wslot, w);
+    unsigned long long* wslot = out.slot();
+    const FastCoef cf = s_coef;
+    float w = 0.0f;
+    bool ok = true;
+    for (int i = 0; i < kn; i++) {
+        const int s0 = (k0 + i) * TSW;
+        Cell2 m;
+        if (inside(k0 + i)) {
+            ok = __all_sync(0xffffffffu, mbar_wait(&xb[i], 0));
+            if (!ok) {
+                if (lane == 0) {
+                    if (out.status) atomicOr(out.status, ST_TIMEOUT);
+                    for (int q = i; q < kn; q++)
+                        if (inside(k0 + q)) mbar_wait(&xb[q], 0, 100000000LL);
+                }
+                __syncwarp();
+                return;
+            }
+#pragma unroll
+            for (int f = 0; f < 5; f++) m.v[f].v = *reinterpret_cast<const float2*>(&xr[i][f][2 + 2 * lane]);
+        } else {
+            x_pair_load(G, src, row, s0, m);
+        }
+        w = fmaxf(w, x_pair_update<LIM>(P, dims, G, dst, row, s0, m, act, cf, wslot != nullptr));
+    }
+    if (wslot) {
+        w = warp_max(w);
+        if (lane == 0) atomic_max_nonneg(wslot, (double)w);
+    }
 }
 
 }  // namespace cg

@@ -13,6 +13,10 @@ CG_D uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shar
 CG_D void mbar_init(unsigned long long* bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
 }
+// Invalidates a barrier that has no phase pending, before it is initialised again.
+CG_D void mbar_inval(unsigned long long* bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 // Makes the initialised barriers visible to the copy engine; the caller follows with __syncthreads.
 CG_D void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 

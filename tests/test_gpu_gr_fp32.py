@@ -33,7 +33,7 @@ def l1_outside(got, want, mask):
 
 @pytest.mark.parametrize("above", [2.0, 0.0])
 def test_gr_fp32_accretion_vs_oracle(cg, oracle, above):
-    """Config-4 geometry at reduced size: [-10,10]^2 as [0,20]^2 with the hole at (10,10), M = 1,
+    """The accretion benchmark's geometry at reduced size: [-10,10]^2 as [0,20]^2 with the hole at (10,10), M = 1,
     excision r <= 2M, rho = 1 + 1% log-normal noise, p = 0.01; 6 steps, RK4 source on both sides."""
     n = 48
     s = accretion(n, 4)
@@ -54,7 +54,7 @@ def test_gr_fp32_accretion_vs_oracle(cg, oracle, above):
 
 
 def test_gr_fp32_long_accretion_stays_finite(cg):
-    """Config-4 geometry at 256^2 for 40 steps: after about a dozen steps the inflow next to the
+    """The accretion benchmark's geometry at 256^2 for 40 steps: after about a dozen steps the inflow next to the
     horizon reaches the reference's rootless recovery states (density floor, superluminal garbage
     velocities whose conserved values outgrow FP32's range); the FP32 path hands those to its FP64
     stage and keeps every cell and the CFL time step finite."""
