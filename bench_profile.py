@@ -36,6 +36,11 @@ def main():
     ap.add_argument("--subcycles", type=int, default=1, help="`adjoint` on a black-hole grid: RK source half-steps")
     ap.add_argument("--warm", type=int, default=0,
                     help="`step` only: steps run before the captured ones (evolved states)")
+    ap.add_argument("--c2p64-above", type=float, default=2.0,
+                    help="FP32 SR and black-hole grids: Lorentz factor above which a primitive recovery "
+                         "finishes in FP64 (0: every recovery)")
+    ap.add_argument("--shape", type=int, nargs=3, default=[256, 64, 1], metavar=("NT", "SEG", "CAP"),
+                    help="`batch`: tile shape (threads per block, Y rows per item, register cap)")
     a = ap.parse_args()
     sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
     import cosmos_gb300 as cg
@@ -48,7 +53,7 @@ def main():
         for k, sh in enumerate(shapes):
             b.set_prim(k, cases.riemann(sh, 1000 + k))
         b.run_begin(0.9, 1e30, 0.0, cg.MINBEE)
-        b.set_shape(128, 64, 1)
+        b.set_shape(*a.shape)
         b.run_steps(10 * a.launches)
         b.run_end()
         b.ctx.synchronize()
@@ -72,7 +77,8 @@ def main():
         dx = 20.0 / n
         bh = cg.BlackHoleSpacetime(1.0, 0.0, 10.0, 10.0, 0.0)
     bc = cg.BC_PERIODIC if a.system != cg.GR else cg.BC_TRANSMISSIVE
-    g = cg.Grid(a.system, (n, n), dx, 1.4 if a.system == 0 else 5.0 / 3.0, prec, bc, bh)
+    g = cg.Grid(a.system, (n, n), dx, 1.4 if a.system == 0 else 5.0 / 3.0, prec, bc, bh,
+                sr_c2p64_above=a.c2p64_above)
     g.set_prim(s)
     dt = 0.25 * dx
     if a.kernel == "sweep":
