@@ -793,13 +793,19 @@ def adjoint_measure(cg, ctx, n=2048, nsteps=100, every=10):
     rng = np.random.default_rng(78)
     target = p0[..., 0] * (1.0 + 0.05 * rng.standard_normal((n, n)))
     g = cg.Grid(cg.NEWTONIAN, (n, n), 1.0 / n, 1.4, cg.FP32, cg.BC_TRANSMISSIVE, ctx=ctx)
-    runs = []
-    for _ in range(3):
-        g.set_prim(p0)
-        runs.append(g.adjoint(target, nsteps, 0.9, 0.0, cg.MINBEE, checkpoint_every=every)[3])
+    runs = {}
+    for keep in (-1, 0):  # sweep inputs kept from the forward pass (default), or every earlier segment recomputed
+        g.set_adjoint_keep(keep)
+        runs[keep] = []
+        for _ in range(3):
+            g.set_prim(p0)
+            runs[keep].append(g.adjoint(target, nsteps, 0.9, 0.0, cg.MINBEE, checkpoint_every=every)[3])
     g.close()
-    fwd = statistics.median(r[0] for r in runs)
-    bwd = statistics.median(r[1] for r in runs)
+    fwd = statistics.median(r[0] for r in runs[-1])
+    bwd = statistics.median(r[1] for r in runs[-1])
+    fwd0 = statistics.median(r[0] for r in runs[0])
+    bwd0 = statistics.median(r[1] for r in runs[0])
+    seg_gb = every * 3 * n * n * 5 * 4 / 1e9
     # finite differences of the FP64 forward (same fixed dts) in one seeded direction
     m = 64
     q0 = cases.smooth_state((m, m), 5)
@@ -832,8 +838,12 @@ def adjoint_measure(cg, ctx, n=2048, nsteps=100, every=10):
     an = float(np.sum(grad * d))
     return {"grid": f"{n}x{n} FP32, seeded Riemann data", "steps": nsteps, "checkpoint_every": every,
             "forward_ms": fwd, "backward_ms": bwd, "adjoint_over_forward": bwd / fwd, "target": 3.0,
-            "what": "backward = recomputation of each checkpoint segment + the sweep adjoints, per forward "
-                    "pass of the same steps (graph-replayed, checkpoints stored)",
+            "what": f"backward = the sweep adjoints, every segment's sweep inputs kept from the forward pass "
+                    f"({nsteps // every} x {seg_gb:.1f} GB in HBM, the default keep budget of half the free "
+                    f"memory), per forward pass of the same steps",
+            "recompute": {"forward_ms": fwd0, "backward_ms": bwd0, "adjoint_over_forward": bwd0 / fwd0,
+                          "what": "keep budget 0: the last segment kept, every earlier one recomputed from its "
+                                  "checkpoint on a second stream while the following segment's adjoints run"},
             "fd_check": {"grid": f"{m}x{m} FP64 smooth data", "steps": nsteps, "h": h,
                          "rule": "h = 1e-6, 1e-7, ... until two successive central differences agree to 1e-5",
                          "fd_by_h": {f"{x:.0e}": v for x, v in zip(hs, fds)},

@@ -84,6 +84,7 @@ SIGNATURES = {
                                ctypes.POINTER(SolveResult)]),
     "cosmos_field_sums_noalloc": (_i, [_p, _i, _i, _i, _i, _sz, _p, _p]),
     "cosmos_grid_adjoint": (_i, [_p, ctypes.POINTER(SolveOpts), _i, _i, _p, _p, _p, _p, _p, _p]),
+    "cosmos_grid_set_adjoint_keep": (_i, [_p, ctypes.c_longlong]),
     "cosmos_amr_create": (_i, [_p, ctypes.POINTER(Params), ctypes.POINTER(_p)]),
     "cosmos_amr_create_level2": (_i, [_p, ctypes.POINTER(Params), ctypes.POINTER(_p)]),
     "cosmos_amr_get_level": (_i, [_p, _i, _p, _p]),

@@ -2,13 +2,17 @@
 // nsteps SLIC steps of a Newtonian grid (or an FP64 SR grid, or an FP64 black-hole grid with its RK
 // source half-steps), with checkpoints every `checkpoint_every` steps.
 //
-// Forward: the grid's own graph-replayed steps (device dt from the CFL rule, or the caller's dts),
-// the state copied to a checkpoint store before every segment and each step's dt logged.
-// Backward, segment by segment from the last: the segment is recomputed from its checkpoint with
-// the same sweep kernels and the same dts, keeping every sweep's input (the last segment keeps
-// them during the forward pass); the sweep adjoints then run in reverse order (X(dt/2) Y(dt)
-// X(dt/2) per 2D step, X(dt) per 1D step).  The next segment's recomputation overlaps the current
-// segment's adjoints on a second stream.
+// Forward: the grid's own steps (device dt from the CFL rule, or the caller's dts) with each
+// step's dt logged.  The last segments -- as many as fit in the keep budget (cosmos_grid_set_
+// adjoint_keep; by default half of the device memory free at the call, at least the last segment)
+// -- run with every sweep's input written to a store of its own (same kernels and device time
+// steps as the graph-replayed steps); the earlier ones run from the captured step graph with the
+// state copied to a checkpoint store before each segment.
+// Backward, segment by segment from the last: a kept segment's sweep inputs are in place; an
+// earlier segment is recomputed from its checkpoint with the same sweep kernels and dts, keeping
+// every sweep's input, on a second stream while the following segment's adjoints run.  The sweep
+// adjoints run in reverse order (X(dt/2) Y(dt) X(dt/2) per 2D step, X(dt) per 1D step).  The
+// gradient is the same bit for bit whatever the budget and the checkpoint interval.
 #include <algorithm>
 #include <climits>
 #include <cstddef>
@@ -40,6 +44,7 @@ struct Scratch {
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     cudaEvent_t rec_done[2] = {nullptr, nullptr}, adj_done[2] = {nullptr, nullptr};
     StepCtl* patched = nullptr;  // controller whose dt pointers point into this scratch
+    std::vector<cudaGraphExec_t> graphs;  // the kept segments' captured forward steps
     cudaError_t alloc(void** p, size_t bytes) {
         cudaError_t e = cudaMallocAsync(p, bytes, st);
         if (e == cudaSuccess) ptrs.push_back(*p);
@@ -53,6 +58,10 @@ struct Scratch {
         patched = nullptr;
     }
     ~Scratch() {
+        if (!graphs.empty()) {
+            cudaStreamSynchronize(st);  // no captured segment is still running when it is destroyed
+            for (cudaGraphExec_t x : graphs) cudaGraphExecDestroy(x);
+        }
         unpatch();
         for (void* p : ptrs) cudaFreeAsync(p, st);
         for (auto& e : ev)
@@ -99,10 +108,21 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
     Scratch sc;
     sc.st = g->ctx->stream;
     cudaStream_t st = sc.st;
-    char *ck, *seg, *adj;
+    // segments c >= ckeep keep their sweep inputs from the forward pass; the others are recomputed
+    const size_t seg_bytes = (size_t)K * spp * sbytes;
+    long long budget = g->adj_keep;
+    if (budget < 0) {
+        size_t fr = 0, tot = 0;
+        ACK(cudaMemGetInfo(&fr, &tot));
+        budget = (long long)(fr / 2);
+    }
+    const int nkeep = (int)std::max<long long>(1, std::min<long long>(nck, budget / (long long)seg_bytes));
+    const int ckeep = nck - nkeep;
+    char *ck, *seg = nullptr, *keep, *adj;
     double *d_target, *d_dts, *d_rows, *d_loss;
-    ACK(sc.alloc((void**)&ck, (size_t)nck * sbytes));
-    ACK(sc.alloc((void**)&seg, (size_t)2 * K * spp * sbytes));  // two segments: recompute one, reverse the other
+    ACK(sc.alloc((void**)&ck, (size_t)std::max(ckeep, 1) * sbytes));  // checkpoints of the recomputed segments (and 0)
+    if (ckeep > 0) ACK(sc.alloc((void**)&seg, 2 * seg_bytes));       // two segments: recompute one, reverse the other
+    ACK(sc.alloc((void**)&keep, (size_t)nkeep * seg_bytes));
     ACK(sc.alloc((void**)&adj, 2 * abytes));
     ACK(sc.alloc((void**)&d_target, ncell * sizeof(double)));
     ACK(sc.alloc((void**)&d_dts, nsteps * sizeof(double)));
@@ -131,28 +151,51 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
     const void* dtp[2] = {logp, fixp};
     sc.patched = g->ctl;
     ACK(cudaMemcpyAsync((char*)g->ctl + offsetof(StepCtl, dt_log), dtp, sizeof dtp, cudaMemcpyHostToDevice, st));
-    auto slot = [&](int c, int q) { return seg + ((size_t)(c & 1) * K * spp + q) * sbytes; };
+    // input of operation q of segment c: the keep store, or the recomputation store's half c & 1
+    auto slot = [&](int c, int q) {
+        return c >= ckeep ? keep + (size_t)(c - ckeep) * seg_bytes + (size_t)q * sbytes
+                          : seg + (size_t)(c & 1) * seg_bytes + (size_t)q * sbytes;
+    };
     for (int c = 0; c < nck; c++) {
-        ACK(cudaMemcpyAsync(ck + (size_t)c * sbytes, g->buf[g->cur], sbytes, cudaMemcpyDeviceToDevice, st));
         const int ns = std::min(K, nsteps - c * K);
-        if (c < nck - 1) {
+        if (c < ckeep) {
+            ACK(cudaMemcpyAsync(ck + (size_t)c * sbytes, g->buf[g->cur], sbytes, cudaMemcpyDeviceToDevice, st));
             if ((rc = cosmos_grid_run_steps(g, ns))) return rc;
             continue;
         }
-        // The last segment, reversed first, keeps every sweep's input in the segment store as it
-        // runs (same kernels and device time steps as the graph-replayed steps), so its reversal
-        // starts without a recomputation; the final state goes to the grid's other buffer.
-        ACK(cudaMemcpyAsync(slot(c, 0), g->buf[g->cur], sbytes, cudaMemcpyDeviceToDevice, st));
-        for (int s = 0; s < ns; s++) {
+        // a kept segment: its first input is the grid's state (c == ckeep) or the previous kept
+        // segment's last output; its own last output goes to the next segment, or for the last
+        // segment to the grid's other buffer
+        if (c == ckeep) ACK(cudaMemcpyAsync(slot(c, 0), g->buf[g->cur], sbytes, cudaMemcpyDeviceToDevice, st));
+        if (c == 0) ACK(cudaMemcpyAsync(ck, slot(c, 0), sbytes, cudaMemcpyDeviceToDevice, st));  // the gradient's state
+        // the segment's steps are captured into one graph and replayed once, so they run with the
+        // launch gaps of the graph-replayed steps
+        cudaGraph_t graph;
+        ACK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        set_capturing(true);
+        for (int s = 0; s < ns && !rc; s++) {
             std::vector<void*> outs(spp);
             for (int k = 0; k < spp; k++) {
                 const int q = s * spp + k + 1;
-                outs[k] = q < ns * spp ? (void*)slot(c, q) : g->buf[g->cur ^ 1];
+                outs[k] = q < ns * spp ? (void*)slot(c, q) : (c + 1 < nck ? (void*)slot(c + 1, 0) : g->buf[g->cur ^ 1]);
             }
-            if ((rc = enqueue_step_into(g, slot(c, s * spp), outs.data()))) return rc;
+            rc = enqueue_step_into(g, slot(c, s * spp), outs.data());
         }
-        g->cur ^= 1;
+        set_capturing(false);
+        const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+        if (ec == cudaSuccess && rc) cudaGraphDestroy(graph);
+        if (rc) return rc;
+        ACK(ec);
+        cudaGraphExec_t exec;
+        const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        ACK(ei);
+        sc.graphs.push_back(exec);
+        ACK(cudaGraphLaunch(exec, st));
+        // per step: the dt kernel, the operations, and a black-hole grid's CFL reduction
+        count_launch((unsigned)(ns * (1 + spp + (g->p.system == COSMOS_GR ? 1 : 0))));
     }
+    g->cur ^= 1;
     ACK(cudaEventRecord(sc.ev[1], st));
     sc.unpatch();  // the controller's dt pointers point into this call's scratch
 
@@ -228,10 +271,9 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
         ACK(cudaEventRecord(sc.rec_done[c & 1], rs));
         return COSMOS_OK;
     };
-    ACK(cudaEventRecord(sc.rec_done[(nck - 1) & 1], st));  // the last segment is in the store already
     for (int c = nck - 1; c >= 0; c--) {
-        if (c > 0 && (rc = recompute(c - 1))) return rc;
-        ACK(cudaStreamWaitEvent(st, sc.rec_done[c & 1], 0));
+        if (c > 0 && c - 1 < ckeep && (rc = recompute(c - 1))) return rc;
+        if (c < ckeep) ACK(cudaStreamWaitEvent(st, sc.rec_done[c & 1], 0));
         for (int q = nops_of(c) - 1; q >= 0; q--) {
             int axis;
             double dt;
@@ -284,5 +326,12 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
         ms[0] = f;
         ms[1] = b;
     }
+    return COSMOS_OK;
+}
+
+extern "C" int cosmos_grid_set_adjoint_keep(cosmos_grid* g, long long bytes) {
+    if (!g) return afail(COSMOS_EINVAL, "null grid");
+    if (bytes < -1) return afail(COSMOS_EINVAL, "keep budget must be -1 (automatic) or a byte count");
+    g->adj_keep = bytes;
     return COSMOS_OK;
 }

@@ -36,6 +36,8 @@ struct cosmos_grid {
     // black-hole grids with FP32 storage: metric tables built once at creation
     void* gr_mem;
     cg::GRTables grt;
+    // adjoint: device bytes for sweep inputs kept from the forward pass (-1: half the free memory)
+    long long adj_keep = -1;
 };
 
 namespace cg {

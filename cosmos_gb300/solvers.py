@@ -287,6 +287,12 @@ class Grid:
         check(load().cosmos_grid_field_sums(self.h, o.ctypes.data))
         return o
 
+    def set_adjoint_keep(self, nbytes):
+        """Device bytes adjoint() may use to keep sweep inputs from its forward pass (the last
+        checkpoint segments that fit are not recomputed); -1: half the free device memory (the
+        default), 0: the last segment only.  The gradient does not depend on it."""
+        check(load().cosmos_grid_set_adjoint_keep(self.h, int(nbytes)))
+
     def adjoint(self, target, nsteps, cfl, bias, limiter, checkpoint_every=10, dts=None, subcycles=1):
         """Gradient of L = 1/2 sum (rho_T - target)^2 after `nsteps` SLIC steps from the current
         state with respect to its primitives (dt of each step held fixed: `dts` if given, else the

@@ -218,7 +218,8 @@ int cosmos_batch_autotune(cosmos_batch* b, const char* cache_path, int* nt, int*
  * recovery's Newton iteration; lines of at least two cells) with
  * each step's dt held fixed: the caller's dts_in[nsteps] if non-NULL, else the CFL rule's dts
  * (o->cfl) of the forward run, which are returned in dts_out[nsteps] if non-NULL.  Checkpoints
- * every `checkpoint_every` steps; each segment is recomputed once.  target: ny*nx doubles (row
+ * every `checkpoint_every` steps; each segment whose sweep inputs were not kept from the forward
+ * pass (cosmos_grid_set_adjoint_keep) is recomputed once.  target: ny*nx doubles (row
  * major, the grid's rows); grad_prim: 5*nx*ny doubles in the layout of cosmos_grid_set_prim;
  * loss and ms (2 doubles: forward and backward milliseconds on the context's stream) may be NULL.
  * On return the grid holds the final state.  FP64 grids differentiate the reference-exact FP64
@@ -226,6 +227,12 @@ int cosmos_batch_autotune(cosmos_batch* b, const char* cache_path, int* nt, int*
 int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, int nsteps, int checkpoint_every,
                         const double* target, const double* dts_in, double* grad_prim, double* loss,
                         double* dts_out, double* ms);
+/* Device memory (bytes) cosmos_grid_adjoint may use to keep sweep inputs from its forward pass:
+ * the last checkpoint segments whose sweep inputs fit (always at least the last one) are not
+ * recomputed in the backward pass, the earlier ones are recomputed once from their checkpoints.
+ * -1 (the default): half of the device memory free when the call starts; 0: keep the last
+ * segment only.  The gradient is the same bit for bit whatever the budget. */
+int cosmos_grid_set_adjoint_keep(cosmos_grid* g, long long bytes);
 
 /* ---- Level-1 adaptive mesh refinement: EulerAMR::solveLevel1AMR / solve2DLevel1AMR
  * (AMR/EulerAMR.cpp:169-592) and RelativisticEulerAMR::solveLevel1AMR / solve2DLevel1AMR

@@ -64,15 +64,29 @@ def test_fp64_adjoint_matches_oracle_tlm_discontinuous(cg, oracle, shape, lim):
         check_vs_tlm(cg, oracle, p0, target, 5, 2, lim, bc, 1e-7, lim + 10 * bc)
 
 
-def test_checkpoint_interval_does_not_change_the_gradient(cg):
+def segment_bytes(shape, K, elem=8, ops=3):
+    """Device bytes of one checkpoint segment's sweep inputs (the library's padded layout)."""
+    pitch = -(-shape[1] // 64) * 64
+    fstride = -(-pitch * shape[0] // 64) * 64
+    return K * ops * fstride * 5 * elem
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_checkpoint_interval_and_keep_budget_do_not_change_the_gradient(cg, precision):
+    """Every checkpoint interval, and every keep budget: all segments' sweep inputs kept from the
+    forward pass (the default), the last segment only (each earlier one recomputed), and two."""
     p0 = cases.smooth_state((20, 24), 3)
     target = p0[..., 0] * 1.1
     grads = []
     for K in (1, 4, 11, 11 + 5):
-        g = grid(cg, p0)
-        _, gr, dts, _ = g.adjoint(target, 11, 0.8, 0.0, 2, checkpoint_every=K)
-        grads.append(gr)
+        for keep in (-1, 0, 2 * segment_bytes((20, 24), K, 8 if precision == 0 else 4)):
+            g = grid(cg, p0, precision)
+            g.set_adjoint_keep(keep)
+            _, gr, dts, _ = g.adjoint(target, 11, 0.8, 0.0, 2, checkpoint_every=K)
+            grads.append(gr)
     assert all(bit_equal(grads[0], x) for x in grads[1:])
+    if precision == 1:
+        return
     # the caller's dts reproduce the CFL run exactly, and the grid ends in the final state
     g = grid(cg, p0)
     loss2, gr2, dts2, _ = g.adjoint(target, 11, 0.8, 0.0, 2, checkpoint_every=4, dts=dts)

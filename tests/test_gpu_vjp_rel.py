@@ -32,6 +32,7 @@ def rel_grid(cg, system, p0, bc=0, precision=0, bh=None):
 def check(cg, oracle, host_adjoint, system, p0, target, dts, lim, bc, bh, bias=0.0, seed=0, sub=0):
     dx = 1.0 / p0.shape[-2]
     g = rel_grid(cg, system, p0, bc, bh=bh)
+    g.set_adjoint_keep(0)  # earlier segments recomputed (keeping them is checked bit for bit below)
     loss, grad, dts_out, _ = g.adjoint(target, len(dts) if dts is not None else 5, 0.6, bias, lim, checkpoint_every=3,
                                        dts=dts, subcycles=sub)
     if dts is None:
@@ -98,3 +99,18 @@ def test_relativistic_adjoint_rejects_fp32_grids(cg):
     q0 = gr_smooth_state((16,), 1)
     with pytest.raises(CosmosError):
         rel_grid(cg, 2, q0, precision=1, bh=HOLES[0]).adjoint(q0[..., 0], 2, 0.5, 0.0, 1)
+
+
+def test_keep_budget_does_not_change_the_relativistic_gradient(cg):
+    """Sweep inputs kept from the forward pass (the default) or recomputed from the checkpoints:
+    the same gradient bit for bit, SR and black hole with source half-steps."""
+    from conftest import bit_equal
+    p0 = sr_smooth_state((8, 10), 4)
+    q0 = gr_smooth_state((8, 10), 5)
+    for system, s0, bh, sub in ((1, p0, None, 0), (2, q0, HOLES[1], 1)):
+        out = []
+        for keep in (-1, 0):
+            g = rel_grid(cg, system, s0, bh=bh)
+            g.set_adjoint_keep(keep)
+            out.append(g.adjoint(s0[..., 0] * 1.05, 5, 0.5, 0.0, 1, checkpoint_every=2, subcycles=sub))
+        assert bit_equal(out[0][1], out[1][1]) and out[0][0] == out[1][0]
