@@ -85,11 +85,36 @@ struct AdjFlux {
     //   ub_mn += gb_rho + vnb / rho,  ub_E += gb_E v_n + (gamma - 1) pb
     template <int AX>
     CG_D void vjp(const V* u, const V* gb, V* ub) const {
-        const V inv = vrcp(u[0]);
-        const V v0 = vmul(u[1], inv), v1 = vmul(u[2], inv), v2 = vmul(u[3], inv);
+        vjp_p<AX>(u, prep(u), gb, ub);
+    }
+    // The quantities flux and vjp share at one state: 1 / rho, the velocity, |v|^2 and p.
+    struct Prep {
+        V inv, v0, v1, v2, vv, p;
+    };
+    CG_D Prep prep(const V* u) const {
+        Prep q;
+        q.inv = vrcp(u[0]);
+        q.v0 = vmul(u[1], q.inv);
+        q.v1 = vmul(u[2], q.inv);
+        q.v2 = vmul(u[3], q.inv);
+        q.vv = vfma(q.v0, q.v0, vfma(q.v1, q.v1, vmul(q.v2, q.v2)));
+        q.p = vfma(ng1h, vmul(u[0], q.vv), vmul(g1, u[4]));
+        return q;
+    }
+    // flux from a state's prep (p from |v|^2: the same value as flux's to rounding)
+    template <int AX>
+    CG_D void flux_p(const V* u, const Prep& q, V* f) const {
+        const V vn = AX == 0 ? q.v0 : q.v1;
+        f[0] = u[1 + AX];
+        f[1] = AX == 0 ? vfma(u[1], vn, q.p) : vmul(u[1], vn);
+        f[2] = AX == 1 ? vfma(u[2], vn, q.p) : vmul(u[2], vn);
+        f[3] = vmul(u[3], vn);
+        f[4] = vmul(vadd(u[4], q.p), vn);
+    }
+    template <int AX>
+    CG_D void vjp_p(const V* u, const Prep& q, const V* gb, V* ub) const {
+        const V inv = q.inv, v0 = q.v0, v1 = q.v1, v2 = q.v2, vv = q.vv, p = q.p;
         const V vn = AX == 0 ? v0 : v1;
-        const V vv = vfma(v0, v0, vfma(v1, v1, vmul(v2, v2)));
-        const V p = vfma(ng1h, vmul(u[0], vv), vmul(g1, u[4]));
         const V pb = vfma(gb[4], vn, gb[1 + AX]);
         const V vnb = vfma(gb[4], vadd(u[4], p), vfma(gb[3], u[3], vfma(gb[2], u[2], vmul(gb[1], u[1]))));
         const V ngp = vmul(ng1, pb);    // -(gamma - 1) pb
@@ -128,9 +153,12 @@ CG_D V limiter_d(const AdjSlope<V>& A, V r, V& d) {
         const V vl = vmul(vmul(two, r), iop);
         val = vsel_lt(xr, vl, xr, vl);
         der = vsel_lt(xr, vl, dxr, vmul(two, vmul(iop, iop)));
-    } else {  // MinBee
-        val = vsel_lt(r, one, r, vsel_lt(xr, one, xr, one));
-        der = vsel_lt(r, one, one, vsel_lt(xr, one, dxr, zero));
+    } else {  // MinBee: r below 1 (xr above 1), xr below 1 (r above 1); 0 for r < 0
+        // value: max(min(r, xr), 0) is the same selection (xr >= 1 >= r for 0 <= r <= 1, xr < 1 < r
+        // above); derivative on the branch taken: 1, dxr, or 0 (r < 0, and at r = 1, where the forward
+        // takes the constant 1)
+        d = vsel_lt(r, one, vsel_lt(r, zero, zero, one), vsel_lt(xr, one, dxr, zero));
+        return vmax(vmin(r, xr), zero);
     }
     d = vsel_lt(r, zero, zero, der);
     return vsel_lt(r, zero, zero, val);
@@ -207,8 +235,9 @@ template <class V, int AX>
 CG_D void adj_force_vjp(const AdjFlux<V>& F, const V* L, const V* R, V c, V d, const V* Fb, V* Lb, V* Rb) {
     const V h = bcv<V>(0.5);
     V fL[5], fR[5], us[5];
-    F.template flux<AX>(L, fL);
-    F.template flux<AX>(R, fR);
+    const typename AdjFlux<V>::Prep qL = F.prep(L), qR = F.prep(R);
+    F.template flux_p<AX>(L, qL, fL);
+    F.template flux_p<AX>(R, qR, fR);
 #pragma unroll
     for (int k = 0; k < 5; k++) us[k] = vmul(h, vfma(d, vsub(fL[k], fR[k]), vadd(L[k], R[k])));
     V usb[5], fsb[5];
@@ -228,8 +257,8 @@ CG_D void adj_force_vjp(const AdjFlux<V>& F, const V* L, const V* R, V c, V d, c
         fLb[k] = vadd(e, f);
         fRb[k] = vsub(f, e);
     }
-    F.template vjp<AX>(L, fLb, Lb);
-    F.template vjp<AX>(R, fRb, Rb);
+    F.template vjp_p<AX>(L, qL, fLb, Lb);
+    F.template vjp_p<AX>(R, qR, fRb, Rb);
 }
 
 // Coefficients of one sweep, formed on the host in both precisions (an FP64 divide per thread
