@@ -872,7 +872,8 @@ def measure_rel_adjoint(cg, ctx, sr_n=2048, sr_steps=2, gr_n=1024, gr_steps=1):
     g.close()
     out["gr"] = {"grid": f"{gr_n}x{gr_n} FP64 accretion, 1 subcycle", "steps": gr_steps, "forward_ms": ms[0],
                  "backward_ms": ms[1], "adjoint_over_forward": ms[1] / ms[0], "finite": bool(np.isfinite(grad).all())}
-    out["what"] = "gather-form vector-Jacobian products in dual numbers (FP64), recomputation per checkpoint"
+    out["what"] = ("gather-form vector-Jacobian products in dual numbers (FP64); every step's sweep inputs kept "
+                   "from the forward pass (the default keep budget)")
     return out
 
 
