@@ -18,8 +18,9 @@
 // The limiter is differentiated piecewise (its derivative on the branch the forward takes; the
 // clamped differences carry no derivative), as a dual-number evaluation of the same code would.
 //
-// Line tiles: P positions along the sweep axis (TS = P - 8 updated cells plus a 4-cell halo on each
-// side) times W lines; one thread per position, five barrier-separated phases in shared memory:
+// Line tiles: P positions along the sweep axis (P - 6 updated cells and a 3-cell halo on each side,
+// 4 where a tile holds a line end: AdjTiles) times W lines; one thread per position, five
+// barrier-separated phases in shared memory:
 //   0 store state and Ubar' (loaded while the previous tile was computed)
 //   1 half-step evolution (keeping each cell's slope and reverse factors)
 //   2 FORCE reverse per face   3 half-step reverse per cell   4 gather per updated cell.
@@ -261,22 +262,40 @@ CG_D void adj_force_vjp(const AdjFlux<V>& F, const V* L, const V* R, V c, V d, c
     F.template vjp_p<AX>(R, qR, fRb, Rb);
 }
 
-// Coefficients of one sweep, formed on the host in both precisions (an FP64 divide per thread
-// would dominate the FP32 kernel: GB300's FP64 rate is 1/64 of FP32).
+// Coefficients of one sweep in both precisions, formed once per sweep (on the host, or by
+// adjoint_coef_kernel from the device's dts), not per thread: an FP64 divide per thread would
+// dominate the FP32 kernel (GB300's FP64 rate is 1/64 of FP32).
 template <class T>
 struct AdjCoef {
     T g1, gam, w, d, c, hs;  // gamma - 1, gamma, bias, dt/dx, dx/dt, dt/(2 dx)
     T ca, cb, w1m, w1p;      // (1 + w)/2, (1 - w)/2, 1 - w, 1 + w
 };
+struct AdjCoefs {
+    AdjCoef<float> f;
+    AdjCoef<double> d;
+};
+CG_HD AdjCoefs adj_coefs(double dt, double dx, double gam, double w) {
+    const AdjCoef<double> D{gam - 1.0,       gam,   w,       dt / dx, dx / dt, 0.5 * (dt / dx),
+                            0.5 * (1.0 + w), 0.5 * (1.0 - w), 1.0 - w, 1.0 + w};
+    const AdjCoef<float> F{(float)D.g1, (float)D.gam, (float)D.w,  (float)D.d,   (float)D.c,
+                           (float)D.hs, (float)D.ca,  (float)D.cb, (float)D.w1m, (float)D.w1p};
+    return AdjCoefs{F, D};
+}
 struct AdjSweepParams {
     Geom G;
     double dx, dt, bias, gamma;
     AdjCoef<float> cf;
     AdjCoef<double> cd;
-    const void* state;     // sweep input in storage precision (FP64 primitives or FP32 conserved)
-    const void* ubar_out;  // adjoint of the sweep output (T, conserved SoA, same layout)
-    void* ubar_in;         // adjoint of the sweep input (written)
+    const AdjCoefs* coefp;  // non-null: the coefficients in device memory, in place of cf / cd
+    const void* state;      // sweep input in storage precision (FP64 primitives or FP32 conserved)
+    const void* ubar_out;   // adjoint of the sweep output (T, conserved SoA, same layout)
+    void* ubar_in;          // adjoint of the sweep input (written)
 };
+
+// The coefficients of every sweep of `nsteps` steps from the forward pass's dts (device memory):
+// sweep m of step s (m = 0..nsw - 1; dt/2 for the X sweeps of a 2D step) at out[s * nsw + m].
+__global__ void adjoint_coef_kernel(const double* dts, int nsteps, int nsw, double dx, double gam, double w,
+                                    AdjCoefs* out);
 
 // Transmissive mirror (exact for up to two cells out) or periodic wrap, clamped into the line for
 // the positions further out that only feed discarded halo work.
@@ -311,13 +330,43 @@ CG_D void st_lanes(float* p, size_t q0, size_t q1, bool vec, bool two, f2 v) {
     }
 }
 
+// Tiles of P positions along a line of n cells.  An interior cell's adjoint gathers the
+// contributions of its two neighbours, so a tile updates positions 3 .. P - 4 (P - 6 cells) and
+// starts 3 cells before its first one; a cell within two of a line end also gathers from the ghost
+// position two away, so it is updated only at positions 4 .. P - 5.  Tile 0 starts at cell -4;
+// the tiles cover cells 0 .. n - 3 this way, and the last two cells join the last tile where they
+// sit within its position P - 5, else one more tile (starting at cell n - 6) updates them.
+struct AdjTiles {
+    int n, P;
+    CG_HD int first(int ts) const { return ts == 0 ? 0 : (P - 7) + (ts - 1) * (P - 6); }
+    CG_HD int start(int ts) const { return ts == 0 ? -4 : first(ts) - 3; }
+    CG_HD int regular() const {
+        const int m = n - 2;
+        return 1 + (m > P - 7 ? (m - (P - 7) + (P - 6) - 1) / (P - 6) : 0);
+    }
+    CG_HD bool extra() const { return n - 1 - start(regular() - 1) > P - 5; }
+    CG_HD int count() const { return regular() + (extra() ? 1 : 0); }
+    // the updated cells [lo, hi) and the start cell s (at position 0) of tile ts
+    CG_HD void range(int ts, int& lo, int& hi, int& s) const {
+        const int r = regular();
+        if (ts < r) {
+            lo = first(ts);
+            s = start(ts);
+            hi = ts < r - 1 ? first(ts + 1) : (extra() ? n - 2 : n);
+        } else {
+            lo = n - 2;
+            hi = n;
+            s = n - 6;
+        }
+    }
+};
+
 template <class V, class S, bool PRIM, int AX, int LIM, int P, int W>
 __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 512 / (P * W) : (sizeof(V) == 4 ? 3 : 1))))
     adjoint_sweep_kernel(AdjSweepParams a) {
     using T = typename Lane<V>::S;
     constexpr int NL = Lane<V>::N;
     static_assert(!PRIM || NL == 1, "primitive storage is the FP64 one-line path");
-    constexpr int TS = P - 8;
     constexpr int NW = P * W;
     extern __shared__ __align__(16) unsigned char adj_smem[];
     V* sA = (V*)adj_smem;   // [5]  state
@@ -330,7 +379,8 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
     const int across = AX == 0 ? threadIdx.y : threadIdx.x;
     const int n = AX == 0 ? G.nx : G.ny;
     const int nl = AX == 0 ? G.ny : G.nx;
-    const int ntile_s = (n + TS - 1) / TS;             // tiles along the sweep axis
+    const AdjTiles tiles{n, P};
+    const int ntile_s = tiles.count();                 // tiles along the sweep axis
     const int ntiles = ntile_s * ((nl + W * NL - 1) / (W * NL));
     const bool per = G.bc == 1;
     // shared index of (across, position): positions contiguous for X, lines contiguous for Y
@@ -339,8 +389,8 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
         return AX == 0 ? (size_t)line * G.pitch + pos : (size_t)pos * G.pitch + line;
     };
     AdjCoef<T> K;
-    if constexpr (sizeof(T) == 4) K = a.cf;
-    else K = a.cd;
+    if constexpr (sizeof(T) == 4) K = a.coefp ? a.coefp->f : a.cf;
+    else K = a.coefp ? a.coefp->d : a.cd;
     const AdjFlux<V> F{bcv<V>(K.g1), bcv<V>(-K.g1), bcv<V>(T(-0.5) * K.g1)};
     const AdjSlope<V> Sl{bcv<V>(K.ca), bcv<V>(K.cb), bcv<V>(K.w1m), bcv<V>(K.w1p)};
     const V d = bcv<V>(K.d), c = bcv<V>(K.c), hs = bcv<V>(K.hs);
@@ -349,10 +399,10 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
     const T* ubo = (const T*)a.ubar_out;
     const int me = si(along);
 
-    // This thread's place in tile t: position k along the sweep, lines l0 and l1 (= l0 when the
-    // second lane has no line of its own).
+    // This thread's place in tile t: position k along the sweep, the tile's updated cells
+    // [lo, hi), lines l0 and l1 (= l0 when the second lane has no line of its own).
     struct Place {
-        int k, l0, l1;
+        int k, lo, hi, l0, l1;
         bool lok, two, vec;
     };
     auto place = [&](int t) {
@@ -362,7 +412,9 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
         q.two = NL == 2 && q.l0 + 1 < nl;
         q.vec = AX == 1 && q.two;  // adjacent columns: one 8-byte access
         q.l1 = q.two ? q.l0 + 1 : q.l0;
-        q.k = (t % ntile_s) * TS - 4 + along;
+        int s0;
+        tiles.range(t % ntile_s, q.lo, q.hi, s0);
+        q.k = s0 + along;
         return q;
     };
     // Inputs at a place, as stored (FP64: primitives), fetched one tile ahead into registers.
@@ -485,7 +537,7 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
         }
         __syncthreads();
         // ---- 4: gather for the updated cells
-        if (lok && along >= 4 && along < 4 + TS && k < n) {
+        if (lok && k >= q.lo && k < q.hi) {
             V acc[5];
 #pragma unroll
             for (int f = 0; f < 5; f++) acc[f] = ub_own[f];
@@ -601,7 +653,6 @@ template <class V, class S, bool PRIM, int AX, int LIM>
 cudaError_t launch_adjoint_sweep_t(const AdjSweepParams& a, cudaStream_t st) {
     constexpr int P = AX == 0 ? (Lane<V>::N == 2 ? 128 : 256) : 64;
     constexpr int W = AX == 0 ? 1 : 4;
-    constexpr int TS = P - 8;
     constexpr int LB = W * Lane<V>::N;  // lines per block
     const size_t smem = (size_t)45 * P * W * sizeof(V);
     auto kern = adjoint_sweep_kernel<V, S, PRIM, AX, LIM, P, W>;
@@ -618,7 +669,7 @@ cudaError_t launch_adjoint_sweep_t(const AdjSweepParams& a, cudaStream_t st) {
     }
     const Geom& G = a.G;
     const int n = AX == 0 ? G.nx : G.ny, nl = AX == 0 ? G.ny : G.nx;
-    const long long ntiles = (long long)((n + TS - 1) / TS) * ((nl + LB - 1) / LB);
+    const long long ntiles = (long long)AdjTiles{n, P}.count() * ((nl + LB - 1) / LB);
     const int blocks = (int)std::min<long long>(ntiles, resident);
     dim3 block = AX == 0 ? dim3(P, W) : dim3(W, P);
     kern<<<blocks, block, smem, st>>>(a);

@@ -203,13 +203,28 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
     int cur = 0;
     ACK(fp64 ? launch_adjoint_loss_exact(G0, g->buf[g->cur], d_target, adj, d_rows, d_loss, st)
              : launch_adjoint_loss_fast(G0, g->buf[g->cur], d_target, adj, d_rows, d_loss, st));
+    // The dts of the forward pass: a recomputation (and the relativistic adjoints) take them as
+    // launch arguments, so the host waits for them here.  A Newtonian run that keeps every
+    // segment reads its sweeps' coefficients from device memory instead, so its backward pass is
+    // queued behind the forward pass with no wait; the forward's status is checked at the end.
+    const bool devdt = !rel && ckeep == 0;
     std::vector<double> dts(nsteps);
-    ACK(cudaMemcpyAsync(dts.data(), d_dts, nsteps * sizeof(double), cudaMemcpyDeviceToHost, st));
     StepCtl h;
-    ACK(cudaMemcpyAsync(&h, g->ctl, sizeof h, cudaMemcpyDeviceToHost, st));
-    ACK(cudaStreamSynchronize(st));  // the recomputation needs the dts on the host
-    if (h.status & ST_NONFINITE) return afail(COSMOS_ENONFINITE, "non-finite or non-positive time step in the forward run");
-    if (h.it != nsteps) return afail(COSMOS_ESTATE, "the forward run stopped after " + std::to_string(h.it) + " steps");
+    AdjCoefs* d_coefs = nullptr;
+    auto check_forward = [&]() -> int {
+        ACK(cudaMemcpyAsync(dts.data(), d_dts, nsteps * sizeof(double), cudaMemcpyDeviceToHost, st));
+        ACK(cudaMemcpyAsync(&h, g->ctl, sizeof h, cudaMemcpyDeviceToHost, st));
+        ACK(cudaStreamSynchronize(st));
+        if (h.status & ST_NONFINITE) return afail(COSMOS_ENONFINITE, "non-finite or non-positive time step in the forward run");
+        if (h.it != nsteps) return afail(COSMOS_ESTATE, "the forward run stopped after " + std::to_string(h.it) + " steps");
+        return COSMOS_OK;
+    };
+    if (devdt) {
+        ACK(sc.alloc((void**)&d_coefs, (size_t)nsteps * nsw * sizeof(AdjCoefs)));
+        ACK(launch_adjoint_coefs(d_dts, nsteps, nsw, g->p.dx, g->p.gamma, o->bias, d_coefs, st));
+    } else if ((rc = check_forward())) {
+        return rc;
+    }
 
     // ---- backward, one checkpoint segment at a time
     SweepArgs fa = base_args(g);
@@ -222,6 +237,7 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
     ap.dx = g->p.dx;
     ap.bias = o->bias;
     ap.gamma = g->p.gamma;
+    ap.coefp = nullptr;
     const double bh[5] = {g->p.bh_mass, g->p.bh_spin, g->p.bh_x, g->p.bh_y, g->p.bh_z};
     // The recomputation of segment c - 1 (forward sweeps, on the context's second stream) runs
     // while the sweep adjoints of segment c run on the compute stream; the two segments use
@@ -271,12 +287,23 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
         ACK(cudaEventRecord(sc.rec_done[c & 1], rs));
         return COSMOS_OK;
     };
-    for (int c = nck - 1; c >= 0; c--) {
-        if (c > 0 && c - 1 < ckeep && (rc = recompute(c - 1))) return rc;
-        if (c < ckeep) ACK(cudaStreamWaitEvent(st, sc.rec_done[c & 1], 0));
+    // the sweep adjoints of segment c in reverse order, on `st`
+    auto reverse = [&](int c) -> int {
         for (int q = nops_of(c) - 1; q >= 0; q--) {
             int axis;
-            double dt;
+            double dt = 0.0;
+            if (devdt) {  // Newtonian: the sweeps only; coefficients from device memory
+                const int m = q % spp;
+                axis = nsw == 3 && m == 1 ? 1 : 0;
+                ap.G.axis = axis;
+                ap.coefp = d_coefs + (size_t)(c * K + q / spp) * nsw + m;
+                ap.state = slot(c, q);
+                ap.ubar_out = adj + (size_t)cur * abytes;
+                ap.ubar_in = adj + (size_t)(cur ^ 1) * abytes;
+                ACK(fp64 ? launch_adjoint_sweep_exact(ap, o->limiter, st) : launch_adjoint_sweep_fast(ap, o->limiter, st));
+                cur ^= 1;
+                continue;
+            }
             if (op_of(c, q, axis, dt)) {
                 ACK(launch_adjoint_rel_rk(G0, g->p.gamma, bh, g->p.dx, dt, slot(c, q), adj + (size_t)cur * abytes,
                                           adj + (size_t)(cur ^ 1) * abytes, st));
@@ -286,13 +313,9 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
             ap.G.axis = axis;
             ap.dt = dt;
             {
-                const double gam = g->p.gamma, dx = g->p.dx;
-                const double w = o->bias;
-                ap.cd = AdjCoef<double>{gam - 1.0, gam,          w,       dt / dx, dx / dt, 0.5 * (dt / dx),
-                                        0.5 * (1.0 + w), 0.5 * (1.0 - w), 1.0 - w, 1.0 + w};
-                const AdjCoef<double>& D = ap.cd;
-                ap.cf = AdjCoef<float>{(float)D.g1, (float)D.gam, (float)D.w,   (float)D.d,   (float)D.c,
-                                       (float)D.hs, (float)D.ca,  (float)D.cb,  (float)D.w1m, (float)D.w1p};
+                const AdjCoefs cs = adj_coefs(dt, g->p.dx, g->p.gamma, o->bias);
+                ap.cd = cs.d;
+                ap.cf = cs.f;
             }
             ap.state = slot(c, q);
             ap.ubar_out = adj + (size_t)cur * abytes;
@@ -304,6 +327,34 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
                 ACK(fp64 ? launch_adjoint_sweep_exact(ap, o->limiter, st) : launch_adjoint_sweep_fast(ap, o->limiter, st));
             cur ^= 1;
         }
+        return COSMOS_OK;
+    };
+    for (int c = nck - 1; c >= 0; c--) {
+        if (c > 0 && c - 1 < ckeep && (rc = recompute(c - 1))) return rc;
+        if (c < ckeep) ACK(cudaStreamWaitEvent(st, sc.rec_done[c & 1], 0));
+        if (c == nck - 1) {  // the first segment reversed launches at once (the device waits for it)
+            if ((rc = reverse(c))) return rc;
+            ACK(cudaEventRecord(sc.adj_done[c & 1], st));
+            continue;
+        }
+        // later segments are captured into one graph each while the device runs the previous
+        // ones, and replayed once: no launch gaps between their kernels beyond the graph's own
+        cudaGraph_t graph;
+        ACK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        set_capturing(true);
+        rc = reverse(c);
+        set_capturing(false);
+        const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+        if (ec == cudaSuccess && rc) cudaGraphDestroy(graph);
+        if (rc) return rc;
+        ACK(ec);
+        cudaGraphExec_t exec;
+        const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        ACK(ei);
+        sc.graphs.push_back(exec);
+        ACK(cudaGraphLaunch(exec, st));
+        count_launch((unsigned)nops_of(c));
         ACK(cudaEventRecord(sc.adj_done[c & 1], st));
     }
     // ---- gradient with respect to the initial primitives
@@ -313,6 +364,7 @@ extern "C" int cosmos_grid_adjoint(cosmos_grid* g, const cosmos_solve_opts* o, i
         ACK(fp64 ? launch_adjoint_grad_exact(G0, g->p.gamma, ck, adj + (size_t)cur * abytes, g->staging, st)
                  : launch_adjoint_grad_fast(G0, g->p.gamma, ck, adj + (size_t)cur * abytes, g->staging, st));
     ACK(cudaEventRecord(sc.ev[2], st));
+    if (devdt && (rc = check_forward())) return rc;  // the forward's dts and status, read only now
     ACK(cudaMemcpyAsync(grad_prim, g->staging, ncell * 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
     double lv = 0.0;
     ACK(cudaMemcpyAsync(&lv, d_loss, sizeof lv, cudaMemcpyDeviceToHost, st));

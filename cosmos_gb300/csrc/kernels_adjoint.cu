@@ -22,4 +22,20 @@ cudaError_t launch_adjoint_grad_exact(const Geom& G, double gamma, const void* s
     return launch_adjoint_grad_t<double, double, true>(G, gamma, state, ubar, grad, st);
 }
 
+__global__ void adjoint_coef_kernel(const double* dts, int nsteps, int nsw, double dx, double gam, double w,
+                                    AdjCoefs* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsteps * nsw) return;
+    const int m = i % nsw;
+    const double d = dts[i / nsw];
+    out[i] = adj_coefs(nsw == 3 && m != 1 ? 0.5 * d : d, dx, gam, w);
+}
+cudaError_t launch_adjoint_coefs(const double* dts, int nsteps, int nsw, double dx, double gamma, double bias,
+                                 AdjCoefs* out, cudaStream_t st) {
+    count_launch();
+    const int n = nsteps * nsw;
+    adjoint_coef_kernel<<<(n + 127) / 128, 128, 0, st>>>(dts, nsteps, nsw, dx, gamma, bias, out);
+    return cudaGetLastError();
+}
+
 }  // namespace cg

@@ -157,6 +157,10 @@ cudaError_t launch_batch_exact(const BatchLaunch& L);
 
 // ---- sweep adjoint (adjoint_kernels.cuh); _exact: FP64 primitive storage, _fast: FP32 conserved
 struct AdjSweepParams;
+struct AdjCoefs;
+// the adjoint coefficients of every sweep from the forward pass's dts (kernels_adjoint.cu)
+cudaError_t launch_adjoint_coefs(const double* dts, int nsteps, int nsw, double dx, double gamma, double bias,
+                                 AdjCoefs* out, cudaStream_t st);
 cudaError_t launch_adjoint_sweep_exact(const AdjSweepParams& a, int lim, cudaStream_t st);
 cudaError_t launch_adjoint_sweep_fast(const AdjSweepParams& a, int lim, cudaStream_t st);
 cudaError_t launch_adjoint_loss_exact(const Geom& G, const void* state, const double* target, void* ubar,
