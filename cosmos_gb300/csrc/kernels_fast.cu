@@ -51,15 +51,20 @@ cudaError_t run_fast(const SweepArgs& a) {
         if (a.order == 2 && !MASKED) {
             const int segs = (G.nx + 59) / 60;
             dim3 grid((segs + kXPairSegs - 1) / kXPairSegs, G.ny);
-            sweep_x_ring_kernel<LIM, kXPairSegs, kXRingMinBlocks><<<grid, 32, 0, a.stream>>>(pol.P, G.dims, G, src, dst,
-                                                                                        a.ds, a.out);
+            if (a.out.slot_set())
+                sweep_x_ring_kernel<LIM, kXPairSegs, kXRingMinBlocks, true><<<grid, 32, 0, a.stream>>>(
+                    pol.P, G.dims, G, src, dst, a.ds, a.out);
+            else
+                sweep_x_ring_kernel<LIM, kXPairSegs, kXRingMinBlocks, false><<<grid, 32, 0, a.stream>>>(
+                    pol.P, G.dims, G, src, dst, a.ds, a.out);
             return cudaSuccess;
         }
         dim3 grid((G.nx + kXThreads - 3) / (kXThreads - 2), G.ny);
         if (a.order == 2) sweep_x_own_kernel<Pol, 2, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
         else sweep_x_own_kernel<Pol, 1, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
     } else if (a.order == 2 && !MASKED) {
-        auto kernel = sweep_y_ring_kernel<LIM, kYPairThreads, kYRingRows, kYRingMinBlocks>;
+        auto kernel = a.out.slot_set() ? sweep_y_ring_kernel<LIM, kYPairThreads, kYRingRows, kYRingMinBlocks, true>
+                                       : sweep_y_ring_kernel<LIM, kYPairThreads, kYRingRows, kYRingMinBlocks, false>;
         const int seg = y_ring_seg((const void*)kernel, G.nx, G.ny);
         dim3 grid((G.nx + 2 * kYPairThreads - 1) / (2 * kYPairThreads), (G.ny + seg - 1) / seg);
         kernel<<<grid, kYPairThreads, 0, a.stream>>>(pol.P, G.dims, G, src, dst, a.ds, a.out, seg);

@@ -42,6 +42,7 @@ struct SweepOut {
     int* status;               // non-null: OR status bits into it
     const unsigned char* mask; // optional per-cell update mask (AMR masked steps)
     CG_D unsigned long long* slot() const { return ws_ctl ? &ws_ctl->smax[ws_ctl->it & 1] : smax; }
+    CG_HD bool slot_set() const { return ws_ctl != nullptr || smax != nullptr; }  // a reduction is wanted
 };
 
 template <class Pol>

@@ -112,53 +112,68 @@ CG_D void x_pair_load(const Geom& G, const float* __restrict__ src, int row, int
     }
 }
 
-// Neighbour cells, the next cell's left face state and the previous pair's right-face flux cross
-// lanes by warp shuffles (no shared memory, no block barrier); lanes 1..30 update and store their
-// two cells (60 per segment).  All 32 lanes call it together.  Returns the lane's wavespeed
-// maximum over its stored cells when want_w.
+// The arithmetic of one X segment: neighbour cells, the next cell's left face state and the
+// previous pair's right-face flux cross lanes by warp shuffles (no shared memory, no block
+// barrier); nc receives the lane's two updated cells.  All 32 lanes call it together.
 template <int LIM>
-CG_D float x_pair_update(const NewtonFastParams& P, int dims, const Geom& G, float* __restrict__ dst, int row, int s0,
-                         const Cell2& m, bool act, const FastCoef& cf, bool want_w) {
+CG_D void x_pair_compute(const NewtonFastParams& P, const Cell2& m, const FastCoef& cf, Cell2& nc) {
     constexpr unsigned FULL = 0xffffffffu;
+    f2 l[5], r[5];
+#pragma unroll
+    for (int f = 0; f < 5; f++) {
+        l[f].v = make_float2(__shfl_up_sync(FULL, m.v[f].v.y, 1), m.v[f].v.x);
+        r[f].v = make_float2(m.v[f].v.y, __shfl_down_sync(FULL, m.v[f].v.x, 1));
+    }
+    f2 L[5], R[5];
+    nf_recon<0, LIM>(P, l, m.v, r, cf.half_dtdx, L, R);
+    f2 Rn[5];  // left face states of the cells right of this lane's two
+#pragma unroll
+    for (int f = 0; f < 5; f++) Rn[f].v = make_float2(L[f].v.y, __shfl_down_sync(FULL, L[f].v.x, 1));
+    f2 Fr[5], Fl[5];
+    const Force4Coef c4 = force4_coef(cf);
+    nf_force4<0>(P, R, Rn, c4.dtdx, c4.dxdt, Fr);
+#pragma unroll
+    for (int f = 0; f < 5; f++) Fl[f].v = make_float2(__shfl_up_sync(FULL, Fr[f].v.y, 1), Fr[f].v.x);
+    nf_update(c4.q_dtdx, m.v, Fl, Fr, nc.v);
+}
+
+// Lanes 1..30 store their two cells of the segment at s0 (60 per segment) and, when WS, return
+// their wavespeed maximum (0 otherwise).  `full`: every lane's two cells lie inside the row (no
+// per-lane bound checks).
+template <bool WS>
+CG_D float x_pair_store(const NewtonFastParams& P, int dims, const Geom& G, float* __restrict__ dst, int row, int s0,
+                        const Cell2& nc, bool full) {
     const int lane = threadIdx.x & 31;
     const int n = G.nx;
     const int p0 = s0 - 2 + 2 * lane;
-    const size_t rb = (size_t)row * G.pitch;
-    Cell2 nc = m;
-    if (act) {
-        f2 l[5], r[5];
-#pragma unroll
-        for (int f = 0; f < 5; f++) {
-            l[f].v = make_float2(__shfl_up_sync(FULL, m.v[f].v.y, 1), m.v[f].v.x);
-            r[f].v = make_float2(m.v[f].v.y, __shfl_down_sync(FULL, m.v[f].v.x, 1));
-        }
-        f2 L[5], R[5];
-        nf_recon<0, LIM>(P, l, m.v, r, cf.half_dtdx, L, R);
-        f2 Rn[5];  // left face states of the cells right of this lane's two
-#pragma unroll
-        for (int f = 0; f < 5; f++) Rn[f].v = make_float2(L[f].v.y, __shfl_down_sync(FULL, L[f].v.x, 1));
-        f2 Fr[5], Fl[5];
-        const Force4Coef c4 = force4_coef(cf);
-        nf_force4<0>(P, R, Rn, c4.dtdx, c4.dxdt, Fr);
-#pragma unroll
-        for (int f = 0; f < 5; f++) Fl[f].v = make_float2(__shfl_up_sync(FULL, Fr[f].v.y, 1), Fr[f].v.x);
-        nf_update(c4.q_dtdx, m.v, Fl, Fr, nc.v);
-    }
+    float* d = dst + (size_t)row * G.pitch + p0;
     float w = 0.0f;
-    if (lane >= 1 && lane <= 30 && p0 < n) {
-        if (p0 + 1 < n) {
+    if (lane < 1 || lane > 30) return w;
+    if (full || p0 + 1 < n) {
+        if (!full && p0 >= n) return w;
 #pragma unroll
-            for (int f = 0; f < 5; f++) *reinterpret_cast<float2*>(dst + f * G.fstride + rb + p0) = nc.v[f].v;
-        } else {
-#pragma unroll
-            for (int f = 0; f < 5; f++) dst[f * G.fstride + rb + p0] = nc.v[f].v.x;
-        }
-        if (want_w && act) {
+        for (int f = 0; f < 5; f++) *reinterpret_cast<float2*>(d + f * G.fstride) = nc.v[f].v;
+        if (WS) {
             const f2 ws = nf_wavespeed(P, nc.v, dims);
-            w = p0 + 1 < n ? fmaxf(ws.v.x, ws.v.y) : fmaxf(ws.v.x, 0.0f);
+            w = fmaxf(ws.v.x, ws.v.y);
         }
+    } else if (p0 < n) {
+#pragma unroll
+        for (int f = 0; f < 5; f++) d[f * G.fstride] = nc.v[f].v.x;
+        if (WS) w = fmaxf(nf_wavespeed(P, nc.v, dims).v.x, 0.0f);
     }
     return w;
+}
+
+// One X segment with run-time flags (the batched launch): compute when `act` (else store the
+// cells unchanged), then store; returns the wavespeed maximum when want_w.
+template <int LIM>
+CG_D float x_pair_update(const NewtonFastParams& P, int dims, const Geom& G, float* __restrict__ dst, int row, int s0,
+                         const Cell2& m, bool act, const FastCoef& cf, bool want_w) {
+    Cell2 nc = m;
+    if (act) x_pair_compute<LIM>(P, m, cf, nc);
+    return want_w && act ? x_pair_store<true>(P, dims, G, dst, row, s0, nc, false)
+                         : x_pair_store<false>(P, dims, G, dst, row, s0, nc, false);
 }
 
 // ---- single-grid kernels
@@ -188,9 +203,9 @@ CG_D void ring_init(unsigned long long* bar, bool reinit) {
 // together, with jw < G.nx.  Returns the lane's wavespeed maximum over its updated cells when
 // want_w.  A wait that runs out (about a second) makes `ok` false (warp-uniform); the warp then
 // waits, again bounded, for its rows still in flight and returns.  On success the ring is drained.
-template <int LIM, int R>
+template <int LIM, int R, bool WS>
 CG_D float y_ring_march(const NewtonFastParams& P, int dims, const Geom& G, const float* __restrict__ src,
-                        float* __restrict__ dst, int jw, int y0, int y1, const FastCoef cf, bool want_w,
+                        float* __restrict__ dst, int jw, int y0, int y1, const FastCoef cf,
                         float (*ring)[5][64], unsigned long long* bar, bool& ok) {
     static_assert(R >= 5 && (R & (R - 1)) == 0, "a power of two above the four prologue rows");
     constexpr unsigned FULL = 0xffffffffu;
@@ -263,7 +278,7 @@ CG_D float y_ring_march(const NewtonFastParams& P, int dims, const Geom& G, cons
                     if (two) *reinterpret_cast<float2*>(o) = nc.v[f].v;
                     else *o = nc.v[f].v.x;
                 }
-                if (want_w) {
+                if (WS) {
                     const f2 ws = nf_wavespeed(P, nc.v, dims);
                     w = fmaxf(w, fmaxf(ws.v.x, ws.v.y));  // a lone column's lanes are equal
                 }
@@ -290,7 +305,7 @@ CG_D float y_ring_march(const NewtonFastParams& P, int dims, const Geom& G, cons
 // grid rows b seg .. (b + 1) seg - 1; each warp owns 64 columns and its own ring, never waits for
 // the other warps (no block barrier after the set-up) and reduces its own CFL maximum.  A ring
 // wait that runs out sets ST_TIMEOUT in the status word.
-template <int LIM, int NT, int R, int MINB>
+template <int LIM, int NT, int R, int MINB, bool WS>
 __global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams P, int dims, Geom G,
                                                           const float* __restrict__ src, float* __restrict__ dst,
                                                           DtSrc ds, SweepOut out, int seg) {
@@ -317,17 +332,16 @@ __global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams
         if (jw + 2 * lane < G.nx) y_pair_march<LIM>(P, dims, G, src, dst, jw + 2 * lane, y0, y1, false, s_coef, false);
         return;
     }
-    unsigned long long* wslot = out.slot();
     bool ok = true;
     const FastCoef cf = s_coef;  // in registers: the ring's waits would make every use re-read shared memory
-    float w = y_ring_march<LIM, R>(P, dims, G, src, dst, jw, y0, y1, cf, wslot != nullptr, ring[wp], bar[wp], ok);
+    float w = y_ring_march<LIM, R, WS>(P, dims, G, src, dst, jw, y0, y1, cf, ring[wp], bar[wp], ok);
     if (!ok) {
         if (lane == 0 && out.status) atomicOr(out.status, ST_TIMEOUT);
         return;
     }
-    if (wslot) {
+    if (WS) {
         w = warp_max(w);
-        if (lane == 0) atomic_max_nonneg(wslot, (double)w);
+        if (lane == 0) atomic_max_nonneg(out.slot(), (double)w);
     }
 }
 
@@ -338,7 +352,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams
 // row's first segment and its last ones (whose windows reach ghost cells) load through
 // x_pair_load.  No registers hold a prefetched segment.  A wait that runs out (about a second)
 // sets ST_TIMEOUT; the warp then waits, again bounded, for its copies still in flight and leaves.
-template <int LIM, int SEGS, int MINB>
+template <int LIM, int SEGS, int MINB, bool WS>
 __global__ void __launch_bounds__(32, MINB) sweep_x_ring_kernel(NewtonFastParams P, int dims, Geom G,
                                                                const float* __restrict__ src, float* __restrict__ dst,
                                                                DtSrc ds, SweepOut out) {
@@ -356,10 +370,17 @@ __global__ void __launch_bounds__(32, MINB) sweep_x_ring_kernel(NewtonFastParams
         mbar_init_fence();
     }
     __syncthreads();
-    const bool act = s_act != 0;
     const int n = G.nx, row = blockIdx.y;
     const int k0 = blockIdx.x * SEGS;
     const int kn = min(SEGS, (n + TSW - 1) / TSW - k0);  // segments of this warp (k0 < segments per row)
+    if (!s_act) {  // inactive step: keep the ping-pong buffers consistent
+        for (int i = 0; i < kn; i++) {
+            Cell2 m;
+            x_pair_load(G, src, row, (k0 + i) * TSW, m);
+            x_pair_store<false>(P, dims, G, dst, row, (k0 + i) * TSW, m, false);
+        }
+        return;
+    }
     // segment k's window s0 - 2 .. s0 + 61 lies inside the row and its copy s0 - 4 .. s0 + 63 too
     auto inside = [&](int k) { return k >= 1 && k * TSW + 64 <= n; };
     const size_t rb = (size_t)row * G.pitch;
@@ -369,16 +390,14 @@ __global__ void __launch_bounds__(32, MINB) sweep_x_ring_kernel(NewtonFastParams
         __syncwarp();
         if (lane < 5) bulk_load(xr[i][lane], src + (size_t)lane * G.fstride + rb + (k0 + i) * TSW - 4, W * 4, &xb[i]);
     }
-    unsigned long long* wslot = out.slot();
     const FastCoef cf = s_coef;
     float w = 0.0f;
-    bool ok = true;
     for (int i = 0; i < kn; i++) {
         const int s0 = (k0 + i) * TSW;
+        const bool in = inside(k0 + i);
         Cell2 m;
-        if (inside(k0 + i)) {
-            ok = __all_sync(0xffffffffu, mbar_wait(&xb[i], 0));
-            if (!ok) {
+        if (in) {
+            if (!__all_sync(0xffffffffu, mbar_wait(&xb[i], 0))) {
                 if (lane == 0) {
                     if (out.status) atomicOr(out.status, ST_TIMEOUT);
                     for (int q = i; q < kn; q++)
@@ -392,11 +411,13 @@ __global__ void __launch_bounds__(32, MINB) sweep_x_ring_kernel(NewtonFastParams
         } else {
             x_pair_load(G, src, row, s0, m);
         }
-        w = fmaxf(w, x_pair_update<LIM>(P, dims, G, dst, row, s0, m, act, cf, wslot != nullptr));
+        Cell2 nc;
+        x_pair_compute<LIM>(P, m, cf, nc);
+        w = fmaxf(w, x_pair_store<WS>(P, dims, G, dst, row, s0, nc, in));
     }
-    if (wslot) {
+    if (WS) {
         w = warp_max(w);
-        if (lane == 0) atomic_max_nonneg(wslot, (double)w);
+        if (lane == 0) atomic_max_nonneg(out.slot(), (double)w);
     }
 }
 
