@@ -153,7 +153,7 @@ RADJ_HD void slope_vector(const D5* ul, const D5* uc, const D5* ur, double w, in
 
 // ---- primitive recovery, RelativisticEulerStateVector.cpp:30-101 (BlackHoleEulerStateVector.cpp
 // divides the densitised state by sqrt(det gamma) first): the quartic in x = 1 / (h W) by Newton
-// from x = 1, stopping when a step moves x by less than tol; floors at 1e-8.
+// from x = 1, stopping when a step moves x by less than tol; floors at 1e-8 (derivative 0).
 struct Prim { D5 rho, vx, vy, vz, p, W, h; };
 RADJ_HD Prim con2prim(const D5* u, double g, double tol) {
     const D5 D = u[0], Sx = u[1], Sy = u[2], Sz = u[3], tau = u[4];
@@ -172,15 +172,25 @@ RADJ_HD Prim con2prim(const D5* u, double g, double tol) {
     const D5 quad = ((((g - 2.0) / g) * ((ec * ec) - 1.0)) + 1.0) - (((dc * dc) * gm) * gm);
     const D5 quart = (ec * ec) - 1.0;
     const D5 eta = (2.0 * dc) * gm;
-    D5 x = D5(1.0);
+    // The Newton iterations run on the values, the forward's arithmetic operation for operation;
+    // the root's tangents come from the implicit-function theorem at the final iterate xv:
+    // f(x; c) = 0 gives dx = -(the tangent of f with x held at xv) / f'(xv), the quartic's
+    // coefficients c carrying the tangents.
+    const double qv = quart.v, ev = eta.v, dv = quad.v, lv = lin.v, cv = cst.v;
+    double xv = 1.0;
     for (int it = 0; it < 1000; it++) {
-        const D5 f = ((((quart * ((x * x) * x)) * (x - eta)) + (quad * (x * x))) + (lin * x)) + cst;
-        const D5 fp = ((lin + ((2.0 * quad) * x)) + ((4.0 * quart) * ((x * x) * x))) -
-                      (((3.0 * eta) * quart) * (x * x));
-        const D5 nx = x - (f / fp);
-        if (fabs(x - nx) < D5(tol)) break;
-        x = nx;
+        const double f = ((((qv * ((xv * xv) * xv)) * (xv - ev)) + (dv * (xv * xv))) + (lv * xv)) + cv;
+        const double fp = ((lv + ((2.0 * dv) * xv)) + ((4.0 * qv) * ((xv * xv) * xv))) - (((3.0 * ev) * qv) * (xv * xv));
+        const double nx = xv - (f / fp);
+        if (::fabs(xv - nx) < tol) break;
+        xv = nx;
     }
+    const double fpv = ((lv + ((2.0 * dv) * xv)) + ((4.0 * qv) * ((xv * xv) * xv))) - (((3.0 * ev) * qv) * (xv * xv));
+    const D5 X(xv);
+    const D5 fx = ((((quart * ((X * X) * X)) * (X - eta)) + (quad * (X * X))) + (lin * X)) + cst;
+    D5 x(xv);
+    const double ifp = 1.0 / fpv;
+    for (int i = 0; i < 5; i++) x.d[i] = -fx.d[i] * ifp;
     Prim r;
     r.W = ((0.5 * ec) * x) * (1.0 + sqrt(1.0 + ((4.0 * gm) * ((1.0 - (dc * x)) / ((ec * ec) * (x * x))))));
     r.h = 1.0 / (dc * x);

@@ -118,8 +118,8 @@ template <class T> struct Newton {
 // BlackHoleEulerStateVector.cpp:30-103, :159-350, :359-430.  tol is 1e-8 everywhere except the
 // GR x-flux (BlackHoleEulerStateVector.cpp:205, 1e-10).  Results: rho, v, p, W, h.
 // Templated on the scalar: double for the restatement, Dual for the tangent-linear model (whose
-// comparisons act on values, so the iteration takes the FP64 run's path and the derivative
-// follows the iterates; the floors have derivative 0).
+// comparisons act on values, so every branch is the FP64 run's; the root's derivative is the
+// implicit-function theorem's at the final iterate; the floors have derivative 0).
 template <class T> struct C2PT { T rho, vx, vy, vz, p, W, h; };
 template <class T>
 static C2PT<T> con2prim_t(T D, T Sx, T Sy, T Sz, T tau, double g, double tol) {
@@ -138,16 +138,22 @@ static C2PT<T> con2prim_t(T D, T Sx, T Sy, T Sz, T tau, double g, double tol) {
                    (((dc * dc) * T((g - 1.0) / g)) * T((g - 1.0) / g)));
     T quartic = (ec * ec) - T(1.0);
     T eta = (T(2.0) * dc) * T((g - 1.0) / g);
-    T x = T(1.0);
+    // Newton on the values (the reference's iteration); for the tangent-linear model the root's
+    // tangent comes from the implicit-function theorem at the final iterate (ift_root).
+    const double qv = val(quartic), ev = val(eta), dv = val(quadratic), lv = val(linear), cv = val(constant);
+    double xv = 1.0;
     int it = 0;
     while (it < 1000) {
-        T f = ((((quartic * ((x * x) * x)) * (x - eta)) + (quadratic * (x * x))) + (linear * x)) + constant;
-        T fp = ((linear + ((T(2.0) * quadratic) * x)) + ((T(4.0) * quartic) * ((x * x) * x))) -
-               (((T(3.0) * eta) * quartic) * (x * x));
-        T nx = x - (f / fp);
-        if (fabs(x - nx) < T(tol)) it = 1000;
-        else { it += 1; x = nx; }
+        double f = ((((qv * ((xv * xv) * xv)) * (xv - ev)) + (dv * (xv * xv))) + (lv * xv)) + cv;
+        double fp = ((lv + ((2.0 * dv) * xv)) + ((4.0 * qv) * ((xv * xv) * xv))) - (((3.0 * ev) * qv) * (xv * xv));
+        double nx = xv - (f / fp);
+        if (std::fabs(xv - nx) < tol) it = 1000;
+        else { it += 1; xv = nx; }
     }
+    const double fpv = ((lv + ((2.0 * dv) * xv)) + ((4.0 * qv) * ((xv * xv) * xv))) - (((3.0 * ev) * qv) * (xv * xv));
+    const T X = T(xv);
+    const T fx = ((((quartic * ((X * X) * X)) * (X - eta)) + (quadratic * (X * X))) + (linear * X)) + constant;
+    T x = ift_root(xv, fx, fpv);
     C2PT<T> r;
     r.W = ((T(0.5) * ec) * x) *
           (T(1.0) + sqrt(T(1.0) + ((T(4.0) * T((g - 1.0) / g)) * ((T(1.0) - (dc * x)) / ((ec * ec) * (x * x))))));

@@ -40,6 +40,10 @@ inline Dual sqrt(Dual a) { double s = std::sqrt(a.v); return Dual(s, a.d / (2.0 
 inline Dual fabs(Dual a) { return a.v < 0 ? -a : a; }
 inline double val(Dual a) { return a.v; }
 inline double val(double a) { return a; }
+// A root xv of f(x; c) with its tangent by the implicit-function theorem: given f evaluated at
+// x = xv held fixed (its tangent is the coefficients' part) and f'(xv), dx = -df / f'(xv).
+inline double ift_root(double xv, double, double) { return xv; }
+inline Dual ift_root(double xv, Dual f_at_xv, double fp) { return Dual(xv, -f_at_xv.d / fp); }
 
 // std::min / std::max semantics (the reference uses them with doubles).
 template <class T> inline T mn(T a, T b) { return (b < a) ? b : a; }
