@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(NT, MINB) batch_pair_kernel(NewtonFastParams P
                         if (ring_used) ring_init<R>(wbar, true);
                         ring_used = true;
                         // the Y phase never reduces the CFL maximum (the last X sweep does)
-                        y_ring_march<LIM, R, false>(P, G.dims, G, sg, dg, it.a, it.b, it.c, cf, ring[warp], wbar, ring_ok);
+                        y_ring_march<LIM, R>(P, G.dims, G, sg, dg, it.a, it.b, it.c, cf, false, ring[warp], wbar, ring_ok);
                         if (!ring_ok && lane == 0) {
                             atomicOr(&ctl->status, ST_TIMEOUT);
                             atomicOr(&B.bar->err, ST_TIMEOUT);

@@ -63,8 +63,7 @@ cudaError_t run_fast(const SweepArgs& a) {
         if (a.order == 2) sweep_x_own_kernel<Pol, 2, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
         else sweep_x_own_kernel<Pol, 1, kXThreads><<<grid, kXThreads, 0, a.stream>>>(pol, G, src, dst, a.ds, a.out);
     } else if (a.order == 2 && !MASKED) {
-        auto kernel = a.out.slot_set() ? sweep_y_ring_kernel<LIM, kYPairThreads, kYRingRows, kYRingMinBlocks, true>
-                                       : sweep_y_ring_kernel<LIM, kYPairThreads, kYRingRows, kYRingMinBlocks, false>;
+        auto kernel = sweep_y_ring_kernel<LIM, kYPairThreads, kYRingRows, kYRingMinBlocks>;
         const int seg = y_ring_seg((const void*)kernel, G.nx, G.ny);
         dim3 grid((G.nx + 2 * kYPairThreads - 1) / (2 * kYPairThreads), (G.ny + seg - 1) / seg);
         kernel<<<grid, kYPairThreads, 0, a.stream>>>(pol.P, G.dims, G, src, dst, a.ds, a.out, seg);

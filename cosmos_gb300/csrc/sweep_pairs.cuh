@@ -203,9 +203,9 @@ CG_D void ring_init(unsigned long long* bar, bool reinit) {
 // together, with jw < G.nx.  Returns the lane's wavespeed maximum over its updated cells when
 // want_w.  A wait that runs out (about a second) makes `ok` false (warp-uniform); the warp then
 // waits, again bounded, for its rows still in flight and returns.  On success the ring is drained.
-template <int LIM, int R, bool WS>
+template <int LIM, int R>
 CG_D float y_ring_march(const NewtonFastParams& P, int dims, const Geom& G, const float* __restrict__ src,
-                        float* __restrict__ dst, int jw, int y0, int y1, const FastCoef cf,
+                        float* __restrict__ dst, int jw, int y0, int y1, const FastCoef cf, bool want_w,
                         float (*ring)[5][64], unsigned long long* bar, bool& ok) {
     static_assert(R >= 5 && (R & (R - 1)) == 0, "a power of two above the four prologue rows");
     constexpr unsigned FULL = 0xffffffffu;
@@ -278,7 +278,7 @@ CG_D float y_ring_march(const NewtonFastParams& P, int dims, const Geom& G, cons
                     if (two) *reinterpret_cast<float2*>(o) = nc.v[f].v;
                     else *o = nc.v[f].v.x;
                 }
-                if (WS) {
+                if (want_w) {
                     const f2 ws = nf_wavespeed(P, nc.v, dims);
                     w = fmaxf(w, fmaxf(ws.v.x, ws.v.y));  // a lone column's lanes are equal
                 }
@@ -305,7 +305,7 @@ CG_D float y_ring_march(const NewtonFastParams& P, int dims, const Geom& G, cons
 // grid rows b seg .. (b + 1) seg - 1; each warp owns 64 columns and its own ring, never waits for
 // the other warps (no block barrier after the set-up) and reduces its own CFL maximum.  A ring
 // wait that runs out sets ST_TIMEOUT in the status word.
-template <int LIM, int NT, int R, int MINB, bool WS>
+template <int LIM, int NT, int R, int MINB>
 __global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams P, int dims, Geom G,
                                                           const float* __restrict__ src, float* __restrict__ dst,
                                                           DtSrc ds, SweepOut out, int seg) {
@@ -334,14 +334,16 @@ __global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams
     }
     bool ok = true;
     const FastCoef cf = s_coef;  // in registers: the ring's waits would make every use re-read shared memory
-    float w = y_ring_march<LIM, R, WS>(P, dims, G, src, dst, jw, y0, y1, cf, ring[wp], bar[wp], ok);
+    // the reduction stays a run-time choice here: the compile-time form measured 3 % slower
+    unsigned long long* wslot = out.slot();
+    float w = y_ring_march<LIM, R>(P, dims, G, src, dst, jw, y0, y1, cf, wslot != nullptr, ring[wp], bar[wp], ok);
     if (!ok) {
         if (lane == 0 && out.status) atomicOr(out.status, ST_TIMEOUT);
         return;
     }
-    if (WS) {
+    if (wslot) {
         w = warp_max(w);
-        if (lane == 0) atomic_max_nonneg(out.slot(), (double)w);
+        if (lane == 0) atomic_max_nonneg(wslot, (double)w);
     }
 }
 
