@@ -9,8 +9,8 @@
 //   C  the Y sweep of every 2D grid (dt);
 //   D  the second X sweep of every 2D grid (dt/2), with each grid's CFL reduction fused in.
 // Work is a list of items per phase (X: a few rows of one grid, tiled; Y: a block of columns
-// times a run of rows), dealt on the host to the workers (resident blocks, or their warps) so that
-// their loads by cells swept are even.  The barrier needs co-residency, so the launch is
+// times a run of rows), longest first: FP64 dealt on the host to the resident blocks so that their
+// loads by cells swept are even, FP32 taken by the warps as they become free.  The barrier needs co-residency, so the launch is
 // cooperative; every wait is bounded and reports a timeout instead of hanging.
 #pragma once
 #include "policies.cuh"
@@ -46,8 +46,10 @@ struct BatchDev {
     const BatchGrid* grids;
     StepCtl* ctl;
     int ngrids;
-    const BatchItem* items[3];  // phases B, C, D, worker by worker
-    const int* offs[3];         // worker w's items: items[offs[w]] .. items[offs[w + 1] - 1]
+    const BatchItem* items[3];  // phases B, C, D: FP64 worker by worker, FP32 longest first
+    const int* offs[3];         // FP64: worker w's items are items[offs[w]] .. items[offs[w + 1] - 1]
+    int nitems[3];
+    unsigned int* take;         // FP32: items taken so far, per phase, by step parity: take[(step & 1) * 3 + phase]
     void* buf[2];
     GridBarrier* bar;
     int* gstep;                 // steps completed by the batch (buffer parity)
@@ -207,8 +209,9 @@ constexpr size_t batch_pair_smem(int nt) {
 }
 
 // FP32 batch on cell pairs (sweep_pairs.cuh), one warp per item and no block barrier inside a
-// phase: X items are runs of 60-cell segments of one grid (the next segment loaded while the
-// current one is computed); Y items are 64 columns (a pair per lane) x a run of rows, marched
+// phase; warps take the items of a phase's longest-first list through an atomic counter, so a
+// warp that finishes early takes more.  X items are runs of 60-cell segments of one grid (the next
+// segment loaded while the current one is computed); Y items are 64 columns (a pair per lane) x a run of rows, marched
 // through the warp's ring of rows staged by bulk copies (y_ring_march), its barriers initialised
 // again before each item.  Each warp reads its item's time step and reduces its own CFL maximum.
 // Same phases, grid barriers and per-grid controllers as batch_step_kernel.  A ring wait that runs
@@ -222,7 +225,6 @@ __global__ void __launch_bounds__(NT, MINB) batch_pair_kernel(NewtonFastParams P
     constexpr unsigned FULL = 0xffffffffu;
     extern __shared__ __align__(128) unsigned char batch_smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int worker = blockIdx.x * W + warp;
     float(*ring)[R][5][64] = reinterpret_cast<float(*)[R][5][64]>(batch_smem);
     unsigned long long* rbar = reinterpret_cast<unsigned long long*>(batch_smem + W * sizeof(float[R][5][64]));
     unsigned long long* wbar = rbar + warp * R;
@@ -233,6 +235,9 @@ __global__ void __launch_bounds__(NT, MINB) batch_pair_kernel(NewtonFastParams P
     for (int s = 0; s < nsteps; s++) {
         const int p = (step0 + s) & 1;
         for (int g = blockIdx.x * NT + threadIdx.x; g < B.ngrids; g += gridDim.x * NT) step_ctl_advance(&B.ctl[g]);
+        // the counters of the next step's parity were last used by the previous step, which every
+        // block has finished (the barriers since); the next step starts after four more
+        if (blockIdx.x == 0 && threadIdx.x < 3) B.take[(p ^ 1) * 3 + threadIdx.x] = 0u;
         if (!grid_sync(B.bar)) return;
         for (int ph = 0; ph < 3; ph++) {
             void* b0 = p ? B.buf[1] : B.buf[0];
@@ -240,9 +245,13 @@ __global__ void __launch_bounds__(NT, MINB) batch_pair_kernel(NewtonFastParams P
             const float* src = (const float*)(ph == 1 ? b1 : b0);
             float* dst = (float*)(ph == 1 ? b0 : b1);
             const BatchItem* items = ph == 0 ? B.items[0] : (ph == 1 ? B.items[1] : B.items[2]);
-            const int* offs = ph == 0 ? B.offs[0] : (ph == 1 ? B.offs[1] : B.offs[2]);
-            const int k1 = offs[worker + 1];
-            for (int k = offs[worker]; k < k1; k++) {  // warp-uniform
+            const int nit = ph == 0 ? B.nitems[0] : (ph == 1 ? B.nitems[1] : B.nitems[2]);
+            unsigned int* ctr = B.take + ((step0 + s) & 1) * 3 + ph;
+            // each warp takes the next item of the longest-first list; the one after it is taken
+            // while this one runs, so the atomic's latency is hidden
+            int k = __shfl_sync(FULL, lane == 0 ? (int)atomicAdd(ctr, 1u) : 0, 0);
+            while (k < nit) {  // warp-uniform
+                const int kn_own = lane == 0 ? (int)atomicAdd(ctr, 1u) : 0;
                 const BatchItem it = items[k];
                 const BatchGrid bg = B.grids[it.g];
                 StepCtl* ctl = &B.ctl[it.g];
@@ -297,6 +306,7 @@ __global__ void __launch_bounds__(NT, MINB) batch_pair_kernel(NewtonFastParams P
                     w = warp_max(w);
                     if (lane == 0) atomic_max_nonneg(&ctl->smax[ctl->it & 1], (double)w);
                 }
+                k = __shfl_sync(FULL, kn_own, 0);
             }
             if (!grid_sync(B.bar)) return;
         }

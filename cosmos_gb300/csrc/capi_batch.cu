@@ -55,6 +55,7 @@ struct cosmos_batch {
     StepCtl* d_ctl;
     GridBarrier* d_bar;
     int* d_gstep;
+    unsigned int* d_take;  // FP32 item counters (2 step parities x 3 phases)
     double* d_staging;
     size_t max_cells;
     // work lists for the current tile shape
@@ -80,11 +81,16 @@ BatchDev dev_desc(cosmos_batch* b) {
     B.grids = b->d_grids;
     B.ctl = b->d_ctl;
     B.ngrids = (int)b->grids.size();
-    for (int k = 0; k < 3; k++) { B.items[k] = b->d_items[k]; B.offs[k] = b->d_offs[k]; }
+    for (int k = 0; k < 3; k++) {
+        B.items[k] = b->d_items[k];
+        B.offs[k] = b->d_offs[k];
+        B.nitems[k] = b->nitems[k];
+    }
     B.buf[0] = b->buf[0];
     B.buf[1] = b->buf[1];
     B.bar = b->d_bar;
     B.gstep = b->d_gstep;
+    B.take = b->d_take;
     return B;
 }
 
@@ -97,9 +103,10 @@ void* kernel_fn(cosmos_batch* b, int nt, int seg, int cap, int lim) {
 // are whole rows of one grid, as many as make about 8 tiles of nt - 2 cells; Y items nt columns x
 // seg rows.  FP32 (cell pairs, one warp per item): X items are runs of kBatchXSegs 60-cell segments
 // of one grid, numbered row by row (a = first, b = one past the last); Y items 64 columns x seg rows.
-// Each list is dealt to the workers (FP64: the resident blocks; FP32: their warps) longest item
-// first, each onto the least-loaded worker, by a cost of cells swept (Y counting its four halo
-// rows) plus a per-item overhead; worker w's items are stored at off[w] .. off[w + 1] - 1.
+// Each list is sorted longest item first by a cost of cells swept (Y counting its four halo rows)
+// plus a per-item overhead.  FP32: the warps take the items in that order as they become free (an
+// atomic counter per phase).  FP64: each item is dealt onto the least-loaded resident block, and
+// block w's items are stored at off[w] .. off[w + 1] - 1.
 int build_items(cosmos_batch* b, int nt, int seg, int cap) {
     void* fn = kernel_fn(b, nt, seg, cap, b->run.limiter);
     if (!fn) return bfail(COSMOS_EUNSUPPORTED, "batch tile shape not provided for this precision");
@@ -110,7 +117,7 @@ int build_items(cosmos_batch* b, int nt, int seg, int cap) {
     if (per_sm < 1) return bfail(COSMOS_EUNSUPPORTED, "batch kernel does not fit on an SM");
     const bool pairs = b->precision == COSMOS_FP32;
     const int blocks = per_sm * sms;
-    const int workers = pairs ? blocks * (nt / 32) : blocks;
+    const int workers = blocks;  // FP64 deal
     struct Costed { long long cost; BatchItem it; };
     std::vector<Costed> ph[3];
     const long long overhead = 32;
@@ -148,8 +155,23 @@ int build_items(cosmos_batch* b, int nt, int seg, int cap) {
         }
     }
     for (int k = 0; k < 3; k++) {
-        // longest processing time first onto the least-loaded worker (ties: the lower index)
+        // longest processing time first (ties: the building order)
         std::stable_sort(ph[k].begin(), ph[k].end(), [](const Costed& x, const Costed& y) { return x.cost > y.cost; });
+        if (b->d_items[k]) cudaFree(b->d_items[k]);
+        if (b->d_offs[k]) cudaFree(b->d_offs[k]);
+        b->d_items[k] = nullptr;
+        b->d_offs[k] = nullptr;
+        b->nitems[k] = (int)ph[k].size();
+        if (pairs) {  // FP32: the warps take the list in this order (an atomic counter per phase)
+            std::vector<BatchItem> flat;
+            flat.reserve(ph[k].size());
+            for (const Costed& c : ph[k]) flat.push_back(c.it);
+            if (flat.empty()) continue;
+            BCK(cudaMalloc(&b->d_items[k], flat.size() * sizeof(BatchItem)));
+            BCK(cudaMemcpy(b->d_items[k], flat.data(), flat.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
+            continue;
+        }
+        // FP64: each item onto the least-loaded block (ties: the lower index)
         using Load = std::pair<long long, int>;
         std::priority_queue<Load, std::vector<Load>, std::greater<Load>> pq;
         for (int w = 0; w < workers; w++) pq.push({0ll, w});
@@ -167,11 +189,6 @@ int build_items(cosmos_batch* b, int nt, int seg, int cap) {
             flat.insert(flat.end(), per[w].begin(), per[w].end());
             off[w + 1] = (int)flat.size();
         }
-        if (b->d_items[k]) cudaFree(b->d_items[k]);
-        if (b->d_offs[k]) cudaFree(b->d_offs[k]);
-        b->d_items[k] = nullptr;
-        b->d_offs[k] = nullptr;
-        b->nitems[k] = (int)flat.size();
         BCK(cudaMalloc(&b->d_offs[k], off.size() * sizeof(int)));
         BCK(cudaMemcpy(b->d_offs[k], off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice));
         if (flat.empty()) continue;
@@ -204,6 +221,7 @@ cudaError_t launch_chunk(cosmos_batch* b, int nsteps) {
 // Controllers reset (t = 0, iteration 0) and the initial CFL reduction of every grid.
 int reset_controllers(cosmos_batch* b) {
     const int n = (int)b->grids.size();
+    BCK(cudaMemsetAsync(b->d_take, 0, 6 * sizeof(unsigned int), b->stream));
     std::vector<StepCtl> h(n);
     for (int g = 0; g < n; g++) {
         memset(&h[g], 0, sizeof(StepCtl));
@@ -312,6 +330,8 @@ int cosmos_batch_create(cosmos_ctx* ctx, int ngrids, const int* dims, const int*
     if (e == cudaSuccess) e = cudaMalloc(&b->d_ctl, ngrids * sizeof(StepCtl));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_bar, sizeof(GridBarrier));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_gstep, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_take, 6 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMemset(b->d_take, 0, 6 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_staging, maxc * 5 * sizeof(double));
     if (e == cudaSuccess) e = cudaMemcpy(b->d_grids, b->grids.data(), ngrids * sizeof(BatchGrid), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(b->d_gstep, 0, sizeof(int));
@@ -344,6 +364,7 @@ int cosmos_batch_destroy(cosmos_batch* b) {
     if (b->d_ctl) cudaFree(b->d_ctl);
     if (b->d_bar) cudaFree(b->d_bar);
     if (b->d_gstep) cudaFree(b->d_gstep);
+    if (b->d_take) cudaFree(b->d_take);
     if (b->d_staging) cudaFree(b->d_staging);
     cosmos_ctx* ctx = b->ctx;
     delete b;
@@ -478,6 +499,7 @@ int cosmos_batch_time_shape(cosmos_batch* b, int nt, int seg, int cap, int steps
     BCK(cudaMemcpyAsync(b->buf[1], (char*)save + bytes, bytes, cudaMemcpyDeviceToDevice, b->stream));
     BCK(cudaMemcpyAsync(b->d_ctl, (char*)save + 2 * bytes, n * sizeof(StepCtl), cudaMemcpyDeviceToDevice, b->stream));
     BCK(cudaMemcpyAsync(b->d_gstep, (char*)save + 2 * bytes + n * sizeof(StepCtl), sizeof(int), cudaMemcpyDeviceToDevice, b->stream));
+    BCK(cudaMemsetAsync(b->d_take, 0, 6 * sizeof(unsigned int), b->stream));  // no item taken at either parity
     BCK(cudaFreeAsync(save, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
     int rc2 = set_shape(b, nt0, seg0, cap0);
