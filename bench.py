@@ -694,8 +694,10 @@ def measure_batch(cg, L, ctx, stream, steps, warmup, l1_steps=20, tiles=False):
     for k, s in enumerate(states):
         b.set_prim(k, s)
     b.run_begin(0.9, 1e30, 0.0, cg.MINBEE)
+    shapes_tried = [(nt, seg, cap) for nt in (128, 256) for seg in (32, 64) for cap in (0, 1)]
+    shapes_tried += [(128, 128, 1), (256, 128, 1)]
     tile_ms = {f"{nt}x{seg}{'c' if cap else ''}": b.time_shape(nt, seg, cap, steps=5)
-               for nt in (128, 256) for seg in (32, 64) for cap in (0, 1)} if tiles else None
+               for nt, seg, cap in shapes_tried} if tiles else None
     tuned, _ = b.autotune(None)
     b.run_steps(warmup)
     launches0 = L.cosmos_kernel_launches()

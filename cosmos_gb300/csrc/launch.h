@@ -150,8 +150,9 @@ struct BatchLaunch {
 };
 // Tile shapes of the batched launch: (threads per block, rows per Y work item, register cap).
 constexpr int kBatchShapes[][3] = {{128, 32, 0}, {128, 64, 0}, {256, 32, 0}, {256, 64, 0},
-                                   {128, 32, 1}, {128, 64, 1}, {256, 32, 1}, {256, 64, 1}};
-constexpr int kNumBatchShapes = 8;
+                                   {128, 32, 1}, {128, 64, 1}, {256, 32, 1}, {256, 64, 1},
+                                   {128, 128, 1}, {256, 128, 1}};
+constexpr int kNumBatchShapes = 10;
 cudaError_t launch_batch_fast(const BatchLaunch& L);
 cudaError_t launch_batch_exact(const BatchLaunch& L);
 

@@ -132,8 +132,10 @@ def test_fp32_autotune_considers_capped_shapes(cg):
     shapes = [(256, 256), (1000,), (77, 130)]
     b = make_batch(cg, [cases.newton_state(rng, sh) for sh in shapes], 0.01, 1, 1)
     b.run_begin(0.9, 1e9, 0.0, 2)
-    times = {(nt, seg, cap): b.time_shape(nt, seg, cap, steps=3)
-             for nt in (128, 256) for seg in (32, 64) for cap in (0, 1)}
+    # the autotuner's shapes: threads {128, 256} x Y rows {32, 64} x cap {0, 1}, and 128 rows capped
+    grid = [(nt, seg, cap) for nt in (128, 256) for seg in (32, 64) for cap in (0, 1)]
+    grid += [(128, 128, 1), (256, 128, 1)]
+    times = {sh: b.time_shape(*sh, steps=3) for sh in grid}
     assert all(v > 0.0 for v in times.values())
     shape, ms = b.autotune(None)
     assert shape in times and ms > 0.0
