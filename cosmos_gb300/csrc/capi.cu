@@ -101,6 +101,7 @@ cudaError_t sweep_launch(cosmos_grid* g, const SweepArgs& a) {
 namespace {
 
 size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+constexpr int kChunkSteps = 8;  // steps per replayed chunk graph (even)
 
 bool valid_params(const cosmos_params* p, std::string& why) {
     if (!p) { why = "null params"; return false; }
@@ -365,6 +366,7 @@ int cosmos_grid_destroy(cosmos_grid* g) {
     cudaStreamSynchronize(g->ctx->stream);
     for (int b = 0; b < 2; b++) {
         if (g->step_graph[b]) cudaGraphExecDestroy(g->step_graph[b]);
+        if (g->chunk_graph[b]) cudaGraphExecDestroy(g->chunk_graph[b]);
         if (g->buf[b]) cudaFree(g->buf[b]);
     }
     if (g->ctl) cudaFree(g->ctl);
@@ -544,24 +546,32 @@ int cosmos_grid_run_begin(cosmos_grid* g, const cosmos_solve_opts* o) {
     if (g->p.precision == COSMOS_FP64) CK(launch_wavespeed_exact(a, &g->ctl->smax[0]));
     else CK(launch_wavespeed_fast(a, &g->ctl->smax[0]));
     if (!same) {
-        for (int b = 0; b < 2; b++) {
-            if (g->step_graph[b]) { cudaGraphExecDestroy(g->step_graph[b]); g->step_graph[b] = nullptr; }
-            cudaGraph_t graph;
-            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            unsigned nk = 0;
-            int end = 0;
-            t_capturing = true;
-            int r = enqueue_step(g, b, &end, &nk);
-            t_capturing = false;
-            cudaError_t ec = cudaStreamEndCapture(st, &graph);
-            if (r) { if (ec == cudaSuccess) cudaGraphDestroy(graph); return r; }
-            if (ec != cudaSuccess) return fail(COSMOS_ECUDA, "graph capture: %s", cudaGetErrorString(ec));
-            if (end != (b ^ 1)) { cudaGraphDestroy(graph); return fail(COSMOS_ESTATE, "step writes an even number of times"); }
-            cudaError_t ei = cudaGraphInstantiate(&g->step_graph[b], graph, 0);
-            cudaGraphDestroy(graph);
-            if (ei != cudaSuccess) return fail(COSMOS_ECUDA, "graph instantiate: %s", cudaGetErrorString(ei));
-            g->step_kernels = nk;
-        }
+        // one step, and kChunkSteps steps, from each starting buffer; replaying a chunk saves the
+        // launch gap between consecutive graphs
+        for (int b = 0; b < 2; b++)
+            for (int chunk = 0; chunk < 2; chunk++) {
+                cudaGraphExec_t& exec = chunk ? g->chunk_graph[b] : g->step_graph[b];
+                if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
+                cudaGraph_t graph;
+                CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                unsigned nk = 0;
+                int cur = b, r = 0;
+                t_capturing = true;
+                for (int s = 0; s < (chunk ? kChunkSteps : 1) && !r; s++) {
+                    int end = 0;
+                    r = enqueue_step(g, cur, &end, &nk);
+                    if (!r && end != (cur ^ 1)) r = fail(COSMOS_ESTATE, "step writes an even number of times");
+                    cur ^= 1;
+                }
+                t_capturing = false;
+                cudaError_t ec = cudaStreamEndCapture(st, &graph);
+                if (r) { if (ec == cudaSuccess) cudaGraphDestroy(graph); return r; }
+                if (ec != cudaSuccess) return fail(COSMOS_ECUDA, "graph capture: %s", cudaGetErrorString(ec));
+                cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+                cudaGraphDestroy(graph);
+                if (ei != cudaSuccess) return fail(COSMOS_ECUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+                if (!chunk) g->step_kernels = nk;
+            }
         g->run_ready = true;
     }
     return COSMOS_OK;
@@ -571,7 +581,12 @@ int cosmos_grid_run_steps(cosmos_grid* g, int n) {
     if (!g) return fail(COSMOS_EINVAL, "null grid");
     if (!g->run_ready) return fail(COSMOS_ESTATE, "cosmos_grid_run_begin has not been called");
     if (n < 0) return fail(COSMOS_EINVAL, "negative step count");
-    for (int s = 0; s < n; s++) {
+    int s = 0;
+    for (; s + kChunkSteps <= n; s += kChunkSteps) {  // an even number of steps: the buffer stays
+        CK(cudaGraphLaunch(g->chunk_graph[g->cur], g->ctx->stream));
+        count_launch(g->step_kernels * kChunkSteps);
+    }
+    for (; s < n; s++) {
         CK(cudaGraphLaunch(g->step_graph[g->cur], g->ctx->stream));
         count_launch(g->step_kernels);
         g->cur ^= 1;  // every step has an odd number of state-writing kernels

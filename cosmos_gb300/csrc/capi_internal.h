@@ -32,6 +32,7 @@ struct cosmos_grid {
     cosmos_solve_opts run;
     bool run_ready;
     cudaGraphExec_t step_graph[2];
+    cudaGraphExec_t chunk_graph[2];  // kChunkSteps steps from each starting buffer (an even count: back to it)
     unsigned step_kernels;   // kernels per captured step
     // black-hole grids with FP32 storage: metric tables built once at creation
     void* gr_mem;
