@@ -202,3 +202,25 @@ def test_fp32_pair_kernels_match_one_cell_kernels(cg, shape, bc, lim):
     got, want = b.get_prim(0), g.get_prim()
     rel = np.abs(got - want) / (np.abs(want) + 1e-3)
     assert np.median(rel) < 1e-6 and rel.max() < 1e-2, (np.median(rel), rel.max())
+
+
+def test_fp32_batch_uneven_step_counts(cg):
+    """The FP32 warps take items through per-phase counters that alternate with the step parity:
+    runs of 3, 10 (one replayed chunk) and 7 steps, and again after a time_shape (which restores the
+    state), give the same states as 20 single steps."""
+    rng = np.random.default_rng(8)
+    shapes = [(64, 96), (300,), (45, 70)]
+    states = [cases.newton_state(rng, sh) for sh in shapes]
+    results = []
+    for plan in ((3, 10, 7), (1,) * 20):
+        b = make_batch(cg, states, [1.0 / sh[-1] for sh in shapes], 1, 1)
+        b.run_begin(0.8, 1e9, 0.0, 2, max_steps=20)
+        if len(plan) > 3:
+            b.time_shape(128, 32, 1, steps=3)
+        for k in plan:
+            b.run_steps(k)
+        res = b.run_end()
+        assert all(r.steps == 20 for r in res)
+        results.append([b.get_prim(k) for k in range(len(shapes))])
+        b.close()
+    assert all(bit_equal(x, y) for x, y in zip(*results))

@@ -200,6 +200,33 @@ def test_fp32_four_quadrant_error(cg, oracle):
     assert abs(m1[0] - m0[0]) / abs(m0[0]) < 1e-6 and abs(m1[4] - m0[4]) / abs(m0[4]) < 1e-6
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_chunk_replay_equals_single_steps(cg, precision):
+    """A run replays 8-step graphs where it can and single-step graphs for the rest: 21 steps in
+    one call (two chunks and five single steps) and in 21 calls of one step give the same state,
+    time and step count bit for bit; a run that reaches its final time inside a chunk stops there."""
+    rng = np.random.default_rng(12)
+    s = cases.newton_state(rng, (40, 56))
+    out = []
+    for split in (False, True):
+        g = grid_from(cg, 0, s, 1.0 / 56, precision=precision, bc=1)
+        g.run_begin(2, 0.8, 1e9, 0.0, 2, max_steps=21)
+        if split:
+            for _ in range(21):
+                g.run_steps(1)
+        else:
+            g.run_steps(21)
+        r = g.run_end()
+        out.append((r.steps, r.t, g.get_prim()))
+    assert out[0][0] == out[1][0] == 21 and out[0][1] == out[1][1]
+    assert bit_equal(out[0][2], out[1][2])
+    g = grid_from(cg, 0, s, 1.0 / 56, precision=precision, bc=1)
+    g.run_begin(2, 0.8, 1e9, 0.0, 2, max_steps=11)
+    g.run_steps(16)  # two chunks; the controller stops the run after step 11
+    r = g.run_end()
+    assert r.steps == 11
+
+
 def test_fp32_sod_error(cg, golden):
     g = grid_from(cg, 0, cases.sod(1000), 1.0 / 1000, precision=1)
     r = g.solve(2, 0.9, 0.25, 0.0, 1)
