@@ -613,6 +613,17 @@ def measure_gr(cg, L, ctx, stream, n, steps, warmup, r_cut=5.0):
                    "what": "FP32 bulk; metric from FP64 tables; primitive recovery finished in FP64 above W = 2 "
                            "or on FP32 non-convergence"}
     out["value"] = out["fp32"]["value"]
+    # the same free run with every primitive recovery's Newton iterations finished in FP64 (the
+    # workload's "FP64 con2prim"); the metric is FP64-evaluated in both
+    g = make(cg.FP32, 0.0)
+    g.run_begin(2, 0.9, 1e30, 0.0, cg.VANLEER, max_steps=steps)
+    ms_c = clock(lambda: g.run_steps(steps)) / steps
+    r = g.run_end()
+    g.close()
+    out["fp32_c2p_fp64"] = {"value": n * n / (ms_c * 1e-3), "ms_per_step": ms_c, "t": r.t,
+                            "steps_completed": r.steps, "status": r.status,
+                            "what": "FP32 bulk; metric from FP64 tables; every primitive recovery's Newton "
+                                    "iterations finished in FP64"}
     # FP64 driven by its own CFL rule, and FP32 (as configured, and with the FP64 Newton stage in
     # every primitive recovery) driven by the FP64 run's dts; density errors at checkpoints.  The
     # FP64 run stops where the reference's own arithmetic produces a non-finite state next to the
