@@ -32,7 +32,7 @@ struct BatchGrid {
 struct BatchItem { int g, a, b, c; };
 
 // Rows' worth of 60-cell segments in one FP32 X item.
-constexpr int kBatchXSegs = 16;
+constexpr int kBatchXSegs = 64;
 
 struct GridBarrier {
     unsigned int count;

@@ -105,8 +105,8 @@ void* kernel_fn(cosmos_batch* b, int nt, int seg, int cap, int lim) {
 // of one grid, numbered row by row (a = first, b = one past the last); Y items 64 columns x seg rows.
 // Each list is sorted longest item first by a cost of cells swept (Y counting its four halo rows)
 // plus a per-item overhead.  FP32: the warps take the items in that order as they become free (an
-// atomic counter per phase).  FP64: each item is dealt onto the least-loaded resident block, and
-// block w's items are stored at off[w] .. off[w + 1] - 1.
+// atomic counter per phase), the list's last items split into quarters.  FP64: each item is dealt
+// onto the least-loaded resident block, and block w's items are stored at off[w] .. off[w + 1] - 1.
 int build_items(cosmos_batch* b, int nt, int seg, int cap) {
     void* fn = kernel_fn(b, nt, seg, cap, b->run.limiter);
     if (!fn) return bfail(COSMOS_EUNSUPPORTED, "batch tile shape not provided for this precision");
@@ -163,9 +163,27 @@ int build_items(cosmos_batch* b, int nt, int seg, int cap) {
         b->d_offs[k] = nullptr;
         b->nitems[k] = (int)ph[k].size();
         if (pairs) {  // FP32: the warps take the list in this order (an atomic counter per phase)
+            // The phase ends when its last items drain: the last (warps) items are each split into
+            // quarters (X: a quarter of the segments; Y: a quarter of the rows) so that the drain
+            // is shorter.  Splitting more of the list, or splitting it twice, measured slower:
+            // every item costs its set-up.
+            const size_t warps = (size_t)blocks * (nt / 32);
+            const size_t keep = ph[k].size() > warps ? ph[k].size() - warps : 0;
             std::vector<BatchItem> flat;
-            flat.reserve(ph[k].size());
-            for (const Costed& c : ph[k]) flat.push_back(c.it);
+            flat.reserve(ph[k].size() + 3 * warps);
+            for (size_t i = 0; i < ph[k].size(); i++) {
+                const BatchItem it = ph[k][i].it;
+                if (i < keep) {
+                    flat.push_back(it);
+                } else if (k == 1) {  // rows b .. c - 1 in four runs (at least one row each)
+                    const int step = std::max(1, (it.c - it.b + 3) / 4);
+                    for (int y = it.b; y < it.c; y += step) flat.push_back({it.g, it.a, y, std::min(y + step, it.c)});
+                } else {  // segments a .. b - 1 in four runs
+                    const int step = std::max(1, (it.b - it.a + 3) / 4);
+                    for (int q = it.a; q < it.b; q += step) flat.push_back({it.g, q, std::min(q + step, it.b), 0});
+                }
+            }
+            b->nitems[k] = (int)flat.size();
             if (flat.empty()) continue;
             BCK(cudaMalloc(&b->d_items[k], flat.size() * sizeof(BatchItem)));
             BCK(cudaMemcpy(b->d_items[k], flat.data(), flat.size() * sizeof(BatchItem), cudaMemcpyHostToDevice));
