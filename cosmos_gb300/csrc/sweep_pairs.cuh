@@ -203,10 +203,10 @@ CG_D void ring_init(unsigned long long* bar, bool reinit) {
 // together, with jw < G.nx.  Returns the lane's wavespeed maximum over its updated cells when
 // want_w.  A wait that runs out (about a second) makes `ok` false (warp-uniform); the warp then
 // waits, again bounded, for its rows still in flight and returns.  On success the ring is drained.
-template <int LIM, int R>
+template <int LIM, int R, bool TM = false>
 CG_D float y_ring_march(const NewtonFastParams& P, int dims, const Geom& G, const float* __restrict__ src,
                         float* __restrict__ dst, int jw, int y0, int y1, const FastCoef cf, bool want_w,
-                        float (*ring)[5][64], unsigned long long* bar, bool& ok) {
+                        float (*ring)[5][64], unsigned long long* bar, bool& ok, const CUtensorMap* tm = nullptr) {
     static_assert(R >= 5 && (R & (R - 1)) == 0, "a power of two above the four prologue rows");
     constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -216,14 +216,22 @@ CG_D float y_ring_march(const NewtonFastParams& P, int dims, const Geom& G, cons
     const uint32_t bytes = ((uint32_t)min(64, G.nx - jw) * 4u + 15u) & ~15u;  // within the padded pitch
     const int ylo = y0 - 2, yhi = y1 + 1;  // rows read
     // Row r of the ring lives in slot (r - ylo) mod R; the slot's k-th use completes phase k mod 2.
-    // Lanes 0-4 each copy one field (lanes 5+ hold a valid pointer they never use).
+    // TM: lane 0 copies the row's five fields as one box of the tensor map; otherwise lanes 0-4
+    // each copy one field (lanes 5+ hold a valid pointer they never use).
     const float* fsrc = src + (size_t)min(lane, 4) * G.fstride + jw;
     int inext = ylo;  // warp-uniform: next row to issue
     auto issue_one = [&]() {
         const int r = inext, q = (r - ylo) & (R - 1);
-        if (lane == 0) mbar_expect_tx(&bar[q], 5 * bytes);
-        __syncwarp();
-        if (lane < 5) bulk_load(ring[q][lane], fsrc + (size_t)ghost_index(r, G.ny, G.bc) * G.pitch, bytes, &bar[q]);
+        if (TM) {  // one copy of the row's five 64-column runs (columns past nx arrive as zeros)
+            if (lane == 0) {
+                mbar_expect_tx(&bar[q], 5 * 64 * 4);
+                tma_load_3d(ring[q], tm, jw, ghost_index(r, G.ny, G.bc), 0, &bar[q]);
+            }
+        } else {
+            if (lane == 0) mbar_expect_tx(&bar[q], 5 * bytes);
+            __syncwarp();
+            if (lane < 5) bulk_load(ring[q][lane], fsrc + (size_t)ghost_index(r, G.ny, G.bc) * G.pitch, bytes, &bar[q]);
+        }
         ++inext;
     };
     for (int k = 0; k < R && inext <= yhi; k++) issue_one();
@@ -301,14 +309,16 @@ CG_D float y_ring_march(const NewtonFastParams& P, int dims, const Geom& G, cons
     return w;
 }
 
-// Y sweep with the rows staged in shared memory by bulk copies (y_ring_march).  Block row b covers
-// grid rows b seg .. (b + 1) seg - 1; each warp owns 64 columns and its own ring, never waits for
-// the other warps (no block barrier after the set-up) and reduces its own CFL maximum.  A ring
-// wait that runs out sets ST_TIMEOUT in the status word.
-template <int LIM, int NT, int R, int MINB>
+// Y sweep with the rows staged in shared memory by bulk copies (y_ring_march; TM: one copy per row
+// through the tensor map `tm` of the source's fields).  Block row b covers grid rows b seg ..
+// (b + 1) seg - 1; each warp owns 64 columns and its own ring, never waits for the other warps (no
+// block barrier after the set-up) and reduces its own CFL maximum.  A ring wait that runs out sets
+// ST_TIMEOUT in the status word.
+template <int LIM, int NT, int R, int MINB, bool TM>
 __global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams P, int dims, Geom G,
                                                           const float* __restrict__ src, float* __restrict__ dst,
-                                                          DtSrc ds, SweepOut out, int seg) {
+                                                          DtSrc ds, SweepOut out, int seg,
+                                                          const __grid_constant__ CUtensorMap tm) {
     static_assert(NT % 32 == 0, "whole warps");
     constexpr int NWP = NT / 32;
     __shared__ __align__(128) float ring[NWP][R][5][64];
@@ -336,7 +346,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams
     const FastCoef cf = s_coef;  // in registers: the ring's waits would make every use re-read shared memory
     // the reduction stays a run-time choice here: the compile-time form measured 3 % slower
     unsigned long long* wslot = out.slot();
-    float w = y_ring_march<LIM, R>(P, dims, G, src, dst, jw, y0, y1, cf, wslot != nullptr, ring[wp], bar[wp], ok);
+    float w = y_ring_march<LIM, R, TM>(P, dims, G, src, dst, jw, y0, y1, cf, wslot != nullptr, ring[wp], bar[wp], ok,
+                                       &tm);
     if (!ok) {
         if (lane == 0 && out.status) atomicOr(out.status, ST_TIMEOUT);
         return;
@@ -350,16 +361,18 @@ __global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams
 // X sweep with each warp's segments staged in shared memory by bulk copies: a one-warp block
 // takes SEGS consecutive 60-cell segments of its row and, at its start, copies every segment whose
 // 64-cell window lies inside the row (cells s0 - 4 .. s0 + 63, a 16-byte aligned run of 272 bytes
-// per field) into its own slot, so all of them are in flight while the first is computed; the
-// row's first segment and its last ones (whose windows reach ghost cells) load through
-// x_pair_load.  No registers hold a prefetched segment.  A wait that runs out (about a second)
+// per field) into its own slot, so all of them are in flight while the first is computed (TM: the
+// five fields' windows as one box of the tensor map `tm`, one copy per segment); the row's first
+// segment and its last ones (whose windows reach ghost cells) load through x_pair_load.  No registers hold a prefetched segment.  A wait that runs out (about a second)
 // sets ST_TIMEOUT; the warp then waits, again bounded, for its copies still in flight and leaves.
-template <int LIM, int SEGS, int MINB, bool WS>
+template <int LIM, int SEGS, int MINB, bool WS, bool TM>
 __global__ void __launch_bounds__(32, MINB) sweep_x_ring_kernel(NewtonFastParams P, int dims, Geom G,
                                                                const float* __restrict__ src, float* __restrict__ dst,
-                                                               DtSrc ds, SweepOut out) {
+                                                               DtSrc ds, SweepOut out,
+                                                               const __grid_constant__ CUtensorMap tm) {
     constexpr int TSW = 60, W = 68;
-    __shared__ __align__(128) float xr[SEGS][5][W];
+    constexpr int SLOT = (5 * W + 31) / 32 * 32;  // a slot holds fields 0-4 at f W; 128-byte aligned slots
+    __shared__ __align__(128) float xr[SEGS][SLOT];
     __shared__ __align__(8) unsigned long long xb[SEGS];
     __shared__ FastCoef s_coef;
     __shared__ int s_act;
@@ -388,9 +401,16 @@ __global__ void __launch_bounds__(32, MINB) sweep_x_ring_kernel(NewtonFastParams
     const size_t rb = (size_t)row * G.pitch;
     for (int i = 0; i < kn; i++) {
         if (!inside(k0 + i)) continue;
-        if (lane == 0) mbar_expect_tx(&xb[i], 5 * W * 4);
-        __syncwarp();
-        if (lane < 5) bulk_load(xr[i][lane], src + (size_t)lane * G.fstride + rb + (k0 + i) * TSW - 4, W * 4, &xb[i]);
+        if (TM) {  // the five fields' windows as one box
+            if (lane == 0) {
+                mbar_expect_tx(&xb[i], 5 * W * 4);
+                tma_load_3d(xr[i], &tm, (k0 + i) * TSW - 4, row, 0, &xb[i]);
+            }
+        } else {
+            if (lane == 0) mbar_expect_tx(&xb[i], 5 * W * 4);
+            __syncwarp();
+            if (lane < 5) bulk_load(&xr[i][lane * W], src + (size_t)lane * G.fstride + rb + (k0 + i) * TSW - 4, W * 4, &xb[i]);
+        }
     }
     const FastCoef cf = s_coef;
     float w = 0.0f;
@@ -409,7 +429,7 @@ __global__ void __launch_bounds__(32, MINB) sweep_x_ring_kernel(NewtonFastParams
                 return;
             }
 #pragma unroll
-            for (int f = 0; f < 5; f++) m.v[f].v = *reinterpret_cast<const float2*>(&xr[i][f][2 + 2 * lane]);
+            for (int f = 0; f < 5; f++) m.v[f].v = *reinterpret_cast<const float2*>(&xr[i][f * W + 2 + 2 * lane]);
         } else {
             x_pair_load(G, src, row, s0, m);
         }

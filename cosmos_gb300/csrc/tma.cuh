@@ -1,6 +1,9 @@
-// Bulk asynchronous copies (TMA, cp.async.bulk) from global to shared memory completing on
-// shared-memory mbarriers, and bounded waits on them.  All inline PTX written here; sm_90+ forms.
+// Bulk asynchronous copies (TMA: cp.async.bulk, and cp.async.bulk.tensor on a tensor map) from
+// global to shared memory completing on shared-memory mbarriers, and bounded waits on them.  All
+// inline PTX written here; sm_90+ forms.
 #pragma once
+#include <cuda.h>  // CUtensorMap (the descriptor type only; no driver call is linked)
+
 #include <cstdint>
 
 #include "device_common.cuh"
@@ -33,6 +36,18 @@ CG_D void bulk_load(void* dst, const void* src, uint32_t bytes, unsigned long lo
                      smem_addr(dst)),
                  "l"(src), "r"(bytes), "r"(smem_addr(bar))
                  : "memory");
+}
+
+// Copy one box of a 3-D tensor map (x, row, field) to shared memory (128-byte aligned), counted
+// against `bar`.  The box's bytes complete the phase in full, parts outside the tensor as zeros.
+// x times the element size must be a multiple of 16 bytes.  `map` is the address of a
+// __grid_constant__ kernel parameter.
+CG_D void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+        : "memory");
 }
 
 // Wait until phase `parity` of `bar` has completed.  Gives up after about `cycles` SM clocks and
