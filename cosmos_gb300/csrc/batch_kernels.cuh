@@ -53,6 +53,7 @@ struct BatchDev {
     void* buf[2];
     GridBarrier* bar;
     int* gstep;                 // steps completed by the batch (buffer parity)
+    const CUtensorMap* maps;    // FP32: tensor map of buffer k's grid g at maps[k * ngrids + g] (null: per-field copies)
 };
 
 // dt of one step from the last CFL reduction (Solvers/EulerSolvers.cpp:130-161); the solver loop's
@@ -211,9 +212,10 @@ constexpr size_t batch_pair_smem(int nt) {
 // FP32 batch on cell pairs (sweep_pairs.cuh), one warp per item and no block barrier inside a
 // phase; warps take the items of a phase's longest-first list through an atomic counter, so a
 // warp that finishes early takes more.  X items are runs of 60-cell segments of one grid (the next
-// segment loaded while the current one is computed); Y items are 64 columns (a pair per lane) x a run of rows, marched
-// through the warp's ring of rows staged by bulk copies (y_ring_march), its barriers initialised
-// again before each item.  Each warp reads its item's time step and reduces its own CFL maximum.
+// segment loaded while the current one is computed); Y items are 64 columns (a pair per lane) x a
+// run of rows, marched through the warp's ring of rows staged by one tensor-map copy per row
+// (y_ring_march; the grid's map of the source buffer), its barriers initialised again before each
+// item.  Each warp reads its item's time step and reduces its own CFL maximum.
 // Same phases, grid barriers and per-grid controllers as batch_step_kernel.  A ring wait that runs
 // out sets ST_TIMEOUT in the grid's status and in the barrier's error word, so every block leaves
 // at the next barrier.
@@ -286,7 +288,9 @@ __global__ void __launch_bounds__(NT, MINB) batch_pair_kernel(NewtonFastParams P
                         if (ring_used) ring_init<R>(wbar, true);
                         ring_used = true;
                         // the Y phase never reduces the CFL maximum (the last X sweep does)
-                        y_ring_march<LIM, R>(P, G.dims, G, sg, dg, it.a, it.b, it.c, cf, false, ring[warp], wbar, ring_ok);
+                        const CUtensorMap* tm = B.maps ? B.maps + (size_t)(p ? 0 : 1) * B.ngrids + it.g : nullptr;
+                        y_ring_march<LIM, R, 2>(P, G.dims, G, sg, dg, it.a, it.b, it.c, cf, false, ring[warp], wbar,
+                                                ring_ok, tm);
                         if (!ring_ok && lane == 0) {
                             atomicOr(&ctl->status, ST_TIMEOUT);
                             atomicOr(&B.bar->err, ST_TIMEOUT);

@@ -56,6 +56,7 @@ struct cosmos_batch {
     GridBarrier* d_bar;
     int* d_gstep;
     unsigned int* d_take;  // FP32 item counters (2 step parities x 3 phases)
+    CUtensorMap* d_maps;   // FP32: per buffer and 2D grid, the Y items' tensor maps (null: per-field copies)
     double* d_staging;
     size_t max_cells;
     // work lists for the current tile shape
@@ -91,6 +92,7 @@ BatchDev dev_desc(cosmos_batch* b) {
     B.bar = b->d_bar;
     B.gstep = b->d_gstep;
     B.take = b->d_take;
+    B.maps = b->d_maps;
     return B;
 }
 
@@ -356,6 +358,20 @@ int cosmos_batch_create(cosmos_ctx* ctx, int ngrids, const int* dims, const int*
     if (e == cudaSuccess) e = cudaMemset(b->d_bar, 0, sizeof(GridBarrier));
     if (e == cudaSuccess) e = cudaMemset(b->d_ctl, 0, ngrids * sizeof(StepCtl));
     for (int k = 0; k < 2 && e == cudaSuccess; k++) e = cudaMemset(b->buf[k], 0, off * b->elem);
+    if (e == cudaSuccess && precision == COSMOS_FP32) {  // the Y items' rows: one tensor-map copy each
+        std::vector<CUtensorMap> maps(2 * (size_t)ngrids);
+        bool ok = true;
+        for (int k = 0; k < 2; k++)
+            for (int g = 0; g < ngrids; g++)
+                if (b->grids[g].G.dims == 2)
+                    ok = ok && field_map(&maps[(size_t)k * ngrids + g], (const float*)b->buf[k] + b->grids[g].off,
+                                         b->grids[g].G, 64);
+        if (ok) {
+            e = cudaMalloc(&b->d_maps, maps.size() * sizeof(CUtensorMap));
+            if (e == cudaSuccess)
+                e = cudaMemcpy(b->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice);
+        }
+    }
     if (e != cudaSuccess) {
         std::string msg = std::string("batch allocation: ") + cudaGetErrorString(e);
         cosmos_batch_destroy(b);
@@ -374,6 +390,7 @@ int cosmos_batch_destroy(cosmos_batch* b) {
     cudaStreamSynchronize(b->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     for (int k = 0; k < 2; k++) if (b->buf[k]) cudaFree(b->buf[k]);
+    if (b->d_maps) cudaFree(b->d_maps);
     for (int k = 0; k < 3; k++) {
         if (b->d_items[k]) cudaFree(b->d_items[k]);
         if (b->d_offs[k]) cudaFree(b->d_offs[k]);

@@ -51,9 +51,8 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
-// A 3-D tensor map of an FP32 SoA state (x: nx cells, y: ny rows of G.pitch, z: the five fields
-// G.fstride apart) whose box is `box_x` cells of one row in every field.  False when the state
-// cannot be described (the sweeps then copy each field by itself).
+}  // namespace
+
 bool field_map(CUtensorMap* m, const float* base, const Geom& G, unsigned box_x) {
     const auto encode = tensor_map_encoder();
     if (!encode || ((uintptr_t)base & 15) || box_x > 256 || (box_x * 4) % 16) return false;
@@ -64,6 +63,8 @@ bool field_map(CUtensorMap* m, const float* base, const Geom& G, unsigned box_x)
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
+
+namespace {
 
 template <int AXIS, int LIM, bool MASKED>
 NewtonFastPolicy<AXIS, LIM, MASKED> make_fast(const SweepArgs& a) {

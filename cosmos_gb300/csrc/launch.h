@@ -6,6 +6,8 @@
 #include "device_common.cuh"
 #include "sweep_kernels.cuh"
 
+struct CUtensorMap_st;  // <cuda.h>'s tensor-map descriptor (CUtensorMap)
+
 namespace cg {
 
 // Metric tables of a black-hole grid with FP32 storage (physics_gr_fast.cuh), built once in FP64.
@@ -110,6 +112,10 @@ cudaError_t launch_spacetime_eval(const SweepArgs& s, size_t n, const double* xy
 
 // FP32 bulk path (conserved SoA storage, float)
 cudaError_t launch_sweep_fast(const SweepArgs& a);
+// A 3-D tensor map of an FP32 SoA state at `base` (x: nx cells, y: ny rows G.pitch apart, z: the
+// five fields G.fstride apart) whose box is `box_x` cells of one row in every field; false when
+// the state cannot be described (the sweeps then copy each field by itself).
+bool field_map(CUtensorMap_st* m, const float* base, const Geom& G, unsigned box_x);
 cudaError_t launch_wavespeed_fast(const SweepArgs& a, unsigned long long* slot);
 cudaError_t launch_prim_in_fast(const double* aos, void* soa, const Geom& G, int system, double gamma,
                                 cudaStream_t st);

@@ -203,7 +203,7 @@ CG_D void ring_init(unsigned long long* bar, bool reinit) {
 // together, with jw < G.nx.  Returns the lane's wavespeed maximum over its updated cells when
 // want_w.  A wait that runs out (about a second) makes `ok` false (warp-uniform); the warp then
 // waits, again bounded, for its rows still in flight and returns.  On success the ring is drained.
-template <int LIM, int R, bool TM = false>
+template <int LIM, int R, int TM = 0>
 CG_D float y_ring_march(const NewtonFastParams& P, int dims, const Geom& G, const float* __restrict__ src,
                         float* __restrict__ dst, int jw, int y0, int y1, const FastCoef cf, bool want_w,
                         float (*ring)[5][64], unsigned long long* bar, bool& ok, const CUtensorMap* tm = nullptr) {
@@ -216,13 +216,14 @@ CG_D float y_ring_march(const NewtonFastParams& P, int dims, const Geom& G, cons
     const uint32_t bytes = ((uint32_t)min(64, G.nx - jw) * 4u + 15u) & ~15u;  // within the padded pitch
     const int ylo = y0 - 2, yhi = y1 + 1;  // rows read
     // Row r of the ring lives in slot (r - ylo) mod R; the slot's k-th use completes phase k mod 2.
-    // TM: lane 0 copies the row's five fields as one box of the tensor map; otherwise lanes 0-4
-    // each copy one field (lanes 5+ hold a valid pointer they never use).
+    // TM = 1 (TM = 2: when tm is not null): lane 0 copies the row's five fields as one box of the
+    // tensor map tm; otherwise lanes 0-4 each copy one field (lanes 5+ hold a valid pointer they
+    // never use).
     const float* fsrc = src + (size_t)min(lane, 4) * G.fstride + jw;
     int inext = ylo;  // warp-uniform: next row to issue
     auto issue_one = [&]() {
         const int r = inext, q = (r - ylo) & (R - 1);
-        if (TM) {  // one copy of the row's five 64-column runs (columns past nx arrive as zeros)
+        if (TM == 1 || (TM == 2 && tm)) {  // one copy of the row's five 64-column runs (columns past nx arrive as zeros)
             if (lane == 0) {
                 mbar_expect_tx(&bar[q], 5 * 64 * 4);
                 tma_load_3d(ring[q], tm, jw, ghost_index(r, G.ny, G.bc), 0, &bar[q]);
@@ -346,7 +347,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_y_ring_kernel(NewtonFastParams
     const FastCoef cf = s_coef;  // in registers: the ring's waits would make every use re-read shared memory
     // the reduction stays a run-time choice here: the compile-time form measured 3 % slower
     unsigned long long* wslot = out.slot();
-    float w = y_ring_march<LIM, R, TM>(P, dims, G, src, dst, jw, y0, y1, cf, wslot != nullptr, ring[wp], bar[wp], ok,
+    float w = y_ring_march<LIM, R, TM ? 1 : 0>(P, dims, G, src, dst, jw, y0, y1, cf, wslot != nullptr, ring[wp], bar[wp], ok,
                                        &tm);
     if (!ok) {
         if (lane == 0 && out.status) atomicOr(out.status, ST_TIMEOUT);
