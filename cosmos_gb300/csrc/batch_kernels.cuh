@@ -33,7 +33,7 @@ struct BatchGrid {
 // reduction are paid once per few thousand cells.
 struct BatchItem { int g, a, b, c; };
 
-// Rows' worth of 60-cell segments in one FP32 X item.
+// Most 60-cell segments in one FP32 X item (fewer when the batch gives each warp few items).
 constexpr int kBatchXSegs = 64;
 
 struct GridBarrier {

@@ -105,8 +105,9 @@ void* kernel_fn(cosmos_batch* b, int nt, int seg, int cap, int lim) {
 
 // Work lists for a tile shape, one per phase.  FP64 (one-cell tiles, one block per item): X items
 // are whole rows of one grid, as many as make about 8 tiles of nt - 2 cells; Y items nt columns x
-// seg rows.  FP32 (cell pairs, one warp per item): X items are runs of kBatchXSegs 60-cell segments
-// of one grid, numbered row by row (a = first, b = one past the last); Y items 64 columns x seg rows.
+// seg rows.  FP32 (cell pairs, one warp per item): X items are runs of up to kBatchXSegs 60-cell
+// segments of one grid, numbered row by row (a = first, b = one past the last); Y items 64 columns
+// x seg rows.
 // Costs are cells swept (Y counting its four halo rows) plus a per-item overhead.  FP32: the warps
 // take the items as they become free (one atomic counter over the launch's steps and phases), grid
 // by grid, the grids by descending cost.  FP64: sorted longest item first, each item is dealt onto
@@ -126,12 +127,24 @@ int build_items(cosmos_batch* b, int nt, int seg, int cap) {
     std::vector<Costed> ph[3];
     std::vector<int> gcount(3 * b->grids.size(), 0);  // FP32: items per grid and phase
     const long long overhead = 32;
+    // FP32 X items: about four per warp in a phase, 8 to kBatchXSegs segments.  An item waits for
+    // its grid's previous phase, so a grid's phase takes at least one item's time: with few
+    // items per warp, long items set the step's critical path (16 grids: 0.675 ms per step with
+    // 64-segment items, 0.188 with 8; 64 grids: 0.928 and 0.485 ms), with many (256 grids) short
+    // items only add set-up (64 segments: 1.575 ms, 16: 1.647).
+    int xsegs = kBatchXSegs;
+    if (pairs) {
+        long long segs = 0;
+        for (const BatchGrid& bg : b->grids) segs += (long long)((bg.G.nx + 59) / 60) * bg.G.ny;
+        const long long per = 4ll * blocks * (nt / 32);
+        xsegs = (int)std::max<long long>(8, std::min<long long>(kBatchXSegs, (segs + per - 1) / per));
+    }
     for (int g = 0; g < (int)b->grids.size(); g++) {
         const Geom& G = b->grids[g].G;
         if (pairs) {
             const int spr = (G.nx + 59) / 60, total = spr * G.ny;
-            for (int q = 0; q < total; q += kBatchXSegs) {
-                const BatchItem it{g, q, std::min(q + kBatchXSegs, total), 0};
+            for (int q = 0; q < total; q += xsegs) {
+                const BatchItem it{g, q, std::min(q + xsegs, total), 0};
                 const long long c = 64ll * (it.b - it.a) + overhead;
                 ph[0].push_back({c, it});
                 if (G.dims == 2) ph[2].push_back({c, it});
