@@ -373,7 +373,11 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
     V* sB = sA + 5 * NW;    // [5]  Ubar' (phase 0-2), then the contribution to the right neighbour
     V* sC = sB + 5 * NW;    // [10] A,B evolved states (1-2), then contributions to self and left neighbour
     V* sD = sC + 10 * NW;   // [10] Abar of the right state, Bbar of the left state per face
-    V* sE = sD + 10 * NW;   // [15] slope sl and reverse factors P, Q of each cell (phase 1 -> 3)
+    // [15] X sweep: slope sl and reverse factors P, Q of each cell (phase 1 -> 3); the Y sweep keeps
+    // them in the thread's registers (its blocks are bound by shared-memory instruction issue; in
+    // the X sweep the registers spill)
+    constexpr bool kRegSlope = AX == 1;
+    V* sE = sD + 10 * NW;
     const Geom& G = a.G;
     const int along = AX == 0 ? threadIdx.x : threadIdx.y;
     const int across = AX == 0 ? threadIdx.y : threadIdx.x;
@@ -473,8 +477,9 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
             for (int f = 0; f < 5; f++) out[f] = arr[f * NW + x];
         };
         // ---- 1: half-step evolution of every cell with both neighbours in the tile
+        V sl[5], Pf[5], Qf[5];
         if (lok && along >= 1 && along < P - 1) {
-            V ul[5], uc[5], ur[5], A[5], B[5], sl[5], Pf[5], Qf[5];
+            V ul[5], uc[5], ur[5], A[5], B[5];
             ld(sA, along - 1, ul);
             ld(sA, along, uc);
             ld(sA, along + 1, ur);
@@ -483,9 +488,11 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
             for (int f = 0; f < 5; f++) {
                 sC[f * NW + me] = A[f];
                 sC[(5 + f) * NW + me] = B[f];
-                sE[f * NW + me] = sl[f];
-                sE[(5 + f) * NW + me] = Pf[f];
-                sE[(10 + f) * NW + me] = Qf[f];
+                if (!kRegSlope) {
+                    sE[f * NW + me] = sl[f];
+                    sE[(5 + f) * NW + me] = Pf[f];
+                    sE[(10 + f) * NW + me] = Qf[f];
+                }
             }
         }
         __syncthreads();
@@ -515,11 +522,13 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
             V gl[5] = {zero, zero, zero, zero, zero}, gc[5] = {zero, zero, zero, zero, zero},
               gr[5] = {zero, zero, zero, zero, zero};
             if (lok && (per || (k >= -1 && k <= n))) {
-                V uc[5], sl[5], Pf[5], Qf[5], Ab[5], Bb[5];
+                V uc[5], Ab[5], Bb[5];
                 ld(sA, along, uc);
-                ld(sE, along, sl);
-                ld(sE + 5 * NW, along, Pf);
-                ld(sE + 10 * NW, along, Qf);
+                if (!kRegSlope) {
+                    ld(sE, along, sl);
+                    ld(sE + 5 * NW, along, Pf);
+                    ld(sE + 10 * NW, along, Qf);
+                }
                 const int pv = si(along - 1);
 #pragma unroll
                 for (int f = 0; f < 5; f++) {
@@ -654,7 +663,7 @@ cudaError_t launch_adjoint_sweep_t(const AdjSweepParams& a, cudaStream_t st) {
     constexpr int P = AX == 0 ? (Lane<V>::N == 2 ? 128 : 256) : 64;
     constexpr int W = AX == 0 ? 1 : 4;
     constexpr int LB = W * Lane<V>::N;  // lines per block
-    const size_t smem = (size_t)45 * P * W * sizeof(V);
+    const size_t smem = (size_t)(AX == 1 ? 30 : 45) * P * W * sizeof(V);
     auto kern = adjoint_sweep_kernel<V, S, PRIM, AX, LIM, P, W>;
     // per instantiation: the attribute and the resident-block count (one GPU model per process)
     static int resident = 0;
