@@ -330,6 +330,49 @@ CG_D void st_lanes(float* p, size_t q0, size_t q1, bool vec, bool two, f2 v) {
     }
 }
 
+// Five-field vectors in shared memory, field f of slot x at arr[f * NW + x].  WIDE, for cell pairs
+// (f2): fields 0-1 and 2-3 share one 16-byte word each instead (the first four field planes read
+// as two float4 planes), so a vector moves in three shared-memory instructions instead of five;
+// `arr` is then 16-byte aligned and NW even.
+template <int NW, bool WIDE, class V>
+CG_D void sv_st(V* arr, int x, const V* v) {
+#pragma unroll
+    for (int f = 0; f < 5; f++) arr[f * NW + x] = v[f];
+}
+template <int NW, bool WIDE, class V>
+CG_D void sv_ld(const V* arr, int x, V* v) {
+#pragma unroll
+    for (int f = 0; f < 5; f++) v[f] = arr[f * NW + x];
+}
+template <int NW, bool WIDE>
+CG_D void sv_st(f2* arr, int x, const f2* v) {
+    if constexpr (WIDE) {
+        static_assert(NW % 2 == 0, "16-byte planes");
+        float4* a4 = reinterpret_cast<float4*>(arr);
+        a4[x] = make_float4(v[0].v.x, v[0].v.y, v[1].v.x, v[1].v.y);
+        a4[NW + x] = make_float4(v[2].v.x, v[2].v.y, v[3].v.x, v[3].v.y);
+        arr[4 * NW + x] = v[4];
+    } else {
+#pragma unroll
+        for (int f = 0; f < 5; f++) arr[f * NW + x] = v[f];
+    }
+}
+template <int NW, bool WIDE>
+CG_D void sv_ld(const f2* arr, int x, f2* v) {
+    if constexpr (WIDE) {
+        const float4* a4 = reinterpret_cast<const float4*>(arr);
+        const float4 p = a4[x], q = a4[NW + x];
+        v[0].v = make_float2(p.x, p.y);
+        v[1].v = make_float2(p.z, p.w);
+        v[2].v = make_float2(q.x, q.y);
+        v[3].v = make_float2(q.z, q.w);
+        v[4] = arr[4 * NW + x];
+    } else {
+#pragma unroll
+        for (int f = 0; f < 5; f++) v[f] = arr[f * NW + x];
+    }
+}
+
 // Tiles of P positions along a line of n cells.  An interior cell's adjoint gathers the
 // contributions of its two neighbours, so a tile updates positions 3 .. P - 4 (P - 6 cells) and
 // starts 3 cells before its first one; a cell within two of a line end also gathers from the ghost
@@ -369,6 +412,7 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
     static_assert(!PRIM || NL == 1, "primitive storage is the FP64 one-line path");
     constexpr int NW = P * W;
     extern __shared__ __align__(16) unsigned char adj_smem[];
+    static_assert(NW % 2 == 0, "every five-field array starts 16-byte aligned");  // (sv_st / sv_ld WIDE)
     V* sA = (V*)adj_smem;   // [5]  state
     V* sB = sA + 5 * NW;    // [5]  Ubar' (phase 0-2), then the contribution to the right neighbour
     V* sC = sB + 5 * NW;    // [10] A,B evolved states (1-2), then contributions to self and left neighbour
@@ -377,6 +421,9 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
     // them in the thread's registers (its blocks are bound by shared-memory instruction issue; in
     // the X sweep the registers spill)
     constexpr bool kRegSlope = AX == 1;
+    // Y: five-field vectors in 16-byte shared-memory words (150.7 against 154 us per 2048^2 sweep);
+    // in the X sweep the same measured slower (121.9 against 119 us)
+    constexpr bool kWide = AX == 1;
     V* sE = sD + 10 * NW;
     const Geom& G = a.G;
     const int along = AX == 0 ? threadIdx.x : threadIdx.y;
@@ -461,21 +508,15 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
 #pragma unroll
                 for (int f = 0; f < 5; f++) u[f] = ru[f];
             }
+            sv_st<NW, kWide>(sA, me, u);
+            sv_st<NW, kWide>(sB, me, rb);
 #pragma unroll
-            for (int f = 0; f < 5; f++) {
-                sA[f * NW + me] = u[f];
-                sB[f * NW + me] = rb[f];
-                ub_own[f] = rb[f];
-            }
+            for (int f = 0; f < 5; f++) ub_own[f] = rb[f];
         }
         __syncthreads();
         // the next tile's inputs load while this one is computed
         if (t + (int)gridDim.x < ntiles) fetch(place(t + gridDim.x));
-        auto ld = [&](const V* arr, int pos, V* out) {
-            const int x = si(pos);
-#pragma unroll
-            for (int f = 0; f < 5; f++) out[f] = arr[f * NW + x];
-        };
+        auto ld = [&](const V* arr, int pos, V* out) { sv_ld<NW, kWide>(arr, si(pos), out); };
         // ---- 1: half-step evolution of every cell with both neighbours in the tile
         V sl[5], Pf[5], Qf[5];
         if (lok && along >= 1 && along < P - 1) {
@@ -484,15 +525,12 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
             ld(sA, along, uc);
             ld(sA, along + 1, ur);
             adj_evolve<V, AX, LIM>(F, Sl, ul, uc, ur, hs, A, B, sl, Pf, Qf);
-#pragma unroll
-            for (int f = 0; f < 5; f++) {
-                sC[f * NW + me] = A[f];
-                sC[(5 + f) * NW + me] = B[f];
-                if (!kRegSlope) {
-                    sE[f * NW + me] = sl[f];
-                    sE[(5 + f) * NW + me] = Pf[f];
-                    sE[(10 + f) * NW + me] = Qf[f];
-                }
+            sv_st<NW, kWide>(sC, me, A);
+            sv_st<NW, kWide>(sC + 5 * NW, me, B);
+            if (!kRegSlope) {
+                sv_st<NW, kWide>(sE, me, sl);
+                sv_st<NW, kWide>(sE + 5 * NW, me, Pf);
+                sv_st<NW, kWide>(sE + 10 * NW, me, Qf);
             }
         }
         __syncthreads();
@@ -500,21 +538,18 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
         if (along >= 1 && along < P - 2) {
             V Lb[5] = {zero, zero, zero, zero, zero}, Rb[5] = {zero, zero, zero, zero, zero};
             if (lok && (per || (k >= -1 && k <= n - 1))) {
-                V L[5], R[5], Fb[5];
+                V L[5], R[5], Fb[5], bn[5], bm[5];
                 const int nx1 = si(along + 1);
+                sv_ld<NW, kWide>(sC + 5 * NW, me, L);
+                sv_ld<NW, kWide>(sC, nx1, R);
+                sv_ld<NW, kWide>(sB, nx1, bn);
+                sv_ld<NW, kWide>(sB, me, bm);
 #pragma unroll
-                for (int f = 0; f < 5; f++) {
-                    L[f] = sC[(5 + f) * NW + me];
-                    R[f] = sC[f * NW + nx1];
-                    Fb[f] = vmul(d, vsub(sB[f * NW + nx1], sB[f * NW + me]));
-                }
+                for (int f = 0; f < 5; f++) Fb[f] = vmul(d, vsub(bn[f], bm[f]));
                 adj_force_vjp<V, AX>(F, L, R, c, d, Fb, Lb, Rb);
             }
-#pragma unroll
-            for (int f = 0; f < 5; f++) {
-                sD[f * NW + me] = Lb[f];        // adjoint of B_k
-                sD[(5 + f) * NW + me] = Rb[f];  // adjoint of A_{k+1}
-            }
+            sv_st<NW, kWide>(sD, me, Lb);           // adjoint of B_k
+            sv_st<NW, kWide>(sD + 5 * NW, me, Rb);  // adjoint of A_{k+1}
         }
         __syncthreads();
         // ---- 3: half-step reverse of this cell; neither sB nor sC is read in this phase
@@ -529,20 +564,13 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
                     ld(sE + 5 * NW, along, Pf);
                     ld(sE + 10 * NW, along, Qf);
                 }
-                const int pv = si(along - 1);
-#pragma unroll
-                for (int f = 0; f < 5; f++) {
-                    Bb[f] = sD[f * NW + me];
-                    Ab[f] = sD[(5 + f) * NW + pv];
-                }
+                sv_ld<NW, kWide>(sD, me, Bb);
+                sv_ld<NW, kWide>(sD + 5 * NW, si(along - 1), Ab);
                 adj_evolve_vjp<V, AX>(F, uc, sl, Pf, Qf, hs, Ab, Bb, gl, gc, gr);
             }
-#pragma unroll
-            for (int f = 0; f < 5; f++) {
-                sC[f * NW + me] = gc[f];
-                sC[(5 + f) * NW + me] = gl[f];
-                sB[f * NW + me] = gr[f];
-            }
+            sv_st<NW, kWide>(sC, me, gc);
+            sv_st<NW, kWide>(sC + 5 * NW, me, gl);
+            sv_st<NW, kWide>(sB, me, gr);
         }
         __syncthreads();
         // ---- 4: gather for the updated cells
@@ -552,10 +580,12 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
             for (int f = 0; f < 5; f++) acc[f] = ub_own[f];
             if (k >= 2 && k <= n - 3) {
                 // interior (n >= 5): the right neighbour of k - 1, k itself, the left neighbour of k + 1
-                const int xl = si(along - 1), xr = si(along + 1);
+                V gr_l[5], gc_k[5], gl_r[5];
+                sv_ld<NW, kWide>(sB, si(along - 1), gr_l);
+                sv_ld<NW, kWide>(sC, me, gc_k);
+                sv_ld<NW, kWide>(sC + 5 * NW, si(along + 1), gl_r);
 #pragma unroll
-                for (int f = 0; f < 5; f++)
-                    acc[f] = vadd(acc[f], vadd(vadd(sB[f * NW + xl], sC[f * NW + me]), sC[(5 + f) * NW + xr]));
+                for (int f = 0; f < 5; f++) acc[f] = vadd(acc[f], vadd(vadd(gr_l[f], gc_k[f]), gl_r[f]));
             } else
 #pragma unroll
             for (int dd = -2; dd <= 2; dd++) {
@@ -568,8 +598,10 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
                     const int tgt = per ? ((i + q) % n + n) % n : (i + q < 0 ? -1 - (i + q) : (i + q >= n ? 2 * n - 1 - (i + q) : i + q));
                     if (tgt != k) continue;
                     const V* src = q == -1 ? sC + 5 * NW : (q == 0 ? sC : sB);
+                    V g[5];
+                    sv_ld<NW, kWide>(src, x, g);
 #pragma unroll
-                    for (int f = 0; f < 5; f++) acc[f] = vadd(acc[f], src[f * NW + x]);
+                    for (int f = 0; f < 5; f++) acc[f] = vadd(acc[f], g[f]);
                 }
             }
             T* ubi = (T*)a.ubar_in;
