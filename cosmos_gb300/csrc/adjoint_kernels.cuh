@@ -424,6 +424,10 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
     // Y: five-field vectors in 16-byte shared-memory words (150.7 against 154 us per 2048^2 sweep);
     // in the X sweep the same measured slower (121.9 against 119 us)
     constexpr bool kWide = AX == 1;
+    // X: the cell's right-face state, its adjoint and the contribution to the cell itself stay in
+    // registers between the phases that write and read them (in the Y sweep, whose registers also
+    // hold the slope factors, they spill)
+    constexpr bool kRegOwn = AX == 0;
     V* sE = sD + 10 * NW;
     const Geom& G = a.G;
     const int along = AX == 0 ? threadIdx.x : threadIdx.y;
@@ -517,16 +521,19 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
         // the next tile's inputs load while this one is computed
         if (t + (int)gridDim.x < ntiles) fetch(place(t + gridDim.x));
         auto ld = [&](const V* arr, int pos, V* out) { sv_ld<NW, kWide>(arr, si(pos), out); };
-        // ---- 1: half-step evolution of every cell with both neighbours in the tile
-        V sl[5], Pf[5], Qf[5];
+        // ---- 1: half-step evolution of every cell with both neighbours in the tile.  kRegOwn: values
+        // that only this thread reads in the next phase stay in its registers -- the cell's
+        // right-face state B (phase 2), the adjoint of B (phase 3), the contribution to the cell
+        // itself (phase 4; also stored, for the gather at line ends)
+        V sl[5], Pf[5], Qf[5], B[5], Lb[5], gc[5];
         if (lok && along >= 1 && along < P - 1) {
-            V ul[5], uc[5], ur[5], A[5], B[5];
+            V ul[5], uc[5], ur[5], A[5];
             ld(sA, along - 1, ul);
             ld(sA, along, uc);
             ld(sA, along + 1, ur);
             adj_evolve<V, AX, LIM>(F, Sl, ul, uc, ur, hs, A, B, sl, Pf, Qf);
             sv_st<NW, kWide>(sC, me, A);
-            sv_st<NW, kWide>(sC + 5 * NW, me, B);
+            if (!kRegOwn) sv_st<NW, kWide>(sC + 5 * NW, me, B);
             if (!kRegSlope) {
                 sv_st<NW, kWide>(sE, me, sl);
                 sv_st<NW, kWide>(sE + 5 * NW, me, Pf);
@@ -536,37 +543,40 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
         __syncthreads();
         // ---- 2: FORCE reverse at the face between this cell (k) and the next (k + 1)
         if (along >= 1 && along < P - 2) {
-            V Lb[5] = {zero, zero, zero, zero, zero}, Rb[5] = {zero, zero, zero, zero, zero};
+            V Rb[5] = {zero, zero, zero, zero, zero};
+#pragma unroll
+            for (int f = 0; f < 5; f++) Lb[f] = zero;
             if (lok && (per || (k >= -1 && k <= n - 1))) {
-                V L[5], R[5], Fb[5], bn[5], bm[5];
+                V R[5], Fb[5], bn[5], bm[5];
                 const int nx1 = si(along + 1);
-                sv_ld<NW, kWide>(sC + 5 * NW, me, L);
+                if (!kRegOwn) sv_ld<NW, kWide>(sC + 5 * NW, me, B);
                 sv_ld<NW, kWide>(sC, nx1, R);
                 sv_ld<NW, kWide>(sB, nx1, bn);
                 sv_ld<NW, kWide>(sB, me, bm);
 #pragma unroll
                 for (int f = 0; f < 5; f++) Fb[f] = vmul(d, vsub(bn[f], bm[f]));
-                adj_force_vjp<V, AX>(F, L, R, c, d, Fb, Lb, Rb);
+                adj_force_vjp<V, AX>(F, B, R, c, d, Fb, Lb, Rb);
             }
-            sv_st<NW, kWide>(sD, me, Lb);           // adjoint of B_k
-            sv_st<NW, kWide>(sD + 5 * NW, me, Rb);  // adjoint of A_{k+1}
+            if (!kRegOwn) sv_st<NW, kWide>(sD, me, Lb);  // adjoint of B_k
+            sv_st<NW, kWide>(sD + 5 * NW, me, Rb);        // adjoint of A_{k+1}
         }
         __syncthreads();
         // ---- 3: half-step reverse of this cell; neither sB nor sC is read in this phase
         if (along >= 2 && along < P - 2) {
-            V gl[5] = {zero, zero, zero, zero, zero}, gc[5] = {zero, zero, zero, zero, zero},
-              gr[5] = {zero, zero, zero, zero, zero};
+            V gl[5] = {zero, zero, zero, zero, zero}, gr[5] = {zero, zero, zero, zero, zero};
+#pragma unroll
+            for (int f = 0; f < 5; f++) gc[f] = zero;
             if (lok && (per || (k >= -1 && k <= n))) {
-                V uc[5], Ab[5], Bb[5];
+                V uc[5], Ab[5];
                 ld(sA, along, uc);
                 if (!kRegSlope) {
                     ld(sE, along, sl);
                     ld(sE + 5 * NW, along, Pf);
                     ld(sE + 10 * NW, along, Qf);
                 }
-                sv_ld<NW, kWide>(sD, me, Bb);
+                if (!kRegOwn) sv_ld<NW, kWide>(sD, me, Lb);
                 sv_ld<NW, kWide>(sD + 5 * NW, si(along - 1), Ab);
-                adj_evolve_vjp<V, AX>(F, uc, sl, Pf, Qf, hs, Ab, Bb, gl, gc, gr);
+                adj_evolve_vjp<V, AX>(F, uc, sl, Pf, Qf, hs, Ab, Lb, gl, gc, gr);
             }
             sv_st<NW, kWide>(sC, me, gc);
             sv_st<NW, kWide>(sC + 5 * NW, me, gl);
@@ -580,12 +590,12 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
             for (int f = 0; f < 5; f++) acc[f] = ub_own[f];
             if (k >= 2 && k <= n - 3) {
                 // interior (n >= 5): the right neighbour of k - 1, k itself, the left neighbour of k + 1
-                V gr_l[5], gc_k[5], gl_r[5];
+                V gr_l[5], gl_r[5];
+                if (!kRegOwn) sv_ld<NW, kWide>(sC, me, gc);
                 sv_ld<NW, kWide>(sB, si(along - 1), gr_l);
-                sv_ld<NW, kWide>(sC, me, gc_k);
                 sv_ld<NW, kWide>(sC + 5 * NW, si(along + 1), gl_r);
 #pragma unroll
-                for (int f = 0; f < 5; f++) acc[f] = vadd(acc[f], vadd(vadd(gr_l[f], gc_k[f]), gl_r[f]));
+                for (int f = 0; f < 5; f++) acc[f] = vadd(acc[f], vadd(vadd(gr_l[f], gc[f]), gl_r[f]));
             } else
 #pragma unroll
             for (int dd = -2; dd <= 2; dd++) {
