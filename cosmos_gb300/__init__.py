@@ -10,7 +10,7 @@ from .solvers import (BlackHoleEulerFirstOrderSolver, BlackHoleEulerForcingSolve
                       BlackHoleEulerSecondOrderSolver, BlackHoleEulerSolvers, BlackHoleSpacetime, Context,
                       EulerFirstOrderSolver, EulerMaterialParameters, EulerSecondOrderSolver, EulerSolvers, Grid,
                       RelativisticEulerFirstOrderSolver, RelativisticEulerSecondOrderSolver, RelativisticEulerSolvers,
-                      default_context, solve_with_steps)
+                      default_context, set_tensor_maps, solve_with_steps)
 from .solvers import (AMR, Batch, EulerAMR, EulerEquationOfState, RelativisticEulerAMR,  # noqa: F401
                       RelativisticEulerEquationOfState, SlopeLimiters, interface_eval, state_eval)
 

@@ -58,6 +58,7 @@ SIGNATURES = {
     "cosmos_version": (ctypes.c_char_p, []),
     "cosmos_last_error": (ctypes.c_char_p, []),
     "cosmos_kernel_launches": (ctypes.c_ulonglong, []),
+    "cosmos_set_tensor_maps": (_i, [_i]),
     "cosmos_params_default": (None, [ctypes.POINTER(Params)]),
     "cosmos_solve_opts_default": (None, [ctypes.POINTER(SolveOpts)]),
     "cosmos_stable_dt_rule": (_d, [_d, _d, _d, _i]),

@@ -1,6 +1,8 @@
 // FP32 bulk kernels (Newtonian system; the SR system's live in kernels_sr_fast.cu): conserved SoA float storage, FMA contraction on.
 #include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
 
+#include <atomic>
+
 #include "launch.h"
 #include "policies.cuh"
 #include "sweep_pairs.cuh"
@@ -53,7 +55,10 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 
 }  // namespace
 
+std::atomic<int> g_tensor_maps{1};
+
 bool field_map(CUtensorMap* m, const float* base, const Geom& G, unsigned box_x) {
+    if (!g_tensor_maps.load(std::memory_order_relaxed)) return false;
     const auto encode = tensor_map_encoder();
     if (!encode || ((uintptr_t)base & 15) || box_x > 256 || (box_x * 4) % 16) return false;
     const cuuint64_t dim[3] = {(cuuint64_t)G.nx, (cuuint64_t)G.ny, 5};
@@ -211,3 +216,5 @@ cudaError_t launch_prim_out_fast(const void* soa, double* aos, const Geom& G, in
 }
 
 }  // namespace cg
+
+extern "C" int cosmos_set_tensor_maps(int enable) { return cg::g_tensor_maps.exchange(enable ? 1 : 0); }

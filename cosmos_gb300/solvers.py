@@ -194,6 +194,13 @@ class Context:
             pass
 
 
+def set_tensor_maps(enable):
+    """FP32 sweeps stage rows through TMA tensor maps (True, the default) or one copy per field
+    (False); results are bit-identical.  Read when a sweep is launched or captured and when a batch
+    is created.  Returns the previous setting."""
+    return bool(load().cosmos_set_tensor_maps(1 if enable else 0))
+
+
 def default_context():
     c = getattr(_tls, "ctx", None)
     if c is None:

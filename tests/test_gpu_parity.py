@@ -227,6 +227,42 @@ def test_chunk_replay_equals_single_steps(cg, precision):
     assert r.steps == 11
 
 
+@pytest.mark.parametrize("bc", [0, 1])
+def test_tensor_map_staging_is_bit_identical(cg, bc):
+    """FP32 rows staged through TMA tensor maps (one copy of a row's five fields: the Y sweep and the
+    CFL-reducing X sweep of single grids, the batch's Y items) and by one copy per field give the
+    same states bit for bit: a grid whose rows hold several inside segments and whose last column
+    run passes nx (300 columns), and a batch of uneven grids."""
+    rng = np.random.default_rng(21)
+    s = cases.newton_state(rng, (136, 300))
+    shapes = [(130, 260), (300,), (70, 190), (64, 64)]
+    states = [cases.newton_state(rng, sh) for sh in shapes]
+    out = []
+    try:
+        for on in (True, False):
+            cg.set_tensor_maps(on)
+            g = grid_from(cg, 0, s, 1.0 / 300, precision=1, bc=bc)
+            g.run_begin(2, 0.8, 1e9, 0.0, 2, max_steps=9)
+            g.run_steps(9)
+            r = g.run_end()
+            b = cg.solvers.Batch(shapes, [1.0 / sh[-1] for sh in shapes], 1.4, 1, bc)
+            for k, st in enumerate(states):
+                b.set_prim(k, st)
+            b.run_begin(0.9, 1e9, 0.0, 2, max_steps=12)
+            b.run_steps(12)
+            rb = b.run_end()
+            out.append((r.steps, r.t, g.get_prim(), [(x.steps, x.t) for x in rb],
+                        [b.get_prim(k) for k in range(len(shapes))]))
+            b.close()
+    finally:
+        cg.set_tensor_maps(True)
+    assert out[0][0] == out[1][0] == 9 and out[0][1] == out[1][1]
+    assert bit_equal(out[0][2], out[1][2])
+    assert out[0][3] == out[1][3] and all(n == 12 for n, _ in out[0][3])
+    for a, c in zip(out[0][4], out[1][4]):
+        assert bit_equal(a, c)
+
+
 def test_fp32_sod_error(cg, golden):
     g = grid_from(cg, 0, cases.sod(1000), 1.0 / 1000, precision=1)
     r = g.solve(2, 0.9, 0.25, 0.0, 1)
