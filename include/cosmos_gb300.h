@@ -110,8 +110,8 @@ unsigned long long cosmos_kernel_launches(void); /* kernels launched by this lib
 const char* cosmos_version(void);
 /* FP32 sweeps stage their rows through TMA tensor maps (one copy of a row's five fields) when
  * `enable` is nonzero (the default), else by one copy per field; the results are bit-identical.
- * Read when a sweep is launched or captured and when a batch is created.  Library-wide (this build
- * has no counterpart in the reference); returns the previous setting. */
+ * Read when a sweep is launched or captured and when a batch is created.  Library-wide (the
+ * reference has no counterpart); returns the previous setting. */
 int cosmos_set_tensor_maps(int enable);
 
 void cosmos_params_default(cosmos_params* p);
