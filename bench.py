@@ -701,6 +701,7 @@ def measure_batch(cg, L, ctx, stream, steps, warmup, l1_steps=20, tiles=False):
     cells = sum(int(np.prod(sh)) for sh in shapes)
     bytes_step = sum(int(np.prod(sh)) * (120 if len(sh) == 2 else 40) for sh in shapes)
     peak, peak_kind = peaks()
+    ratio = traffic_per_launch("batch_step_fp32_ratio")
     b = cg.Batch(shapes, dxs, 1.4, cg.FP32, cg.BC_TRANSMISSIVE, ctx=ctx)
     for k, s in enumerate(states):
         b.set_prim(k, s)
@@ -720,9 +721,12 @@ def measure_batch(cg, L, ctx, stream, steps, warmup, l1_steps=20, tiles=False):
            "cells": cells, "tile_shape": list(tuned), "steps": steps,
            "value": cells / (ms * 1e-3), "ms_per_step": ms, "gpu_launches": int(launches),
            "roofline": {"bound": "hbm", "kernel": "batch_pair_kernel (whole step)",
-                        "achieved": bytes_step / (ms * 1e-3) / 1e9, "peak": peak,
+                        "achieved": bytes_step / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                         "frac": bytes_step / (ms * 1e-3) / 1e9 / peak,
-                        "bytes_per_cell_update": "40 (1D), 120 (2D)"},
+                        "bytes_per_cell_update": "40 (1D), 120 (2D)", "algorithmic_bytes_per_step": bytes_step,
+                        "traffic": (ratio * bytes_step) if ratio else None,
+                        "traffic_note": "per step: the algorithmic bytes times the DRAM-traffic ratio of an ncu "
+                                        "capture of the first 64 grids (every grid is swept the same way)"},
            "status": [x.status for x in res if x.status][:8]}
     if tile_ms:
         out["tile_ms_per_step"] = tile_ms
