@@ -428,6 +428,9 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
     // registers between the phases that write and read them (in the Y sweep, whose registers also
     // hold the slope factors, they spill)
     constexpr bool kRegOwn = AX == 0;
+    // the adjoint of B, computed at the end of phase 2 and read at the start of phase 3, stays in
+    // registers in both sweeps
+    constexpr bool kRegLb = true;
     V* sE = sD + 10 * NW;
     const Geom& G = a.G;
     const int along = AX == 0 ? threadIdx.x : threadIdx.y;
@@ -560,7 +563,7 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
                 for (int f = 0; f < 5; f++) Fb[f] = vmul(d, vsub(bn[f], bm[f]));
                 adj_force_vjp<V, AX>(F, B, R, c, d, Fb, Lb, Rb);
             }
-            if (!kRegOwn) sv_st<NW, kWide>(sD, me, Lb);  // adjoint of B_k
+            if (!kRegLb) sv_st<NW, kWide>(sD, me, Lb);  // adjoint of B_k
             sv_st<NW, kWide>(sD + 5 * NW, me, Rb);        // adjoint of A_{k+1}
         }
         __syncthreads();
@@ -578,7 +581,7 @@ __global__ void __launch_bounds__(P * W, (P * W >= 512 ? 1 : (Lane<V>::N == 2 ? 
                     ld(sE + 5 * NW, along, Pf);
                     ld(sE + 10 * NW, along, Qf);
                 }
-                if (!kRegOwn) sv_ld<NW, kWide>(sD, me, Lb);
+                if (!kRegLb) sv_ld<NW, kWide>(sD, me, Lb);
                 sv_ld<NW, kWide>(sD + 5 * NW, si(along - 1), Ab);
                 adj_evolve_vjp<V, AX>(F, uc, sl, Pf, Qf, hs, Ab, Lb, gl, gc, gr);
             }
